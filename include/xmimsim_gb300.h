@@ -1,0 +1,123 @@
+/*
+ * C-ABI of the GB300 XRF Monte Carlo engine (libxmimsim_gb300.so).
+ *
+ * Drop-in for the simulation call of XMI-MSIM 8.1: the entry points keep the
+ * reference's names, argument meaning, output layouts and ownership rules,
+ * so a caller written against the reference (bin/xmimsim.c:249-669,
+ * tests/libxmimsim-test.c:182-270) links against this library instead.
+ * Each declaration cites the reference interface it replaces.
+ *
+ * Conventions kept from the reference:
+ *  - int-returning calls return 1 on success and 0 on failure; the library
+ *    never calls exit() -- the reason of the last failure is available from
+ *    xmi_gpu_last_error();
+ *  - output arrays are allocated by the callee and released with xmi_free();
+ *  - channels[(N+1)*nchannels]: row i (i = 0..N) is the spectrum after at
+ *    most i interactions (cumulative over orders), times live_time;
+ *  - histories[100*385*N]: element (Z, line, k) at ((Z-1)*385 + line-1)*N + k-1,
+ *    line = -xraylib macro (1..383), 384 Rayleigh, 385 Compton.
+ */
+#ifndef XMIMSIM_GB300_H
+#define XMIMSIM_GB300_H
+
+#include "xmi_data_structs.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* opaque handles (reference: void* to Fortran TYPEs, include/xmi_data.h:29
+ * and include/xmi_aux.h) */
+typedef struct xmi_input_handle *xmi_inputFPtr;
+typedef struct xmi_tables_handle *xmi_hdf5FPtr;
+
+/* GPU-specific settings, kept out of xmi_main_options so that struct stays
+ * layout-identical to the reference */
+typedef struct {
+  int precision;            /* 0: FP64 transport; 1: FP32 transport, FP64 tallies */
+  int use_surrogate;        /* 1: solid angle from the MLP surrogate (VR only) */
+  double surrogate_tolerance; /* fall back to the grid where held-out error exceeds this */
+  int threads_per_block;    /* 0: default */
+  int blocks_per_sm;        /* 0: default */
+  unsigned long long seed;  /* Philox key; 0: fixed default key (0x5EED0001) */
+} xmi_gpu_options;
+
+/* ---- data model helpers (reference src/xmi_data_structs.c) ---- */
+xmi_input *xmi_input_init_empty(void);                 /* src/xmi_data_structs.c:551 */
+void xmi_input_free(xmi_input *input);                 /* include/xmi_data_structs.h:331 */
+void xmi_input_copy(xmi_input *A, xmi_input **B);      /* include/xmi_data_structs.h:332 */
+xmi_main_options *xmi_main_options_new(void);          /* include/xmi_data_structs.h:497 */
+void xmi_main_options_free(xmi_main_options *options); /* include/xmi_data_structs.h:498 */
+void xmi_free(void *ptr);                              /* src/xmi_aux.c (g_free wrapper) */
+const char *xmi_gpu_last_error(void);
+void xmi_gpu_default_options(xmi_gpu_options *gpu);
+
+/* ---- initialisation chain (bin/xmimsim.c:275-294) ---- */
+int xmi_input_C2F(xmi_input *input, xmi_inputFPtr *inputFPtr);   /* src/xmi_aux_f.F90:782 */
+void xmi_free_input_F(xmi_inputFPtr *inputFPtr);                 /* src/xmi_aux_f.F90:1027 */
+int xmi_init_input(xmi_inputFPtr *inputFPtr);                    /* src/xmi_main.F90:1741 */
+int xmi_init_input_escape_ratios(xmi_inputFPtr *inputFPtr);      /* src/xmi_main.F90:1687 */
+/* hdf5_file is accepted for signature compatibility; the tables come from the
+ * host tabulator (there is no xraylib data file on the target machines) */
+int xmi_init_from_hdf5(char *hdf5_file, xmi_inputFPtr inputFPtr,
+                       xmi_hdf5FPtr *hdf5FPtr, xmi_main_options *options); /* include/xmi_data.h:45 */
+int xmi_update_input_from_hdf5(xmi_inputFPtr inputFPtr, xmi_hdf5FPtr hdf5FPtr); /* include/xmi_data.h:50 */
+void xmi_free_hdf5_F(xmi_hdf5FPtr *hdf5FPtr);                    /* include/xmi_data.h:48 */
+int xmi_gpu_set_options(xmi_inputFPtr inputFPtr, const xmi_gpu_options *gpu);
+
+/* ---- solid-angle grid (include/xmi_solid_angle.h:39) ---- */
+extern long hits_per_single; /* samples per grid point, src/xmi_solid_angle_f.F90:43-44 */
+void xmi_solid_angle_calculation(xmi_inputFPtr inputFPtr, xmi_solid_angle **solid_angle,
+                                 char *input_string, xmi_main_options *options);
+/* backend-plugin symbol with the XmiSolidAngleCalculation typedef of
+ * src/xmi_solid_angle.c:50 (the slot the OpenCL/Metal plugins fill) */
+int xmi_solid_angle_calculation_cuda(xmi_inputFPtr inputFPtr, xmi_solid_angle **solid_angle,
+                                     char *input_string, xmi_main_options *options);
+void xmi_free_solid_angle(xmi_solid_angle *solid_angle);          /* include/xmi_solid_angle.h:52 */
+
+/* ---- transport (include/xmi_main.h:29) ---- */
+int xmi_main_msim(xmi_inputFPtr inputFPtr, xmi_hdf5FPtr hdf5FPtr, int n_mpi_hosts,
+                  double **channels, xmi_main_options *options, double **brute_history,
+                  double **var_red_history, xmi_solid_angle *solid_angles);
+
+/* ---- detector response (include/xmi_main.h:31-37) ---- */
+void xmi_detector_convolute_spectrum(xmi_inputFPtr inputFPtr, double *channels_noconv,
+                                     double **channels_conv, xmi_main_options *options,
+                                     xmi_escape_ratios *escape_ratios, int n_interactions);
+void xmi_detector_convolute_all(xmi_inputFPtr inputFPtr, double **channels_noconv,
+                                double **channels_conv, double *brute_history,
+                                double *var_red_history, xmi_main_options *options,
+                                xmi_escape_ratios *escape_ratios, int n_interactions_all,
+                                int zero_interaction);
+void xmi_detector_convolute_history(xmi_inputFPtr inputFPtr, double *history,
+                                    xmi_main_options *options);
+/* custom-detector-response plugin symbol (typedef XmiDetectorConvoluteAll,
+ * include/xmi_main.h:37; loaded by bin/xmimsim.c:505-526) */
+void xmi_detector_convolute_all_custom(xmi_inputFPtr inputFPtr, double **channels_noconv,
+                                       double **channels_conv, double *brute_history,
+                                       double *var_red_history, xmi_main_options *options,
+                                       xmi_escape_ratios *escape_ratios, int n_interactions_all,
+                                       int zero_interaction);
+
+/* ---- escape ratios (include/xmi_detector.h:55-57) ---- */
+xmi_escape_ratios_options xmi_get_default_escape_ratios_options(void);
+void xmi_escape_ratios_calculation(xmi_input *inputPtr, xmi_escape_ratios **escape_ratios,
+                                   char *input_string, char *hdf5_file,
+                                   xmi_main_options *options, xmi_escape_ratios_options ero);
+void xmi_free_escape_ratios(xmi_escape_ratios *escape_ratios);   /* include/xmi_detector.h:71 */
+
+/* ---- introspection used by the test-suite and benchmark ---- */
+struct xmi_bundle_s; /* see xmimsim_bundle.h */
+const void *xmi_gpu_bundle(xmi_hdf5FPtr hdf5FPtr);
+/* prepares the run-dependent part of the bundle (source items, options)
+ * exactly as xmi_main_msim would, without running it */
+int xmi_gpu_prepare_run(xmi_inputFPtr inputFPtr, xmi_hdf5FPtr hdf5FPtr,
+                        xmi_main_options *options, int n_mpi_hosts,
+                        xmi_solid_angle *solid_angles);
+/* device time (ms, CUDA events) and kernel launches of the last call */
+int xmi_gpu_last_timing(double *transport_ms, double *total_ms, int *launches);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

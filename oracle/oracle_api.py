@@ -1,0 +1,111 @@
+"""TEST INFRASTRUCTURE: ctypes access to the FP64 CPU oracle (oracle/*.c).
+
+Only the test-suite, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU
+baseline use this module, always as the checker or the timed CPU baseline,
+never inside the engine.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+LIB = Path(__file__).resolve().parent / "_build" / "liboracle_xmimsim.so"
+_lib = None
+
+
+class OracleEscape(C.Structure):
+    _fields_ = [("n_el", C.c_int), ("nfe", C.c_int), ("nce", C.c_int), ("nco", C.c_int),
+                ("edge", C.POINTER(C.c_double)), ("line_e", C.POINTER(C.c_double)),
+                ("fluo", C.POINTER(C.c_double)), ("fe", C.POINTER(C.c_double)),
+                ("comp", C.POINTER(C.c_double)), ("ce", C.POINTER(C.c_double)), ("co", C.POINTER(C.c_double))]
+
+
+def load() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        if not LIB.exists():
+            raise RuntimeError(f"{LIB} missing: run __graft_entry__.build()")
+        _lib = C.CDLL(str(LIB))
+        dp = C.POINTER(C.c_double)
+        _lib.oracle_xmi_main_msim.restype = C.c_int
+        _lib.oracle_xmi_main_msim.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int64, dp, dp, dp,
+                                              C.POINTER(C.c_long)]
+        _lib.oracle_solid_angle_points.restype = None
+        _lib.oracle_solid_angle_points.argtypes = [C.c_void_p, dp, C.c_int, dp, C.c_int64, C.c_int64, C.c_long, dp]
+        _lib.oracle_poly_solve_quadratic.restype = C.c_int
+        _lib.oracle_poly_solve_quadratic.argtypes = [C.c_double, C.c_double, C.c_double, dp, dp]
+        _lib.oracle_words_counted.restype = C.c_longlong
+        _lib.oracle_words_counted.argtypes = []
+        _lib.oracle_philox_block.restype = None
+        _lib.oracle_philox_block.argtypes = [C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]
+        _lib.oracle_convolute_spectrum.restype = C.c_int
+        _lib.oracle_convolute_spectrum.argtypes = [dp, dp, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
+                                                   C.c_int, C.c_double, C.c_double, C.POINTER(OracleEscape), C.c_int,
+                                                   C.c_uint64, dp]
+    return _lib
+
+
+def _dp(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def msim(bundle_ptr: int, n_interactions: int, nchannels: int, n_mpi_hosts: int = 1, threads: int = 0,
+         max_photons_per_item: int = -1) -> dict:
+    lib = load()
+    ch = np.zeros((n_interactions + 1) * nchannels)
+    br = np.zeros(100 * 385 * n_interactions)
+    vr = np.zeros(100 * 385 * n_interactions)
+    nf = C.c_long(0)
+    rv = lib.oracle_xmi_main_msim(C.c_void_p(bundle_ptr), n_mpi_hosts, threads, max_photons_per_item, _dp(ch),
+                                  _dp(br), _dp(vr), C.byref(nf))
+    if rv != 1:
+        raise RuntimeError("oracle transport failed")
+    return {"channels": ch.reshape(n_interactions + 1, nchannels), "brute": br.reshape(100, 385, n_interactions),
+            "var_red": vr.reshape(100, 385, n_interactions), "not_found": nf.value}
+
+
+def words_counted() -> int:
+    """Algorithmic table words read by the oracle since the previous call."""
+    return int(load().oracle_words_counted())
+
+
+def solid_angle_points(bundle_ptr: int, r_vals: np.ndarray, t_vals: np.ndarray, p0: int, p1: int,
+                       hits_per_single: int = 5000) -> np.ndarray:
+    lib = load()
+    out = np.zeros(p1 - p0)
+    r = np.ascontiguousarray(r_vals, dtype=np.float64)
+    t = np.ascontiguousarray(t_vals, dtype=np.float64)
+    lib.oracle_solid_angle_points(C.c_void_p(bundle_ptr), _dp(r), len(r), _dp(t), p0, p1, hits_per_single, _dp(out))
+    return out
+
+
+def poly_solve_quadratic(a: float, b: float, c: float):
+    lib = load()
+    r1, r2 = C.c_double(0.0), C.c_double(0.0)
+    n = lib.oracle_poly_solve_quadratic(a, b, c, C.byref(r1), C.byref(r2))
+    return n, r1.value, r2.value
+
+
+def philox_block(ctr, key):
+    lib = load()
+    c = (C.c_uint32 * 4)(*ctr)
+    k = (C.c_uint32 * 2)(*key)
+    o = (C.c_uint32 * 4)()
+    lib.oracle_philox_block(c, k, o)
+    return list(o)
+
+
+def convolute_spectrum(noconv, det_corr, gain, zero, fano, noise, det_type, live_time, pulse_width,
+                       escape: OracleEscape | None = None, use_sum_peaks: int = 0, pile_seed: int = 0):
+    lib = load()
+    nc = np.ascontiguousarray(noconv, dtype=np.float64)
+    dc = np.ascontiguousarray(det_corr, dtype=np.float64)
+    out = np.zeros_like(nc)
+    rv = lib.oracle_convolute_spectrum(_dp(nc), _dp(dc), len(nc), gain, zero, fano, noise, det_type, live_time,
+                                       pulse_width, C.byref(escape) if escape is not None else None, use_sum_peaks,
+                                       pile_seed, _dp(out))
+    if rv != 1:
+        raise RuntimeError("oracle convolution failed")
+    return out

@@ -1,0 +1,220 @@
+"""GPU parity: the CUDA engine, called through its C-ABI, against the FP64 CPU
+oracle on the same tables, Philox streams and solid-angle grid.
+
+Tolerances: FP64 transport and grids are compared at rtol 1e-6 (identical
+random sequences and arithmetic up to FMA contraction / last-ulp differences of
+the math libraries; a rare channel-boundary flip moves one contribution to a
+neighbouring channel, hence the channel check on sums and at 1e-4 per
+channel); the FP32 transport consumes the same draws and is compared at 2e-3
+on the main line intensities; the detector convolution at 1e-9.
+"""
+import ctypes as C
+import json
+import math
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from xmimsim_gb300 import DiscreteLine, ContinuousPoint, InputSpec, Layer, Simulation, configs, gpu_options
+
+pytestmark = pytest.mark.gpu
+GOLDEN = Path(__file__).resolve().parent / "golden"
+SEED = 0x5EED0001
+
+
+def oracle():
+    from oracle import oracle_api
+    return oracle_api
+
+
+def run_pair(spec, options, precision=0, hits=None):
+    sim = Simulation(spec, options=options, gpu=gpu_options(precision=precision, seed=SEED))
+    if options.get("use_variance_reduction", 1):
+        sim.solid_angle()
+    gpu = sim.msim()
+    sim.prepare()
+    ref = oracle().msim(sim.bundle_ptr(), spec.n_interactions_trajectory, spec.nchannels)
+    return sim, gpu, ref
+
+
+def assert_transport_equal(gpu, ref, rtol=1e-6):
+    for key in ("var_red", "brute"):
+        g, o = gpu[key], ref[key]
+        if g is None:
+            assert not o.any()
+            continue
+        scale = max(abs(o).max(), 1e-300)
+        np.testing.assert_allclose(g, o, rtol=rtol, atol=rtol * scale * 1e-3)
+    cg, co = gpu["channels"], ref["channels"]
+    np.testing.assert_allclose(cg.sum(axis=1), co.sum(axis=1), rtol=rtol)
+    np.testing.assert_allclose(cg, co, rtol=1e-4, atol=1e-4 * max(co.max(), 1e-300))
+
+
+def test_solid_angle_grid_matches_oracle_exactly():
+    spec = configs.config1(n_photons_line=10)
+    sim = Simulation(spec, options=configs.C1_OPTIONS, gpu=gpu_options(seed=SEED))
+    g = sim.solid_angle_grid()
+    sim.prepare()
+    nr, nt = len(g["r"]), len(g["theta"])
+    rng = np.random.default_rng(1)
+    pts = np.sort(rng.choice(nr * nt, size=256, replace=False))
+    vals = np.array([oracle().solid_angle_points(sim.bundle_ptr(), g["r"], g["theta"], int(p), int(p) + 1, 5000)[0]
+                     for p in pts])
+    gpu_vals = g["grid"].reshape(-1)[pts]
+    # identical hit counts: equal values; allow a single boundary flip on a handful of points
+    diff = np.abs(gpu_vals - vals)
+    quantum = np.maximum(vals, gpu_vals) / 5000.0 * 1.5 + 1e-300
+    assert (diff <= quantum).all()
+    assert (diff == 0).mean() > 0.95
+    sim.close()
+
+
+def test_solid_angle_grid_fp32_close_to_fp64():
+    spec = configs.config1(n_photons_line=10)
+    s64 = Simulation(spec, options=configs.C1_OPTIONS, gpu=gpu_options(seed=SEED))
+    s32 = Simulation(spec, options=configs.C1_OPTIONS, gpu=gpu_options(precision=1, seed=SEED))
+    g64, g32 = s64.solid_angle_grid()["grid"], s32.solid_angle_grid()["grid"]
+    m = g64 > 1e-4
+    assert np.median(np.abs(g32[m] - g64[m]) / g64[m]) < 1e-3
+    s64.close()
+    s32.close()
+
+
+def test_transport_fp64_config1_matches_oracle():
+    spec = configs.config1(n_photons_line=20000)
+    sim, gpu, ref = run_pair(spec, configs.C1_OPTIONS)
+    assert_transport_equal(gpu, ref)
+    assert gpu["var_red"][26 - 1, 3 - 1].sum() > 0  # Fe-KL3
+    sim.close()
+
+
+def mixed_source_spec():
+    layers = configs.random_layers(seed=11, n_layers=3, nel=(2, 5), thick=(1e-4, 0.05))
+    cont = [ContinuousPoint(5.0 + i, 1e8 * (1 + 0.1 * i), 5e7) for i in range(12)]
+    disc = [DiscreteLine(16.0, 1e9, 1e8, distribution_type=1, scale_parameter=0.05),
+            DiscreteLine(12.0, 5e8, 5e8, distribution_type=2, scale_parameter=0.02),
+            DiscreteLine(9.0, 1e9, 0.0, sigma_x=0.01, sigma_xp=0.001, sigma_y=0.01, sigma_yp=0.001)]
+    return InputSpec(layers=layers, reference_layer=2, n_photons_interval=300, n_photons_line=1500,
+                     n_interactions_trajectory=5, p_detector_window=(0.0, 10.0, 100.0), discrete=disc,
+                     continuous=cont, exc_layers=[Layer([13], [1.0], 2.7, 0.01)])
+
+
+def test_transport_fp64_mixed_sources_multilayer_matches_oracle():
+    spec = mixed_source_spec()
+    sim, gpu, ref = run_pair(spec, dict(configs.C1_OPTIONS))
+    assert_transport_equal(gpu, ref)
+    sim.close()
+
+
+@pytest.mark.parametrize("cascade", [(0, 0), (1, 0), (0, 1)])
+def test_transport_cascade_options_match_oracle(cascade):
+    spec = configs.config1(n_photons_line=5000)
+    opts = dict(configs.C1_OPTIONS, use_cascade_auger=cascade[0], use_cascade_radiative=cascade[1], use_M_lines=0)
+    sim, gpu, ref = run_pair(spec, opts)
+    assert_transport_equal(gpu, ref)
+    sim.close()
+
+
+def test_transport_analog_brute_force_matches_oracle():
+    spec = configs.config1(n_photons_line=200000)
+    spec.p_detector_window = (0.0, 1.0, 100.0)
+    opts = dict(configs.C1_OPTIONS, use_variance_reduction=0)
+    sim, gpu, ref = run_pair(spec, opts)
+    assert gpu["var_red"] is None
+    assert_transport_equal(gpu, ref)
+    sim.close()
+
+
+def collimator_spec(n=5000):
+    spec = configs.config1(n_photons_line=n)
+    spec.collimator_height = 1.0
+    spec.collimator_diameter = 0.2
+    return spec
+
+
+def test_transport_collimator_matches_oracle():
+    sim, gpu, ref = run_pair(collimator_spec(), configs.C1_OPTIONS)
+    assert_transport_equal(gpu, ref)
+    sim.close()
+
+
+def test_transport_fp32_tracks_fp64():
+    spec = configs.config1(n_photons_line=50000)
+    s64 = Simulation(spec, options=configs.C1_OPTIONS, gpu=gpu_options(precision=0, seed=SEED))
+    s32 = Simulation(spec, options=configs.C1_OPTIONS, gpu=gpu_options(precision=1, seed=SEED))
+    r64, r32 = s64.msim(), s32.msim()
+    for Z, line in ((26, 3), (29, 3), (30, 3), (26, 2), (29, 6)):
+        a, b = r64["var_red"][Z - 1, line - 1].sum(), r32["var_red"][Z - 1, line - 1].sum()
+        assert b == pytest.approx(a, rel=2e-3)
+    np.testing.assert_allclose(r32["channels"].sum(axis=1), r64["channels"].sum(axis=1), rtol=2e-3)
+    s64.close()
+    s32.close()
+
+
+def test_invalid_input_fails_cleanly():
+    from xmimsim_gb300 import XmiError
+    spec = configs.config1(n_photons_line=10)
+    spec.n_interactions_trajectory = 99
+    with pytest.raises(XmiError):
+        Simulation(spec, options=configs.C1_OPTIONS)
+
+
+def test_detector_convolution_matches_oracle():
+    spec = configs.config1(n_photons_line=20000)
+    sim = Simulation(spec, options=dict(configs.C1_OPTIONS, use_escape_peaks=0), gpu=gpu_options(seed=SEED))
+    out = sim.msim()
+    conv = sim.convolute(out["channels"])
+    # channel absorption factors the engine applies, recomputed with the data model
+    import xmimsim_gb300.tube as tube
+    lib = tube._xrl()
+
+    def layer_mu(l, E):
+        w = np.array(l.weight) / sum(l.weight)
+        return sum(wi * lib.xrl_CS_Total_Kissel(z, E) for z, wi in zip(l.Z, w))
+    dc = []
+    for i in range(spec.nchannels):
+        E = i * spec.gain + spec.zero
+        d = 1.0
+        for l in spec.det_layers:
+            d *= math.exp(-l.density * l.thickness * layer_mu(l, E))
+        for l in spec.crystal_layers:
+            d = -d * math.expm1(-l.density * l.thickness * layer_mu(l, E))
+        dc.append(d)
+    for k in range(1, spec.n_interactions_trajectory + 1):
+        ref = oracle().convolute_spectrum(out["channels"][k], np.array(dc), spec.gain, spec.zero, spec.fano,
+                                          spec.noise, spec.detector_type, spec.live_time, spec.pulse_width)
+        np.testing.assert_allclose(conv[k], ref, rtol=1e-9, atol=1e-12 * ref.max())
+    sim.close()
+
+
+def test_pile_up_reference_srm1155():
+    """tests/test-pile-up.c: with pile-up the counts at channel 1077 of the
+    srm1155 example rise more than a hundredfold."""
+    from xmimsim_gb300 import xmlio
+    g = json.loads((GOLDEN / "srm1155.json").read_text())
+    spec = xmlio.read_xmsi(g["xmsi"])
+    spec.n_photons_line = spec.n_photons_interval = 1
+    sim = Simulation(spec, options=dict(use_escape_peaks=0, use_sum_peaks=0, use_default_seeds=1))
+    unconv = np.zeros((spec.n_interactions_trajectory + 1, spec.nchannels))
+    unconv[-1] = g["unconv_last"]
+    without = sim.convolute(unconv)[-1][g["pileup_channel"]]
+    sim.options.use_sum_peaks = 1
+    with_pu = sim.convolute(unconv)[-1][g["pileup_channel"]]
+    assert with_pu / without > g["pileup_min_ratio"]
+    sim.close()
+
+
+def test_escape_ratios_plausible():
+    spec = configs.config1(n_photons_line=10)
+    sim = Simulation(spec, options=configs.C1_OPTIONS, gpu=gpu_options(seed=SEED))
+    er = sim.escape_ratios(n_photons=20000, n_input_energies=100).contents
+    nel, nE = er.n_elements, er.n_fluo_input_energies
+    fluo = np.ctypeslib.as_array(er.fluo_escape_ratios, (nE * 109 * nel,)).reshape(nE, 109, nel)
+    E = np.ctypeslib.as_array(er.fluo_escape_input_energies, (nE,))
+    si_k = fluo[:, 2, 0] + fluo[:, 1, 0]  # Si KL3 + KL2
+    above = E > 2.0
+    assert (si_k[above] > 0).all() and (si_k[above] < 0.2).all()
+    assert (si_k[E < 1.8] == 0).all()
+    sim.lib.xmi_free_escape_ratios(C.pointer(er))
+    sim.close()

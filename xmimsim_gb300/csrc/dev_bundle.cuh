@@ -1,0 +1,67 @@
+/* Device view of the table bundle and small device helpers shared by the
+ * transport, solid-angle and detector kernels. */
+#ifndef XMIMSIM_GB300_DEV_BUNDLE_CUH
+#define XMIMSIM_GB300_DEV_BUNDLE_CUH
+
+#include <cstdint>
+#include "../../include/xmimsim_bundle.h"
+#include "philox.h"
+
+namespace xmi {
+
+constexpr double kEnergyThreshold = 1.0;  /* src/xmi_aux_f.F90:673 */
+constexpr double kEnergyMax = 200.0;      /* src/xmi_aux_f.F90:674 */
+constexpr double kPi = 3.14159265358979323846;
+
+/* Device copy of an xmi_bundle.  R is the precision of the physics tables
+ * and of the per-photon arithmetic except positions, which are always FP64
+ * (FP32 cannot resolve 10 nm layers at 10-100 cm from the origin). */
+template <typename R>
+struct DevBundle {
+  int N, nch, use_vr, use_M_lines, line_last, max_shell, escape_mode;
+  int n_layers, n_elem, n_lines, n_slots, n_nodes, n_seg, n_items;
+  int coll_present, sa_nr, sa_nt, sa_hits;
+  unsigned long long seed;
+  long long n_photons_total;
+  double gain, zero;
+  double n_sample[3], p_det[3], n_det[3], det_new[9], det_inv[9];
+  double det_radius, coll_radius, coll_height, coll_half_apex, coll_vertex_x;
+  double d_source_slit, slit_x, slit_y;
+  double zbeg[XMI_MAXL], zend[XMI_MAXL];
+  R rho[XMI_MAXL];
+  int nel[XMI_MAXL], off[XMI_MAXL];
+  /* sa grid metadata (uniform axes) */
+  double sa_r0, sa_rinv, sa_t0, sa_tinv;
+
+  const int *layer_el;
+  const R *layer_w;
+  const int *elem_Z;
+  const R *yield_corr, *fluor_yield, *ck;
+  const int *line_off, *shell_off;
+  const int *line_index, *line_shell;
+  const R *line_energy, *line_rate;
+  const R *precalc_mu, *precalc_xrf;
+  const double *seg_lo, *seg_lnlo, *seg_invh;
+  const int *seg_off, *seg_n;
+  const R *el_tab, *mu_tab, *exc_tab;
+  const R *icdf_e, *icdf_r, *rayl_icdf, *compt_icdf, *phi_t, *phi_icdf, *dop_r, *dop_icdf, *ff2, *sf;
+  const xmi_source_item *items;
+  const long long *item_first; /* [n_items] global id of the first photon */
+  const double *sa_r, *sa_t;
+  const R *sa_grid;
+};
+
+/* Tally buffers of one run (device pointers). */
+struct DevTally {
+  double *hist_vr;    /* [N][n_slots] */
+  double *hist_brute; /* [N][n_slots] */
+  double *chan;       /* [N+1][nch] per order (non-cumulative) */
+  unsigned long long *counters; /* [0] off-grid solid angles, [1] error code, [2] photons done */
+};
+
+__host__ __device__ inline double dot3(const double *a, const double *b) {
+  return a[0] * b[0] + a[1] * b[1] + a[2] * b[2];
+}
+
+}  // namespace xmi
+#endif

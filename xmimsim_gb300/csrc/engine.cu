@@ -1,0 +1,592 @@
+/*
+ * GB300 engine: device mirror of the table bundle, the transport and
+ * solid-angle launches behind the C-ABI, and the reshaping of the device
+ * tallies into the reference's output layouts.
+ */
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+
+#include "solid_angle.cuh"
+#include "transport.cuh"
+#include "xmi_internal.h"
+
+long hits_per_single = 5000; /* src/xmi_solid_angle_f.F90:43-44 */
+
+namespace {
+
+struct Timing {
+  double transport_ms = 0.0, total_ms = 0.0;
+  int launches = 0;
+};
+thread_local Timing g_timing;
+
+bool cuda_ok(cudaError_t e, const char *what) {
+  if (e != cudaSuccess) {
+    xmi_set_error("%s: %s", what, cudaGetErrorString(e));
+    return false;
+  }
+  return true;
+}
+
+/* device allocations of one precision */
+struct DevSide {
+  std::vector<void *> allocs;
+  bool valid = false;
+  void *b = nullptr; /* DevBundle<R> (host copy of the device struct) */
+  void release() {
+    for (void *p : allocs) cudaFree(p);
+    allocs.clear();
+    valid = false;
+  }
+};
+
+struct DevState {
+  DevSide d64, d32;
+  xmi::DevBundle<double> b64;
+  xmi::DevBundle<float> b32;
+  /* run buffers */
+  xmi_source_item *items = nullptr;
+  long long *item_first = nullptr;
+  int items_cap = 0;
+  double *sa_r = nullptr, *sa_t = nullptr, *sa_g64 = nullptr;
+  float *sa_g32 = nullptr;
+  int sa_n = 0;
+  const double *sa_src = nullptr;
+  double *tally = nullptr;
+  size_t tally_cap = 0;
+  unsigned long long *counters = nullptr;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+};
+
+template <typename R>
+const R *upload(DevSide &s, const double *src, size_t n) {
+  if (n == 0) n = 1;
+  std::vector<R> tmp(n);
+  for (size_t i = 0; i < n; i++) tmp[i] = src ? (R)src[i] : (R)0;
+  void *p = nullptr;
+  if (cudaMalloc(&p, sizeof(R) * n) != cudaSuccess) return nullptr;
+  s.allocs.push_back(p);
+  cudaMemcpy(p, tmp.data(), sizeof(R) * n, cudaMemcpyHostToDevice);
+  return (const R *)p;
+}
+
+const int *upload_int(DevSide &s, const int *src, size_t n) {
+  if (n == 0) n = 1;
+  void *p = nullptr;
+  if (cudaMalloc(&p, sizeof(int) * n) != cudaSuccess) return nullptr;
+  s.allocs.push_back(p);
+  if (src) cudaMemcpy(p, src, sizeof(int) * n, cudaMemcpyHostToDevice);
+  else cudaMemset(p, 0, sizeof(int) * n);
+  return (const int *)p;
+}
+
+const double *upload_d(DevSide &s, const double *src, size_t n) {
+  if (n == 0) n = 1;
+  void *p = nullptr;
+  if (cudaMalloc(&p, sizeof(double) * n) != cudaSuccess) return nullptr;
+  s.allocs.push_back(p);
+  if (src) cudaMemcpy(p, src, sizeof(double) * n, cudaMemcpyHostToDevice);
+  return (const double *)p;
+}
+
+/* fills the scalar part of a DevBundle from the host bundle */
+template <typename R>
+void fill_scalars(const xmi_bundle &h, xmi::DevBundle<R> &d) {
+  d.N = h.n_interactions;
+  d.nch = h.nchannels;
+  d.use_vr = h.use_vr;
+  d.use_M_lines = h.use_M_lines;
+  d.line_last = h.line_last;
+  d.max_shell = h.max_shell;
+  d.escape_mode = h.escape_mode;
+  d.n_layers = h.n_layers;
+  d.n_elem = h.n_elem;
+  d.n_lines = h.n_lines;
+  d.n_slots = h.n_slots;
+  d.n_nodes = h.n_nodes;
+  d.n_seg = h.n_seg;
+  d.n_items = h.n_items;
+  d.coll_present = h.coll_present;
+  d.seed = h.seed;
+  d.n_photons_total = h.n_photons_total;
+  d.gain = h.gain;
+  d.zero = h.zero;
+  for (int k = 0; k < 3; k++) {
+    d.n_sample[k] = h.n_sample[k];
+    d.p_det[k] = h.p_det[k];
+    d.n_det[k] = h.n_det[k];
+  }
+  for (int k = 0; k < 9; k++) {
+    d.det_new[k] = h.det_new[k];
+    d.det_inv[k] = h.det_inv[k];
+  }
+  d.det_radius = h.det_radius;
+  d.coll_radius = h.coll_radius;
+  d.coll_height = h.coll_height;
+  d.coll_half_apex = h.coll_half_apex;
+  d.coll_vertex_x = h.coll_vertex_x;
+  d.d_source_slit = h.d_source_slit;
+  d.slit_x = h.slit_x;
+  d.slit_y = h.slit_y;
+  for (int j = 0; j < XMI_MAXL; j++) {
+    d.zbeg[j] = h.layer_zbeg[j];
+    d.zend[j] = h.layer_zend[j];
+    d.rho[j] = (R)h.layer_rho[j];
+    d.nel[j] = h.layer_nel[j];
+    d.off[j] = h.layer_off[j];
+  }
+}
+
+template <typename R>
+bool upload_tables(const xmi_bundle &h, DevSide &s, xmi::DevBundle<R> &d) {
+  s.release();
+  fill_scalars(h, d);
+  const size_t E = h.n_elem, NL = h.n_lines;
+  d.layer_el = upload_int(s, h.layer_el, h.n_layer_el);
+  d.layer_w = upload<R>(s, h.layer_w, h.n_layer_el);
+  d.elem_Z = upload_int(s, h.elem_Z, E);
+  d.yield_corr = upload<R>(s, h.elem_yield_corr, 9 * E);
+  d.fluor_yield = upload<R>(s, h.elem_fluor_yield, 9 * E);
+  d.ck = upload<R>(s, h.elem_ck, XMI_NCK * E);
+  d.line_off = upload_int(s, h.elem_line_off, E + 1);
+  d.shell_off = upload_int(s, h.elem_shell_off, 10 * E);
+  d.line_index = upload_int(s, h.line_index, NL);
+  d.line_shell = upload_int(s, h.line_shell, NL);
+  d.line_energy = upload<R>(s, h.line_energy, NL);
+  d.line_rate = upload<R>(s, h.line_rate, NL);
+  d.precalc_mu = upload<R>(s, h.precalc_mu, (size_t)h.n_layers * NL);
+  d.precalc_xrf = upload<R>(s, h.precalc_xrf, E * 9 * NL);
+  d.seg_lo = upload_d(s, h.seg_lo, h.n_seg + 1);
+  d.seg_lnlo = upload_d(s, h.seg_lnlo, h.n_seg);
+  d.seg_invh = upload_d(s, h.seg_invh, h.n_seg);
+  d.seg_off = upload_int(s, h.seg_off, h.n_seg);
+  d.seg_n = upload_int(s, h.seg_n, h.n_seg);
+  d.el_tab = upload<R>(s, h.el_tab, E * h.n_nodes * XMI_EL_REC);
+  d.mu_tab = upload<R>(s, h.mu_tab, (size_t)h.n_nodes * XMI_MAXL);
+  d.exc_tab = upload<R>(s, h.exc_tab, h.n_nodes);
+  d.icdf_e = upload<R>(s, h.icdf_energies, XMI_ICDF_NE);
+  d.icdf_r = upload<R>(s, h.icdf_rs, XMI_ICDF_NR);
+  d.rayl_icdf = upload<R>(s, h.rayl_icdf, E * XMI_ICDF_NE * XMI_ICDF_NR);
+  d.compt_icdf = upload<R>(s, h.compt_icdf, E * XMI_ICDF_NE * XMI_ICDF_NR);
+  d.phi_t = upload<R>(s, h.phi_thetas, XMI_PHI_NT);
+  d.phi_icdf = upload<R>(s, h.phi_icdf, (size_t)XMI_PHI_NT * XMI_ICDF_NR);
+  d.dop_r = upload<R>(s, h.doppler_rs, XMI_DOPPLER_N);
+  d.dop_icdf = upload<R>(s, h.doppler_icdf, E * XMI_DOPPLER_N);
+  d.ff2 = upload<R>(s, h.ff2, E * XMI_NQ);
+  d.sf = upload<R>(s, h.sf, E * XMI_NQ);
+  if (cudaGetLastError() != cudaSuccess || !d.sf) {
+    xmi_set_error("device table upload failed");
+    s.release();
+    return false;
+  }
+  s.valid = true;
+  return true;
+}
+
+DevState *state_of(struct xmi_tables_handle *t) {
+  if (!t->dev) {
+    DevState *s = new DevState();
+    cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
+    cudaEventCreate(&s->ev0);
+    cudaEventCreate(&s->ev1);
+    t->dev = s;
+  }
+  return (DevState *)t->dev;
+}
+
+bool ensure_device() {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n < 1) {
+    xmi_set_error("no CUDA device available: the engine has no CPU fallback");
+    return false;
+  }
+  return true;
+}
+
+int num_sms() {
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  return sms > 0 ? sms : 1;
+}
+
+}  // namespace
+
+extern "C" {
+
+int xmi_dev_sync_tables(struct xmi_tables_handle *t, int precision) {
+  if (!ensure_device()) return 0;
+  DevState *s = state_of(t);
+  if (precision == 0) {
+    if (!s->d64.valid) return upload_tables<double>(t->b, s->d64, s->b64) ? 1 : 0;
+    fill_scalars(t->b, s->b64);
+  } else {
+    if (!s->d32.valid) return upload_tables<float>(t->b, s->d32, s->b32) ? 1 : 0;
+    fill_scalars(t->b, s->b32);
+  }
+  return 1;
+}
+
+int xmi_dev_bundle_copy64(struct xmi_tables_handle *t, void *out) {
+  DevState *s = state_of(t);
+  if (!s->d64.valid) return 0;
+  fill_scalars(t->b, s->b64);
+  *(xmi::DevBundle<double> *)out = s->b64;
+  return 1;
+}
+
+void xmi_dev_free_tables(struct xmi_tables_handle *t) {
+  if (!t || !t->dev) return;
+  DevState *s = (DevState *)t->dev;
+  s->d64.release();
+  s->d32.release();
+  cudaFree(s->items);
+  cudaFree(s->item_first);
+  cudaFree(s->sa_r);
+  cudaFree(s->sa_t);
+  cudaFree(s->sa_g64);
+  cudaFree(s->sa_g32);
+  cudaFree(s->tally);
+  cudaFree(s->counters);
+  if (s->ev0) cudaEventDestroy(s->ev0);
+  if (s->ev1) cudaEventDestroy(s->ev1);
+  if (s->stream) cudaStreamDestroy(s->stream);
+  delete s;
+  t->dev = nullptr;
+}
+
+void xmi_free_hdf5_F(xmi_hdf5FPtr *p) {
+  if (!p || !*p) return;
+  xmi_dev_free_tables(*p);
+  xmi_bundle_free(&(*p)->b);
+  free(*p);
+  *p = nullptr;
+}
+
+int xmi_gpu_last_timing(double *transport_ms, double *total_ms, int *launches) {
+  if (transport_ms) *transport_ms = g_timing.transport_ms;
+  if (total_ms) *total_ms = g_timing.total_ms;
+  if (launches) *launches = g_timing.launches;
+  return 1;
+}
+
+/* ---------------------------------------------------------------- */
+/* solid angle grid                                                  */
+/* ---------------------------------------------------------------- */
+static int solid_angle_impl(xmi_inputFPtr in, xmi_solid_angle **out, char *input_string, int precision,
+                            unsigned long long seed) {
+  const int nr = 1024, nt = 1024;
+  if (!in || !out || !in->initialized) {
+    xmi_set_error("xmi_solid_angle_calculation: input not initialised");
+    return 0;
+  }
+  if (!ensure_device()) return 0;
+  xmi_solid_angle *sa = (xmi_solid_angle *)calloc(1, sizeof(xmi_solid_angle));
+  sa->grid_dims_r_n = nr;
+  sa->grid_dims_theta_n = nt;
+  sa->grid_dims_r_vals = (double *)malloc(sizeof(double) * nr);
+  sa->grid_dims_theta_vals = (double *)malloc(sizeof(double) * nt);
+  sa->solid_angles = (double *)malloc(sizeof(double) * nr * nt);
+  sa->xmi_input_string = input_string ? strdup(input_string) : nullptr;
+  xmi_solid_angle_axes(in, nr, nt, sa->grid_dims_r_vals, sa->grid_dims_theta_vals);
+
+  double *dr = nullptr, *dt = nullptr, *dout = nullptr;
+  bool ok = cuda_ok(cudaMalloc(&dr, sizeof(double) * nr), "cudaMalloc") &&
+            cuda_ok(cudaMalloc(&dt, sizeof(double) * nt), "cudaMalloc") &&
+            cuda_ok(cudaMalloc(&dout, sizeof(double) * nr * nt), "cudaMalloc");
+  if (ok) {
+    cudaMemcpy(dr, sa->grid_dims_r_vals, sizeof(double) * nr, cudaMemcpyHostToDevice);
+    cudaMemcpy(dt, sa->grid_dims_theta_vals, sizeof(double) * nt, cudaMemcpyHostToDevice);
+    xmi::SaGeom g{in->det_radius, in->coll_radius, in->coll_height, in->coll_present};
+    int blocks = num_sms() * 8;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0);
+    if (precision == 0)
+      xmi::solid_angle_grid_kernel<double><<<blocks, 256>>>(g, dr, nr, dt, 0, (long long)nr * nt,
+                                                              (int)hits_per_single, seed, dout);
+    else
+      xmi::solid_angle_grid_kernel<float><<<blocks, 256>>>(g, dr, nr, dt, 0, (long long)nr * nt,
+                                                             (int)hits_per_single, seed, dout);
+    cudaEventRecord(e1);
+    ok = cuda_ok(cudaGetLastError(), "solid_angle_grid_kernel") && cuda_ok(cudaEventSynchronize(e1), "sync");
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    g_timing.transport_ms = ms;
+    g_timing.total_ms = ms;
+    g_timing.launches = 1;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (ok) ok = cuda_ok(cudaMemcpy(sa->solid_angles, dout, sizeof(double) * nr * nt, cudaMemcpyDeviceToHost), "copy");
+  }
+  cudaFree(dr);
+  cudaFree(dt);
+  cudaFree(dout);
+  if (!ok) {
+    xmi_free_solid_angle(sa);
+    return 0;
+  }
+  *out = sa;
+  return 1;
+}
+
+static unsigned long long sa_seed(xmi_inputFPtr in, xmi_main_options *options) {
+  if (in && in->gpu.seed) return in->gpu.seed;
+  if (options && options->use_default_seeds) return 0x5EED0001ull;
+  unsigned long long s = 0;
+  FILE *f = fopen("/dev/urandom", "rb");
+  if (f) {
+    if (fread(&s, sizeof(s), 1, f) != 1) s = 0;
+    fclose(f);
+  }
+  return s ? s : 0x5EED0001ull;
+}
+
+int xmi_solid_angle_calculation_cuda(xmi_inputFPtr inputFPtr, xmi_solid_angle **solid_angle, char *input_string,
+                                     xmi_main_options *options) {
+  return solid_angle_impl(inputFPtr, solid_angle, input_string, inputFPtr ? inputFPtr->gpu.precision : 0,
+                          sa_seed(inputFPtr, options));
+}
+
+void xmi_solid_angle_calculation(xmi_inputFPtr inputFPtr, xmi_solid_angle **solid_angle, char *input_string,
+                                 xmi_main_options *options) {
+  if (!xmi_solid_angle_calculation_cuda(inputFPtr, solid_angle, input_string, options)) *solid_angle = nullptr;
+}
+
+void xmi_free_solid_angle(xmi_solid_angle *sa) {
+  if (!sa) return;
+  free(sa->solid_angles);
+  free(sa->grid_dims_r_vals);
+  free(sa->grid_dims_theta_vals);
+  free(sa->xmi_input_string);
+  free(sa);
+}
+
+/* ---------------------------------------------------------------- */
+/* transport                                                         */
+/* ---------------------------------------------------------------- */
+static int attach_solid_angles(struct xmi_tables_handle *t, xmi_solid_angle *sa) {
+  xmi_bundle *b = &t->b;
+  if (!sa || !sa->solid_angles) {
+    b->sa_nr = b->sa_nt = 0;
+    return 1;
+  }
+  b->sa_nr = (int)sa->grid_dims_r_n;
+  b->sa_nt = (int)sa->grid_dims_theta_n;
+  b->sa_r = sa->grid_dims_r_vals;
+  b->sa_t = sa->grid_dims_theta_vals;
+  b->sa_grid = sa->solid_angles;
+  b->sa_hits_per_single = (int)hits_per_single;
+  return 1;
+}
+
+int xmi_gpu_prepare_run(xmi_inputFPtr in, xmi_hdf5FPtr t, xmi_main_options *options, int n_mpi_hosts,
+                        xmi_solid_angle *sa) {
+  if (!in || !t || !options) {
+    xmi_set_error("xmi_gpu_prepare_run: NULL argument");
+    return 0;
+  }
+  int cascade;
+  if (options->use_cascade_auger == 0 && options->use_cascade_radiative == 0) cascade = XMI_CASCADE_NONE;
+  else if (options->use_cascade_auger == 1 && options->use_cascade_radiative == 0) cascade = XMI_CASCADE_NONRADIATIVE;
+  else if (options->use_cascade_auger == 0 && options->use_cascade_radiative == 1) cascade = XMI_CASCADE_RADIATIVE;
+  else cascade = XMI_CASCADE_FULL;
+  if (cascade != t->cascade_type || options->use_M_lines != t->use_M_lines) {
+    /* tables depend on the cascade type and M-line option: rebuild */
+    xmi_dev_free_tables(t);
+    xmi_bundle_free(&t->b);
+    if (!xmi_bundle_build(in, t, options)) return 0;
+  }
+  xmi_bundle_set_run(in, t, options, n_mpi_hosts, 0, 1);
+  attach_solid_angles(t, sa);
+  if (options->use_variance_reduction && (!sa || !sa->solid_angles)) {
+    xmi_set_error("variance reduction requires a solid angle grid");
+    return 0;
+  }
+  return 1;
+}
+
+}  // extern "C"
+
+template <typename R>
+static bool launch_transport(DevState *s, xmi::DevBundle<R> &d, const xmi_bundle &h, int threads, int blocks_per_sm,
+                             double *ms) {
+  const size_t nh = (size_t)h.n_interactions * h.n_slots;
+  const size_t nc = (size_t)(h.n_interactions + 1) * h.nchannels;
+  const size_t need = 2 * nh + nc;
+  if (need > s->tally_cap) {
+    cudaFree(s->tally);
+    if (!cuda_ok(cudaMalloc(&s->tally, need * sizeof(double)), "cudaMalloc tally")) return false;
+    s->tally_cap = need;
+  }
+  if (!s->counters && !cuda_ok(cudaMalloc(&s->counters, 8 * sizeof(unsigned long long)), "cudaMalloc")) return false;
+  cudaMemsetAsync(s->tally, 0, need * sizeof(double), s->stream);
+  cudaMemsetAsync(s->counters, 0, 8 * sizeof(unsigned long long), s->stream);
+  xmi::DevTally tl;
+  tl.hist_vr = s->tally;
+  tl.hist_brute = s->tally + nh;
+  tl.chan = s->tally + 2 * nh;
+  tl.counters = s->counters;
+  d.items = s->items;
+  d.item_first = s->item_first;
+  d.sa_r = s->sa_r;
+  d.sa_t = s->sa_t;
+  d.sa_nr = h.sa_nr;
+  d.sa_nt = h.sa_nt;
+  d.sa_hits = h.sa_hits_per_single;
+  if (h.sa_nr > 1) {
+    d.sa_r0 = h.sa_r[0];
+    d.sa_rinv = (h.sa_nr - 1) / (h.sa_r[h.sa_nr - 1] - h.sa_r[0]);
+    d.sa_t0 = h.sa_t[0];
+    d.sa_tinv = (h.sa_nt - 1) / (h.sa_t[h.sa_nt - 1] - h.sa_t[0]);
+  }
+  if (sizeof(R) == 8) d.sa_grid = (const R *)s->sa_g64;
+  else d.sa_grid = (const R *)s->sa_g32;
+
+  size_t smem = nh * sizeof(double);
+  int use_smem = (h.use_vr && smem <= 160 * 1024) ? 1 : 0;
+  if (use_smem && smem > 48 * 1024)
+    cudaFuncSetAttribute(xmi::transport_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (!use_smem) smem = 0;
+  int blocks = num_sms() * blocks_per_sm;
+  long long n = h.n_photons_total;
+  if ((long long)blocks * threads > n) blocks = (int)((n + threads - 1) / threads);
+  if (blocks < 1) blocks = 1;
+  cudaEventRecord(s->ev0, s->stream);
+  if (n > 0) xmi::transport_kernel<R><<<blocks, threads, smem, s->stream>>>(d, tl, 0, n, use_smem);
+  cudaEventRecord(s->ev1, s->stream);
+  if (!cuda_ok(cudaGetLastError(), "transport_kernel launch")) return false;
+  if (!cuda_ok(cudaEventSynchronize(s->ev1), "transport_kernel")) return false;
+  float f = 0.f;
+  cudaEventElapsedTime(&f, s->ev0, s->ev1);
+  *ms = f;
+  return true;
+}
+
+extern "C" int xmi_main_msim(xmi_inputFPtr in, xmi_hdf5FPtr t, int n_mpi_hosts, double **channels_out,
+                  xmi_main_options *options, double **brute_out, double **var_red_out, xmi_solid_angle *sa) {
+  cudaEvent_t all0, all1;
+  if (!ensure_device()) return 0;
+  if (!xmi_gpu_prepare_run(in, t, options, n_mpi_hosts, sa)) return 0;
+  const xmi_bundle &h = t->b;
+  const int precision = in->gpu.precision;
+  if (!xmi_dev_sync_tables(t, precision)) return 0;
+  DevState *s = state_of(t);
+  cudaEventCreate(&all0);
+  cudaEventCreate(&all1);
+  cudaEventRecord(all0, s->stream);
+
+  /* source items and their work offsets */
+  std::vector<long long> first(h.n_items > 0 ? h.n_items : 1, 0);
+  for (int i = 1; i < h.n_items; i++) first[i] = first[i - 1] + h.items[i - 1].n_photons;
+  if (h.n_items > s->items_cap) {
+    cudaFree(s->items);
+    cudaFree(s->item_first);
+    if (!cuda_ok(cudaMalloc(&s->items, sizeof(xmi_source_item) * h.n_items), "cudaMalloc items") ||
+        !cuda_ok(cudaMalloc(&s->item_first, sizeof(long long) * h.n_items), "cudaMalloc items"))
+      return 0;
+    s->items_cap = h.n_items;
+  }
+  if (h.n_items > 0) {
+    cudaMemcpyAsync(s->items, h.items, sizeof(xmi_source_item) * h.n_items, cudaMemcpyHostToDevice, s->stream);
+    cudaMemcpyAsync(s->item_first, first.data(), sizeof(long long) * h.n_items, cudaMemcpyHostToDevice, s->stream);
+  }
+  /* solid-angle grid (kept on the device while the caller's grid is the same) */
+  if (h.sa_nr > 0 && (s->sa_src != h.sa_grid || s->sa_n != h.sa_nr * h.sa_nt)) {
+    size_t n = (size_t)h.sa_nr * h.sa_nt;
+    cudaFree(s->sa_r);
+    cudaFree(s->sa_t);
+    cudaFree(s->sa_g64);
+    cudaFree(s->sa_g32);
+    if (!cuda_ok(cudaMalloc(&s->sa_r, sizeof(double) * h.sa_nr), "cudaMalloc") ||
+        !cuda_ok(cudaMalloc(&s->sa_t, sizeof(double) * h.sa_nt), "cudaMalloc") ||
+        !cuda_ok(cudaMalloc(&s->sa_g64, sizeof(double) * n), "cudaMalloc") ||
+        !cuda_ok(cudaMalloc(&s->sa_g32, sizeof(float) * n), "cudaMalloc"))
+      return 0;
+    std::vector<float> g32(n);
+    for (size_t i = 0; i < n; i++) g32[i] = (float)h.sa_grid[i];
+    cudaMemcpy(s->sa_r, h.sa_r, sizeof(double) * h.sa_nr, cudaMemcpyHostToDevice);
+    cudaMemcpy(s->sa_t, h.sa_t, sizeof(double) * h.sa_nt, cudaMemcpyHostToDevice);
+    cudaMemcpy(s->sa_g64, h.sa_grid, sizeof(double) * n, cudaMemcpyHostToDevice);
+    cudaMemcpy(s->sa_g32, g32.data(), sizeof(float) * n, cudaMemcpyHostToDevice);
+    s->sa_src = h.sa_grid;
+    s->sa_n = (int)n;
+  }
+
+  const int threads = in->gpu.threads_per_block > 0 ? in->gpu.threads_per_block : 128;
+  const int bps = in->gpu.blocks_per_sm > 0 ? in->gpu.blocks_per_sm : 4;
+  double ms = 0.0;
+  bool ok = precision == 0 ? launch_transport<double>(s, s->b64, h, threads, bps, &ms)
+                           : launch_transport<float>(s, s->b32, h, threads, bps, &ms);
+  if (!ok) return 0;
+
+  const int N = h.n_interactions, nch = h.nchannels, S = h.n_slots;
+  const size_t nh = (size_t)N * S, nc = (size_t)(N + 1) * nch;
+  std::vector<double> tally(2 * nh + nc);
+  unsigned long long counters[8];
+  cudaMemcpyAsync(tally.data(), s->tally, sizeof(double) * tally.size(), cudaMemcpyDeviceToHost, s->stream);
+  cudaMemcpyAsync(counters, s->counters, sizeof(counters), cudaMemcpyDeviceToHost, s->stream);
+  cudaEventRecord(all1, s->stream);
+  if (!cuda_ok(cudaStreamSynchronize(s->stream), "copy back")) return 0;
+  if (counters[1] != 0) {
+    xmi_set_error("transport kernel reported error code %llu", counters[1]);
+    return 0;
+  }
+  const double *hv = tally.data(), *hb = tally.data() + nh, *chan = tally.data() + 2 * nh;
+
+  /* channels: per-order scatter tallies plus the fluorescence lines derived
+   * from the per-order line histories, then cumulative over orders */
+  double *channels = (double *)calloc(nc, sizeof(double));
+  std::vector<double> per(nc, 0.0);
+  for (size_t i = 0; i < nc; i++) per[i] = chan[i];
+  if (h.use_vr)
+    for (int n = 1; n <= N; n++)
+      for (int sl = 0; sl < h.n_lines; sl++) {
+        int ch = h.line_channel[sl];
+        if (ch >= 0) per[(size_t)n * nch + ch] += hv[(size_t)(n - 1) * S + sl];
+      }
+  for (int i = 0; i <= N; i++)
+    for (int k = 0; k <= i; k++)
+      for (int c = 0; c < nch; c++) channels[(size_t)i * nch + c] += per[(size_t)k * nch + c];
+  for (size_t i = 0; i < nc; i++) channels[i] *= h.live_time;
+
+  /* histories in the reference layout ((Z-1)*385 + line-1)*N + k-1 */
+  const size_t hsz = (size_t)100 * 385 * N;
+  double *brute = (double *)calloc(hsz, sizeof(double));
+  double *var_red = h.use_vr ? (double *)calloc(hsz, sizeof(double)) : nullptr;
+  const double scale = h.live_time * n_mpi_hosts;
+  for (int n = 1; n <= N; n++)
+    for (int sl = 0; sl < S; sl++) {
+      int e, line;
+      if (sl < h.n_lines) {
+        e = h.line_elem[sl];
+        line = h.line_index[sl];
+      } else {
+        e = (sl - h.n_lines) / 2;
+        line = 384 + (sl - h.n_lines) % 2;
+      }
+      size_t idx = ((size_t)(h.elem_Z[e] - 1) * 385 + (line - 1)) * N + (n - 1);
+      brute[idx] = hb[(size_t)(n - 1) * S + sl] * scale;
+      if (var_red) var_red[idx] = hv[(size_t)(n - 1) * S + sl] * scale;
+    }
+  float tot = 0.f;
+  cudaEventElapsedTime(&tot, all0, all1);
+  cudaEventDestroy(all0);
+  cudaEventDestroy(all1);
+  g_timing.transport_ms = ms;
+  g_timing.total_ms = tot;
+  g_timing.launches = 1;
+  *channels_out = channels;
+  *brute_out = brute;
+  *var_red_out = var_red;
+  return 1;
+}
+
+

@@ -1,0 +1,123 @@
+/*
+ * Solid-angle grid kernel: xmi_solid_angle_calculation_f
+ * (src/xmi_solid_angle_f.F90:303-429) / the OpenCL kernel
+ * (src/xmi_kernels.cl:219-453), one warp per (r, theta) grid point.
+ *
+ * Each cone sample i of a point draws its two uniforms from Philox block i
+ * of the point's stream (seed, point, 0xF0000000), so the lanes of a warp
+ * take samples i = lane, lane+32, ... independently and the hit count is
+ * exactly that of the sequential oracle.  FP32 and FP64 variants use the
+ * same draws.  The work is FP32/FP64 issue-bound (about 40 flops and 3-5
+ * transcendental ops per sample, no memory traffic beyond the result).
+ */
+#ifndef XMIMSIM_GB300_SOLID_ANGLE_CUH
+#define XMIMSIM_GB300_SOLID_ANGLE_CUH
+
+#include "transport.cuh"
+
+namespace xmi {
+
+struct SaGeom {
+  double det_radius, coll_radius, coll_height;
+  int coll_present;
+};
+
+template <typename R>
+__device__ __forceinline__ bool sa_setup(const SaGeom &s, R r1, R theta1, R &cfca, R &fcsa, R &st, R &ct, R &py,
+                                         R &pz, bool &outside) {
+  R r, theta, fcbr;
+  const R detr = (R)s.det_radius, collr = (R)s.coll_radius, collh = (R)s.coll_height;
+  if (!s.coll_present) {
+    r = r1; theta = theta1; fcbr = detr; outside = false;
+  } else if (fabs(collr - detr) < (R)0.000001) {
+    if (r1 * cos(theta1) <= detr) {
+      r = r1; theta = theta1; fcbr = detr;
+    } else {
+      r = sqrt(r1 * r1 - (R)2.0 * r1 * sin(theta1) * collh + collh * collh);
+      theta = acos(r1 * cos(theta1) / r);
+      fcbr = collr;
+    }
+    outside = r1 * sin(theta1) > collh;
+  } else {
+    if (r1 * cos(theta1) <= detr && r1 * sin(theta1) <= collh * (r1 * cos(theta1) - detr) / (collr - detr)) {
+      r = r1; theta = theta1; fcbr = detr;
+    } else if (r1 * sin(theta1) <= collh) {
+      return false;
+    } else {
+      r = sqrt(r1 * r1 - (R)2.0 * r1 * sin(theta1) * collh + collh * collh);
+      theta = acos(r1 * cos(theta1) / r);
+      fcbr = collr;
+    }
+    outside = r1 * sin(theta1) > collh;
+  }
+  R beta = atan(fcbr / r);
+  R alpha1 = atan(fcbr * sin(theta) / (r - fcbr * cos(theta)));
+  if (alpha1 <= (R)0) alpha1 = alpha1 + (R)kPi;
+  R fca = beta > alpha1 ? beta : alpha1;
+  cfca = cos(fca);
+  fcsa = (R)(2 * kPi) * ((R)1 - cfca);
+  st = sin(theta);
+  ct = cos(theta);
+  py = r1 * cos(theta1);
+  pz = r1 * sin(theta1);
+  return true;
+}
+
+template <typename R>
+__device__ __forceinline__ int sa_sample(const SaGeom &s, R cfca, R st, R ct, R py, R pz, bool outside, R u1, R u2) {
+  const R detr = (R)s.det_radius, collr = (R)s.coll_radius, collh = (R)s.coll_height;
+  R th = acos((R)1 - u1 * ((R)1 - cfca));
+  R ph = u2 * (R)2 * (R)kPi;
+  R sth = sin(th);
+  R dcx = sth * cos(ph), dcy = sth * sin(ph), dcz = cos(th);
+  R dx = dcx, dy = -st * dcy - ct * dcz, dz = ct * dcy - st * dcz;
+  if (dz >= (R)0) return 0;
+  if (outside) {
+    R q = (collh - pz) / dz;
+    R ix = q * dx, iy = q * dy + py;
+    if (sqrt(ix * ix + iy * iy) > collr) return 0;
+  }
+  R q = (-pz) / dz;
+  R ix = q * dx, iy = q * dy + py, iz = q * dz + pz;
+  return sqrt(ix * ix + iy * iy + iz * iz) <= detr ? 1 : 0;
+}
+
+/* out[t*nr + r] = solid angle of grid point (r_vals[r], t_vals[t]) */
+template <typename R>
+__global__ void __launch_bounds__(256) solid_angle_grid_kernel(SaGeom s, const double *r_vals, int nr,
+                                                                const double *t_vals, long long p0, long long p1,
+                                                                int hits_per_single, unsigned long long seed,
+                                                                double *out) {
+  const int lane = threadIdx.x & 31;
+  const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
+  for (long long p = p0 + (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); p < p1; p += warps) {
+    const int it = (int)(p / nr), ir = (int)(p % nr);
+    R cfca, fcsa, st, ct, py, pz;
+    bool outside;
+    int hits = 0;
+    bool live = sa_setup<R>(s, (R)r_vals[ir], (R)t_vals[it], cfca, fcsa, st, ct, py, pz, outside);
+    if (live) {
+      for (int i = lane; i < hits_per_single; i += 32) {
+        xmi_u32x4 c;
+        c.v[0] = (uint32_t)i;
+        c.v[1] = 0xF0000000u;
+        c.v[2] = (uint32_t)p;
+        c.v[3] = (uint32_t)((unsigned long long)p >> 32);
+        xmi_u32x4 o = xmi_philox4x32_10(c, (uint32_t)seed, (uint32_t)(seed >> 32));
+        double d1 = ((double)(o.v[0] >> 5) * 67108864.0 + (double)(o.v[1] >> 6)) * (1.0 / 9007199254740992.0);
+        double d2 = ((double)(o.v[2] >> 5) * 67108864.0 + (double)(o.v[3] >> 6)) * (1.0 / 9007199254740992.0);
+        R u1 = (R)d1, u2 = (R)d2;
+        if (sizeof(R) == 4) {
+          u1 = u1 < (R)1 ? u1 : (R)0x1.fffffep-1f;
+          u2 = u2 < (R)1 ? u2 : (R)0x1.fffffep-1f;
+        }
+        hits += sa_sample<R>(s, cfca, st, ct, py, pz, outside, u1, u2);
+      }
+    }
+    hits = __reduce_add_sync(0xffffffffu, hits);
+    if (lane == 0) out[p - p0] = live ? (double)(fcsa * (R)hits / (R)hits_per_single) : 0.0;
+  }
+}
+
+}  // namespace xmi
+#endif

@@ -1,0 +1,1070 @@
+/*
+ * Photon transport with the point-detector variance-reduction estimator,
+ * GB300 kernel.  Behaviour follows the reference step for step
+ * (src/xmi_main.F90:1188-1685 xmi_simulate_photon and the interaction
+ * routines, src/xmi_variance_reduction.F90:29-1101); the structure is the
+ * GPU's own:
+ *  - one thread per photon history, persistent grid-stride loop over a
+ *    compact work index (history-based: with variance reduction every photon
+ *    makes the same number of forced interactions, so trip counts are
+ *    uniform and the estimator -- the dominant cost -- runs converged);
+ *  - random numbers from Philox streams keyed (photon, phase, draw), so a
+ *    photon's sequence does not depend on the launch shape;
+ *  - layer loops fully unrolled over XMI_MAXL with predicates, keeping the
+ *    per-layer attenuation state in registers;
+ *  - one energy-grid location per energy change, reused by every table;
+ *  - line-history tallies accumulated per CTA in shared memory (warp
+ *    pre-reduced when the lanes agree), flushed once with FP64 atomics;
+ *    fluorescence channel contributions are derived from those histories
+ *    after the kernel, Rayleigh/Compton channel contributions go straight to
+ *    FP64 global atomics.
+ */
+#ifndef XMIMSIM_GB300_TRANSPORT_CUH
+#define XMIMSIM_GB300_TRANSPORT_CUH
+
+#include "dev_bundle.cuh"
+
+namespace xmi {
+
+enum : unsigned long long { kErrNone = 0, kErrGeometry = 1, kErrTable = 2, kErrCompton = 3,
+                            kErrSource = 4, kErrLayer = 5 };
+
+template <typename R>
+struct Photon {
+  double c[3];
+  R d[3], el[3];
+  R theta, phi, E, w, we;
+  R mus[XMI_MAXL];
+  int layer, elem, n_int, last, inside, hit;
+  int h_type, h_elem, h_slot; /* most recent recorded interaction */
+  long long id;
+};
+
+__device__ __forceinline__ void set_error(const DevTally &t, unsigned long long code) {
+  atomicCAS(&t.counters[1], 0ull, code);
+}
+
+/* ---------------- math helpers ---------------- */
+template <typename R> __device__ __forceinline__ R rdot(const R *a, const R *b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+template <typename R> __device__ __forceinline__ void rnorm(R *a) {
+  R n = sqrt(rdot(a, a));
+  a[0] /= n; a[1] /= n; a[2] /= n;
+}
+template <typename R> __device__ __forceinline__ void matvec(const double *m, const R *v, R *r) {
+  r[0] = (R)m[0] * v[0] + (R)m[1] * v[1] + (R)m[2] * v[2];
+  r[1] = (R)m[3] * v[0] + (R)m[4] * v[1] + (R)m[5] * v[2];
+  r[2] = (R)m[6] * v[0] + (R)m[7] * v[1] + (R)m[8] * v[2];
+}
+__device__ __forceinline__ void matvec_d(const double *m, const double *v, double *r) {
+  r[0] = m[0] * v[0] + m[1] * v[1] + m[2] * v[2];
+  r[1] = m[3] * v[0] + m[4] * v[1] + m[5] * v[2];
+  r[2] = m[6] * v[0] + m[7] * v[1] + m[8] * v[2];
+}
+
+/* distance from p along direction d (unit) to the plane z' = zp of the sample
+ * frame (normal n), computed in FP64: xmi_intersection_plane_line +
+ * xmi_distance_two_points */
+template <typename R>
+__device__ __forceinline__ bool plane_step(const double *p, const R *d, const double *n, double zp,
+                                           double *ip, double *dist) {
+  double dd[3] = {(double)d[0], (double)d[1], (double)d[2]};
+  double itn = dd[0] * n[0] + dd[1] * n[1] + dd[2] * n[2];
+  if (itn == 0.0) return false;
+  double s = ((0.0 - p[0]) * n[0] + (0.0 - p[1]) * n[1] + (zp - p[2]) * n[2]) / itn;
+  ip[0] = s * dd[0] + p[0];
+  ip[1] = s * dd[1] + p[1];
+  ip[2] = s * dd[2] + p[2];
+  double e0 = p[0] - ip[0], e1 = p[1] - ip[1], e2 = p[2] - ip[2];
+  *dist = sqrt(e0 * e0 + e1 * e1 + e2 * e2);
+  return true;
+}
+
+/* uniform draw in the working precision; FP32 uses the rounded FP64 draw so
+ * that FP32 and FP64 runs consume identical random sequences */
+template <typename R> __device__ __forceinline__ R uni(xmi_rng *g);
+template <> __device__ __forceinline__ double uni<double>(xmi_rng *g) { return xmi_rng_uniform(g); }
+template <> __device__ __forceinline__ float uni<float>(xmi_rng *g) {
+  float u = (float)xmi_rng_uniform(g);
+  return u < 1.0f ? u : 0x1.fffffep-1f;
+}
+
+/* energy-grid location, same rule as xmi_grid_locate of the bundle */
+template <typename R>
+__device__ __forceinline__ void locate(const DevBundle<R> &b, R E, int &node, R &f) {
+  double Ed = (double)E;
+  if (Ed <= b.seg_lo[0]) { node = 0; f = (R)0; return; }
+  if (Ed >= b.seg_lo[b.n_seg]) { node = b.n_nodes - 2; f = (R)1; return; }
+  int lo = 0, hi = b.n_seg - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (Ed >= b.seg_lo[mid]) lo = mid; else hi = mid - 1;
+  }
+  R t = (log(E) - (R)b.seg_lnlo[lo]) * (R)b.seg_invh[lo];
+  int i = (int)t;
+  int n = b.seg_n[lo];
+  if (i < 0) i = 0;
+  if (i > n - 2) i = n - 2;
+  node = b.seg_off[lo] + i;
+  f = t - (R)i;
+}
+
+template <typename R>
+__device__ __forceinline__ R el_val(const DevBundle<R> &b, int e, int col, int node, R f) {
+  const R *t = b.el_tab + ((size_t)e * b.n_nodes + node) * XMI_EL_REC + col;
+  R v0 = __ldg(t), v1 = __ldg(t + XMI_EL_REC);
+  return v0 + f * (v1 - v0);
+}
+
+template <typename R>
+__device__ __forceinline__ void mu_calc(const DevBundle<R> &b, R E, R *mus) {
+  int node;
+  R f;
+  locate(b, E, node, f);
+  const R *t = b.mu_tab + (size_t)node * XMI_MAXL;
+#pragma unroll
+  for (int j = 0; j < XMI_MAXL; j++) {
+    R v0 = __ldg(t + j), v1 = __ldg(t + XMI_MAXL + j);
+    mus[j] = v0 + f * (v1 - v0);
+  }
+}
+
+/* findpos (src/xmi_aux_f.F90:1305) on a uniform axis: same result as the
+ * linear scan, found from an arithmetic guess and a +-1 correction */
+template <typename R>
+__device__ __forceinline__ int findpos_u(const R *a, int n, R x, R a0, R inv_dx) {
+  if (fabs(x - __ldg(a)) < (R)1e-10) return 0;
+  R gr = ceil((x - a0) * inv_dx);
+  int i = gr < (R)1 ? 1 : (gr > (R)(n - 1) ? n - 1 : (int)gr);
+  while (i > 1 && x <= __ldg(a + i - 1)) i--;
+  while (i < n && x > __ldg(a + i)) i++;
+  return i >= n ? -1 : i - 1;
+}
+
+/* bilinear_interpolation (src/xmi_aux_f.F90:1337) of a2[i2*n1+i1] */
+template <typename R>
+__device__ __forceinline__ R bilinear(const R *a2, const R *a, int n1, R a0, R ainv, const R *bb, int n2, R b0,
+                                      R binv, R x1, R x2, bool &ok) {
+  int p1 = findpos_u(a, n1, x1, a0, ainv), p2 = findpos_u(bb, n2, x2, b0, binv);
+  if (p1 < 0 || p2 < 0) { ok = false; return (R)0; }
+  R a_0 = __ldg(a + p1), a_1 = __ldg(a + p1 + 1), b_0 = __ldg(bb + p2), b_1 = __ldg(bb + p2 + 1);
+  R denom = (a_1 - a_0) * (b_1 - b_0);
+  R c1 = (a_1 - x1) * (b_1 - x2) / denom;
+  R c2 = (x1 - a_0) * (b_1 - x2) / denom;
+  R c3 = (a_1 - x1) * (x2 - b_0) / denom;
+  R c4 = (x1 - a_0) * (x2 - b_0) / denom;
+  const R *r0 = a2 + (size_t)p2 * n1 + p1, *r1 = r0 + n1;
+  return c1 * __ldg(r0) + c2 * __ldg(r0 + 1) + c3 * __ldg(r1) + c4 * __ldg(r1 + 1);
+}
+
+template <typename R>
+__device__ __forceinline__ R qtab(const R *t, R q) {
+  R x = q * (R)((XMI_NQ - 1) / XMI_QMAX);
+  int i = (int)x;
+  if (i < 0) i = 0;
+  if (i > XMI_NQ - 2) i = XMI_NQ - 2;
+  R f = x - (R)i;
+  R v0 = __ldg(t + i), v1 = __ldg(t + i + 1);
+  return v0 + f * (v1 - v0);
+}
+
+/* ---------------- tallies ---------------- */
+__device__ __forceinline__ double warp_sum(unsigned mask, double v) {
+  for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(mask, v, off);
+  return v;
+}
+
+/* atomicAdd with warp pre-reduction when every active lane targets the same
+ * address (the common case in the estimator's element and line loops) */
+__device__ __forceinline__ void tally_add(double *addr, double v) {
+  unsigned mask = __activemask();
+  int pred;
+  __match_all_sync(mask, (unsigned long long)addr, &pred);
+  if (pred && mask == 0xffffffffu) {
+    double s = warp_sum(mask, v);
+    if ((threadIdx.x & 31) == 0) atomicAdd(addr, s);
+  } else {
+    atomicAdd(addr, v);
+  }
+}
+
+template <typename R>
+__device__ __forceinline__ void tally_channel(const DevBundle<R> &b, const DevTally &t, int n, R E, double w) {
+  int ch = -1;
+  if (E >= (R)kEnergyThreshold) ch = (int)(((double)E - b.zero) / b.gain);
+  if (ch >= 0 && ch <= b.nch - 1) tally_add(&t.chan[(size_t)n * b.nch + ch], w);
+}
+
+/* ---------------- solid angle ---------------- */
+/* xmi_single_solid_angle_calculation (src/xmi_solid_angle_f.F90:432-710) */
+template <typename R>
+__device__ R single_solid_angle(const DevBundle<R> &b, R r1, R theta1, xmi_rng *g, int hits_per_single) {
+  R r, theta, fcbr;
+  bool outside;
+  const R detr = (R)b.det_radius, collr = (R)b.coll_radius, collh = (R)b.coll_height;
+  if (!b.coll_present) {
+    r = r1; theta = theta1; fcbr = detr; outside = false;
+  } else if (fabs(collr - detr) < (R)0.000001) {
+    if (r1 * cos(theta1) <= detr) {
+      r = r1; theta = theta1; fcbr = detr;
+    } else {
+      r = sqrt(r1 * r1 - (R)2.0 * r1 * sin(theta1) * collh + collh * collh);
+      theta = acos(r1 * cos(theta1) / r);
+      fcbr = collr;
+    }
+    outside = r1 * sin(theta1) > collh;
+  } else {
+    if (r1 * cos(theta1) <= detr && r1 * sin(theta1) <= collh * (r1 * cos(theta1) - detr) / (collr - detr)) {
+      r = r1; theta = theta1; fcbr = detr;
+    } else if (r1 * sin(theta1) <= collh) {
+      return (R)0;
+    } else {
+      r = sqrt(r1 * r1 - (R)2.0 * r1 * sin(theta1) * collh + collh * collh);
+      theta = acos(r1 * cos(theta1) / r);
+      fcbr = collr;
+    }
+    outside = r1 * sin(theta1) > collh;
+  }
+  R beta = atan(fcbr / r);
+  R alpha1 = atan(fcbr * sin(theta) / (r - fcbr * cos(theta)));
+  if (alpha1 <= (R)0) alpha1 = alpha1 + (R)kPi;
+  R fca = beta > alpha1 ? beta : alpha1;
+  R cfca = cos(fca);
+  R fcsa = (R)(2 * kPi) * ((R)1 - cfca);
+  R st = sin(theta), ct = cos(theta);
+  R py = r1 * cos(theta1), pz = r1 * sin(theta1);
+  int hits = 0;
+  for (int i = 0; i < hits_per_single; i++) {
+    R th = acos((R)1 - uni<R>(g) * ((R)1 - cfca));
+    R ph = uni<R>(g) * (R)2 * (R)kPi;
+    R sth = sin(th);
+    R dcx = sth * cos(ph), dcy = sth * sin(ph), dcz = cos(th);
+    /* rotation rows (1,0,0), (0,-sin,-cos), (0,cos,-sin) */
+    R dx = dcx, dy = -st * dcy - ct * dcz, dz = ct * dcy - st * dcz;
+    if (dz >= (R)0) continue;
+    if (outside) {
+      R s = (collh - pz) / dz;
+      R ix = s * dx, iy = s * dy + py;
+      if (sqrt(ix * ix + iy * iy) > collr) continue;
+    }
+    R s = (-pz) / dz;
+    R ix = s * dx, iy = s * dy + py, iz = s * dz + pz;
+    if (sqrt(ix * ix + iy * iy + iz * iz) <= detr) hits++;
+  }
+  return fcsa * (R)hits / (R)hits_per_single;
+}
+
+/* xmi_get_solid_angle (src/xmi_solid_angle_f.F90:712-801) */
+template <typename R>
+__device__ R get_solid_angle(const DevBundle<R> &b, const double *coords, const Photon<R> &p, const DevTally &t,
+                             bool &ok) {
+  double dv[3] = {coords[0] - b.p_det[0], coords[1] - b.p_det[1], coords[2] - b.p_det[2]};
+  double rr = sqrt(dv[0] * dv[0] + dv[1] * dv[1] + dv[2] * dv[2]);
+  double inv = 1.0 / rr;
+  R dn[3] = {(R)(dv[0] * inv), (R)(dv[1] * inv), (R)(dv[2] * inv)};
+  R nd[3] = {(R)b.n_det[0], (R)b.n_det[1], (R)b.n_det[2]};
+  R tt = acos(rdot(dn, nd));
+  R r = (R)rr;
+  if (tt > (R)(kPi / 2.0)) tt = (R)kPi - tt;
+  R theta = (R)(kPi / 2.0) - tt;
+  if (theta < (R)b.sa_t[0]) return (R)0;
+  int p1 = findpos_u<double>(b.sa_r, b.sa_nr, (double)r, b.sa_r0, b.sa_rinv);
+  int p2 = findpos_u<double>(b.sa_t, b.sa_nt, (double)theta, b.sa_t0, b.sa_tinv);
+  if (p1 == -1 || p2 == -1) {
+    xmi_rng g;
+    xmi_rng_init(&g, b.seed, (uint64_t)p.id, 0x80000000u | (uint32_t)p.n_int);
+    atomicAdd(&t.counters[0], 1ull);
+    return single_solid_angle(b, r, theta, &g, b.sa_hits);
+  }
+  /* bilinear on the grid; axes are FP64, values in R */
+  double a0 = b.sa_r[p1], a1 = b.sa_r[p1 + 1], b0 = b.sa_t[p2], b1 = b.sa_t[p2 + 1];
+  double x1 = (double)r, x2 = (double)theta;
+  R denom = (R)((a1 - a0) * (b1 - b0));
+  R c1 = (R)((a1 - x1) * (b1 - x2)) / denom;
+  R c2 = (R)((x1 - a0) * (b1 - x2)) / denom;
+  R c3 = (R)((a1 - x1) * (x2 - b0)) / denom;
+  R c4 = (R)((x1 - a0) * (x2 - b0)) / denom;
+  const R *g0 = b.sa_grid + (size_t)p2 * b.sa_nr + p1, *g1 = g0 + b.sa_nr;
+  (void)ok;
+  return c1 * __ldg(g0) + c2 * __ldg(g0 + 1) + c3 * __ldg(g1) + c4 * __ldg(g1 + 1);
+}
+
+/* ---------------- photon kinematics ---------------- */
+/* xmi_update_photon_dirv (src/xmi_main.F90:5071-5148) */
+template <typename R>
+__device__ __forceinline__ void update_dirv(Photon<R> &p, R theta_i, R phi_i) {
+  R phn;
+  if (phi_i > (R)(2.0 * kPi)) phn = phi_i - (R)(2.0 * kPi);
+  else if (phi_i < (R)0) phn = phi_i + (R)(2.0 * kPi);
+  else phn = phi_i;
+  R cphi = cos(p.phi), sphi = sin(p.phi), cth = cos(p.theta), sth = sin(p.theta);
+  R ts = sin(theta_i);
+  R dx = ts * cos(phn), dy = ts * sin(phn), dz = cos(theta_i);
+  p.d[0] = cth * cphi * dx - sphi * dy + sth * cphi * dz;
+  p.d[1] = cth * sphi * dx + cphi * dy + sth * sphi * dz;
+  p.d[2] = -sth * dx + cth * dz;
+  rnorm(p.d);
+  p.theta = acos(p.d[2]);
+  p.phi = atan2(p.d[1], p.d[0]);
+  if (p.phi > (R)(2.0 * kPi)) p.phi = p.phi - (R)(2.0 * kPi);
+  else if (p.phi < (R)0) p.phi = p.phi + (R)(2.0 * kPi);
+}
+
+/* xmi_update_photon_elecv (src/xmi_main.F90:5150-5182) */
+template <typename R>
+__device__ __forceinline__ void update_elecv(Photon<R> &p) {
+  R cosalfa = rdot(p.d, p.el);
+  R c_alfa = acos(cosalfa);
+  R c_ae = (R)1 / sin(c_alfa), c_be = -c_ae * cosalfa;
+#pragma unroll
+  for (int k = 0; k < 3; k++) p.el[k] = c_ae * p.el[k] + c_be * p.d[k];
+  rnorm(p.el);
+}
+
+template <typename R>
+__device__ __forceinline__ R polarisation_phi0(const Photon<R> &p) {
+  R cphi = cos(p.phi), sphi = sin(p.phi), cth = cos(p.theta), sth = sin(p.theta);
+  R cosphi0 = p.el[0] * cphi * cth + p.el[1] * cth * sphi - p.el[2] * sth;
+  R sinphi0 = p.el[0] * sphi - p.el[1] * cphi;
+  if (fabs(cosphi0) > (R)1) cosphi0 = cosphi0 > (R)0 ? (R)1 : (R)-1;
+  R phi0 = acos(cosphi0);
+  if (sinphi0 > (R)0) phi0 = -phi0;
+  return phi0;
+}
+
+/* Doppler-broadened Compton energy: src/xmi_main.F90:4985-5067 (transport)
+ * and src/xmi_variance_reduction.F90:1010-1101 (estimator) */
+template <typename R>
+__device__ R compton_energy(const DevBundle<R> &b, int e, R E, R theta_i, xmi_rng *g, bool varred, bool &ok) {
+  const R c = (R)(double)1.2399e-6f, c0 = (R)(double)4.85e-12f, c1 = (R)(double)1.456e-2f;
+  const R *rn = b.dop_r, *icdf = b.dop_icdf + (size_t)e * XMI_DOPPLER_N;
+  const R dr = __ldg(rn + 1) - __ldg(rn);
+  R energy = E * (R)1000, c_lamb0 = c / energy, sth2 = sin(theta_i / (R)2);
+  int it = 0;
+  for (int tries = 0; tries < 100000; tries++) {
+    R r = uni<R>(g);
+    int pos = (int)(r / dr);
+    if (varred && pos == XMI_DOPPLER_N - 2) continue;
+    if (pos > XMI_DOPPLER_N - 2) pos = XMI_DOPPLER_N - 2;
+    R r0 = __ldg(rn + pos), r1 = __ldg(rn + pos + 1), q0 = __ldg(icdf + pos), q1 = __ldg(icdf + pos + 1);
+    R pz = q0 + ((q1 - q0) * (r - r0) / (r1 - r0));
+    if (uni<R>(g) < (R)0.5) pz = -pz;
+    R dlamb = c0 * sth2 * sth2 - c1 * c_lamb0 * sth2 * pz;
+    R c_lamb = c_lamb0 + dlamb;
+    energy = c / c_lamb / (R)1000;
+    if (energy <= E) return energy;
+    if (varred) {
+      if (it == 100) break;
+      it++;
+    }
+  }
+  ok = false;
+  return (R)0;
+}
+
+/* ---------------- variance reduction ---------------- */
+/* xmi_variance_reduction (src/xmi_variance_reduction.F90:29-726) */
+template <typename R>
+__device__ void variance_reduction(const DevBundle<R> &b, Photon<R> &p, xmi_rng *g, const DevTally &t,
+                                   double *s_hist, bool use_smem, bool &ok) {
+  if (p.E <= (R)kEnergyThreshold) return;
+  const int n = p.n_int, layer = p.layer;
+  R radius = sqrt(uni<R>(g)) * (R)b.det_radius;
+  R ang = (R)(2.0 * kPi) * uni<R>(g);
+  R dp[3] = {(R)0, cos(ang) * radius, sin(ang) * radius};
+  double rel[3] = {p.c[0] - b.p_det[0], p.c[1] - b.p_det[1], p.c[2] - b.p_det[2]};
+  double lcp_d[3];
+  matvec_d(b.det_inv, rel, lcp_d);
+  R lcp[3] = {(R)lcp_d[0], (R)lcp_d[1], (R)lcp_d[2]};
+  R dirv[3];
+  matvec(b.det_inv, p.d, dirv);
+  R lcd[3] = {dp[0] - lcp[0], dp[1] - lcp[1], dp[2] - lcp[2]};
+  if (lcd[0] >= (R)0) return;
+  double total_distance;
+  {
+    double e0 = (double)dp[0] - lcp_d[0], e1 = (double)dp[1] - lcp_d[1], e2 = (double)dp[2] - lcp_d[2];
+    total_distance = sqrt(e0 * e0 + e1 * e1 + e2 * e2);
+  }
+  rnorm(dirv);
+  rnorm(lcd);
+  R ndc[3];
+  matvec(b.det_new, lcd, ndc);
+  R dotprod = rdot(dirv, lcd);
+  dotprod = dotprod > (R)1 ? (R)1 : (dotprod < (R)-1 ? (R)-1 : dotprod);
+  const R theta = acos(dotprod);
+  R proj[3];
+  {
+    R d = rdot(ndc, p.d);
+#pragma unroll
+    for (int k = 0; k < 3; k++) proj[k] = ndc[k] - d * p.d[k];
+    rnorm(proj);
+    R ne = sqrt(rdot(p.el, p.el));
+    dotprod = (proj[0] * (p.el[0] / ne) + proj[1] * (p.el[1] / ne) + proj[2] * (p.el[2] / ne));
+  }
+  dotprod = dotprod > (R)1 ? (R)1 : (dotprod < (R)-1 ? (R)-1 : dotprod);
+  const R phi = acos(dotprod);
+  R nsam[3] = {(R)b.n_sample[0], (R)b.n_sample[1], (R)b.n_sample[2]};
+  const bool up = rdot(ndc, nsam) > (R)0;
+
+  /* distances toward the detector point through the layers */
+  R dist[XMI_MAXL];
+#pragma unroll
+  for (int j = 0; j < XMI_MAXL; j++) dist[j] = (R)0;
+  {
+    double tc[3] = {p.c[0], p.c[1], p.c[2]}, ip[3], dd;
+    bool done = false;
+#pragma unroll
+    for (int k = 0; k < XMI_MAXL; k++) {
+      int j = up ? k : XMI_MAXL - 1 - k;
+      bool active = up ? (j >= layer && j < b.n_layers) : (j <= layer);
+      if (active && !done) {
+        if (!plane_step(tc, ndc, b.n_sample, up ? b.zend[j] : b.zbeg[j], ip, &dd)) { ok = false; return; }
+        if (dd > total_distance) {
+          dist[j] = (R)total_distance;
+          done = true;
+        } else {
+          dist[j] = (R)dd;
+          tc[0] = ip[0]; tc[1] = ip[1]; tc[2] = ip[2];
+          total_distance = total_distance - dd;
+        }
+      }
+    }
+  }
+  R murhod = (R)0;
+#pragma unroll
+  for (int j = 0; j < XMI_MAXL; j++) murhod += p.mus[j] * b.rho[j] * dist[j];
+  const R pesc_rayl = exp(-murhod);
+  const R omega = get_solid_angle(b, p.c, p, t, ok);
+  const R pdir_fluo = omega / (R)4 / (R)kPi;
+
+  int node;
+  R f;
+  locate(b, p.E, node, f);
+  const R mu_here = p.mus[layer];
+  const R q = p.E / (R)12.39852 * sin(theta / (R)2);
+  const R st = sin(theta), cp = cos(phi), ct = cos(theta);
+  const R thomson = (R)1 - st * st * cp * cp;
+  const R k0k = (R)1 + ((R)1 - ct) * p.E / (R)510.998928, kk0 = (R)1 / k0k;
+  const R kn = (R)0.25 * kk0 * kk0 * (kk0 + k0k - (R)2 * st * st * cp * cp);
+  const bool after_fluo = (n > 1 && p.h_type < 0);
+  const int nel = b.nel[layer], off = b.off[layer];
+
+  for (int i = 0; i < nel; i++) {
+    const int e = __ldg(b.layer_el + off + i);
+    const R w = __ldg(b.layer_w + off + i);
+    /* Rayleigh */
+    R pconv = w / mu_here;
+    R pdir = omega * thomson * qtab(b.ff2 + (size_t)e * XMI_NQ, q);
+    double tw = (double)(pconv * pdir * pesc_rayl * p.w);
+    const int rs = b.n_lines + 2 * e;
+    if (use_smem) tally_add(&s_hist[(size_t)(n - 1) * b.n_slots + rs], tw);
+    else tally_add(&t.hist_vr[(size_t)(n - 1) * b.n_slots + rs], tw);
+    tally_channel(b, t, n, p.E, tw);
+    /* Compton */
+    R ec = compton_energy(b, e, p.E, theta, g, true, ok);
+    if (!ok) return;
+    R mus_c[XMI_MAXL];
+    mu_calc(b, ec, mus_c);
+    murhod = (R)0;
+#pragma unroll
+    for (int j = 0; j < XMI_MAXL; j++) murhod += mus_c[j] * b.rho[j] * dist[j];
+    R pesc = exp(-murhod);
+    pdir = omega * kn * qtab(b.sf + (size_t)e * XMI_NQ, q);
+    tw = (double)(pconv * pdir * pesc * p.w);
+    if (use_smem) tally_add(&s_hist[(size_t)(n - 1) * b.n_slots + rs + 1], tw);
+    else tally_add(&t.hist_vr[(size_t)(n - 1) * b.n_slots + rs + 1], tw);
+    tally_channel(b, t, n, ec, tw);
+    /* fluorescence */
+    R P[XMI_NSHELL];
+    if (after_fluo) {
+#pragma unroll
+      for (int s = 0; s < XMI_NSHELL; s++) P[s] = __ldg(b.precalc_xrf + ((size_t)e * XMI_NSHELL + s) * b.n_lines + p.h_slot);
+    } else {
+#pragma unroll
+      for (int s = 0; s < XMI_NSHELL; s++) P[s] = el_val(b, e, XMI_REC_XRF + s, node, f);
+    }
+    if (!b.use_M_lines) {
+#pragma unroll
+      for (int s = 4; s < XMI_NSHELL; s++) P[s] = (R)0;
+    }
+    const int l0 = __ldg(b.line_off + e), l1 = __ldg(b.line_off + e + 1);
+    const R *fy = b.fluor_yield + (size_t)e * XMI_NSHELL;
+    for (int sl = l0; sl < l1; sl++) {
+      const int line = __ldg(b.line_index + sl);
+      if (line > b.line_last) break; /* slots are sorted by line index */
+      const R efl = __ldg(b.line_energy + sl);
+      if (efl < (R)kEnergyThreshold) continue;
+      if (line == 30 || line == 31 || line == 59) continue;
+      const int sh = __ldg(b.line_shell + sl);
+      R ps = (R)0;
+#pragma unroll
+      for (int s = 0; s < XMI_NSHELL; s++)
+        if (s == sh) ps = P[s];
+      if (ps == (R)0) continue;
+      pconv = w * ps * __ldg(fy + sh) * __ldg(b.line_rate + sl) / mu_here;
+      murhod = (R)0;
+#pragma unroll
+      for (int j = 0; j < XMI_MAXL; j++)
+        if (j < b.n_layers) murhod += __ldg(b.precalc_mu + (size_t)j * b.n_lines + sl) * b.rho[j] * dist[j];
+      pesc = exp(-murhod);
+      tw = (double)(pconv * pdir_fluo * pesc * p.w);
+      if (tw == 0.0) continue;
+      if (use_smem) tally_add(&s_hist[(size_t)(n - 1) * b.n_slots + sl], tw);
+      else tally_add(&t.hist_vr[(size_t)(n - 1) * b.n_slots + sl], tw);
+    }
+  }
+}
+
+/* ---------------- interactions ---------------- */
+template <typename R>
+__device__ bool rayleigh(const DevBundle<R> &b, Photon<R> &p, xmi_rng *g) {
+  bool ok = true;
+  const int e = p.elem;
+  const R rinv = (R)(XMI_ICDF_NR - 1), einv = (R)((XMI_ICDF_NE - 1) / (200.0 - 0.1));
+  R r = uni<R>(g);
+  R theta_i = bilinear(b.rayl_icdf + (size_t)e * XMI_ICDF_NE * XMI_ICDF_NR, b.icdf_r, XMI_ICDF_NR, (R)0, rinv,
+                       b.icdf_e, XMI_ICDF_NE, (R)0.1, einv, r, p.E, ok);
+  if (!ok) return false;
+  R tt = sin(theta_i) * sin(theta_i);
+  tt = tt / ((R)4 - (R)2 * tt);
+  r = uni<R>(g);
+  R phi_i = bilinear(b.phi_icdf, b.icdf_r, XMI_ICDF_NR, (R)0, rinv, b.phi_t, XMI_PHI_NT, (R)0,
+                     (R)((XMI_PHI_NT - 1) / 0.5), r, tt, ok);
+  if (!ok) return false;
+  R phi0 = polarisation_phi0(p);
+  update_dirv(p, theta_i, phi0 + phi_i);
+  update_elecv(p);
+  p.h_type = XMI_RAYLEIGH;
+  p.h_elem = e;
+  return true;
+}
+
+template <typename R>
+__device__ bool compton(const DevBundle<R> &b, Photon<R> &p, xmi_rng *g) {
+  bool ok = true;
+  const int e = p.elem;
+  const R rinv = (R)(XMI_ICDF_NR - 1), einv = (R)((XMI_ICDF_NE - 1) / (200.0 - 0.1));
+  const R mec2 = (R)(9.10938188e-31 * 2.99792458e8 * 2.99792458e8 / 1.602176487e-19 / 1000.0);
+  R r = uni<R>(g);
+  R theta_i = bilinear(b.compt_icdf + (size_t)e * XMI_ICDF_NE * XMI_ICDF_NR, b.icdf_r, XMI_ICDF_NR, (R)0, rinv,
+                       b.icdf_e, XMI_ICDF_NE, (R)0.1, einv, r, p.E, ok);
+  if (!ok) return false;
+  R k0k = (R)1 + p.E * ((R)1 - cos(theta_i)) / mec2;
+  R tt = sin(theta_i) * sin(theta_i);
+  tt = tt / (k0k + ((R)1 / k0k) - tt) / (R)2;
+  r = uni<R>(g);
+  R phi_i = bilinear(b.phi_icdf, b.icdf_r, XMI_ICDF_NR, (R)0, rinv, b.phi_t, XMI_PHI_NT, (R)0,
+                     (R)((XMI_PHI_NT - 1) / 0.5), r, tt, ok);
+  if (!ok) return false;
+  R phi0 = polarisation_phi0(p);
+  p.E = compton_energy(b, e, p.E, theta_i, g, false, ok);
+  if (!ok) return false;
+  mu_calc(b, p.E, p.mus);
+  if (p.E == (R)0) return true;
+  update_dirv(p, theta_i, phi_i + phi0);
+  update_elecv(p);
+  R cti = cos(theta_i), cpi = cos(phi_i), spi = sin(phi_i);
+  R pp = (R)2 * ((cti * cpi) * (cti * cpi) + spi * spi);
+  R rat = (R)1 / ((R)1 + ((R)1 - cti) * p.E / (R)(double)510.998910f);
+  R rk = rat - (R)2 + (R)1 / rat;
+  pp = pp / (rk + pp);
+  r = uni<R>(g);
+  R w_h = ((R)1 + pp) / (R)2;
+  if (r > w_h) {
+    R c0 = p.d[1] * p.el[2] - p.d[2] * p.el[1];
+    R c1 = p.d[2] * p.el[0] - p.d[0] * p.el[2];
+    R c2 = p.d[0] * p.el[1] - p.d[1] * p.el[0];
+    p.el[0] = c0; p.el[1] = c1; p.el[2] = c2;
+  }
+  p.h_type = XMI_COMPTON;
+  p.h_elem = e;
+  return true;
+}
+
+/* xmi_coster_kronig_check (src/xmi_main.F90:5184-5323) */
+template <typename R>
+__device__ __forceinline__ int coster_kronig(const R *ck, int shell, xmi_rng *g) {
+  for (int guard = 0; guard < 16; guard++) {
+    R r, s;
+    switch (shell) {
+      case 2:
+        r = uni<R>(g);
+        return r < __ldg(ck + XMI_FL23) ? 3 : 2;
+      case 1:
+        r = uni<R>(g);
+        s = __ldg(ck + XMI_FL12);
+        if (r < s) { shell = 2; continue; }
+        s += __ldg(ck + XMI_FL13);
+        return r < s ? 3 : 1;
+      case 7:
+        r = uni<R>(g);
+        return r < __ldg(ck + XMI_FM45) ? 8 : 7;
+      case 6:
+        r = uni<R>(g);
+        s = __ldg(ck + XMI_FM34);
+        if (r < s) { shell = 7; continue; }
+        s += __ldg(ck + XMI_FM35);
+        return r < s ? 8 : 6;
+      case 5:
+        r = uni<R>(g);
+        s = __ldg(ck + XMI_FM23);
+        if (r < s) { shell = 6; continue; }
+        s += __ldg(ck + XMI_FM24);
+        if (r < s) { shell = 7; continue; }
+        s += __ldg(ck + XMI_FM25);
+        return r < s ? 8 : 5;
+      case 4:
+        r = uni<R>(g);
+        s = __ldg(ck + XMI_FM12);
+        if (r < s) { shell = 5; continue; }
+        s += __ldg(ck + XMI_FM13);
+        if (r < s) { shell = 6; continue; }
+        s += __ldg(ck + XMI_FM14);
+        if (r < s) { shell = 7; continue; }
+        s += __ldg(ck + XMI_FM15);
+        return r < s ? 8 : 4;
+      default:
+        return shell;
+    }
+  }
+  return shell;
+}
+
+template <typename R>
+__device__ bool fluorescence(const DevBundle<R> &b, Photon<R> &p, xmi_rng *g) {
+  const int e = p.elem;
+  int node;
+  R f;
+  locate(b, p.E, node, f);
+  R photo_total = el_val(b, e, XMI_REC_PHOTO, node, f);
+  R sumz = (R)0, r = uni<R>(g);
+  int shell = -1;
+  for (int s = 0; s <= b.max_shell; s++) {
+    sumz = sumz + el_val(b, e, XMI_REC_PART + s, node, f) / photo_total;
+    if (r < sumz) { shell = s; break; }
+  }
+  if (shell < 0) {
+    p.E = (R)0;
+    return true;
+  }
+  const R yc = __ldg(b.yield_corr + (size_t)e * XMI_NSHELL + shell);
+  if (b.use_vr == 0 && b.escape_mode == 0) {
+    r = uni<R>(g);
+    if (r > yc) {
+      p.E = (R)0;
+      return true;
+    }
+  } else {
+    (void)uni<R>(g);
+    if (b.escape_mode) p.we = p.we * yc;
+    else p.w = p.w * yc;
+  }
+  shell = coster_kronig(b.ck + (size_t)e * XMI_NCK, shell, g);
+  r = uni<R>(g);
+  sumz = (R)0;
+  int slot = -1;
+  const int s0 = __ldg(b.shell_off + 10 * e + shell), s1 = __ldg(b.shell_off + 10 * e + shell + 1);
+  for (int sl = s0; sl < s1; sl++) {
+    sumz = sumz + __ldg(b.line_rate + sl);
+    if (r < sumz) { slot = sl; break; }
+  }
+  if (slot < 0) {
+    p.E = (R)0;
+    return true;
+  }
+  p.E = __ldg(b.line_energy + slot);
+#pragma unroll
+  for (int j = 0; j < XMI_MAXL; j++)
+    p.mus[j] = j < b.n_layers ? __ldg(b.precalc_mu + (size_t)j * b.n_lines + slot) : (R)0;
+  R theta_i = acos((R)-2 * uni<R>(g) + (R)1);
+  R phi_i = (R)(2.0 * kPi) * uni<R>(g);
+  update_dirv(p, theta_i, phi_i);
+  update_elecv(p);
+  p.h_type = -__ldg(b.line_index + slot);
+  p.h_elem = e;
+  p.h_slot = slot;
+  return true;
+}
+
+/* ---------------- analog detector checks ---------------- */
+/* xmi_check_detector_intersection (src/xmi_aux_f.F90:1622-1834), including
+ * the reference's use of the scalar segment length as the direction of the
+ * collimator-free branch; evaluated in FP64 */
+__device__ inline int check_detector_intersection(const double *p_det, const double *det_inv, int coll_present,
+                                           double det_radius, double coll_height, double half_apex,
+                                           double vx, const double *bc, const double *ec) {
+  double t0[3] = {bc[0] - p_det[0], bc[1] - p_det[1], bc[2] - p_det[2]};
+  double t1[3] = {ec[0] - p_det[0], ec[1] - p_det[1], ec[2] - p_det[2]};
+  double bd[3], ed[3];
+  matvec_d(det_inv, t0, bd);
+  matvec_d(det_inv, t1, ed);
+  if (!coll_present) {
+    if (bd[0] * ed[0] > 0) return 0;
+    double s = sqrt((ed[0] - bd[0]) * (ed[0] - bd[0]) + (ed[1] - bd[1]) * (ed[1] - bd[1]) + (ed[2] - bd[2]) * (ed[2] - bd[2]));
+    if (s == 0.0) return 3;
+    double d = (0.0 - ed[0]) / s;
+    double iy = d * s + ed[1], iz = d * s + ed[2];
+    if (sqrt(iy * iy + iz * iz) <= det_radius) return 3; /* direction component along x is s >= 0 */
+    return 0;
+  }
+  double dv[3] = {ed[0] - bd[0], ed[1] - bd[1], ed[2] - bd[2]};
+  double tb = (bd[0] - ed[0]) / dv[0], te = (ed[0] - ed[0]) / dv[0];
+  double delta[3] = {ed[0] - vx, ed[1], ed[2]};
+  double cos2t = cos(half_apex) * cos(half_apex);
+  double c2 = dv[0] * (1.0 - cos2t) * dv[0] - dv[1] * cos2t * dv[1] - dv[2] * cos2t * dv[2];
+  double c1 = dv[0] * (1.0 - cos2t) * delta[0] - dv[1] * cos2t * delta[1] - dv[2] * cos2t * delta[2];
+  double c0 = delta[0] * (1.0 - cos2t) * delta[0] - delta[1] * cos2t * delta[1] - delta[2] * cos2t * delta[2];
+  double disc = c1 * c1 - c0 * c2;
+  if (disc < 0.0) return 0;
+  double tt1 = (-c1 + sqrt(disc)) / c2, tt2 = (-c1 - sqrt(disc)) / c2;
+  double X1x = ed[0] + tt1 * dv[0], X2x = ed[0] + tt2 * dv[0];
+  int nvalid = 0;
+  if (-(X1x - vx) >= 0.0) nvalid = 1;
+  if (-(X2x - vx) >= 0.0) nvalid = (nvalid == 1) ? 3 : 2;
+  double tmax = tb > te ? tb : te, tmin = tb < te ? tb : te;
+  if (nvalid == 0) return 0;
+  if (nvalid == 3) {
+    if (tt1 <= tmax && tt1 >= tmin && X1x <= coll_height) return 1;
+    if (tt2 <= tmax && tt2 >= tmin && X2x <= coll_height) return 1;
+    return 0;
+  }
+  double tsel = nvalid == 1 ? tt1 : tt2, Xsx = nvalid == 1 ? X1x : X2x;
+  if (tsel <= tmax && tsel >= tmin && Xsx <= coll_height) return 1;
+  if (dv[0] == 0.0) return 3;
+  double d = (0.0 - ed[0]) / dv[0];
+  double iy = d * dv[1] + ed[1], iz = d * dv[2] + ed[2];
+  double db = sqrt(bd[0] * bd[0] + (bd[1] - iy) * (bd[1] - iy) + (bd[2] - iz) * (bd[2] - iz));
+  double de = sqrt((bd[0] - ed[0]) * (bd[0] - ed[0]) + (bd[1] - ed[1]) * (bd[1] - ed[1]) + (bd[2] - ed[2]) * (bd[2] - ed[2]));
+  if (sqrt(iy * iy + iz * iz) <= det_radius && db <= de) {
+    if (dv[0] >= 0.0) return 3;
+    return 2;
+  }
+  return 0;
+}
+
+/* xmi_check_photon_detector_hit (src/xmi_main.F90:1920-1984) */
+template <typename R>
+__device__ bool check_photon_detector_hit(const DevBundle<R> &b, const Photon<R> &p) {
+  double dvd[3] = {(double)p.d[0], (double)p.d[1], (double)p.d[2]};
+  if (dot3(dvd, b.n_det) >= 0.0) return false;
+  double dd[3], cd[3], t[3] = {p.c[0] - b.p_det[0], p.c[1] - b.p_det[1], p.c[2] - b.p_det[2]};
+  matvec_d(b.det_inv, dvd, dd);
+  matvec_d(b.det_inv, t, cd);
+  if (dd[0] == 0.0) return false;
+  double s = (0.0 - cd[0]) / dd[0];
+  double iy = s * dd[1] + cd[1], iz = s * dd[2] + cd[2];
+  if (sqrt(iy * iy + iz * iz) > b.det_radius) return false;
+  if (!b.coll_present) return true;
+  s = (b.coll_height - cd[0]) / dd[0];
+  iy = s * dd[1] + cd[1];
+  iz = s * dd[2] + cd[2];
+  return sqrt(iy * iy + iz * iz) <= b.coll_radius;
+}
+
+/* ---------------- one history ---------------- */
+template <typename R>
+__device__ bool simulate_photon(const DevBundle<R> &b, Photon<R> &p, const DevTally &t, double *s_hist,
+                                bool use_smem) {
+  for (int guard = 0; guard < 4 * XMI_MAXN + 8; guard++) {
+    if (p.E < (R)kEnergyThreshold) break;
+    p.inside = 0;
+    xmi_rng g;
+    xmi_rng_init(&g, b.seed, (uint64_t)p.id, (uint32_t)(p.n_int + 1));
+    R dn[3] = {(R)b.n_sample[0], (R)b.n_sample[1], (R)b.n_sample[2]};
+    const bool up = rdot(p.d, dn) > (R)0;
+    const R R0 = uni<R>(&g);
+    if ((b.escape_mode == 1 && p.n_int == 1) || (b.use_vr == 0 && b.escape_mode == 0)) {
+      R minr = (R)0, maxr = (R)0, blbs = (R)1;
+      bool stop = false;
+#pragma unroll
+      for (int k = 0; k < XMI_MAXL; k++) {
+        int j = up ? k : XMI_MAXL - 1 - k;
+        bool active = up ? (j >= p.layer && j < b.n_layers) : (j <= p.layer);
+        if (active && !stop) {
+          double ip[3], dd;
+          if (!plane_step(p.c, p.d, b.n_sample, up ? b.zend[j] : b.zbeg[j], ip, &dd)) return false;
+          R tp = (R)-1 * (R)dd * b.rho[j] * p.mus[j];
+          R tempexp = exp(tp);
+          minr = maxr;
+          maxr = maxr - blbs * expm1(tp);
+          if (R0 <= maxr) {
+            R dist = (R)-1 * log1p((R)-1 * (R0 - minr) / blbs) / p.mus[j] / b.rho[j];
+            double tc[3] = {p.c[0], p.c[1], p.c[2]};
+#pragma unroll
+            for (int q = 0; q < 3; q++) p.c[q] = p.c[q] + (double)dist * (double)p.d[q];
+            if (b.escape_mode != 1) {
+              int rc = check_detector_intersection(b.p_det, b.det_inv, b.coll_present, b.det_radius, b.coll_height,
+                                                   b.coll_half_apex, b.coll_vertex_x, tc, p.c);
+              if (rc == 1 || rc == 3) return true;
+              if (rc == 2) { p.hit = 1; return true; }
+            }
+            p.layer = j;
+            p.inside = 1;
+            stop = true;
+          } else {
+            if (b.escape_mode != 1) {
+              int rc = check_detector_intersection(b.p_det, b.det_inv, b.coll_present, b.det_radius, b.coll_height,
+                                                   b.coll_half_apex, b.coll_vertex_x, p.c, ip);
+              if (rc == 1 || rc == 3) return true;
+              if (rc == 2) { p.hit = 1; return true; }
+            }
+            p.c[0] = ip[0]; p.c[1] = ip[1]; p.c[2] = ip[2];
+            blbs = blbs * tempexp;
+          }
+        }
+      }
+    } else {
+      if (p.n_int == b.N) break;
+      R dist[XMI_MAXL];
+      double lp[3] = {p.c[0], p.c[1], p.c[2]};
+      R pabs = (R)0;
+#pragma unroll
+      for (int k = 0; k < XMI_MAXL; k++) {
+        int j = up ? k : XMI_MAXL - 1 - k;
+        bool active = up ? (j >= p.layer && j < b.n_layers) : (j <= p.layer);
+        dist[j] = (R)0;
+        if (active) {
+          double ip[3], dd;
+          if (!plane_step(lp, p.d, b.n_sample, up ? b.zend[j] : b.zbeg[j], ip, &dd)) return false;
+          dist[j] = (R)dd;
+          lp[0] = ip[0]; lp[1] = ip[1]; lp[2] = ip[2];
+          pabs = pabs + p.mus[j] * b.rho[j] * dist[j];
+        }
+      }
+      R pabs2 = (R)-1 * expm1((R)-1 * pabs);
+      p.w = p.w * pabs2;
+      if (b.escape_mode == 1) p.we = p.w;
+      R negln = (R)-1 * log1p((R)-1 * R0 * pabs2);
+      int my_index = p.layer;
+      R my_sum = (R)0, mr_sel = (R)0;
+      bool found = false;
+#pragma unroll
+      for (int k = 0; k < XMI_MAXL; k++) {
+        int j = up ? k : XMI_MAXL - 1 - k;
+        bool active = up ? (j >= p.layer && j < b.n_layers) : (j <= p.layer);
+        if (active && !found) {
+          my_sum = my_sum + p.mus[j] * b.rho[j] * dist[j];
+          if (my_sum > negln) { my_index = j; found = true; }
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < XMI_MAXL; j++)
+        if (j == my_index) mr_sel = p.mus[j] * b.rho[j];
+      R temp_sum = (R)0;
+#pragma unroll
+      for (int k = 0; k < XMI_MAXL; k++) {
+        int j = up ? k : XMI_MAXL - 1 - k;
+        bool active = up ? (j >= p.layer && j <= my_index) : (j <= p.layer && j >= my_index);
+        if (active) temp_sum = temp_sum + ((R)1 - (p.mus[j] * b.rho[j] / mr_sel)) * dist[j];
+      }
+      temp_sum = temp_sum - (R)1 * log1p((R)-1 * R0 * pabs2) / mr_sel;
+#pragma unroll
+      for (int q = 0; q < 3; q++) p.c[q] = p.c[q] + (double)temp_sum * (double)p.d[q];
+      p.inside = 1;
+      p.layer = my_index;
+    }
+    if (!p.inside) {
+      if (b.escape_mode != 1) p.hit = check_photon_detector_hit(b, p) ? 1 : 0;
+      break;
+    }
+    if (p.n_int == b.N) break;
+    p.n_int = p.n_int + 1;
+    if (b.use_vr == 1) {
+      bool ok = true;
+      variance_reduction(b, p, &g, t, s_hist, use_smem, ok);
+      if (!ok) { set_error(t, kErrTable); return false; }
+    }
+    /* atom selection and interaction type, src/xmi_main.F90:1556-1652 */
+    int node;
+    R f;
+    locate(b, p.E, node, f);
+    R r = uni<R>(&g);
+    const int L = p.layer, nel = b.nel[L], off = b.off[L];
+    R mu_l = (R)0;
+#pragma unroll
+    for (int j = 0; j < XMI_MAXL; j++)
+      if (j == L) mu_l = p.mus[j];
+    R thr = (R)0;
+    int sel = nel - 1;
+    for (int i = 0; i < nel; i++) {
+      thr = thr + __ldg(b.layer_w + off + i) * el_val(b, __ldg(b.layer_el + off + i), XMI_REC_TOT, node, f) / mu_l;
+      if (r < thr) { sel = i; break; }
+    }
+    p.elem = __ldg(b.layer_el + off + sel);
+    r = uni<R>(&g);
+    R pr = el_val(b, p.elem, XMI_REC_PR, node, f);
+    R prc = el_val(b, p.elem, XMI_REC_PRC, node, f);
+    bool ok;
+    if (r < pr) {
+      p.last = XMI_RAYLEIGH;
+      ok = rayleigh(b, p, &g);
+    } else if (r < prc) {
+      p.last = XMI_COMPTON;
+      ok = compton(b, p, &g);
+    } else {
+      p.last = XMI_PHOTOELECTRIC;
+      ok = fluorescence(b, p, &g);
+    }
+    if (!ok) { set_error(t, kErrTable); return false; }
+  }
+  return true;
+}
+
+/* ---------------- source sampling (src/xmi_main.F90:319-858) ---------------- */
+template <typename R>
+__device__ __forceinline__ R ran_gauss(xmi_rng *g, R sigma) {
+  double u1 = xmi_rng_uniform(g), u2 = xmi_rng_uniform(g);
+  if (u1 <= 0.0) u1 = 1.0 / 9007199254740992.0;
+  return (R)(sigma * sqrt(-2.0 * log(u1)) * cos(2.0 * kPi * u2));
+}
+
+template <typename R>
+__device__ bool start_photon(const DevBundle<R> &b, const xmi_source_item &it, long long j, Photon<R> &p,
+                             bool &skip) {
+  xmi_rng g;
+  xmi_rng_init(&g, b.seed, (uint64_t)p.id, 0u);
+  skip = false;
+  double hvr = 0.0;
+  if (it.kind == 0) {
+    /* xmi_ran_trap + xmi_poly_solve_quadratic */
+    double m = it.trap[1], denom = it.trap[0], x1 = it.trap[2], x2 = it.trap[3], y1 = it.trap[4];
+    double a = m / 2.0, bq = y1 - x1 * m, c = -x1 * y1 + m * x1 * x1 / 2.0 - denom * xmi_rng_uniform(&g);
+    double E;
+    if (a == 0.0) {
+      if (bq == 0.0) return false;
+      E = -1.0 * c / bq;
+      if (!(x1 <= E && E <= x2)) return false;
+    } else {
+      double delta = bq * bq - 4.0 * a * c;
+      if (delta < 0.0) return false;
+      double sd = sqrt(delta), t1 = (-bq + sd) / 2.0 / a, t2 = (-bq - sd) / 2.0 / a;
+      double r1 = t1 < t2 ? t1 : t2, r2 = t1 > t2 ? t1 : t2;
+      if (x1 <= r1 && r1 <= x2) E = r1;
+      else if (x1 <= r2 && r2 <= x2) E = r2;
+      else return false;
+    }
+    p.E = (R)E;
+    hvr = (it.h0 + ((it.h1 - it.h0) * (E - it.e0) / (it.e1 - it.e0))) /
+          (it.i0 + ((it.i1 - it.i0) * (E - it.e0) / (it.e1 - it.e0)));
+    int node;
+    R f;
+    locate(b, p.E, node, f);
+    R ex0 = __ldg(b.exc_tab + node), ex1 = __ldg(b.exc_tab + node + 1);
+    R exc_corr = exp((R)-1 * (ex0 + f * (ex1 - ex0)));
+    mu_calc(b, p.E, p.mus);
+    p.w = (R)it.weight * exc_corr;
+  } else {
+    if (it.dist_type == 1) {
+      p.E = ran_gauss<R>(&g, (R)it.scale) + (R)it.e0;
+      if (p.E <= (R)kEnergyThreshold || p.E > (R)kEnergyMax) { skip = true; return true; }
+    } else if (it.dist_type == 2) {
+      double u;
+      do { u = xmi_rng_uniform(&g); } while (u == 0.5);
+      p.E = (R)(it.scale * tan(kPi * u) + it.e0);
+      if (p.E <= (R)kEnergyThreshold || p.E > (R)kEnergyMax) { skip = true; return true; }
+    } else {
+      p.E = (R)it.e0;
+    }
+    mu_calc(b, p.E, p.mus);
+    p.w = (R)it.weight;
+  }
+  /* xmi_coords_dir */
+  double x1, y1;
+  if (fabs(it.sigma_x * it.sigma_y) < (double)1.0e-20f) {
+    double x1m = atan(b.slit_x / b.d_source_slit / 2.0), y1m = atan(b.slit_y / b.d_source_slit / 2.0);
+    double u = xmi_rng_uniform(&g);
+    x1 = x1m * (-1.0 * (1.0 - u) + 1.0 * u);
+    u = xmi_rng_uniform(&g);
+    y1 = y1m * (-1.0 * (1.0 - u) + 1.0 * u);
+    p.c[0] = p.c[1] = p.c[2] = 0.0;
+  } else {
+    x1 = ran_gauss<double>(&g, it.sigma_xp);
+    y1 = ran_gauss<double>(&g, it.sigma_yp);
+    p.c[0] = ran_gauss<double>(&g, it.sigma_x) - b.d_source_slit * sin(x1);
+    p.c[1] = ran_gauss<double>(&g, it.sigma_y) - b.d_source_slit * sin(y1);
+    p.c[2] = 0.0;
+  }
+  {
+    double dx = tan(x1), dy = tan(y1), dz = 1.0, nn = sqrt(dx * dx + dy * dy + dz * dz);
+    p.d[0] = (R)(dx / nn); p.d[1] = (R)(dy / nn); p.d[2] = (R)(dz / nn);
+  }
+  p.theta = acos(p.d[2]);
+  p.phi = atan2(p.d[1], p.d[0]);
+  bool horizontal;
+  if (it.kind == 0) horizontal = xmi_rng_uniform(&g) <= hvr;
+  else horizontal = (double)(it.local0 + j + 1) <= it.hor_ver_ratio;
+  if (horizontal) { p.el[0] = (R)0; p.el[1] = (R)1; p.el[2] = (R)0; }
+  else { p.el[0] = (R)1; p.el[1] = (R)0; p.el[2] = (R)0; }
+  p.we = p.w;
+  R cosalfa = rdot(p.el, p.d);
+  if (fabs(cosalfa) > (R)1) return false;
+  R c_alfa = acos(cosalfa);
+  R c_ae = (R)1.0 / sin(c_alfa), c_be = -c_ae * cosalfa;
+#pragma unroll
+  for (int k = 0; k < 3; k++) p.el[k] = c_ae * p.el[k] + c_be * p.d[k];
+  /* xmi_photon_shift_first_layer */
+  p.layer = -1;
+  if (p.c[2] >= b.zbeg[0]) {
+    for (int i = 0; i < b.n_layers; i++)
+      if (p.c[2] < b.zend[i]) { p.layer = i; break; }
+    if (p.layer < 0) return false;
+  } else {
+    double ip[3], dd;
+    if (!plane_step(p.c, p.d, b.n_sample, b.zbeg[0], ip, &dd)) return false;
+    p.c[0] = ip[0]; p.c[1] = ip[1]; p.c[2] = ip[2];
+    p.layer = 0;
+  }
+  return true;
+}
+
+template <typename R>
+__global__ void __launch_bounds__(256) transport_kernel(DevBundle<R> b, DevTally t, long long w0, long long w1,
+                                                        int use_smem) {
+  extern __shared__ double s_hist[];
+  const int nh = b.N * b.n_slots;
+  if (use_smem) {
+    for (int i = threadIdx.x; i < nh; i += blockDim.x) s_hist[i] = 0.0;
+    __syncthreads();
+  }
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long w = w0 + (long long)blockIdx.x * blockDim.x + threadIdx.x; w < w1; w += stride) {
+    /* work index -> (item, index within item) */
+    int lo = 0, hi = b.n_items - 1;
+    while (lo < hi) {
+      int mid = (lo + hi + 1) >> 1;
+      if (w >= __ldg(b.item_first + mid)) lo = mid; else hi = mid - 1;
+    }
+    const xmi_source_item &it = b.items[lo];
+    const long long j = w - __ldg(b.item_first + lo);
+    Photon<R> p;
+    p.id = it.first + j;
+    p.n_int = 0;
+    p.last = XMI_NO_INTERACTION;
+    p.hit = 0;
+    p.h_type = XMI_NO_INTERACTION;
+    p.h_elem = 0;
+    p.h_slot = 0;
+    p.elem = 0;
+    bool skip;
+    if (!start_photon(b, it, j, p, skip)) { set_error(t, kErrSource); continue; }
+    if (skip) continue;
+    if (!simulate_photon(b, p, t, s_hist, use_smem != 0)) continue;
+    if (p.hit) {
+      if (b.use_vr == 0) tally_channel(b, t, p.n_int, p.E, (double)p.w);
+      if (p.n_int > 0) {
+        int slot = -1;
+        if (p.h_type < 0) slot = p.h_slot;
+        else if (p.h_type == XMI_RAYLEIGH) slot = b.n_lines + 2 * p.h_elem;
+        else if (p.h_type == XMI_COMPTON) slot = b.n_lines + 2 * p.h_elem + 1;
+        if (slot >= 0) atomicAdd(&t.hist_brute[(size_t)(p.n_int - 1) * b.n_slots + slot], (double)p.w);
+      }
+    }
+  }
+  if (use_smem) {
+    __syncthreads();
+    for (int i = threadIdx.x; i < nh; i += blockDim.x)
+      if (s_hist[i] != 0.0) atomicAdd(&t.hist_vr[i], s_hist[i]);
+  }
+}
+
+}  // namespace xmi
+#endif
