@@ -114,6 +114,12 @@ const void *xmi_gpu_bundle(xmi_hdf5FPtr hdf5FPtr);
 int xmi_gpu_prepare_run(xmi_inputFPtr inputFPtr, xmi_hdf5FPtr hdf5FPtr,
                         xmi_main_options *options, int n_mpi_hosts,
                         xmi_solid_angle *solid_angles);
+/* Replicas: this process simulates photons [r*n/R, (r+1)*n/R) of every source
+ * item (r = replica, R = n_replicas), with the weights of the full budget, so
+ * the element-wise sum of the outputs of all R replicas is the single-process
+ * result.  Replaces the reference's MPI photon split (src/xmi_main.F90:314,574;
+ * bin/xmimsim.c:396-413). */
+int xmi_gpu_set_replica(xmi_hdf5FPtr hdf5FPtr, int replica, int n_replicas);
 /* device time (ms, CUDA events) and kernel launches of the last call */
 int xmi_gpu_last_timing(double *transport_ms, double *total_ms, int *launches);
 

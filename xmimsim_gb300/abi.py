@@ -150,6 +150,7 @@ PROTOTYPES = {
     "xmi_gpu_prepare_run": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(XmiMainOptions), C.c_int,
                                       C.POINTER(XmiSolidAngle)]),
     "xmi_gpu_last_timing": (C.c_int, [c_double_p, c_double_p, c_int_p]),
+    "xmi_gpu_set_replica": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
 }
 
 _lib = None
@@ -160,7 +161,7 @@ def load(path: str | os.PathLike | None = None) -> C.CDLL:
     global _lib
     if _lib is not None and path is None:
         return _lib
-    p = Path(path) if path else LIB_PATH
+    p = Path(path) if path else Path(os.environ.get("XMIMSIM_GB300_LIB", LIB_PATH))
     if not p.exists():
         raise RuntimeError(f"{p} is missing: build the CUDA engine first (python -c 'import __graft_entry__ as g; "
                            "g.build()'); there is no CPU fallback")

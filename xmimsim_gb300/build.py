@@ -56,27 +56,33 @@ def _deps() -> list[Path]:
         sorted((ROOT / "include").glob("*.h"))
 
 
-def build_engine(verbose: bool = False) -> Path:
-    """Compiles the engine and returns the path of the shared library."""
+def build_engine(verbose: bool = False, checked: bool = False) -> Path:
+    """Compiles the engine and returns the path of the shared library.
+
+    checked=True builds the diagnostic variant libxmimsim_gb300_checked.so in
+    which every table load and tally store of the transport kernel is
+    bounds-checked (violations are recorded, not executed)."""
     nvcc = _nvcc()
-    OBJDIR.mkdir(parents=True, exist_ok=True)
+    objdir = OBJDIR / "checked" if checked else OBJDIR
+    objdir.mkdir(parents=True, exist_ok=True)
     LIBDIR.mkdir(parents=True, exist_ok=True)
+    nvflags = NVFLAGS + (["-DXMI_CHECKED"] if checked else [])
     deps = _deps()
     jobs = []
     objs = []
     for src in HOST_SOURCES:
-        obj = OBJDIR / (src + ".o")
+        obj = objdir / (src + ".o")
         objs.append(obj)
         if _stale(obj, deps + [CSRC / src]):
             jobs.append(["gcc", *CFLAGS, "-c", str(CSRC / src), "-o", str(obj)])
     for src in CUDA_SOURCES:
-        obj = OBJDIR / (src + ".o")
+        obj = objdir / (src + ".o")
         objs.append(obj)
         if _stale(obj, deps + [CSRC / src]):
-            jobs.append([nvcc, *NVFLAGS, "-c", str(CSRC / src), "-o", str(obj)])
+            jobs.append([nvcc, *nvflags, "-c", str(CSRC / src), "-o", str(obj)])
     with cf.ThreadPoolExecutor(max_workers=max(1, len(jobs))) as ex:
         list(ex.map(_run, jobs))
-    lib = LIBDIR / "libxmimsim_gb300.so"
+    lib = LIBDIR / ("libxmimsim_gb300_checked.so" if checked else "libxmimsim_gb300.so")
     if _stale(lib, objs):
         _run([nvcc, *ARCH, "-shared", "-Xcompiler", "-fopenmp", "-o", str(lib), *map(str, objs),
               "-lgomp", "-lm"])

@@ -19,7 +19,7 @@ constexpr double kPi = 3.14159265358979323846;
 template <typename R>
 struct DevBundle {
   int N, nch, use_vr, use_M_lines, line_last, max_shell, escape_mode;
-  int n_layers, n_elem, n_lines, n_slots, n_nodes, n_seg, n_items;
+  int n_layers, n_elem, n_lines, n_slots, n_nodes, n_seg, n_items, n_layer_el;
   int coll_present, sa_nr, sa_nt, sa_hits;
   unsigned long long seed;
   long long n_photons_total;

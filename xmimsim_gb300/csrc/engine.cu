@@ -112,6 +112,7 @@ void fill_scalars(const xmi_bundle &h, xmi::DevBundle<R> &d) {
   d.n_nodes = h.n_nodes;
   d.n_seg = h.n_seg;
   d.n_items = h.n_items;
+  d.n_layer_el = h.n_layer_el;
   d.coll_present = h.coll_present;
   d.seed = h.seed;
   d.n_photons_total = h.n_photons_total;
@@ -269,6 +270,14 @@ void xmi_free_hdf5_F(xmi_hdf5FPtr *p) {
   *p = nullptr;
 }
 
+#ifdef XMI_CHECKED
+/* first bounds violation recorded by the diagnostic build: tag, index, limit, count */
+int xmi_gpu_check_record(unsigned long long *out) {
+  if (cudaMemcpyFromSymbol(out, xmi::xmi_check_record, sizeof(unsigned long long) * 4) != cudaSuccess) return 0;
+  return 1;
+}
+#endif
+
 int xmi_gpu_last_timing(double *transport_ms, double *total_ms, int *launches) {
   if (transport_ms) *transport_ms = g_timing.transport_ms;
   if (total_ms) *total_ms = g_timing.total_ms;
@@ -404,7 +413,13 @@ int xmi_gpu_prepare_run(xmi_inputFPtr in, xmi_hdf5FPtr t, xmi_main_options *opti
     xmi_bundle_free(&t->b);
     if (!xmi_bundle_build(in, t, options)) return 0;
   }
-  xmi_bundle_set_run(in, t, options, n_mpi_hosts, 0, 1);
+  {
+    /* n_mpi_hosts > 1 keeps the reference's per-host share n/n_mpi_hosts */
+    int R = t->n_replicas > 0 ? t->n_replicas : 1, r = t->replica;
+    if (n_mpi_hosts > R) R = n_mpi_hosts;
+    if (r >= R) r = R - 1;
+    xmi_bundle_set_run(in, t, options, n_mpi_hosts, r, R);
+  }
   attach_solid_angles(t, sa);
   if (options->use_variance_reduction && (!sa || !sa->solid_angles)) {
     xmi_set_error("variance reduction requires a solid angle grid");

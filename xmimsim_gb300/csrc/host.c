@@ -1091,6 +1091,16 @@ int xmi_init_from_hdf5(char *hdf5_file, xmi_inputFPtr inputFPtr, xmi_hdf5FPtr *h
 
 const void *xmi_gpu_bundle(xmi_hdf5FPtr t) { return t ? (const void *)&t->b : NULL; }
 
+int xmi_gpu_set_replica(xmi_hdf5FPtr t, int replica, int n_replicas) {
+  if (!t || n_replicas < 1 || replica < 0 || replica >= n_replicas) {
+    xmi_set_error("xmi_gpu_set_replica: invalid replica %d of %d", replica, n_replicas);
+    return 0;
+  }
+  t->replica = replica;
+  t->n_replicas = n_replicas;
+  return 1;
+}
+
 /* grid axes of the solid-angle table, xmi_solid_angle_inputs_f
  * (src/xmi_solid_angle_f.F90:62-301): r from the detector distance of the
  * depths S1/S2 at which R1=1e-5 / R2=0.99999 of the beam is absorbed at the

@@ -44,6 +44,31 @@ __device__ __forceinline__ void set_error(const DevTally &t, unsigned long long 
   atomicCAS(&t.counters[1], 0ull, code);
 }
 
+/* Diagnostic build (-DXMI_CHECKED): every table load and tally store is
+ * bounds-checked; the first violation is recorded in xmi_check_record
+ * (tag, index, limit, count) and the access is skipped instead of faulting. */
+#ifdef XMI_CHECKED
+static __device__ unsigned long long xmi_check_record[4];
+static __device__ __noinline__ bool xmi_check(long long idx, long long lim, int tag) {
+  if (idx >= 0 && idx < lim) return true;
+  if (atomicCAS(&xmi_check_record[0], 0ull, (unsigned long long)tag) == 0ull) {
+    xmi_check_record[1] = (unsigned long long)idx;
+    xmi_check_record[2] = (unsigned long long)lim;
+  }
+  atomicAdd(&xmi_check_record[3], 1ull);
+  return false;
+}
+template <typename T>
+__device__ __forceinline__ T xmi_ldg_checked(const T *p, long long idx, long long lim, int tag) {
+  return xmi_check(idx, lim, tag) ? __ldg(p + idx) : (T)0;
+}
+#define XMI_LDG(p, idx, lim, tag) xmi::xmi_ldg_checked((p), (long long)(idx), (long long)(lim), (tag))
+#define XMI_CHK(idx, lim, tag) xmi::xmi_check((long long)(idx), (long long)(lim), (tag))
+#else
+#define XMI_LDG(p, idx, lim, tag) __ldg((p) + (idx))
+#define XMI_CHK(idx, lim, tag) true
+#endif
+
 /* ---------------- math helpers ---------------- */
 template <typename R> __device__ __forceinline__ R rdot(const R *a, const R *b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
 template <typename R> __device__ __forceinline__ void rnorm(R *a) {
@@ -110,8 +135,9 @@ __device__ __forceinline__ void locate(const DevBundle<R> &b, R E, int &node, R 
 
 template <typename R>
 __device__ __forceinline__ R el_val(const DevBundle<R> &b, int e, int col, int node, R f) {
-  const R *t = b.el_tab + ((size_t)e * b.n_nodes + node) * XMI_EL_REC + col;
-  R v0 = __ldg(t), v1 = __ldg(t + XMI_EL_REC);
+  const long long base = ((long long)e * b.n_nodes + node) * XMI_EL_REC + col;
+  const long long lim = (long long)b.n_elem * b.n_nodes * XMI_EL_REC;
+  R v0 = XMI_LDG(b.el_tab, base, lim, 1), v1 = XMI_LDG(b.el_tab, base + XMI_EL_REC, lim, 1);
   return v0 + f * (v1 - v0);
 }
 
@@ -120,10 +146,10 @@ __device__ __forceinline__ void mu_calc(const DevBundle<R> &b, R E, R *mus) {
   int node;
   R f;
   locate(b, E, node, f);
-  const R *t = b.mu_tab + (size_t)node * XMI_MAXL;
+  const long long base = (long long)node * XMI_MAXL, lim = (long long)b.n_nodes * XMI_MAXL;
 #pragma unroll
   for (int j = 0; j < XMI_MAXL; j++) {
-    R v0 = __ldg(t + j), v1 = __ldg(t + XMI_MAXL + j);
+    R v0 = XMI_LDG(b.mu_tab, base + j, lim, 2), v1 = XMI_LDG(b.mu_tab, base + XMI_MAXL + j, lim, 2);
     mus[j] = v0 + f * (v1 - v0);
   }
 }
@@ -132,11 +158,15 @@ __device__ __forceinline__ void mu_calc(const DevBundle<R> &b, R E, R *mus) {
  * linear scan, found from an arithmetic guess and a +-1 correction */
 template <typename R>
 __device__ __forceinline__ int findpos_u(const R *a, int n, R x, R a0, R inv_dx) {
-  if (fabs(x - __ldg(a)) < (R)1e-10) return 0;
+  /* NaN never compares <= an axis value: not found (the linear scan's answer).
+   * The guess is clamped in floating point before the integer conversion,
+   * since an FP64 NaN converts to INT_MIN. */
+  if (!(x == x)) return -1;
+  if (fabs(x - XMI_LDG(a, 0, n, 3)) < (R)1e-10) return 0;
   R gr = ceil((x - a0) * inv_dx);
-  int i = gr < (R)1 ? 1 : (gr > (R)(n - 1) ? n - 1 : (int)gr);
-  while (i > 1 && x <= __ldg(a + i - 1)) i--;
-  while (i < n && x > __ldg(a + i)) i++;
+  int i = !(gr >= (R)1) ? 1 : (!(gr <= (R)(n - 1)) ? n - 1 : (int)gr);
+  while (i > 1 && x <= XMI_LDG(a, i - 1, n, 3)) i--;
+  while (i < n && x > XMI_LDG(a, i, n, 3)) i++;
   return i >= n ? -1 : i - 1;
 }
 
@@ -146,14 +176,16 @@ __device__ __forceinline__ R bilinear(const R *a2, const R *a, int n1, R a0, R a
                                       R binv, R x1, R x2, bool &ok) {
   int p1 = findpos_u(a, n1, x1, a0, ainv), p2 = findpos_u(bb, n2, x2, b0, binv);
   if (p1 < 0 || p2 < 0) { ok = false; return (R)0; }
-  R a_0 = __ldg(a + p1), a_1 = __ldg(a + p1 + 1), b_0 = __ldg(bb + p2), b_1 = __ldg(bb + p2 + 1);
+  R a_0 = XMI_LDG(a, p1, n1, 4), a_1 = XMI_LDG(a, p1 + 1, n1, 4), b_0 = XMI_LDG(bb, p2, n2, 4),
+    b_1 = XMI_LDG(bb, p2 + 1, n2, 4);
   R denom = (a_1 - a_0) * (b_1 - b_0);
   R c1 = (a_1 - x1) * (b_1 - x2) / denom;
   R c2 = (x1 - a_0) * (b_1 - x2) / denom;
   R c3 = (a_1 - x1) * (x2 - b_0) / denom;
   R c4 = (x1 - a_0) * (x2 - b_0) / denom;
-  const R *r0 = a2 + (size_t)p2 * n1 + p1, *r1 = r0 + n1;
-  return c1 * __ldg(r0) + c2 * __ldg(r0 + 1) + c3 * __ldg(r1) + c4 * __ldg(r1 + 1);
+  const long long o = (long long)p2 * n1 + p1, lim = (long long)n1 * n2;
+  return c1 * XMI_LDG(a2, o, lim, 5) + c2 * XMI_LDG(a2, o + 1, lim, 5) + c3 * XMI_LDG(a2, o + n1, lim, 5) +
+         c4 * XMI_LDG(a2, o + n1 + 1, lim, 5);
 }
 
 template <typename R>
@@ -163,8 +195,30 @@ __device__ __forceinline__ R qtab(const R *t, R q) {
   if (i < 0) i = 0;
   if (i > XMI_NQ - 2) i = XMI_NQ - 2;
   R f = x - (R)i;
-  R v0 = __ldg(t + i), v1 = __ldg(t + i + 1);
+  R v0 = XMI_LDG(t, i, XMI_NQ, 6), v1 = XMI_LDG(t, i + 1, XMI_NQ, 6);
   return v0 + f * (v1 - v0);
+}
+
+/* visits the layers in the direction of travel with compile-time indices
+ * (both orders fully unrolled) so per-layer arrays stay in registers */
+template <typename F>
+__device__ __forceinline__ void layers_in_direction(bool up, F &&f) {
+  if (up) {
+#pragma unroll
+    for (int j = 0; j < XMI_MAXL; j++) f(j);
+  } else {
+#pragma unroll
+    for (int j = XMI_MAXL - 1; j >= 0; j--) f(j);
+  }
+}
+
+template <typename R>
+__device__ __forceinline__ R select_layer(const R *v, int layer) {
+  R out = (R)0;
+#pragma unroll
+  for (int j = 0; j < XMI_MAXL; j++)
+    if (j == layer) out = v[j];
+  return out;
 }
 
 /* ---------------- tallies ---------------- */
@@ -191,7 +245,17 @@ template <typename R>
 __device__ __forceinline__ void tally_channel(const DevBundle<R> &b, const DevTally &t, int n, R E, double w) {
   int ch = -1;
   if (E >= (R)kEnergyThreshold) ch = (int)(((double)E - b.zero) / b.gain);
-  if (ch >= 0 && ch <= b.nch - 1) tally_add(&t.chan[(size_t)n * b.nch + ch], w);
+  if (ch >= 0 && ch <= b.nch - 1 && XMI_CHK((long long)n * b.nch + ch, (long long)(b.N + 1) * b.nch, 30))
+    tally_add(&t.chan[(size_t)n * b.nch + ch], w);
+}
+
+template <typename R>
+__device__ __forceinline__ void tally_hist(const DevBundle<R> &b, const DevTally &t, double *s_hist, bool use_smem,
+                                           int n, int slot, double w) {
+  const long long idx = (long long)(n - 1) * b.n_slots + slot;
+  if (!XMI_CHK(idx, (long long)b.N * b.n_slots, 31)) return;
+  if (use_smem) tally_add(&s_hist[idx], w);
+  else tally_add(&t.hist_vr[idx], w);
 }
 
 /* ---------------- solid angle ---------------- */
@@ -283,9 +347,10 @@ __device__ R get_solid_angle(const DevBundle<R> &b, const double *coords, const 
   R c2 = (R)((x1 - a0) * (b1 - x2)) / denom;
   R c3 = (R)((a1 - x1) * (x2 - b0)) / denom;
   R c4 = (R)((x1 - a0) * (x2 - b0)) / denom;
-  const R *g0 = b.sa_grid + (size_t)p2 * b.sa_nr + p1, *g1 = g0 + b.sa_nr;
+  const long long o = (long long)p2 * b.sa_nr + p1, lim = (long long)b.sa_nr * b.sa_nt;
   (void)ok;
-  return c1 * __ldg(g0) + c2 * __ldg(g0 + 1) + c3 * __ldg(g1) + c4 * __ldg(g1 + 1);
+  return c1 * XMI_LDG(b.sa_grid, o, lim, 7) + c2 * XMI_LDG(b.sa_grid, o + 1, lim, 7) +
+         c3 * XMI_LDG(b.sa_grid, o + b.sa_nr, lim, 7) + c4 * XMI_LDG(b.sa_grid, o + b.sa_nr + 1, lim, 7);
 }
 
 /* ---------------- photon kinematics ---------------- */
@@ -314,7 +379,21 @@ template <typename R>
 __device__ __forceinline__ void update_elecv(Photon<R> &p) {
   R cosalfa = rdot(p.d, p.el);
   R c_alfa = acos(cosalfa);
-  R c_ae = (R)1 / sin(c_alfa), c_be = -c_ae * cosalfa;
+  R sinalfa = sin(c_alfa);
+  if (!(fabs(sinalfa) > (R)0)) {
+    /* direction parallel to the E-vector after rounding (reachable in FP32 only):
+     * any unit vector perpendicular to the direction is a valid E-vector, the
+     * reference formula would produce inf/NaN here */
+    R ax[3] = {(R)0, (R)0, (R)0};
+    int k = fabs(p.d[0]) < fabs(p.d[1]) ? (fabs(p.d[0]) < fabs(p.d[2]) ? 0 : 2) : (fabs(p.d[1]) < fabs(p.d[2]) ? 1 : 2);
+    ax[k] = (R)1;
+    p.el[0] = p.d[1] * ax[2] - p.d[2] * ax[1];
+    p.el[1] = p.d[2] * ax[0] - p.d[0] * ax[2];
+    p.el[2] = p.d[0] * ax[1] - p.d[1] * ax[0];
+    rnorm(p.el);
+    return;
+  }
+  R c_ae = (R)1 / sinalfa, c_be = -c_ae * cosalfa;
 #pragma unroll
   for (int k = 0; k < 3; k++) p.el[k] = c_ae * p.el[k] + c_be * p.d[k];
   rnorm(p.el);
@@ -345,7 +424,8 @@ __device__ R compton_energy(const DevBundle<R> &b, int e, R E, R theta_i, xmi_rn
     int pos = (int)(r / dr);
     if (varred && pos == XMI_DOPPLER_N - 2) continue;
     if (pos > XMI_DOPPLER_N - 2) pos = XMI_DOPPLER_N - 2;
-    R r0 = __ldg(rn + pos), r1 = __ldg(rn + pos + 1), q0 = __ldg(icdf + pos), q1 = __ldg(icdf + pos + 1);
+    R r0 = XMI_LDG(rn, pos, XMI_DOPPLER_N, 8), r1 = XMI_LDG(rn, pos + 1, XMI_DOPPLER_N, 8);
+    R q0 = XMI_LDG(icdf, pos, XMI_DOPPLER_N, 8), q1 = XMI_LDG(icdf, pos + 1, XMI_DOPPLER_N, 8);
     R pz = q0 + ((q1 - q0) * (r - r0) / (r1 - r0));
     if (uni<R>(g) < (R)0.5) pz = -pz;
     R dlamb = c0 * sth2 * sth2 - c1 * c_lamb0 * sth2 * pz;
@@ -367,6 +447,7 @@ template <typename R>
 __device__ void variance_reduction(const DevBundle<R> &b, Photon<R> &p, xmi_rng *g, const DevTally &t,
                                    double *s_hist, bool use_smem, bool &ok) {
   if (p.E <= (R)kEnergyThreshold) return;
+  if (!XMI_CHK(p.layer, b.n_layers, 34)) { ok = false; return; }
   const int n = p.n_int, layer = p.layer;
   R radius = sqrt(uni<R>(g)) * (R)b.det_radius;
   R ang = (R)(2.0 * kPi) * uni<R>(g);
@@ -396,9 +477,14 @@ __device__ void variance_reduction(const DevBundle<R> &b, Photon<R> &p, xmi_rng 
     R d = rdot(ndc, p.d);
 #pragma unroll
     for (int k = 0; k < 3; k++) proj[k] = ndc[k] - d * p.d[k];
-    rnorm(proj);
+    R pn = sqrt(rdot(proj, proj));
     R ne = sqrt(rdot(p.el, p.el));
-    dotprod = (proj[0] * (p.el[0] / ne) + proj[1] * (p.el[1] / ne) + proj[2] * (p.el[2] / ne));
+    if (pn > (R)0) {
+      proj[0] /= pn; proj[1] /= pn; proj[2] /= pn;
+      dotprod = (proj[0] * (p.el[0] / ne) + proj[1] * (p.el[1] / ne) + proj[2] * (p.el[2] / ne));
+    } else {
+      dotprod = (R)1; /* forward direction: the azimuth is undefined, take 0 */
+    }
   }
   dotprod = dotprod > (R)1 ? (R)1 : (dotprod < (R)-1 ? (R)-1 : dotprod);
   const R phi = acos(dotprod);
@@ -410,14 +496,13 @@ __device__ void variance_reduction(const DevBundle<R> &b, Photon<R> &p, xmi_rng 
 #pragma unroll
   for (int j = 0; j < XMI_MAXL; j++) dist[j] = (R)0;
   {
-    double tc[3] = {p.c[0], p.c[1], p.c[2]}, ip[3], dd;
-    bool done = false;
-#pragma unroll
-    for (int k = 0; k < XMI_MAXL; k++) {
-      int j = up ? k : XMI_MAXL - 1 - k;
+    double tc[3] = {p.c[0], p.c[1], p.c[2]};
+    bool done = false, fail = false;
+    layers_in_direction(up, [&](int j) {
       bool active = up ? (j >= layer && j < b.n_layers) : (j <= layer);
-      if (active && !done) {
-        if (!plane_step(tc, ndc, b.n_sample, up ? b.zend[j] : b.zbeg[j], ip, &dd)) { ok = false; return; }
+      if (active && !done && !fail) {
+        double ip[3], dd;
+        if (!plane_step(tc, ndc, b.n_sample, up ? b.zend[j] : b.zbeg[j], ip, &dd)) { fail = true; return; }
         if (dd > total_distance) {
           dist[j] = (R)total_distance;
           done = true;
@@ -427,7 +512,8 @@ __device__ void variance_reduction(const DevBundle<R> &b, Photon<R> &p, xmi_rng 
           total_distance = total_distance - dd;
         }
       }
-    }
+    });
+    if (fail) { ok = false; return; }
   }
   R murhod = (R)0;
 #pragma unroll
@@ -439,7 +525,7 @@ __device__ void variance_reduction(const DevBundle<R> &b, Photon<R> &p, xmi_rng 
   int node;
   R f;
   locate(b, p.E, node, f);
-  const R mu_here = p.mus[layer];
+  const R mu_here = select_layer(p.mus, layer);
   const R q = p.E / (R)12.39852 * sin(theta / (R)2);
   const R st = sin(theta), cp = cos(phi), ct = cos(theta);
   const R thomson = (R)1 - st * st * cp * cp;
@@ -449,15 +535,14 @@ __device__ void variance_reduction(const DevBundle<R> &b, Photon<R> &p, xmi_rng 
   const int nel = b.nel[layer], off = b.off[layer];
 
   for (int i = 0; i < nel; i++) {
-    const int e = __ldg(b.layer_el + off + i);
-    const R w = __ldg(b.layer_w + off + i);
+    const int e = XMI_LDG(b.layer_el, off + i, b.n_layer_el, 9);
+    const R w = XMI_LDG(b.layer_w, off + i, b.n_layer_el, 9);
     /* Rayleigh */
     R pconv = w / mu_here;
     R pdir = omega * thomson * qtab(b.ff2 + (size_t)e * XMI_NQ, q);
     double tw = (double)(pconv * pdir * pesc_rayl * p.w);
     const int rs = b.n_lines + 2 * e;
-    if (use_smem) tally_add(&s_hist[(size_t)(n - 1) * b.n_slots + rs], tw);
-    else tally_add(&t.hist_vr[(size_t)(n - 1) * b.n_slots + rs], tw);
+    tally_hist(b, t, s_hist, use_smem, n, rs, tw);
     tally_channel(b, t, n, p.E, tw);
     /* Compton */
     R ec = compton_energy(b, e, p.E, theta, g, true, ok);
@@ -470,14 +555,16 @@ __device__ void variance_reduction(const DevBundle<R> &b, Photon<R> &p, xmi_rng 
     R pesc = exp(-murhod);
     pdir = omega * kn * qtab(b.sf + (size_t)e * XMI_NQ, q);
     tw = (double)(pconv * pdir * pesc * p.w);
-    if (use_smem) tally_add(&s_hist[(size_t)(n - 1) * b.n_slots + rs + 1], tw);
-    else tally_add(&t.hist_vr[(size_t)(n - 1) * b.n_slots + rs + 1], tw);
+    tally_hist(b, t, s_hist, use_smem, n, rs + 1, tw);
     tally_channel(b, t, n, ec, tw);
     /* fluorescence */
     R P[XMI_NSHELL];
+    if (after_fluo && !XMI_CHK(p.h_slot, b.n_lines, 43)) { ok = false; return; }
     if (after_fluo) {
 #pragma unroll
-      for (int s = 0; s < XMI_NSHELL; s++) P[s] = __ldg(b.precalc_xrf + ((size_t)e * XMI_NSHELL + s) * b.n_lines + p.h_slot);
+      for (int s = 0; s < XMI_NSHELL; s++)
+        P[s] = XMI_LDG(b.precalc_xrf, ((long long)e * XMI_NSHELL + s) * b.n_lines + p.h_slot,
+                       (long long)b.n_elem * XMI_NSHELL * b.n_lines, 10);
     } else {
 #pragma unroll
       for (int s = 0; s < XMI_NSHELL; s++) P[s] = el_val(b, e, XMI_REC_XRF + s, node, f);
@@ -486,30 +573,32 @@ __device__ void variance_reduction(const DevBundle<R> &b, Photon<R> &p, xmi_rng 
 #pragma unroll
       for (int s = 4; s < XMI_NSHELL; s++) P[s] = (R)0;
     }
-    const int l0 = __ldg(b.line_off + e), l1 = __ldg(b.line_off + e + 1);
+    const int l0 = XMI_LDG(b.line_off, e, b.n_elem + 1, 11), l1 = XMI_LDG(b.line_off, e + 1, b.n_elem + 1, 11);
     const R *fy = b.fluor_yield + (size_t)e * XMI_NSHELL;
     for (int sl = l0; sl < l1; sl++) {
-      const int line = __ldg(b.line_index + sl);
+      const int line = XMI_LDG(b.line_index, sl, b.n_lines, 12);
       if (line > b.line_last) break; /* slots are sorted by line index */
-      const R efl = __ldg(b.line_energy + sl);
+      const R efl = XMI_LDG(b.line_energy, sl, b.n_lines, 12);
       if (efl < (R)kEnergyThreshold) continue;
       if (line == 30 || line == 31 || line == 59) continue;
-      const int sh = __ldg(b.line_shell + sl);
+      const int sh = XMI_LDG(b.line_shell, sl, b.n_lines, 12);
       R ps = (R)0;
 #pragma unroll
       for (int s = 0; s < XMI_NSHELL; s++)
         if (s == sh) ps = P[s];
       if (ps == (R)0) continue;
-      pconv = w * ps * __ldg(fy + sh) * __ldg(b.line_rate + sl) / mu_here;
+      pconv = w * ps * XMI_LDG(b.fluor_yield, (long long)e * XMI_NSHELL + sh, (long long)b.n_elem * XMI_NSHELL, 13) *
+              XMI_LDG(b.line_rate, sl, b.n_lines, 12) / mu_here;
       murhod = (R)0;
 #pragma unroll
       for (int j = 0; j < XMI_MAXL; j++)
-        if (j < b.n_layers) murhod += __ldg(b.precalc_mu + (size_t)j * b.n_lines + sl) * b.rho[j] * dist[j];
+        if (j < b.n_layers)
+          murhod += XMI_LDG(b.precalc_mu, (long long)j * b.n_lines + sl, (long long)b.n_layers * b.n_lines, 14) *
+                    b.rho[j] * dist[j];
       pesc = exp(-murhod);
       tw = (double)(pconv * pdir_fluo * pesc * p.w);
       if (tw == 0.0) continue;
-      if (use_smem) tally_add(&s_hist[(size_t)(n - 1) * b.n_slots + sl], tw);
-      else tally_add(&t.hist_vr[(size_t)(n - 1) * b.n_slots + sl], tw);
+      tally_hist(b, t, s_hist, use_smem, n, sl, tw);
     }
   }
 }
@@ -646,7 +735,7 @@ __device__ bool fluorescence(const DevBundle<R> &b, Photon<R> &p, xmi_rng *g) {
     p.E = (R)0;
     return true;
   }
-  const R yc = __ldg(b.yield_corr + (size_t)e * XMI_NSHELL + shell);
+  const R yc = XMI_LDG(b.yield_corr, (long long)e * XMI_NSHELL + shell, (long long)b.n_elem * XMI_NSHELL, 15);
   if (b.use_vr == 0 && b.escape_mode == 0) {
     r = uni<R>(g);
     if (r > yc) {
@@ -662,24 +751,26 @@ __device__ bool fluorescence(const DevBundle<R> &b, Photon<R> &p, xmi_rng *g) {
   r = uni<R>(g);
   sumz = (R)0;
   int slot = -1;
-  const int s0 = __ldg(b.shell_off + 10 * e + shell), s1 = __ldg(b.shell_off + 10 * e + shell + 1);
+  const int s0 = XMI_LDG(b.shell_off, 10 * e + shell, 10 * b.n_elem, 16);
+  const int s1 = XMI_LDG(b.shell_off, 10 * e + shell + 1, 10 * b.n_elem, 16);
   for (int sl = s0; sl < s1; sl++) {
-    sumz = sumz + __ldg(b.line_rate + sl);
+    sumz = sumz + XMI_LDG(b.line_rate, sl, b.n_lines, 17);
     if (r < sumz) { slot = sl; break; }
   }
   if (slot < 0) {
     p.E = (R)0;
     return true;
   }
-  p.E = __ldg(b.line_energy + slot);
+  p.E = XMI_LDG(b.line_energy, slot, b.n_lines, 17);
 #pragma unroll
   for (int j = 0; j < XMI_MAXL; j++)
-    p.mus[j] = j < b.n_layers ? __ldg(b.precalc_mu + (size_t)j * b.n_lines + slot) : (R)0;
+    p.mus[j] = j < b.n_layers ? XMI_LDG(b.precalc_mu, (long long)j * b.n_lines + slot,
+                                        (long long)b.n_layers * b.n_lines, 18) : (R)0;
   R theta_i = acos((R)-2 * uni<R>(g) + (R)1);
   R phi_i = (R)(2.0 * kPi) * uni<R>(g);
   update_dirv(p, theta_i, phi_i);
   update_elecv(p);
-  p.h_type = -__ldg(b.line_index + slot);
+  p.h_type = -XMI_LDG(b.line_index, slot, b.n_lines, 17);
   p.h_elem = e;
   p.h_slot = slot;
   return true;
@@ -775,88 +866,88 @@ __device__ bool simulate_photon(const DevBundle<R> &b, Photon<R> &p, const DevTa
     if ((b.escape_mode == 1 && p.n_int == 1) || (b.use_vr == 0 && b.escape_mode == 0)) {
       R minr = (R)0, maxr = (R)0, blbs = (R)1;
       bool stop = false;
-#pragma unroll
-      for (int k = 0; k < XMI_MAXL; k++) {
-        int j = up ? k : XMI_MAXL - 1 - k;
+      int outcome = 0; /* 0 continue, 1 photon absorbed by collimator/bad hit, 2 detector hit, 3 error */
+      layers_in_direction(up, [&](int j) {
         bool active = up ? (j >= p.layer && j < b.n_layers) : (j <= p.layer);
-        if (active && !stop) {
-          double ip[3], dd;
-          if (!plane_step(p.c, p.d, b.n_sample, up ? b.zend[j] : b.zbeg[j], ip, &dd)) return false;
-          R tp = (R)-1 * (R)dd * b.rho[j] * p.mus[j];
-          R tempexp = exp(tp);
-          minr = maxr;
-          maxr = maxr - blbs * expm1(tp);
-          if (R0 <= maxr) {
-            R dist = (R)-1 * log1p((R)-1 * (R0 - minr) / blbs) / p.mus[j] / b.rho[j];
-            double tc[3] = {p.c[0], p.c[1], p.c[2]};
+        if (!active || stop) return;
+        double ip[3], dd;
+        if (!plane_step(p.c, p.d, b.n_sample, up ? b.zend[j] : b.zbeg[j], ip, &dd)) { outcome = 3; stop = true; return; }
+        R tp = (R)-1 * (R)dd * b.rho[j] * p.mus[j];
+        R tempexp = exp(tp);
+        minr = maxr;
+        maxr = maxr - blbs * expm1(tp);
+        if (R0 <= maxr) {
+          R dist = (R)-1 * log1p((R)-1 * (R0 - minr) / blbs) / p.mus[j] / b.rho[j];
+          double tc[3] = {p.c[0], p.c[1], p.c[2]};
 #pragma unroll
-            for (int q = 0; q < 3; q++) p.c[q] = p.c[q] + (double)dist * (double)p.d[q];
-            if (b.escape_mode != 1) {
-              int rc = check_detector_intersection(b.p_det, b.det_inv, b.coll_present, b.det_radius, b.coll_height,
-                                                   b.coll_half_apex, b.coll_vertex_x, tc, p.c);
-              if (rc == 1 || rc == 3) return true;
-              if (rc == 2) { p.hit = 1; return true; }
-            }
-            p.layer = j;
-            p.inside = 1;
-            stop = true;
-          } else {
-            if (b.escape_mode != 1) {
-              int rc = check_detector_intersection(b.p_det, b.det_inv, b.coll_present, b.det_radius, b.coll_height,
-                                                   b.coll_half_apex, b.coll_vertex_x, p.c, ip);
-              if (rc == 1 || rc == 3) return true;
-              if (rc == 2) { p.hit = 1; return true; }
-            }
-            p.c[0] = ip[0]; p.c[1] = ip[1]; p.c[2] = ip[2];
-            blbs = blbs * tempexp;
+          for (int q = 0; q < 3; q++) p.c[q] = p.c[q] + (double)dist * (double)p.d[q];
+          if (b.escape_mode != 1) {
+            int rc = check_detector_intersection(b.p_det, b.det_inv, b.coll_present, b.det_radius, b.coll_height,
+                                                 b.coll_half_apex, b.coll_vertex_x, tc, p.c);
+            if (rc == 1 || rc == 3) { outcome = 1; stop = true; return; }
+            if (rc == 2) { outcome = 2; stop = true; return; }
           }
+          p.layer = j;
+          p.inside = 1;
+          stop = true;
+        } else {
+          if (b.escape_mode != 1) {
+            int rc = check_detector_intersection(b.p_det, b.det_inv, b.coll_present, b.det_radius, b.coll_height,
+                                                 b.coll_half_apex, b.coll_vertex_x, p.c, ip);
+            if (rc == 1 || rc == 3) { outcome = 1; stop = true; return; }
+            if (rc == 2) { outcome = 2; stop = true; return; }
+          }
+          p.c[0] = ip[0]; p.c[1] = ip[1]; p.c[2] = ip[2];
+          blbs = blbs * tempexp;
         }
-      }
+      });
+      if (outcome == 3) return false;
+      if (outcome == 1) return true;
+      if (outcome == 2) { p.hit = 1; return true; }
     } else {
       if (p.n_int == b.N) break;
       R dist[XMI_MAXL];
       double lp[3] = {p.c[0], p.c[1], p.c[2]};
       R pabs = (R)0;
-#pragma unroll
-      for (int k = 0; k < XMI_MAXL; k++) {
-        int j = up ? k : XMI_MAXL - 1 - k;
-        bool active = up ? (j >= p.layer && j < b.n_layers) : (j <= p.layer);
+      bool fail = false;
+      const int cur = p.layer;
+      layers_in_direction(up, [&](int j) {
+        bool active = up ? (j >= cur && j < b.n_layers) : (j <= cur);
         dist[j] = (R)0;
-        if (active) {
+        if (active && !fail) {
           double ip[3], dd;
-          if (!plane_step(lp, p.d, b.n_sample, up ? b.zend[j] : b.zbeg[j], ip, &dd)) return false;
+          if (!plane_step(lp, p.d, b.n_sample, up ? b.zend[j] : b.zbeg[j], ip, &dd)) { fail = true; return; }
           dist[j] = (R)dd;
           lp[0] = ip[0]; lp[1] = ip[1]; lp[2] = ip[2];
           pabs = pabs + p.mus[j] * b.rho[j] * dist[j];
         }
-      }
+      });
+      if (fail) return false;
       R pabs2 = (R)-1 * expm1((R)-1 * pabs);
       p.w = p.w * pabs2;
       if (b.escape_mode == 1) p.we = p.w;
       R negln = (R)-1 * log1p((R)-1 * R0 * pabs2);
-      int my_index = p.layer;
-      R my_sum = (R)0, mr_sel = (R)0;
+      int my_index = cur;
+      R my_sum = (R)0;
       bool found = false;
-#pragma unroll
-      for (int k = 0; k < XMI_MAXL; k++) {
-        int j = up ? k : XMI_MAXL - 1 - k;
-        bool active = up ? (j >= p.layer && j < b.n_layers) : (j <= p.layer);
+      layers_in_direction(up, [&](int j) {
+        bool active = up ? (j >= cur && j < b.n_layers) : (j <= cur);
         if (active && !found) {
           my_sum = my_sum + p.mus[j] * b.rho[j] * dist[j];
           if (my_sum > negln) { my_index = j; found = true; }
         }
-      }
+      });
+      R mr_sel = (R)0;
 #pragma unroll
       for (int j = 0; j < XMI_MAXL; j++)
         if (j == my_index) mr_sel = p.mus[j] * b.rho[j];
       R temp_sum = (R)0;
-#pragma unroll
-      for (int k = 0; k < XMI_MAXL; k++) {
-        int j = up ? k : XMI_MAXL - 1 - k;
-        bool active = up ? (j >= p.layer && j <= my_index) : (j <= p.layer && j >= my_index);
+      layers_in_direction(up, [&](int j) {
+        bool active = up ? (j >= cur && j <= my_index) : (j <= cur && j >= my_index);
         if (active) temp_sum = temp_sum + ((R)1 - (p.mus[j] * b.rho[j] / mr_sel)) * dist[j];
-      }
+      });
       temp_sum = temp_sum - (R)1 * log1p((R)-1 * R0 * pabs2) / mr_sel;
+      if (!XMI_CHK(my_index, b.n_layers, 41)) return false;
 #pragma unroll
       for (int q = 0; q < 3; q++) p.c[q] = p.c[q] + (double)temp_sum * (double)p.d[q];
       p.inside = 1;
@@ -878,6 +969,7 @@ __device__ bool simulate_photon(const DevBundle<R> &b, Photon<R> &p, const DevTa
     R f;
     locate(b, p.E, node, f);
     R r = uni<R>(&g);
+    if (!XMI_CHK(p.layer, b.n_layers, 33)) return false;
     const int L = p.layer, nel = b.nel[L], off = b.off[L];
     R mu_l = (R)0;
 #pragma unroll
@@ -886,10 +978,12 @@ __device__ bool simulate_photon(const DevBundle<R> &b, Photon<R> &p, const DevTa
     R thr = (R)0;
     int sel = nel - 1;
     for (int i = 0; i < nel; i++) {
-      thr = thr + __ldg(b.layer_w + off + i) * el_val(b, __ldg(b.layer_el + off + i), XMI_REC_TOT, node, f) / mu_l;
+      thr = thr + XMI_LDG(b.layer_w, off + i, b.n_layer_el, 19) *
+                      el_val(b, XMI_LDG(b.layer_el, off + i, b.n_layer_el, 19), XMI_REC_TOT, node, f) / mu_l;
       if (r < thr) { sel = i; break; }
     }
-    p.elem = __ldg(b.layer_el + off + sel);
+    p.elem = XMI_LDG(b.layer_el, off + sel, b.n_layer_el, 19);
+    if (!XMI_CHK(p.elem, b.n_elem, 42)) return false;
     r = uni<R>(&g);
     R pr = el_val(b, p.elem, XMI_REC_PR, node, f);
     R prc = el_val(b, p.elem, XMI_REC_PRC, node, f);
@@ -948,7 +1042,7 @@ __device__ bool start_photon(const DevBundle<R> &b, const xmi_source_item &it, l
     int node;
     R f;
     locate(b, p.E, node, f);
-    R ex0 = __ldg(b.exc_tab + node), ex1 = __ldg(b.exc_tab + node + 1);
+    R ex0 = XMI_LDG(b.exc_tab, node, b.n_nodes, 20), ex1 = XMI_LDG(b.exc_tab, node + 1, b.n_nodes, 20);
     R exc_corr = exp((R)-1 * (ex0 + f * (ex1 - ex0)));
     mu_calc(b, p.E, p.mus);
     p.w = (R)it.weight * exc_corr;
@@ -1031,10 +1125,11 @@ __global__ void __launch_bounds__(256) transport_kernel(DevBundle<R> b, DevTally
     int lo = 0, hi = b.n_items - 1;
     while (lo < hi) {
       int mid = (lo + hi + 1) >> 1;
-      if (w >= __ldg(b.item_first + mid)) lo = mid; else hi = mid - 1;
+      if (w >= XMI_LDG(b.item_first, mid, b.n_items, 21)) lo = mid; else hi = mid - 1;
     }
+    if (!XMI_CHK(lo, b.n_items, 40)) continue;
     const xmi_source_item &it = b.items[lo];
-    const long long j = w - __ldg(b.item_first + lo);
+    const long long j = w - XMI_LDG(b.item_first, lo, b.n_items, 21);
     Photon<R> p;
     p.id = it.first + j;
     p.n_int = 0;
@@ -1055,7 +1150,8 @@ __global__ void __launch_bounds__(256) transport_kernel(DevBundle<R> b, DevTally
         if (p.h_type < 0) slot = p.h_slot;
         else if (p.h_type == XMI_RAYLEIGH) slot = b.n_lines + 2 * p.h_elem;
         else if (p.h_type == XMI_COMPTON) slot = b.n_lines + 2 * p.h_elem + 1;
-        if (slot >= 0) atomicAdd(&t.hist_brute[(size_t)(p.n_int - 1) * b.n_slots + slot], (double)p.w);
+        if (slot >= 0 && XMI_CHK((long long)(p.n_int - 1) * b.n_slots + slot, (long long)b.N * b.n_slots, 32))
+          atomicAdd(&t.hist_brute[(size_t)(p.n_int - 1) * b.n_slots + slot], (double)p.w);
       }
     }
   }

@@ -31,6 +31,7 @@ struct xmi_tables_handle {
   xmi_bundle b;
   int cascade_type, use_M_lines;
   double *exc_tab;   /* [n_nodes] sum over excitation absorbers of rho*t*mu(E) */
+  int replica, n_replicas; /* photon-range partition of this process (0 of 1 by default) */
   void *dev;         /* device mirror, owned by the CUDA side */
   const double *dev_sa_src; /* host grid pointer the device copy was made from */
 };

@@ -224,6 +224,10 @@ class Simulation:
         _check(self.lib.xmi_gpu_prepare_run(self.inputF, self.tables, C.byref(self.options), n_mpi_hosts, sa),
                "xmi_gpu_prepare_run")
 
+    def set_replica(self, replica: int, n_replicas: int) -> None:
+        """This process simulates photons [r*n/R, (r+1)*n/R) of every source item."""
+        _check(self.lib.xmi_gpu_set_replica(self.tables, replica, n_replicas), "xmi_gpu_set_replica")
+
     def bundle_ptr(self) -> int:
         return self.lib.xmi_gpu_bundle(self.tables)
 
