@@ -40,6 +40,9 @@ typedef struct {
   int threads_per_block;    /* 0: default */
   int blocks_per_sm;        /* 0: default */
   unsigned long long seed;  /* Philox key; 0: fixed default key (0x5EED0001) */
+  int solid_angle_stream;   /* 0: Philox grid draws; 1: the OpenCL backend's Threefry
+                               stream (src/xmi_kernels.cl:226-227), for point-by-point
+                               comparison with that kernel */
 } xmi_gpu_options;
 
 /* ---- data model helpers (reference src/xmi_data_structs.c) ---- */

@@ -40,6 +40,11 @@ def load() -> C.CDLL:
         _lib.oracle_words_counted.argtypes = []
         _lib.oracle_philox_block.restype = None
         _lib.oracle_philox_block.argtypes = [C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]
+        _lib.oracle_solid_angle_points_cl_stream.restype = None
+        _lib.oracle_solid_angle_points_cl_stream.argtypes = [C.c_void_p, dp, dp, C.POINTER(C.c_int),
+                                                             C.POINTER(C.c_int), C.c_int, C.c_long, dp]
+        _lib.oracle_threefry_block.restype = None
+        _lib.oracle_threefry_block.argtypes = [C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]
         _lib.oracle_convolute_spectrum.restype = C.c_int
         _lib.oracle_convolute_spectrum.argtypes = [dp, dp, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
                                                    C.c_int, C.c_double, C.c_double, C.POINTER(OracleEscape), C.c_int,
@@ -79,6 +84,63 @@ def solid_angle_points(bundle_ptr: int, r_vals: np.ndarray, t_vals: np.ndarray, 
     t = np.ascontiguousarray(t_vals, dtype=np.float64)
     lib.oracle_solid_angle_points(C.c_void_p(bundle_ptr), _dp(r), len(r), _dp(t), p0, p1, hits_per_single, _dp(out))
     return out
+
+
+def solid_angle_points_cl_stream(bundle_ptr: int, r_vals: np.ndarray, t_vals: np.ndarray, ir, it,
+                                 hits_per_single: int = 5000) -> np.ndarray:
+    """Grid points (ir[k], it[k]) with the OpenCL kernel's Threefry stream."""
+    lib = load()
+    r = np.ascontiguousarray(r_vals, dtype=np.float64)
+    t = np.ascontiguousarray(t_vals, dtype=np.float64)
+    ir = np.ascontiguousarray(ir, dtype=np.int32)
+    it = np.ascontiguousarray(it, dtype=np.int32)
+    out = np.zeros(len(ir))
+    ip = C.POINTER(C.c_int)
+    lib.oracle_solid_angle_points_cl_stream(C.c_void_p(bundle_ptr), _dp(r), _dp(t), ir.ctypes.data_as(ip),
+                                            it.ctypes.data_as(ip), len(ir), hits_per_single, _dp(out))
+    return out
+
+
+def threefry_block(ctr, key):
+    lib = load()
+    c = (C.c_uint32 * 4)(*ctr)
+    k = (C.c_uint32 * 4)(*key)
+    o = (C.c_uint32 * 4)()
+    lib.oracle_threefry_block(c, k, o)
+    return list(o)
+
+
+REF_CL_LIB = Path(__file__).resolve().parent / "_ref" / "libref_cl.so"
+
+
+def ref_cl_solid_angle_points(r_vals, t_vals, ir, it, collimator_present: int, detector_radius: float,
+                              collimator_radius: float, collimator_height: float, hits_per_single: int = 5000):
+    """The reference's own OpenCL solid-angle kernel run on the host
+    (oracle/_ref/libref_cl.so, built by oracle/ref_cl/Makefile from the
+    reference tree).  FP32 axes and results, as the reference uploads them."""
+    lib = C.CDLL(str(REF_CL_LIB))
+    f = lib.ref_cl_solid_angle_points
+    fp, ip = C.POINTER(C.c_float), C.POINTER(C.c_int)
+    f.restype = None
+    f.argtypes = [fp, C.c_int, fp, C.c_int, ip, ip, C.c_int, C.c_int, C.c_float, C.c_float, C.c_float, C.c_int, fp]
+    r = np.ascontiguousarray(r_vals, dtype=np.float32)
+    t = np.ascontiguousarray(t_vals, dtype=np.float32)
+    ir = np.ascontiguousarray(ir, dtype=np.int32)
+    it = np.ascontiguousarray(it, dtype=np.int32)
+    out = np.zeros(len(ir), dtype=np.float32)
+    f(r.ctypes.data_as(fp), len(r), t.ctypes.data_as(fp), len(t), ir.ctypes.data_as(ip), it.ctypes.data_as(ip),
+      len(ir), collimator_present, detector_radius, collimator_radius, collimator_height, hits_per_single,
+      out.ctypes.data_as(fp))
+    return out
+
+
+def ref_cl_threefry_block(ctr, key):
+    lib = C.CDLL(str(REF_CL_LIB))
+    c = (C.c_uint32 * 4)(*ctr)
+    k = (C.c_uint32 * 4)(*key)
+    o = (C.c_uint32 * 4)()
+    lib.ref_cl_threefry4x32(c, k, o)
+    return list(o)
 
 
 def poly_solve_quadratic(a: float, b: float, c: float):

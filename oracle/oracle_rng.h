@@ -58,4 +58,63 @@ static inline double orng_uniform(orng *g) {
   g->used++;
   return ((double)(a >> 5) * 67108864.0 + (double)(b >> 6)) / 9007199254740992.0;
 }
+
+/* Threefry4x32-20 (Salmon et al., SC'11), the generator of the reference's
+ * OpenCL solid-angle kernel (src/xmi_kernels.cl through Random123), written
+ * from the published description: Threefish-style add/rotate/xor rounds on
+ * word pairs (0,1),(2,3) in even rounds and (0,3),(2,1) in odd rounds, a key
+ * injection after every fourth round, Skein parity word 0x1BD11BDA. */
+static inline uint32_t orot32(uint32_t x, unsigned n) { return (x << n) | (x >> (32u - n)); }
+
+static inline void othreefry4x32(const uint32_t in[4], const uint32_t key[4], uint32_t out[4]) {
+  static const unsigned rot_a[8] = {10, 11, 13, 23, 6, 17, 25, 18};
+  static const unsigned rot_b[8] = {26, 21, 27, 5, 20, 11, 10, 20};
+  uint32_t ks[5], x[4];
+  int round, i;
+  ks[4] = 0x1BD11BDAu;
+  for (i = 0; i < 4; i++) {
+    ks[i] = key[i];
+    ks[4] ^= key[i];
+    x[i] = in[i] + key[i];
+  }
+  for (round = 0; round < 20; round++) {
+    const int a = (round & 1) ? 3 : 1, c = (round & 1) ? 1 : 3;
+    x[0] += x[a];
+    x[a] = orot32(x[a], rot_a[round & 7]) ^ x[0];
+    x[2] += x[c];
+    x[c] = orot32(x[c], rot_b[round & 7]) ^ x[2];
+    if ((round & 3) == 3) {
+      const unsigned s = (unsigned)(round + 1) / 4u;
+      for (i = 0; i < 4; i++) x[i] += ks[(s + (unsigned)i) % 5u];
+      x[3] += s;
+    }
+  }
+  for (i = 0; i < 4; i++) out[i] = x[i];
+}
+
+/* the OpenCL kernel's per-point stream (src/xmi_kernels.cl:226-227,393-404):
+ * key (r index, 0xdecafbad, 0xfacebead, theta index), counter
+ * (j, 0xf00dcafe, 0xdeadbeef, 0xbeeff00d), j incremented before each block;
+ * the four words of a block are consumed in order as float(word) / 2^32 */
+typedef struct {
+  uint32_t key[4], ctr[4], out[4];
+  int used;
+} oclrng;
+
+static inline void oclrng_init(oclrng *g, uint32_t ir, uint32_t it) {
+  g->key[0] = ir; g->key[1] = 0xdecafbadu; g->key[2] = 0xfacebeadu; g->key[3] = it;
+  g->ctr[0] = 0u; g->ctr[1] = 0xf00dcafeu; g->ctr[2] = 0xdeadbeefu; g->ctr[3] = 0xbeeff00du;
+  g->used = 4;
+}
+
+static inline double oclrng_uniform(oclrng *g) {
+  float u;
+  if (g->used == 4) {
+    g->ctr[0] += 1u;
+    othreefry4x32(g->ctr, g->key, g->out);
+    g->used = 0;
+  }
+  u = (float)g->out[g->used++] / 4294967296.0f;
+  return (double)u;
+}
 #endif

@@ -189,7 +189,12 @@ static double dcsp_compt(const xmi_bundle *b, int e, double E, double theta, dou
 /* solid angle                                                          */
 /* ------------------------------------------------------------------ */
 /* xmi_single_solid_angle_calculation, src/xmi_solid_angle_f.F90:432-710 */
-double oracle_single_solid_angle(const xmi_bundle *b, double r1, double theta1, orng *g, long hits_per_single) {
+typedef double (*ouniform_fn)(void *);
+static double ouni_philox(void *g) { return orng_uniform((orng *)g); }
+static double ouni_cl(void *g) { return oclrng_uniform((oclrng *)g); }
+
+static double single_solid_angle(const xmi_bundle *b, double r1, double theta1, ouniform_fn uni, void *g,
+                                 long hits_per_single) {
   double r, theta, fcbr, beta, alpha1, fca, cfca, fcsa, rot[9];
   double line_point[3];
   long hits = 0, i;
@@ -239,8 +244,8 @@ double oracle_single_solid_angle(const xmi_bundle *b, double r1, double theta1, 
   line_point[1] = r1 * cos(theta1);
   line_point[2] = r1 * sin(theta1);
   for (i = 0; i < hits_per_single; i++) {
-    double th = acos(1.0 - orng_uniform(g) * (1.0 - cfca));
-    double ph = orng_uniform(g) * 2.0 * M_PI;
+    double th = acos(1.0 - uni(g) * (1.0 - cfca));
+    double ph = uni(g) * 2.0 * M_PI;
     double dc[3], dd[3], ip[3];
     static const double dn[3] = {0.0, 0.0, 1.0}, origin[3] = {0.0, 0.0, 0.0};
     dc[0] = sin(th) * cos(ph);
@@ -258,6 +263,23 @@ double oracle_single_solid_angle(const xmi_bundle *b, double r1, double theta1, 
     if (norm3(ip) <= detr) hits++;
   }
   return fcsa * (double)hits / (double)hits_per_single;
+}
+
+double oracle_single_solid_angle(const xmi_bundle *b, double r1, double theta1, orng *g, long hits_per_single) {
+  return single_solid_angle(b, r1, theta1, ouni_philox, g, hits_per_single);
+}
+
+/* grid points (ir[k], it[k]) with the OpenCL kernel's Threefry stream, for
+ * the point-by-point comparison with that kernel */
+void oracle_solid_angle_points_cl_stream(const xmi_bundle *b, const double *r_vals, const double *t_vals,
+                                         const int *ir, const int *it, int n, long hits_per_single, double *out) {
+  int k;
+#pragma omp parallel for schedule(dynamic, 1)
+  for (k = 0; k < n; k++) {
+    oclrng g;
+    oclrng_init(&g, (uint32_t)ir[k], (uint32_t)it[k]);
+    out[k] = single_solid_angle(b, r_vals[ir[k]], t_vals[it[k]], ouni_cl, &g, hits_per_single);
+  }
 }
 
 /* full grid (xmi_solid_angle_calculation_f, src/xmi_solid_angle_f.F90:303-429)
@@ -1153,3 +1175,5 @@ long long oracle_words_counted(void) {
 
 /* known-answer helper: raw Philox block */
 void oracle_philox_block(const uint32_t *ctr, const uint32_t *key, uint32_t *out) { orng_block(ctr, key, out); }
+
+void oracle_threefry_block(const uint32_t *ctr, const uint32_t *key, uint32_t *out) { othreefry4x32(ctr, key, out); }

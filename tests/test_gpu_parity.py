@@ -70,6 +70,39 @@ def test_solid_angle_grid_matches_oracle_exactly():
     sim.close()
 
 
+@pytest.mark.parametrize("precision", [1, 0])
+@pytest.mark.parametrize("name", ["no_collimator", "conical_collimator", "conical_collimator_wide"])
+def test_solid_angle_grid_matches_reference_opencl_kernel(name, precision):
+    """The GPU grid drawn from the OpenCL kernel's own Threefry stream against
+    that kernel's results at 600 points per geometry (src/xmi_kernels.cl run
+    on the host, tests/golden/cl_solid_angle.json).  FP32 follows the kernel's
+    arithmetic, so hit counts agree at nearly every point; FP64 agrees with
+    the FP64 oracle exactly and with the FP32 kernel up to rim flips."""
+    import test_oracle as T
+    g = json.loads((GOLDEN / "cl_solid_angle.json").read_text())
+    d = g["geometries"][name]
+    sim = Simulation(T.cl_geometries()[name], options=dict(use_variance_reduction=1, use_escape_peaks=0,
+                                                           use_default_seeds=1),
+                     gpu=gpu_options(precision=precision, seed=SEED, solid_angle_stream=1))
+    grid = sim.solid_angle_grid()
+    vals = grid["grid"][d["it"], d["ir"]]
+    hg = T.hits_of(vals, d["cone_solid_angle"], g["hits_per_single"])
+    hr = T.hits_of(d["value"], d["cone_solid_angle"], g["hits_per_single"])
+    dh = hg - hr
+    if precision == 1:
+        assert (dh == 0).mean() > 0.95
+        assert np.abs(dh).max() <= 3
+    else:
+        sim.prepare()
+        o = oracle().solid_angle_points_cl_stream(sim.bundle_ptr(), grid["r"], grid["theta"], d["ir"], d["it"],
+                                                  g["hits_per_single"])
+        ho = T.hits_of(o, d["cone_solid_angle"], g["hits_per_single"])
+        assert (hg == ho).mean() > 0.99
+        assert (dh == 0).mean() > 0.85
+        assert np.abs(dh).max() <= 5
+    sim.close()
+
+
 def test_solid_angle_grid_fp32_close_to_fp64():
     spec = configs.config1(n_photons_line=10)
     s64 = Simulation(spec, options=configs.C1_OPTIONS, gpu=gpu_options(seed=SEED))

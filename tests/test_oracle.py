@@ -27,6 +27,68 @@ def test_philox_known_answers_oracle_and_engine():
         assert list(out) == v["out"]
 
 
+def test_threefry_matches_reference_random123():
+    """Threefry4x32-20 of the oracle and of the engine against blocks computed
+    by the reference's vendored Random123 header (src/Random123/threefry.h)."""
+    from oracle import oracle_api as O
+    from xmimsim_gb300 import abi
+    lib = abi.load()
+    lib.xmi_gpu_threefry_block.restype = None
+    for v in load("cl_solid_angle.json")["threefry4x32_20"]:
+        assert O.threefry_block(v["ctr"], v["key"]) == v["out"]
+        out = (C.c_uint32 * 4)()
+        lib.xmi_gpu_threefry_block((C.c_uint32 * 4)(*v["ctr"]), (C.c_uint32 * 4)(*v["key"]), out)
+        assert list(out) == v["out"]
+
+
+def cl_geometries():
+    from xmimsim_gb300 import configs
+    plain = configs.config1(n_photons_line=10)
+    con = configs.config1(n_photons_line=10)
+    con.collimator_height, con.collimator_diameter = 1.0, 0.2
+    wide = configs.config1(n_photons_line=10)
+    wide.collimator_height, wide.collimator_diameter = 0.5, 0.4
+    return {"no_collimator": plain, "conical_collimator": con, "conical_collimator_wide": wide}
+
+
+def hits_of(values, cone, hits_per_single):
+    cone = np.asarray(cone)
+    m = cone > 0
+    return np.where(m, np.rint(np.asarray(values) / np.where(m, cone, 1.0) * hits_per_single), 0.0)
+
+
+@pytest.mark.parametrize("name", ["no_collimator", "conical_collimator", "conical_collimator_wide"])
+def test_oracle_solid_angle_matches_reference_opencl_kernel(name):
+    """The FP64 restatement, fed the OpenCL kernel's own Threefry stream,
+    against that kernel's results (src/xmi_kernels.cl run on the host,
+    tests/golden/make_cl_solid_angle.py).  The kernel computes in FP32, so a
+    sample near the detector or aperture rim can fall the other way: hit
+    counts agree exactly at most points, within a few hits everywhere, with
+    no bias in the sum."""
+    from oracle import oracle_api as O
+    from xmimsim_gb300 import Simulation
+    g = load("cl_solid_angle.json")
+    d = g["geometries"][name]
+    sim = Simulation(cl_geometries()[name], options=dict(use_variance_reduction=1, use_escape_peaks=0,
+                                                         use_default_seeds=1))
+    r, t = sim.grid_axes(1024, 1024)
+    assert np.array_equal(np.float32(r[d["ir"]]), np.float32(d["r"]))
+    assert np.array_equal(np.float32(t[d["it"]]), np.float32(d["theta"]))
+    sim.set_solid_angle(r, t, np.zeros((1024, 1024)))
+    sim.prepare()
+    o = O.solid_angle_points_cl_stream(sim.bundle_ptr(), r, t, d["ir"], d["it"], g["hits_per_single"])
+    sim.close()
+    ho = hits_of(o, d["cone_solid_angle"], g["hits_per_single"])
+    hr = hits_of(d["value"], d["cone_solid_angle"], g["hits_per_single"])
+    dh = ho - hr
+    assert (dh == 0).mean() > 0.85
+    assert np.abs(dh).max() <= 5
+    assert abs(dh.sum()) <= 4.0 * math.sqrt(max(1.0, (dh ** 2).sum()))
+    ref = np.array(d["value"])
+    if (ref == 0).any():
+        assert (o[ref == 0] == 0).mean() > 0.97
+
+
 def test_quadratic_solver_matches_reference_test():
     """tests/test-poly-solve-quadratic.F90: same root count, roots within 1e-7."""
     from oracle import oracle_api as O

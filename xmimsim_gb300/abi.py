@@ -105,7 +105,8 @@ class XmiEscapeRatiosOptions(C.Structure):
 
 class XmiGpuOptions(C.Structure):
     _fields_ = [("precision", C.c_int), ("use_surrogate", C.c_int), ("surrogate_tolerance", C.c_double),
-                ("threads_per_block", C.c_int), ("blocks_per_sm", C.c_int), ("seed", C.c_ulonglong)]
+                ("threads_per_block", C.c_int), ("blocks_per_sm", C.c_int), ("seed", C.c_ulonglong),
+                ("solid_angle_stream", C.c_int)]
 
 
 # exported symbols and their prototypes (name -> (restype, argtypes))

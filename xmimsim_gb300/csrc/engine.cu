@@ -320,10 +320,12 @@ static int solid_angle_impl(xmi_inputFPtr in, xmi_solid_angle **out, char *input
     cudaEventRecord(e0);
     if (precision == 0)
       xmi::solid_angle_grid_kernel<double><<<blocks, 256>>>(g, dr, nr, dt, 0, (long long)nr * nt,
-                                                              (int)hits_per_single, seed, dout);
+                                                              (int)hits_per_single, seed, in->gpu.solid_angle_stream,
+                                                              dout);
     else
       xmi::solid_angle_grid_kernel<float><<<blocks, 256>>>(g, dr, nr, dt, 0, (long long)nr * nt,
-                                                             (int)hits_per_single, seed, dout);
+                                                             (int)hits_per_single, seed, in->gpu.solid_angle_stream,
+                                                             dout);
     cudaEventRecord(e1);
     ok = cuda_ok(cudaGetLastError(), "solid_angle_grid_kernel") && cuda_ok(cudaEventSynchronize(e1), "sync");
     float ms = 0.f;
@@ -400,6 +402,11 @@ int xmi_gpu_prepare_run(xmi_inputFPtr in, xmi_hdf5FPtr t, xmi_main_options *opti
                         xmi_solid_angle *sa) {
   if (!in || !t || !options) {
     xmi_set_error("xmi_gpu_prepare_run: NULL argument");
+    return 0;
+  }
+  if (options->use_advanced_compton == 1) {
+    /* the per-shell impulse-approximation Compton of src/xmi_main.F90:4785-4983 is not implemented */
+    xmi_set_error("use_advanced_compton = 1 is not supported; the default Doppler-broadened Compton is used with 0");
     return 0;
   }
   int cascade;

@@ -1164,6 +1164,18 @@ void xmi_gpu_philox_block(const uint32_t *ctr, const uint32_t *key, uint32_t *ou
   for (i = 0; i < 4; i++) out[i] = r.v[i];
 }
 
+/* raw Threefry4x32-20 block of the engine's reference solid-angle stream */
+void xmi_gpu_threefry_block(const uint32_t *ctr, const uint32_t *key, uint32_t *out) {
+  xmi_u32x4 c, k, r;
+  int i;
+  for (i = 0; i < 4; i++) {
+    c.v[i] = ctr[i];
+    k.v[i] = key[i];
+  }
+  r = xmi_threefry4x32_20(c, k);
+  for (i = 0; i < 4; i++) out[i] = r.v[i];
+}
+
 /* exported names of the atomic data model and the line table (used by the
  * host-side tube model and by tests) */
 const char *xmi_gpu_line_name(int line) { return xrl_line_name(line); }

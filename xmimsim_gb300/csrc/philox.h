@@ -94,4 +94,50 @@ XMI_HD double xmi_rng_uniform(xmi_rng *g) {
   return ((double)(a >> 5) * 67108864.0 + (double)(b >> 6)) * (1.0 / 9007199254740992.0);
 }
 
+/* Threefry4x32-20 (Salmon et al., SC'11; the Threefish-style ARX round with
+ * the 4x32 rotation schedule of that paper and the Skein key-schedule parity
+ * 0x1BD11BDA), written from the published description.  The engine uses it
+ * only for the reference solid-angle stream of the OpenCL backend
+ * (src/xmi_kernels.cl:219-453): key (r index, 0xdecafbad, 0xfacebead,
+ * theta index), counter (j, 0xf00dcafe, 0xdeadbeef, 0xbeeff00d) for the
+ * j-th pair of cone samples (j = 1, 2, ...). */
+XMI_HD uint32_t xmi_rotl32(uint32_t x, int r) { return (x << r) | (x >> (32 - r)); }
+
+XMI_HD xmi_u32x4 xmi_threefry4x32_20(xmi_u32x4 c, xmi_u32x4 k) {
+  const int rot[8][2] = {{10, 26}, {11, 21}, {13, 27}, {23, 5}, {6, 20}, {17, 11}, {25, 10}, {18, 20}};
+  uint32_t ks[5];
+  uint32_t x0, x1, x2, x3;
+  int r;
+  ks[4] = 0x1BD11BDAu;
+  for (r = 0; r < 4; r++) {
+    ks[r] = k.v[r];
+    ks[4] ^= k.v[r];
+  }
+  x0 = c.v[0] + ks[0];
+  x1 = c.v[1] + ks[1];
+  x2 = c.v[2] + ks[2];
+  x3 = c.v[3] + ks[3];
+#ifdef __CUDA_ARCH__
+#pragma unroll
+#endif
+  for (r = 0; r < 20; r++) {
+    if ((r & 1) == 0) {
+      x0 += x1; x1 = xmi_rotl32(x1, rot[r & 7][0]); x1 ^= x0;
+      x2 += x3; x3 = xmi_rotl32(x3, rot[r & 7][1]); x3 ^= x2;
+    } else {
+      x0 += x3; x3 = xmi_rotl32(x3, rot[r & 7][0]); x3 ^= x0;
+      x2 += x1; x1 = xmi_rotl32(x1, rot[r & 7][1]); x1 ^= x2;
+    }
+    if ((r & 3) == 3) {
+      const uint32_t inj = (uint32_t)((r + 1) >> 2);
+      x0 += ks[inj % 5];
+      x1 += ks[(inj + 1) % 5];
+      x2 += ks[(inj + 2) % 5];
+      x3 += ks[(inj + 3) % 5] + inj;
+    }
+  }
+  c.v[0] = x0; c.v[1] = x1; c.v[2] = x2; c.v[3] = x3;
+  return c;
+}
+
 #endif

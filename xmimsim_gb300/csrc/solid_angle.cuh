@@ -9,6 +9,14 @@
  * exactly that of the sequential oracle.  FP32 and FP64 variants use the
  * same draws.  The work is FP32/FP64 issue-bound (about 40 flops and 3-5
  * transcendental ops per sample, no memory traffic beyond the result).
+ *
+ * stream = 1 replaces the Philox draws by the OpenCL backend's own stream
+ * (src/xmi_kernels.cl:226-227,393-404): Threefry4x32-20 with key
+ * (r index, 0xdecafbad, 0xfacebead, theta index) and counter
+ * (j, 0xf00dcafe, 0xdeadbeef, 0xbeeff00d) for the j-th pair of samples
+ * (j = 1, 2, ...), each uniform a 32-bit word / 2^32 in single precision.
+ * With it the grid can be checked point by point against the reference
+ * kernel itself; lanes then take sample pairs j = lane + 1, lane + 33, ....
  */
 #ifndef XMIMSIM_GB300_SOLID_ANGLE_CUH
 #define XMIMSIM_GB300_SOLID_ANGLE_CUH
@@ -87,7 +95,7 @@ template <typename R>
 __global__ void __launch_bounds__(256) solid_angle_grid_kernel(SaGeom s, const double *r_vals, int nr,
                                                                 const double *t_vals, long long p0, long long p1,
                                                                 int hits_per_single, unsigned long long seed,
-                                                                double *out) {
+                                                                int stream, double *out) {
   const int lane = threadIdx.x & 31;
   const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
   for (long long p = p0 + (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); p < p1; p += warps) {
@@ -96,7 +104,26 @@ __global__ void __launch_bounds__(256) solid_angle_grid_kernel(SaGeom s, const d
     bool outside;
     int hits = 0;
     bool live = sa_setup<R>(s, (R)r_vals[ir], (R)t_vals[it], cfca, fcsa, st, ct, py, pz, outside);
-    if (live) {
+    if (live && stream == 1) {
+      xmi_u32x4 key, c;
+      key.v[0] = (uint32_t)ir;
+      key.v[1] = 0xdecafbadu;
+      key.v[2] = 0xfacebeadu;
+      key.v[3] = (uint32_t)it;
+      c.v[1] = 0xf00dcafeu;
+      c.v[2] = 0xdeadbeefu;
+      c.v[3] = 0xbeeff00du;
+      const int pairs = (hits_per_single + 1) / 2;
+      for (int j = lane; j < pairs; j += 32) {
+        c.v[0] = (uint32_t)(j + 1);
+        xmi_u32x4 o = xmi_threefry4x32_20(c, key);
+        const float inv = 4294967296.0f;
+        hits += sa_sample<R>(s, cfca, st, ct, py, pz, outside, (R)((float)o.v[0] / inv), (R)((float)o.v[1] / inv));
+        if (2 * j + 1 < hits_per_single)
+          hits += sa_sample<R>(s, cfca, st, ct, py, pz, outside, (R)((float)o.v[2] / inv),
+                               (R)((float)o.v[3] / inv));
+      }
+    } else if (live) {
       for (int i = lane; i < hits_per_single; i += 32) {
         xmi_u32x4 c;
         c.v[0] = (uint32_t)i;

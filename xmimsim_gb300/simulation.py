@@ -139,10 +139,11 @@ def make_options(**kw) -> abi.XmiMainOptions:
 
 
 def gpu_options(precision: int = 0, seed: int = 0, threads_per_block: int = 0, blocks_per_sm: int = 0,
-                use_surrogate: int = 0, surrogate_tolerance: float = 1e-3) -> abi.XmiGpuOptions:
+                use_surrogate: int = 0, surrogate_tolerance: float = 1e-3,
+                solid_angle_stream: int = 0) -> abi.XmiGpuOptions:
     g = abi.XmiGpuOptions()
     abi.load().xmi_gpu_default_options(C.byref(g))
-    g.precision, g.seed = precision, seed
+    g.precision, g.seed, g.solid_angle_stream = precision, seed, solid_angle_stream
     g.threads_per_block, g.blocks_per_sm = threads_per_block, blocks_per_sm
     g.use_surrogate, g.surrogate_tolerance = use_surrogate, surrogate_tolerance
     return g
