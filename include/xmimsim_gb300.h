@@ -102,6 +102,23 @@ void xmi_detector_convolute_all_custom(xmi_inputFPtr inputFPtr, double **channel
                                        xmi_escape_ratios *escape_ratios, int n_interactions_all,
                                        int zero_interaction);
 
+/* Allocation-free detector convolution.  No counterpart in the reference.
+ * For callers that cannot allocate device memory when they convolve (a
+ * real-time acquisition or fitting loop under a device-memory budget fixed up
+ * front, an application whose GPU memory belongs to another allocator): same
+ * result as xmi_detector_convolute_spectrum with use_escape_peaks = 0 and
+ * use_sum_peaks = 0 (channel absorption, Gaussian + tail convolution, optional
+ * Poisson noise), written into the caller's channels_conv[nchannels].
+ * It calls no cudaMalloc/cudaFree: the device scratch is a fixed array of
+ * 3 x 16384 doubles (384 KiB) kept on every GPU that loads the library until
+ * exit.  Returns 0 with an error for nchannels > 16384 or when escape peaks
+ * or pile-up are requested.  The first call on a device looks up the
+ * scratch address for that device; make it before any stream capture.  All
+ * calls share the scratch, which keeps the last call's contents; calls that
+ * overlap on the GPU (concurrent host threads) race. */
+int xmi_detector_convolute_spectrum_noalloc(xmi_inputFPtr inputFPtr, const double *channels_noconv,
+                                            double *channels_conv, xmi_main_options *options);
+
 /* ---- escape ratios (include/xmi_detector.h:55-57) ---- */
 xmi_escape_ratios_options xmi_get_default_escape_ratios_options(void);
 void xmi_escape_ratios_calculation(xmi_input *inputPtr, xmi_escape_ratios **escape_ratios,

@@ -143,6 +143,8 @@ PROTOTYPES = {
                                                  c_double_p, c_double_p, C.POINTER(XmiMainOptions),
                                                  C.POINTER(XmiEscapeRatios), C.c_int, C.c_int]),
     "xmi_detector_convolute_history": (None, [C.c_void_p, c_double_p, C.POINTER(XmiMainOptions)]),
+    "xmi_detector_convolute_spectrum_noalloc": (C.c_int, [C.c_void_p, c_double_p, c_double_p,
+                                                          C.POINTER(XmiMainOptions)]),
     "xmi_get_default_escape_ratios_options": (XmiEscapeRatiosOptions, []),
     "xmi_escape_ratios_calculation": (None, [C.POINTER(XmiInput), C.POINTER(C.POINTER(XmiEscapeRatios)), C.c_char_p,
                                              C.c_char_p, C.POINTER(XmiMainOptions), XmiEscapeRatiosOptions]),

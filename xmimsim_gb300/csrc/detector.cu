@@ -800,3 +800,104 @@ extern "C" void xmi_escape_ratios_calculation(xmi_input *inputPtr, xmi_escape_ra
   if (h) xmi_free_input_F(&h);
   *escape_ratios = er;
 }
+
+/* ---------------------------------------------------------------- */
+/* Allocation-free detector convolution                               */
+/* ---------------------------------------------------------------- */
+/* Some callers cannot call cudaMalloc at the point where they need a
+ * spectrum convolved: a real-time acquisition or spectrum-fitting loop that
+ * runs under a fixed device-memory budget set up front, a host application
+ * whose GPU memory is owned by another allocator (a framework's caching
+ * allocator, a pool shared with other work) and must not be fragmented or
+ * competed with, or code that must not block on the driver's allocator.
+ * For them the convolution below uses a fixed scratch area that lives as long
+ * as the library is loaded: XMI_NOALLOC_MAX_CHANNELS channels, three buffers
+ * of doubles (384 KiB on every GPU that loads the library, until exit). */
+#define XMI_NOALLOC_MAX_CHANNELS 16384
+
+static __device__ __align__(256) double xmi_noalloc_scratch[3 * XMI_NOALLOC_MAX_CHANNELS];
+
+namespace {
+/* device address of the scratch array per device, looked up once per device
+ * with that device current; the host-side symbol is only a stand-in */
+double *g_noalloc_ptr[64];
+
+double *noalloc_scratch_for_current_device() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+    xmi_set_error("xmi_detector_convolute_spectrum_noalloc: no current CUDA device");
+    return nullptr;
+  }
+  if (!g_noalloc_ptr[dev]) {
+    double *p = nullptr;
+    cudaError_t rc = cudaGetSymbolAddress((void **)&p, xmi_noalloc_scratch);
+    if (rc != cudaSuccess || !p) {
+      xmi_set_error("xmi_detector_convolute_spectrum_noalloc: cudaGetSymbolAddress failed: %s",
+                    cudaGetErrorString(rc));
+      return nullptr;
+    }
+    g_noalloc_ptr[dev] = p;
+  }
+  return g_noalloc_ptr[dev];
+}
+
+/* host staging of the absorption-corrected input, per calling thread */
+thread_local double g_noalloc_stage[XMI_NOALLOC_MAX_CHANNELS];
+}  // namespace
+
+extern "C" int xmi_detector_convolute_spectrum_noalloc(xmi_inputFPtr inputFPtr, const double *channels_noconv,
+                                                      double *channels_conv, xmi_main_options *options) {
+  if (!inputFPtr || !channels_noconv || !channels_conv || !options) {
+    xmi_set_error("xmi_detector_convolute_spectrum_noalloc: NULL argument");
+    return 0;
+  }
+  const xmi_input *in = inputFPtr->input;
+  const xmi_detector *det = in->detector;
+  const int nch = det->nchannels;
+  if (nch < 1 || nch > XMI_NOALLOC_MAX_CHANNELS) {
+    xmi_set_error("xmi_detector_convolute_spectrum_noalloc: %d channels exceed the fixed scratch of %d channels",
+                  nch, XMI_NOALLOC_MAX_CHANNELS);
+    return 0;
+  }
+  if (options->use_escape_peaks == 1 || options->use_sum_peaks == 1) {
+    xmi_set_error("xmi_detector_convolute_spectrum_noalloc: escape peaks and pile-up need per-call device tables; "
+                  "use xmi_detector_convolute_spectrum");
+    return 0;
+  }
+  double *scratch = noalloc_scratch_for_current_device();
+  if (!scratch) return 0;
+  /* detector window / crystal absorption per channel, src/xmi_detector_f.F90:437-454 */
+  for (int i = 0; i < nch; i++) {
+    double E = i * det->gain + det->zero, dc = 1.0;
+    for (int j = 0; j < in->absorbers->n_det_layers; j++) {
+      const xmi_layer *l = &in->absorbers->det_layers[j];
+      dc = dc * exp(-1.0 * l->density * l->thickness * xmi_layer_mu(l, E));
+    }
+    for (int j = 0; j < det->n_crystal_layers; j++) {
+      const xmi_layer *l = &det->crystal_layers[j];
+      dc = -1.0 * dc * expm1(-1.0 * l->density * l->thickness * xmi_layer_mu(l, E));
+    }
+    g_noalloc_stage[i] = channels_noconv[i] * dc;
+  }
+  double *d_in = scratch, *d_norm = scratch + XMI_NOALLOC_MAX_CHANNELS, *d_out = scratch + 2 * XMI_NOALLOC_MAX_CHANNELS;
+  if (!ck(cudaMemcpy(d_in, g_noalloc_stage, sizeof(double) * nch, cudaMemcpyHostToDevice), "noalloc copy in"))
+    return 0;
+  ConvParams p;
+  p.nch = nch;
+  p.det_type = (int)det->detector_type;
+  p.gain = det->gain;
+  p.zero = det->zero;
+  p.a = det->noise * det->noise;
+  p.b = (double)((float)(2.3548f * 2.3548f) * 3.85f) * det->fano / 1000.0;
+  p.c = sqrt(2.0) / (2.0 * sqrt(2.0 * log(2.0)));
+  const int T = 128, B = (nch + T - 1) / T;
+  conv_norm_kernel<<<B, T>>>(p, d_norm);
+  conv_gather_kernel<<<B, T>>>(p, d_in, d_norm, d_out);
+  if (!ck(cudaGetLastError(), "noalloc convolution")) return 0;
+  if (options->use_poisson == 1) {
+    poisson_kernel<<<B, T>>>(nch, seed_for(inputFPtr, options, 0x9015ull), d_out);
+    if (!ck(cudaGetLastError(), "noalloc poisson")) return 0;
+  }
+  return ck(cudaMemcpy(channels_conv, d_out, sizeof(double) * nch, cudaMemcpyDeviceToHost), "noalloc copy out") ? 1
+                                                                                                                : 0;
+}
