@@ -108,13 +108,6 @@ def workload_spec(photons: int):
     return configs.config2(total_photons=int(photons)), dict(configs.C2_OPTIONS, use_sum_peaks=0)
 
 
-def bytes_per_history(spec_options, precision: str) -> tuple[float, float]:
-    """Algorithmic table bytes per history, counted by the instrumented oracle
-    on a small sample of the same workload; returns (bytes, cpu_seconds)."""
-    from oracle import oracle_api
-    return 0.0, 0.0
-
-
 def run_cpu_sample(spec, options, n_sample: int, threads: int):
     """Times the FP64 CPU restatement (all threads) on a bounded sample of the
     workload; returns (histories/s, histories, seconds, words/history)."""
@@ -131,15 +124,15 @@ def run_cpu_sample(spec, options, n_sample: int, threads: int):
     g = oracle_api.solid_angle_points(sim.bundle_ptr(), r, t, 0, 64 * 64, 500).reshape(64, 64)
     sim.set_solid_angle(r, t, g)
     sim.prepare()
-    oracle_api.words_counted()
+    oracle_api.words_counted_split()
     t0 = time.perf_counter()
     oracle_api.msim(sim.bundle_ptr(), spec.n_interactions_trajectory, spec.nchannels, threads=threads,
                     max_photons_per_item=per_item)
     dt = time.perf_counter() - t0
-    words = oracle_api.words_counted()
+    words, words_est = oracle_api.words_counted_split()
     n = per_item * n_items
     sim.close()
-    return n / dt, n, dt, words / n
+    return n / dt, n, dt, (words - words_est) / n, words_est / n
 
 
 def reference_arm(args):
@@ -151,7 +144,7 @@ def reference_arm(args):
     threads = os.cpu_count() or 1
     vals = []
     for i in range(args.warmup + args.steps):
-        v, n, dt, _ = run_cpu_sample(spec, options, args.cpu_sample, threads)
+        v, n, dt, _, _ = run_cpu_sample(spec, options, args.cpu_sample, threads)
         if i >= args.warmup:
             vals.append((v, n, dt))
     value = statistics.median(v for v, _, _ in vals)
@@ -215,13 +208,14 @@ def main():
         dist.barrier()
     if cudart is not None:
         cudart.cudaDeviceSynchronize()
-    kernel_ms, launches = [], 0
+    kernel_ms, launches, phases = [], 0, []
     with ClockSampler(local) as clocks:
         t0 = time.perf_counter()
         for _ in range(args.steps):
             out, tm = step()
             kernel_ms.append(tm["kernel_ms"])
             launches += tm["launches"]
+            phases.append(tm)
         if cudart is not None:
             cudart.cudaDeviceSynchronize()
         wall = time.perf_counter() - t0
@@ -252,6 +246,9 @@ def main():
                        "l2": "inputs larger than L2 (angular tables of all elements exceed 129 MB)",
                        "solid_angle_grid_s": t_setup},
             "gpu_launches": launches,
+            "phases_ms_per_step": {k: statistics.mean(p[k + "_ms"] for p in phases)
+                                   for k in ("transport", "sort", "estimator")},
+            "events_per_step": statistics.mean(p["events"] for p in phases),
             "e2e": {"value": e2e, "unit": "histories/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "clocks": clocks.summary()}
     # host<->device bytes of one public call: source items in, tallies out
@@ -260,21 +257,27 @@ def main():
     nslots = 0
     line["e2e"]["d2h_bytes_per_step"] = int(8 * (spec.n_interactions_trajectory + 1) * spec.nchannels)
     if not args.no_cpu_baseline:
-        cv, cn, cdt, words = run_cpu_sample(spec, options, args.cpu_sample, os.cpu_count() or 1)
+        cv, cn, cdt, words_tr, words_est = run_cpu_sample(spec, options, args.cpu_sample, os.cpu_count() or 1)
         line["cpu_baseline"] = {"value": cv, "unit": "histories/s", "cores": os.cpu_count(), "kind": "port",
                                 "sample": "%d photons (%.2f s) of the same workload" % (cn, cdt)}
+        # dominant kernel: algorithmic table bytes it reads per history (counted
+        # by the instrumented oracle on the sample) over its device time
         word = 8 if precision == 0 else 4
-        bph = words * word
+        ph = line["phases_ms_per_step"]
+        kern = "estimator_kernel" if ph["estimator"] >= ph["transport"] else "transport_kernel"
+        kms = ph["estimator"] if kern == "estimator_kernel" else ph["transport"]
+        bph = (words_est if kern == "estimator_kernel" else words_tr) * word
         peaks = {}
         try:
             peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
         except Exception:
             pass
         peak = peaks.get("hbm_gbs", 6800.0)
-        achieved = bph * value / 1e9
-        line["roofline"] = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+        achieved = bph * n_hist / (kms / 1e3) / 1e9 if kms > 0 else 0.0
+        line["roofline"] = {"bound": "hbm", "kernel": kern, "achieved": achieved, "peak": peak, "unit": "GB/s",
                             "frac": achieved / peak, "traffic": None,
-                            "bytes_per_history": bph, "peak_source": "measured" if peaks else "fallback"}
+                            "algorithmic_bytes_per_history": bph,
+                            "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if peaks else "fallback 6.8 TB/s"}
     print(json.dumps(line))
     sim.close()
     if ws > 1:

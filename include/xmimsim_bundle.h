@@ -175,6 +175,18 @@ typedef struct {
 
   /* tally layout */
   int n_slots;           /* n_lines + 2*n_elem: Rayleigh at n_lines+2e, Compton +1 */
+
+  /* ---- estimator line lists ----
+   * Per (layer, element) pair, the line slots the variance-reduction
+   * estimator visits (src/xmi_variance_reduction.F90:575-709): energy >= 1 keV,
+   * line <= line_last, not L1L2/L1L3/L2L3, FluorYield x RadRate > 0.
+   * Entries of pair k: [ent_off[k], ent_off[k+1]). */
+  int n_ent;
+  int *ent_off;          /* [n_layer_el+1] */
+  int *ent_slot;         /* [n_ent] line slot */
+  int *ent_shell;        /* [n_ent] 0..8 */
+  double *ent_coef;      /* [n_ent] FluorYield(Z, shell) x RadRate(Z, line) */
+  double *ent_pmu;       /* [n_ent][XMI_MAXL] precalc_mu of every layer at the line energy (0 beyond n_layers) */
 } xmi_bundle;
 
 /* Evaluation rule of every energy table of the bundle: E is located in the

@@ -142,6 +142,10 @@ int xmi_gpu_prepare_run(xmi_inputFPtr inputFPtr, xmi_hdf5FPtr hdf5FPtr,
 int xmi_gpu_set_replica(xmi_hdf5FPtr hdf5FPtr, int replica, int n_replicas);
 /* device time (ms, CUDA events) and kernel launches of the last call */
 int xmi_gpu_last_timing(double *transport_ms, double *total_ms, int *launches);
+/* device time of the phases of the last xmi_main_msim (transport kernel,
+ * sort of the estimator events, estimator kernel) and the number of
+ * estimator events */
+int xmi_gpu_last_phases(double *transport_kernel_ms, double *sort_ms, double *estimator_ms, long long *events);
 
 #ifdef __cplusplus
 }

@@ -37,7 +37,7 @@ def load() -> C.CDLL:
         _lib.oracle_poly_solve_quadratic.restype = C.c_int
         _lib.oracle_poly_solve_quadratic.argtypes = [C.c_double, C.c_double, C.c_double, dp, dp]
         _lib.oracle_words_counted.restype = C.c_longlong
-        _lib.oracle_words_counted.argtypes = []
+        _lib.oracle_words_counted.argtypes = [C.POINTER(C.c_longlong)]
         _lib.oracle_philox_block.restype = None
         _lib.oracle_philox_block.argtypes = [C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]
         _lib.oracle_solid_angle_points_cl_stream.restype = None
@@ -73,7 +73,14 @@ def msim(bundle_ptr: int, n_interactions: int, nchannels: int, n_mpi_hosts: int 
 
 def words_counted() -> int:
     """Algorithmic table words read by the oracle since the previous call."""
-    return int(load().oracle_words_counted())
+    return int(load().oracle_words_counted(None))
+
+
+def words_counted_split() -> tuple[int, int]:
+    """(all words, words of the estimator's element and line loops) since the previous call."""
+    est = C.c_longlong(0)
+    total = int(load().oracle_words_counted(C.byref(est)))
+    return total, int(est.value)
 
 
 def solid_angle_points(bundle_ptr: int, r_vals: np.ndarray, t_vals: np.ndarray, p0: int, p1: int,

@@ -49,8 +49,8 @@ static const double O_MEC2 = 9.10938188e-31 * 2.99792458e8 * 2.99792458e8 / 1.60
 
 /* algorithmic table words read per lookup (interpolation corners counted
  * once), accumulated per thread to define the roofline bytes per history */
-static __thread long long o_words = 0;
-static long long o_words_total = 0;
+static __thread long long o_words = 0, o_words_est = 0;
+static long long o_words_total = 0, o_words_est_total = 0;
 
 typedef struct {
   double coords[3], dirv[3], elecv[3];
@@ -497,12 +497,20 @@ static int check_photon_detector_hit(const xmi_bundle *b, const ophoton *p) {
 /* ------------------------------------------------------------------ */
 /* variance reduction, src/xmi_variance_reduction.F90:29-726            */
 /* ------------------------------------------------------------------ */
-static void variance_reduction(const xmi_bundle *b, ophoton *p, orng *g, otally *t) {
+/* The estimator's draws come from streams of their own (engine convention):
+ * (photon, 0x40000000 | n << 8 | 0xFF) for the point on the detector and
+ * (photon, 0x40000000 | n << 8 | i) for the Compton energy of the i-th element
+ * of the layer; the reference draws them from the photon's single stream. */
+static uint32_t vr_stream(int n, int sub) { return 0x40000000u | ((uint32_t)n << 8) | (uint32_t)sub; }
+
+static void variance_reduction(const xmi_bundle *b, ophoton *p, otally *t) {
+  orng gp, *g = &gp;
   double radius, theta, dp[3], lcp[3], dirv[3], lcd[3], tmp[3], total_distance, ndc[3];
   double dotprod, phi, proj[3], en[3], distances[XMI_MAXL], tc[3], murhod, pesc_rayl, omega, pdir_fluo;
   int step_max, step_dir, i, k, n = p->n_int, layer = p->cur_layer, err = 0, node;
   double f;
   if (p->energy <= O_ENERGY_THRESHOLD) return;
+  orng_init(g, b->seed, (uint64_t)p->id, vr_stream(n, 0xFF));
   radius = sqrt(orng_uniform(g)) * b->det_radius;
   theta = 2.0 * M_PI * orng_uniform(g);
   dp[0] = 0.0;
@@ -564,6 +572,7 @@ static void variance_reduction(const xmi_bundle *b, ophoton *p, orng *g, otally 
   pdir_fluo = omega / 4.0 / M_PI;
 
   xmi_grid_locate(b, p->energy, &node, &f);
+  const long long words_before = o_words;
   for (i = 0; i < b->layer_nel[layer]; i++) {
     int pair = b->layer_off[layer] + i, e = b->layer_el[pair], Z = b->elem_Z[e], s, sl;
     double w = b->layer_w[pair], pconv, pdir, tw, P[9], mus_c[XMI_MAXL], ec, pesc;
@@ -574,6 +583,7 @@ static void variance_reduction(const xmi_bundle *b, ophoton *p, orng *g, otally 
     t->var_red[hidx(b, Z, 384, n)] += tw;
     tally_channel(b, t, n, p->energy, tw);
     /* Compton (N_COMPTON_VARRED = 1), xmi_compton_varred2 */
+    orng_init(g, b->seed, (uint64_t)p->id, vr_stream(n, i));
     ec = compton_energy(b, e, p->energy, theta, g, 1, &err);
     if (err) { t->error = 6; return; }
     mu_calc(b, ec, mus_c);
@@ -620,6 +630,7 @@ static void variance_reduction(const xmi_bundle *b, ophoton *p, orng *g, otally 
       tally_channel(b, t, n, efl, tw);
     }
   }
+  o_words_est += o_words - words_before;
 }
 
 /* ------------------------------------------------------------------ */
@@ -899,7 +910,7 @@ static int simulate_photon(const xmi_bundle *b, ophoton *p, otally *t) {
     if (p->n_int == b->n_interactions) break;
     p->n_int = p->n_int + 1;
     if (b->use_vr == 1) {
-      variance_reduction(b, p, &g, t);
+      variance_reduction(b, p, t);
       if (t->error) return 0;
     }
     /* atom selection, src/xmi_main.F90:1556-1572 */
@@ -1152,7 +1163,9 @@ int oracle_xmi_main_msim(const xmi_bundle *b, int n_mpi_hosts, int nthreads, int
       *not_found += t.not_found;
       if (t.error) ok = 0;
       o_words_total += o_words;
+      o_words_est_total += o_words_est;
       o_words = 0;
+      o_words_est = 0;
     }
     free(t.channels);
     free(t.brute);
@@ -1166,10 +1179,13 @@ int oracle_xmi_main_msim(const xmi_bundle *b, int n_mpi_hosts, int nthreads, int
   return ok;
 }
 
-/* table words read since the last call (all threads) */
-long long oracle_words_counted(void) {
+/* table words read since the last call (all threads); *estimator receives
+ * the part read by the estimator's element and line loops */
+long long oracle_words_counted(long long *estimator) {
   long long w = o_words_total;
+  if (estimator) *estimator = o_words_est_total;
   o_words_total = 0;
+  o_words_est_total = 0;
   return w;
 }
 

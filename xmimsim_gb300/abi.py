@@ -153,6 +153,7 @@ PROTOTYPES = {
     "xmi_gpu_prepare_run": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(XmiMainOptions), C.c_int,
                                       C.POINTER(XmiSolidAngle)]),
     "xmi_gpu_last_timing": (C.c_int, [c_double_p, c_double_p, c_int_p]),
+    "xmi_gpu_last_phases": (C.c_int, [c_double_p, c_double_p, c_double_p, C.POINTER(C.c_longlong)]),
     "xmi_gpu_set_replica": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
 }
 

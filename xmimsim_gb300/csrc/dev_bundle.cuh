@@ -41,7 +41,7 @@ struct DevBundle {
   const int *line_index, *line_shell;
   const R *line_energy, *line_rate;
   const R *precalc_mu, *precalc_xrf;
-  const double *seg_lo, *seg_lnlo, *seg_invh;
+  const R *seg_lo, *seg_lnlo, *seg_invh;
   const int *seg_off, *seg_n;
   const R *el_tab, *mu_tab, *exc_tab;
   const R *icdf_e, *icdf_r, *rayl_icdf, *compt_icdf, *phi_t, *phi_icdf, *dop_r, *dop_icdf, *ff2, *sf;
@@ -49,6 +49,10 @@ struct DevBundle {
   const long long *item_first; /* [n_items] global id of the first photon */
   const double *sa_r, *sa_t;
   const R *sa_grid;
+  /* estimator line lists per (layer, element) pair */
+  int n_ent;
+  const int *ent_off, *ent_slot, *ent_shell;
+  const R *ent_coef, *ent_pmu;
 };
 
 /* Tally buffers of one run (device pointers). */

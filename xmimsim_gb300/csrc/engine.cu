@@ -11,6 +11,7 @@
 #include <cstring>
 #include <vector>
 
+#include "estimator.cuh"
 #include "solid_angle.cuh"
 #include "transport.cuh"
 #include "xmi_internal.h"
@@ -22,6 +23,9 @@ namespace {
 struct Timing {
   double transport_ms = 0.0, total_ms = 0.0;
   int launches = 0;
+  /* phases of the last xmi_main_msim: transport kernel, event sort, estimator kernel */
+  double phase_ms[3] = {0.0, 0.0, 0.0};
+  long long events = 0;
 };
 thread_local Timing g_timing;
 
@@ -62,6 +66,13 @@ struct DevState {
   unsigned long long *counters = nullptr;
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  /* estimator event queue of one chunk */
+  void *q_events = nullptr;
+  int *q_key = nullptr, *q_order = nullptr;
+  unsigned *q_hist = nullptr; /* [2][XMI_MAXL * XMI_MAXN]: counts, cursors */
+  unsigned long long *q_count = nullptr;
+  size_t q_bytes = 0;
+  long long q_cap = 0;
 };
 
 template <typename R>
@@ -113,6 +124,7 @@ void fill_scalars(const xmi_bundle &h, xmi::DevBundle<R> &d) {
   d.n_seg = h.n_seg;
   d.n_items = h.n_items;
   d.n_layer_el = h.n_layer_el;
+  d.n_ent = h.n_ent;
   d.coll_present = h.coll_present;
   d.seed = h.seed;
   d.n_photons_total = h.n_photons_total;
@@ -163,9 +175,9 @@ bool upload_tables(const xmi_bundle &h, DevSide &s, xmi::DevBundle<R> &d) {
   d.line_rate = upload<R>(s, h.line_rate, NL);
   d.precalc_mu = upload<R>(s, h.precalc_mu, (size_t)h.n_layers * NL);
   d.precalc_xrf = upload<R>(s, h.precalc_xrf, E * 9 * NL);
-  d.seg_lo = upload_d(s, h.seg_lo, h.n_seg + 1);
-  d.seg_lnlo = upload_d(s, h.seg_lnlo, h.n_seg);
-  d.seg_invh = upload_d(s, h.seg_invh, h.n_seg);
+  d.seg_lo = upload<R>(s, h.seg_lo, h.n_seg + 1);
+  d.seg_lnlo = upload<R>(s, h.seg_lnlo, h.n_seg);
+  d.seg_invh = upload<R>(s, h.seg_invh, h.n_seg);
   d.seg_off = upload_int(s, h.seg_off, h.n_seg);
   d.seg_n = upload_int(s, h.seg_n, h.n_seg);
   d.el_tab = upload<R>(s, h.el_tab, E * h.n_nodes * XMI_EL_REC);
@@ -181,7 +193,12 @@ bool upload_tables(const xmi_bundle &h, DevSide &s, xmi::DevBundle<R> &d) {
   d.dop_icdf = upload<R>(s, h.doppler_icdf, E * XMI_DOPPLER_N);
   d.ff2 = upload<R>(s, h.ff2, E * XMI_NQ);
   d.sf = upload<R>(s, h.sf, E * XMI_NQ);
-  if (cudaGetLastError() != cudaSuccess || !d.sf) {
+  d.ent_off = upload_int(s, h.ent_off, (size_t)h.n_layer_el + 1);
+  d.ent_slot = upload_int(s, h.ent_slot, h.n_ent);
+  d.ent_shell = upload_int(s, h.ent_shell, h.n_ent);
+  d.ent_coef = upload<R>(s, h.ent_coef, h.n_ent);
+  d.ent_pmu = upload<R>(s, h.ent_pmu, (size_t)h.n_ent * XMI_MAXL);
+  if (cudaGetLastError() != cudaSuccess || !d.sf || !d.ent_pmu) {
     xmi_set_error("device table upload failed");
     s.release();
     return false;
@@ -255,6 +272,11 @@ void xmi_dev_free_tables(struct xmi_tables_handle *t) {
   cudaFree(s->sa_g32);
   cudaFree(s->tally);
   cudaFree(s->counters);
+  cudaFree(s->q_events);
+  cudaFree(s->q_key);
+  cudaFree(s->q_order);
+  cudaFree(s->q_hist);
+  cudaFree(s->q_count);
   if (s->ev0) cudaEventDestroy(s->ev0);
   if (s->ev1) cudaEventDestroy(s->ev1);
   if (s->stream) cudaStreamDestroy(s->stream);
@@ -282,6 +304,14 @@ int xmi_gpu_last_timing(double *transport_ms, double *total_ms, int *launches) {
   if (transport_ms) *transport_ms = g_timing.transport_ms;
   if (total_ms) *total_ms = g_timing.total_ms;
   if (launches) *launches = g_timing.launches;
+  return 1;
+}
+
+int xmi_gpu_last_phases(double *transport_kernel_ms, double *sort_ms, double *estimator_ms, long long *events) {
+  if (transport_kernel_ms) *transport_kernel_ms = g_timing.phase_ms[0];
+  if (sort_ms) *sort_ms = g_timing.phase_ms[1];
+  if (estimator_ms) *estimator_ms = g_timing.phase_ms[2];
+  if (events) *events = g_timing.events;
   return 1;
 }
 
@@ -437,6 +467,37 @@ int xmi_gpu_prepare_run(xmi_inputFPtr in, xmi_hdf5FPtr t, xmi_main_options *opti
 
 }  // extern "C"
 
+/* events held on the device per chunk; a chunk is as many photons as can
+ * each make N estimator events (one per interaction) within it */
+constexpr long long kMaxQueuedEvents = 1ll << 25;
+
+template <typename R>
+static bool ensure_queue(DevState *s, long long cap) {
+  const size_t bytes = (size_t)cap * sizeof(xmi::VrEvent<R>);
+  if (bytes <= s->q_bytes && cap <= s->q_cap) return true;
+  cudaFree(s->q_events);
+  cudaFree(s->q_key);
+  cudaFree(s->q_order);
+  s->q_events = nullptr;
+  s->q_key = s->q_order = nullptr;
+  s->q_bytes = 0;
+  s->q_cap = 0;
+  if (!cuda_ok(cudaMalloc(&s->q_events, bytes), "cudaMalloc event queue") ||
+      !cuda_ok(cudaMalloc(&s->q_key, sizeof(int) * cap), "cudaMalloc event keys") ||
+      !cuda_ok(cudaMalloc(&s->q_order, sizeof(int) * cap), "cudaMalloc event order"))
+    return false;
+  if (!s->q_hist && !cuda_ok(cudaMalloc(&s->q_hist, 2 * sizeof(unsigned) * XMI_MAXL * XMI_MAXN), "cudaMalloc"))
+    return false;
+  if (!s->q_count && !cuda_ok(cudaMalloc(&s->q_count, sizeof(unsigned long long)), "cudaMalloc")) return false;
+  s->q_bytes = bytes;
+  s->q_cap = cap;
+  return true;
+}
+
+/* Runs the photons of the bundle's source items: per chunk, the transport
+ * kernel (events into the queue), the counting sort of the events by
+ * (layer, order) and the estimator kernel.  All launches go to the handle's
+ * stream; CUDA events around each phase give the device times. */
 template <typename R>
 static bool launch_transport(DevState *s, xmi::DevBundle<R> &d, const xmi_bundle &h, int threads, int blocks_per_sm,
                              double *ms) {
@@ -472,23 +533,88 @@ static bool launch_transport(DevState *s, xmi::DevBundle<R> &d, const xmi_bundle
   if (sizeof(R) == 8) d.sa_grid = (const R *)s->sa_g64;
   else d.sa_grid = (const R *)s->sa_g32;
 
+  const long long n = h.n_photons_total;
+  const int N = h.n_interactions, nkeys = h.n_layers * N;
+  const int sms = num_sms();
+  long long chunk = n > 0 ? n : 1;
+  xmi::VrQueue<R> vq{nullptr, nullptr, nullptr, 0};
+  if (h.use_vr) {
+    chunk = kMaxQueuedEvents / N;
+    if (chunk > n) chunk = n;
+    if (chunk < 1) chunk = 1;
+    if (!ensure_queue<R>(s, chunk * N)) return false;
+    vq.ev = (xmi::VrEvent<R> *)s->q_events;
+    vq.key = s->q_key;
+    vq.count = s->q_count;
+    vq.cap = chunk * N;
+  }
+  /* estimator: per-CTA shared-memory histories when they fit */
   size_t smem = nh * sizeof(double);
-  int use_smem = (h.use_vr && smem <= 160 * 1024) ? 1 : 0;
+  int use_smem = (h.use_vr && smem <= 200 * 1024) ? 1 : 0;
   if (use_smem && smem > 48 * 1024)
-    cudaFuncSetAttribute(xmi::transport_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(xmi::estimator_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (!use_smem) smem = 0;
-  int blocks = num_sms() * blocks_per_sm;
-  long long n = h.n_photons_total;
-  if ((long long)blocks * threads > n) blocks = (int)((n + threads - 1) / threads);
-  if (blocks < 1) blocks = 1;
-  cudaEventRecord(s->ev0, s->stream);
-  if (n > 0) xmi::transport_kernel<R><<<blocks, threads, smem, s->stream>>>(d, tl, 0, n, use_smem);
-  cudaEventRecord(s->ev1, s->stream);
-  if (!cuda_ok(cudaGetLastError(), "transport_kernel launch")) return false;
-  if (!cuda_ok(cudaEventSynchronize(s->ev1), "transport_kernel")) return false;
-  float f = 0.f;
-  cudaEventElapsedTime(&f, s->ev0, s->ev1);
-  *ms = f;
+  int est_per_sm = 1;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&est_per_sm, xmi::estimator_kernel<R>, 256, smem);
+  if (est_per_sm < 1) est_per_sm = 1;
+  const int est_blocks = sms * est_per_sm;
+
+  std::vector<cudaEvent_t> marks;
+  auto mark = [&]() {
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    cudaEventRecord(e, s->stream);
+    marks.push_back(e);
+  };
+  int launches = 0;
+  mark();
+  for (long long w0 = 0; w0 < n; w0 += chunk) {
+    const long long w1 = w0 + chunk < n ? w0 + chunk : n;
+    long long blocks = (long long)sms * blocks_per_sm;
+    if (blocks * threads > w1 - w0) blocks = (w1 - w0 + threads - 1) / threads;
+    if (blocks < 1) blocks = 1;
+    if (h.use_vr) {
+      cudaMemsetAsync(s->q_count, 0, sizeof(unsigned long long), s->stream);
+      cudaMemsetAsync(s->q_hist, 0, sizeof(unsigned) * XMI_MAXL * XMI_MAXN, s->stream);
+    }
+    xmi::transport_kernel<R><<<(int)blocks, threads, 0, s->stream>>>(d, tl, vq, w0, w1);
+    launches++;
+    mark();
+    if (h.use_vr) {
+      /* positions of events whose key the sort would skip stay -1 and are refused by the estimator */
+      cudaMemsetAsync(s->q_order, 0xff, sizeof(int) * (w1 - w0) * N, s->stream);
+      xmi::event_key_histogram<<<sms * 2, 256, 0, s->stream>>>(s->q_key, s->q_count, vq.cap, nkeys, s->q_hist);
+      xmi::event_key_scan<<<1, 32, 0, s->stream>>>(s->q_hist, nkeys, s->q_hist + XMI_MAXL * XMI_MAXN, s->q_count,
+                                                   &s->counters[3]);
+      xmi::event_key_scatter<<<sms * 4, 256, 0, s->stream>>>(s->q_key, s->q_count, vq.cap, nkeys,
+                                                              s->q_hist + XMI_MAXL * XMI_MAXN, s->q_order);
+      mark();
+      xmi::estimator_kernel<R><<<est_blocks, 256, smem, s->stream>>>(d, tl, vq.ev, s->q_order, s->q_count, vq.cap,
+                                                                     use_smem);
+      mark();
+      launches += 4;
+    }
+    if (!cuda_ok(cudaGetLastError(), "transport launch")) break;
+  }
+  bool ok = cuda_ok(cudaGetLastError(), "transport launch") &&
+            cuda_ok(cudaEventSynchronize(marks.back()), "transport_kernel");
+  double phase[3] = {0.0, 0.0, 0.0};
+  float total = 0.f;
+  if (ok) {
+    cudaEventElapsedTime(&total, marks.front(), marks.back());
+    const size_t per = h.use_vr ? 3 : 1;
+    for (size_t i = 0; i + per < marks.size(); i += per)
+      for (size_t k = 0; k < per; k++) {
+        float f = 0.f;
+        cudaEventElapsedTime(&f, marks[i + k], marks[i + k + 1]);
+        phase[k] += f;
+      }
+  }
+  for (cudaEvent_t e : marks) cudaEventDestroy(e);
+  if (!ok) return false;
+  *ms = total;
+  g_timing.launches = launches;
+  for (int k = 0; k < 3; k++) g_timing.phase_ms[k] = phase[k];
   return true;
 }
 
@@ -604,7 +730,7 @@ extern "C" int xmi_main_msim(xmi_inputFPtr in, xmi_hdf5FPtr t, int n_mpi_hosts, 
   cudaEventDestroy(all1);
   g_timing.transport_ms = ms;
   g_timing.total_ms = tot;
-  g_timing.launches = 1;
+  g_timing.events = (long long)counters[3];
   *channels_out = channels;
   *brute_out = brute;
   *var_red_out = var_red;

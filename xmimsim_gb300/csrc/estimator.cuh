@@ -1,0 +1,227 @@
+/*
+ * Point-detector estimator kernel (src/xmi_variance_reduction.F90:29-726,
+ * the element and line loops 300-709, and xmi_compton_varred2 949-1101).
+ *
+ * Input: the VrEvents of a chunk of photons, in an order sorted by
+ * (layer, interaction order).  One lane evaluates one event; the 32 events of
+ * a warp then share the layer and the order almost always, so every lane
+ * walks the same element list and the same line list in lockstep: table
+ * loads of a line are warp-uniform (one transaction, broadcast), nothing
+ * diverges except the Compton rejection loop, and the 32 contributions to a
+ * history slot are summed across the warp before one shared-memory FP64 add.
+ * Warps whose events mix keys (at most one per key boundary) run the same
+ * code per lane with per-lane atomics.
+ *
+ * Per (event, line): 8 FMA for the escape path, one exp, a handful of
+ * multiplies; per (event, element): two form-factor lookups, one Doppler
+ * Compton energy, one mu(E') over the layers, 9 shell probabilities.
+ */
+#ifndef XMIMSIM_GB300_ESTIMATOR_CUH
+#define XMIMSIM_GB300_ESTIMATOR_CUH
+
+#include "transport.cuh"
+
+namespace xmi {
+
+template <typename R>
+__device__ __forceinline__ R warp_sum_r(R v) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+  return v;
+}
+
+/* adds one contribution per lane to history slot `idx` (the same for every
+ * lane when Uniform) */
+template <typename R, bool Uniform>
+__device__ __forceinline__ void hist_add(double *hist, long long idx, R v) {
+  if (Uniform) {
+    if (__any_sync(0xffffffffu, v != (R)0)) {
+      R s = warp_sum_r(v);
+      if ((threadIdx.x & 31) == 0) atomicAdd(&hist[idx], (double)s);
+    }
+  } else if (v != (R)0) {
+    atomicAdd(&hist[idx], (double)v);
+  }
+}
+
+template <typename R>
+__device__ __forceinline__ void chan_add(const DevBundle<R> &b, const DevTally &t, int n, R E, R w) {
+  if (w == (R)0 || E < (R)kEnergyThreshold) return;
+  const int ch = channel_of(b, E);
+  if (ch >= 0 && ch <= b.nch - 1 && XMI_CHK((long long)n * b.nch + ch, (long long)(b.N + 1) * b.nch, 30))
+    atomicAdd(&t.chan[(size_t)n * b.nch + ch], (double)w);
+}
+
+template <typename R, bool Uniform>
+__device__ void estimate_event(const DevBundle<R> &b, const DevTally &t, double *hist, const VrEvent<R> &ev,
+                               bool valid, bool &ok) {
+  const int layer = ev.layer, n = ev.n;
+  const int nel = b.nel[layer], off = b.off[layer];
+  const long long hbase = (long long)(n - 1) * b.n_slots;
+  const R live = valid ? (R)1 : (R)0;
+  for (int i = 0; i < nel; i++) {
+    const int pair = off + i;
+    const int e = XMI_LDG(b.layer_el, pair, b.n_layer_el, 9);
+    const R wi = XMI_LDG(b.layer_w, pair, b.n_layer_el, 9);
+    const R pconv = wi / ev.mu_here;
+    const int rs = b.n_lines + 2 * e;
+    /* Rayleigh */
+    const R twr = live * (pconv * (ev.pR * qtab(b.ff2 + (size_t)e * XMI_NQ, ev.q)) * ev.pesc_rayl * ev.w);
+    hist_add<R, Uniform>(hist, hbase + rs, twr);
+    if (valid) chan_add(b, t, n, ev.E, twr);
+    /* Compton: one Doppler-broadened energy per element (N_COMPTON_VARRED = 1) */
+    xmi_rng g;
+    xmi_rng_init(&g, b.seed, (uint64_t)ev.id, vr_stream(n, i));
+    bool cok = true;
+    const R ec = compton_energy(b, e, ev.E, ev.theta, &g, true, cok);
+    R twc = (R)0;
+    if (cok) {
+      R mus_c[XMI_MAXL];
+      mu_calc(b, ec, mus_c);
+      R murhod = (R)0;
+#pragma unroll
+      for (int j = 0; j < XMI_MAXL; j++) murhod += mus_c[j] * ev.rd[j];
+      twc = live * (pconv * (ev.pC * qtab(b.sf + (size_t)e * XMI_NQ, ev.q)) * exp(-murhod) * ev.w);
+    } else if (valid) {
+      ok = false;
+    }
+    hist_add<R, Uniform>(hist, hbase + rs + 1, twc);
+    if (valid) chan_add(b, t, n, ec, twc);
+    /* fluorescence: shell probabilities at the photon energy (first order or
+     * after scattering) or at the exciting line's energy (after fluorescence) */
+    R P[XMI_NSHELL];
+    if (ev.h_slot >= 0) {
+#pragma unroll
+      for (int s = 0; s < XMI_NSHELL; s++)
+        P[s] = XMI_LDG(b.precalc_xrf, ((long long)e * XMI_NSHELL + s) * b.n_lines + ev.h_slot,
+                       (long long)b.n_elem * XMI_NSHELL * b.n_lines, 10);
+    } else {
+#pragma unroll
+      for (int s = 0; s < XMI_NSHELL; s++) P[s] = el_val(b, e, XMI_REC_XRF + s, ev.node, ev.f);
+    }
+    if (!b.use_M_lines) {
+#pragma unroll
+      for (int s = 4; s < XMI_NSHELL; s++) P[s] = (R)0;
+    }
+    const R scale = live * wi / ev.mu_here * ev.pdir_fluo * ev.w;
+    const int k0 = XMI_LDG(b.ent_off, pair, b.n_layer_el + 1, 15), k1 = XMI_LDG(b.ent_off, pair + 1, b.n_layer_el + 1, 15);
+    for (int k = k0; k < k1; k++) {
+      const int sl = XMI_LDG(b.ent_slot, k, b.n_ent, 16), sh = XMI_LDG(b.ent_shell, k, b.n_ent, 16);
+      R ps = (R)0;
+#pragma unroll
+      for (int s = 0; s < XMI_NSHELL; s++)
+        if (s == sh) ps = P[s];
+      R murhod = (R)0;
+#pragma unroll
+      for (int j = 0; j < XMI_MAXL; j++)
+        murhod += XMI_LDG(b.ent_pmu, (long long)k * XMI_MAXL + j, (long long)b.n_ent * XMI_MAXL, 17) * ev.rd[j];
+      const R tw = ps * XMI_LDG(b.ent_coef, k, b.n_ent, 16) * scale * exp(-murhod);
+      hist_add<R, Uniform>(hist, hbase + sl, tw);
+    }
+  }
+}
+
+/* number of events the queue holds: the count, capped at the capacity (a
+ * count past the capacity means events were dropped and the run is flagged) */
+__device__ __forceinline__ long long queued_events(const unsigned long long *count, long long cap) {
+  const long long n = (long long)*count;
+  return n < cap ? n : cap;
+}
+
+/* events [0, min(*count, cap)) of the queue, visited in `order` */
+template <typename R>
+__global__ void __launch_bounds__(256) estimator_kernel(DevBundle<R> b, DevTally t, const VrEvent<R> *events,
+                                                        const int *order, const unsigned long long *count,
+                                                        long long cap, int use_smem) {
+  extern __shared__ double s_hist[];
+  const int nh = b.N * b.n_slots;
+  if (use_smem) {
+    for (int i = threadIdx.x; i < nh; i += blockDim.x) s_hist[i] = 0.0;
+    __syncthreads();
+  }
+  double *hist = use_smem ? s_hist : t.hist_vr;
+  const long long n_ev = queued_events(count, cap);
+  const int lane = threadIdx.x & 31;
+  const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+  bool ok = true;
+  for (long long base = warp * 32; base < n_ev; base += nwarps * 32) {
+    const long long k = base + lane;
+    bool valid = k < n_ev;
+    /* lanes past the end carry the warp's first event with zero weight */
+    long long oi = order[valid ? k : base];
+    if (oi < 0 || oi >= n_ev) { oi = 0; valid = false; ok = false; }
+    VrEvent<R> ev = events[oi];
+    if (ev.layer < 0 || ev.layer >= b.n_layers || ev.n < 1 || ev.n > b.N || ev.h_slot >= b.n_lines) {
+      /* never produced by the transport kernel: refuse the event, flag the run */
+      ev.layer = 0;
+      ev.n = 1;
+      ev.h_slot = -1;
+      valid = false;
+      ok = false;
+    }
+    const int key = ev.layer * b.N + ev.n - 1;
+    if (__all_sync(0xffffffffu, key == __shfl_sync(0xffffffffu, key, 0)))
+      estimate_event<R, true>(b, t, hist, ev, valid, ok);
+    else
+      estimate_event<R, false>(b, t, hist, ev, valid, ok);
+  }
+  if (!ok) set_error(t, kErrCompton);
+  if (use_smem) {
+    __syncthreads();
+    for (int i = threadIdx.x; i < nh; i += blockDim.x)
+      if (s_hist[i] != 0.0) atomicAdd(&t.hist_vr[i], s_hist[i]);
+  }
+}
+
+/* counting sort of the chunk's events by key = layer * N + n - 1 */
+__global__ void event_key_histogram(const int *key, const unsigned long long *count, long long cap, int nkeys,
+                                    unsigned *hist) {
+  __shared__ unsigned h[XMI_MAXL * XMI_MAXN];
+  for (int i = threadIdx.x; i < nkeys; i += blockDim.x) h[i] = 0u;
+  __syncthreads();
+  const long long n = queued_events(count, cap);
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const int k = key[i];
+    if (k >= 0 && k < nkeys) atomicAdd(&h[k], 1u);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < nkeys; i += blockDim.x)
+    if (h[i]) atomicAdd(&hist[i], h[i]);
+}
+
+/* exclusive scan of the key counts into the scatter cursors; also adds the
+ * chunk's event count to the run total */
+__global__ void event_key_scan(const unsigned *hist, int nkeys, unsigned *cursor, const unsigned long long *count,
+                               unsigned long long *total) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    unsigned acc = 0;
+    for (int i = 0; i < nkeys; i++) {
+      cursor[i] = acc;
+      acc += hist[i];
+    }
+    *total += *count;
+  }
+}
+
+__global__ void event_key_scatter(const int *key, const unsigned long long *count, long long cap, int nkeys,
+                                  unsigned *cursor, int *order) {
+  const long long n = queued_events(count, cap);
+  const int lane = threadIdx.x & 31;
+  for (long long base = ((long long)blockIdx.x * blockDim.x + threadIdx.x) & ~31ll; base < n;
+       base += (long long)gridDim.x * blockDim.x) {
+    const long long i = base + lane;
+    const int k = i < n ? key[i] : -1;
+    const unsigned peers = __match_any_sync(0xffffffffu, k);
+    if (k >= 0 && k < nkeys) {
+      const int leader = __ffs(peers) - 1;
+      unsigned pos = 0;
+      if (lane == leader) pos = atomicAdd(&cursor[k], (unsigned)__popc(peers));
+      pos = __shfl_sync(peers, pos, leader) + __popc(peers & ((1u << lane) - 1u));
+      if ((long long)pos < n) order[pos] = (int)i;
+    }
+  }
+}
+
+}  // namespace xmi
+#endif

@@ -638,6 +638,7 @@ void xmi_bundle_free(xmi_bundle *b) {
   free(b->seg_n); free(b->el_tab); free(b->mu_tab); free(b->exc_tab); free(b->icdf_energies);
   free(b->icdf_rs); free(b->rayl_icdf); free(b->compt_icdf); free(b->phi_thetas); free(b->phi_icdf);
   free(b->doppler_rs); free(b->doppler_icdf); free(b->ff2); free(b->sf); free(b->items);
+  free(b->ent_off); free(b->ent_slot); free(b->ent_shell); free(b->ent_coef); free(b->ent_pmu);
   memset(b, 0, sizeof(*b));
 }
 
@@ -909,6 +910,42 @@ int xmi_bundle_build(struct xmi_input_handle *in, struct xmi_tables_handle *t,
       for (s = 0; s < 9; s++)
         b->precalc_xrf[((size_t)e * 9 + s) * b->n_lines + i] =
             grid_eval(b, b->el_tab + (size_t)e * b->n_nodes * XMI_EL_REC, XMI_EL_REC, XMI_REC_XRF + s, E);
+  }
+
+  /* estimator line lists per (layer, element) pair */
+  {
+    int k, sl, n = 0;
+    b->ent_off = (int *)malloc(sizeof(int) * (size_t)(b->n_layer_el + 1));
+    for (k = 0; k < b->n_layer_el; k++) {
+      e = b->layer_el[k];
+      b->ent_off[k] = n;
+      for (sl = b->elem_line_off[e]; sl < b->elem_line_off[e + 1]; sl++) {
+        int line = b->line_index[sl];
+        if (line > b->line_last || b->line_energy[sl] < 1.0 || line == 30 || line == 31 || line == 59) continue;
+        if (b->elem_fluor_yield[9 * e + b->line_shell[sl]] * b->line_rate[sl] == 0.0) continue;
+        n++;
+      }
+    }
+    b->ent_off[b->n_layer_el] = n;
+    b->n_ent = n;
+    b->ent_slot = (int *)malloc(sizeof(int) * (size_t)(n > 0 ? n : 1));
+    b->ent_shell = (int *)malloc(sizeof(int) * (size_t)(n > 0 ? n : 1));
+    b->ent_coef = (double *)malloc(sizeof(double) * (size_t)(n > 0 ? n : 1));
+    b->ent_pmu = (double *)calloc((size_t)(n > 0 ? n : 1) * XMI_MAXL, sizeof(double));
+    n = 0;
+    for (k = 0; k < b->n_layer_el; k++) {
+      e = b->layer_el[k];
+      for (sl = b->elem_line_off[e]; sl < b->elem_line_off[e + 1]; sl++) {
+        int line = b->line_index[sl], sh = b->line_shell[sl];
+        if (line > b->line_last || b->line_energy[sl] < 1.0 || line == 30 || line == 31 || line == 59) continue;
+        if (b->elem_fluor_yield[9 * e + sh] * b->line_rate[sl] == 0.0) continue;
+        b->ent_slot[n] = sl;
+        b->ent_shell[n] = sh;
+        b->ent_coef[n] = b->elem_fluor_yield[9 * e + sh] * b->line_rate[sl];
+        for (j = 0; j < b->n_layers; j++) b->ent_pmu[(size_t)n * XMI_MAXL + j] = b->precalc_mu[(size_t)j * b->n_lines + sl];
+        n++;
+      }
+    }
   }
 
   /* angular tables */

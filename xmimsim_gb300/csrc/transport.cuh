@@ -27,7 +27,7 @@
 namespace xmi {
 
 enum : unsigned long long { kErrNone = 0, kErrGeometry = 1, kErrTable = 2, kErrCompton = 3,
-                            kErrSource = 4, kErrLayer = 5 };
+                            kErrSource = 4, kErrLayer = 5, kErrQueue = 6 };
 
 template <typename R>
 struct Photon {
@@ -113,20 +113,20 @@ template <> __device__ __forceinline__ float uni<float>(xmi_rng *g) {
   return u < 1.0f ? u : 0x1.fffffep-1f;
 }
 
-/* energy-grid location, same rule as xmi_grid_locate of the bundle */
+/* energy-grid location, same rule as xmi_grid_locate of the bundle, in the
+ * working precision (the FP32 build keeps the FP64 pipe free) */
 template <typename R>
 __device__ __forceinline__ void locate(const DevBundle<R> &b, R E, int &node, R &f) {
-  double Ed = (double)E;
-  if (Ed <= b.seg_lo[0]) { node = 0; f = (R)0; return; }
-  if (Ed >= b.seg_lo[b.n_seg]) { node = b.n_nodes - 2; f = (R)1; return; }
+  if (E <= __ldg(b.seg_lo)) { node = 0; f = (R)0; return; }
+  if (E >= __ldg(b.seg_lo + b.n_seg)) { node = b.n_nodes - 2; f = (R)1; return; }
   int lo = 0, hi = b.n_seg - 1;
   while (lo < hi) {
     int mid = (lo + hi + 1) >> 1;
-    if (Ed >= b.seg_lo[mid]) lo = mid; else hi = mid - 1;
+    if (E >= __ldg(b.seg_lo + mid)) lo = mid; else hi = mid - 1;
   }
-  R t = (log(E) - (R)b.seg_lnlo[lo]) * (R)b.seg_invh[lo];
+  R t = (log(E) - __ldg(b.seg_lnlo + lo)) * __ldg(b.seg_invh + lo);
   int i = (int)t;
-  int n = b.seg_n[lo];
+  int n = __ldg(b.seg_n + lo);
   if (i < 0) i = 0;
   if (i > n - 2) i = n - 2;
   node = b.seg_off[lo] + i;
@@ -241,21 +241,19 @@ __device__ __forceinline__ void tally_add(double *addr, double v) {
   }
 }
 
+/* channel of energy E: INT((E - zero) / gain), src/xmi_main.F90 (tallies);
+ * evaluated in the working precision */
 template <typename R>
-__device__ __forceinline__ void tally_channel(const DevBundle<R> &b, const DevTally &t, int n, R E, double w) {
-  int ch = -1;
-  if (E >= (R)kEnergyThreshold) ch = (int)(((double)E - b.zero) / b.gain);
-  if (ch >= 0 && ch <= b.nch - 1 && XMI_CHK((long long)n * b.nch + ch, (long long)(b.N + 1) * b.nch, 30))
-    tally_add(&t.chan[(size_t)n * b.nch + ch], w);
+__device__ __forceinline__ int channel_of(const DevBundle<R> &b, R E) {
+  return (int)((E - (R)b.zero) / (R)b.gain);
 }
 
 template <typename R>
-__device__ __forceinline__ void tally_hist(const DevBundle<R> &b, const DevTally &t, double *s_hist, bool use_smem,
-                                           int n, int slot, double w) {
-  const long long idx = (long long)(n - 1) * b.n_slots + slot;
-  if (!XMI_CHK(idx, (long long)b.N * b.n_slots, 31)) return;
-  if (use_smem) tally_add(&s_hist[idx], w);
-  else tally_add(&t.hist_vr[idx], w);
+__device__ __forceinline__ void tally_channel(const DevBundle<R> &b, const DevTally &t, int n, R E, double w) {
+  int ch = -1;
+  if (E >= (R)kEnergyThreshold) ch = channel_of(b, E);
+  if (ch >= 0 && ch <= b.nch - 1 && XMI_CHK((long long)n * b.nch + ch, (long long)(b.N + 1) * b.nch, 30))
+    tally_add(&t.chan[(size_t)n * b.nch + ch], w);
 }
 
 /* ---------------- solid angle ---------------- */
@@ -441,16 +439,52 @@ __device__ R compton_energy(const DevBundle<R> &b, int e, R E, R theta_i, xmi_rn
   return (R)0;
 }
 
-/* ---------------- variance reduction ---------------- */
-/* xmi_variance_reduction (src/xmi_variance_reduction.F90:29-726) */
+/* ---------------- variance reduction: event prologue ---------------- */
+/* The point-detector estimator of one interaction
+ * (src/xmi_variance_reduction.F90:29-726) is split in two.  The transport
+ * kernel evaluates the part that depends on the photon's geometry -- a point
+ * on the detector, the scattering angles toward it, the path through the
+ * layers, the solid angle -- and stores it as one VrEvent; the estimator
+ * kernel later evaluates every element and line of the layer for it.  The
+ * estimator's random draws come from streams of their own,
+ * (photon, 0x40000000 | n << 8 | 0xFF) for the detector point and
+ * (photon, 0x40000000 | n << 8 | i) for the Compton energy of the i-th
+ * element of the layer, so neither part depends on the other's draws. */
 template <typename R>
-__device__ void variance_reduction(const DevBundle<R> &b, Photon<R> &p, xmi_rng *g, const DevTally &t,
-                                   double *s_hist, bool use_smem, bool &ok) {
-  if (p.E <= (R)kEnergyThreshold) return;
-  if (!XMI_CHK(p.layer, b.n_layers, 34)) { ok = false; return; }
+struct __align__(16) VrEvent {
+  R E, w, mu_here;
+  R pR, pC;          /* omega x Thomson factor, omega x Klein-Nishina factor */
+  R q, theta;        /* momentum transfer, scattering angle toward the detector point */
+  R pdir_fluo;       /* omega / 4 pi */
+  R pesc_rayl;       /* escape probability at the photon energy */
+  R f;               /* energy-grid fraction of E */
+  R rd[XMI_MAXL];    /* density x path length toward the detector point, per layer */
+  int node, layer, n, h_slot; /* h_slot >= 0: exciting line of a fluorescence photon */
+  long long id;
+};
+
+template <typename R>
+struct VrQueue {
+  VrEvent<R> *ev;
+  int *key;                   /* layer * N + n - 1 */
+  unsigned long long *count;
+  long long cap;
+};
+
+__device__ __forceinline__ uint32_t vr_stream(int n, int sub) {
+  return 0x40000000u | ((uint32_t)n << 8) | (uint32_t)sub;
+}
+
+template <typename R>
+__device__ bool vr_prologue(const DevBundle<R> &b, const Photon<R> &p, const DevTally &t, VrEvent<R> &ev,
+                            bool &ok) {
+  if (p.E <= (R)kEnergyThreshold) return false;
+  if (!XMI_CHK(p.layer, b.n_layers, 34)) { ok = false; return false; }
   const int n = p.n_int, layer = p.layer;
-  R radius = sqrt(uni<R>(g)) * (R)b.det_radius;
-  R ang = (R)(2.0 * kPi) * uni<R>(g);
+  xmi_rng g;
+  xmi_rng_init(&g, b.seed, (uint64_t)p.id, vr_stream(n, 0xFF));
+  R radius = sqrt(uni<R>(&g)) * (R)b.det_radius;
+  R ang = (R)(2.0 * kPi) * uni<R>(&g);
   R dp[3] = {(R)0, cos(ang) * radius, sin(ang) * radius};
   double rel[3] = {p.c[0] - b.p_det[0], p.c[1] - b.p_det[1], p.c[2] - b.p_det[2]};
   double lcp_d[3];
@@ -459,7 +493,7 @@ __device__ void variance_reduction(const DevBundle<R> &b, Photon<R> &p, xmi_rng 
   R dirv[3];
   matvec(b.det_inv, p.d, dirv);
   R lcd[3] = {dp[0] - lcp[0], dp[1] - lcp[1], dp[2] - lcp[2]};
-  if (lcd[0] >= (R)0) return;
+  if (lcd[0] >= (R)0) return false;
   double total_distance;
   {
     double e0 = (double)dp[0] - lcp_d[0], e1 = (double)dp[1] - lcp_d[1], e2 = (double)dp[2] - lcp_d[2];
@@ -491,10 +525,9 @@ __device__ void variance_reduction(const DevBundle<R> &b, Photon<R> &p, xmi_rng 
   R nsam[3] = {(R)b.n_sample[0], (R)b.n_sample[1], (R)b.n_sample[2]};
   const bool up = rdot(ndc, nsam) > (R)0;
 
-  /* distances toward the detector point through the layers */
-  R dist[XMI_MAXL];
+  /* path toward the detector point through the layers, as density x length */
 #pragma unroll
-  for (int j = 0; j < XMI_MAXL; j++) dist[j] = (R)0;
+  for (int j = 0; j < XMI_MAXL; j++) ev.rd[j] = (R)0;
   {
     double tc[3] = {p.c[0], p.c[1], p.c[2]};
     bool done = false, fail = false;
@@ -504,103 +537,59 @@ __device__ void variance_reduction(const DevBundle<R> &b, Photon<R> &p, xmi_rng 
         double ip[3], dd;
         if (!plane_step(tc, ndc, b.n_sample, up ? b.zend[j] : b.zbeg[j], ip, &dd)) { fail = true; return; }
         if (dd > total_distance) {
-          dist[j] = (R)total_distance;
+          ev.rd[j] = b.rho[j] * (R)total_distance;
           done = true;
         } else {
-          dist[j] = (R)dd;
+          ev.rd[j] = b.rho[j] * (R)dd;
           tc[0] = ip[0]; tc[1] = ip[1]; tc[2] = ip[2];
           total_distance = total_distance - dd;
         }
       }
     });
-    if (fail) { ok = false; return; }
+    if (fail) { ok = false; return false; }
   }
   R murhod = (R)0;
 #pragma unroll
-  for (int j = 0; j < XMI_MAXL; j++) murhod += p.mus[j] * b.rho[j] * dist[j];
-  const R pesc_rayl = exp(-murhod);
+  for (int j = 0; j < XMI_MAXL; j++) murhod += p.mus[j] * ev.rd[j];
+  ev.pesc_rayl = exp(-murhod);
   const R omega = get_solid_angle(b, p.c, p, t, ok);
-  const R pdir_fluo = omega / (R)4 / (R)kPi;
-
-  int node;
-  R f;
-  locate(b, p.E, node, f);
-  const R mu_here = select_layer(p.mus, layer);
-  const R q = p.E / (R)12.39852 * sin(theta / (R)2);
+  ev.pdir_fluo = omega / (R)4 / (R)kPi;
+  locate(b, p.E, ev.node, ev.f);
+  ev.mu_here = select_layer(p.mus, layer);
+  ev.q = p.E / (R)12.39852 * sin(theta / (R)2);
   const R st = sin(theta), cp = cos(phi), ct = cos(theta);
   const R thomson = (R)1 - st * st * cp * cp;
   const R k0k = (R)1 + ((R)1 - ct) * p.E / (R)510.998928, kk0 = (R)1 / k0k;
   const R kn = (R)0.25 * kk0 * kk0 * (kk0 + k0k - (R)2 * st * st * cp * cp);
-  const bool after_fluo = (n > 1 && p.h_type < 0);
-  const int nel = b.nel[layer], off = b.off[layer];
-
-  for (int i = 0; i < nel; i++) {
-    const int e = XMI_LDG(b.layer_el, off + i, b.n_layer_el, 9);
-    const R w = XMI_LDG(b.layer_w, off + i, b.n_layer_el, 9);
-    /* Rayleigh */
-    R pconv = w / mu_here;
-    R pdir = omega * thomson * qtab(b.ff2 + (size_t)e * XMI_NQ, q);
-    double tw = (double)(pconv * pdir * pesc_rayl * p.w);
-    const int rs = b.n_lines + 2 * e;
-    tally_hist(b, t, s_hist, use_smem, n, rs, tw);
-    tally_channel(b, t, n, p.E, tw);
-    /* Compton */
-    R ec = compton_energy(b, e, p.E, theta, g, true, ok);
-    if (!ok) return;
-    R mus_c[XMI_MAXL];
-    mu_calc(b, ec, mus_c);
-    murhod = (R)0;
-#pragma unroll
-    for (int j = 0; j < XMI_MAXL; j++) murhod += mus_c[j] * b.rho[j] * dist[j];
-    R pesc = exp(-murhod);
-    pdir = omega * kn * qtab(b.sf + (size_t)e * XMI_NQ, q);
-    tw = (double)(pconv * pdir * pesc * p.w);
-    tally_hist(b, t, s_hist, use_smem, n, rs + 1, tw);
-    tally_channel(b, t, n, ec, tw);
-    /* fluorescence */
-    R P[XMI_NSHELL];
-    if (after_fluo && !XMI_CHK(p.h_slot, b.n_lines, 43)) { ok = false; return; }
-    if (after_fluo) {
-#pragma unroll
-      for (int s = 0; s < XMI_NSHELL; s++)
-        P[s] = XMI_LDG(b.precalc_xrf, ((long long)e * XMI_NSHELL + s) * b.n_lines + p.h_slot,
-                       (long long)b.n_elem * XMI_NSHELL * b.n_lines, 10);
-    } else {
-#pragma unroll
-      for (int s = 0; s < XMI_NSHELL; s++) P[s] = el_val(b, e, XMI_REC_XRF + s, node, f);
-    }
-    if (!b.use_M_lines) {
-#pragma unroll
-      for (int s = 4; s < XMI_NSHELL; s++) P[s] = (R)0;
-    }
-    const int l0 = XMI_LDG(b.line_off, e, b.n_elem + 1, 11), l1 = XMI_LDG(b.line_off, e + 1, b.n_elem + 1, 11);
-    const R *fy = b.fluor_yield + (size_t)e * XMI_NSHELL;
-    for (int sl = l0; sl < l1; sl++) {
-      const int line = XMI_LDG(b.line_index, sl, b.n_lines, 12);
-      if (line > b.line_last) break; /* slots are sorted by line index */
-      const R efl = XMI_LDG(b.line_energy, sl, b.n_lines, 12);
-      if (efl < (R)kEnergyThreshold) continue;
-      if (line == 30 || line == 31 || line == 59) continue;
-      const int sh = XMI_LDG(b.line_shell, sl, b.n_lines, 12);
-      R ps = (R)0;
-#pragma unroll
-      for (int s = 0; s < XMI_NSHELL; s++)
-        if (s == sh) ps = P[s];
-      if (ps == (R)0) continue;
-      pconv = w * ps * XMI_LDG(b.fluor_yield, (long long)e * XMI_NSHELL + sh, (long long)b.n_elem * XMI_NSHELL, 13) *
-              XMI_LDG(b.line_rate, sl, b.n_lines, 12) / mu_here;
-      murhod = (R)0;
-#pragma unroll
-      for (int j = 0; j < XMI_MAXL; j++)
-        if (j < b.n_layers)
-          murhod += XMI_LDG(b.precalc_mu, (long long)j * b.n_lines + sl, (long long)b.n_layers * b.n_lines, 14) *
-                    b.rho[j] * dist[j];
-      pesc = exp(-murhod);
-      tw = (double)(pconv * pdir_fluo * pesc * p.w);
-      if (tw == 0.0) continue;
-      tally_hist(b, t, s_hist, use_smem, n, sl, tw);
-    }
+  ev.pR = omega * thomson;
+  ev.pC = omega * kn;
+  ev.theta = theta;
+  ev.E = p.E;
+  ev.w = p.w;
+  ev.layer = layer;
+  ev.n = n;
+  ev.id = p.id;
+  ev.h_slot = -1;
+  if (n > 1 && p.h_type < 0) {
+    if (!XMI_CHK(p.h_slot, b.n_lines, 43)) { ok = false; return false; }
+    ev.h_slot = p.h_slot;
   }
+  return true;
+}
+
+/* appends one event; lanes that emit together share one atomic */
+template <typename R>
+__device__ __forceinline__ bool vr_emit(const VrQueue<R> &q, const VrEvent<R> &ev, int key) {
+  const unsigned mask = __activemask();
+  const int lane = threadIdx.x & 31, leader = __ffs(mask) - 1;
+  unsigned long long base = 0;
+  if (lane == leader) base = atomicAdd(q.count, (unsigned long long)__popc(mask));
+  base = __shfl_sync(mask, base, leader);
+  const long long i = (long long)base + __popc(mask & ((1u << lane) - 1u));
+  if (i >= q.cap) return false;
+  q.ev[i] = ev;
+  q.key[i] = key;
+  return true;
 }
 
 /* ---------------- interactions ---------------- */
@@ -853,8 +842,7 @@ __device__ bool check_photon_detector_hit(const DevBundle<R> &b, const Photon<R>
 
 /* ---------------- one history ---------------- */
 template <typename R>
-__device__ bool simulate_photon(const DevBundle<R> &b, Photon<R> &p, const DevTally &t, double *s_hist,
-                                bool use_smem) {
+__device__ bool simulate_photon(const DevBundle<R> &b, Photon<R> &p, const DevTally &t, const VrQueue<R> &vq) {
   for (int guard = 0; guard < 4 * XMI_MAXN + 8; guard++) {
     if (p.E < (R)kEnergyThreshold) break;
     p.inside = 0;
@@ -961,7 +949,9 @@ __device__ bool simulate_photon(const DevBundle<R> &b, Photon<R> &p, const DevTa
     p.n_int = p.n_int + 1;
     if (b.use_vr == 1) {
       bool ok = true;
-      variance_reduction(b, p, &g, t, s_hist, use_smem, ok);
+      VrEvent<R> ev;
+      if (vr_prologue(b, p, t, ev, ok) &&
+          !vr_emit(vq, ev, ev.layer * b.N + ev.n - 1)) { set_error(t, kErrQueue); return false; }
       if (!ok) { set_error(t, kErrTable); return false; }
     }
     /* atom selection and interaction type, src/xmi_main.F90:1556-1652 */
@@ -1110,15 +1100,12 @@ __device__ bool start_photon(const DevBundle<R> &b, const xmi_source_item &it, l
   return true;
 }
 
+/* Transport of the photons with work index [w0, w1): each thread follows
+ * one photon from the source to its last interaction; estimator events go to
+ * the queue, analog detector hits straight to the brute-force tallies. */
 template <typename R>
-__global__ void __launch_bounds__(256) transport_kernel(DevBundle<R> b, DevTally t, long long w0, long long w1,
-                                                        int use_smem) {
-  extern __shared__ double s_hist[];
-  const int nh = b.N * b.n_slots;
-  if (use_smem) {
-    for (int i = threadIdx.x; i < nh; i += blockDim.x) s_hist[i] = 0.0;
-    __syncthreads();
-  }
+__global__ void __launch_bounds__(128) transport_kernel(DevBundle<R> b, DevTally t, VrQueue<R> vq, long long w0,
+                                                        long long w1) {
   const long long stride = (long long)gridDim.x * blockDim.x;
   for (long long w = w0 + (long long)blockIdx.x * blockDim.x + threadIdx.x; w < w1; w += stride) {
     /* work index -> (item, index within item) */
@@ -1142,7 +1129,7 @@ __global__ void __launch_bounds__(256) transport_kernel(DevBundle<R> b, DevTally
     bool skip;
     if (!start_photon(b, it, j, p, skip)) { set_error(t, kErrSource); continue; }
     if (skip) continue;
-    if (!simulate_photon(b, p, t, s_hist, use_smem != 0)) continue;
+    if (!simulate_photon(b, p, t, vq)) continue;
     if (p.hit) {
       if (b.use_vr == 0) tally_channel(b, t, p.n_int, p.E, (double)p.w);
       if (p.n_int > 0) {
@@ -1154,11 +1141,6 @@ __global__ void __launch_bounds__(256) transport_kernel(DevBundle<R> b, DevTally
           atomicAdd(&t.hist_brute[(size_t)(p.n_int - 1) * b.n_slots + slot], (double)p.w);
       }
     }
-  }
-  if (use_smem) {
-    __syncthreads();
-    for (int i = threadIdx.x; i < nh; i += blockDim.x)
-      if (s_hist[i] != 0.0) atomicAdd(&t.hist_vr[i], s_hist[i]);
   }
 }
 

@@ -255,7 +255,11 @@ class Simulation:
     def timing(self) -> dict:
         t, tot, n = C.c_double(), C.c_double(), C.c_int()
         self.lib.xmi_gpu_last_timing(C.byref(t), C.byref(tot), C.byref(n))
-        return {"kernel_ms": t.value, "total_ms": tot.value, "launches": n.value}
+        out = {"kernel_ms": t.value, "total_ms": tot.value, "launches": n.value}
+        tr, so, es, ev = C.c_double(), C.c_double(), C.c_double(), C.c_longlong()
+        self.lib.xmi_gpu_last_phases(C.byref(tr), C.byref(so), C.byref(es), C.byref(ev))
+        out.update(transport_ms=tr.value, sort_ms=so.value, estimator_ms=es.value, events=ev.value)
+        return out
 
     # -- detector response -------------------------------------------------
     def escape_ratios(self, n_photons: int | None = None, n_input_energies: int | None = None):
