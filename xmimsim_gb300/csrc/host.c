@@ -9,6 +9,7 @@
 #include "xrlite.h"
 
 #include <math.h>
+#include <pthread.h>
 #include <stdarg.h>
 #include <stdio.h>
 #include <stdlib.h>
@@ -629,6 +630,60 @@ static void phi_icdf_row(double t, const double *rs, double *out) {
   out[XMI_ICDF_NR - 1] = 2.0 * M_PI;
 }
 
+/* Tables that depend on Z alone (theta inverse CDFs on the fixed 400 x 2000
+ * grid, the Doppler momentum inverse CDF, form factor and scattering
+ * function): computed once per element per process and shared by every
+ * bundle built afterwards -- the role of the per-Z records of the reference's
+ * data file (src/xmi_data_f.F90:880-1481).  Filling is serialised; reads of
+ * filled entries need no lock since entries are never modified once set. */
+typedef struct {
+  double *rayl, *compt, *dop, *ff2, *sf;
+  int ready;
+} z_tables;
+static z_tables z_cache[XRL_MAXZ + 1];
+static pthread_mutex_t z_cache_lock = PTHREAD_MUTEX_INITIALIZER;
+
+static void z_tables_fill(const int *Zs, int n, const double *energies, const double *rs, const double *dop_rs) {
+  int todo[XRL_MAXZ + 1], nt = 0, i, k;
+  pthread_mutex_lock(&z_cache_lock);
+  for (i = 0; i < n; i++) {
+    int Z = Zs[i], seen = 0;
+    if (Z < 1 || Z > XRL_MAXZ || z_cache[Z].ready) continue;
+    for (k = 0; k < nt; k++) seen |= todo[k] == Z;
+    if (!seen) todo[nt++] = Z;
+  }
+  for (k = 0; k < nt; k++) {
+    z_tables *zt = &z_cache[todo[k]];
+    zt->rayl = (double *)malloc(sizeof(double) * XMI_ICDF_NE * XMI_ICDF_NR);
+    zt->compt = (double *)malloc(sizeof(double) * XMI_ICDF_NE * XMI_ICDF_NR);
+    zt->dop = (double *)malloc(sizeof(double) * XMI_DOPPLER_N);
+    zt->ff2 = (double *)malloc(sizeof(double) * XMI_NQ);
+    zt->sf = (double *)malloc(sizeof(double) * XMI_NQ);
+  }
+#pragma omp parallel for schedule(dynamic, 4) collapse(2)
+  for (k = 0; k < nt; k++)
+    for (i = 0; i < XMI_ICDF_NE; i++) {
+      z_tables *zt = &z_cache[todo[k]];
+      theta_icdf(todo[k], energies[i], 1, rs, zt->rayl + (size_t)i * XMI_ICDF_NR);
+      theta_icdf(todo[k], energies[i], 0, rs, zt->compt + (size_t)i * XMI_ICDF_NR);
+    }
+#pragma omp parallel for schedule(dynamic, 1)
+  for (k = 0; k < nt; k++) doppler_icdf(todo[k], dop_rs, z_cache[todo[k]].dop);
+  for (k = 0; k < nt; k++) {
+    int Z = todo[k];
+    z_tables *zt = &z_cache[Z];
+    double scale = XRL_RE2 * XRL_AVOGNUM / xrl_AtomicWeight(Z);
+    for (i = 0; i < XMI_NQ; i++) {
+      double q = XMI_QMAX * i / (XMI_NQ - 1.0);
+      double ff = xrl_FF_Rayl(Z, q);
+      zt->ff2[i] = ff * ff * scale;
+      zt->sf[i] = xrl_SF_Compt(Z, q) * scale;
+    }
+    zt->ready = 1;
+  }
+  pthread_mutex_unlock(&z_cache_lock);
+}
+
 void xmi_bundle_free(xmi_bundle *b) {
   free(b->layer_el); free(b->layer_w); free(b->elem_Z); free(b->elem_yield_corr);
   free(b->elem_fluor_yield); free(b->elem_ck); free(b->elem_edge); free(b->elem_line_off);
@@ -955,35 +1010,26 @@ int xmi_bundle_build(struct xmi_input_handle *in, struct xmi_tables_handle *t,
   for (i = 0; i < XMI_ICDF_NR; i++) b->icdf_rs[i] = (double)i / (XMI_ICDF_NR - 1.0);
   b->rayl_icdf = (double *)malloc(sizeof(double) * (size_t)b->n_elem * XMI_ICDF_NE * XMI_ICDF_NR);
   b->compt_icdf = (double *)malloc(sizeof(double) * (size_t)b->n_elem * XMI_ICDF_NE * XMI_ICDF_NR);
-#pragma omp parallel for schedule(dynamic, 4) collapse(2)
-  for (e = 0; e < b->n_elem; e++)
-    for (i = 0; i < XMI_ICDF_NE; i++) {
-      size_t off = ((size_t)e * XMI_ICDF_NE + i) * XMI_ICDF_NR;
-      theta_icdf(b->elem_Z[e], b->icdf_energies[i], 1, b->icdf_rs, b->rayl_icdf + off);
-      theta_icdf(b->elem_Z[e], b->icdf_energies[i], 0, b->icdf_rs, b->compt_icdf + off);
-    }
+  b->doppler_rs = (double *)malloc(sizeof(double) * XMI_DOPPLER_N);
+  for (i = 0; i < XMI_DOPPLER_N; i++) b->doppler_rs[i] = (double)i / (XMI_DOPPLER_N - 1.0);
+  b->doppler_icdf = (double *)malloc(sizeof(double) * (size_t)b->n_elem * XMI_DOPPLER_N);
+  b->ff2 = (double *)malloc(sizeof(double) * (size_t)b->n_elem * XMI_NQ);
+  b->sf = (double *)malloc(sizeof(double) * (size_t)b->n_elem * XMI_NQ);
+  z_tables_fill(b->elem_Z, b->n_elem, b->icdf_energies, b->icdf_rs, b->doppler_rs);
+  for (e = 0; e < b->n_elem; e++) {
+    const z_tables *zt = &z_cache[b->elem_Z[e]];
+    memcpy(b->rayl_icdf + (size_t)e * XMI_ICDF_NE * XMI_ICDF_NR, zt->rayl, sizeof(double) * XMI_ICDF_NE * XMI_ICDF_NR);
+    memcpy(b->compt_icdf + (size_t)e * XMI_ICDF_NE * XMI_ICDF_NR, zt->compt,
+           sizeof(double) * XMI_ICDF_NE * XMI_ICDF_NR);
+    memcpy(b->doppler_icdf + (size_t)e * XMI_DOPPLER_N, zt->dop, sizeof(double) * XMI_DOPPLER_N);
+    memcpy(b->ff2 + (size_t)e * XMI_NQ, zt->ff2, sizeof(double) * XMI_NQ);
+    memcpy(b->sf + (size_t)e * XMI_NQ, zt->sf, sizeof(double) * XMI_NQ);
+  }
   b->phi_thetas = (double *)malloc(sizeof(double) * XMI_PHI_NT);
   b->phi_icdf = (double *)malloc(sizeof(double) * XMI_PHI_NT * XMI_ICDF_NR);
   for (i = 0; i < XMI_PHI_NT; i++) b->phi_thetas[i] = 0.5 * i / (XMI_PHI_NT - 1.0);
 #pragma omp parallel for schedule(dynamic, 4)
   for (i = 0; i < XMI_PHI_NT; i++) phi_icdf_row(b->phi_thetas[i], b->icdf_rs, b->phi_icdf + (size_t)i * XMI_ICDF_NR);
-  b->doppler_rs = (double *)malloc(sizeof(double) * XMI_DOPPLER_N);
-  for (i = 0; i < XMI_DOPPLER_N; i++) b->doppler_rs[i] = (double)i / (XMI_DOPPLER_N - 1.0);
-  b->doppler_icdf = (double *)malloc(sizeof(double) * (size_t)b->n_elem * XMI_DOPPLER_N);
-#pragma omp parallel for schedule(dynamic, 1)
-  for (e = 0; e < b->n_elem; e++) doppler_icdf(b->elem_Z[e], b->doppler_rs, b->doppler_icdf + (size_t)e * XMI_DOPPLER_N);
-  b->ff2 = (double *)malloc(sizeof(double) * (size_t)b->n_elem * XMI_NQ);
-  b->sf = (double *)malloc(sizeof(double) * (size_t)b->n_elem * XMI_NQ);
-  for (e = 0; e < b->n_elem; e++) {
-    int Z = b->elem_Z[e];
-    double scale = XRL_RE2 * XRL_AVOGNUM / xrl_AtomicWeight(Z);
-    for (i = 0; i < XMI_NQ; i++) {
-      double q = XMI_QMAX * i / (XMI_NQ - 1.0);
-      double ff = xrl_FF_Rayl(Z, q);
-      b->ff2[(size_t)e * XMI_NQ + i] = ff * ff * scale;
-      b->sf[(size_t)e * XMI_NQ + i] = xrl_SF_Compt(Z, q) * scale;
-    }
-  }
   return 1;
 }
 
