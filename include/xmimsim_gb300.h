@@ -119,6 +119,19 @@ void xmi_detector_convolute_all_custom(xmi_inputFPtr inputFPtr, double **channel
 int xmi_detector_convolute_spectrum_noalloc(xmi_inputFPtr inputFPtr, const double *channels_noconv,
                                             double *channels_conv, xmi_main_options *options);
 
+/* Batched transport.  No counterpart in the reference, which simulates one
+ * configuration per call (a quantification front-end such as
+ * bin/xmimsim-pymca.c:597-620 loops over xmi_main_msim).  Runs n prepared
+ * configurations (each handle built by the initialisation chain above, all
+ * with the same xmi_gpu_options precision) in one chunked launch sequence,
+ * captured as one CUDA graph: their photons share the transport, sort and
+ * estimator kernels.  Outputs per configuration as xmi_main_msim's, in
+ * channels[c], brute_histories[c], var_red_histories[c] (n_mpi_hosts = 1).
+ * Calls are serialised within a process. */
+int xmi_main_msim_batch(int n, xmi_inputFPtr *inputFPtrs, xmi_hdf5FPtr *hdf5FPtrs, xmi_main_options **options,
+                        xmi_solid_angle **solid_angles, double **channels, double **brute_histories,
+                        double **var_red_histories);
+
 /* ---- escape ratios (include/xmi_detector.h:55-57) ---- */
 xmi_escape_ratios_options xmi_get_default_escape_ratios_options(void);
 void xmi_escape_ratios_calculation(xmi_input *inputPtr, xmi_escape_ratios **escape_ratios,

@@ -399,7 +399,9 @@ static double compton_energy(const xmi_bundle *b, int e, double E, double theta_
     dlamb = c0 * sth2 * sth2 - c1 * c_lamb0 * sth2 * pz;
     c_lamb = c_lamb0 + dlamb;
     energy = c / c_lamb / 1000.0;
-    if (energy <= E) break;
+    /* the reference accepts when energy <= E; dlamb >= 0 is the same test in
+     * exact arithmetic and cannot be defeated by rounding when dlamb is tiny */
+    if (dlamb >= 0.0) break;
     if (varred) {
       if (it == 100) { *err = 3; return 0.0; }
       it++;

@@ -251,3 +251,26 @@ def test_escape_ratios_plausible():
     assert (si_k[E < 1.8] == 0).all()
     sim.lib.xmi_free_escape_ratios(C.pointer(er))
     sim.close()
+
+
+def test_batched_run_matches_single_runs_and_oracle():
+    """xmi_main_msim_batch: three different configurations in one launch
+    sequence give each configuration's single-run result (same photon
+    streams; only the order of FP64 additions differs) and the oracle's."""
+    specs = [configs.config1(n_photons_line=4000), mixed_source_spec(), collimator_spec(3000)]
+    specs[0].n_interactions_trajectory = 3
+    sims = [Simulation(sp, options=configs.C1_OPTIONS, gpu=gpu_options(seed=SEED)) for sp in specs]
+    for s in sims:
+        s.solid_angle()
+    batched = Simulation.msim_batch(sims)
+    for s, b in zip(sims, batched):
+        single = s.msim()
+        np.testing.assert_allclose(b["var_red"], single["var_red"], rtol=1e-9, atol=1e-12 * abs(single["var_red"]).max())
+        np.testing.assert_allclose(b["channels"], single["channels"], rtol=1e-9,
+                                   atol=1e-12 * abs(single["channels"]).max())
+        s.prepare()
+        ref = oracle().msim(s.bundle_ptr(), s.spec.n_interactions_trajectory, s.spec.nchannels)
+        assert_transport_equal(b, ref)
+        s.free_raw(b)
+        s.free_raw(single)
+        s.close()

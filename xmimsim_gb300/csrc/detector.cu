@@ -651,7 +651,7 @@ __global__ void __launch_bounds__(256) escape_kernel(xmi::DevBundle<R> b, xmi::D
       p.c[0] = ip[0]; p.c[1] = ip[1]; p.c[2] = ip[2];
       p.layer = 0;
     }
-    if (!simulate_photon(b, p, t, xmi::VrQueue<R>{nullptr, nullptr, nullptr, 0})) continue;
+    if (!simulate_photon(b, p, t, xmi::VrQueue<R>{nullptr, nullptr, nullptr, 0}, 0)) continue;
     if (p.last != XMI_NO_INTERACTION) atomicAdd(&et.interacted[iE], (double)p.w);
     if (!p.inside && p.last != XMI_NO_INTERACTION) {
       if (p.last == XMI_COMPTON) {

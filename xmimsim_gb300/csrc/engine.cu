@@ -9,6 +9,8 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <chrono>
+#include <mutex>
 #include <vector>
 
 #include "estimator.cuh"
@@ -49,6 +51,25 @@ struct DevSide {
   }
 };
 
+/* device buffers of the estimator event queue of one chunk */
+struct EventQueue {
+  void *events = nullptr;
+  int *key = nullptr, *order = nullptr;
+  unsigned *hist = nullptr; /* [2][nkeys]: counts, then scatter cursors */
+  unsigned long long *count = nullptr;
+  size_t bytes = 0;
+  long long cap = 0;
+  int nkeys = 0;
+  void release() {
+    cudaFree(events);
+    cudaFree(key);
+    cudaFree(order);
+    cudaFree(hist);
+    cudaFree(count);
+    *this = EventQueue();
+  }
+};
+
 struct DevState {
   DevSide d64, d32;
   xmi::DevBundle<double> b64;
@@ -66,13 +87,7 @@ struct DevState {
   unsigned long long *counters = nullptr;
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-  /* estimator event queue of one chunk */
-  void *q_events = nullptr;
-  int *q_key = nullptr, *q_order = nullptr;
-  unsigned *q_hist = nullptr; /* [2][XMI_MAXL * XMI_MAXN]: counts, cursors */
-  unsigned long long *q_count = nullptr;
-  size_t q_bytes = 0;
-  long long q_cap = 0;
+  EventQueue q; /* estimator event queue of one chunk */
 };
 
 template <typename R>
@@ -272,11 +287,7 @@ void xmi_dev_free_tables(struct xmi_tables_handle *t) {
   cudaFree(s->sa_g32);
   cudaFree(s->tally);
   cudaFree(s->counters);
-  cudaFree(s->q_events);
-  cudaFree(s->q_key);
-  cudaFree(s->q_order);
-  cudaFree(s->q_hist);
-  cudaFree(s->q_count);
+  s->q.release();
   if (s->ev0) cudaEventDestroy(s->ev0);
   if (s->ev1) cudaEventDestroy(s->ev1);
   if (s->stream) cudaStreamDestroy(s->stream);
@@ -472,47 +483,180 @@ int xmi_gpu_prepare_run(xmi_inputFPtr in, xmi_hdf5FPtr t, xmi_main_options *opti
 constexpr long long kMaxQueuedEvents = 1ll << 25;
 
 template <typename R>
-static bool ensure_queue(DevState *s, long long cap) {
+static bool ensure_queue(EventQueue &q, long long cap, int nkeys) {
   const size_t bytes = (size_t)cap * sizeof(xmi::VrEvent<R>);
-  if (bytes <= s->q_bytes && cap <= s->q_cap) return true;
-  cudaFree(s->q_events);
-  cudaFree(s->q_key);
-  cudaFree(s->q_order);
-  s->q_events = nullptr;
-  s->q_key = s->q_order = nullptr;
-  s->q_bytes = 0;
-  s->q_cap = 0;
-  if (!cuda_ok(cudaMalloc(&s->q_events, bytes), "cudaMalloc event queue") ||
-      !cuda_ok(cudaMalloc(&s->q_key, sizeof(int) * cap), "cudaMalloc event keys") ||
-      !cuda_ok(cudaMalloc(&s->q_order, sizeof(int) * cap), "cudaMalloc event order"))
-    return false;
-  if (!s->q_hist && !cuda_ok(cudaMalloc(&s->q_hist, 2 * sizeof(unsigned) * XMI_MAXL * XMI_MAXN), "cudaMalloc"))
-    return false;
-  if (!s->q_count && !cuda_ok(cudaMalloc(&s->q_count, sizeof(unsigned long long)), "cudaMalloc")) return false;
-  s->q_bytes = bytes;
-  s->q_cap = cap;
+  if (bytes > q.bytes || cap > q.cap) {
+    cudaFree(q.events);
+    cudaFree(q.key);
+    cudaFree(q.order);
+    q.events = nullptr;
+    q.key = q.order = nullptr;
+    q.bytes = 0;
+    q.cap = 0;
+    if (!cuda_ok(cudaMalloc(&q.events, bytes), "cudaMalloc event queue") ||
+        !cuda_ok(cudaMalloc(&q.key, sizeof(int) * cap), "cudaMalloc event keys") ||
+        !cuda_ok(cudaMalloc(&q.order, sizeof(int) * cap), "cudaMalloc event order"))
+      return false;
+    q.bytes = bytes;
+    q.cap = cap;
+  }
+  if (nkeys > q.nkeys) {
+    cudaFree(q.hist);
+    q.hist = nullptr;
+    q.nkeys = 0;
+    if (!cuda_ok(cudaMalloc(&q.hist, 2 * sizeof(unsigned) * nkeys), "cudaMalloc key histogram")) return false;
+    q.nkeys = nkeys;
+  }
+  if (!q.count && !cuda_ok(cudaMalloc(&q.count, sizeof(unsigned long long)), "cudaMalloc")) return false;
   return true;
 }
 
-/* Runs the photons of the bundle's source items: per chunk, the transport
- * kernel (events into the queue), the counting sort of the events by
- * (layer, order) and the estimator kernel.  All launches go to the handle's
- * stream; CUDA events around each phase give the device times. */
+struct Phases {
+  double ms[3] = {0.0, 0.0, 0.0}; /* transport kernel, event sort, estimator kernel */
+  double total_ms = 0.0;
+  int launches = 0;
+};
+
+/* Runs work indices [0, n) in chunks on stream st: per chunk the transport
+ * launch (events into the queue), the counting sort of the events by key and
+ * the estimator launch.  CUDA events around each phase give the device times.
+ * transport(w0, w1, vq) and estimator(vq, order) enqueue the two kernels. */
+template <typename R, typename TF, typename EF>
+static bool run_chunks(cudaStream_t st, EventQueue &q, long long n, int N, int nkeys, bool vr,
+                       unsigned long long *total_events, TF &&transport, EF &&estimator, Phases &ph,
+                       bool graph = false) {
+  const int sms = num_sms();
+  long long chunk = n > 0 ? n : 1;
+  xmi::VrQueue<R> vq{nullptr, nullptr, nullptr, 0};
+  if (vr) {
+    chunk = kMaxQueuedEvents / (N > 0 ? N : 1);
+    if (chunk > n) chunk = n;
+    if (chunk < 1) chunk = 1;
+    if (!ensure_queue<R>(q, chunk * N, nkeys)) return false;
+    vq.ev = (xmi::VrEvent<R> *)q.events;
+    vq.key = q.key;
+    vq.count = q.count;
+    vq.cap = chunk * N;
+  }
+  std::vector<cudaEvent_t> marks;
+  auto mark = [&]() {
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    cudaEventRecord(e, st);
+    marks.push_back(e);
+  };
+  int launches = 0;
+  cudaGraph_t g = nullptr;
+  cudaGraphExec_t ge = nullptr;
+  if (graph && !cuda_ok(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "graph capture")) return false;
+  mark();
+  for (long long w0 = 0; w0 < n; w0 += chunk) {
+    const long long w1 = w0 + chunk < n ? w0 + chunk : n;
+    if (vr) {
+      cudaMemsetAsync(q.count, 0, sizeof(unsigned long long), st);
+      cudaMemsetAsync(q.hist, 0, sizeof(unsigned) * nkeys, st);
+    }
+    transport(w0, w1, vq);
+    launches++;
+    mark();
+    if (vr) {
+      /* positions of events whose key the sort would skip stay -1 and are refused by the estimator */
+      cudaMemsetAsync(q.order, 0xff, sizeof(int) * (w1 - w0) * N, st);
+      xmi::event_key_histogram<<<sms * 4, 256, 0, st>>>(q.key, q.count, vq.cap, nkeys, q.hist);
+      xmi::event_key_scan<<<1, 32, 0, st>>>(q.hist, nkeys, q.hist + nkeys, q.count, total_events);
+      xmi::event_key_scatter<<<sms * 4, 256, 0, st>>>(q.key, q.count, vq.cap, nkeys, q.hist + nkeys, q.order);
+      mark();
+      estimator(vq, (const int *)q.order);
+      mark();
+      launches += 4;
+    }
+    if (!cuda_ok(cudaGetLastError(), "transport launch")) break;
+  }
+  bool ok = cuda_ok(cudaGetLastError(), "transport launch");
+  if (graph) {
+    /* the whole chunk sequence as one graph launch */
+    ok = cuda_ok(cudaStreamEndCapture(st, &g), "graph capture") && ok &&
+         cuda_ok(cudaGraphInstantiate(&ge, g, 0), "graph instantiate") && cuda_ok(cudaGraphLaunch(ge, st), "graph launch");
+  }
+  ok = ok && cuda_ok(cudaEventSynchronize(marks.back()), "transport");
+  if (ge) cudaGraphExecDestroy(ge);
+  if (g) cudaGraphDestroy(g);
+  if (ok) {
+    float total = 0.f;
+    cudaEventElapsedTime(&total, marks.front(), marks.back());
+    ph.total_ms = total;
+    const size_t per = vr ? 3 : 1;
+    for (size_t i = 0; i + per < marks.size(); i += per)
+      for (size_t k = 0; k < per; k++) {
+        float f = 0.f;
+        cudaEventElapsedTime(&f, marks[i + k], marks[i + k + 1]);
+        ph.ms[k] += f;
+      }
+    ph.launches = launches;
+  }
+  for (cudaEvent_t e : marks) cudaEventDestroy(e);
+  return ok;
+}
+
+/* Uploads what one run of a configuration needs besides its tables (source
+ * items, solid-angle grid), clears its tallies and fills the run fields of
+ * its device bundle and tally view.  Copies go to the handle's stream. */
 template <typename R>
-static bool launch_transport(DevState *s, xmi::DevBundle<R> &d, const xmi_bundle &h, int threads, int blocks_per_sm,
-                             double *ms) {
+static bool stage_run(DevState *s, xmi::DevBundle<R> &d, const xmi_bundle &h, xmi::DevTally &tl) {
+  std::vector<long long> first(h.n_items > 0 ? h.n_items : 1, 0);
+  for (int i = 1; i < h.n_items; i++) first[i] = first[i - 1] + h.items[i - 1].n_photons;
+  if (h.n_items > s->items_cap) {
+    cudaFree(s->items);
+    cudaFree(s->item_first);
+    s->items = nullptr;
+    s->item_first = nullptr;
+    s->items_cap = 0;
+    if (!cuda_ok(cudaMalloc(&s->items, sizeof(xmi_source_item) * h.n_items), "cudaMalloc items") ||
+        !cuda_ok(cudaMalloc(&s->item_first, sizeof(long long) * h.n_items), "cudaMalloc items"))
+      return false;
+    s->items_cap = h.n_items;
+  }
+  if (h.n_items > 0) {
+    cudaMemcpyAsync(s->items, h.items, sizeof(xmi_source_item) * h.n_items, cudaMemcpyHostToDevice, s->stream);
+    cudaMemcpyAsync(s->item_first, first.data(), sizeof(long long) * h.n_items, cudaMemcpyHostToDevice, s->stream);
+  }
+  /* solid-angle grid (kept on the device while the caller's grid is the same) */
+  if (h.sa_nr > 0 && (s->sa_src != h.sa_grid || s->sa_n != h.sa_nr * h.sa_nt)) {
+    size_t n = (size_t)h.sa_nr * h.sa_nt;
+    cudaFree(s->sa_r);
+    cudaFree(s->sa_t);
+    cudaFree(s->sa_g64);
+    cudaFree(s->sa_g32);
+    s->sa_r = s->sa_t = s->sa_g64 = nullptr;
+    s->sa_g32 = nullptr;
+    s->sa_src = nullptr;
+    if (!cuda_ok(cudaMalloc(&s->sa_r, sizeof(double) * h.sa_nr), "cudaMalloc") ||
+        !cuda_ok(cudaMalloc(&s->sa_t, sizeof(double) * h.sa_nt), "cudaMalloc") ||
+        !cuda_ok(cudaMalloc(&s->sa_g64, sizeof(double) * n), "cudaMalloc") ||
+        !cuda_ok(cudaMalloc(&s->sa_g32, sizeof(float) * n), "cudaMalloc"))
+      return false;
+    std::vector<float> g32(n);
+    for (size_t i = 0; i < n; i++) g32[i] = (float)h.sa_grid[i];
+    cudaMemcpy(s->sa_r, h.sa_r, sizeof(double) * h.sa_nr, cudaMemcpyHostToDevice);
+    cudaMemcpy(s->sa_t, h.sa_t, sizeof(double) * h.sa_nt, cudaMemcpyHostToDevice);
+    cudaMemcpy(s->sa_g64, h.sa_grid, sizeof(double) * n, cudaMemcpyHostToDevice);
+    cudaMemcpy(s->sa_g32, g32.data(), sizeof(float) * n, cudaMemcpyHostToDevice);
+    s->sa_src = h.sa_grid;
+    s->sa_n = (int)n;
+  }
   const size_t nh = (size_t)h.n_interactions * h.n_slots;
   const size_t nc = (size_t)(h.n_interactions + 1) * h.nchannels;
   const size_t need = 2 * nh + nc;
   if (need > s->tally_cap) {
     cudaFree(s->tally);
+    s->tally = nullptr;
+    s->tally_cap = 0;
     if (!cuda_ok(cudaMalloc(&s->tally, need * sizeof(double)), "cudaMalloc tally")) return false;
     s->tally_cap = need;
   }
   if (!s->counters && !cuda_ok(cudaMalloc(&s->counters, 8 * sizeof(unsigned long long)), "cudaMalloc")) return false;
   cudaMemsetAsync(s->tally, 0, need * sizeof(double), s->stream);
   cudaMemsetAsync(s->counters, 0, 8 * sizeof(unsigned long long), s->stream);
-  xmi::DevTally tl;
   tl.hist_vr = s->tally;
   tl.hist_brute = s->tally + nh;
   tl.chan = s->tally + 2 * nh;
@@ -532,25 +676,17 @@ static bool launch_transport(DevState *s, xmi::DevBundle<R> &d, const xmi_bundle
   }
   if (sizeof(R) == 8) d.sa_grid = (const R *)s->sa_g64;
   else d.sa_grid = (const R *)s->sa_g32;
+  return true;
+}
 
-  const long long n = h.n_photons_total;
-  const int N = h.n_interactions, nkeys = h.n_layers * N;
+/* one configuration on its handle's stream */
+template <typename R>
+static bool launch_single(DevState *s, xmi::DevBundle<R> &d, const xmi::DevTally &tl, const xmi_bundle &h,
+                          int threads, int blocks_per_sm, Phases &ph) {
   const int sms = num_sms();
-  long long chunk = n > 0 ? n : 1;
-  xmi::VrQueue<R> vq{nullptr, nullptr, nullptr, 0};
-  if (h.use_vr) {
-    chunk = kMaxQueuedEvents / N;
-    if (chunk > n) chunk = n;
-    if (chunk < 1) chunk = 1;
-    if (!ensure_queue<R>(s, chunk * N)) return false;
-    vq.ev = (xmi::VrEvent<R> *)s->q_events;
-    vq.key = s->q_key;
-    vq.count = s->q_count;
-    vq.cap = chunk * N;
-  }
-  /* estimator: per-CTA shared-memory histories when they fit */
+  const size_t nh = (size_t)h.n_interactions * h.n_slots;
   size_t smem = nh * sizeof(double);
-  int use_smem = (h.use_vr && smem <= 200 * 1024) ? 1 : 0;
+  const int use_smem = (h.use_vr && smem <= 200 * 1024) ? 1 : 0;
   if (use_smem && smem > 48 * 1024)
     cudaFuncSetAttribute(xmi::estimator_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (!use_smem) smem = 0;
@@ -558,135 +694,34 @@ static bool launch_transport(DevState *s, xmi::DevBundle<R> &d, const xmi_bundle
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&est_per_sm, xmi::estimator_kernel<R>, 256, smem);
   if (est_per_sm < 1) est_per_sm = 1;
   const int est_blocks = sms * est_per_sm;
-
-  std::vector<cudaEvent_t> marks;
-  auto mark = [&]() {
-    cudaEvent_t e;
-    cudaEventCreate(&e);
-    cudaEventRecord(e, s->stream);
-    marks.push_back(e);
-  };
-  int launches = 0;
-  mark();
-  for (long long w0 = 0; w0 < n; w0 += chunk) {
-    const long long w1 = w0 + chunk < n ? w0 + chunk : n;
+  auto transport = [&](long long w0, long long w1, const xmi::VrQueue<R> &vq) {
     long long blocks = (long long)sms * blocks_per_sm;
     if (blocks * threads > w1 - w0) blocks = (w1 - w0 + threads - 1) / threads;
     if (blocks < 1) blocks = 1;
-    if (h.use_vr) {
-      cudaMemsetAsync(s->q_count, 0, sizeof(unsigned long long), s->stream);
-      cudaMemsetAsync(s->q_hist, 0, sizeof(unsigned) * XMI_MAXL * XMI_MAXN, s->stream);
-    }
     xmi::transport_kernel<R><<<(int)blocks, threads, 0, s->stream>>>(d, tl, vq, w0, w1);
-    launches++;
-    mark();
-    if (h.use_vr) {
-      /* positions of events whose key the sort would skip stay -1 and are refused by the estimator */
-      cudaMemsetAsync(s->q_order, 0xff, sizeof(int) * (w1 - w0) * N, s->stream);
-      xmi::event_key_histogram<<<sms * 2, 256, 0, s->stream>>>(s->q_key, s->q_count, vq.cap, nkeys, s->q_hist);
-      xmi::event_key_scan<<<1, 32, 0, s->stream>>>(s->q_hist, nkeys, s->q_hist + XMI_MAXL * XMI_MAXN, s->q_count,
-                                                   &s->counters[3]);
-      xmi::event_key_scatter<<<sms * 4, 256, 0, s->stream>>>(s->q_key, s->q_count, vq.cap, nkeys,
-                                                              s->q_hist + XMI_MAXL * XMI_MAXN, s->q_order);
-      mark();
-      xmi::estimator_kernel<R><<<est_blocks, 256, smem, s->stream>>>(d, tl, vq.ev, s->q_order, s->q_count, vq.cap,
-                                                                     use_smem);
-      mark();
-      launches += 4;
-    }
-    if (!cuda_ok(cudaGetLastError(), "transport launch")) break;
-  }
-  bool ok = cuda_ok(cudaGetLastError(), "transport launch") &&
-            cuda_ok(cudaEventSynchronize(marks.back()), "transport_kernel");
-  double phase[3] = {0.0, 0.0, 0.0};
-  float total = 0.f;
-  if (ok) {
-    cudaEventElapsedTime(&total, marks.front(), marks.back());
-    const size_t per = h.use_vr ? 3 : 1;
-    for (size_t i = 0; i + per < marks.size(); i += per)
-      for (size_t k = 0; k < per; k++) {
-        float f = 0.f;
-        cudaEventElapsedTime(&f, marks[i + k], marks[i + k + 1]);
-        phase[k] += f;
-      }
-  }
-  for (cudaEvent_t e : marks) cudaEventDestroy(e);
-  if (!ok) return false;
-  *ms = total;
-  g_timing.launches = launches;
-  for (int k = 0; k < 3; k++) g_timing.phase_ms[k] = phase[k];
-  return true;
+  };
+  auto estimator = [&](const xmi::VrQueue<R> &vq, const int *order) {
+    xmi::estimator_kernel<R><<<est_blocks, 256, smem, s->stream>>>(d, tl, vq.ev, order, vq.count, vq.cap, use_smem);
+  };
+  return run_chunks<R>(s->stream, s->q, h.n_photons_total, h.n_interactions, XMI_MAXL * XMI_MAXN, h.use_vr != 0,
+                       &s->counters[3], transport, estimator, ph);
 }
 
-extern "C" int xmi_main_msim(xmi_inputFPtr in, xmi_hdf5FPtr t, int n_mpi_hosts, double **channels_out,
-                  xmi_main_options *options, double **brute_out, double **var_red_out, xmi_solid_angle *sa) {
-  cudaEvent_t all0, all1;
-  if (!ensure_device()) return 0;
-  if (!xmi_gpu_prepare_run(in, t, options, n_mpi_hosts, sa)) return 0;
-  const xmi_bundle &h = t->b;
-  const int precision = in->gpu.precision;
-  if (!xmi_dev_sync_tables(t, precision)) return 0;
-  DevState *s = state_of(t);
-  cudaEventCreate(&all0);
-  cudaEventCreate(&all1);
-  cudaEventRecord(all0, s->stream);
-
-  /* source items and their work offsets */
-  std::vector<long long> first(h.n_items > 0 ? h.n_items : 1, 0);
-  for (int i = 1; i < h.n_items; i++) first[i] = first[i - 1] + h.items[i - 1].n_photons;
-  if (h.n_items > s->items_cap) {
-    cudaFree(s->items);
-    cudaFree(s->item_first);
-    if (!cuda_ok(cudaMalloc(&s->items, sizeof(xmi_source_item) * h.n_items), "cudaMalloc items") ||
-        !cuda_ok(cudaMalloc(&s->item_first, sizeof(long long) * h.n_items), "cudaMalloc items"))
-      return 0;
-    s->items_cap = h.n_items;
-  }
-  if (h.n_items > 0) {
-    cudaMemcpyAsync(s->items, h.items, sizeof(xmi_source_item) * h.n_items, cudaMemcpyHostToDevice, s->stream);
-    cudaMemcpyAsync(s->item_first, first.data(), sizeof(long long) * h.n_items, cudaMemcpyHostToDevice, s->stream);
-  }
-  /* solid-angle grid (kept on the device while the caller's grid is the same) */
-  if (h.sa_nr > 0 && (s->sa_src != h.sa_grid || s->sa_n != h.sa_nr * h.sa_nt)) {
-    size_t n = (size_t)h.sa_nr * h.sa_nt;
-    cudaFree(s->sa_r);
-    cudaFree(s->sa_t);
-    cudaFree(s->sa_g64);
-    cudaFree(s->sa_g32);
-    if (!cuda_ok(cudaMalloc(&s->sa_r, sizeof(double) * h.sa_nr), "cudaMalloc") ||
-        !cuda_ok(cudaMalloc(&s->sa_t, sizeof(double) * h.sa_nt), "cudaMalloc") ||
-        !cuda_ok(cudaMalloc(&s->sa_g64, sizeof(double) * n), "cudaMalloc") ||
-        !cuda_ok(cudaMalloc(&s->sa_g32, sizeof(float) * n), "cudaMalloc"))
-      return 0;
-    std::vector<float> g32(n);
-    for (size_t i = 0; i < n; i++) g32[i] = (float)h.sa_grid[i];
-    cudaMemcpy(s->sa_r, h.sa_r, sizeof(double) * h.sa_nr, cudaMemcpyHostToDevice);
-    cudaMemcpy(s->sa_t, h.sa_t, sizeof(double) * h.sa_nt, cudaMemcpyHostToDevice);
-    cudaMemcpy(s->sa_g64, h.sa_grid, sizeof(double) * n, cudaMemcpyHostToDevice);
-    cudaMemcpy(s->sa_g32, g32.data(), sizeof(float) * n, cudaMemcpyHostToDevice);
-    s->sa_src = h.sa_grid;
-    s->sa_n = (int)n;
-  }
-
-  const int threads = in->gpu.threads_per_block > 0 ? in->gpu.threads_per_block : 128;
-  const int bps = in->gpu.blocks_per_sm > 0 ? in->gpu.blocks_per_sm : 4;
-  double ms = 0.0;
-  bool ok = precision == 0 ? launch_transport<double>(s, s->b64, h, threads, bps, &ms)
-                           : launch_transport<float>(s, s->b32, h, threads, bps, &ms);
-  if (!ok) return 0;
-
+/* device tallies -> the reference's output layouts (host) */
+static int collect_outputs(DevState *s, const xmi_bundle &h, int n_mpi_hosts, double **channels_out,
+                           double **brute_out, double **var_red_out, unsigned long long *events) {
   const int N = h.n_interactions, nch = h.nchannels, S = h.n_slots;
   const size_t nh = (size_t)N * S, nc = (size_t)(N + 1) * nch;
   std::vector<double> tally(2 * nh + nc);
   unsigned long long counters[8];
   cudaMemcpyAsync(tally.data(), s->tally, sizeof(double) * tally.size(), cudaMemcpyDeviceToHost, s->stream);
   cudaMemcpyAsync(counters, s->counters, sizeof(counters), cudaMemcpyDeviceToHost, s->stream);
-  cudaEventRecord(all1, s->stream);
   if (!cuda_ok(cudaStreamSynchronize(s->stream), "copy back")) return 0;
   if (counters[1] != 0) {
     xmi_set_error("transport kernel reported error code %llu", counters[1]);
     return 0;
   }
+  if (events) *events = counters[3];
   const double *hv = tally.data(), *hb = tally.data() + nh, *chan = tally.data() + 2 * nh;
 
   /* channels: per-order scatter tallies plus the fluorescence lines derived
@@ -724,17 +759,177 @@ extern "C" int xmi_main_msim(xmi_inputFPtr in, xmi_hdf5FPtr t, int n_mpi_hosts, 
       brute[idx] = hb[(size_t)(n - 1) * S + sl] * scale;
       if (var_red) var_red[idx] = hv[(size_t)(n - 1) * S + sl] * scale;
     }
-  float tot = 0.f;
-  cudaEventElapsedTime(&tot, all0, all1);
-  cudaEventDestroy(all0);
-  cudaEventDestroy(all1);
-  g_timing.transport_ms = ms;
-  g_timing.total_ms = tot;
-  g_timing.events = (long long)counters[3];
   *channels_out = channels;
   *brute_out = brute;
   *var_red_out = var_red;
   return 1;
 }
 
+extern "C" int xmi_main_msim(xmi_inputFPtr in, xmi_hdf5FPtr t, int n_mpi_hosts, double **channels_out,
+                  xmi_main_options *options, double **brute_out, double **var_red_out, xmi_solid_angle *sa) {
+  cudaEvent_t all0, all1;
+  if (!ensure_device()) return 0;
+  if (!xmi_gpu_prepare_run(in, t, options, n_mpi_hosts, sa)) return 0;
+  const xmi_bundle &h = t->b;
+  const int precision = in->gpu.precision;
+  if (!xmi_dev_sync_tables(t, precision)) return 0;
+  DevState *s = state_of(t);
+  cudaEventCreate(&all0);
+  cudaEventCreate(&all1);
+  cudaEventRecord(all0, s->stream);
+  xmi::DevTally tl;
+  const int threads = in->gpu.threads_per_block > 0 ? in->gpu.threads_per_block : 128;
+  const int bps = in->gpu.blocks_per_sm > 0 ? in->gpu.blocks_per_sm : 4;
+  Phases ph;
+  bool ok = precision == 0 ? stage_run<double>(s, s->b64, h, tl) && launch_single<double>(s, s->b64, tl, h, threads, bps, ph)
+                           : stage_run<float>(s, s->b32, h, tl) && launch_single<float>(s, s->b32, tl, h, threads, bps, ph);
+  if (!ok) return 0;
+  unsigned long long events = 0;
+  if (!collect_outputs(s, h, n_mpi_hosts, channels_out, brute_out, var_red_out, &events)) return 0;
+  cudaEventRecord(all1, s->stream);
+  cudaEventSynchronize(all1);
+  float tot = 0.f;
+  cudaEventElapsedTime(&tot, all0, all1);
+  cudaEventDestroy(all0);
+  cudaEventDestroy(all1);
+  g_timing.transport_ms = ph.total_ms;
+  g_timing.total_ms = tot;
+  g_timing.launches = ph.launches;
+  for (int k = 0; k < 3; k++) g_timing.phase_ms[k] = ph.ms[k];
+  g_timing.events = (long long)events;
+  return 1;
+}
 
+/* ---------------------------------------------------------------- */
+/* batched runs                                                       */
+/* ---------------------------------------------------------------- */
+namespace {
+template <typename R> xmi::DevBundle<R> &dev_bundle_of(DevState *s);
+template <> xmi::DevBundle<double> &dev_bundle_of<double>(DevState *s) { return s->b64; }
+template <> xmi::DevBundle<float> &dev_bundle_of<float>(DevState *s) { return s->b32; }
+
+/* device arrays of the batched call, kept while large enough */
+struct BatchState {
+  void *bundles = nullptr;
+  size_t bundles_bytes = 0;
+  xmi::DevTally *tallies = nullptr;
+  long long *cfg_first = nullptr;
+  int cap = 0;
+  unsigned long long *flags = nullptr; /* [0] estimator error, [1] events */
+  EventQueue q;
+  cudaStream_t stream = nullptr;
+};
+BatchState g_batch;
+std::mutex g_batch_lock;
+
+template <typename R>
+bool launch_batch(int n, DevState **st, xmi_hdf5FPtr *t, const xmi::DevTally *tl, int threads, int blocks_per_sm,
+                  bool graph, Phases &ph) {
+  BatchState &B = g_batch;
+  std::vector<xmi::DevBundle<R>> bundles(n);
+  std::vector<long long> first(n + 1, 0);
+  int N = 1;
+  bool vr = false;
+  for (int c = 0; c < n; c++) {
+    bundles[c] = dev_bundle_of<R>(st[c]);
+    first[c + 1] = first[c] + t[c]->b.n_photons_total;
+    if (t[c]->b.n_interactions > N) N = t[c]->b.n_interactions;
+    vr = vr || t[c]->b.use_vr;
+  }
+  if (!B.stream) cudaStreamCreateWithFlags(&B.stream, cudaStreamNonBlocking);
+  if (n > B.cap || sizeof(xmi::DevBundle<R>) * n > B.bundles_bytes) {
+    cudaFree(B.bundles);
+    cudaFree(B.tallies);
+    cudaFree(B.cfg_first);
+    B.bundles = nullptr;
+    B.tallies = nullptr;
+    B.cfg_first = nullptr;
+    B.cap = 0;
+    B.bundles_bytes = 0;
+    if (!cuda_ok(cudaMalloc(&B.bundles, sizeof(xmi::DevBundle<double>) * n), "cudaMalloc bundles") ||
+        !cuda_ok(cudaMalloc(&B.tallies, sizeof(xmi::DevTally) * n), "cudaMalloc tallies") ||
+        !cuda_ok(cudaMalloc(&B.cfg_first, sizeof(long long) * (n + 1)), "cudaMalloc offsets"))
+      return false;
+    B.cap = n;
+    B.bundles_bytes = sizeof(xmi::DevBundle<double>) * n;
+  }
+  if (!B.flags && !cuda_ok(cudaMalloc(&B.flags, 2 * sizeof(unsigned long long)), "cudaMalloc")) return false;
+  cudaMemcpyAsync(B.bundles, bundles.data(), sizeof(xmi::DevBundle<R>) * n, cudaMemcpyHostToDevice, B.stream);
+  cudaMemcpyAsync(B.tallies, tl, sizeof(xmi::DevTally) * n, cudaMemcpyHostToDevice, B.stream);
+  cudaMemcpyAsync(B.cfg_first, first.data(), sizeof(long long) * (n + 1), cudaMemcpyHostToDevice, B.stream);
+  cudaMemsetAsync(B.flags, 0, 2 * sizeof(unsigned long long), B.stream);
+  const xmi::DevBundle<R> *db = (const xmi::DevBundle<R> *)B.bundles;
+  const int sms = num_sms();
+  int est_per_sm = 1;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&est_per_sm, xmi::estimator_kernel_batch<R>, 256, 0);
+  if (est_per_sm < 1) est_per_sm = 1;
+  const int est_blocks = sms * est_per_sm;
+  auto transport = [&](long long w0, long long w1, const xmi::VrQueue<R> &vq) {
+    long long blocks = (long long)sms * blocks_per_sm;
+    if (blocks * threads > w1 - w0) blocks = (w1 - w0 + threads - 1) / threads;
+    if (blocks < 1) blocks = 1;
+    xmi::transport_kernel_batch<R><<<(int)blocks, threads, 0, B.stream>>>(db, B.tallies, B.cfg_first, n, vq, w0, w1);
+  };
+  auto estimator = [&](const xmi::VrQueue<R> &vq, const int *order) {
+    xmi::estimator_kernel_batch<R><<<est_blocks, 256, 0, B.stream>>>(db, B.tallies, n, vq.ev, order, vq.count, vq.cap,
+                                                                    B.flags);
+  };
+  if (!run_chunks<R>(B.stream, B.q, first[n], N, n * XMI_MAXL * XMI_MAXN, vr, &B.flags[1], transport, estimator, ph,
+                     graph))
+    return false;
+  unsigned long long flags[2];
+  cudaMemcpy(flags, B.flags, sizeof(flags), cudaMemcpyDeviceToHost);
+  if (flags[0] != 0) {
+    xmi_set_error("estimator kernel reported error code %llu", flags[0]);
+    return false;
+  }
+  g_timing.events = (long long)flags[1];
+  return true;
+}
+}  // namespace
+
+extern "C" int xmi_main_msim_batch(int n, xmi_inputFPtr *inputFPtrs, xmi_hdf5FPtr *hdf5FPtrs,
+                                   xmi_main_options **options, xmi_solid_angle **solid_angles, double **channels,
+                                   double **brute_histories, double **var_red_histories) {
+  if (n < 1 || !inputFPtrs || !hdf5FPtrs || !options || !channels || !brute_histories || !var_red_histories) {
+    xmi_set_error("xmi_main_msim_batch: invalid arguments");
+    return 0;
+  }
+  if (!ensure_device()) return 0;
+  std::lock_guard<std::mutex> lock(g_batch_lock);
+  const int precision = inputFPtrs[0]->gpu.precision;
+  std::vector<DevState *> st(n);
+  std::vector<xmi::DevTally> tl(n);
+  const auto wall0 = std::chrono::steady_clock::now();
+  for (int c = 0; c < n; c++) {
+    channels[c] = brute_histories[c] = var_red_histories[c] = nullptr;
+    if (inputFPtrs[c]->gpu.precision != precision) {
+      xmi_set_error("xmi_main_msim_batch: configurations %d and 0 differ in precision", c);
+      return 0;
+    }
+    xmi_solid_angle *sa = solid_angles ? solid_angles[c] : nullptr;
+    if (!xmi_gpu_prepare_run(inputFPtrs[c], hdf5FPtrs[c], options[c], 1, sa)) return 0;
+    if (!xmi_dev_sync_tables(hdf5FPtrs[c], precision)) return 0;
+    st[c] = state_of(hdf5FPtrs[c]);
+    const xmi_bundle &h = hdf5FPtrs[c]->b;
+    bool ok = precision == 0 ? stage_run<double>(st[c], st[c]->b64, h, tl[c]) : stage_run<float>(st[c], st[c]->b32, h, tl[c]);
+    if (!ok) return 0;
+  }
+  for (int c = 0; c < n; c++)
+    if (!cuda_ok(cudaStreamSynchronize(st[c]->stream), "staging")) return 0;
+  const int threads = inputFPtrs[0]->gpu.threads_per_block > 0 ? inputFPtrs[0]->gpu.threads_per_block : 128;
+  const int bps = inputFPtrs[0]->gpu.blocks_per_sm > 0 ? inputFPtrs[0]->gpu.blocks_per_sm : 4;
+  Phases ph;
+  bool ok = precision == 0 ? launch_batch<double>(n, st.data(), hdf5FPtrs, tl.data(), threads, bps, true, ph)
+                           : launch_batch<float>(n, st.data(), hdf5FPtrs, tl.data(), threads, bps, true, ph);
+  if (!ok) return 0;
+  for (int c = 0; c < n; c++)
+    if (!collect_outputs(st[c], hdf5FPtrs[c]->b, 1, &channels[c], &brute_histories[c], &var_red_histories[c],
+                         nullptr))
+      return 0;
+  g_timing.transport_ms = ph.total_ms;
+  g_timing.total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - wall0).count();
+  g_timing.launches = ph.launches;
+  for (int k = 0; k < 3; k++) g_timing.phase_ms[k] = ph.ms[k];
+  return 1;
+}

@@ -128,6 +128,20 @@ __device__ __forceinline__ long long queued_events(const unsigned long long *cou
   return n < cap ? n : cap;
 }
 
+/* an event the transport kernel could not have produced is replaced by a
+ * harmless one (and refused by the caller) */
+template <typename R>
+__device__ __forceinline__ bool event_in_range(const DevBundle<R> &b, VrEvent<R> &ev, int n_cfg) {
+  if (ev.layer >= 0 && ev.layer < b.n_layers && ev.n >= 1 && ev.n <= b.N && ev.h_slot < b.n_lines && ev.cfg >= 0 &&
+      ev.cfg < n_cfg)
+    return true;
+  ev.layer = 0;
+  ev.n = 1;
+  ev.h_slot = -1;
+  ev.cfg = 0;
+  return false;
+}
+
 /* events [0, min(*count, cap)) of the queue, visited in `order` */
 template <typename R>
 __global__ void __launch_bounds__(256) estimator_kernel(DevBundle<R> b, DevTally t, const VrEvent<R> *events,
@@ -152,15 +166,11 @@ __global__ void __launch_bounds__(256) estimator_kernel(DevBundle<R> b, DevTally
     long long oi = order[valid ? k : base];
     if (oi < 0 || oi >= n_ev) { oi = 0; valid = false; ok = false; }
     VrEvent<R> ev = events[oi];
-    if (ev.layer < 0 || ev.layer >= b.n_layers || ev.n < 1 || ev.n > b.N || ev.h_slot >= b.n_lines) {
-      /* never produced by the transport kernel: refuse the event, flag the run */
-      ev.layer = 0;
-      ev.n = 1;
-      ev.h_slot = -1;
+    if (!event_in_range(b, ev, 1)) {
       valid = false;
       ok = false;
     }
-    const int key = ev.layer * b.N + ev.n - 1;
+    const int key = vr_key(ev);
     if (__all_sync(0xffffffffu, key == __shfl_sync(0xffffffffu, key, 0)))
       estimate_event<R, true>(b, t, hist, ev, valid, ok);
     else
@@ -174,20 +184,51 @@ __global__ void __launch_bounds__(256) estimator_kernel(DevBundle<R> b, DevTally
   }
 }
 
-/* counting sort of the chunk's events by key = layer * N + n - 1 */
+/* Batched estimator: the configuration of each event selects its bundle and
+ * tallies; histories go straight to the configuration's global table (after
+ * the same warp reduction). */
+template <typename R>
+__global__ void __launch_bounds__(256) estimator_kernel_batch(const DevBundle<R> *bundles, const DevTally *tallies,
+                                                              int n_cfg, const VrEvent<R> *events, const int *order,
+                                                              const unsigned long long *count, long long cap,
+                                                              unsigned long long *flags) {
+  const long long n_ev = queued_events(count, cap);
+  const int lane = threadIdx.x & 31;
+  const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+  bool ok = true;
+  for (long long base = warp * 32; base < n_ev; base += nwarps * 32) {
+    const long long k = base + lane;
+    bool valid = k < n_ev;
+    long long oi = order[valid ? k : base];
+    if (oi < 0 || oi >= n_ev) { oi = 0; valid = false; ok = false; }
+    VrEvent<R> ev = events[oi];
+    if (ev.cfg < 0 || ev.cfg >= n_cfg) { ev.cfg = 0; valid = false; ok = false; }
+    const DevBundle<R> &b = bundles[ev.cfg];
+    if (!event_in_range(b, ev, n_cfg)) { valid = false; ok = false; }
+    const DevTally &t = tallies[ev.cfg];
+    const int key = vr_key(ev);
+    if (__all_sync(0xffffffffu, key == __shfl_sync(0xffffffffu, key, 0)))
+      estimate_event<R, true>(b, t, t.hist_vr, ev, valid, ok);
+    else
+      estimate_event<R, false>(b, t, t.hist_vr, ev, valid, ok);
+  }
+  if (!ok) atomicCAS(flags, 0ull, kErrCompton);
+}
+
+/* counting sort of the chunk's events by key (vr_key): histogram with one
+ * atomic per group of equal keys in a warp, exclusive scan, scatter */
 __global__ void event_key_histogram(const int *key, const unsigned long long *count, long long cap, int nkeys,
                                     unsigned *hist) {
-  __shared__ unsigned h[XMI_MAXL * XMI_MAXN];
-  for (int i = threadIdx.x; i < nkeys; i += blockDim.x) h[i] = 0u;
-  __syncthreads();
   const long long n = queued_events(count, cap);
-  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    const int k = key[i];
-    if (k >= 0 && k < nkeys) atomicAdd(&h[k], 1u);
+  const int lane = threadIdx.x & 31;
+  for (long long base = ((long long)blockIdx.x * blockDim.x + threadIdx.x) & ~31ll; base < n;
+       base += (long long)gridDim.x * blockDim.x) {
+    const long long i = base + lane;
+    const int k = i < n ? key[i] : -1;
+    const unsigned peers = __match_any_sync(0xffffffffu, k);
+    if (k >= 0 && k < nkeys && lane == __ffs(peers) - 1) atomicAdd(&hist[k], (unsigned)__popc(peers));
   }
-  __syncthreads();
-  for (int i = threadIdx.x; i < nkeys; i += blockDim.x)
-    if (h[i]) atomicAdd(&hist[i], h[i]);
 }
 
 /* exclusive scan of the key counts into the scatter cursors; also adds the

@@ -80,6 +80,21 @@ XMI_HD void xmi_rng_init(xmi_rng *g, uint64_t seed, uint64_t id, uint32_t stream
   g->pos = 2;
 }
 
+/* consumes one draw (two words) and returns its first word: the 32 most
+ * significant of the 53 random bits of the uniform xmi_rng_uniform would
+ * have returned */
+XMI_HD uint32_t xmi_rng_word(xmi_rng *g) {
+  uint32_t a;
+  if (g->pos >= 2) {
+    g->buf = xmi_philox4x32_10(g->ctr, g->k0, g->k1);
+    g->ctr.v[0]++;
+    g->pos = 0;
+  }
+  a = g->buf.v[2 * g->pos];
+  g->pos++;
+  return a;
+}
+
 /* uniform double in [0, 1) with 53 random bits */
 XMI_HD double xmi_rng_uniform(xmi_rng *g) {
   uint32_t a, b;

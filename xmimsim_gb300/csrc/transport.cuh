@@ -109,8 +109,9 @@ __device__ __forceinline__ bool plane_step(const double *p, const R *d, const do
 template <typename R> __device__ __forceinline__ R uni(xmi_rng *g);
 template <> __device__ __forceinline__ double uni<double>(xmi_rng *g) { return xmi_rng_uniform(g); }
 template <> __device__ __forceinline__ float uni<float>(xmi_rng *g) {
-  float u = (float)xmi_rng_uniform(g);
-  return u < 1.0f ? u : 0x1.fffffep-1f;
+  /* the same two words as the FP64 draw, truncated to 24 bits: within one
+   * FP32 ulp of the FP64 run's value, without FP64 arithmetic */
+  return (float)(xmi_rng_word(g) >> 8) * 0x1p-24f;
 }
 
 /* energy-grid location, same rule as xmi_grid_locate of the bundle, in the
@@ -429,7 +430,11 @@ __device__ R compton_energy(const DevBundle<R> &b, int e, R E, R theta_i, xmi_rn
     R dlamb = c0 * sth2 * sth2 - c1 * c_lamb0 * sth2 * pz;
     R c_lamb = c_lamb0 + dlamb;
     energy = c / c_lamb / (R)1000;
-    if (energy <= E) return energy;
+    /* the reference accepts when energy <= E; dlamb >= 0 is the same test in
+     * exact arithmetic, and unlike it cannot be defeated by rounding (in FP32
+     * c / (c / E) exceeds E for about half of all E, which near theta = 0
+     * would reject every draw) */
+    if (dlamb >= (R)0) return energy;
     if (varred) {
       if (it == 100) break;
       it++;
@@ -461,7 +466,14 @@ struct __align__(16) VrEvent {
   R rd[XMI_MAXL];    /* density x path length toward the detector point, per layer */
   int node, layer, n, h_slot; /* h_slot >= 0: exciting line of a fluorescence photon */
   long long id;
+  int cfg;           /* configuration of a batched run (0 otherwise) */
 };
+
+/* sort key of an event: configuration, layer, interaction order */
+template <typename R>
+__device__ __forceinline__ int vr_key(const VrEvent<R> &ev) {
+  return (ev.cfg * XMI_MAXL + ev.layer) * XMI_MAXN + ev.n - 1;
+}
 
 template <typename R>
 struct VrQueue {
@@ -842,7 +854,8 @@ __device__ bool check_photon_detector_hit(const DevBundle<R> &b, const Photon<R>
 
 /* ---------------- one history ---------------- */
 template <typename R>
-__device__ bool simulate_photon(const DevBundle<R> &b, Photon<R> &p, const DevTally &t, const VrQueue<R> &vq) {
+__device__ bool simulate_photon(const DevBundle<R> &b, Photon<R> &p, const DevTally &t, const VrQueue<R> &vq,
+                                int cfg) {
   for (int guard = 0; guard < 4 * XMI_MAXN + 8; guard++) {
     if (p.E < (R)kEnergyThreshold) break;
     p.inside = 0;
@@ -950,8 +963,8 @@ __device__ bool simulate_photon(const DevBundle<R> &b, Photon<R> &p, const DevTa
     if (b.use_vr == 1) {
       bool ok = true;
       VrEvent<R> ev;
-      if (vr_prologue(b, p, t, ev, ok) &&
-          !vr_emit(vq, ev, ev.layer * b.N + ev.n - 1)) { set_error(t, kErrQueue); return false; }
+      ev.cfg = cfg;
+      if (vr_prologue(b, p, t, ev, ok) && !vr_emit(vq, ev, vr_key(ev))) { set_error(t, kErrQueue); return false; }
       if (!ok) { set_error(t, kErrTable); return false; }
     }
     /* atom selection and interaction type, src/xmi_main.F90:1556-1652 */
@@ -1100,47 +1113,71 @@ __device__ bool start_photon(const DevBundle<R> &b, const xmi_source_item &it, l
   return true;
 }
 
-/* Transport of the photons with work index [w0, w1): each thread follows
- * one photon from the source to its last interaction; estimator events go to
- * the queue, analog detector hits straight to the brute-force tallies. */
+/* one photon: work index w of the configuration's source items, from the
+ * source to its last interaction; estimator events go to the queue, analog
+ * detector hits straight to the brute-force tallies */
+template <typename R>
+__device__ __forceinline__ void run_photon(const DevBundle<R> &b, const DevTally &t, const VrQueue<R> &vq,
+                                           long long w, int cfg) {
+  /* work index -> (item, index within item) */
+  int lo = 0, hi = b.n_items - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (w >= XMI_LDG(b.item_first, mid, b.n_items, 21)) lo = mid; else hi = mid - 1;
+  }
+  if (!XMI_CHK(lo, b.n_items, 40)) return;
+  const xmi_source_item &it = b.items[lo];
+  const long long j = w - XMI_LDG(b.item_first, lo, b.n_items, 21);
+  Photon<R> p;
+  p.id = it.first + j;
+  p.n_int = 0;
+  p.last = XMI_NO_INTERACTION;
+  p.hit = 0;
+  p.h_type = XMI_NO_INTERACTION;
+  p.h_elem = 0;
+  p.h_slot = 0;
+  p.elem = 0;
+  bool skip;
+  if (!start_photon(b, it, j, p, skip)) { set_error(t, kErrSource); return; }
+  if (skip) return;
+  if (!simulate_photon(b, p, t, vq, cfg)) return;
+  if (p.hit) {
+    if (b.use_vr == 0) tally_channel(b, t, p.n_int, p.E, (double)p.w);
+    if (p.n_int > 0) {
+      int slot = -1;
+      if (p.h_type < 0) slot = p.h_slot;
+      else if (p.h_type == XMI_RAYLEIGH) slot = b.n_lines + 2 * p.h_elem;
+      else if (p.h_type == XMI_COMPTON) slot = b.n_lines + 2 * p.h_elem + 1;
+      if (slot >= 0 && XMI_CHK((long long)(p.n_int - 1) * b.n_slots + slot, (long long)b.N * b.n_slots, 32))
+        atomicAdd(&t.hist_brute[(size_t)(p.n_int - 1) * b.n_slots + slot], (double)p.w);
+    }
+  }
+}
+
+/* Transport of the photons with work index [w0, w1) of one configuration */
 template <typename R>
 __global__ void __launch_bounds__(128) transport_kernel(DevBundle<R> b, DevTally t, VrQueue<R> vq, long long w0,
                                                         long long w1) {
   const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long w = w0 + (long long)blockIdx.x * blockDim.x + threadIdx.x; w < w1; w += stride)
+    run_photon(b, t, vq, w, 0);
+}
+
+/* Batched transport: work indices [w0, w1) of the concatenation of the
+ * configurations' photon ranges (cfg_first[c] = first work index of
+ * configuration c, n_cfg + 1 entries) */
+template <typename R>
+__global__ void __launch_bounds__(128) transport_kernel_batch(const DevBundle<R> *bundles, const DevTally *tallies,
+                                                              const long long *cfg_first, int n_cfg, VrQueue<R> vq,
+                                                              long long w0, long long w1) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
   for (long long w = w0 + (long long)blockIdx.x * blockDim.x + threadIdx.x; w < w1; w += stride) {
-    /* work index -> (item, index within item) */
-    int lo = 0, hi = b.n_items - 1;
+    int lo = 0, hi = n_cfg - 1;
     while (lo < hi) {
       int mid = (lo + hi + 1) >> 1;
-      if (w >= XMI_LDG(b.item_first, mid, b.n_items, 21)) lo = mid; else hi = mid - 1;
+      if (w >= __ldg(cfg_first + mid)) lo = mid; else hi = mid - 1;
     }
-    if (!XMI_CHK(lo, b.n_items, 40)) continue;
-    const xmi_source_item &it = b.items[lo];
-    const long long j = w - XMI_LDG(b.item_first, lo, b.n_items, 21);
-    Photon<R> p;
-    p.id = it.first + j;
-    p.n_int = 0;
-    p.last = XMI_NO_INTERACTION;
-    p.hit = 0;
-    p.h_type = XMI_NO_INTERACTION;
-    p.h_elem = 0;
-    p.h_slot = 0;
-    p.elem = 0;
-    bool skip;
-    if (!start_photon(b, it, j, p, skip)) { set_error(t, kErrSource); continue; }
-    if (skip) continue;
-    if (!simulate_photon(b, p, t, vq)) continue;
-    if (p.hit) {
-      if (b.use_vr == 0) tally_channel(b, t, p.n_int, p.E, (double)p.w);
-      if (p.n_int > 0) {
-        int slot = -1;
-        if (p.h_type < 0) slot = p.h_slot;
-        else if (p.h_type == XMI_RAYLEIGH) slot = b.n_lines + 2 * p.h_elem;
-        else if (p.h_type == XMI_COMPTON) slot = b.n_lines + 2 * p.h_elem + 1;
-        if (slot >= 0 && XMI_CHK((long long)(p.n_int - 1) * b.n_slots + slot, (long long)b.N * b.n_slots, 32))
-          atomicAdd(&t.hist_brute[(size_t)(p.n_int - 1) * b.n_slots + slot], (double)p.w);
-      }
-    }
+    run_photon(bundles[lo], tallies[lo], vq, w - __ldg(cfg_first + lo), lo);
   }
 }
 

@@ -247,6 +247,31 @@ class Simulation:
                "raw": (ch, br, vr)}
         return out
 
+    @staticmethod
+    def msim_batch(sims: "Sequence[Simulation]") -> list[dict]:
+        """Runs several configurations in one batched launch sequence
+        (xmi_main_msim_batch); one output dict per configuration, as msim()."""
+        lib = abi.load()
+        n = len(sims)
+        ins = (C.c_void_p * n)(*[s.inputF.value for s in sims])
+        tabs = (C.c_void_p * n)(*[s.tables.value for s in sims])
+        opts = (C.POINTER(abi.XmiMainOptions) * n)(*[C.pointer(s.options) for s in sims])
+        sas = (C.POINTER(abi.XmiSolidAngle) * n)(
+            *[s.solid_angle() if s.options.use_variance_reduction else C.POINTER(abi.XmiSolidAngle)() for s in sims])
+        ch = (abi.c_double_p * n)()
+        br = (abi.c_double_p * n)()
+        vr = (abi.c_double_p * n)()
+        _check(lib.xmi_main_msim_batch(n, ins, tabs, opts, sas, ch, br, vr), "xmi_main_msim_batch")
+        outs = []
+        for i, s in enumerate(sims):
+            N = s.spec.n_interactions_trajectory
+            nch = s.spec.nchannels
+            outs.append({"channels": np.ctypeslib.as_array(ch[i], ((N + 1), nch)).copy(),
+                         "brute": np.ctypeslib.as_array(br[i], (100, 385, N)).copy(),
+                         "var_red": np.ctypeslib.as_array(vr[i], (100, 385, N)).copy() if vr[i] else None,
+                         "raw": (ch[i], br[i], vr[i])})
+        return outs
+
     def free_raw(self, out: dict) -> None:
         for p in out.pop("raw", ()):
             if p:
