@@ -539,10 +539,13 @@ static bool run_chunks(cudaStream_t st, EventQueue &q, long long n, int N, int n
     vq.cap = chunk * N;
   }
   std::vector<cudaEvent_t> marks;
+  /* under stream capture an event record must be marked external to become a
+   * real record when the graph runs (so that it can be timed and waited on) */
   auto mark = [&]() {
     cudaEvent_t e;
     cudaEventCreate(&e);
-    cudaEventRecord(e, st);
+    if (graph) cudaEventRecordWithFlags(e, st, cudaEventRecordExternal);
+    else cudaEventRecord(e, st);
     marks.push_back(e);
   };
   int launches = 0;
