@@ -330,8 +330,12 @@ __device__ R get_solid_angle(const DevBundle<R> &b, const double *coords, const 
   if (tt > (R)(kPi / 2.0)) tt = (R)kPi - tt;
   R theta = (R)(kPi / 2.0) - tt;
   if (theta < (R)b.sa_t[0]) return (R)0;
+  /* theta <= pi/2 by construction; in FP32, pi/2 itself rounds above the
+   * axis end (the FP64 pi/2), which would send every point on the detector
+   * axis to the Monte Carlo fallback */
+  const double th = fmin((double)theta, b.sa_t[b.sa_nt - 1]);
   int p1 = findpos_u<double>(b.sa_r, b.sa_nr, (double)r, b.sa_r0, b.sa_rinv);
-  int p2 = findpos_u<double>(b.sa_t, b.sa_nt, (double)theta, b.sa_t0, b.sa_tinv);
+  int p2 = findpos_u<double>(b.sa_t, b.sa_nt, th, b.sa_t0, b.sa_tinv);
   if (p1 == -1 || p2 == -1) {
     xmi_rng g;
     xmi_rng_init(&g, b.seed, (uint64_t)p.id, 0x80000000u | (uint32_t)p.n_int);
@@ -340,7 +344,7 @@ __device__ R get_solid_angle(const DevBundle<R> &b, const double *coords, const 
   }
   /* bilinear on the grid; axes are FP64, values in R */
   double a0 = b.sa_r[p1], a1 = b.sa_r[p1 + 1], b0 = b.sa_t[p2], b1 = b.sa_t[p2 + 1];
-  double x1 = (double)r, x2 = (double)theta;
+  double x1 = (double)r, x2 = th;
   R denom = (R)((a1 - a0) * (b1 - b0));
   R c1 = (R)((a1 - x1) * (b1 - x2)) / denom;
   R c2 = (R)((x1 - a0) * (b1 - x2)) / denom;
