@@ -187,6 +187,7 @@ typedef struct {
   int *ent_shell;        /* [n_ent] 0..8 */
   double *ent_coef;      /* [n_ent] FluorYield(Z, shell) x RadRate(Z, line) */
   double *ent_pmu;       /* [n_ent][XMI_MAXL] precalc_mu of every layer at the line energy (0 beyond n_layers) */
+  int stage_max;         /* max over layers of (line entries + 2 x elements): history slots one layer feeds */
 } xmi_bundle;
 
 /* Evaluation rule of every energy table of the bundle: E is located in the

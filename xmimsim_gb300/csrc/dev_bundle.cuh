@@ -50,7 +50,7 @@ struct DevBundle {
   const double *sa_r, *sa_t;
   const R *sa_grid;
   /* estimator line lists per (layer, element) pair */
-  int n_ent;
+  int n_ent, stage_max;
   const int *ent_off, *ent_slot, *ent_shell;
   const R *ent_coef, *ent_pmu;
 };

@@ -56,7 +56,7 @@ struct EventQueue {
   void *events = nullptr;
   int *key = nullptr, *order = nullptr;
   unsigned *hist = nullptr; /* [2][nkeys]: counts, then scatter cursors */
-  unsigned long long *count = nullptr;
+  unsigned long long *count = nullptr; /* [0] events queued, [1] estimator work counter */
   size_t bytes = 0;
   long long cap = 0;
   int nkeys = 0;
@@ -88,6 +88,8 @@ struct DevState {
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   EventQueue q; /* estimator event queue of one chunk */
+  void *d_bundle = nullptr;      /* device copy of the run's DevBundle (estimator argument) */
+  xmi::DevTally *d_tally = nullptr;
 };
 
 template <typename R>
@@ -140,6 +142,7 @@ void fill_scalars(const xmi_bundle &h, xmi::DevBundle<R> &d) {
   d.n_items = h.n_items;
   d.n_layer_el = h.n_layer_el;
   d.n_ent = h.n_ent;
+  d.stage_max = h.stage_max;
   d.coll_present = h.coll_present;
   d.seed = h.seed;
   d.n_photons_total = h.n_photons_total;
@@ -288,6 +291,8 @@ void xmi_dev_free_tables(struct xmi_tables_handle *t) {
   cudaFree(s->tally);
   cudaFree(s->counters);
   s->q.release();
+  cudaFree(s->d_bundle);
+  cudaFree(s->d_tally);
   if (s->ev0) cudaEventDestroy(s->ev0);
   if (s->ev1) cudaEventDestroy(s->ev1);
   if (s->stream) cudaStreamDestroy(s->stream);
@@ -507,7 +512,7 @@ static bool ensure_queue(EventQueue &q, long long cap, int nkeys) {
     if (!cuda_ok(cudaMalloc(&q.hist, 2 * sizeof(unsigned) * nkeys), "cudaMalloc key histogram")) return false;
     q.nkeys = nkeys;
   }
-  if (!q.count && !cuda_ok(cudaMalloc(&q.count, sizeof(unsigned long long)), "cudaMalloc")) return false;
+  if (!q.count && !cuda_ok(cudaMalloc(&q.count, 2 * sizeof(unsigned long long)), "cudaMalloc")) return false;
   return true;
 }
 
@@ -568,8 +573,9 @@ static bool run_chunks(cudaStream_t st, EventQueue &q, long long n, int N, int n
       xmi::event_key_histogram<<<sms * 4, 256, 0, st>>>(q.key, q.count, vq.cap, nkeys, q.hist);
       xmi::event_key_scan<<<1, 32, 0, st>>>(q.hist, nkeys, q.hist + nkeys, q.count, total_events);
       xmi::event_key_scatter<<<sms * 4, 256, 0, st>>>(q.key, q.count, vq.cap, nkeys, q.hist + nkeys, q.order);
+      cudaMemsetAsync(q.count + 1, 0, sizeof(unsigned long long), st);
       mark();
-      estimator(vq, (const int *)q.order);
+      estimator(vq, (const int *)q.order, q.count + 1);
       mark();
       launches += 4;
     }
@@ -682,29 +688,47 @@ static bool stage_run(DevState *s, xmi::DevBundle<R> &d, const xmi_bundle &h, xm
   return true;
 }
 
+/* stage rows of the estimator: values per warp row, capped so that the eight
+ * rows of a CTA fit shared memory (layers that need more run per-lane) */
+template <typename R>
+static int stage_cap_for(int stage_max) {
+  const int limit = (int)(200 * 1024 / (8 * sizeof(R)));
+  return stage_max < limit ? stage_max : limit;
+}
+
+template <typename R>
+static int estimator_blocks(int stage_cap, size_t *smem) {
+  *smem = (size_t)8 * stage_cap * sizeof(R);
+  if (*smem > 48 * 1024)
+    cudaFuncSetAttribute(xmi::estimator_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)*smem);
+  int per_sm = 1;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, xmi::estimator_kernel<R>, 256, *smem);
+  if (per_sm < 1) per_sm = 1;
+  return num_sms() * per_sm;
+}
+
 /* one configuration on its handle's stream */
 template <typename R>
 static bool launch_single(DevState *s, xmi::DevBundle<R> &d, const xmi::DevTally &tl, const xmi_bundle &h,
                           int threads, int blocks_per_sm, Phases &ph) {
   const int sms = num_sms();
-  const size_t nh = (size_t)h.n_interactions * h.n_slots;
-  size_t smem = nh * sizeof(double);
-  const int use_smem = (h.use_vr && smem <= 200 * 1024) ? 1 : 0;
-  if (use_smem && smem > 48 * 1024)
-    cudaFuncSetAttribute(xmi::estimator_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (!use_smem) smem = 0;
-  int est_per_sm = 1;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&est_per_sm, xmi::estimator_kernel<R>, 256, smem);
-  if (est_per_sm < 1) est_per_sm = 1;
-  const int est_blocks = sms * est_per_sm;
+  if (!s->d_bundle && !cuda_ok(cudaMalloc(&s->d_bundle, sizeof(xmi::DevBundle<double>)), "cudaMalloc")) return false;
+  if (!s->d_tally && !cuda_ok(cudaMalloc(&s->d_tally, sizeof(xmi::DevTally)), "cudaMalloc")) return false;
+  cudaMemcpyAsync(s->d_bundle, &d, sizeof(d), cudaMemcpyHostToDevice, s->stream);
+  cudaMemcpyAsync(s->d_tally, &tl, sizeof(tl), cudaMemcpyHostToDevice, s->stream);
+  const int stage_cap = stage_cap_for<R>(h.stage_max);
+  size_t smem = 0;
+  const int est_blocks = estimator_blocks<R>(stage_cap, &smem);
   auto transport = [&](long long w0, long long w1, const xmi::VrQueue<R> &vq) {
     long long blocks = (long long)sms * blocks_per_sm;
     if (blocks * threads > w1 - w0) blocks = (w1 - w0 + threads - 1) / threads;
     if (blocks < 1) blocks = 1;
     xmi::transport_kernel<R><<<(int)blocks, threads, 0, s->stream>>>(d, tl, vq, w0, w1);
   };
-  auto estimator = [&](const xmi::VrQueue<R> &vq, const int *order) {
-    xmi::estimator_kernel<R><<<est_blocks, 256, smem, s->stream>>>(d, tl, vq.ev, order, vq.count, vq.cap, use_smem);
+  auto estimator = [&](const xmi::VrQueue<R> &vq, const int *order, unsigned long long *work) {
+    xmi::estimator_kernel<R><<<est_blocks, 256, smem, s->stream>>>(
+        (const xmi::DevBundle<R> *)s->d_bundle, s->d_tally, 1, vq.ev, order, vq.count, vq.cap, work, stage_cap,
+        &s->counters[1]);
   };
   return run_chunks<R>(s->stream, s->q, h.n_photons_total, h.n_interactions, XMI_MAXL * XMI_MAXN, h.use_vr != 0,
                        &s->counters[3], transport, estimator, ph);
@@ -863,19 +887,20 @@ bool launch_batch(int n, DevState **st, xmi_hdf5FPtr *t, const xmi::DevTally *tl
   cudaMemsetAsync(B.flags, 0, 2 * sizeof(unsigned long long), B.stream);
   const xmi::DevBundle<R> *db = (const xmi::DevBundle<R> *)B.bundles;
   const int sms = num_sms();
-  int est_per_sm = 1;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&est_per_sm, xmi::estimator_kernel_batch<R>, 256, 0);
-  if (est_per_sm < 1) est_per_sm = 1;
-  const int est_blocks = sms * est_per_sm;
+  int stage_max = 1;
+  for (int c = 0; c < n; c++) stage_max = t[c]->b.stage_max > stage_max ? t[c]->b.stage_max : stage_max;
+  const int stage_cap = stage_cap_for<R>(stage_max);
+  size_t smem = 0;
+  const int est_blocks = estimator_blocks<R>(stage_cap, &smem);
   auto transport = [&](long long w0, long long w1, const xmi::VrQueue<R> &vq) {
     long long blocks = (long long)sms * blocks_per_sm;
     if (blocks * threads > w1 - w0) blocks = (w1 - w0 + threads - 1) / threads;
     if (blocks < 1) blocks = 1;
     xmi::transport_kernel_batch<R><<<(int)blocks, threads, 0, B.stream>>>(db, B.tallies, B.cfg_first, n, vq, w0, w1);
   };
-  auto estimator = [&](const xmi::VrQueue<R> &vq, const int *order) {
-    xmi::estimator_kernel_batch<R><<<est_blocks, 256, 0, B.stream>>>(db, B.tallies, n, vq.ev, order, vq.count, vq.cap,
-                                                                    B.flags);
+  auto estimator = [&](const xmi::VrQueue<R> &vq, const int *order, unsigned long long *work) {
+    xmi::estimator_kernel<R><<<est_blocks, 256, smem, B.stream>>>(db, B.tallies, n, vq.ev, order, vq.count, vq.cap,
+                                                                  work, stage_cap, B.flags);
   };
   if (!run_chunks<R>(B.stream, B.q, first[n], N, n * XMI_MAXL * XMI_MAXN, vr, &B.flags[1], transport, estimator, ph,
                      graph))

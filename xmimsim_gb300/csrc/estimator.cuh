@@ -30,20 +30,6 @@ __device__ __forceinline__ R warp_sum_r(R v) {
   return v;
 }
 
-/* adds one contribution per lane to history slot `idx` (the same for every
- * lane when Uniform) */
-template <typename R, bool Uniform>
-__device__ __forceinline__ void hist_add(double *hist, long long idx, R v) {
-  if (Uniform) {
-    if (__any_sync(0xffffffffu, v != (R)0)) {
-      R s = warp_sum_r(v);
-      if ((threadIdx.x & 31) == 0) atomicAdd(&hist[idx], (double)s);
-    }
-  } else if (v != (R)0) {
-    atomicAdd(&hist[idx], (double)v);
-  }
-}
-
 template <typename R>
 __device__ __forceinline__ void chan_add(const DevBundle<R> &b, const DevTally &t, int n, R E, R w) {
   if (w == (R)0 || E < (R)kEnergyThreshold) return;
@@ -52,12 +38,75 @@ __device__ __forceinline__ void chan_add(const DevBundle<R> &b, const DevTally &
     atomicAdd(&t.chan[(size_t)n * b.nch + ch], (double)w);
 }
 
+/* History contributions of the events of one key (configuration, layer,
+ * order) are summed across the warp and staged in a warp-private
+ * shared-memory row, stage[j]: j < n_line = the layer's line entries (entry
+ * k at j = k - first entry of the layer), then 2 i / 2 i + 1 = Rayleigh /
+ * Compton of the layer's i-th element.  The row is flushed to the FP64
+ * history table (one atomic per non-zero slot) when the warp's key changes. */
+template <typename R>
+struct StageRow {
+  R *v;
+  int key = -1, layer = 0, n = 1, k_first = 0, n_line = 0, size = 0;
+};
+
+template <typename R>
+__device__ __forceinline__ void stage_open(const DevBundle<R> &b, StageRow<R> &st, int key, int layer, int n) {
+  const int off = b.off[layer], nel = b.nel[layer];
+  st.key = key;
+  st.layer = layer;
+  st.n = n;
+  st.k_first = XMI_LDG(b.ent_off, off, b.n_layer_el + 1, 15);
+  st.n_line = XMI_LDG(b.ent_off, off + nel, b.n_layer_el + 1, 15) - st.k_first;
+  st.size = st.n_line + 2 * nel;
+}
+
+template <typename R>
+__device__ __forceinline__ void stage_flush(const DevBundle<R> &b, const DevTally &t, StageRow<R> &st) {
+  __syncwarp();
+  if (st.key >= 0) {
+    const long long hbase = (long long)(st.n - 1) * b.n_slots;
+    const int off = b.off[st.layer];
+    for (int j = threadIdx.x & 31; j < st.size; j += 32) {
+      const R v = st.v[j];
+      if (v == (R)0) continue;
+      st.v[j] = (R)0;
+      int slot;
+      if (j < st.n_line) {
+        slot = XMI_LDG(b.ent_slot, st.k_first + j, b.n_ent, 16);
+      } else {
+        const int q = j - st.n_line;
+        slot = b.n_lines + 2 * XMI_LDG(b.layer_el, off + q / 2, b.n_layer_el, 9) + (q & 1);
+      }
+      if (XMI_CHK(hbase + slot, (long long)b.N * b.n_slots, 31)) atomicAdd(&t.hist_vr[hbase + slot], (double)v);
+    }
+  }
+  __syncwarp();
+  st.key = -1;
+}
+
+/* one contribution per lane to stage position j (Uniform: the same j in every
+ * lane, warp-summed into the stage) or history slot `slot` (per-lane atomic) */
 template <typename R, bool Uniform>
-__device__ void estimate_event(const DevBundle<R> &b, const DevTally &t, double *hist, const VrEvent<R> &ev,
+__device__ __forceinline__ void contribute(const DevTally &t, const StageRow<R> &st, int j, long long slot, R v) {
+  if (Uniform) {
+    if (__any_sync(0xffffffffu, v != (R)0)) {
+      const R s = warp_sum_r(v);
+      if ((threadIdx.x & 31) == 0) st.v[j] += s;
+    }
+  } else if (v != (R)0) {
+    atomicAdd(&t.hist_vr[slot], (double)v);
+  }
+}
+
+template <typename R, bool Uniform>
+__device__ void estimate_event(const DevBundle<R> &b, const DevTally &t, const StageRow<R> &st, const VrEvent<R> &ev,
                                bool valid, bool &ok) {
   const int layer = ev.layer, n = ev.n;
   const int nel = b.nel[layer], off = b.off[layer];
   const long long hbase = (long long)(n - 1) * b.n_slots;
+  const int k_first = XMI_LDG(b.ent_off, off, b.n_layer_el + 1, 15);
+  const int n_line = XMI_LDG(b.ent_off, off + nel, b.n_layer_el + 1, 15) - k_first;
   const R live = valid ? (R)1 : (R)0;
   for (int i = 0; i < nel; i++) {
     const int pair = off + i;
@@ -67,7 +116,7 @@ __device__ void estimate_event(const DevBundle<R> &b, const DevTally &t, double 
     const int rs = b.n_lines + 2 * e;
     /* Rayleigh */
     const R twr = live * (pconv * (ev.pR * qtab(b.ff2 + (size_t)e * XMI_NQ, ev.q)) * ev.pesc_rayl * ev.w);
-    hist_add<R, Uniform>(hist, hbase + rs, twr);
+    contribute<R, Uniform>(t, st, n_line + 2 * i, hbase + rs, twr);
     if (valid) chan_add(b, t, n, ev.E, twr);
     /* Compton: one Doppler-broadened energy per element (N_COMPTON_VARRED = 1) */
     xmi_rng g;
@@ -85,7 +134,7 @@ __device__ void estimate_event(const DevBundle<R> &b, const DevTally &t, double 
     } else if (valid) {
       ok = false;
     }
-    hist_add<R, Uniform>(hist, hbase + rs + 1, twc);
+    contribute<R, Uniform>(t, st, n_line + 2 * i + 1, hbase + rs + 1, twc);
     if (valid) chan_add(b, t, n, ec, twc);
     /* fluorescence: shell probabilities at the photon energy (first order or
      * after scattering) or at the exciting line's energy (after fluorescence) */
@@ -116,7 +165,7 @@ __device__ void estimate_event(const DevBundle<R> &b, const DevTally &t, double 
       for (int j = 0; j < XMI_MAXL; j++)
         murhod += XMI_LDG(b.ent_pmu, (long long)k * XMI_MAXL + j, (long long)b.n_ent * XMI_MAXL, 17) * ev.rd[j];
       const R tw = ps * XMI_LDG(b.ent_coef, k, b.n_ent, 16) * scale * exp(-murhod);
-      hist_add<R, Uniform>(hist, hbase + sl, tw);
+      contribute<R, Uniform>(t, st, k - k_first, hbase + sl, tw);
     }
   }
 }
@@ -142,77 +191,65 @@ __device__ __forceinline__ bool event_in_range(const DevBundle<R> &b, VrEvent<R>
   return false;
 }
 
-/* events [0, min(*count, cap)) of the queue, visited in `order` */
-template <typename R>
-__global__ void __launch_bounds__(256) estimator_kernel(DevBundle<R> b, DevTally t, const VrEvent<R> *events,
-                                                        const int *order, const unsigned long long *count,
-                                                        long long cap, int use_smem) {
-  extern __shared__ double s_hist[];
-  const int nh = b.N * b.n_slots;
-  if (use_smem) {
-    for (int i = threadIdx.x; i < nh; i += blockDim.x) s_hist[i] = 0.0;
-    __syncthreads();
-  }
-  double *hist = use_smem ? s_hist : t.hist_vr;
-  const long long n_ev = queued_events(count, cap);
-  const int lane = threadIdx.x & 31;
-  const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
-  bool ok = true;
-  for (long long base = warp * 32; base < n_ev; base += nwarps * 32) {
-    const long long k = base + lane;
-    bool valid = k < n_ev;
-    /* lanes past the end carry the warp's first event with zero weight */
-    long long oi = order[valid ? k : base];
-    if (oi < 0 || oi >= n_ev) { oi = 0; valid = false; ok = false; }
-    VrEvent<R> ev = events[oi];
-    if (!event_in_range(b, ev, 1)) {
-      valid = false;
-      ok = false;
-    }
-    const int key = vr_key(ev);
-    if (__all_sync(0xffffffffu, key == __shfl_sync(0xffffffffu, key, 0)))
-      estimate_event<R, true>(b, t, hist, ev, valid, ok);
-    else
-      estimate_event<R, false>(b, t, hist, ev, valid, ok);
-  }
-  if (!ok) set_error(t, kErrCompton);
-  if (use_smem) {
-    __syncthreads();
-    for (int i = threadIdx.x; i < nh; i += blockDim.x)
-      if (s_hist[i] != 0.0) atomicAdd(&t.hist_vr[i], s_hist[i]);
-  }
-}
+/* events per work grab of a warp: consecutive in the sorted order, so a
+ * warp's stage row keeps its key across grabs */
+constexpr int kEventsPerGrab = 256;
 
-/* Batched estimator: the configuration of each event selects its bundle and
- * tallies; histories go straight to the configuration's global table (after
- * the same warp reduction). */
+/* Estimator over the events [0, min(*count, cap)) of the queue in `order`;
+ * bundles[cfg] / tallies[cfg] of each event's configuration (one entry when
+ * not batched).  Warps grab kEventsPerGrab consecutive events at a time from
+ * the counter `work`; stage rows of stage_cap values per warp sit in dynamic
+ * shared memory. */
 template <typename R>
-__global__ void __launch_bounds__(256) estimator_kernel_batch(const DevBundle<R> *bundles, const DevTally *tallies,
-                                                              int n_cfg, const VrEvent<R> *events, const int *order,
-                                                              const unsigned long long *count, long long cap,
-                                                              unsigned long long *flags) {
-  const long long n_ev = queued_events(count, cap);
+__global__ void __launch_bounds__(256, 2) estimator_kernel(const DevBundle<R> *bundles, const DevTally *tallies,
+                                                           int n_cfg, const VrEvent<R> *events, const int *order,
+                                                           const unsigned long long *count, long long cap,
+                                                           unsigned long long *work, int stage_cap,
+                                                           unsigned long long *flags) {
+  extern __shared__ unsigned char stage_mem[];
+  StageRow<R> st;
+  st.v = (R *)stage_mem + (size_t)(threadIdx.x >> 5) * stage_cap;
   const int lane = threadIdx.x & 31;
-  const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+  for (int j = lane; j < stage_cap; j += 32) st.v[j] = (R)0;
+  __syncwarp();
+  int st_cfg = 0;
+  const long long n_ev = queued_events(count, cap);
   bool ok = true;
-  for (long long base = warp * 32; base < n_ev; base += nwarps * 32) {
-    const long long k = base + lane;
-    bool valid = k < n_ev;
-    long long oi = order[valid ? k : base];
-    if (oi < 0 || oi >= n_ev) { oi = 0; valid = false; ok = false; }
-    VrEvent<R> ev = events[oi];
-    if (ev.cfg < 0 || ev.cfg >= n_cfg) { ev.cfg = 0; valid = false; ok = false; }
-    const DevBundle<R> &b = bundles[ev.cfg];
-    if (!event_in_range(b, ev, n_cfg)) { valid = false; ok = false; }
-    const DevTally &t = tallies[ev.cfg];
-    const int key = vr_key(ev);
-    if (__all_sync(0xffffffffu, key == __shfl_sync(0xffffffffu, key, 0)))
-      estimate_event<R, true>(b, t, t.hist_vr, ev, valid, ok);
-    else
-      estimate_event<R, false>(b, t, t.hist_vr, ev, valid, ok);
+  for (;;) {
+    unsigned long long grab = 0;
+    if (lane == 0) grab = atomicAdd(work, (unsigned long long)kEventsPerGrab);
+    grab = __shfl_sync(0xffffffffu, grab, 0);
+    if ((long long)grab >= n_ev) break;
+    for (int sub = 0; sub < kEventsPerGrab; sub += 32) {
+      const long long base = (long long)grab + sub;
+      if (base >= n_ev) break;
+      const long long k = base + lane;
+      bool valid = k < n_ev;
+      /* lanes past the end carry the warp's first event with zero weight */
+      long long oi = order[valid ? k : base];
+      if (oi < 0 || oi >= n_ev) { oi = 0; valid = false; ok = false; }
+      VrEvent<R> ev = events[oi];
+      if (ev.cfg < 0 || ev.cfg >= n_cfg) { ev.cfg = 0; valid = false; ok = false; }
+      const DevBundle<R> &b = bundles[ev.cfg];
+      if (!event_in_range(b, ev, n_cfg)) { valid = false; ok = false; }
+      const DevTally &t = tallies[ev.cfg];
+      const int key = vr_key(ev);
+      if (__all_sync(0xffffffffu, key == __shfl_sync(0xffffffffu, key, 0))) {
+        if (key != st.key) {
+          stage_flush(bundles[st_cfg], tallies[st_cfg], st);
+          if (b.stage_max <= stage_cap) {
+            stage_open(b, st, key, ev.layer, ev.n);
+            st_cfg = ev.cfg;
+          }
+        }
+        if (st.key == key) estimate_event<R, true>(b, t, st, ev, valid, ok);
+        else estimate_event<R, false>(b, t, st, ev, valid, ok);
+      } else {
+        estimate_event<R, false>(b, t, st, ev, valid, ok);
+      }
+    }
   }
+  stage_flush(bundles[st_cfg], tallies[st_cfg], st);
   if (!ok) atomicCAS(flags, 0ull, kErrCompton);
 }
 

@@ -1001,6 +1001,12 @@ int xmi_bundle_build(struct xmi_input_handle *in, struct xmi_tables_handle *t,
         n++;
       }
     }
+    b->stage_max = 1;
+    for (j = 0; j < b->n_layers; j++) {
+      int o = b->layer_off[j], ne = b->layer_nel[j];
+      int m = b->ent_off[o + ne] - b->ent_off[o] + 2 * ne;
+      if (m > b->stage_max) b->stage_max = m;
+    }
   }
 
   /* angular tables */
