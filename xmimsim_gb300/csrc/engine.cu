@@ -16,6 +16,7 @@
 #include "estimator.cuh"
 #include "solid_angle.cuh"
 #include "transport.cuh"
+#include "wavefront.cuh"
 #include "xmi_internal.h"
 
 long hits_per_single = 5000; /* src/xmi_solid_angle_f.F90:43-44 */
@@ -70,6 +71,21 @@ struct EventQueue {
   }
 };
 
+/* photon states and lists of the wavefront transport of one chunk */
+struct WfBuffers {
+  void *st = nullptr;
+  int *lists = nullptr; /* 5 lists of cap entries */
+  unsigned *count = nullptr;
+  size_t st_bytes = 0;
+  long long cap = 0;
+  void release() {
+    cudaFree(st);
+    cudaFree(lists);
+    cudaFree(count);
+    *this = WfBuffers();
+  }
+};
+
 struct DevState {
   DevSide d64, d32;
   xmi::DevBundle<double> b64;
@@ -88,6 +104,7 @@ struct DevState {
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   EventQueue q; /* estimator event queue of one chunk */
+  WfBuffers wf; /* wavefront transport state of one chunk */
   void *d_bundle = nullptr;      /* device copy of the run's DevBundle (estimator argument) */
   xmi::DevTally *d_tally = nullptr;
 };
@@ -291,6 +308,7 @@ void xmi_dev_free_tables(struct xmi_tables_handle *t) {
   cudaFree(s->tally);
   cudaFree(s->counters);
   s->q.release();
+  s->wf.release();
   cudaFree(s->d_bundle);
   cudaFree(s->d_tally);
   if (s->ev0) cudaEventDestroy(s->ev0);
@@ -486,6 +504,56 @@ int xmi_gpu_prepare_run(xmi_inputFPtr in, xmi_hdf5FPtr t, xmi_main_options *opti
 /* events held on the device per chunk; a chunk is as many photons as can
  * each make N estimator events (one per interaction) within it */
 constexpr long long kMaxQueuedEvents = 1ll << 25;
+/* photons per chunk without variance reduction (wavefront state ~170 B each) */
+constexpr long long kMaxChunkPhotons = 1ll << 23;
+
+template <typename R>
+static bool ensure_wf(WfBuffers &wb, long long cap) {
+  const size_t bytes = (size_t)cap * sizeof(xmi::WfPhoton<R>);
+  if (bytes <= wb.st_bytes && cap <= wb.cap) return true;
+  wb.release();
+  if (!cuda_ok(cudaMalloc(&wb.st, bytes), "cudaMalloc photon states") ||
+      !cuda_ok(cudaMalloc(&wb.lists, sizeof(int) * 5 * cap), "cudaMalloc photon lists") ||
+      !cuda_ok(cudaMalloc(&wb.count, sizeof(unsigned) * 5), "cudaMalloc"))
+    return false;
+  wb.st_bytes = bytes;
+  wb.cap = cap;
+  return true;
+}
+
+/* the wavefront transport of work indices [w0, w1): start, then max_iter
+ * rounds of step + the three interaction kernels; returns the launches */
+template <typename R, bool Batched>
+static int launch_wavefront(cudaStream_t st, WfBuffers &wb, const xmi::DevBundle<R> &b0, const xmi::DevTally &t0,
+                            const xmi::DevBundle<R> *bundles, const xmi::DevTally *tallies, const long long *cfg_first,
+                            int n_cfg, long long w0, long long w1, int max_iter, const xmi::VrQueue<R> &vq,
+                            int threads, int blocks) {
+  const long long cap = wb.cap;
+  xmi::WfLists q;
+  q.active[0] = wb.lists;
+  q.active[1] = wb.lists + cap;
+  for (int k = 0; k < 3; k++) q.inter[k] = wb.lists + (2 + k) * cap;
+  q.count = wb.count;
+  xmi::WfPhoton<R> *ps = (xmi::WfPhoton<R> *)wb.st;
+  cudaMemsetAsync(wb.count, 0, sizeof(unsigned) * 5, st);
+  xmi::wf_start<R, Batched><<<blocks, threads, 0, st>>>(b0, t0, bundles, tallies, cfg_first, n_cfg, w0, w1, ps, q);
+  int launches = 1, cur = 0;
+  for (int it = 0; it < max_iter; it++) {
+    const int next = cur ^ 1;
+    xmi::wf_reset<<<1, 32, 0, st>>>(q, next);
+    xmi::wf_step<R, Batched><<<blocks, threads, 0, st>>>(b0, t0, bundles, tallies, ps, q, cur, cap, vq);
+    for (int k = 0; k < 3; k++)
+      xmi::wf_interact<R, Batched><<<blocks, threads, 0, st>>>(b0, t0, bundles, tallies, ps, q, k, next, cap);
+    launches += 5;
+    cur = next;
+  }
+  return launches;
+}
+
+/* rounds of the wavefront: with variance reduction every photon interacts at
+ * most N times (N + 1 steps); analog histories end within the guard of the
+ * history loop */
+static int wavefront_rounds(const xmi_bundle &h) { return h.use_vr ? h.n_interactions + 1 : 4 * XMI_MAXN + 8; }
 
 template <typename R>
 static bool ensure_queue(EventQueue &q, long long cap, int nkeys) {
@@ -531,7 +599,8 @@ static bool run_chunks(cudaStream_t st, EventQueue &q, long long n, int N, int n
                        unsigned long long *total_events, TF &&transport, EF &&estimator, Phases &ph,
                        bool graph = false) {
   const int sms = num_sms();
-  long long chunk = n > 0 ? n : 1;
+  long long chunk = n < kMaxChunkPhotons ? n : kMaxChunkPhotons;
+  if (chunk < 1) chunk = 1;
   xmi::VrQueue<R> vq{nullptr, nullptr, nullptr, 0};
   if (vr) {
     chunk = kMaxQueuedEvents / (N > 0 ? N : 1);
@@ -564,8 +633,7 @@ static bool run_chunks(cudaStream_t st, EventQueue &q, long long n, int N, int n
       cudaMemsetAsync(q.count, 0, sizeof(unsigned long long), st);
       cudaMemsetAsync(q.hist, 0, sizeof(unsigned) * nkeys, st);
     }
-    transport(w0, w1, vq);
-    launches++;
+    launches += transport(w0, w1, vq);
     mark();
     if (vr) {
       /* positions of events whose key the sort would skip stay -1 and are refused by the estimator */
@@ -719,11 +787,15 @@ static bool launch_single(DevState *s, xmi::DevBundle<R> &d, const xmi::DevTally
   const int stage_cap = stage_cap_for<R>(h.stage_max);
   size_t smem = 0;
   const int est_blocks = estimator_blocks<R>(stage_cap, &smem);
+  const long long chunk_cap = h.use_vr ? kMaxQueuedEvents / (h.n_interactions > 0 ? h.n_interactions : 1)
+                                       : kMaxChunkPhotons;
+  if (!ensure_wf<R>(s->wf, h.n_photons_total < chunk_cap ? (h.n_photons_total > 0 ? h.n_photons_total : 1)
+                                                           : chunk_cap))
+    return false;
+  const int rounds = wavefront_rounds(h);
   auto transport = [&](long long w0, long long w1, const xmi::VrQueue<R> &vq) {
-    long long blocks = (long long)sms * blocks_per_sm;
-    if (blocks * threads > w1 - w0) blocks = (w1 - w0 + threads - 1) / threads;
-    if (blocks < 1) blocks = 1;
-    xmi::transport_kernel<R><<<(int)blocks, threads, 0, s->stream>>>(d, tl, vq, w0, w1);
+    return launch_wavefront<R, false>(s->stream, s->wf, d, tl, nullptr, nullptr, nullptr, 1, w0, w1, rounds, vq,
+                                      threads, sms * blocks_per_sm);
   };
   auto estimator = [&](const xmi::VrQueue<R> &vq, const int *order, unsigned long long *work) {
     xmi::estimator_kernel<R><<<est_blocks, 256, smem, s->stream>>>(
@@ -806,7 +878,7 @@ extern "C" int xmi_main_msim(xmi_inputFPtr in, xmi_hdf5FPtr t, int n_mpi_hosts, 
   cudaEventRecord(all0, s->stream);
   xmi::DevTally tl;
   const int threads = in->gpu.threads_per_block > 0 ? in->gpu.threads_per_block : 128;
-  const int bps = in->gpu.blocks_per_sm > 0 ? in->gpu.blocks_per_sm : 4;
+  const int bps = in->gpu.blocks_per_sm > 0 ? in->gpu.blocks_per_sm : 8;
   Phases ph;
   bool ok = precision == 0 ? stage_run<double>(s, s->b64, h, tl) && launch_single<double>(s, s->b64, tl, h, threads, bps, ph)
                            : stage_run<float>(s, s->b32, h, tl) && launch_single<float>(s, s->b32, tl, h, threads, bps, ph);
@@ -844,6 +916,7 @@ struct BatchState {
   int cap = 0;
   unsigned long long *flags = nullptr; /* [0] estimator error, [1] events */
   EventQueue q;
+  WfBuffers wf;
   cudaStream_t stream = nullptr;
 };
 BatchState g_batch;
@@ -892,11 +965,15 @@ bool launch_batch(int n, DevState **st, xmi_hdf5FPtr *t, const xmi::DevTally *tl
   const int stage_cap = stage_cap_for<R>(stage_max);
   size_t smem = 0;
   const int est_blocks = estimator_blocks<R>(stage_cap, &smem);
+  int rounds = 1;
+  for (int c = 0; c < n; c++) rounds = wavefront_rounds(t[c]->b) > rounds ? wavefront_rounds(t[c]->b) : rounds;
+  const long long chunk_cap = vr ? kMaxQueuedEvents / N : kMaxChunkPhotons;
+  if (!ensure_wf<R>(B.wf, first[n] < chunk_cap ? (first[n] > 0 ? first[n] : 1) : chunk_cap)) return false;
+  xmi::DevBundle<R> unused_b{};
+  xmi::DevTally unused_t{};
   auto transport = [&](long long w0, long long w1, const xmi::VrQueue<R> &vq) {
-    long long blocks = (long long)sms * blocks_per_sm;
-    if (blocks * threads > w1 - w0) blocks = (w1 - w0 + threads - 1) / threads;
-    if (blocks < 1) blocks = 1;
-    xmi::transport_kernel_batch<R><<<(int)blocks, threads, 0, B.stream>>>(db, B.tallies, B.cfg_first, n, vq, w0, w1);
+    return launch_wavefront<R, true>(B.stream, B.wf, unused_b, unused_t, db, B.tallies, B.cfg_first, n, w0, w1,
+                                     rounds, vq, threads, sms * blocks_per_sm);
   };
   auto estimator = [&](const xmi::VrQueue<R> &vq, const int *order, unsigned long long *work) {
     xmi::estimator_kernel<R><<<est_blocks, 256, smem, B.stream>>>(db, B.tallies, n, vq.ev, order, vq.count, vq.cap,
@@ -946,7 +1023,7 @@ extern "C" int xmi_main_msim_batch(int n, xmi_inputFPtr *inputFPtrs, xmi_hdf5FPt
   for (int c = 0; c < n; c++)
     if (!cuda_ok(cudaStreamSynchronize(st[c]->stream), "staging")) return 0;
   const int threads = inputFPtrs[0]->gpu.threads_per_block > 0 ? inputFPtrs[0]->gpu.threads_per_block : 128;
-  const int bps = inputFPtrs[0]->gpu.blocks_per_sm > 0 ? inputFPtrs[0]->gpu.blocks_per_sm : 4;
+  const int bps = inputFPtrs[0]->gpu.blocks_per_sm > 0 ? inputFPtrs[0]->gpu.blocks_per_sm : 8;
   Phases ph;
   bool ok = precision == 0 ? launch_batch<double>(n, st.data(), hdf5FPtrs, tl.data(), threads, bps, true, ph)
                            : launch_batch<float>(n, st.data(), hdf5FPtrs, tl.data(), threads, bps, true, ph);

@@ -80,6 +80,18 @@ XMI_HD void xmi_rng_init(xmi_rng *g, uint64_t seed, uint64_t id, uint32_t stream
   g->pos = 2;
 }
 
+/* restarts a stream at a saved position: next block counter ctr0 and the
+ * number of draws already taken from the block before it (pos, 2 = none left) */
+XMI_HD void xmi_rng_resume(xmi_rng *g, uint64_t seed, uint64_t id, uint32_t stream, uint32_t ctr0, int pos) {
+  xmi_rng_init(g, seed, id, stream);
+  if (pos < 2) {
+    g->ctr.v[0] = ctr0 - 1u;
+    g->buf = xmi_philox4x32_10(g->ctr, g->k0, g->k1);
+  }
+  g->ctr.v[0] = ctr0;
+  g->pos = pos;
+}
+
 /* consumes one draw (two words) and returns its first word: the 32 most
  * significant of the 53 random bits of the uniform xmi_rng_uniform would
  * have returned */

@@ -857,155 +857,175 @@ __device__ bool check_photon_detector_hit(const DevBundle<R> &b, const Photon<R>
 }
 
 /* ---------------- one history ---------------- */
+enum StepStatus { kStepDone = 0, kStepInteract = 1, kStepError = 2 };
+
+/* One step of a photon (one pass of the loop of xmi_simulate_photon,
+ * src/xmi_main.F90:1188-1685): transport to the next interaction point
+ * (forced with variance reduction, analog otherwise), the estimator event of
+ * that interaction, and the choice of atom and interaction type (p.elem,
+ * p.last).  Returns kStepInteract with g positioned on the draws of the
+ * interaction, or kStepDone when the history ends (p.hit marks a detector
+ * hit), or kStepError. */
+template <typename R>
+__device__ int step_photon(const DevBundle<R> &b, Photon<R> &p, const DevTally &t, const VrQueue<R> &vq, int cfg,
+                           xmi_rng &g) {
+  if (p.E < (R)kEnergyThreshold) return kStepDone;
+  p.inside = 0;
+  xmi_rng_init(&g, b.seed, (uint64_t)p.id, (uint32_t)(p.n_int + 1));
+  R dn[3] = {(R)b.n_sample[0], (R)b.n_sample[1], (R)b.n_sample[2]};
+  const bool up = rdot(p.d, dn) > (R)0;
+  const R R0 = uni<R>(&g);
+  if ((b.escape_mode == 1 && p.n_int == 1) || (b.use_vr == 0 && b.escape_mode == 0)) {
+    R minr = (R)0, maxr = (R)0, blbs = (R)1;
+    bool stop = false;
+    int outcome = 0; /* 0 continue, 1 photon absorbed by collimator/bad hit, 2 detector hit, 3 error */
+    layers_in_direction(up, [&](int j) {
+      bool active = up ? (j >= p.layer && j < b.n_layers) : (j <= p.layer);
+      if (!active || stop) return;
+      double ip[3], dd;
+      if (!plane_step(p.c, p.d, b.n_sample, up ? b.zend[j] : b.zbeg[j], ip, &dd)) { outcome = 3; stop = true; return; }
+      R tp = (R)-1 * (R)dd * b.rho[j] * p.mus[j];
+      R tempexp = exp(tp);
+      minr = maxr;
+      maxr = maxr - blbs * expm1(tp);
+      if (R0 <= maxr) {
+        R dist = (R)-1 * log1p((R)-1 * (R0 - minr) / blbs) / p.mus[j] / b.rho[j];
+        double tc[3] = {p.c[0], p.c[1], p.c[2]};
+#pragma unroll
+        for (int q = 0; q < 3; q++) p.c[q] = p.c[q] + (double)dist * (double)p.d[q];
+        if (b.escape_mode != 1) {
+          int rc = check_detector_intersection(b.p_det, b.det_inv, b.coll_present, b.det_radius, b.coll_height,
+                                               b.coll_half_apex, b.coll_vertex_x, tc, p.c);
+          if (rc == 1 || rc == 3) { outcome = 1; stop = true; return; }
+          if (rc == 2) { outcome = 2; stop = true; return; }
+        }
+        p.layer = j;
+        p.inside = 1;
+        stop = true;
+      } else {
+        if (b.escape_mode != 1) {
+          int rc = check_detector_intersection(b.p_det, b.det_inv, b.coll_present, b.det_radius, b.coll_height,
+                                               b.coll_half_apex, b.coll_vertex_x, p.c, ip);
+          if (rc == 1 || rc == 3) { outcome = 1; stop = true; return; }
+          if (rc == 2) { outcome = 2; stop = true; return; }
+        }
+        p.c[0] = ip[0]; p.c[1] = ip[1]; p.c[2] = ip[2];
+        blbs = blbs * tempexp;
+      }
+    });
+    if (outcome == 3) return kStepError;
+    if (outcome == 1) return kStepDone;
+    if (outcome == 2) { p.hit = 1; return kStepDone; }
+  } else {
+    if (p.n_int == b.N) return kStepDone;
+    R dist[XMI_MAXL];
+    double lp[3] = {p.c[0], p.c[1], p.c[2]};
+    R pabs = (R)0;
+    bool fail = false;
+    const int cur = p.layer;
+    layers_in_direction(up, [&](int j) {
+      bool active = up ? (j >= cur && j < b.n_layers) : (j <= cur);
+      dist[j] = (R)0;
+      if (active && !fail) {
+        double ip[3], dd;
+        if (!plane_step(lp, p.d, b.n_sample, up ? b.zend[j] : b.zbeg[j], ip, &dd)) { fail = true; return; }
+        dist[j] = (R)dd;
+        lp[0] = ip[0]; lp[1] = ip[1]; lp[2] = ip[2];
+        pabs = pabs + p.mus[j] * b.rho[j] * dist[j];
+      }
+    });
+    if (fail) return kStepError;
+    R pabs2 = (R)-1 * expm1((R)-1 * pabs);
+    p.w = p.w * pabs2;
+    if (b.escape_mode == 1) p.we = p.w;
+    R negln = (R)-1 * log1p((R)-1 * R0 * pabs2);
+    int my_index = cur;
+    R my_sum = (R)0;
+    bool found = false;
+    layers_in_direction(up, [&](int j) {
+      bool active = up ? (j >= cur && j < b.n_layers) : (j <= cur);
+      if (active && !found) {
+        my_sum = my_sum + p.mus[j] * b.rho[j] * dist[j];
+        if (my_sum > negln) { my_index = j; found = true; }
+      }
+    });
+    R mr_sel = (R)0;
+#pragma unroll
+    for (int j = 0; j < XMI_MAXL; j++)
+      if (j == my_index) mr_sel = p.mus[j] * b.rho[j];
+    R temp_sum = (R)0;
+    layers_in_direction(up, [&](int j) {
+      bool active = up ? (j >= cur && j <= my_index) : (j <= cur && j >= my_index);
+      if (active) temp_sum = temp_sum + ((R)1 - (p.mus[j] * b.rho[j] / mr_sel)) * dist[j];
+    });
+    temp_sum = temp_sum - (R)1 * log1p((R)-1 * R0 * pabs2) / mr_sel;
+    if (!XMI_CHK(my_index, b.n_layers, 41)) return kStepError;
+#pragma unroll
+    for (int q = 0; q < 3; q++) p.c[q] = p.c[q] + (double)temp_sum * (double)p.d[q];
+    p.inside = 1;
+    p.layer = my_index;
+  }
+  if (!p.inside) {
+    if (b.escape_mode != 1) p.hit = check_photon_detector_hit(b, p) ? 1 : 0;
+    return kStepDone;
+  }
+  if (p.n_int == b.N) return kStepDone;
+  p.n_int = p.n_int + 1;
+  if (b.use_vr == 1) {
+    bool ok = true;
+    VrEvent<R> ev;
+    ev.cfg = cfg;
+    if (vr_prologue(b, p, t, ev, ok) && !vr_emit(vq, ev, vr_key(ev))) { set_error(t, kErrQueue); return kStepError; }
+    if (!ok) { set_error(t, kErrTable); return kStepError; }
+  }
+  /* atom selection and interaction type, src/xmi_main.F90:1556-1652 */
+  int node;
+  R f;
+  locate(b, p.E, node, f);
+  R r = uni<R>(&g);
+  if (!XMI_CHK(p.layer, b.n_layers, 33)) return kStepError;
+  const int L = p.layer, nel = b.nel[L], off = b.off[L];
+  R mu_l = (R)0;
+#pragma unroll
+  for (int j = 0; j < XMI_MAXL; j++)
+    if (j == L) mu_l = p.mus[j];
+  R thr = (R)0;
+  int sel = nel - 1;
+  for (int i = 0; i < nel; i++) {
+    thr = thr + XMI_LDG(b.layer_w, off + i, b.n_layer_el, 19) *
+                    el_val(b, XMI_LDG(b.layer_el, off + i, b.n_layer_el, 19), XMI_REC_TOT, node, f) / mu_l;
+    if (r < thr) { sel = i; break; }
+  }
+  p.elem = XMI_LDG(b.layer_el, off + sel, b.n_layer_el, 19);
+  if (!XMI_CHK(p.elem, b.n_elem, 42)) return kStepError;
+  r = uni<R>(&g);
+  R pr = el_val(b, p.elem, XMI_REC_PR, node, f);
+  R prc = el_val(b, p.elem, XMI_REC_PRC, node, f);
+  p.last = r < pr ? XMI_RAYLEIGH : (r < prc ? XMI_COMPTON : XMI_PHOTOELECTRIC);
+  return kStepInteract;
+}
+
+/* the interaction chosen by step_photon, drawing from g */
+template <typename R>
+__device__ __forceinline__ bool interact(const DevBundle<R> &b, Photon<R> &p, const DevTally &t, xmi_rng &g) {
+  bool ok;
+  if (p.last == XMI_RAYLEIGH) ok = rayleigh(b, p, &g);
+  else if (p.last == XMI_COMPTON) ok = compton(b, p, &g);
+  else ok = fluorescence(b, p, &g);
+  if (!ok) set_error(t, kErrTable);
+  return ok;
+}
+
+/* a whole history in one thread: false on an error (no tally) */
 template <typename R>
 __device__ bool simulate_photon(const DevBundle<R> &b, Photon<R> &p, const DevTally &t, const VrQueue<R> &vq,
                                 int cfg) {
   for (int guard = 0; guard < 4 * XMI_MAXN + 8; guard++) {
-    if (p.E < (R)kEnergyThreshold) break;
-    p.inside = 0;
     xmi_rng g;
-    xmi_rng_init(&g, b.seed, (uint64_t)p.id, (uint32_t)(p.n_int + 1));
-    R dn[3] = {(R)b.n_sample[0], (R)b.n_sample[1], (R)b.n_sample[2]};
-    const bool up = rdot(p.d, dn) > (R)0;
-    const R R0 = uni<R>(&g);
-    if ((b.escape_mode == 1 && p.n_int == 1) || (b.use_vr == 0 && b.escape_mode == 0)) {
-      R minr = (R)0, maxr = (R)0, blbs = (R)1;
-      bool stop = false;
-      int outcome = 0; /* 0 continue, 1 photon absorbed by collimator/bad hit, 2 detector hit, 3 error */
-      layers_in_direction(up, [&](int j) {
-        bool active = up ? (j >= p.layer && j < b.n_layers) : (j <= p.layer);
-        if (!active || stop) return;
-        double ip[3], dd;
-        if (!plane_step(p.c, p.d, b.n_sample, up ? b.zend[j] : b.zbeg[j], ip, &dd)) { outcome = 3; stop = true; return; }
-        R tp = (R)-1 * (R)dd * b.rho[j] * p.mus[j];
-        R tempexp = exp(tp);
-        minr = maxr;
-        maxr = maxr - blbs * expm1(tp);
-        if (R0 <= maxr) {
-          R dist = (R)-1 * log1p((R)-1 * (R0 - minr) / blbs) / p.mus[j] / b.rho[j];
-          double tc[3] = {p.c[0], p.c[1], p.c[2]};
-#pragma unroll
-          for (int q = 0; q < 3; q++) p.c[q] = p.c[q] + (double)dist * (double)p.d[q];
-          if (b.escape_mode != 1) {
-            int rc = check_detector_intersection(b.p_det, b.det_inv, b.coll_present, b.det_radius, b.coll_height,
-                                                 b.coll_half_apex, b.coll_vertex_x, tc, p.c);
-            if (rc == 1 || rc == 3) { outcome = 1; stop = true; return; }
-            if (rc == 2) { outcome = 2; stop = true; return; }
-          }
-          p.layer = j;
-          p.inside = 1;
-          stop = true;
-        } else {
-          if (b.escape_mode != 1) {
-            int rc = check_detector_intersection(b.p_det, b.det_inv, b.coll_present, b.det_radius, b.coll_height,
-                                                 b.coll_half_apex, b.coll_vertex_x, p.c, ip);
-            if (rc == 1 || rc == 3) { outcome = 1; stop = true; return; }
-            if (rc == 2) { outcome = 2; stop = true; return; }
-          }
-          p.c[0] = ip[0]; p.c[1] = ip[1]; p.c[2] = ip[2];
-          blbs = blbs * tempexp;
-        }
-      });
-      if (outcome == 3) return false;
-      if (outcome == 1) return true;
-      if (outcome == 2) { p.hit = 1; return true; }
-    } else {
-      if (p.n_int == b.N) break;
-      R dist[XMI_MAXL];
-      double lp[3] = {p.c[0], p.c[1], p.c[2]};
-      R pabs = (R)0;
-      bool fail = false;
-      const int cur = p.layer;
-      layers_in_direction(up, [&](int j) {
-        bool active = up ? (j >= cur && j < b.n_layers) : (j <= cur);
-        dist[j] = (R)0;
-        if (active && !fail) {
-          double ip[3], dd;
-          if (!plane_step(lp, p.d, b.n_sample, up ? b.zend[j] : b.zbeg[j], ip, &dd)) { fail = true; return; }
-          dist[j] = (R)dd;
-          lp[0] = ip[0]; lp[1] = ip[1]; lp[2] = ip[2];
-          pabs = pabs + p.mus[j] * b.rho[j] * dist[j];
-        }
-      });
-      if (fail) return false;
-      R pabs2 = (R)-1 * expm1((R)-1 * pabs);
-      p.w = p.w * pabs2;
-      if (b.escape_mode == 1) p.we = p.w;
-      R negln = (R)-1 * log1p((R)-1 * R0 * pabs2);
-      int my_index = cur;
-      R my_sum = (R)0;
-      bool found = false;
-      layers_in_direction(up, [&](int j) {
-        bool active = up ? (j >= cur && j < b.n_layers) : (j <= cur);
-        if (active && !found) {
-          my_sum = my_sum + p.mus[j] * b.rho[j] * dist[j];
-          if (my_sum > negln) { my_index = j; found = true; }
-        }
-      });
-      R mr_sel = (R)0;
-#pragma unroll
-      for (int j = 0; j < XMI_MAXL; j++)
-        if (j == my_index) mr_sel = p.mus[j] * b.rho[j];
-      R temp_sum = (R)0;
-      layers_in_direction(up, [&](int j) {
-        bool active = up ? (j >= cur && j <= my_index) : (j <= cur && j >= my_index);
-        if (active) temp_sum = temp_sum + ((R)1 - (p.mus[j] * b.rho[j] / mr_sel)) * dist[j];
-      });
-      temp_sum = temp_sum - (R)1 * log1p((R)-1 * R0 * pabs2) / mr_sel;
-      if (!XMI_CHK(my_index, b.n_layers, 41)) return false;
-#pragma unroll
-      for (int q = 0; q < 3; q++) p.c[q] = p.c[q] + (double)temp_sum * (double)p.d[q];
-      p.inside = 1;
-      p.layer = my_index;
-    }
-    if (!p.inside) {
-      if (b.escape_mode != 1) p.hit = check_photon_detector_hit(b, p) ? 1 : 0;
-      break;
-    }
-    if (p.n_int == b.N) break;
-    p.n_int = p.n_int + 1;
-    if (b.use_vr == 1) {
-      bool ok = true;
-      VrEvent<R> ev;
-      ev.cfg = cfg;
-      if (vr_prologue(b, p, t, ev, ok) && !vr_emit(vq, ev, vr_key(ev))) { set_error(t, kErrQueue); return false; }
-      if (!ok) { set_error(t, kErrTable); return false; }
-    }
-    /* atom selection and interaction type, src/xmi_main.F90:1556-1652 */
-    int node;
-    R f;
-    locate(b, p.E, node, f);
-    R r = uni<R>(&g);
-    if (!XMI_CHK(p.layer, b.n_layers, 33)) return false;
-    const int L = p.layer, nel = b.nel[L], off = b.off[L];
-    R mu_l = (R)0;
-#pragma unroll
-    for (int j = 0; j < XMI_MAXL; j++)
-      if (j == L) mu_l = p.mus[j];
-    R thr = (R)0;
-    int sel = nel - 1;
-    for (int i = 0; i < nel; i++) {
-      thr = thr + XMI_LDG(b.layer_w, off + i, b.n_layer_el, 19) *
-                      el_val(b, XMI_LDG(b.layer_el, off + i, b.n_layer_el, 19), XMI_REC_TOT, node, f) / mu_l;
-      if (r < thr) { sel = i; break; }
-    }
-    p.elem = XMI_LDG(b.layer_el, off + sel, b.n_layer_el, 19);
-    if (!XMI_CHK(p.elem, b.n_elem, 42)) return false;
-    r = uni<R>(&g);
-    R pr = el_val(b, p.elem, XMI_REC_PR, node, f);
-    R prc = el_val(b, p.elem, XMI_REC_PRC, node, f);
-    bool ok;
-    if (r < pr) {
-      p.last = XMI_RAYLEIGH;
-      ok = rayleigh(b, p, &g);
-    } else if (r < prc) {
-      p.last = XMI_COMPTON;
-      ok = compton(b, p, &g);
-    } else {
-      p.last = XMI_PHOTOELECTRIC;
-      ok = fluorescence(b, p, &g);
-    }
-    if (!ok) { set_error(t, kErrTable); return false; }
+    const int st = step_photon(b, p, t, vq, cfg, g);
+    if (st == kStepDone) return true;
+    if (st == kStepError) return false;
+    if (!interact(b, p, t, g)) return false;
   }
   return true;
 }
@@ -1117,22 +1137,34 @@ __device__ bool start_photon(const DevBundle<R> &b, const xmi_source_item &it, l
   return true;
 }
 
-/* one photon: work index w of the configuration's source items, from the
- * source to its last interaction; estimator events go to the queue, analog
- * detector hits straight to the brute-force tallies */
+/* tallies of a finished history: an analog detector hit goes to the
+ * brute-force histories (and, without variance reduction, the spectrum) */
 template <typename R>
-__device__ __forceinline__ void run_photon(const DevBundle<R> &b, const DevTally &t, const VrQueue<R> &vq,
-                                           long long w, int cfg) {
-  /* work index -> (item, index within item) */
+__device__ __forceinline__ void finish_photon(const DevBundle<R> &b, const DevTally &t, const Photon<R> &p) {
+  if (!p.hit) return;
+  if (b.use_vr == 0) tally_channel(b, t, p.n_int, p.E, (double)p.w);
+  if (p.n_int > 0) {
+    int slot = -1;
+    if (p.h_type < 0) slot = p.h_slot;
+    else if (p.h_type == XMI_RAYLEIGH) slot = b.n_lines + 2 * p.h_elem;
+    else if (p.h_type == XMI_COMPTON) slot = b.n_lines + 2 * p.h_elem + 1;
+    if (slot >= 0 && XMI_CHK((long long)(p.n_int - 1) * b.n_slots + slot, (long long)b.N * b.n_slots, 32))
+      atomicAdd(&t.hist_brute[(size_t)(p.n_int - 1) * b.n_slots + slot], (double)p.w);
+  }
+}
+
+/* photon of work index w (within its configuration) at the source: false if
+ * there is none (skipped draw or a source error, which is flagged) */
+template <typename R>
+__device__ __forceinline__ bool init_photon(const DevBundle<R> &b, const DevTally &t, long long w, Photon<R> &p) {
   int lo = 0, hi = b.n_items - 1;
   while (lo < hi) {
     int mid = (lo + hi + 1) >> 1;
     if (w >= XMI_LDG(b.item_first, mid, b.n_items, 21)) lo = mid; else hi = mid - 1;
   }
-  if (!XMI_CHK(lo, b.n_items, 40)) return;
+  if (!XMI_CHK(lo, b.n_items, 40)) return false;
   const xmi_source_item &it = b.items[lo];
   const long long j = w - XMI_LDG(b.item_first, lo, b.n_items, 21);
-  Photon<R> p;
   p.id = it.first + j;
   p.n_int = 0;
   p.last = XMI_NO_INTERACTION;
@@ -1142,47 +1174,8 @@ __device__ __forceinline__ void run_photon(const DevBundle<R> &b, const DevTally
   p.h_slot = 0;
   p.elem = 0;
   bool skip;
-  if (!start_photon(b, it, j, p, skip)) { set_error(t, kErrSource); return; }
-  if (skip) return;
-  if (!simulate_photon(b, p, t, vq, cfg)) return;
-  if (p.hit) {
-    if (b.use_vr == 0) tally_channel(b, t, p.n_int, p.E, (double)p.w);
-    if (p.n_int > 0) {
-      int slot = -1;
-      if (p.h_type < 0) slot = p.h_slot;
-      else if (p.h_type == XMI_RAYLEIGH) slot = b.n_lines + 2 * p.h_elem;
-      else if (p.h_type == XMI_COMPTON) slot = b.n_lines + 2 * p.h_elem + 1;
-      if (slot >= 0 && XMI_CHK((long long)(p.n_int - 1) * b.n_slots + slot, (long long)b.N * b.n_slots, 32))
-        atomicAdd(&t.hist_brute[(size_t)(p.n_int - 1) * b.n_slots + slot], (double)p.w);
-    }
-  }
-}
-
-/* Transport of the photons with work index [w0, w1) of one configuration */
-template <typename R>
-__global__ void __launch_bounds__(128) transport_kernel(DevBundle<R> b, DevTally t, VrQueue<R> vq, long long w0,
-                                                        long long w1) {
-  const long long stride = (long long)gridDim.x * blockDim.x;
-  for (long long w = w0 + (long long)blockIdx.x * blockDim.x + threadIdx.x; w < w1; w += stride)
-    run_photon(b, t, vq, w, 0);
-}
-
-/* Batched transport: work indices [w0, w1) of the concatenation of the
- * configurations' photon ranges (cfg_first[c] = first work index of
- * configuration c, n_cfg + 1 entries) */
-template <typename R>
-__global__ void __launch_bounds__(128) transport_kernel_batch(const DevBundle<R> *bundles, const DevTally *tallies,
-                                                              const long long *cfg_first, int n_cfg, VrQueue<R> vq,
-                                                              long long w0, long long w1) {
-  const long long stride = (long long)gridDim.x * blockDim.x;
-  for (long long w = w0 + (long long)blockIdx.x * blockDim.x + threadIdx.x; w < w1; w += stride) {
-    int lo = 0, hi = n_cfg - 1;
-    while (lo < hi) {
-      int mid = (lo + hi + 1) >> 1;
-      if (w >= __ldg(cfg_first + mid)) lo = mid; else hi = mid - 1;
-    }
-    run_photon(bundles[lo], tallies[lo], vq, w - __ldg(cfg_first + lo), lo);
-  }
+  if (!start_photon(b, it, j, p, skip)) { set_error(t, kErrSource); return false; }
+  return !skip;
 }
 
 }  // namespace xmi
