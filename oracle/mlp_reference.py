@@ -1,0 +1,64 @@
+"""TEST INFRASTRUCTURE: NumPy restatement of the solid-angle surrogate network
+(xmimsim_gb300/csrc/mlp.cu) used as the checker of the tensor-core kernels.
+
+Same parameter layout and the same rounding points as the GPU kernels: BF16
+weights, inputs and hidden activations (round to nearest even), FP32
+accumulation (evaluated here in FP64 and rounded to FP32), SiLU, FP32 output
+layer.  Gradients follow the same graph (straight-through through the BF16
+roundings) for the checks of the backward kernels."""
+from __future__ import annotations
+
+import numpy as np
+
+H, NIN = 128, 3
+NPARAM = H * NIN + H + 3 * (H * H + H) + H + 1
+
+
+def bf16(x: np.ndarray) -> np.ndarray:
+    """Round float32 values to bfloat16 (nearest even), returned as float32."""
+    u = np.ascontiguousarray(x, dtype=np.float32).view(np.uint32)
+    r = ((u >> 16) & np.uint32(1)) + np.uint32(0x7FFF)
+    return ((u + r) & np.uint32(0xFFFF0000)).view(np.float32)
+
+
+def unpack(theta: np.ndarray):
+    t = np.asarray(theta, dtype=np.float32)
+    o = 0
+    W0 = t[o:o + H * NIN].reshape(H, NIN); o += H * NIN
+    b0 = t[o:o + H]; o += H
+    Ws, bs = [W0], [b0]
+    for _ in range(3):
+        Ws.append(t[o:o + H * H].reshape(H, H)); o += H * H
+        bs.append(t[o:o + H]); o += H
+    wo = t[o:o + H]; o += H
+    bo = t[o]
+    return Ws, bs, wo, bo
+
+
+def silu(z):
+    return z / (1.0 + np.exp(-z))
+
+
+def forward(theta: np.ndarray, x: np.ndarray, keep: bool = False):
+    Ws, bs, wo, bo = unpack(theta)
+    a = bf16(np.asarray(x, dtype=np.float32))
+    acts, zs = [a], []
+    h = None
+    for l in range(4):
+        z = (a.astype(np.float64) @ bf16(Ws[l]).astype(np.float64).T).astype(np.float32) + bs[l]
+        h = silu(z.astype(np.float64)).astype(np.float32)
+        zs.append(z)
+        a = bf16(h) if l < 3 else h
+        acts.append(a)
+    y = (h.astype(np.float64) @ wo.astype(np.float64)).astype(np.float32) + bo
+    return (y, acts, zs) if keep else y
+
+
+def init_params(seed: int) -> np.ndarray:
+    """He-style initialisation of the parameter vector."""
+    rng = np.random.default_rng(seed)
+    parts = [rng.normal(0, np.sqrt(2.0 / NIN), H * NIN), np.zeros(H)]
+    for _ in range(3):
+        parts += [rng.normal(0, np.sqrt(2.0 / H), H * H), np.zeros(H)]
+    parts += [rng.normal(0, np.sqrt(1.0 / H), H), np.zeros(1)]
+    return np.concatenate(parts).astype(np.float32)

@@ -27,7 +27,7 @@ NVFLAGS = ARCH + ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC",
                   "-Xcompiler", "-fopenmp"]
 
 HOST_SOURCES = ["xrlite.c", "host.c"]
-CUDA_SOURCES = ["engine.cu", "detector.cu"]
+CUDA_SOURCES = ["engine.cu", "detector.cu", "mlp.cu"]
 ORACLE_SOURCES = ["oracle_transport.c", "oracle_detector.c"]
 
 
