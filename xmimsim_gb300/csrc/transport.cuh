@@ -104,6 +104,36 @@ __device__ __forceinline__ bool plane_step(const double *p, const R *d, const do
   return true;
 }
 
+/* Walk along a fixed direction through the parallel layer planes.  A point x
+ * is at height dot(x, n); the boundary plane zp of the sample frame (through
+ * (0, 0, zp)) is at height zp * n[2].  One division per direction instead of
+ * one per plane: the parametric step to the next plane is its height
+ * difference times 1/dot(d, n), and the path length is |step| x |d| (the
+ * reference intersects each plane and measures the distance, which is the
+ * same quantity). */
+struct PlaneWalk {
+  double h, inv, dlen;
+};
+
+template <typename R>
+__device__ __forceinline__ bool plane_walk_init(const double *p, const R *d, const double *n, PlaneWalk &w) {
+  const double dd[3] = {(double)d[0], (double)d[1], (double)d[2]};
+  const double itn = dd[0] * n[0] + dd[1] * n[1] + dd[2] * n[2];
+  if (itn == 0.0) return false;
+  w.h = p[0] * n[0] + p[1] * n[1] + p[2] * n[2];
+  w.inv = 1.0 / itn;
+  w.dlen = sqrt(dd[0] * dd[0] + dd[1] * dd[1] + dd[2] * dd[2]);
+  return true;
+}
+
+/* signed parametric step to boundary plane zp; the walk moves onto it */
+__device__ __forceinline__ double plane_walk(PlaneWalk &w, double zp, const double *n) {
+  const double P = zp * n[2];
+  const double s = (P - w.h) * w.inv;
+  w.h = P;
+  return s;
+}
+
 /* uniform draw in the working precision; FP32 uses the rounded FP64 draw so
  * that FP32 and FP64 runs consume identical random sequences */
 template <typename R> __device__ __forceinline__ R uni(xmi_rng *g);
@@ -545,24 +575,22 @@ __device__ bool vr_prologue(const DevBundle<R> &b, const Photon<R> &p, const Dev
 #pragma unroll
   for (int j = 0; j < XMI_MAXL; j++) ev.rd[j] = (R)0;
   {
-    double tc[3] = {p.c[0], p.c[1], p.c[2]};
-    bool done = false, fail = false;
+    PlaneWalk pw;
+    if (!plane_walk_init(p.c, ndc, b.n_sample, pw)) { ok = false; return false; }
+    bool done = false;
     layers_in_direction(up, [&](int j) {
       bool active = up ? (j >= layer && j < b.n_layers) : (j <= layer);
-      if (active && !done && !fail) {
-        double ip[3], dd;
-        if (!plane_step(tc, ndc, b.n_sample, up ? b.zend[j] : b.zbeg[j], ip, &dd)) { fail = true; return; }
+      if (active && !done) {
+        const double dd = fabs(plane_walk(pw, up ? b.zend[j] : b.zbeg[j], b.n_sample)) * pw.dlen;
         if (dd > total_distance) {
           ev.rd[j] = b.rho[j] * (R)total_distance;
           done = true;
         } else {
           ev.rd[j] = b.rho[j] * (R)dd;
-          tc[0] = ip[0]; tc[1] = ip[1]; tc[2] = ip[2];
           total_distance = total_distance - dd;
         }
       }
     });
-    if (fail) { ok = false; return false; }
   }
   R murhod = (R)0;
 #pragma unroll
@@ -879,11 +907,16 @@ __device__ int step_photon(const DevBundle<R> &b, Photon<R> &p, const DevTally &
     R minr = (R)0, maxr = (R)0, blbs = (R)1;
     bool stop = false;
     int outcome = 0; /* 0 continue, 1 photon absorbed by collimator/bad hit, 2 detector hit, 3 error */
+    PlaneWalk pw;
+    if (!plane_walk_init(p.c, p.d, b.n_sample, pw)) return kStepError;
     layers_in_direction(up, [&](int j) {
       bool active = up ? (j >= p.layer && j < b.n_layers) : (j <= p.layer);
       if (!active || stop) return;
-      double ip[3], dd;
-      if (!plane_step(p.c, p.d, b.n_sample, up ? b.zend[j] : b.zbeg[j], ip, &dd)) { outcome = 3; stop = true; return; }
+      const double sw = plane_walk(pw, up ? b.zend[j] : b.zbeg[j], b.n_sample);
+      const double dd = fabs(sw) * pw.dlen;
+      double ip[3];
+#pragma unroll
+      for (int q = 0; q < 3; q++) ip[q] = sw * (double)p.d[q] + p.c[q];
       R tp = (R)-1 * (R)dd * b.rho[j] * p.mus[j];
       R tempexp = exp(tp);
       minr = maxr;
@@ -919,22 +952,18 @@ __device__ int step_photon(const DevBundle<R> &b, Photon<R> &p, const DevTally &
   } else {
     if (p.n_int == b.N) return kStepDone;
     R dist[XMI_MAXL];
-    double lp[3] = {p.c[0], p.c[1], p.c[2]};
     R pabs = (R)0;
-    bool fail = false;
     const int cur = p.layer;
+    PlaneWalk pw;
+    if (!plane_walk_init(p.c, p.d, b.n_sample, pw)) return kStepError;
     layers_in_direction(up, [&](int j) {
       bool active = up ? (j >= cur && j < b.n_layers) : (j <= cur);
       dist[j] = (R)0;
-      if (active && !fail) {
-        double ip[3], dd;
-        if (!plane_step(lp, p.d, b.n_sample, up ? b.zend[j] : b.zbeg[j], ip, &dd)) { fail = true; return; }
-        dist[j] = (R)dd;
-        lp[0] = ip[0]; lp[1] = ip[1]; lp[2] = ip[2];
+      if (active) {
+        dist[j] = (R)(fabs(plane_walk(pw, up ? b.zend[j] : b.zbeg[j], b.n_sample)) * pw.dlen);
         pabs = pabs + p.mus[j] * b.rho[j] * dist[j];
       }
     });
-    if (fail) return kStepError;
     R pabs2 = (R)-1 * expm1((R)-1 * pabs);
     p.w = p.w * pabs2;
     if (b.escape_mode == 1) p.we = p.w;
