@@ -14,15 +14,20 @@ H, NIN = 128, 3
 NPARAM = H * NIN + H + 3 * (H * H + H) + H + 1
 
 
+ROUND_BF16 = True  # False: exact arithmetic (for checking the backward formulas)
+
+
 def bf16(x: np.ndarray) -> np.ndarray:
     """Round float32 values to bfloat16 (nearest even), returned as float32."""
+    if not ROUND_BF16:
+        return np.asarray(x, dtype=np.float64)
     u = np.ascontiguousarray(x, dtype=np.float32).view(np.uint32)
     r = ((u >> 16) & np.uint32(1)) + np.uint32(0x7FFF)
     return ((u + r) & np.uint32(0xFFFF0000)).view(np.float32)
 
 
 def unpack(theta: np.ndarray):
-    t = np.asarray(theta, dtype=np.float32)
+    t = np.asarray(theta, dtype=np.float32 if ROUND_BF16 else np.float64)
     o = 0
     W0 = t[o:o + H * NIN].reshape(H, NIN); o += H * NIN
     b0 = t[o:o + H]; o += H
@@ -41,16 +46,17 @@ def silu(z):
 
 def forward(theta: np.ndarray, x: np.ndarray, keep: bool = False):
     Ws, bs, wo, bo = unpack(theta)
-    a = bf16(np.asarray(x, dtype=np.float32))
+    a = bf16(np.asarray(x, dtype=np.float32 if ROUND_BF16 else np.float64))
     acts, zs = [a], []
     h = None
     for l in range(4):
-        z = (a.astype(np.float64) @ bf16(Ws[l]).astype(np.float64).T).astype(np.float32) + bs[l]
-        h = silu(z.astype(np.float64)).astype(np.float32)
+        ft = np.float32 if ROUND_BF16 else np.float64
+        z = (a.astype(np.float64) @ bf16(Ws[l]).astype(np.float64).T).astype(ft) + bs[l]
+        h = silu(z.astype(np.float64)).astype(ft)
         zs.append(z)
         a = bf16(h) if l < 3 else h
         acts.append(a)
-    y = (h.astype(np.float64) @ wo.astype(np.float64)).astype(np.float32) + bo
+    y = (h.astype(np.float64) @ wo.astype(np.float64)).astype(np.float32 if ROUND_BF16 else np.float64) + bo
     return (y, acts, zs) if keep else y
 
 
@@ -62,3 +68,36 @@ def init_params(seed: int) -> np.ndarray:
         parts += [rng.normal(0, np.sqrt(2.0 / H), H * H), np.zeros(H)]
     parts += [rng.normal(0, np.sqrt(1.0 / H), H), np.zeros(1)]
     return np.concatenate(parts).astype(np.float32)
+
+
+def dsilu(z):
+    s = 1.0 / (1.0 + np.exp(-z))
+    return s * (1.0 + z * (1.0 - s))
+
+
+def grad(theta: np.ndarray, x: np.ndarray, t: np.ndarray):
+    """Gradient of mean((y - t)^2) with the GPU kernels' rounding points: the
+    backward GEMMs take BF16 dZ, BF16 activations and BF16 weights; bias,
+    output-layer and dZ values stay FP32."""
+    Ws, bs, wo, bo = unpack(theta)
+    y, acts, zs = forward(theta, x, keep=True)
+    n = len(y)
+    dy = (2.0 * (y.astype(np.float64) - t) / n)
+    g = {}
+    h3 = acts[4].astype(np.float64)
+    g["wo"] = dy @ h3
+    g["bo"] = dy.sum()
+    ft = np.float32 if ROUND_BF16 else np.float64
+    dz = (dy[:, None] * wo[None, :].astype(np.float64) * dsilu(zs[3].astype(np.float64))).astype(ft)
+    for l in range(3, -1, -1):
+        g[f"b{l}"] = dz.astype(np.float64).sum(axis=0)
+        dzb = bf16(dz).astype(np.float64)
+        g[f"W{l}"] = dzb.T @ acts[l].astype(np.float64)
+        if l > 0:
+            dh = dzb @ bf16(Ws[l]).astype(np.float64)
+            dz = (dh * dsilu(zs[l - 1].astype(np.float64))).astype(ft)
+    parts = [g["W0"].ravel(), g["b0"]]
+    for l in range(1, 4):
+        parts += [g[f"W{l}"].ravel(), g[f"b{l}"]]
+    parts += [g["wo"], np.array([g["bo"]])]
+    return np.concatenate(parts), float(np.mean((y.astype(np.float64) - t) ** 2))

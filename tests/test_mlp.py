@@ -45,3 +45,85 @@ def test_forward_kernel_matches_reference():
     err = np.abs(out - y)
     assert np.median(err) < 2e-3 * (1 + np.median(np.abs(y)))
     assert err.max() < 2e-2 * (1 + np.abs(y).max())
+
+
+def test_reference_gradient_matches_finite_differences():
+    """The NumPy backward formulas against central differences of the loss,
+    in exact arithmetic (BF16 rounding off): a few parameters of every
+    block."""
+    r = ref()
+    theta = r.init_params(5).astype(np.float64)
+    rng = np.random.default_rng(6)
+    x = rng.uniform(-1, 1, size=(64, 3))
+    t = rng.normal(0, 1, size=64)
+    r.ROUND_BF16 = False
+    try:
+        g, _ = r.grad(theta, x, t)
+
+        def loss(th):
+            return float(np.mean((r.forward(th, x) - t) ** 2))
+        o, idx = 0, []
+        for size in [r.H * r.NIN, r.H] + [r.H * r.H, r.H] * 3 + [r.H, 1]:
+            idx += [o, o + size // 2]
+            o += size
+        for i in sorted(set(idx)):
+            h = 1e-5
+            tp, tm = theta.copy(), theta.copy()
+            tp[i] += h
+            tm[i] -= h
+            fd = (loss(tp) - loss(tm)) / (2 * h)
+            assert fd == pytest.approx(g[i], rel=1e-4, abs=1e-9), i
+    finally:
+        r.ROUND_BF16 = True
+
+
+@pytest.mark.gpu
+def test_backward_kernel_matches_reference_gradient():
+    from xmimsim_gb300 import abi
+    r = ref()
+    lib = abi.load()
+    fp = C.POINTER(C.c_float)
+    lib.xmi_gpu_mlp_grad.restype = C.c_int
+    lib.xmi_gpu_mlp_grad.argtypes = [fp, C.c_int, fp, fp, fp, C.POINTER(C.c_double)]
+    theta = r.init_params(7)
+    rng = np.random.default_rng(8)
+    n = 300
+    x = rng.uniform(-1, 1, size=(n, 3)).astype(np.float32)
+    t = rng.normal(0, 1, size=n).astype(np.float32)
+    g = np.zeros(r.NPARAM, dtype=np.float32)
+    loss = C.c_double()
+    assert lib.xmi_gpu_mlp_grad(theta.ctypes.data_as(fp), n, x.ctypes.data_as(fp), t.ctypes.data_as(fp),
+                                g.ctypes.data_as(fp), C.byref(loss)) == 1, abi.last_error()
+    gr, lr = r.grad(theta, x, t.astype(np.float64))
+    assert loss.value == pytest.approx(lr, rel=1e-3)
+    assert np.linalg.norm(g - gr) <= 3e-2 * np.linalg.norm(gr)
+    # block by block
+    o = 0
+    for size in [r.H * r.NIN, r.H] + [r.H * r.H, r.H] * 3 + [r.H, 1]:
+        a, b = g[o:o + size], gr[o:o + size]
+        if np.linalg.norm(b) > 0:
+            assert np.linalg.norm(a - b) <= 5e-2 * np.linalg.norm(b) + 1e-7, o
+        o += size
+
+
+@pytest.mark.gpu
+def test_training_fits_a_smooth_function():
+    """A few epochs of the tensor-core training loop bring the loss of a
+    smooth target well below its variance."""
+    from xmimsim_gb300 import abi
+    r = ref()
+    lib = abi.load()
+    fp = C.POINTER(C.c_float)
+    lib.xmi_gpu_mlp_train.restype = C.c_int
+    lib.xmi_gpu_mlp_train.argtypes = [fp, C.c_int, fp, fp, C.c_int, C.c_float, C.POINTER(C.c_double)]
+    rng = np.random.default_rng(9)
+    n = 128 * 200
+    x = rng.uniform(-1, 1, size=(n, 3)).astype(np.float32)
+    t = (np.sin(2 * x[:, 0]) + x[:, 1] * x[:, 2] - 0.5 * x[:, 2] ** 2).astype(np.float32)
+    theta = r.init_params(10)
+    hist = np.zeros(100)
+    assert lib.xmi_gpu_mlp_train(theta.ctypes.data_as(fp), n, x.ctypes.data_as(fp), t.ctypes.data_as(fp), 100, 3e-3,
+                                 hist.ctypes.data_as(C.POINTER(C.c_double))) == 1, abi.last_error()
+    assert hist[-1] < 0.02 * t.var()
+    y = r.forward(theta, x[:2000])
+    assert np.mean((y - t[:2000]) ** 2) < 0.03 * t.var()

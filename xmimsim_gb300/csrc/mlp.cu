@@ -23,6 +23,7 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include <cmath>
 #include <cstdio>
 #include <vector>
 
@@ -163,12 +164,389 @@ __global__ void __launch_bounds__(128, 1) forward_kernel(const unsigned char *pa
   if (warp == 0) umma::tmem_dealloc(tmem, 128);
 }
 
+/* ---------------- training ---------------- */
+/* transposed hidden weights W_l^T (l = 1..3) as K-major tiles: element
+ * (in, out) = W_l[out][in]; the B operand of dX = dZ W_l */
+__global__ void pack_weights_t(const float *theta, unsigned char *packed_t) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < 3 * H * H) {
+    const int l = 1 + i / (H * H), r = i % (H * H), o = r / H, k = r % H;
+    *(__nv_bfloat16 *)(packed_t + (l - 1) * WL_BYTES + umma::kmajor_offset(k, o, H)) =
+        __float2bfloat16_rn(theta[off_w(l) + o * H + k]);
+  }
+}
+
+/* shared-memory plan of the training kernel */
+constexpr int TR_SW = 0;                  /* weight tile W_l (forward) or W_l^T (backward) */
+constexpr int TR_SA = TR_SW + WL_BYTES;   /* activations (forward) / dZ rows (backward) */
+constexpr int TR_SDT = TR_SA + WL_BYTES;  /* dZ^T (A operand of dW) */
+constexpr int TR_SB = TR_SDT + WL_BYTES;  /* a_l^T (B operand of dW) */
+constexpr int TR_SX0 = TR_SB + WL_BYTES;  /* input tile [128 x 16] */
+constexpr int TR_BIAS = TR_SX0 + H * KIN * 2;
+constexpr int TR_WO = TR_BIAS + 4 * H * 4;
+constexpr int TR_G = TR_WO + H * 4;       /* per-CTA partial gradients of b_0..b_3, w_o, b_o */
+constexpr int TR_NG = 4 * H + H + 1;
+constexpr int TR_BAR = TR_G + ((TR_NG * 4 + 15) / 16) * 16;
+constexpr int TR_TOTAL = TR_BAR + 16;
+static_assert(TR_TOTAL <= 227 * 1024, "training kernel shared memory");
+
+/* per-CTA global scratch: pre-activations Z_l^T [4][128 units][128 rows] FP32
+ * and input activations a_l^T as K-major tiles [4][32 KB] */
+constexpr size_t TR_SCRATCH_Z = (size_t)4 * H * H * 4;
+constexpr size_t TR_SCRATCH = TR_SCRATCH_Z + (size_t)4 * WL_BYTES;
+
+__device__ __forceinline__ void copy_tile(unsigned char *dst, const unsigned char *src, int bytes) {
+  for (int i = threadIdx.x; i < bytes / 16; i += blockDim.x) ((uint4 *)dst)[i] = ((const uint4 *)src)[i];
+}
+
+__device__ __forceinline__ float dsilu(float z) {
+  const float s = 1.0f / (1.0f + __expf(-z));
+  return s * (1.0f + z * (1.0f - s));
+}
+
+/* issues the MMAs of one GEMM: D (+)= A[128 x K] B[N x K]^T, K = 16 ksteps */
+__device__ __forceinline__ void gemm_issue(uint32_t d, uint32_t a, uint32_t a_sbo, uint32_t b, uint32_t b_sbo,
+                                           int ksteps, uint32_t idesc) {
+  for (int kk = 0; kk < ksteps; kk++)
+    umma::mma_bf16(d, umma::smem_desc(a + kk * 256, 128, a_sbo), umma::smem_desc(b + kk * 256, 128, b_sbo), idesc,
+                   kk > 0);
+}
+
+/* One gradient pass: each CTA takes the 128-row tiles tile0 + blockIdx.x,
+ * tile0 + blockIdx.x + gridDim.x, ... below n_tiles_used, runs forward and
+ * backward, and adds the gradient of sum((y - t)^2) * inv_batch to grad
+ * (FP32 atomics) and sum((y - t)^2) to *loss. */
+__global__ void __launch_bounds__(128, 1) train_kernel(const unsigned char *packed, const unsigned char *packed_t,
+                                                       const float *theta, const float *features,
+                                                       const float *targets, int n, int tile0, int n_tiles_used,
+                                                       float inv_batch, unsigned char *scratch, float *grad,
+                                                       double *loss, int *err) {
+  extern __shared__ __align__(1024) unsigned char sm[];
+  const int tid = threadIdx.x, warp = tid >> 5;
+  uint64_t *mbar = (uint64_t *)(sm + TR_BAR);
+  uint32_t *tmem_slot = (uint32_t *)(sm + TR_BAR + 8);
+  float *bias = (float *)(sm + TR_BIAS), *wo = (float *)(sm + TR_WO), *g = (float *)(sm + TR_G);
+  float *zt = (float *)(scratch + (size_t)blockIdx.x * TR_SCRATCH);
+  unsigned char *at = scratch + (size_t)blockIdx.x * TR_SCRATCH + TR_SCRATCH_Z;
+
+  for (int i = tid; i < H; i += blockDim.x) {
+    bias[i] = theta[OFF_B0 + i];
+    for (int l = 1; l <= 3; l++) bias[l * H + i] = theta[off_b(l) + i];
+    wo[i] = theta[OFF_WO + i];
+  }
+  for (int i = tid; i < TR_NG; i += blockDim.x) g[i] = 0.0f;
+  for (int i = tid; i < H * KIN * 2 / 16; i += blockDim.x) ((uint4 *)(sm + TR_SX0))[i] = make_uint4(0, 0, 0, 0);
+  const float bo = theta[OFF_BO];
+  if (warp == 0) umma::tmem_alloc(tmem_slot, 256);
+  if (tid == 0) {
+    umma::mbar_init(mbar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  umma::fence_proxy_async_smem();
+  umma::fence_before_sync();
+  __syncthreads();
+  umma::fence_after_sync();
+  const uint32_t tmem = *tmem_slot;
+  const uint32_t d1 = tmem, d2 = tmem + 128; /* dW accumulators, forward / dX accumulators */
+  const uint32_t lane_off = (uint32_t)(warp * 32) << 16;
+  const uint32_t s_w = umma::smem_u32(sm + TR_SW), s_a = umma::smem_u32(sm + TR_SA),
+                 s_dt = umma::smem_u32(sm + TR_SDT), s_b = umma::smem_u32(sm + TR_SB),
+                 s_x0 = umma::smem_u32(sm + TR_SX0);
+  uint32_t phase = 0;
+  bool failed = false;
+
+  /* issue (thread 0) after the CTA's operand writes, then wait for completion */
+  auto run_mma = [&](auto &&issue) -> bool {
+    umma::fence_proxy_async_smem();
+    umma::fence_before_sync();
+    __syncthreads();
+    if (tid == 0) {
+      umma::fence_after_sync();
+      issue();
+      umma::mma_commit(mbar);
+    }
+    const bool ok = umma::mbar_wait(mbar, phase);
+    phase ^= 1u;
+    const bool any_fail = __syncthreads_or(!ok);
+    umma::fence_after_sync();
+    return !any_fail;
+  };
+
+  for (int tile = tile0 + blockIdx.x; tile < tile0 + n_tiles_used && !failed; tile += gridDim.x) {
+    const int row = tile * 128 + tid;
+    const bool valid = row < n;
+    /* ---- forward ---- */
+    for (int k = 0; k < NIN; k++) {
+      const __nv_bfloat16 v = __float2bfloat16_rn(valid ? features[(size_t)row * NIN + k] : 0.0f);
+      *(__nv_bfloat16 *)(sm + TR_SX0 + umma::kmajor_offset(tid, k, KIN)) = v;
+      *(__nv_bfloat16 *)(at + umma::kmajor_offset(k, tid, H)) = v;
+    }
+    for (int k = NIN; k < KIN; k++) *(__nv_bfloat16 *)(at + umma::kmajor_offset(k, tid, H)) = __float2bfloat16_rn(0.0f);
+    float y = bo;
+    for (int l = 0; l < 4 && !failed; l++) {
+      copy_tile(sm + TR_SW, packed + (l == 0 ? 0 : W0_BYTES + (l - 1) * WL_BYTES), l == 0 ? W0_BYTES : WL_BYTES);
+      const uint32_t idesc = umma::idesc_bf16_f32(128, 128);
+      if (!run_mma([&] {
+            if (l == 0) gemm_issue(d2, s_x0, 256, s_w, 256, 1, idesc);
+            else gemm_issue(d2, s_a, 2048, s_w, 2048, H / 16, idesc);
+          })) {
+        failed = true;
+        break;
+      }
+#pragma unroll 1
+      for (int c = 0; c < H / 32; c++) {
+        float v[32];
+        umma::tmem_ld_32x32b_x32(d2 + lane_off + c * 32, v);
+#pragma unroll
+        for (int j = 0; j < 32; j++) {
+          const int col = c * 32 + j;
+          const float z = v[j] + bias[l * H + col];
+          zt[((size_t)l * H + col) * H + tid] = z;
+          const float h = silu(z);
+          if (l < 3) {
+            const __nv_bfloat16 a = __float2bfloat16_rn(h);
+            *(__nv_bfloat16 *)(sm + TR_SA + umma::kmajor_offset(tid, col, H)) = a;
+            *(__nv_bfloat16 *)(at + (size_t)(l + 1) * WL_BYTES + umma::kmajor_offset(col, tid, H)) = a;
+          } else {
+            y += h * wo[col];
+          }
+        }
+      }
+    }
+    if (failed) break;
+    /* ---- loss and output layer ---- */
+    const float diff = valid ? y - targets[row] : 0.0f;
+    const float dy = 2.0f * diff * inv_batch;
+    atomicAdd(loss, (double)diff * (double)diff);
+    atomicAdd(&g[4 * H + H], dy);
+    for (int col = 0; col < H; col++) {
+      const float z = zt[((size_t)3 * H + col) * H + tid];
+      atomicAdd(&g[4 * H + col], dy * silu(z));
+      const float dz = dy * wo[col] * dsilu(z);
+      atomicAdd(&g[3 * H + col], dz);
+      const __nv_bfloat16 bz = __float2bfloat16_rn(dz);
+      *(__nv_bfloat16 *)(sm + TR_SA + umma::kmajor_offset(tid, col, H)) = bz;
+      *(__nv_bfloat16 *)(sm + TR_SDT + umma::kmajor_offset(col, tid, H)) = bz;
+    }
+    /* ---- hidden layers, l = 3 .. 0: dW_l = dZ_l^T a_l, dZ_{l-1} = (dZ_l W_l) * SiLU'(Z_{l-1}) ---- */
+    for (int l = 3; l >= 0 && !failed; l--) {
+      const int nin = l == 0 ? KIN : H;
+      copy_tile(sm + TR_SB, at + (size_t)l * WL_BYTES, l == 0 ? KIN * H * 2 : WL_BYTES);
+      if (l > 0) copy_tile(sm + TR_SW, packed_t + (l - 1) * WL_BYTES, WL_BYTES);
+      if (!run_mma([&] {
+            gemm_issue(d1, s_dt, 2048, s_b, 2048, H / 16, umma::idesc_bf16_f32(128, nin));
+            if (l > 0) gemm_issue(d2, s_a, 2048, s_w, 2048, H / 16, umma::idesc_bf16_f32(128, 128));
+          })) {
+        failed = true;
+        break;
+      }
+      /* dW_l rows: thread = output unit */
+#pragma unroll 1
+      for (int c = 0; c < (nin + 31) / 32; c++) {
+        float v[32];
+        umma::tmem_ld_32x32b_x32(d1 + lane_off + c * 32, v);
+#pragma unroll
+        for (int j = 0; j < 32; j++) {
+          const int col = c * 32 + j;
+          if (l == 0) {
+            if (col < NIN) atomicAdd(&grad[OFF_W0 + tid * NIN + col], v[j]);
+          } else {
+            atomicAdd(&grad[off_w(l) + tid * H + col], v[j]);
+          }
+        }
+      }
+      if (l > 0) {
+        /* dZ_{l-1} rows: thread = sample */
+        __syncthreads(); /* every dZ_l operand read by the MMAs above is complete; safe to overwrite */
+#pragma unroll 1
+        for (int c = 0; c < H / 32; c++) {
+          float v[32];
+          umma::tmem_ld_32x32b_x32(d2 + lane_off + c * 32, v);
+#pragma unroll
+          for (int j = 0; j < 32; j++) {
+            const int col = c * 32 + j;
+            const float dz = valid ? v[j] * dsilu(zt[((size_t)(l - 1) * H + col) * H + tid]) : 0.0f;
+            atomicAdd(&g[(l - 1) * H + col], dz);
+            const __nv_bfloat16 bz = __float2bfloat16_rn(dz);
+            *(__nv_bfloat16 *)(sm + TR_SA + umma::kmajor_offset(tid, col, H)) = bz;
+            *(__nv_bfloat16 *)(sm + TR_SDT + umma::kmajor_offset(col, tid, H)) = bz;
+          }
+        }
+      }
+    }
+  }
+  __syncthreads();
+  for (int i = tid; i < TR_NG; i += blockDim.x) {
+    const float v = g[i];
+    if (v == 0.0f) continue;
+    int at_index;
+    if (i < 4 * H) at_index = (i < H ? OFF_B0 : off_b(i / H)) + i % H;
+    else if (i < 5 * H) at_index = OFF_WO + (i - 4 * H);
+    else at_index = OFF_BO;
+    atomicAdd(&grad[at_index], v);
+  }
+  if (failed && tid == 0) atomicExch(err, 1);
+  umma::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) umma::tmem_dealloc(tmem, 256);
+}
+
+/* Adam step on the FP32 master parameters; clears the gradient */
+__global__ void adam_kernel(float *theta, float *m, float *v, float *grad, float lr, float b1, float b2, float eps,
+                            float bc1, float bc2) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= NPARAM) return;
+  const float gi = grad[i];
+  grad[i] = 0.0f;
+  const float mi = b1 * m[i] + (1.0f - b1) * gi, vi = b2 * v[i] + (1.0f - b2) * gi * gi;
+  m[i] = mi;
+  v[i] = vi;
+  theta[i] -= lr * (mi / bc1) / (sqrtf(vi / bc2) + eps);
+}
+
 }  // namespace mlp
 }  // namespace xmi
 
 extern "C" {
 
 int xmi_mlp_nparam(void) { return xmi::mlp::NPARAM; }
+
+namespace {
+/* device state of one training / gradient session */
+struct MlpTrainer {
+  float *theta = nullptr, *m = nullptr, *v = nullptr, *grad = nullptr, *feat = nullptr, *targ = nullptr;
+  unsigned char *packed = nullptr, *packed_t = nullptr, *scratch = nullptr;
+  double *loss = nullptr;
+  int *err = nullptr;
+  int n = 0, grid = 1;
+  bool alloc(int n_rows, const float *theta_h, const float *feat_h, const float *targ_h) {
+    using namespace xmi::mlp;
+    n = n_rows;
+    int dev = 0, sms = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int tiles = (n + 127) / 128;
+    grid = tiles < sms ? tiles : sms;
+    bool ok = cudaMalloc(&theta, sizeof(float) * NPARAM) == cudaSuccess &&
+              cudaMalloc(&m, sizeof(float) * NPARAM) == cudaSuccess &&
+              cudaMalloc(&v, sizeof(float) * NPARAM) == cudaSuccess &&
+              cudaMalloc(&grad, sizeof(float) * NPARAM) == cudaSuccess &&
+              cudaMalloc(&feat, sizeof(float) * 3 * (size_t)n) == cudaSuccess &&
+              cudaMalloc(&targ, sizeof(float) * (size_t)n) == cudaSuccess &&
+              cudaMalloc(&packed, PACK_BYTES) == cudaSuccess && cudaMalloc(&packed_t, 3 * WL_BYTES) == cudaSuccess &&
+              cudaMalloc(&scratch, TR_SCRATCH * (size_t)grid) == cudaSuccess &&
+              cudaMalloc(&loss, sizeof(double)) == cudaSuccess && cudaMalloc(&err, sizeof(int)) == cudaSuccess;
+    if (!ok) return false;
+    cudaMemcpy(theta, theta_h, sizeof(float) * NPARAM, cudaMemcpyHostToDevice);
+    cudaMemcpy(feat, feat_h, sizeof(float) * 3 * (size_t)n, cudaMemcpyHostToDevice);
+    cudaMemcpy(targ, targ_h, sizeof(float) * (size_t)n, cudaMemcpyHostToDevice);
+    cudaMemset(m, 0, sizeof(float) * NPARAM);
+    cudaMemset(v, 0, sizeof(float) * NPARAM);
+    cudaMemset(grad, 0, sizeof(float) * NPARAM);
+    cudaMemset(err, 0, sizeof(int));
+    cudaFuncSetAttribute(train_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, TR_TOTAL);
+    return true;
+  }
+  /* gradient of the mean squared error over tiles [tile0, tile0 + ntiles) */
+  void grad_pass(int tile0, int ntiles, int rows) {
+    using namespace xmi::mlp;
+    pack_weights<<<(3 * H * H + 255) / 256, 256>>>(theta, packed);
+    pack_weights_t<<<(3 * H * H + 255) / 256, 256>>>(theta, packed_t);
+    cudaMemsetAsync(loss, 0, sizeof(double));
+    const int g = ntiles < grid ? ntiles : grid;
+    train_kernel<<<g, 128, TR_TOTAL>>>(packed, packed_t, theta, feat, targ, n, tile0, ntiles, 1.0f / (float)rows,
+                                       scratch, grad, loss, err);
+  }
+  void release() {
+    cudaFree(theta); cudaFree(m); cudaFree(v); cudaFree(grad); cudaFree(feat); cudaFree(targ);
+    cudaFree(packed); cudaFree(packed_t); cudaFree(scratch); cudaFree(loss); cudaFree(err);
+  }
+};
+
+bool finish(MlpTrainer &tr, const char *what) {
+  cudaError_t e = cudaDeviceSynchronize();
+  int h_err = 0;
+  if (e == cudaSuccess) cudaMemcpy(&h_err, tr.err, sizeof(int), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) {
+    xmi_set_error("%s: %s", what, cudaGetErrorString(e));
+    return false;
+  }
+  if (h_err) {
+    xmi_set_error("%s: tensor-core wait ran out", what);
+    return false;
+  }
+  return true;
+}
+}  // namespace
+
+/* Gradient of the mean squared error of the network over n rows (host
+ * arrays): grad[NPARAM], *loss = mean squared error.  For the checks of the
+ * tensor-core backward pass. */
+int xmi_gpu_mlp_grad(const float *theta, int n, const float *features, const float *targets, float *grad,
+                     double *loss) {
+  using namespace xmi::mlp;
+  if (!theta || !features || !targets || !grad || n < 1) {
+    xmi_set_error("xmi_gpu_mlp_grad: invalid arguments");
+    return 0;
+  }
+  MlpTrainer tr;
+  bool ok = tr.alloc(n, theta, features, targets);
+  if (ok) {
+    tr.grad_pass(0, (n + 127) / 128, n);
+    ok = finish(tr, "xmi_gpu_mlp_grad");
+    if (ok) {
+      double l = 0.0;
+      cudaMemcpy(grad, tr.grad, sizeof(float) * NPARAM, cudaMemcpyDeviceToHost);
+      cudaMemcpy(&l, tr.loss, sizeof(double), cudaMemcpyDeviceToHost);
+      if (loss) *loss = l / n;
+    }
+  } else {
+    xmi_set_error("xmi_gpu_mlp_grad: cudaMalloc failed");
+  }
+  tr.release();
+  return ok ? 1 : 0;
+}
+
+/* Adam training of the network on n rows (host arrays), in place on theta:
+ * each step takes one 128-row tile per SM (the rows are used in order, so
+ * shuffle them beforehand), epochs passes over the data, learning rate lr
+ * decaying by a cosine to lr/100.  loss_per_epoch[epochs] (may be NULL)
+ * receives the mean squared error seen during each epoch. */
+int xmi_gpu_mlp_train(float *theta, int n, const float *features, const float *targets, int epochs, float lr,
+                      double *loss_per_epoch) {
+  using namespace xmi::mlp;
+  if (!theta || !features || !targets || n < 1 || epochs < 1) {
+    xmi_set_error("xmi_gpu_mlp_train: invalid arguments");
+    return 0;
+  }
+  MlpTrainer tr;
+  bool ok = tr.alloc(n, theta, features, targets);
+  if (!ok) xmi_set_error("xmi_gpu_mlp_train: cudaMalloc failed");
+  const int tiles = (n + 127) / 128;
+  const int steps_per_epoch = (tiles + tr.grid - 1) / tr.grid;
+  const int total = steps_per_epoch * epochs;
+  int step = 0;
+  for (int ep = 0; ok && ep < epochs; ep++) {
+    double ep_loss = 0.0;
+    for (int s = 0; s < steps_per_epoch; s++, step++) {
+      const int tile0 = s * tr.grid, nt = tile0 + tr.grid <= tiles ? tr.grid : tiles - tile0;
+      const int rows = (tile0 + nt) * 128 <= n ? nt * 128 : n - tile0 * 128;
+      tr.grad_pass(tile0, nt, rows);
+      const float frac = (float)step / (float)(total > 1 ? total - 1 : 1);
+      const float lr_t = lr * (0.01f + 0.99f * 0.5f * (1.0f + cosf(3.14159265f * frac)));
+      const float bc1 = 1.0f - powf(0.9f, (float)(step + 1)), bc2 = 1.0f - powf(0.999f, (float)(step + 1));
+      adam_kernel<<<(NPARAM + 255) / 256, 256>>>(tr.theta, tr.m, tr.v, tr.grad, lr_t, 0.9f, 0.999f, 1e-8f, bc1, bc2);
+      double l = 0.0;
+      cudaMemcpy(&l, tr.loss, sizeof(double), cudaMemcpyDeviceToHost);
+      ep_loss += l;
+    }
+    if (loss_per_epoch) loss_per_epoch[ep] = ep_loss / n;
+    ok = finish(tr, "xmi_gpu_mlp_train");
+  }
+  if (ok) cudaMemcpy(theta, tr.theta, sizeof(float) * NPARAM, cudaMemcpyDeviceToHost);
+  tr.release();
+  return ok ? 1 : 0;
+}
 
 /* Network outputs for n feature rows with the FP32 parameter vector theta
  * (host arrays); for tests of the tensor-core kernels. */
