@@ -132,6 +132,35 @@ int xmi_main_msim_batch(int n, xmi_inputFPtr *inputFPtrs, xmi_hdf5FPtr *hdf5FPtr
                         xmi_solid_angle **solid_angles, double **channels, double **brute_histories,
                         double **var_red_histories);
 
+/* ---- solid-angle surrogate network (no counterpart in the reference) ----
+ * A 3 -> 4 x 128 (SiLU) -> 1 network, BF16 weights and FP32 accumulation on
+ * the tensor cores, maps a point's (log r, axial distance, cos angle) to the
+ * log of its collimated detector solid angle.  xmi_gpu_build_surrogate trains
+ * it for an initialised input: n_train points uniform in (log r, theta) over
+ * the box of the solid-angle grid, targets from the engine's own integrator
+ * (hits_train cone samples each, FP32), Adam for `epochs` passes; then checks
+ * it on 4 points per cell of a 32 x 32 partition of the box against the FP64
+ * integrator (hits_check samples) and flags the cells whose error exceeds
+ * xmi_gpu_options.surrogate_tolerance: there the integrator keeps serving.
+ * report[6]: median relative error of the checking points, largest error in
+ * an unflagged cell, fraction of flagged cells, final training loss, seconds,
+ * number of cells.  With xmi_gpu_options.use_surrogate = 1, xmi_main_msim
+ * then needs no solid-angle grid. */
+int xmi_gpu_build_surrogate(xmi_inputFPtr inputFPtr, int n_train, int hits_train, int epochs, int hits_check,
+                            double *report);
+int xmi_gpu_surrogate_report(xmi_inputFPtr inputFPtr, double *report);
+/* device time of the surrogate phase of the last xmi_main_msim and the
+ * number of estimator events served by the integrator fallback */
+int xmi_gpu_last_surrogate(double *surrogate_ms, long long *fallbacks);
+/* the network alone, for tests of the tensor-core kernels: parameter count,
+ * outputs, gradient of the mean squared error, Adam training */
+int xmi_mlp_nparam(void);
+int xmi_gpu_mlp_forward(const float *theta, int n, const float *features, float *out);
+int xmi_gpu_mlp_grad(const float *theta, int n, const float *features, const float *targets, float *grad,
+                     double *loss);
+int xmi_gpu_mlp_train(float *theta, int n, const float *features, const float *targets, int epochs, float lr,
+                      double *loss_per_epoch);
+
 /* ---- escape ratios (include/xmi_detector.h:55-57) ---- */
 xmi_escape_ratios_options xmi_get_default_escape_ratios_options(void);
 void xmi_escape_ratios_calculation(xmi_input *inputPtr, xmi_escape_ratios **escape_ratios,

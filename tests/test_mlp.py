@@ -127,3 +127,39 @@ def test_training_fits_a_smooth_function():
     assert hist[-1] < 0.02 * t.var()
     y = r.forward(theta, x[:2000])
     assert np.mean((y - t[:2000]) ** 2) < 0.03 * t.var()
+
+
+def collimated_spec(n_photons: int):
+    """The surrogate workload: config-1 sample, conical collimator of height
+    1 cm and opening radius 0.1 cm, 45 degrees, 10 cm from the sample."""
+    from xmimsim_gb300 import configs
+    spec = configs.config1(n_photons_line=n_photons)
+    spec.collimator_height = 1.0
+    spec.collimator_diameter = 0.2
+    return spec
+
+
+@pytest.mark.gpu
+def test_surrogate_replaces_the_grid_in_transport():
+    """Trains the surrogate on the collimated geometry (reduced budget), then
+    runs the transport with it: every first-order line intensity within 3%
+    of the grid run (whose own grid noise is ~1.4% per point) and the total
+    within 1%; the training report is sane."""
+    from xmimsim_gb300 import Simulation, configs, gpu_options
+    spec = collimated_spec(20000)
+    grid = Simulation(spec, options=configs.C1_OPTIONS, gpu=gpu_options(seed=0x5EED0001))
+    ref_out = grid.msim()
+    sur = Simulation(spec, options=configs.C1_OPTIONS, gpu=gpu_options(seed=0x5EED0001, use_surrogate=1,
+                                                                       surrogate_tolerance=2e-2))
+    rep = sur.build_surrogate(n_train=1 << 18, hits_train=2048, epochs=20, hits_check=1 << 16)
+    assert rep["cells"] == 1024 and 0 <= rep["flagged_fraction"] < 1
+    assert rep["median_rel_err"] < 0.05
+    out = sur.msim()
+    tm = sur.timing()
+    assert tm["surrogate_ms"] > 0
+    v_g, v_s = ref_out["var_red"][:, :, 0], out["var_red"][:, :, 0]
+    assert v_s.sum() == pytest.approx(v_g.sum(), rel=1e-2)
+    big = v_g > 1e-3 * v_g.max()
+    np.testing.assert_allclose(v_s[big], v_g[big], rtol=3e-2)
+    grid.close()
+    sur.close()

@@ -155,6 +155,15 @@ PROTOTYPES = {
     "xmi_gpu_last_timing": (C.c_int, [c_double_p, c_double_p, c_int_p]),
     "xmi_gpu_last_phases": (C.c_int, [c_double_p, c_double_p, c_double_p, C.POINTER(C.c_longlong)]),
     "xmi_gpu_set_replica": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
+    "xmi_gpu_build_surrogate": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, c_double_p]),
+    "xmi_gpu_surrogate_report": (C.c_int, [C.c_void_p, c_double_p]),
+    "xmi_gpu_last_surrogate": (C.c_int, [c_double_p, C.POINTER(C.c_longlong)]),
+    "xmi_mlp_nparam": (C.c_int, []),
+    "xmi_gpu_mlp_forward": (C.c_int, [C.POINTER(C.c_float), C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
+    "xmi_gpu_mlp_grad": (C.c_int, [C.POINTER(C.c_float), C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_float),
+                                   C.POINTER(C.c_float), c_double_p]),
+    "xmi_gpu_mlp_train": (C.c_int, [C.POINTER(C.c_float), C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_float),
+                                    C.c_int, C.c_float, c_double_p]),
     "xmi_main_msim_batch": (C.c_int, [C.c_int, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p),
                                       C.POINTER(C.POINTER(XmiMainOptions)), C.POINTER(C.POINTER(XmiSolidAngle)),
                                       C.POINTER(c_double_p), C.POINTER(c_double_p), C.POINTER(c_double_p)]),

@@ -21,6 +21,7 @@ struct DevBundle {
   int N, nch, use_vr, use_M_lines, line_last, max_shell, escape_mode;
   int n_layers, n_elem, n_lines, n_slots, n_nodes, n_seg, n_items, n_layer_el;
   int coll_present, sa_nr, sa_nt, sa_hits;
+  int use_surrogate; /* solid angles of the estimator from the surrogate network */
   unsigned long long seed;
   long long n_photons_total;
   double gain, zero;

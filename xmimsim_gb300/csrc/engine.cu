@@ -26,9 +26,9 @@ namespace {
 struct Timing {
   double transport_ms = 0.0, total_ms = 0.0;
   int launches = 0;
-  /* phases of the last xmi_main_msim: transport kernel, event sort, estimator kernel */
-  double phase_ms[3] = {0.0, 0.0, 0.0};
-  long long events = 0;
+  /* phases of the last xmi_main_msim: transport, event sort, surrogate solid angles, estimator */
+  double phase_ms[4] = {0.0, 0.0, 0.0, 0.0};
+  long long events = 0, surrogate_fallbacks = 0;
 };
 thread_local Timing g_timing;
 
@@ -344,8 +344,14 @@ int xmi_gpu_last_timing(double *transport_ms, double *total_ms, int *launches) {
 int xmi_gpu_last_phases(double *transport_kernel_ms, double *sort_ms, double *estimator_ms, long long *events) {
   if (transport_kernel_ms) *transport_kernel_ms = g_timing.phase_ms[0];
   if (sort_ms) *sort_ms = g_timing.phase_ms[1];
-  if (estimator_ms) *estimator_ms = g_timing.phase_ms[2];
+  if (estimator_ms) *estimator_ms = g_timing.phase_ms[3];
   if (events) *events = g_timing.events;
+  return 1;
+}
+
+int xmi_gpu_last_surrogate(double *surrogate_ms, long long *fallbacks) {
+  if (surrogate_ms) *surrogate_ms = g_timing.phase_ms[2];
+  if (fallbacks) *fallbacks = g_timing.surrogate_fallbacks;
   return 1;
 }
 
@@ -492,14 +498,19 @@ int xmi_gpu_prepare_run(xmi_inputFPtr in, xmi_hdf5FPtr t, xmi_main_options *opti
     xmi_bundle_set_run(in, t, options, n_mpi_hosts, r, R);
   }
   attach_solid_angles(t, sa);
-  if (options->use_variance_reduction && (!sa || !sa->solid_angles)) {
-    xmi_set_error("variance reduction requires a solid angle grid");
+  if (options->use_variance_reduction && (!sa || !sa->solid_angles) && !(in->gpu.use_surrogate && in->surrogate)) {
+    xmi_set_error("variance reduction requires a solid angle grid (or a trained surrogate with use_surrogate = 1)");
     return 0;
   }
   return 1;
 }
 
 }  // extern "C"
+
+/* the estimator's solid angles come from the input's trained surrogate */
+static bool surrogate_in_use(xmi_inputFPtr in, const xmi_main_options *options) {
+  return in && in->gpu.use_surrogate && in->surrogate && options && options->use_variance_reduction == 1;
+}
 
 /* events held on the device per chunk; a chunk is as many photons as can
  * each make N estimator events (one per interaction) within it */
@@ -585,7 +596,7 @@ static bool ensure_queue(EventQueue &q, long long cap, int nkeys) {
 }
 
 struct Phases {
-  double ms[3] = {0.0, 0.0, 0.0}; /* transport kernel, event sort, estimator kernel */
+  double ms[4] = {0.0, 0.0, 0.0, 0.0}; /* transport kernel, event sort, surrogate solid angles, estimator kernel */
   double total_ms = 0.0;
   int launches = 0;
 };
@@ -594,9 +605,9 @@ struct Phases {
  * launch (events into the queue), the counting sort of the events by key and
  * the estimator launch.  CUDA events around each phase give the device times.
  * transport(w0, w1, vq) and estimator(vq, order) enqueue the two kernels. */
-template <typename R, typename TF, typename EF>
+template <typename R, typename TF, typename SF, typename EF>
 static bool run_chunks(cudaStream_t st, EventQueue &q, long long n, int N, int nkeys, bool vr,
-                       unsigned long long *total_events, TF &&transport, EF &&estimator, Phases &ph,
+                       unsigned long long *total_events, TF &&transport, SF &&surrogate, EF &&estimator, Phases &ph,
                        bool graph = false) {
   const int sms = num_sms();
   long long chunk = n < kMaxChunkPhotons ? n : kMaxChunkPhotons;
@@ -643,6 +654,8 @@ static bool run_chunks(cudaStream_t st, EventQueue &q, long long n, int N, int n
       xmi::event_key_scatter<<<sms * 4, 256, 0, st>>>(q.key, q.count, vq.cap, nkeys, q.hist + nkeys, q.order);
       cudaMemsetAsync(q.count + 1, 0, sizeof(unsigned long long), st);
       mark();
+      launches += surrogate(vq);
+      mark();
       estimator(vq, (const int *)q.order, q.count + 1);
       mark();
       launches += 4;
@@ -662,7 +675,7 @@ static bool run_chunks(cudaStream_t st, EventQueue &q, long long n, int N, int n
     float total = 0.f;
     cudaEventElapsedTime(&total, marks.front(), marks.back());
     ph.total_ms = total;
-    const size_t per = vr ? 3 : 1;
+    const size_t per = vr ? 4 : 1;
     for (size_t i = 0; i + per < marks.size(); i += per)
       for (size_t k = 0; k < per; k++) {
         float f = 0.f;
@@ -679,7 +692,7 @@ static bool run_chunks(cudaStream_t st, EventQueue &q, long long n, int N, int n
  * items, solid-angle grid), clears its tallies and fills the run fields of
  * its device bundle and tally view.  Copies go to the handle's stream. */
 template <typename R>
-static bool stage_run(DevState *s, xmi::DevBundle<R> &d, const xmi_bundle &h, xmi::DevTally &tl) {
+static bool stage_run(DevState *s, xmi::DevBundle<R> &d, const xmi_bundle &h, xmi::DevTally &tl, bool surrogate) {
   std::vector<long long> first(h.n_items > 0 ? h.n_items : 1, 0);
   for (int i = 1; i < h.n_items; i++) first[i] = first[i - 1] + h.items[i - 1].n_photons;
   if (h.n_items > s->items_cap) {
@@ -744,7 +757,8 @@ static bool stage_run(DevState *s, xmi::DevBundle<R> &d, const xmi_bundle &h, xm
   d.sa_t = s->sa_t;
   d.sa_nr = h.sa_nr;
   d.sa_nt = h.sa_nt;
-  d.sa_hits = h.sa_hits_per_single;
+  d.sa_hits = h.sa_hits_per_single > 0 ? h.sa_hits_per_single : (int)hits_per_single;
+  d.use_surrogate = surrogate ? 1 : 0;
   if (h.sa_nr > 1) {
     d.sa_r0 = h.sa_r[0];
     d.sa_rinv = (h.sa_nr - 1) / (h.sa_r[h.sa_nr - 1] - h.sa_r[0]);
@@ -778,7 +792,7 @@ static int estimator_blocks(int stage_cap, size_t *smem) {
 /* one configuration on its handle's stream */
 template <typename R>
 static bool launch_single(DevState *s, xmi::DevBundle<R> &d, const xmi::DevTally &tl, const xmi_bundle &h,
-                          int threads, int blocks_per_sm, Phases &ph) {
+                          int threads, int blocks_per_sm, const void *sg, Phases &ph) {
   const int sms = num_sms();
   if (!s->d_bundle && !cuda_ok(cudaMalloc(&s->d_bundle, sizeof(xmi::DevBundle<double>)), "cudaMalloc")) return false;
   if (!s->d_tally && !cuda_ok(cudaMalloc(&s->d_tally, sizeof(xmi::DevTally)), "cudaMalloc")) return false;
@@ -802,13 +816,20 @@ static bool launch_single(DevState *s, xmi::DevBundle<R> &d, const xmi::DevTally
         (const xmi::DevBundle<R> *)s->d_bundle, s->d_tally, 1, vq.ev, order, vq.count, vq.cap, work, stage_cap,
         &s->counters[1]);
   };
+  auto surrogate = [&](const xmi::VrQueue<R> &vq) -> int {
+    if (!d.use_surrogate) return 0;
+    xmi_surrogate_apply(sg, sizeof(R) == 8 ? 0 : 1, s->d_bundle, vq.ev, vq.count, vq.cap, &s->counters[4],
+                        (int *)&s->counters[5], s->stream);
+    return 1;
+  };
   return run_chunks<R>(s->stream, s->q, h.n_photons_total, h.n_interactions, XMI_MAXL * XMI_MAXN, h.use_vr != 0,
-                       &s->counters[3], transport, estimator, ph);
+                       &s->counters[3], transport, surrogate, estimator, ph);
 }
 
 /* device tallies -> the reference's output layouts (host) */
 static int collect_outputs(DevState *s, const xmi_bundle &h, int n_mpi_hosts, double **channels_out,
-                           double **brute_out, double **var_red_out, unsigned long long *events) {
+                           double **brute_out, double **var_red_out, unsigned long long *events,
+                           unsigned long long *fallbacks = nullptr) {
   const int N = h.n_interactions, nch = h.nchannels, S = h.n_slots;
   const size_t nh = (size_t)N * S, nc = (size_t)(N + 1) * nch;
   std::vector<double> tally(2 * nh + nc);
@@ -820,7 +841,12 @@ static int collect_outputs(DevState *s, const xmi_bundle &h, int n_mpi_hosts, do
     xmi_set_error("transport kernel reported error code %llu", counters[1]);
     return 0;
   }
+  if (counters[5] != 0) {
+    xmi_set_error("surrogate solid-angle kernel: tensor-core wait ran out");
+    return 0;
+  }
   if (events) *events = counters[3];
+  if (fallbacks) *fallbacks = counters[4];
   const double *hv = tally.data(), *hb = tally.data() + nh, *chan = tally.data() + 2 * nh;
 
   /* channels: per-order scatter tallies plus the fluorescence lines derived
@@ -880,11 +906,14 @@ extern "C" int xmi_main_msim(xmi_inputFPtr in, xmi_hdf5FPtr t, int n_mpi_hosts, 
   const int threads = in->gpu.threads_per_block > 0 ? in->gpu.threads_per_block : 128;
   const int bps = in->gpu.blocks_per_sm > 0 ? in->gpu.blocks_per_sm : 8;
   Phases ph;
-  bool ok = precision == 0 ? stage_run<double>(s, s->b64, h, tl) && launch_single<double>(s, s->b64, tl, h, threads, bps, ph)
-                           : stage_run<float>(s, s->b32, h, tl) && launch_single<float>(s, s->b32, tl, h, threads, bps, ph);
+  const bool use_sg = surrogate_in_use(in, options);
+  const void *sg = use_sg ? in->surrogate : nullptr;
+  bool ok = precision == 0
+                ? stage_run<double>(s, s->b64, h, tl, use_sg) && launch_single<double>(s, s->b64, tl, h, threads, bps, sg, ph)
+                : stage_run<float>(s, s->b32, h, tl, use_sg) && launch_single<float>(s, s->b32, tl, h, threads, bps, sg, ph);
   if (!ok) return 0;
-  unsigned long long events = 0;
-  if (!collect_outputs(s, h, n_mpi_hosts, channels_out, brute_out, var_red_out, &events)) return 0;
+  unsigned long long events = 0, fallbacks = 0;
+  if (!collect_outputs(s, h, n_mpi_hosts, channels_out, brute_out, var_red_out, &events, &fallbacks)) return 0;
   cudaEventRecord(all1, s->stream);
   cudaEventSynchronize(all1);
   float tot = 0.f;
@@ -894,8 +923,9 @@ extern "C" int xmi_main_msim(xmi_inputFPtr in, xmi_hdf5FPtr t, int n_mpi_hosts, 
   g_timing.transport_ms = ph.total_ms;
   g_timing.total_ms = tot;
   g_timing.launches = ph.launches;
-  for (int k = 0; k < 3; k++) g_timing.phase_ms[k] = ph.ms[k];
+  for (int k = 0; k < 4; k++) g_timing.phase_ms[k] = ph.ms[k];
   g_timing.events = (long long)events;
+  g_timing.surrogate_fallbacks = (long long)fallbacks;
   return 1;
 }
 
@@ -979,7 +1009,9 @@ bool launch_batch(int n, DevState **st, xmi_hdf5FPtr *t, const xmi::DevTally *tl
     xmi::estimator_kernel<R><<<est_blocks, 256, smem, B.stream>>>(db, B.tallies, n, vq.ev, order, vq.count, vq.cap,
                                                                   work, stage_cap, B.flags);
   };
-  if (!run_chunks<R>(B.stream, B.q, first[n], N, n * XMI_MAXL * XMI_MAXN, vr, &B.flags[1], transport, estimator, ph,
+  auto no_surrogate = [](const xmi::VrQueue<R> &) -> int { return 0; };
+  if (!run_chunks<R>(B.stream, B.q, first[n], N, n * XMI_MAXL * XMI_MAXN, vr, &B.flags[1], transport, no_surrogate,
+                     estimator, ph,
                      graph))
     return false;
   unsigned long long flags[2];
@@ -1017,7 +1049,8 @@ extern "C" int xmi_main_msim_batch(int n, xmi_inputFPtr *inputFPtrs, xmi_hdf5FPt
     if (!xmi_dev_sync_tables(hdf5FPtrs[c], precision)) return 0;
     st[c] = state_of(hdf5FPtrs[c]);
     const xmi_bundle &h = hdf5FPtrs[c]->b;
-    bool ok = precision == 0 ? stage_run<double>(st[c], st[c]->b64, h, tl[c]) : stage_run<float>(st[c], st[c]->b32, h, tl[c]);
+    bool ok = precision == 0 ? stage_run<double>(st[c], st[c]->b64, h, tl[c], false)
+                             : stage_run<float>(st[c], st[c]->b32, h, tl[c], false);
     if (!ok) return 0;
   }
   for (int c = 0; c < n; c++)
@@ -1035,6 +1068,6 @@ extern "C" int xmi_main_msim_batch(int n, xmi_inputFPtr *inputFPtrs, xmi_hdf5FPt
   g_timing.transport_ms = ph.total_ms;
   g_timing.total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - wall0).count();
   g_timing.launches = ph.launches;
-  for (int k = 0; k < 3; k++) g_timing.phase_ms[k] = ph.ms[k];
+  for (int k = 0; k < 4; k++) g_timing.phase_ms[k] = ph.ms[k];
   return 1;
 }

@@ -316,6 +316,7 @@ int xmi_input_C2F(xmi_input *input, xmi_inputFPtr *inputFPtr) {
 void xmi_free_input_F(xmi_inputFPtr *p) {
   if (!p || !*p) return;
   xmi_input_free((*p)->input);
+  xmi_surrogate_free((*p)->surrogate);
   free(*p);
   *p = NULL;
 }

@@ -23,10 +23,14 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
+#include <random>
 #include <vector>
 
+#include "solid_angle.cuh"
 #include "umma.cuh"
 #include "xmi_internal.h"
 
@@ -73,95 +77,193 @@ __global__ void pack_weights(const float *theta, unsigned char *packed) {
 
 __device__ __forceinline__ float silu(float z) { return z / (1.0f + __expf(-z)); }
 
-/* features [n][3] (already scaled) -> out [n] = network output (log solid
- * angle); *err set non-zero when a wait ran out */
-__global__ void __launch_bounds__(128, 1) forward_kernel(const unsigned char *packed, const float *theta,
-                                                         const float *features, float *out, int n, int *err) {
-  extern __shared__ __align__(1024) unsigned char sm[];
-  const int tid = threadIdx.x, warp = tid >> 5;
-  uint64_t *mbar = (uint64_t *)(sm + SM_BAR);
-  uint32_t *tmem_slot = (uint32_t *)(sm + SM_BAR + 8);
-  float *bias = (float *)(sm + SM_BIAS), *wo = (float *)(sm + SM_WO);
+/* per-CTA context of the tensor-core forward pass (weights resident in
+ * shared memory, one 128-column TMEM accumulator) */
+struct FwdCtx {
+  uint64_t *mbar;
+  float *bias, *wo;
+  float bo;
+  uint32_t tmem, trow, s_x0, s_a, s_w, phase;
+};
 
-  /* weights and biases into shared memory */
+__device__ void fwd_setup(unsigned char *sm, const unsigned char *packed, const float *theta, FwdCtx &c) {
+  const int tid = threadIdx.x, warp = tid >> 5;
+  c.mbar = (uint64_t *)(sm + SM_BAR);
+  uint32_t *tmem_slot = (uint32_t *)(sm + SM_BAR + 8);
+  c.bias = (float *)(sm + SM_BIAS);
+  c.wo = (float *)(sm + SM_WO);
   for (int i = tid; i < PACK_BYTES / 16; i += blockDim.x) ((uint4 *)(sm + SM_W))[i] = ((const uint4 *)packed)[i];
   for (int i = tid; i < H; i += blockDim.x) {
-    bias[i] = theta[OFF_B0 + i];
-    for (int l = 1; l <= 3; l++) bias[l * H + i] = theta[off_b(l) + i];
-    wo[i] = theta[OFF_WO + i];
+    c.bias[i] = theta[OFF_B0 + i];
+    for (int l = 1; l <= 3; l++) c.bias[l * H + i] = theta[off_b(l) + i];
+    c.wo[i] = theta[OFF_WO + i];
   }
   for (int i = tid; i < H * KIN * 2 / 16; i += blockDim.x) ((uint4 *)(sm + SM_X0))[i] = make_uint4(0, 0, 0, 0);
-  const float bo = theta[OFF_BO];
+  c.bo = theta[OFF_BO];
   if (warp == 0) umma::tmem_alloc(tmem_slot, 128);
   if (tid == 0) {
-    umma::mbar_init(mbar, 1);
+    umma::mbar_init(c.mbar, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   umma::fence_proxy_async_smem();
   umma::fence_before_sync();
   __syncthreads();
   umma::fence_after_sync();
-  const uint32_t tmem = *tmem_slot;
-  const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
-  const uint32_t idesc = umma::idesc_bf16_f32(128, 128);
-  const uint32_t s_x0 = umma::smem_u32(sm + SM_X0), s_a = umma::smem_u32(sm + SM_A), s_w = umma::smem_u32(sm + SM_W);
-  uint32_t phase = 0;
-  bool failed = false;
+  c.tmem = *tmem_slot;
+  c.trow = c.tmem + ((uint32_t)(warp * 32) << 16);
+  c.s_x0 = umma::smem_u32(sm + SM_X0);
+  c.s_a = umma::smem_u32(sm + SM_A);
+  c.s_w = umma::smem_u32(sm + SM_W);
+  c.phase = 0;
+}
 
-  for (int tile = blockIdx.x; tile * 128 < n && !failed; tile += gridDim.x) {
-    const int row = tile * 128 + tid;
-    const bool valid = row < n;
+/* network output for this thread's feature row f (tile row = thread); all
+ * 128 threads call it together; false (for every thread) when a wait ran out */
+__device__ bool fwd_tile(unsigned char *sm, FwdCtx &c, const float *f, float &y) {
+  const int tid = threadIdx.x;
+  const uint32_t idesc = umma::idesc_bf16_f32(128, 128);
 #pragma unroll
-    for (int k = 0; k < NIN; k++) {
-      const float v = valid ? features[(size_t)row * NIN + k] : 0.0f;
-      *(__nv_bfloat16 *)(sm + SM_X0 + umma::kmajor_offset(tid, k, KIN)) = __float2bfloat16_rn(v);
-    }
-    float acc_out = bo;
-    for (int l = 0; l < 4; l++) {
-      umma::fence_proxy_async_smem();
-      umma::fence_before_sync();
-      __syncthreads();
-      if (tid == 0) {
-        umma::fence_after_sync();
-        if (l == 0) {
-          umma::mma_bf16(tmem, umma::smem_desc(s_x0, 128, 256), umma::smem_desc(s_w, 128, 256), idesc, false);
-        } else {
-          const uint32_t wl = s_w + W0_BYTES + (l - 1) * WL_BYTES;
-#pragma unroll
-          for (int kk = 0; kk < H / 16; kk++)
-            umma::mma_bf16(tmem, umma::smem_desc(s_a + kk * 256, 128, 2048), umma::smem_desc(wl + kk * 256, 128, 2048),
-                           idesc, kk > 0);
-        }
-        umma::mma_commit(mbar);
-      }
-      const bool ok = umma::mbar_wait(mbar, phase);
-      phase ^= 1u;
-      if (__syncthreads_or(!ok)) {
-        failed = true;
-        break;
-      }
+  for (int k = 0; k < NIN; k++)
+    *(__nv_bfloat16 *)(sm + SM_X0 + umma::kmajor_offset(tid, k, KIN)) = __float2bfloat16_rn(f[k]);
+  y = c.bo;
+  for (int l = 0; l < 4; l++) {
+    umma::fence_proxy_async_smem();
+    umma::fence_before_sync();
+    __syncthreads();
+    if (tid == 0) {
       umma::fence_after_sync();
-      /* epilogue of layer l: bias, SiLU; the next layer's operand or the output */
-#pragma unroll 1
-      for (int c = 0; c < H / 32; c++) {
-        float v[32];
-        umma::tmem_ld_32x32b_x32(trow + c * 32, v);
+      if (l == 0) {
+        umma::mma_bf16(c.tmem, umma::smem_desc(c.s_x0, 128, 256), umma::smem_desc(c.s_w, 128, 256), idesc, false);
+      } else {
+        const uint32_t wl = c.s_w + W0_BYTES + (l - 1) * WL_BYTES;
 #pragma unroll
-        for (int j = 0; j < 32; j++) {
-          const float h = silu(v[j] + bias[l * H + c * 32 + j]);
-          if (l < 3)
-            *(__nv_bfloat16 *)(sm + SM_A + umma::kmajor_offset(tid, c * 32 + j, H)) = __float2bfloat16_rn(h);
-          else
-            acc_out += h * wo[c * 32 + j];
-        }
+        for (int kk = 0; kk < H / 16; kk++)
+          umma::mma_bf16(c.tmem, umma::smem_desc(c.s_a + kk * 256, 128, 2048), umma::smem_desc(wl + kk * 256, 128, 2048),
+                         idesc, kk > 0);
+      }
+      umma::mma_commit(c.mbar);
+    }
+    const bool ok = umma::mbar_wait(c.mbar, c.phase);
+    c.phase ^= 1u;
+    if (__syncthreads_or(!ok)) return false;
+    umma::fence_after_sync();
+    /* epilogue of layer l: bias, SiLU; the next layer's operand or the output */
+#pragma unroll 1
+    for (int q = 0; q < H / 32; q++) {
+      float v[32];
+      umma::tmem_ld_32x32b_x32(c.trow + q * 32, v);
+#pragma unroll
+      for (int j = 0; j < 32; j++) {
+        const float h = silu(v[j] + c.bias[l * H + q * 32 + j]);
+        if (l < 3)
+          *(__nv_bfloat16 *)(sm + SM_A + umma::kmajor_offset(tid, q * 32 + j, H)) = __float2bfloat16_rn(h);
+        else
+          y += h * c.wo[q * 32 + j];
       }
     }
-    if (!failed && valid) out[row] = acc_out;
   }
-  if (failed && tid == 0) atomicExch(err, 1);
+  return true;
+}
+
+__device__ void fwd_teardown(FwdCtx &c) {
   umma::fence_before_sync();
   __syncthreads();
-  if (warp == 0) umma::tmem_dealloc(tmem, 128);
+  if ((threadIdx.x >> 5) == 0) umma::tmem_dealloc(c.tmem, 128);
+}
+
+/* features [n][3] (already scaled) -> out [n] = network output (log solid
+ * angle); *err set non-zero when a wait ran out */
+__global__ void __launch_bounds__(128, 1) forward_kernel(const unsigned char *packed, const float *theta,
+                                                         const float *features, float *out, int n, int *err) {
+  extern __shared__ __align__(1024) unsigned char sm[];
+  FwdCtx c;
+  fwd_setup(sm, packed, theta, c);
+  bool failed = false;
+  for (int tile = blockIdx.x; tile * 128 < n; tile += gridDim.x) {
+    const int row = tile * 128 + threadIdx.x;
+    const bool valid = row < n;
+    float f[NIN], y;
+    for (int k = 0; k < NIN; k++) f[k] = valid ? features[(size_t)row * NIN + k] : 0.0f;
+    if (!fwd_tile(sm, c, f, y)) {
+      failed = true;
+      break;
+    }
+    if (valid) out[row] = y;
+  }
+  if (failed && threadIdx.x == 0) atomicExch(err, 1);
+  fwd_teardown(c);
+}
+
+/* ---------------- surrogate of the solid-angle grid ---------------- */
+/* input domain and feature scaling: the (r, theta) box of the solid-angle
+ * grid, features (log r, axial distance r sin(theta), sin(theta) = cosine of
+ * the angle to the detector axis) mapped to [-1, 1]; cells of the box on
+ * which the network is checked (flag 1: use the integrator instead) */
+struct Domain {
+  float lr0, lr1, amax, t0, t1;
+  int ncr, nct;
+  float eps; /* log target = log(omega + eps) */
+};
+
+template <typename R>
+__host__ __device__ __forceinline__ void features_of(const Domain &d, R r, R t, float *f, bool &inside, int &cell) {
+  const float lr = logf((float)r), tt = (float)t;
+  inside = lr >= d.lr0 && lr <= d.lr1 && tt >= d.t0 && tt <= d.t1;
+  const float st = sinf(tt);
+  f[0] = 2.0f * (lr - d.lr0) / (d.lr1 - d.lr0) - 1.0f;
+  f[1] = 2.0f * (float)r * st / d.amax - 1.0f;
+  f[2] = 2.0f * st - 1.0f;
+  int cr = (int)((lr - d.lr0) / (d.lr1 - d.lr0) * d.ncr), ct = (int)((tt - d.t0) / (d.t1 - d.t0) * d.nct);
+  cr = cr < 0 ? 0 : (cr >= d.ncr ? d.ncr - 1 : cr);
+  ct = ct < 0 ? 0 : (ct >= d.nct ? d.nct - 1 : ct);
+  cell = ct * d.ncr + cr;
+}
+
+/* Fills the solid angle of every queued estimator event: the network on the
+ * tensor cores for 128 events per tile, the integrator (the same Monte Carlo
+ * as an off-grid point of the grid path) in flagged cells and outside the
+ * box, zero below the box's lowest theta (as the grid path). */
+template <typename R>
+__global__ void __launch_bounds__(128, 1) omega_kernel(const unsigned char *packed, const float *theta, Domain dom,
+                                                       const unsigned char *flags, const DevBundle<R> *bundle,
+                                                       VrEvent<R> *ev, const unsigned long long *count, long long cap,
+                                                       unsigned long long *fallbacks, int *err) {
+  extern __shared__ __align__(1024) unsigned char sm[];
+  FwdCtx c;
+  fwd_setup(sm, packed, theta, c);
+  const long long n = (long long)*count < cap ? (long long)*count : cap;
+  bool failed = false;
+  for (long long tile = blockIdx.x; tile * 128 < n; tile += gridDim.x) {
+    const long long i = tile * 128 + threadIdx.x;
+    const bool valid = i < n;
+    const R r = valid ? ev[i].sa_r : (R)1, t = valid ? ev[i].sa_t : (R)dom.t0;
+    float f[NIN], y;
+    bool inside;
+    int cell;
+    features_of(dom, r, t, f, inside, cell);
+    if (!fwd_tile(sm, c, f, y)) {
+      failed = true;
+      break;
+    }
+    if (!valid) continue;
+    R omega;
+    if (!(t >= (R)dom.t0)) {
+      omega = (R)0;
+    } else if (!inside || flags[cell]) {
+      xmi_rng g;
+      xmi_rng_init(&g, bundle->seed, (uint64_t)ev[i].id, 0x80000000u | (uint32_t)ev[i].n);
+      omega = single_solid_angle(*bundle, r, t, &g, bundle->sa_hits);
+      atomicAdd(fallbacks, 1ull);
+    } else {
+      const float o = __expf(y) - dom.eps;
+      omega = (R)(o > 0.0f ? o : 0.0f);
+    }
+    ev[i].pR *= omega;
+    ev[i].pC *= omega;
+    ev[i].pdir_fluo *= omega;
+  }
+  if (failed && threadIdx.x == 0) atomicExch(err, 1);
+  fwd_teardown(c);
 }
 
 /* ---------------- training ---------------- */
@@ -463,6 +565,10 @@ struct MlpTrainer {
   }
 };
 
+/* Adam over the trainer's rows (in order): one 128-row tile per SM per step,
+ * learning rate decaying by a cosine from lr to lr/100 */
+bool train_loop(MlpTrainer &tr, int epochs, float lr, double *loss_per_epoch);
+
 bool finish(MlpTrainer &tr, const char *what) {
   cudaError_t e = cudaDeviceSynchronize();
   int h_err = 0;
@@ -522,27 +628,7 @@ int xmi_gpu_mlp_train(float *theta, int n, const float *features, const float *t
   MlpTrainer tr;
   bool ok = tr.alloc(n, theta, features, targets);
   if (!ok) xmi_set_error("xmi_gpu_mlp_train: cudaMalloc failed");
-  const int tiles = (n + 127) / 128;
-  const int steps_per_epoch = (tiles + tr.grid - 1) / tr.grid;
-  const int total = steps_per_epoch * epochs;
-  int step = 0;
-  for (int ep = 0; ok && ep < epochs; ep++) {
-    double ep_loss = 0.0;
-    for (int s = 0; s < steps_per_epoch; s++, step++) {
-      const int tile0 = s * tr.grid, nt = tile0 + tr.grid <= tiles ? tr.grid : tiles - tile0;
-      const int rows = (tile0 + nt) * 128 <= n ? nt * 128 : n - tile0 * 128;
-      tr.grad_pass(tile0, nt, rows);
-      const float frac = (float)step / (float)(total > 1 ? total - 1 : 1);
-      const float lr_t = lr * (0.01f + 0.99f * 0.5f * (1.0f + cosf(3.14159265f * frac)));
-      const float bc1 = 1.0f - powf(0.9f, (float)(step + 1)), bc2 = 1.0f - powf(0.999f, (float)(step + 1));
-      adam_kernel<<<(NPARAM + 255) / 256, 256>>>(tr.theta, tr.m, tr.v, tr.grad, lr_t, 0.9f, 0.999f, 1e-8f, bc1, bc2);
-      double l = 0.0;
-      cudaMemcpy(&l, tr.loss, sizeof(double), cudaMemcpyDeviceToHost);
-      ep_loss += l;
-    }
-    if (loss_per_epoch) loss_per_epoch[ep] = ep_loss / n;
-    ok = finish(tr, "xmi_gpu_mlp_train");
-  }
+  ok = ok && train_loop(tr, epochs, lr, loss_per_epoch);
   if (ok) cudaMemcpy(theta, tr.theta, sizeof(float) * NPARAM, cudaMemcpyDeviceToHost);
   tr.release();
   return ok ? 1 : 0;
@@ -595,5 +681,270 @@ int xmi_gpu_mlp_forward(const float *theta, int n, const float *features, float 
   cudaFree(d_pack);
   cudaFree(d_err);
   return ok ? 1 : 0;
+}
+
+}  // extern "C"
+
+namespace {
+bool train_loop(MlpTrainer &tr, int epochs, float lr, double *loss_per_epoch) {
+  using namespace xmi::mlp;
+  const int n = tr.n, tiles = (n + 127) / 128;
+  const int steps_per_epoch = (tiles + tr.grid - 1) / tr.grid;
+  const int total = steps_per_epoch * epochs;
+  int step = 0;
+  bool ok = true;
+  for (int ep = 0; ok && ep < epochs; ep++) {
+    double ep_loss = 0.0;
+    for (int s = 0; s < steps_per_epoch; s++, step++) {
+      const int tile0 = s * tr.grid, nt = tile0 + tr.grid <= tiles ? tr.grid : tiles - tile0;
+      const int rows = (tile0 + nt) * 128 <= n ? nt * 128 : n - tile0 * 128;
+      tr.grad_pass(tile0, nt, rows);
+      const float frac = (float)step / (float)(total > 1 ? total - 1 : 1);
+      const float lr_t = lr * (0.01f + 0.99f * 0.5f * (1.0f + cosf(3.14159265f * frac)));
+      const float bc1 = 1.0f - powf(0.9f, (float)(step + 1)), bc2 = 1.0f - powf(0.999f, (float)(step + 1));
+      adam_kernel<<<(NPARAM + 255) / 256, 256>>>(tr.theta, tr.m, tr.v, tr.grad, lr_t, 0.9f, 0.999f, 1e-8f, bc1, bc2);
+      double l = 0.0;
+      cudaMemcpy(&l, tr.loss, sizeof(double), cudaMemcpyDeviceToHost);
+      ep_loss += l;
+    }
+    if (loss_per_epoch) loss_per_epoch[ep] = ep_loss / n;
+    ok = finish(tr, "surrogate training");
+  }
+  return ok;
+}
+
+/* trained surrogate of one input's solid-angle grid */
+struct SurrogateState {
+  xmi::mlp::Domain dom;
+  std::vector<float> theta;
+  float *theta_d = nullptr;
+  unsigned char *packed_d = nullptr, *flags_d = nullptr;
+  double report[6] = {0, 0, 0, 0, 0, 0};
+};
+
+/* network outputs on the device for n feature rows already on the device */
+bool device_forward(const SurrogateState &sg, const float *feat_d, float *out_d, int n, int *err_d) {
+  using namespace xmi::mlp;
+  cudaFuncSetAttribute(forward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SM_TOTAL);
+  int dev = 0, sms = 1;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int tiles = (n + 127) / 128;
+  forward_kernel<<<tiles < sms ? tiles : sms, 128, SM_TOTAL>>>(sg.packed_d, sg.theta_d, feat_d, out_d, n, err_d);
+  return cudaDeviceSynchronize() == cudaSuccess;
+}
+}  // namespace
+
+extern "C" {
+
+void xmi_surrogate_free(void *p) {
+  SurrogateState *sg = (SurrogateState *)p;
+  if (!sg) return;
+  cudaFree(sg->theta_d);
+  cudaFree(sg->packed_d);
+  cudaFree(sg->flags_d);
+  delete sg;
+}
+
+/* Trains the solid-angle surrogate of an initialised input handle (see
+ * xmi_gpu_build_surrogate in the public header for the procedure). */
+int xmi_gpu_build_surrogate(xmi_inputFPtr in, int n_train, int hits_train, int epochs, int hits_check,
+                            double *report) {
+  using namespace xmi::mlp;
+  if (!in || !in->initialized || n_train < 128 || hits_train < 1 || epochs < 1 || hits_check < 1) {
+    xmi_set_error("xmi_gpu_build_surrogate: invalid arguments");
+    return 0;
+  }
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
+    xmi_set_error("no CUDA device available: the engine has no CPU fallback");
+    return 0;
+  }
+  const auto t_start = std::chrono::steady_clock::now();
+  SurrogateState *sg = new SurrogateState();
+  std::vector<double> rv(1024), tv(1024);
+  xmi_solid_angle_axes(in, 1024, 1024, rv.data(), tv.data());
+  sg->dom.lr0 = (float)std::log(rv.front());
+  sg->dom.lr1 = (float)std::log(rv.back());
+  sg->dom.amax = (float)rv.back();
+  sg->dom.t0 = (float)tv.front();
+  sg->dom.t1 = (float)tv.back();
+  sg->dom.ncr = 32;
+  sg->dom.nct = 32;
+  sg->dom.eps = 1e-10f;
+  const xmi::SaGeom geom{in->det_radius, in->coll_radius, in->coll_height, in->coll_present};
+  const int ncell = sg->dom.ncr * sg->dom.nct, per_cell = 4, n_check = ncell * per_cell;
+
+  /* training points uniform in (log r, theta) over the grid's box; checking
+   * points uniform within each cell */
+  std::mt19937_64 rng(0x5EED0004ull);
+  std::uniform_real_distribution<double> u01(0.0, 1.0);
+  std::vector<double> r_h(n_train + n_check), t_h(n_train + n_check);
+  for (int i = 0; i < n_train; i++) {
+    r_h[i] = std::exp(sg->dom.lr0 + (sg->dom.lr1 - sg->dom.lr0) * u01(rng));
+    t_h[i] = sg->dom.t0 + (sg->dom.t1 - sg->dom.t0) * u01(rng);
+  }
+  for (int c = 0; c < ncell; c++)
+    for (int k = 0; k < per_cell; k++) {
+      const int i = n_train + c * per_cell + k, cr = c % sg->dom.ncr, ct = c / sg->dom.ncr;
+      const double fr = (cr + u01(rng)) / sg->dom.ncr, ft = (ct + u01(rng)) / sg->dom.nct;
+      r_h[i] = std::exp(sg->dom.lr0 + (sg->dom.lr1 - sg->dom.lr0) * fr);
+      t_h[i] = sg->dom.t0 + (sg->dom.t1 - sg->dom.t0) * ft;
+    }
+  double *r_d = nullptr, *t_d = nullptr, *o_d = nullptr;
+  float *feat_d = nullptr, *pred_d = nullptr;
+  int *err_d = nullptr;
+  const int ntot = n_train + n_check;
+  bool ok = cudaMalloc(&r_d, sizeof(double) * ntot) == cudaSuccess &&
+            cudaMalloc(&t_d, sizeof(double) * ntot) == cudaSuccess &&
+            cudaMalloc(&o_d, sizeof(double) * ntot) == cudaSuccess &&
+            cudaMalloc(&feat_d, sizeof(float) * 3 * n_check) == cudaSuccess &&
+            cudaMalloc(&pred_d, sizeof(float) * n_check) == cudaSuccess &&
+            cudaMalloc(&err_d, sizeof(int)) == cudaSuccess;
+  std::vector<double> o_h(ntot);
+  if (ok) {
+    cudaMemcpy(r_d, r_h.data(), sizeof(double) * ntot, cudaMemcpyHostToDevice);
+    cudaMemcpy(t_d, t_h.data(), sizeof(double) * ntot, cudaMemcpyHostToDevice);
+    cudaMemset(err_d, 0, sizeof(int));
+    int dev = 0, sms = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const unsigned long long seed = in->gpu.seed ? in->gpu.seed : 0x5EED0001ull;
+    /* training targets: FP32 integrator; checking values: FP64 integrator */
+    xmi::solid_angle_points_kernel<float><<<sms * 8, 256>>>(geom, r_d, t_d, n_train, hits_train, seed, o_d);
+    xmi::solid_angle_points_kernel<double><<<sms * 8, 256>>>(geom, r_d + n_train, t_d + n_train, n_check, hits_check,
+                                                             seed ^ 0x9E3779B97F4A7C15ull, o_d + n_train);
+    ok = cudaDeviceSynchronize() == cudaSuccess;
+    if (ok) cudaMemcpy(o_h.data(), o_d, sizeof(double) * ntot, cudaMemcpyDeviceToHost);
+  }
+  if (ok) {
+    std::vector<float> feat(3 * (size_t)n_train), targ(n_train);
+    for (int i = 0; i < n_train; i++) {
+      bool inside;
+      int cell;
+      features_of(sg->dom, r_h[i], t_h[i], &feat[3 * (size_t)i], inside, cell);
+      targ[i] = (float)std::log(o_h[i] + sg->dom.eps);
+    }
+    sg->theta.resize(NPARAM);
+    /* He initialisation, fixed seed */
+    std::normal_distribution<double> nrm(0.0, 1.0);
+    for (int i = 0; i < NPARAM; i++) sg->theta[i] = 0.0f;
+    for (int i = 0; i < H * NIN; i++) sg->theta[OFF_W0 + i] = (float)(nrm(rng) * std::sqrt(2.0 / NIN));
+    for (int l = 1; l <= 3; l++)
+      for (int i = 0; i < H * H; i++) sg->theta[off_w(l) + i] = (float)(nrm(rng) * std::sqrt(2.0 / H));
+    for (int i = 0; i < H; i++) sg->theta[OFF_WO + i] = (float)(nrm(rng) * std::sqrt(1.0 / H));
+    double mean = 0.0;
+    for (int i = 0; i < n_train; i++) mean += targ[i];
+    sg->theta[OFF_BO] = (float)(mean / n_train);
+    MlpTrainer tr;
+    std::vector<double> hist(epochs);
+    ok = tr.alloc(n_train, sg->theta.data(), feat.data(), targ.data()) && train_loop(tr, epochs, 2e-3f, hist.data());
+    if (ok) {
+      cudaMemcpy(sg->theta.data(), tr.theta, sizeof(float) * NPARAM, cudaMemcpyDeviceToHost);
+      sg->report[3] = hist.back();
+    }
+    tr.release();
+  }
+  if (ok) {
+    ok = cudaMalloc(&sg->theta_d, sizeof(float) * NPARAM) == cudaSuccess &&
+         cudaMalloc(&sg->packed_d, PACK_BYTES) == cudaSuccess && cudaMalloc(&sg->flags_d, ncell) == cudaSuccess;
+  }
+  if (ok) {
+    cudaMemcpy(sg->theta_d, sg->theta.data(), sizeof(float) * NPARAM, cudaMemcpyHostToDevice);
+    pack_weights<<<(3 * H * H + 255) / 256, 256>>>(sg->theta_d, sg->packed_d);
+    std::vector<float> fc(3 * (size_t)n_check);
+    for (int i = 0; i < n_check; i++) {
+      bool inside;
+      int cell;
+      features_of(sg->dom, r_h[n_train + i], t_h[n_train + i], &fc[3 * (size_t)i], inside, cell);
+    }
+    cudaMemcpy(feat_d, fc.data(), sizeof(float) * 3 * n_check, cudaMemcpyHostToDevice);
+    ok = device_forward(*sg, feat_d, pred_d, n_check, err_d);
+    int h_err = 0;
+    cudaMemcpy(&h_err, err_d, sizeof(int), cudaMemcpyDeviceToHost);
+    if (h_err) {
+      xmi_set_error("xmi_gpu_build_surrogate: tensor-core wait ran out");
+      ok = false;
+    }
+  }
+  if (ok) {
+    /* cells whose checking points miss the integrator by more than the
+     * tolerance are served by the integrator */
+    std::vector<float> pred(n_check);
+    cudaMemcpy(pred.data(), pred_d, sizeof(float) * n_check, cudaMemcpyDeviceToHost);
+    std::vector<unsigned char> flags(ncell, 0);
+    std::vector<double> errs;
+    double worst_kept = 0.0;
+    const double tol = in->gpu.surrogate_tolerance > 0 ? in->gpu.surrogate_tolerance : 1e-3;
+    for (int c = 0; c < ncell; c++) {
+      double cell_max = 0.0;
+      for (int k = 0; k < per_cell; k++) {
+        const int i = c * per_cell + k;
+        const double truth = o_h[n_train + i], net = std::max(0.0, std::exp((double)pred[i]) - sg->dom.eps);
+        const double e = truth > 0.0 ? std::fabs(net - truth) / truth : (net > 1e3 * sg->dom.eps ? 1.0 : 0.0);
+        errs.push_back(e);
+        cell_max = std::max(cell_max, e);
+      }
+      flags[c] = cell_max > tol ? 1 : 0;
+      if (!flags[c]) worst_kept = std::max(worst_kept, cell_max);
+    }
+    std::vector<double> sorted = errs;
+    std::nth_element(sorted.begin(), sorted.begin() + sorted.size() / 2, sorted.end());
+    int nflag = 0;
+    for (unsigned char f : flags) nflag += f;
+    sg->report[0] = sorted[sorted.size() / 2];
+    sg->report[1] = worst_kept;
+    sg->report[2] = (double)nflag / ncell;
+    cudaMemcpy(sg->flags_d, flags.data(), ncell, cudaMemcpyHostToDevice);
+  }
+  cudaFree(r_d);
+  cudaFree(t_d);
+  cudaFree(o_d);
+  cudaFree(feat_d);
+  cudaFree(pred_d);
+  cudaFree(err_d);
+  if (!ok) {
+    if (!*xmi_gpu_last_error()) xmi_set_error("xmi_gpu_build_surrogate failed");
+    xmi_surrogate_free(sg);
+    return 0;
+  }
+  sg->report[4] = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
+  sg->report[5] = ncell;
+  xmi_surrogate_free(in->surrogate);
+  in->surrogate = sg;
+  if (report)
+    for (int k = 0; k < 6; k++) report[k] = sg->report[k];
+  return 1;
+}
+
+int xmi_surrogate_apply(const void *p, int precision, const void *dev_bundle, void *events,
+                        const unsigned long long *count, long long cap, unsigned long long *fallbacks, int *err,
+                        void *stream) {
+  using namespace xmi::mlp;
+  const SurrogateState *sg = (const SurrogateState *)p;
+  if (!sg) return 0;
+  int dev = 0, sms = 1;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaStream_t st = (cudaStream_t)stream;
+  if (precision == 0) {
+    cudaFuncSetAttribute(omega_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, SM_TOTAL);
+    omega_kernel<double><<<sms, 128, SM_TOTAL, st>>>(sg->packed_d, sg->theta_d, sg->dom, sg->flags_d,
+                                                      (const xmi::DevBundle<double> *)dev_bundle,
+                                                      (xmi::VrEvent<double> *)events, count, cap, fallbacks, err);
+  } else {
+    cudaFuncSetAttribute(omega_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, SM_TOTAL);
+    omega_kernel<float><<<sms, 128, SM_TOTAL, st>>>(sg->packed_d, sg->theta_d, sg->dom, sg->flags_d,
+                                                     (const xmi::DevBundle<float> *)dev_bundle,
+                                                     (xmi::VrEvent<float> *)events, count, cap, fallbacks, err);
+  }
+  return cudaGetLastError() == cudaSuccess ? 1 : 0;
+}
+
+int xmi_gpu_surrogate_report(xmi_inputFPtr in, double *report) {
+  if (!in || !in->surrogate || !report) return 0;
+  const SurrogateState *sg = (const SurrogateState *)in->surrogate;
+  for (int k = 0; k < 6; k++) report[k] = sg->report[k];
+  return 1;
 }
 }

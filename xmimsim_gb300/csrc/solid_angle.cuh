@@ -146,5 +146,42 @@ __global__ void __launch_bounds__(256) solid_angle_grid_kernel(SaGeom s, const d
   }
 }
 
+/* solid angle at arbitrary points (r[i], t[i]), i < n: one warp per point,
+ * Philox block k of stream (seed, point, 0xF1000000) for sample k (the
+ * integrator behind the surrogate network's training targets and checks) */
+template <typename R>
+__global__ void __launch_bounds__(256) solid_angle_points_kernel(SaGeom s, const double *r, const double *t,
+                                                                 long long n, int hits_per_single,
+                                                                 unsigned long long seed, double *out) {
+  const int lane = threadIdx.x & 31;
+  const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
+  for (long long p = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); p < n; p += warps) {
+    R cfca, fcsa, st, ct, py, pz;
+    bool outside;
+    int hits = 0;
+    const bool live = sa_setup<R>(s, (R)r[p], (R)t[p], cfca, fcsa, st, ct, py, pz, outside);
+    if (live) {
+      for (int i = lane; i < hits_per_single; i += 32) {
+        xmi_u32x4 c;
+        c.v[0] = (uint32_t)i;
+        c.v[1] = 0xF1000000u;
+        c.v[2] = (uint32_t)p;
+        c.v[3] = (uint32_t)((unsigned long long)p >> 32);
+        xmi_u32x4 o = xmi_philox4x32_10(c, (uint32_t)seed, (uint32_t)(seed >> 32));
+        double d1 = ((double)(o.v[0] >> 5) * 67108864.0 + (double)(o.v[1] >> 6)) * (1.0 / 9007199254740992.0);
+        double d2 = ((double)(o.v[2] >> 5) * 67108864.0 + (double)(o.v[3] >> 6)) * (1.0 / 9007199254740992.0);
+        R u1 = (R)d1, u2 = (R)d2;
+        if (sizeof(R) == 4) {
+          u1 = u1 < (R)1 ? u1 : (R)0x1.fffffep-1f;
+          u2 = u2 < (R)1 ? u2 : (R)0x1.fffffep-1f;
+        }
+        hits += sa_sample<R>(s, cfca, st, ct, py, pz, outside, u1, u2);
+      }
+    }
+    hits = __reduce_add_sync(0xffffffffu, hits);
+    if (lane == 0) out[p] = live ? (double)fcsa * (double)hits / (double)hits_per_single : 0.0;
+  }
+}
+
 }  // namespace xmi
 #endif

@@ -346,6 +346,21 @@ __device__ R single_solid_angle(const DevBundle<R> &b, R r1, R theta1, xmi_rng *
   return fcsa * (R)hits / (R)hits_per_single;
 }
 
+/* (r, theta) of a point in the solid-angle grid's frame: distance to the
+ * detector centre and the complement of the angle to the detector normal */
+template <typename R>
+__device__ __forceinline__ void sa_coords(const DevBundle<R> &b, const double *coords, R &r, R &theta) {
+  double dv[3] = {coords[0] - b.p_det[0], coords[1] - b.p_det[1], coords[2] - b.p_det[2]};
+  double rr = sqrt(dv[0] * dv[0] + dv[1] * dv[1] + dv[2] * dv[2]);
+  double inv = 1.0 / rr;
+  R dn[3] = {(R)(dv[0] * inv), (R)(dv[1] * inv), (R)(dv[2] * inv)};
+  R nd[3] = {(R)b.n_det[0], (R)b.n_det[1], (R)b.n_det[2]};
+  R tt = acos(rdot(dn, nd));
+  r = (R)rr;
+  if (tt > (R)(kPi / 2.0)) tt = (R)kPi - tt;
+  theta = (R)(kPi / 2.0) - tt;
+}
+
 /* xmi_get_solid_angle (src/xmi_solid_angle_f.F90:712-801) */
 template <typename R>
 __device__ R get_solid_angle(const DevBundle<R> &b, const double *coords, const Photon<R> &p, const DevTally &t,
@@ -497,6 +512,7 @@ struct __align__(16) VrEvent {
   R pdir_fluo;       /* omega / 4 pi */
   R pesc_rayl;       /* escape probability at the photon energy */
   R f;               /* energy-grid fraction of E */
+  R sa_r, sa_t;      /* the point's (r, theta) of the solid-angle grid (the surrogate's input) */
   R rd[XMI_MAXL];    /* density x path length toward the detector point, per layer */
   int node, layer, n, h_slot; /* h_slot >= 0: exciting line of a fluorescence photon */
   long long id;
@@ -596,7 +612,15 @@ __device__ bool vr_prologue(const DevBundle<R> &b, const Photon<R> &p, const Dev
 #pragma unroll
   for (int j = 0; j < XMI_MAXL; j++) murhod += p.mus[j] * ev.rd[j];
   ev.pesc_rayl = exp(-murhod);
-  const R omega = get_solid_angle(b, p.c, p, t, ok);
+  R omega;
+  if (b.use_surrogate) {
+    /* the solid angle comes later from the surrogate network: the factors
+     * below are stored without it, with the point's (r, theta) */
+    sa_coords(b, p.c, ev.sa_r, ev.sa_t);
+    omega = (R)1;
+  } else {
+    omega = get_solid_angle(b, p.c, p, t, ok);
+  }
   ev.pdir_fluo = omega / (R)4 / (R)kPi;
   locate(b, p.E, ev.node, ev.f);
   ev.mu_here = select_layer(p.mus, layer);

@@ -24,6 +24,7 @@ struct xmi_input_handle {
   double layer_zbeg[XMI_MAXL], layer_zend[XMI_MAXL], layer_thickz[XMI_MAXL];
   int escape_geometry; /* built by xmi_init_input_escape_ratios */
   xmi_gpu_options gpu;
+  void *surrogate; /* trained solid-angle network (owned by the CUDA side) */
 };
 
 /* opaque table handle behind xmi_hdf5FPtr */
@@ -53,6 +54,14 @@ int xmi_dev_sync_tables(struct xmi_tables_handle *t, int precision);
 void xmi_dev_free_tables(struct xmi_tables_handle *t);
 /* copies the FP64 device view (xmi::DevBundle<double>) into out */
 int xmi_dev_bundle_copy64(struct xmi_tables_handle *t, void *out);
+
+/* surrogate network (mlp.cu) */
+void xmi_surrogate_free(void *sg);
+/* multiplies the solid-angle factors of the queued estimator events by the
+ * network's solid angle (integrator fallback in flagged cells); all on stream */
+int xmi_surrogate_apply(const void *sg, int precision, const void *dev_bundle, void *events,
+                        const unsigned long long *count, long long cap, unsigned long long *fallbacks,
+                        int *err, void *stream);
 
 #ifdef __cplusplus
 }

@@ -170,6 +170,7 @@ class Simulation:
         self.tables = C.c_void_p()
         _check(self.lib.xmi_input_C2F(C.byref(self.cinput.input), C.byref(self.inputF)), "xmi_input_C2F")
         _check(self.lib.xmi_init_input(C.byref(self.inputF)), "xmi_init_input")
+        self.gpu = gpu if gpu is not None else gpu_options()
         if gpu is not None:
             _check(self.lib.xmi_gpu_set_options(self.inputF, C.byref(gpu)), "xmi_gpu_set_options")
         _check(self.lib.xmi_init_from_hdf5(None, self.inputF, C.byref(self.tables), C.byref(self.options)),
@@ -217,8 +218,14 @@ class Simulation:
 
     def set_gpu(self, gpu: abi.XmiGpuOptions) -> None:
         _check(self.lib.xmi_gpu_set_options(self.inputF, C.byref(gpu)), "xmi_gpu_set_options")
+        self.gpu = gpu
 
     # -- transport -----------------------------------------------------------
+    def surrogate_on(self) -> bool:
+        rep = np.zeros(6)
+        return bool(self.gpu.use_surrogate) and \
+            self.lib.xmi_gpu_surrogate_report(self.inputF, rep.ctypes.data_as(abi.c_double_p)) == 1
+
     def prepare(self, n_mpi_hosts: int = 1) -> None:
         """Builds the run part of the bundle exactly as xmi_main_msim does (no GPU)."""
         sa = self._sa if self.options.use_variance_reduction else None
@@ -238,7 +245,7 @@ class Simulation:
         ch = abi.c_double_p()
         br = abi.c_double_p()
         vr = abi.c_double_p()
-        sa = self.solid_angle() if self.options.use_variance_reduction else None
+        sa = self.solid_angle() if self.options.use_variance_reduction and not self.surrogate_on() else None
         _check(self.lib.xmi_main_msim(self.inputF, self.tables, n_mpi_hosts, C.byref(ch), C.byref(self.options),
                                       C.byref(br), C.byref(vr), sa), "xmi_main_msim")
         out = {"channels": np.ctypeslib.as_array(ch, ((N + 1), nch)).copy(),
@@ -272,6 +279,15 @@ class Simulation:
                          "raw": (ch[i], br[i], vr[i])})
         return outs
 
+    def build_surrogate(self, n_train: int = 1 << 21, hits_train: int = 2048, epochs: int = 8,
+                        hits_check: int = 1 << 20) -> dict:
+        """Trains the solid-angle surrogate network (xmi_gpu_build_surrogate)."""
+        rep = np.zeros(6)
+        _check(self.lib.xmi_gpu_build_surrogate(self.inputF, n_train, hits_train, epochs, hits_check,
+                                                rep.ctypes.data_as(abi.c_double_p)), "xmi_gpu_build_surrogate")
+        keys = ("median_rel_err", "max_rel_err_kept", "flagged_fraction", "train_loss", "seconds", "cells")
+        return dict(zip(keys, rep.tolist()))
+
     def free_raw(self, out: dict) -> None:
         for p in out.pop("raw", ()):
             if p:
@@ -284,6 +300,9 @@ class Simulation:
         tr, so, es, ev = C.c_double(), C.c_double(), C.c_double(), C.c_longlong()
         self.lib.xmi_gpu_last_phases(C.byref(tr), C.byref(so), C.byref(es), C.byref(ev))
         out.update(transport_ms=tr.value, sort_ms=so.value, estimator_ms=es.value, events=ev.value)
+        sg, fb = C.c_double(), C.c_longlong()
+        self.lib.xmi_gpu_last_surrogate(C.byref(sg), C.byref(fb))
+        out.update(surrogate_ms=sg.value, surrogate_fallbacks=fb.value)
         return out
 
     # -- detector response -------------------------------------------------
