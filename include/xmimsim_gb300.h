@@ -136,15 +136,17 @@ int xmi_main_msim_batch(int n, xmi_inputFPtr *inputFPtrs, xmi_hdf5FPtr *hdf5FPtr
  * A 3 -> 4 x 128 (SiLU) -> 1 network, BF16 weights and FP32 accumulation on
  * the tensor cores, maps a point's (log r, axial distance, cos angle) to the
  * log of its collimated detector solid angle.  xmi_gpu_build_surrogate trains
- * it for an initialised input: n_train points uniform in (log r, theta) over
- * the box of the solid-angle grid, targets from the engine's own integrator
- * (hits_train cone samples each, FP32), Adam for `epochs` passes; then checks
- * it on 4 points per cell of a 32 x 32 partition of the box against the FP64
- * integrator (hits_check samples) and flags the cells whose error exceeds
- * xmi_gpu_options.surrogate_tolerance: there the integrator keeps serving.
- * report[6]: median relative error of the checking points, largest error in
- * an unflagged cell, fraction of flagged cells, final training loss, seconds,
- * number of cells.  With xmi_gpu_options.use_surrogate = 1, xmi_main_msim
+ * it for an initialised input: n_train points uniform over the sample volume
+ * (the slab of the layers within 2 cm of the beam axis), targets from the
+ * engine's own integrator (hits_train cone samples each, FP32), Adam for
+ * `epochs` passes; then checks it on 16 x 1024 further points against the
+ * FP64 integrator (hits_check samples) and flags the cells of a 32 x 32
+ * partition of the grid's (log r, theta) box whose error exceeds
+ * xmi_gpu_options.surrogate_tolerance (and the cells no point reached):
+ * there the integrator keeps serving.  report[6]: median relative error of
+ * the checking points, largest error in an unflagged cell, share of checking
+ * points in flagged cells (the expected fallback rate), final training loss,
+ * seconds, number of cells.  With xmi_gpu_options.use_surrogate = 1, xmi_main_msim
  * then needs no solid-angle grid. */
 int xmi_gpu_build_surrogate(xmi_inputFPtr inputFPtr, int n_train, int hits_train, int epochs, int hits_check,
                             double *report);

@@ -774,13 +774,13 @@ static bool stage_run(DevState *s, xmi::DevBundle<R> &d, const xmi_bundle &h, xm
  * rows of a CTA fit shared memory (layers that need more run per-lane) */
 template <typename R>
 static int stage_cap_for(int stage_max) {
-  const int limit = (int)(200 * 1024 / (8 * sizeof(R)));
+  const int limit = (int)(200 * 1024 / (8 * sizeof(R))) - xmi::kScratchPerWarp;
   return stage_max < limit ? stage_max : limit;
 }
 
 template <typename R>
 static int estimator_blocks(int stage_cap, size_t *smem) {
-  *smem = (size_t)8 * stage_cap * sizeof(R);
+  *smem = (size_t)8 * (stage_cap + xmi::kScratchPerWarp) * sizeof(R);
   if (*smem > 48 * 1024)
     cudaFuncSetAttribute(xmi::estimator_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)*smem);
   int per_sm = 1;

@@ -170,6 +170,96 @@ __device__ void estimate_event(const DevBundle<R> &b, const DevTally &t, const S
   }
 }
 
+/* per-warp scratch of the uniform path: the 32 events' path sums rho*d per
+ * layer and, per element, shell probability x event scale */
+constexpr int kScratchPerWarp = 32 * XMI_MAXL + 32 * XMI_NSHELL;
+
+/* The estimator for the 32 events of a warp that share configuration, layer
+ * and order.  Elements: lane = event, as in the per-lane path, contributions
+ * summed across the warp into the stage row.  Lines: lane = line entry, each
+ * lane looping over the 32 events (their path sums and shell factors read
+ * from shared memory, broadcast) and accumulating its own line's history in a
+ * register -- no cross-lane reduction per line. */
+template <typename R>
+__device__ void estimate_event_uniform(const DevBundle<R> &b, const DevTally &t, const StageRow<R> &st, R *scratch,
+                                       const VrEvent<R> &ev, bool valid, bool &ok) {
+  const int lane = threadIdx.x & 31;
+  const int layer = ev.layer, n = ev.n;
+  const int nel = b.nel[layer], off = b.off[layer];
+  const long long hbase = (long long)(n - 1) * b.n_slots;
+  R *s_rd = scratch, *s_a = scratch + 32 * XMI_MAXL;
+  const R live = valid ? (R)1 : (R)0;
+#pragma unroll
+  for (int j = 0; j < XMI_MAXL; j++) s_rd[lane * XMI_MAXL + j] = ev.rd[j];
+  for (int i = 0; i < nel; i++) {
+    const int pair = off + i;
+    const int e = XMI_LDG(b.layer_el, pair, b.n_layer_el, 9);
+    const R wi = XMI_LDG(b.layer_w, pair, b.n_layer_el, 9);
+    const R pconv = wi / ev.mu_here;
+    const int rs = b.n_lines + 2 * e;
+    /* Rayleigh */
+    const R twr = live * (pconv * (ev.pR * qtab(b.ff2 + (size_t)e * XMI_NQ, ev.q)) * ev.pesc_rayl * ev.w);
+    contribute<R, true>(t, st, st.n_line + 2 * i, hbase + rs, twr);
+    if (valid) chan_add(b, t, n, ev.E, twr);
+    /* Compton: one Doppler-broadened energy per element (N_COMPTON_VARRED = 1) */
+    xmi_rng g;
+    xmi_rng_init(&g, b.seed, (uint64_t)ev.id, vr_stream(n, i));
+    bool cok = true;
+    const R ec = compton_energy(b, e, ev.E, ev.theta, &g, true, cok);
+    R twc = (R)0;
+    if (cok) {
+      R mus_c[XMI_MAXL];
+      mu_calc(b, ec, mus_c);
+      R murhod = (R)0;
+#pragma unroll
+      for (int j = 0; j < XMI_MAXL; j++) murhod += mus_c[j] * ev.rd[j];
+      twc = live * (pconv * (ev.pC * qtab(b.sf + (size_t)e * XMI_NQ, ev.q)) * exp(-murhod) * ev.w);
+    } else if (valid) {
+      ok = false;
+    }
+    contribute<R, true>(t, st, st.n_line + 2 * i + 1, hbase + rs + 1, twc);
+    if (valid) chan_add(b, t, n, ec, twc);
+    /* shell factors of this event for element i */
+    R P[XMI_NSHELL];
+    if (ev.h_slot >= 0) {
+#pragma unroll
+      for (int s = 0; s < XMI_NSHELL; s++)
+        P[s] = XMI_LDG(b.precalc_xrf, ((long long)e * XMI_NSHELL + s) * b.n_lines + ev.h_slot,
+                       (long long)b.n_elem * XMI_NSHELL * b.n_lines, 10);
+    } else {
+#pragma unroll
+      for (int s = 0; s < XMI_NSHELL; s++) P[s] = el_val(b, e, XMI_REC_XRF + s, ev.node, ev.f);
+    }
+    const R scale = live * wi / ev.mu_here * ev.pdir_fluo * ev.w;
+#pragma unroll
+    for (int s = 0; s < XMI_NSHELL; s++)
+      s_a[lane * XMI_NSHELL + s] = (s >= 4 && !b.use_M_lines) ? (R)0 : P[s] * scale;
+    __syncwarp();
+    /* lines of element i: lane = entry */
+    const int k0 = XMI_LDG(b.ent_off, pair, b.n_layer_el + 1, 15), k1 = XMI_LDG(b.ent_off, pair + 1, b.n_layer_el + 1, 15);
+    for (int kb = k0; kb < k1; kb += 32) {
+      const int k = kb + lane;
+      if (k < k1) {
+        const int sh = XMI_LDG(b.ent_shell, k, b.n_ent, 16);
+        R pmu[XMI_MAXL];
+#pragma unroll
+        for (int j = 0; j < XMI_MAXL; j++)
+          pmu[j] = XMI_LDG(b.ent_pmu, (long long)k * XMI_MAXL + j, (long long)b.n_ent * XMI_MAXL, 17);
+        R acc = (R)0;
+#pragma unroll 4
+        for (int q = 0; q < 32; q++) {
+          R murhod = (R)0;
+#pragma unroll
+          for (int j = 0; j < XMI_MAXL; j++) murhod += pmu[j] * s_rd[q * XMI_MAXL + j];
+          acc += s_a[q * XMI_NSHELL + sh] * exp(-murhod);
+        }
+        st.v[k - st.k_first] += acc * XMI_LDG(b.ent_coef, k, b.n_ent, 16);
+      }
+    }
+    __syncwarp();
+  }
+}
+
 /* number of events the queue holds: the count, capped at the capacity (a
  * count past the capacity means events were dropped and the run is flagged) */
 __device__ __forceinline__ long long queued_events(const unsigned long long *count, long long cap) {
@@ -208,7 +298,8 @@ __global__ void __launch_bounds__(256, 2) estimator_kernel(const DevBundle<R> *b
                                                            unsigned long long *flags) {
   extern __shared__ unsigned char stage_mem[];
   StageRow<R> st;
-  st.v = (R *)stage_mem + (size_t)(threadIdx.x >> 5) * stage_cap;
+  st.v = (R *)stage_mem + (size_t)(threadIdx.x >> 5) * (stage_cap + kScratchPerWarp);
+  R *scratch = st.v + stage_cap;
   const int lane = threadIdx.x & 31;
   for (int j = lane; j < stage_cap; j += 32) st.v[j] = (R)0;
   __syncwarp();
@@ -242,7 +333,7 @@ __global__ void __launch_bounds__(256, 2) estimator_kernel(const DevBundle<R> *b
             st_cfg = ev.cfg;
           }
         }
-        if (st.key == key) estimate_event<R, true>(b, t, st, ev, valid, ok);
+        if (st.key == key) estimate_event_uniform<R>(b, t, st, scratch, ev, valid, ok);
         else estimate_event<R, false>(b, t, st, ev, valid, ok);
       } else {
         estimate_event<R, false>(b, t, st, ev, valid, ok);

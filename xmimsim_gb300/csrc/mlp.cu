@@ -773,24 +773,39 @@ int xmi_gpu_build_surrogate(xmi_inputFPtr in, int n_train, int hits_train, int e
   sg->dom.nct = 32;
   sg->dom.eps = 1e-10f;
   const xmi::SaGeom geom{in->det_radius, in->coll_radius, in->coll_height, in->coll_present};
-  const int ncell = sg->dom.ncr * sg->dom.nct, per_cell = 4, n_check = ncell * per_cell;
+  const int ncell = sg->dom.ncr * sg->dom.nct, n_check = 16 * ncell;
 
-  /* training points uniform in (log r, theta) over the grid's box; checking
-   * points uniform within each cell */
+  /* training and checking points uniform over the sample volume: the slab
+   * between the first and last layer planes, within kLateral of the beam
+   * axis, mapped to the (r, theta) of the solid-angle grid */
   std::mt19937_64 rng(0x5EED0004ull);
   std::uniform_real_distribution<double> u01(0.0, 1.0);
   std::vector<double> r_h(n_train + n_check), t_h(n_train + n_check);
-  for (int i = 0; i < n_train; i++) {
-    r_h[i] = std::exp(sg->dom.lr0 + (sg->dom.lr1 - sg->dom.lr0) * u01(rng));
-    t_h[i] = sg->dom.t0 + (sg->dom.t1 - sg->dom.t0) * u01(rng);
-  }
-  for (int c = 0; c < ncell; c++)
-    for (int k = 0; k < per_cell; k++) {
-      const int i = n_train + c * per_cell + k, cr = c % sg->dom.ncr, ct = c / sg->dom.ncr;
-      const double fr = (cr + u01(rng)) / sg->dom.ncr, ft = (ct + u01(rng)) / sg->dom.nct;
-      r_h[i] = std::exp(sg->dom.lr0 + (sg->dom.lr1 - sg->dom.lr0) * fr);
-      t_h[i] = sg->dom.t0 + (sg->dom.t1 - sg->dom.t0) * ft;
+  {
+    const double kLateral = 2.0; /* cm */
+    const double *nv = in->n_sample;
+    double e1[3] = {1.0, 0.0, 0.0};
+    if (std::fabs(nv[0]) > 0.9) e1[0] = 0.0, e1[1] = 1.0;
+    const double d1 = e1[0] * nv[0] + e1[1] * nv[1] + e1[2] * nv[2];
+    for (int k = 0; k < 3; k++) e1[k] -= d1 * nv[k];
+    const double l1 = std::sqrt(e1[0] * e1[0] + e1[1] * e1[1] + e1[2] * e1[2]);
+    for (int k = 0; k < 3; k++) e1[k] /= l1;
+    const double e2[3] = {nv[1] * e1[2] - nv[2] * e1[1], nv[2] * e1[0] - nv[0] * e1[2], nv[0] * e1[1] - nv[1] * e1[0]};
+    const int nl = in->input->composition->n_layers;
+    const double h0 = in->layer_zbeg[0] * nv[2], h1 = in->layer_zend[nl - 1] * nv[2];
+    for (int i = 0; i < n_train + n_check; i++) {
+      const double a = (2.0 * u01(rng) - 1.0) * kLateral, b = (2.0 * u01(rng) - 1.0) * kLateral;
+      const double h = h0 + (h1 - h0) * u01(rng);
+      double x[3], dv[3];
+      for (int k = 0; k < 3; k++) x[k] = h * nv[k] + a * e1[k] + b * e2[k];
+      for (int k = 0; k < 3; k++) dv[k] = x[k] - in->p_det[k];
+      const double r = std::sqrt(dv[0] * dv[0] + dv[1] * dv[1] + dv[2] * dv[2]);
+      double tt = std::acos((dv[0] * in->n_det[0] + dv[1] * in->n_det[1] + dv[2] * in->n_det[2]) / r);
+      if (tt > M_PI / 2.0) tt = M_PI - tt;
+      r_h[i] = r;
+      t_h[i] = M_PI / 2.0 - tt;
     }
+  }
   double *r_d = nullptr, *t_d = nullptr, *o_d = nullptr;
   float *feat_d = nullptr, *pred_d = nullptr;
   int *err_d = nullptr;
@@ -872,29 +887,43 @@ int xmi_gpu_build_surrogate(xmi_inputFPtr in, int n_train, int hits_train, int e
      * tolerance are served by the integrator */
     std::vector<float> pred(n_check);
     cudaMemcpy(pred.data(), pred_d, sizeof(float) * n_check, cudaMemcpyDeviceToHost);
+    /* per cell: largest relative error of its checking points; cells
+     * without checking points (outside the sample volume) are flagged */
+    std::vector<double> cell_max(ncell, -1.0), errs;
+    for (int i = 0; i < n_check; i++) {
+      bool inside;
+      int cell;
+      float f[NIN];
+      features_of(sg->dom, r_h[n_train + i], t_h[n_train + i], f, inside, cell);
+      if (!inside) continue;
+      const double truth = o_h[n_train + i], net = std::max(0.0, std::exp((double)pred[i]) - sg->dom.eps);
+      const double e = truth > 0.0 ? std::fabs(net - truth) / truth : (net > 1e3 * sg->dom.eps ? 1.0 : 0.0);
+      errs.push_back(e);
+      cell_max[cell] = std::max(cell_max[cell], e);
+    }
+    if (errs.empty()) errs.push_back(1.0);
     std::vector<unsigned char> flags(ncell, 0);
-    std::vector<double> errs;
     double worst_kept = 0.0;
     const double tol = in->gpu.surrogate_tolerance > 0 ? in->gpu.surrogate_tolerance : 1e-3;
     for (int c = 0; c < ncell; c++) {
-      double cell_max = 0.0;
-      for (int k = 0; k < per_cell; k++) {
-        const int i = c * per_cell + k;
-        const double truth = o_h[n_train + i], net = std::max(0.0, std::exp((double)pred[i]) - sg->dom.eps);
-        const double e = truth > 0.0 ? std::fabs(net - truth) / truth : (net > 1e3 * sg->dom.eps ? 1.0 : 0.0);
-        errs.push_back(e);
-        cell_max = std::max(cell_max, e);
-      }
-      flags[c] = cell_max > tol ? 1 : 0;
-      if (!flags[c]) worst_kept = std::max(worst_kept, cell_max);
+      flags[c] = (cell_max[c] < 0.0 || cell_max[c] > tol) ? 1 : 0;
+      if (!flags[c]) worst_kept = std::max(worst_kept, cell_max[c]);
     }
     std::vector<double> sorted = errs;
     std::nth_element(sorted.begin(), sorted.begin() + sorted.size() / 2, sorted.end());
-    int nflag = 0;
-    for (unsigned char f : flags) nflag += f;
+    /* share of checking points (drawn like the queries) that land in flagged cells */
+    int nflag = 0, ntot = 0;
+    for (int i = 0; i < n_check; i++) {
+      bool inside;
+      int cell;
+      float f[NIN];
+      features_of(sg->dom, r_h[n_train + i], t_h[n_train + i], f, inside, cell);
+      ntot++;
+      nflag += (!inside || flags[cell]) ? 1 : 0;
+    }
     sg->report[0] = sorted[sorted.size() / 2];
     sg->report[1] = worst_kept;
-    sg->report[2] = (double)nflag / ncell;
+    sg->report[2] = (double)nflag / (ntot > 0 ? ntot : 1);
     cudaMemcpy(sg->flags_d, flags.data(), ncell, cudaMemcpyHostToDevice);
   }
   cudaFree(r_d);
