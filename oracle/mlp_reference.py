@@ -45,13 +45,18 @@ def silu(z):
 
 
 def forward(theta: np.ndarray, x: np.ndarray, keep: bool = False):
+    """Layer 0 in FP32 with unrounded inputs and W0 (the GPU computes it on
+    the CUDA cores); layers 1-3 with BF16 activations and weights.  acts[0]
+    is the BF16 input the backward pass's dW0 GEMM uses."""
     Ws, bs, wo, bo = unpack(theta)
-    a = bf16(np.asarray(x, dtype=np.float32 if ROUND_BF16 else np.float64))
-    acts, zs = [a], []
+    ft = np.float32 if ROUND_BF16 else np.float64
+    xin = np.asarray(x, dtype=ft)
+    acts, zs = [bf16(xin)], []
     h = None
+    a = xin
     for l in range(4):
-        ft = np.float32 if ROUND_BF16 else np.float64
-        z = (a.astype(np.float64) @ bf16(Ws[l]).astype(np.float64).T).astype(ft) + bs[l]
+        W = Ws[l].astype(np.float64) if l == 0 else bf16(Ws[l]).astype(np.float64)
+        z = (a.astype(np.float64) @ W.T + bs[l].astype(np.float64)).astype(ft)
         h = silu(z.astype(np.float64)).astype(ft)
         zs.append(z)
         a = bf16(h) if l < 3 else h

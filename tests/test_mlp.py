@@ -152,8 +152,8 @@ def test_surrogate_replaces_the_grid_in_transport():
     sur = Simulation(spec, options=configs.C1_OPTIONS, gpu=gpu_options(seed=0x5EED0001, use_surrogate=1,
                                                                        surrogate_tolerance=2e-2))
     rep = sur.build_surrogate(n_train=1 << 18, hits_train=2048, epochs=20, hits_check=1 << 16)
-    assert rep["cells"] == 1024 and 0 <= rep["flagged_fraction"] < 1
-    assert rep["median_rel_err"] < 0.05
+    assert rep["cells"] == 1024 and 0 <= rep["flagged_fraction"] < 0.5, rep
+    assert rep["median_rel_err"] < 0.02, rep
     out = sur.msim()
     tm = sur.timing()
     assert tm["surrogate_ms"] > 0

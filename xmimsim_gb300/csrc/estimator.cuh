@@ -181,7 +181,7 @@ constexpr int kScratchPerWarp = 32 * XMI_MAXL + 32 * XMI_NSHELL;
  * from shared memory, broadcast) and accumulating its own line's history in a
  * register -- no cross-lane reduction per line. */
 template <typename R>
-__device__ void estimate_event_uniform(const DevBundle<R> &b, const DevTally &t, const StageRow<R> &st, R *scratch,
+__device__ __forceinline__ void estimate_event_uniform(const DevBundle<R> &b, const DevTally &t, const StageRow<R> &st, R *scratch,
                                        const VrEvent<R> &ev, bool valid, bool &ok) {
   const int lane = threadIdx.x & 31;
   const int layer = ev.layer, n = ev.n;
@@ -291,7 +291,7 @@ constexpr int kEventsPerGrab = 256;
  * the counter `work`; stage rows of stage_cap values per warp sit in dynamic
  * shared memory. */
 template <typename R>
-__global__ void __launch_bounds__(256, 2) estimator_kernel(const DevBundle<R> *bundles, const DevTally *tallies,
+__global__ void __launch_bounds__(256, 3) estimator_kernel(const DevBundle<R> *bundles, const DevTally *tallies,
                                                            int n_cfg, const VrEvent<R> *events, const int *order,
                                                            const unsigned long long *count, long long cap,
                                                            unsigned long long *work, int stage_cap,

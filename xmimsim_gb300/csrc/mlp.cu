@@ -12,13 +12,16 @@
  *     W0 [128][3], b0 [128], then for l = 1..3: W_l [128][128], b_l [128],
  *     then w_o [128], b_o.
  *
+ * Layer 0 (three FP32 inputs) runs on the CUDA cores in FP32: BF16 inputs
+ * would quantise the features to 2^-9 of their range, far coarser than the
+ * solid angle varies.  Layers 1-3 run on the tensor cores.
+ *
  * Forward kernel: one CTA of 128 threads per SM, weights resident in shared
  * memory (packed once per launch), 128 queries per tile.  Thread t owns
- * query row t of the tile: it writes the row's features / activations into
- * the K-major operand tile, and after each layer reads its accumulator row
- * back from tensor memory (TMEM lanes 32 w .. 32 w + 31 belong to warp w).
- * Thread 0 issues the MMAs: layer 0 is one M128 N128 K16 instruction,
- * layers 1-3 eight K16 steps each.
+ * query row t of the tile: it computes the row's layer-0 activations, writes
+ * them into the K-major operand tile, and after each tensor-core layer reads
+ * its accumulator row back from tensor memory (TMEM lanes 32 w .. 32 w + 31
+ * belong to warp w).  Thread 0 issues the MMAs, eight K16 steps per layer.
  */
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -98,7 +101,9 @@ __device__ void fwd_setup(unsigned char *sm, const unsigned char *packed, const 
     for (int l = 1; l <= 3; l++) c.bias[l * H + i] = theta[off_b(l) + i];
     c.wo[i] = theta[OFF_WO + i];
   }
-  for (int i = tid; i < H * KIN * 2 / 16; i += blockDim.x) ((uint4 *)(sm + SM_X0))[i] = make_uint4(0, 0, 0, 0);
+  /* FP32 W0 of the CUDA-core layer 0, in the (otherwise unused) input-tile area */
+  float *w0 = (float *)(sm + SM_X0);
+  for (int i = tid; i < H * NIN; i += blockDim.x) w0[i] = theta[OFF_W0 + i];
   c.bo = theta[OFF_BO];
   if (warp == 0) umma::tmem_alloc(tmem_slot, 128);
   if (tid == 0) {
@@ -117,30 +122,37 @@ __device__ void fwd_setup(unsigned char *sm, const unsigned char *packed, const 
   c.phase = 0;
 }
 
+/* layer 0 of this thread's row in FP32 on the CUDA cores; BF16 activations
+ * into the operand tile (and, when zrow is given, the pre-activations) */
+__device__ __forceinline__ void layer0_row(unsigned char *sm, const float *w0, const float *b0, const float *f,
+                                           float *zrow, size_t zstride) {
+  const int tid = threadIdx.x;
+#pragma unroll 4
+  for (int j = 0; j < H; j++) {
+    const float z = b0[j] + w0[j * NIN] * f[0] + w0[j * NIN + 1] * f[1] + w0[j * NIN + 2] * f[2];
+    if (zrow) zrow[(size_t)j * zstride] = z;
+    *(__nv_bfloat16 *)(sm + SM_A + umma::kmajor_offset(tid, j, H)) = __float2bfloat16_rn(silu(z));
+  }
+}
+
 /* network output for this thread's feature row f (tile row = thread); all
  * 128 threads call it together; false (for every thread) when a wait ran out */
 __device__ bool fwd_tile(unsigned char *sm, FwdCtx &c, const float *f, float &y) {
   const int tid = threadIdx.x;
   const uint32_t idesc = umma::idesc_bf16_f32(128, 128);
-#pragma unroll
-  for (int k = 0; k < NIN; k++)
-    *(__nv_bfloat16 *)(sm + SM_X0 + umma::kmajor_offset(tid, k, KIN)) = __float2bfloat16_rn(f[k]);
+  layer0_row(sm, (const float *)(sm + SM_X0), c.bias, f, nullptr, 0);
   y = c.bo;
-  for (int l = 0; l < 4; l++) {
+  for (int l = 1; l < 4; l++) {
     umma::fence_proxy_async_smem();
     umma::fence_before_sync();
     __syncthreads();
     if (tid == 0) {
       umma::fence_after_sync();
-      if (l == 0) {
-        umma::mma_bf16(c.tmem, umma::smem_desc(c.s_x0, 128, 256), umma::smem_desc(c.s_w, 128, 256), idesc, false);
-      } else {
-        const uint32_t wl = c.s_w + W0_BYTES + (l - 1) * WL_BYTES;
+      const uint32_t wl = c.s_w + W0_BYTES + (l - 1) * WL_BYTES;
 #pragma unroll
-        for (int kk = 0; kk < H / 16; kk++)
-          umma::mma_bf16(c.tmem, umma::smem_desc(c.s_a + kk * 256, 128, 2048), umma::smem_desc(wl + kk * 256, 128, 2048),
-                         idesc, kk > 0);
-      }
+      for (int kk = 0; kk < H / 16; kk++)
+        umma::mma_bf16(c.tmem, umma::smem_desc(c.s_a + kk * 256, 128, 2048), umma::smem_desc(wl + kk * 256, 128, 2048),
+                       idesc, kk > 0);
       umma::mma_commit(c.mbar);
     }
     const bool ok = umma::mbar_wait(c.mbar, c.phase);
@@ -195,24 +207,35 @@ __global__ void __launch_bounds__(128, 1) forward_kernel(const unsigned char *pa
 }
 
 /* ---------------- surrogate of the solid-angle grid ---------------- */
-/* input domain and feature scaling: the (r, theta) box of the solid-angle
- * grid, features (log r, axial distance r sin(theta), sin(theta) = cosine of
- * the angle to the detector axis) mapped to [-1, 1]; cells of the box on
- * which the network is checked (flag 1: use the integrator instead) */
+/* Input scaling and checked region.  Raw features of a point (r, theta):
+ * log r, the axial distance r sin(theta), and sin(theta) = cosine of the
+ * angle to the detector axis; each mapped to [-1, 1] over the range the
+ * training points cover.  The (log r, theta) box of the training points is
+ * split into ncr x nct cells, each checked against the integrator (flag 1:
+ * use the integrator there). */
 struct Domain {
-  float lr0, lr1, amax, t0, t1;
+  float fmid[3], fhalf[3];
+  float lr0, lr1, t0, t1; /* checked box */
+  float tmin;             /* below the grid's lowest theta the solid angle is 0 */
   int ncr, nct;
-  float eps; /* log target = log(omega + eps) */
+  float eps;              /* log target = log(omega + eps) */
 };
 
 template <typename R>
+__host__ __device__ __forceinline__ void raw_features(R r, R t, float *raw) {
+  const float st = sinf((float)t);
+  raw[0] = logf((float)r);
+  raw[1] = (float)r * st;
+  raw[2] = st;
+}
+
+template <typename R>
 __host__ __device__ __forceinline__ void features_of(const Domain &d, R r, R t, float *f, bool &inside, int &cell) {
-  const float lr = logf((float)r), tt = (float)t;
+  float raw[3];
+  raw_features(r, t, raw);
+  for (int k = 0; k < 3; k++) f[k] = (raw[k] - d.fmid[k]) / d.fhalf[k];
+  const float lr = raw[0], tt = (float)t;
   inside = lr >= d.lr0 && lr <= d.lr1 && tt >= d.t0 && tt <= d.t1;
-  const float st = sinf(tt);
-  f[0] = 2.0f * (lr - d.lr0) / (d.lr1 - d.lr0) - 1.0f;
-  f[1] = 2.0f * (float)r * st / d.amax - 1.0f;
-  f[2] = 2.0f * st - 1.0f;
   int cr = (int)((lr - d.lr0) / (d.lr1 - d.lr0) * d.ncr), ct = (int)((tt - d.t0) / (d.t1 - d.t0) * d.nct);
   cr = cr < 0 ? 0 : (cr >= d.ncr ? d.ncr - 1 : cr);
   ct = ct < 0 ? 0 : (ct >= d.nct ? d.nct - 1 : ct);
@@ -236,7 +259,7 @@ __global__ void __launch_bounds__(128, 1) omega_kernel(const unsigned char *pack
   for (long long tile = blockIdx.x; tile * 128 < n; tile += gridDim.x) {
     const long long i = tile * 128 + threadIdx.x;
     const bool valid = i < n;
-    const R r = valid ? ev[i].sa_r : (R)1, t = valid ? ev[i].sa_t : (R)dom.t0;
+    const R r = valid ? ev[i].sa_r : (R)1, t = valid ? ev[i].sa_t : (R)dom.tmin;
     float f[NIN], y;
     bool inside;
     int cell;
@@ -247,7 +270,7 @@ __global__ void __launch_bounds__(128, 1) omega_kernel(const unsigned char *pack
     }
     if (!valid) continue;
     R omega;
-    if (!(t >= (R)dom.t0)) {
+    if (!(t >= (R)dom.tmin)) {
       omega = (R)0;
     } else if (!inside || flags[cell]) {
       xmi_rng g;
@@ -385,13 +408,23 @@ __global__ void __launch_bounds__(128, 1) train_kernel(const unsigned char *pack
     }
     for (int k = NIN; k < KIN; k++) *(__nv_bfloat16 *)(at + umma::kmajor_offset(k, tid, H)) = __float2bfloat16_rn(0.0f);
     float y = bo;
-    for (int l = 0; l < 4 && !failed; l++) {
-      copy_tile(sm + TR_SW, packed + (l == 0 ? 0 : W0_BYTES + (l - 1) * WL_BYTES), l == 0 ? W0_BYTES : WL_BYTES);
+    {
+      /* layer 0 in FP32 on the CUDA cores (as the forward kernel) */
+      float f[NIN];
+      for (int k = 0; k < NIN; k++) f[k] = valid ? features[(size_t)row * NIN + k] : 0.0f;
+      for (int j = 0; j < H; j++) {
+        const float z = bias[j] + theta[OFF_W0 + j * NIN] * f[0] + theta[OFF_W0 + j * NIN + 1] * f[1] +
+                        theta[OFF_W0 + j * NIN + 2] * f[2];
+        zt[(size_t)j * H + tid] = z;
+        const __nv_bfloat16 a = __float2bfloat16_rn(silu(z));
+        *(__nv_bfloat16 *)(sm + TR_SA + umma::kmajor_offset(tid, j, H)) = a;
+        *(__nv_bfloat16 *)(at + (size_t)WL_BYTES + umma::kmajor_offset(j, tid, H)) = a;
+      }
+    }
+    for (int l = 1; l < 4 && !failed; l++) {
+      copy_tile(sm + TR_SW, packed + W0_BYTES + (l - 1) * WL_BYTES, WL_BYTES);
       const uint32_t idesc = umma::idesc_bf16_f32(128, 128);
-      if (!run_mma([&] {
-            if (l == 0) gemm_issue(d2, s_x0, 256, s_w, 256, 1, idesc);
-            else gemm_issue(d2, s_a, 2048, s_w, 2048, H / 16, idesc);
-          })) {
+      if (!run_mma([&] { gemm_issue(d2, s_a, 2048, s_w, 2048, H / 16, idesc); })) {
         failed = true;
         break;
       }
@@ -764,11 +797,7 @@ int xmi_gpu_build_surrogate(xmi_inputFPtr in, int n_train, int hits_train, int e
   SurrogateState *sg = new SurrogateState();
   std::vector<double> rv(1024), tv(1024);
   xmi_solid_angle_axes(in, 1024, 1024, rv.data(), tv.data());
-  sg->dom.lr0 = (float)std::log(rv.front());
-  sg->dom.lr1 = (float)std::log(rv.back());
-  sg->dom.amax = (float)rv.back();
-  sg->dom.t0 = (float)tv.front();
-  sg->dom.t1 = (float)tv.back();
+  sg->dom.tmin = (float)tv.front();
   sg->dom.ncr = 32;
   sg->dom.nct = 32;
   sg->dom.eps = 1e-10f;
@@ -805,6 +834,27 @@ int xmi_gpu_build_surrogate(xmi_inputFPtr in, int n_train, int hits_train, int e
       r_h[i] = r;
       t_h[i] = M_PI / 2.0 - tt;
     }
+    /* feature scaling and checked box from the training points */
+    float lo[3] = {1e30f, 1e30f, 1e30f}, hi[3] = {-1e30f, -1e30f, -1e30f};
+    float tlo = 1e30f, thi = -1e30f;
+    for (int i = 0; i < n_train; i++) {
+      float raw[3];
+      raw_features(r_h[i], t_h[i], raw);
+      for (int k = 0; k < 3; k++) {
+        lo[k] = std::min(lo[k], raw[k]);
+        hi[k] = std::max(hi[k], raw[k]);
+      }
+      tlo = std::min(tlo, (float)t_h[i]);
+      thi = std::max(thi, (float)t_h[i]);
+    }
+    for (int k = 0; k < 3; k++) {
+      sg->dom.fmid[k] = 0.5f * (lo[k] + hi[k]);
+      sg->dom.fhalf[k] = std::max(0.5f * (hi[k] - lo[k]), 1e-6f);
+    }
+    sg->dom.lr0 = lo[0];
+    sg->dom.lr1 = std::max(hi[0], lo[0] + 1e-6f);
+    sg->dom.t0 = tlo;
+    sg->dom.t1 = std::max(thi, tlo + 1e-6f);
   }
   double *r_d = nullptr, *t_d = nullptr, *o_d = nullptr;
   float *feat_d = nullptr, *pred_d = nullptr;

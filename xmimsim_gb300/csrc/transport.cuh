@@ -461,7 +461,8 @@ __device__ __forceinline__ R polarisation_phi0(const Photon<R> &p) {
 /* Doppler-broadened Compton energy: src/xmi_main.F90:4985-5067 (transport)
  * and src/xmi_variance_reduction.F90:1010-1101 (estimator) */
 template <typename R>
-__device__ R compton_energy(const DevBundle<R> &b, int e, R E, R theta_i, xmi_rng *g, bool varred, bool &ok) {
+__device__ __forceinline__ R compton_energy(const DevBundle<R> &b, int e, R E, R theta_i, xmi_rng *g, bool varred,
+                                           bool &ok) {
   const R c = (R)(double)1.2399e-6f, c0 = (R)(double)4.85e-12f, c1 = (R)(double)1.456e-2f;
   const R *rn = b.dop_r, *icdf = b.dop_icdf + (size_t)e * XMI_DOPPLER_N;
   const R dr = __ldg(rn + 1) - __ldg(rn);
