@@ -1,30 +1,48 @@
 #!/usr/bin/env python3
 """Benchmark: photon histories/s of the XRF transport on GB300.
 
-Workload (default): the production-size plain configuration -- 5 random
-layers (seed 2) of 3-12 elements, Rh tube at 40 kV behind 125 um Be in 400
-intervals plus the Rh K/L lines, 1e8 photons per step, 6 interactions,
-variance reduction on, all-FP64 transport (``--precision fp32`` for the FP32
-transport / FP64 tallies variant).
+Default workload (``--workload batched``): the batched quantification sweep
+-- 512 independent sample configurations in the 45/45 geometry of the small
+plain configuration (1-8 layers of 2-20 elements, weight fractions +-20%
+around the Si/O/Fe/Cu/Zn sample, 1-5 discrete lines or 50-400 intervals of the
+Rh-tube spectrum, photon budgets log-uniform in [1e6, 1e8], 4 interactions,
+variance reduction on), FP32 transport with FP64 tallies, solid angles from
+one surrogate network trained for the detector and shared by all 512, all
+configurations in one graph-captured xmi_main_msim_batch call.
 
-One step = one xmi_main_msim call over the full photon budget.
-  value  -- histories / kernel time (CUDA events on the launching stream;
-            tables and solid-angle grid resident on the device),
-  e2e    -- histories / wall time of the public C-ABI call from the host
-            (source items uploaded, tallies copied back and reshaped into the
-            reference's output layouts inside the timed region).
-Multi-GPU (torchrun): every rank simulates its own disjoint photon range of
-the same size (weak scaling, no data-path collective); the tallies are summed
-over ranks with one reduce after the timed region.
+One step = one xmi_main_msim_batch call over all 512 configurations with
+1/16 of each one's photon budget (``--budget-scale``): the full budgets are
+16 steps.
+  value  -- histories / device time of the call (CUDA events on its stream:
+            transport, event sort, surrogate solid angles, estimator),
+  e2e    -- histories / wall time of the public call from the host (source
+            items and run descriptors uploaded, tallies copied back and
+            reshaped into the reference's output layouts).
+  plain  -- the same 512 configurations one by one with the plain GPU method
+            (FP32, xmi_solid_angle_calculation grid + xmi_main_msim each):
+            the one-by-one transport is timed over all 512, the grid on a
+            sample of them; both full jobs (all 16 steps, the network's
+            training, every grid) are compared.
+  line_error -- surrogate + batched FP32 lines against the all-FP64 plain
+            run (own FP64 grid, same photon streams) on a few configurations.
+
+``--workload plain``: the production-size plain configuration -- 5 random
+layers (seed 2) of 3-12 elements, Rh tube at 40 kV behind 125 um Be in 400
+intervals plus the Rh K/L lines, 6 interactions, one xmi_main_msim per step.
+
+Multi-GPU (torchrun): every rank runs its own configurations (weak scaling,
+no data-path collective).
 
 ``--impl reference`` times the reference algorithm's CPU path: the FP64 C
 restatement under oracle/ (the reference's Fortran build needs gfortran and
-xraylib, absent here) with all host threads, each step a bounded sample.
+xraylib, absent here) with all host threads, each step a bounded sample of
+the same workload.
 """
 from __future__ import annotations
 
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -35,6 +53,9 @@ import time
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
+METRIC = "photon histories/s on 1 GB300: surrogate+batched vs plain, at <=0.5% line error"
+PLAIN_METRIC = "photon histories/s"
+
 
 def parse():
     p = argparse.ArgumentParser()
@@ -42,9 +63,18 @@ def parse():
     p.add_argument("--steps", type=int, default=3)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--photons", type=float, default=1e8, help="photons per step (per GPU)")
-    p.add_argument("--precision", default="fp64", choices=["fp64", "fp32"])
-    p.add_argument("--cpu-sample", type=int, default=200000, help="photons of the CPU-baseline sample")
+    p.add_argument("--workload", default="batched", choices=["batched", "plain"])
+    p.add_argument("--configs", type=int, default=512, help="configurations of the batched workload")
+    p.add_argument("--budget-scale", type=float, default=1.0 / 16, help="share of each budget per step")
+    p.add_argument("--n-train", type=int, default=1 << 21, help="integrator samples the surrogate trains on")
+    p.add_argument("--epochs", type=int, default=8)
+    p.add_argument("--tolerance", type=float, default=1e-3, help="surrogate held-out error limit")
+    p.add_argument("--plain-grids", type=int, default=4, help="grids timed for the plain comparison")
+    p.add_argument("--line-configs", type=int, default=3, help="configurations of the FP64 line-error check")
+    p.add_argument("--no-plain", action="store_true")
+    p.add_argument("--photons", type=float, default=1e7, help="photons per step of the plain workload")
+    p.add_argument("--precision", default="fp32", choices=["fp64", "fp32"])
+    p.add_argument("--cpu-sample", type=int, default=100000, help="photons of the CPU-baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
     return p.parse_args()
 
@@ -103,62 +133,343 @@ def dist_env():
     return ws, rank, local
 
 
-def workload_spec(photons: int):
+def histories(spec) -> int:
+    """Photon histories one xmi_main_msim of spec simulates (src/xmi_main.F90:240-858)."""
+    return int(spec.n_photons_interval) * max(0, len(spec.continuous) - 1) + \
+        int(spec.n_photons_line) * len(spec.discrete)
+
+
+def peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        return {}
+
+
+# --------------------------------------------------------------------------
+# workloads
+# --------------------------------------------------------------------------
+def plain_workload(photons: float):
     from xmimsim_gb300 import configs
-    return configs.config2(total_photons=int(photons)), dict(configs.C2_OPTIONS, use_sum_peaks=0)
+    spec = configs.config2(total_photons=int(photons))
+    return spec, dict(configs.C2_OPTIONS, use_sum_peaks=0)
 
 
-def run_cpu_sample(spec, options, n_sample: int, threads: int):
+def batched_specs(n: int, scale: float, rank: int = 0):
+    from xmimsim_gb300 import configs
+    return configs.config5(n, seed=5 + 1000 * rank, budget_scale=scale), dict(configs.C5_OPTIONS)
+
+
+def total_thickness(spec) -> float:
+    return sum(l.thickness for l in spec.layers)
+
+
+# --------------------------------------------------------------------------
+# CPU baseline (the oracle: FP64 restatement of the reference's algorithm)
+# --------------------------------------------------------------------------
+def run_cpu_sample(specs, options, n_sample: int, threads: int):
     """Times the FP64 CPU restatement (all threads) on a bounded sample of the
-    workload; returns (histories/s, histories, seconds, words/history)."""
+    workload: about n_sample photons spread over the given configurations.
+    Returns (histories/s, histories, seconds, words/history of transport,
+    words/history of the estimator loops)."""
     from oracle import oracle_api
     from xmimsim_gb300 import Simulation, gpu_options
     import numpy as np
-    n_items = len(spec.discrete) + max(0, len(spec.continuous) - 1)
-    per_item = max(1, n_sample // max(1, n_items))
-    sim = Simulation(spec, options=options, gpu=gpu_options(seed=0x5EED0001))
-    # the CPU path uses a coarse grid over the same axes, built here (untimed) so that no GPU is needed
-    r, t = sim.grid_axes(64, 64)
-    sim.set_solid_angle(r, t, np.zeros((64, 64)))
-    sim.prepare()
-    g = oracle_api.solid_angle_points(sim.bundle_ptr(), r, t, 0, 64 * 64, 500).reshape(64, 64)
-    sim.set_solid_angle(r, t, g)
-    sim.prepare()
-    oracle_api.words_counted_split()
-    t0 = time.perf_counter()
-    oracle_api.msim(sim.bundle_ptr(), spec.n_interactions_trajectory, spec.nchannels, threads=threads,
-                    max_photons_per_item=per_item)
-    dt = time.perf_counter() - t0
-    words, words_est = oracle_api.words_counted_split()
-    n = per_item * n_items
-    sim.close()
-    return n / dt, n, dt, (words - words_est) / n, words_est / n
+    n_hist, dt, words_tr, words_est = 0, 0.0, 0, 0
+    per_cfg = max(1, n_sample // len(specs))
+    for spec in specs:
+        n_items = len(spec.discrete) + max(0, len(spec.continuous) - 1)
+        per_item = max(1, per_cfg // max(1, n_items))
+        sim = Simulation(spec, options=options, gpu=gpu_options(seed=0x5EED0001))
+        # the CPU path uses a coarse grid over the same axes, built here (untimed) so that no GPU is needed
+        r, t = sim.grid_axes(64, 64)
+        sim.set_solid_angle(r, t, np.zeros((64, 64)))
+        sim.prepare()
+        g = oracle_api.solid_angle_points(sim.bundle_ptr(), r, t, 0, 64 * 64, 500).reshape(64, 64)
+        sim.set_solid_angle(r, t, g)
+        sim.prepare()
+        oracle_api.words_counted_split()
+        t0 = time.perf_counter()
+        oracle_api.msim(sim.bundle_ptr(), spec.n_interactions_trajectory, spec.nchannels, threads=threads,
+                        max_photons_per_item=per_item)
+        dt += time.perf_counter() - t0
+        w, we = oracle_api.words_counted_split()
+        words_tr += w - we
+        words_est += we
+        n_hist += min(per_item, int(spec.n_photons_line)) * len(spec.discrete) + \
+            min(per_item, int(spec.n_photons_interval)) * max(0, len(spec.continuous) - 1)
+        sim.close()
+    return n_hist / dt, n_hist, dt, words_tr / n_hist, words_est / n_hist
+
+
+def cpu_sample_specs(args, rank=0):
+    if args.workload == "plain":
+        spec, options = plain_workload(args.photons)
+        return [spec], options, "the %.0e-photon plain workload" % args.photons
+    specs, options = batched_specs(args.configs, args.budget_scale, rank)
+    pick = [specs[i] for i in range(0, len(specs), max(1, len(specs) // 8))][:8]
+    return pick, options, "8 of the %d batched configurations" % len(specs)
 
 
 def reference_arm(args):
     ws, rank, _ = dist_env()
     if rank != 0:
         return
-    from xmimsim_gb300 import Simulation
-    spec, options = workload_spec(args.photons)
+    specs, options, what = cpu_sample_specs(args)
     threads = os.cpu_count() or 1
     vals = []
     for i in range(args.warmup + args.steps):
-        v, n, dt, _, _ = run_cpu_sample(spec, options, args.cpu_sample, threads)
+        v, n, dt, _, _ = run_cpu_sample(specs, options, args.cpu_sample, threads)
         if i >= args.warmup:
             vals.append((v, n, dt))
     value = statistics.median(v for v, _, _ in vals)
-    sample = "%d photons per step of the %.0e-photon workload" % (vals[0][1], args.photons)
-    line = {"metric": "photon histories/s", "value": value, "unit": "histories/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": statistics.median(d for _, _, d in vals) * 1e3,
+    sample = "%d photons per step over %s" % (vals[0][1], what)
+    batched = args.workload == "batched"
+    line = {"metric": METRIC if batched else PLAIN_METRIC, "value": value, "unit": "histories/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": statistics.median(d for _, _, d in vals) * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic (seeded random 5-layer sample, Rh tube spectrum)",
-            "config": {"workload": "plain 5-layer Rh 40 kV, 6 interactions, VR on", "photons_per_step": vals[0][1]},
+            "data": "synthetic (seeded random samples, Rh tube spectrum / discrete lines)",
+            "config": workload_config(args, None),
             "impl": "reference",
             "cpu_baseline": {"value": value, "unit": "histories/s", "cores": threads, "kind": "port",
                              "sample": sample},
             "e2e": {"value": value, "unit": "histories/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
+
+
+def workload_config(args, extra):
+    if args.workload == "plain":
+        cfg = {"workload": "plain 5-layer Rh 40 kV, 400 intervals + Rh K/L lines, 6 interactions, VR on",
+               "photons_per_step": int(args.photons)}
+    else:
+        cfg = {"workload": "%d-configuration quantification sweep: 1-8 layers of 2-20 elements, 1-5 lines or "
+                           "50-400 Rh-tube intervals, budgets log-uniform 1e6-1e8, 4 interactions, VR on, "
+                           "FP32 + shared surrogate, one graph-captured batched call" % args.configs,
+               "configs": args.configs, "budget_share_per_step": args.budget_scale,
+               "steps_per_full_job": round(1.0 / args.budget_scale)}
+    if extra:
+        cfg.update(extra)
+    return cfg
+
+
+# --------------------------------------------------------------------------
+# our arm
+# --------------------------------------------------------------------------
+def load_cudart():
+    import ctypes as C
+    try:
+        return C.CDLL("libcudart.so")
+    except OSError:
+        import glob
+        c = glob.glob("/usr/local/cuda/lib64/libcudart.so*")
+        return C.CDLL(c[0]) if c else None
+
+
+def timed_steps(args, step, local):
+    """W untimed steps, then K timed ones between device synchronisations;
+    returns (per-step timing dicts, wall seconds, clocks summary)."""
+    cudart = load_cudart()
+    for _ in range(args.warmup):
+        step()
+    if cudart is not None:
+        cudart.cudaDeviceSynchronize()
+    tms = []
+    with ClockSampler(local) as clocks:
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            tms.append(step())
+        if cudart is not None:
+            cudart.cudaDeviceSynchronize()
+        wall = time.perf_counter() - t0
+    return tms, wall, clocks.summary()
+
+
+def roofline_block(ph_ms: dict, n_hist_per_step: int, words_tr: float, words_est: float, word: int):
+    """Dominant kernel: algorithmic table bytes it reads per history (counted
+    by the instrumented oracle on the CPU sample) over its device time."""
+    kern = "estimator_kernel" if ph_ms["estimator"] >= ph_ms["transport"] else "wf_step + wf_interact"
+    kms = ph_ms["estimator"] if kern == "estimator_kernel" else ph_ms["transport"]
+    bph = (words_est if kern == "estimator_kernel" else words_tr) * word
+    pk = peaks()
+    peak = pk.get("hbm_gbs", 6800.0)
+    achieved = bph * n_hist_per_step / (kms / 1e3) / 1e9 if kms > 0 else 0.0
+    return {"bound": "hbm", "kernel": kern, "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "traffic": None, "algorithmic_bytes_per_history": bph,
+            "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if pk else "fallback 6.8 TB/s"}
+
+
+def line_error(sur_out: dict, ref_out: dict, floor: float = 1e-2) -> dict:
+    """Relative error of every line (summed over interaction orders) carrying
+    at least `floor` of the configuration's strongest line."""
+    import numpy as np
+    a = sur_out["var_red"].sum(axis=2).ravel()
+    b = ref_out["var_red"].sum(axis=2).ravel()
+    m = b > floor * b.max()
+    rel = np.abs(a[m] - b[m]) / b[m]
+    return {"lines": int(m.sum()), "max": float(rel.max()) if m.any() else 0.0,
+            "median": float(np.median(rel)) if m.any() else 0.0,
+            "within_0.5pct": float((rel <= 5e-3).mean()) if m.any() else 1.0,
+            "total": float(abs(a.sum() - b.sum()) / b.sum()) if b.sum() > 0 else 0.0}
+
+
+def batched_arm(args, ws, rank, local):
+    import numpy as np
+    from xmimsim_gb300 import Simulation, gpu_options, last_timing
+    specs, options = batched_specs(args.configs, args.budget_scale, rank)
+    seed = 0x5EED0005 + rank
+    g_sur = gpu_options(precision=1, seed=seed, use_surrogate=1, surrogate_tolerance=args.tolerance)
+    t0 = time.perf_counter()
+    sims = [Simulation(s, options=options, gpu=g_sur) for s in specs]
+    host_tables_s = time.perf_counter() - t0
+    n_hist = sum(histories(s) for s in specs)
+    full_specs, _ = batched_specs(args.configs, 1.0, rank)
+    full_hist = sum(histories(s) for s in full_specs)
+
+    # one network for the detector, trained on the deepest sample's volume
+    deep = max(range(len(specs)), key=lambda i: total_thickness(specs[i]))
+    t0 = time.perf_counter()
+    rep = sims[deep].build_surrogate(n_train=args.n_train, hits_train=1024, epochs=args.epochs, hits_check=1 << 20)
+    train_s = time.perf_counter() - t0
+    for i, s in enumerate(sims):
+        if i != deep:
+            s.share_surrogate(sims[deep])
+
+    last = {}
+
+    def step():
+        outs = Simulation.msim_batch(sims)
+        tm = last_timing()
+        if "outs" in last:
+            for s, o in zip(sims, last["outs"]):
+                s.free_raw(o)
+        last["outs"] = outs
+        return tm
+
+    tms, wall, clocks = timed_steps(args, step, local)
+    ksum = sum(t["kernel_ms"] for t in tms)
+    value = n_hist * args.steps / (ksum / 1e3)
+    e2e = n_hist * args.steps / wall
+    phases = {k: statistics.mean(t[k + "_ms"] for t in tms) for k in ("transport", "sort", "surrogate", "estimator")}
+    extra = {"photons_per_step": n_hist, "photons_full_job": full_hist,
+             "elements_per_config_mean": statistics.mean(sum(len(l.Z) for l in s.layers) for s in specs),
+             "l2": "inputs larger than L2 (tables of 512 configurations, several GB)",
+             "host_tables_s": host_tables_s,
+             "surrogate": dict(rep, n_train=args.n_train, epochs=args.epochs, tolerance=args.tolerance,
+                               wall_s=train_s)}
+    line = {"metric": METRIC, "value": value, "unit": "histories/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ksum / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 transport, f64 tallies",
+            "data": "synthetic (seeded random samples, Rh tube spectrum / discrete lines)",
+            "config": workload_config(args, extra),
+            "gpu_launches": sum(t["launches"] for t in tms),
+            "phases_ms_per_step": phases,
+            "events_per_step": statistics.mean(t["events"] for t in tms),
+            "surrogate_fallbacks_per_step": statistics.mean(t["surrogate_fallbacks"] for t in tms),
+            "e2e": {"value": e2e, "unit": "histories/s",
+                    "h2d_bytes_per_step": int(statistics.mean(t["h2d_bytes"] for t in tms)),
+                    "d2h_bytes_per_step": int(statistics.mean(t["d2h_bytes"] for t in tms))},
+            "clocks": clocks}
+    steps_full = 1.0 / args.budget_scale
+    sb_full_s = train_s + steps_full * wall / args.steps
+
+    if not args.no_plain:
+        # the plain GPU method one by one: a grid per configuration, then its transport
+        g_plain = gpu_options(precision=1, seed=seed)
+        grid_s = []
+        for i in np.linspace(0, len(sims) - 1, args.plain_grids).astype(int):
+            ps = Simulation(specs[i], options=options, gpu=g_plain)
+            t0 = time.perf_counter()
+            ps.solid_angle()
+            grid_s.append(time.perf_counter() - t0)
+            ps.close()
+        # transport of all configurations one by one, each on a grid (the
+        # deepest sample's, whose axes span every other's) -- timed
+        gd = sims[deep]
+        gd.set_gpu(g_plain)
+        ax = gd.solid_angle_grid()
+        for s in sims:
+            s.set_gpu(g_plain)
+            s.set_solid_angle(ax["r"], ax["theta"], ax["grid"])
+        load_cudart().cudaDeviceSynchronize()
+        t0 = time.perf_counter()
+        dev_ms = 0.0
+        for s in sims:
+            o = s.msim()
+            dev_ms += s.timing()["kernel_ms"]
+            s.free_raw(o)
+        one_by_one_s = time.perf_counter() - t0
+        plain_full_s = len(sims) * statistics.mean(grid_s) + steps_full * one_by_one_s
+        line["plain"] = {
+            "method": "one xmi_solid_angle_calculation grid + one xmi_main_msim per configuration, FP32",
+            "value": n_hist / one_by_one_s, "unit": "histories/s",
+            "note": "value: one-by-one transport of one step's budgets (wall, grids excluded)",
+            "device_value": n_hist / (dev_ms / 1e3),
+            "grid_s_per_config": statistics.mean(grid_s), "grids_timed": len(grid_s),
+            "full_job_s": plain_full_s, "full_job_histories_per_s": full_hist / plain_full_s}
+        line["surrogate_batched_full_job"] = {"full_job_s": sb_full_s,
+                                              "full_job_histories_per_s": full_hist / sb_full_s,
+                                              "includes": "network training + 16 batched steps (wall)"}
+        line["speedup_full_job_vs_plain"] = plain_full_s / sb_full_s
+        for s in sims:
+            s.set_gpu(g_sur)
+
+    if args.line_configs > 0 and "outs" in last:
+        # all-FP64 plain runs (own FP64 grid, same seed) of a few configurations
+        errs = []
+        order = sorted(range(len(specs)), key=lambda i: histories(specs[i]))
+        pick = [order[len(order) * (k + 1) // (args.line_configs + 1)] for k in range(args.line_configs)]
+        for i in pick:
+            ref = Simulation(specs[i], options=options, gpu=gpu_options(precision=0, seed=seed))
+            r = ref.msim()
+            e = line_error(last["outs"][i], r)
+            e.update(config=int(i), photons=histories(specs[i]))
+            errs.append(e)
+            ref.free_raw(r)
+            ref.close()
+        line["line_error"] = {"reference": "all-FP64 plain GPU run, own FP64 grid, same photon streams",
+                              "lines": "lines with >= 1% of the configuration's strongest", "configs": errs}
+    if "outs" in last:
+        for s, o in zip(sims, last["outs"]):
+            s.free_raw(o)
+    return line, sims, specs, options
+
+
+def plain_arm(args, ws, rank, local):
+    from xmimsim_gb300 import Simulation, gpu_options
+    spec, options = plain_workload(args.photons)
+    precision = 0 if args.precision == "fp64" else 1
+    t0 = time.perf_counter()
+    sim = Simulation(spec, options=options, gpu=gpu_options(precision=precision, seed=0x5EED0001 + rank))
+    sim.solid_angle()
+    grid_s = time.perf_counter() - t0
+    n_hist = histories(spec)
+
+    def step():
+        out = sim.msim()
+        tm = sim.timing()
+        sim.free_raw(out)
+        return tm
+
+    tms, wall, clocks = timed_steps(args, step, local)
+    ksum = sum(t["kernel_ms"] for t in tms)
+    line = {"metric": PLAIN_METRIC, "value": n_hist * args.steps / (ksum / 1e3), "unit": "histories/s",
+            "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ksum / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if precision == 0 else "f32 transport, f64 tallies",
+            "data": "synthetic (seeded random 5-layer sample, Rh tube spectrum)",
+            "config": workload_config(args, {"elements": sum(len(l.Z) for l in spec.layers),
+                                             "l2": "inputs larger than L2 (angular tables exceed 129 MB)",
+                                             "solid_angle_grid_s": grid_s}),
+            "gpu_launches": sum(t["launches"] for t in tms),
+            "phases_ms_per_step": {k: statistics.mean(t[k + "_ms"] for t in tms)
+                                   for k in ("transport", "sort", "estimator")},
+            "events_per_step": statistics.mean(t["events"] for t in tms),
+            "e2e": {"value": n_hist * args.steps / wall, "unit": "histories/s",
+                    "h2d_bytes_per_step": int(statistics.mean(t["h2d_bytes"] for t in tms)),
+                    "d2h_bytes_per_step": int(statistics.mean(t["d2h_bytes"] for t in tms))},
+            "clocks": clocks}
+    return line, [sim], [spec], options
 
 
 def main():
@@ -167,119 +478,37 @@ def main():
         reference_arm(args)
         return
     ws, rank, local = dist_env()
-    import ctypes as C
-    import numpy as np
     if ws > 1:
         import torch
         import torch.distributed as dist
         torch.cuda.set_device(local)
         dist.init_process_group("nccl")
-    from xmimsim_gb300 import Simulation, abi, gpu_options
+        cudart = load_cudart()
+        if cudart is not None:
+            cudart.cudaSetDevice(local)
     from xmimsim_gb300.build import build_all
     build_all()
-    lib = abi.load()
-    cudart = None
-    try:
-        cudart = C.CDLL("libcudart.so")
-    except OSError:
-        import glob
-        c = glob.glob("/usr/local/cuda/lib64/libcudart.so*")
-        cudart = C.CDLL(c[0]) if c else None
-    if cudart is not None and ws > 1:
-        cudart.cudaSetDevice(local)
-
-    spec, options = workload_spec(args.photons)
-    precision = 0 if args.precision == "fp64" else 1
-    t_setup = time.perf_counter()
-    sim = Simulation(spec, options=options, gpu=gpu_options(precision=precision, seed=0x5EED0001 + rank))
-    sim.solid_angle()
-    t_setup = time.perf_counter() - t_setup
-    n_hist = int(spec.n_photons_interval) * (len(spec.continuous) - 1) + int(spec.n_photons_line) * len(spec.discrete)
-
-    def step():
-        out = sim.msim()
-        tm = sim.timing()
-        sim.free_raw(out)
-        return out, tm
-
-    for _ in range(args.warmup):
-        step()
-    if ws > 1:
-        dist.barrier()
-    if cudart is not None:
-        cudart.cudaDeviceSynchronize()
-    kernel_ms, launches, phases = [], 0, []
-    with ClockSampler(local) as clocks:
-        t0 = time.perf_counter()
-        for _ in range(args.steps):
-            out, tm = step()
-            kernel_ms.append(tm["kernel_ms"])
-            launches += tm["launches"]
-            phases.append(tm)
-        if cudart is not None:
-            cudart.cudaDeviceSynchronize()
-        wall = time.perf_counter() - t0
+    arm = batched_arm if args.workload == "batched" else plain_arm
+    line, sims, specs, options = arm(args, ws, rank, local)
     if ws > 1:
         import torch
-        t = torch.tensor([wall, sum(kernel_ms)], dtype=torch.float64, device="cuda")
+        t = torch.tensor([line["ms_per_step"]], dtype=torch.float64, device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        wall, ksum = t.tolist()
-        # the reference's MPI reduce of the tallies (bin/xmimsim.c:402-410), after the timed region
-        ch = torch.tensor(out["channels"], device="cuda")
-        dist.all_reduce(ch)
-    else:
-        ksum = sum(kernel_ms)
-    total_hist = n_hist * ws * args.steps
-    value = total_hist / (ksum / 1e3)
-    e2e = total_hist / wall
-    if rank != 0:
-        if ws > 1:
-            dist.destroy_process_group()
-        return
-    line = {"metric": "photon histories/s", "value": value, "unit": "histories/s", "n_gpus": ws,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ksum / args.steps,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64" if precision == 0 else "f32 transport, f64 tallies",
-            "data": "synthetic (seeded random 5-layer sample, Rh tube spectrum)",
-            "config": {"workload": "plain 5-layer Rh 40 kV, 400 intervals + Rh K/L lines, 6 interactions, VR on",
-                       "photons_per_step": n_hist, "elements": sum(len(l.Z) for l in spec.layers),
-                       "l2": "inputs larger than L2 (angular tables of all elements exceed 129 MB)",
-                       "solid_angle_grid_s": t_setup},
-            "gpu_launches": launches,
-            "phases_ms_per_step": {k: statistics.mean(p[k + "_ms"] for p in phases)
-                                   for k in ("transport", "sort", "estimator")},
-            "events_per_step": statistics.mean(p["events"] for p in phases),
-            "e2e": {"value": e2e, "unit": "histories/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-            "clocks": clocks.summary()}
-    # host<->device bytes of one public call: source items in, tallies out
-    n_items = (len(spec.continuous) - 1) + len(spec.discrete)
-    line["e2e"]["h2d_bytes_per_step"] = n_items * (128 + 8)
-    nslots = 0
-    line["e2e"]["d2h_bytes_per_step"] = int(8 * (spec.n_interactions_trajectory + 1) * spec.nchannels)
-    if not args.no_cpu_baseline:
-        cv, cn, cdt, words_tr, words_est = run_cpu_sample(spec, options, args.cpu_sample, os.cpu_count() or 1)
+        line["ms_per_step"] = t.item()
+        n_step = line["value"] * line["ms_per_step"] / 1e3  # per-rank histories per step
+        line["value"] = n_step * ws / (line["ms_per_step"] / 1e3)
+    if rank == 0 and not args.no_cpu_baseline:
+        cspecs, coptions, what = cpu_sample_specs(args, rank)
+        cv, cn, cdt, words_tr, words_est = run_cpu_sample(cspecs, coptions, args.cpu_sample, os.cpu_count() or 1)
         line["cpu_baseline"] = {"value": cv, "unit": "histories/s", "cores": os.cpu_count(), "kind": "port",
-                                "sample": "%d photons (%.2f s) of the same workload" % (cn, cdt)}
-        # dominant kernel: algorithmic table bytes it reads per history (counted
-        # by the instrumented oracle on the sample) over its device time
-        word = 8 if precision == 0 else 4
-        ph = line["phases_ms_per_step"]
-        kern = "estimator_kernel" if ph["estimator"] >= ph["transport"] else "transport_kernel"
-        kms = ph["estimator"] if kern == "estimator_kernel" else ph["transport"]
-        bph = (words_est if kern == "estimator_kernel" else words_tr) * word
-        peaks = {}
-        try:
-            peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
-        except Exception:
-            pass
-        peak = peaks.get("hbm_gbs", 6800.0)
-        achieved = bph * n_hist / (kms / 1e3) / 1e9 if kms > 0 else 0.0
-        line["roofline"] = {"bound": "hbm", "kernel": kern, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                            "frac": achieved / peak, "traffic": None,
-                            "algorithmic_bytes_per_history": bph,
-                            "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if peaks else "fallback 6.8 TB/s"}
-    print(json.dumps(line))
-    sim.close()
+                                "sample": "%d photons (%.2f s) over %s" % (cn, cdt, what)}
+        word = 4 if line["dtype"].startswith("f32") else 8
+        line["roofline"] = roofline_block(line["phases_ms_per_step"], line["config"]["photons_per_step"],
+                                          words_tr, words_est, word)
+    if rank == 0:
+        print(json.dumps(line))
+    for s in sims:
+        s.close()
     if ws > 1:
         dist.destroy_process_group()
 

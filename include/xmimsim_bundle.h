@@ -30,7 +30,7 @@ extern "C" {
 #define XMI_MAXN 10       /* maximum interactions per trajectory */
 #define XMI_NSHELL 9      /* K..M5 */
 #define XMI_NCK 14        /* Coster-Kronig transitions FL12..FM45 */
-#define XMI_MAXSEG 256    /* maximum energy-grid segments */
+#define XMI_MAXSEG 2048   /* maximum energy-grid segments */
 
 /* per-node record of element tables (el_tab) */
 enum {
@@ -153,14 +153,16 @@ typedef struct {
   /* ---- angular tables ---- */
   double *icdf_energies;  /* [400] 0.1..200 keV */
   double *icdf_rs;        /* [2000] 0..1 */
-  double *rayl_icdf;      /* [n_elem][400][2000] theta */
-  double *compt_icdf;     /* [n_elem][400][2000] theta */
+  /* tables that depend on Z alone are shared by every bundle of the process:
+   * per element a pointer into the cache, not owned by the bundle */
+  const double **rayl_icdf;  /* [n_elem] -> [400][2000] theta */
+  const double **compt_icdf; /* [n_elem] -> [400][2000] theta */
   double *phi_thetas;     /* [200] 0..0.5 */
-  double *phi_icdf;       /* [200][2000] */
+  const double *phi_icdf; /* [200][2000], shared by every bundle of the process */
   double *doppler_rs;     /* [10001] */
-  double *doppler_icdf;   /* [n_elem][10001] pz */
-  double *ff2;            /* [n_elem][XMI_NQ] Rayleigh form factor squared x N_A/A x r_e^2 */
-  double *sf;             /* [n_elem][XMI_NQ] incoherent scattering function x N_A/A */
+  const double **doppler_icdf; /* [n_elem] -> [10001] pz */
+  const double **ff2;      /* [n_elem] -> [XMI_NQ] Rayleigh form factor squared x N_A/A x r_e^2 */
+  const double **sf;       /* [n_elem] -> [XMI_NQ] incoherent scattering function x N_A/A */
 
   /* ---- source ---- */
   int n_items;

@@ -125,7 +125,10 @@ int xmi_detector_convolute_spectrum_noalloc(xmi_inputFPtr inputFPtr, const doubl
  * configurations (each handle built by the initialisation chain above, all
  * with the same xmi_gpu_options precision) in one chunked launch sequence,
  * captured as one CUDA graph: their photons share the transport, sort and
- * estimator kernels.  Outputs per configuration as xmi_main_msim's, in
+ * estimator kernels.  Configurations with xmi_gpu_options.use_surrogate = 1
+ * and a trained surrogate take their solid angles from it (all such
+ * configurations of one call must share one network, see
+ * xmi_gpu_share_surrogate); the others from their grid.  Outputs per configuration as xmi_main_msim's, in
  * channels[c], brute_histories[c], var_red_histories[c] (n_mpi_hosts = 1).
  * Calls are serialised within a process. */
 int xmi_main_msim_batch(int n, xmi_inputFPtr *inputFPtrs, xmi_hdf5FPtr *hdf5FPtrs, xmi_main_options **options,
@@ -140,8 +143,10 @@ int xmi_main_msim_batch(int n, xmi_inputFPtr *inputFPtrs, xmi_hdf5FPtr *hdf5FPtr
  * (the slab of the layers within 2 cm of the beam axis), targets from the
  * engine's own integrator (hits_train cone samples each, FP32), Adam for
  * `epochs` passes; then checks it on 16 x 1024 further points against the
- * FP64 integrator (hits_check samples) and flags the cells of a 32 x 32
- * partition of the grid's (log r, theta) box whose error exceeds
+ * FP64 integrator (two independent integrations of hits_check / 2 samples
+ * per point, whose difference measures the reference values' own noise) and
+ * flags the cells of a 32 x 32 partition of the grid's (log r, theta) box
+ * whose RMS relative error, less that noise, exceeds
  * xmi_gpu_options.surrogate_tolerance (and the cells no point reached):
  * there the integrator keeps serving.  report[6]: median relative error of
  * the checking points, largest error in an unflagged cell, share of checking
@@ -151,9 +156,18 @@ int xmi_main_msim_batch(int n, xmi_inputFPtr *inputFPtrs, xmi_hdf5FPtr *hdf5FPtr
 int xmi_gpu_build_surrogate(xmi_inputFPtr inputFPtr, int n_train, int hits_train, int epochs, int hits_check,
                             double *report);
 int xmi_gpu_surrogate_report(xmi_inputFPtr inputFPtr, double *report);
+/* lets input `to` use the network trained for input `from` (same detector
+ * radius and collimator required; points outside the network's checked box
+ * are served by the integrator) -- one training serves a batch of samples
+ * measured with one detector */
+int xmi_gpu_share_surrogate(xmi_inputFPtr from, xmi_inputFPtr to);
 /* device time of the surrogate phase of the last xmi_main_msim and the
  * number of estimator events served by the integrator fallback */
 int xmi_gpu_last_surrogate(double *surrogate_ms, long long *fallbacks);
+/* bytes copied host -> device and device -> host by the last xmi_main_msim
+ * or xmi_main_msim_batch call (source items, run descriptors, a changed
+ * solid-angle grid; tallies and status words) */
+int xmi_gpu_last_transfers(long long *h2d_bytes, long long *d2h_bytes);
 /* the network alone, for tests of the tensor-core kernels: parameter count,
  * outputs, gradient of the mean squared error, Adam training */
 int xmi_mlp_nparam(void);

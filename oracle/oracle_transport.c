@@ -176,13 +176,13 @@ static double qtab(const double *t, double q) {
 /* DCSP_Rayl and DCSP_Compt (xraylib) from the bundle's form-factor tables */
 static double dcsp_rayl(const xmi_bundle *b, int e, double E, double theta, double phi) {
   double q = E / 12.39852 * sin(theta / 2.0), st = sin(theta), cp = cos(phi);
-  return (1.0 - st * st * cp * cp) * qtab(b->ff2 + (size_t)e * XMI_NQ, q);
+  return (1.0 - st * st * cp * cp) * qtab(b->ff2[e], q);
 }
 static double dcsp_compt(const xmi_bundle *b, int e, double E, double theta, double phi) {
   double q = E / 12.39852 * sin(theta / 2.0), ct = cos(theta), st = sin(theta), cp = cos(phi);
   double k0k = 1.0 + (1.0 - ct) * E / 510.998928, kk0 = 1.0 / k0k;
   double kn = 0.25 * kk0 * kk0 * (kk0 + k0k - 2.0 * st * st * cp * cp);
-  return kn * qtab(b->sf + (size_t)e * XMI_NQ, q);
+  return kn * qtab(b->sf[e], q);
 }
 
 /* ------------------------------------------------------------------ */
@@ -384,7 +384,7 @@ static double polarisation_phi0(const ophoton *p) {
 static double compton_energy(const xmi_bundle *b, int e, double E, double theta_i, orng *g,
                              int varred, int *err) {
   const double c = (double)1.2399e-6f, c0 = (double)4.85e-12f, c1 = (double)1.456e-2f;
-  const double *rn = b->doppler_rs, *icdf = b->doppler_icdf + (size_t)e * XMI_DOPPLER_N;
+  const double *rn = b->doppler_rs, *icdf = b->doppler_icdf[e];
   double energy = E * 1000.0, c_lamb0 = c / energy, sth2 = sin(theta_i / 2.0);
   int it = 0, tries = 0;
   for (;;) {
@@ -642,7 +642,7 @@ static int rayleigh(const xmi_bundle *b, ophoton *p, orng *g) {
   int e = p->cur_elem, err = 0;
   double theta_i, tt, phi_i, phi0, r;
   r = orng_uniform(g);
-  theta_i = bilinear(b->rayl_icdf + (size_t)e * XMI_ICDF_NE * XMI_ICDF_NR, b->icdf_rs, XMI_ICDF_NR,
+  theta_i = bilinear(b->rayl_icdf[e], b->icdf_rs, XMI_ICDF_NR,
                      b->icdf_energies, XMI_ICDF_NE, r, p->energy, &err);
   if (err) return 0;
   tt = sin(theta_i) * sin(theta_i);
@@ -662,7 +662,7 @@ static int compton(const xmi_bundle *b, ophoton *p, orng *g) {
   int e = p->cur_elem, err = 0;
   double theta_i, k0k, tt, phi_i, phi0, r, pp, rat, rk, w_h;
   r = orng_uniform(g);
-  theta_i = bilinear(b->compt_icdf + (size_t)e * XMI_ICDF_NE * XMI_ICDF_NR, b->icdf_rs, XMI_ICDF_NR,
+  theta_i = bilinear(b->compt_icdf[e], b->icdf_rs, XMI_ICDF_NR,
                      b->icdf_energies, XMI_ICDF_NE, r, p->energy, &err);
   if (err) return 0;
   k0k = 1.0 + p->energy * (1.0 - cos(theta_i)) / O_MEC2;

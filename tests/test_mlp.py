@@ -163,3 +163,41 @@ def test_surrogate_replaces_the_grid_in_transport():
     np.testing.assert_allclose(v_s[big], v_g[big], rtol=3e-2)
     grid.close()
     sur.close()
+
+
+@pytest.mark.gpu
+def test_shared_surrogate_in_a_batch_matches_single_runs():
+    """One network trained for the thickest of three samples measured with the
+    same collimated detector serves two of them in one batched launch
+    (xmi_gpu_share_surrogate); the third keeps its grid.  Each configuration
+    gets its single-run result (same photon streams and network; only the
+    order of FP64 additions differs).  A detector of another radius is
+    refused."""
+    from xmimsim_gb300 import Simulation, configs, gpu_options
+    specs = [collimated_spec(6000) for _ in range(3)]
+    specs[1].layers[1].thickness *= 0.5
+    specs[1].layers[1].weight = [0.35, 0.55, 0.05, 0.03, 0.02]
+    specs[2].layers[1].thickness *= 0.25
+    opts = configs.C1_OPTIONS
+    g_sur = gpu_options(seed=0x5EED0002, use_surrogate=1, surrogate_tolerance=2e-2)
+    sims = [Simulation(specs[0], options=opts, gpu=g_sur), Simulation(specs[1], options=opts, gpu=g_sur),
+            Simulation(specs[2], options=opts, gpu=gpu_options(seed=0x5EED0002))]
+    sims[0].build_surrogate(n_train=1 << 17, hits_train=1024, epochs=10, hits_check=1 << 14)
+    sims[1].share_surrogate(sims[0])
+    assert sims[1].surrogate_on() and not sims[2].surrogate_on()
+    batched = Simulation.msim_batch(sims)
+    for s, b in zip(sims, batched):
+        single = s.msim()
+        np.testing.assert_allclose(b["var_red"], single["var_red"], rtol=1e-9,
+                                   atol=1e-12 * abs(single["var_red"]).max())
+        np.testing.assert_allclose(b["channels"], single["channels"], rtol=1e-9,
+                                   atol=1e-12 * abs(single["channels"]).max())
+        s.free_raw(b)
+        s.free_raw(single)
+    other = collimated_spec(1000)
+    other.area_detector = 0.5
+    odd = Simulation(other, options=opts, gpu=g_sur)
+    with pytest.raises(RuntimeError, match="detector or collimator"):
+        odd.share_surrogate(sims[0])
+    for s in sims + [odd]:
+        s.close()

@@ -4,7 +4,7 @@ this package holds the build recipe, the ctypes mirror of the C-ABI and the
 Python host mirror of the reference's call chain."""
 from . import abi
 from .simulation import (ContinuousPoint, DiscreteLine, InputSpec, Layer, Simulation, XmiError, gpu_options,
-                         make_options)
+                         last_timing, make_options)
 
 __all__ = ["abi", "ContinuousPoint", "DiscreteLine", "InputSpec", "Layer", "Simulation", "XmiError",
-           "gpu_options", "make_options"]
+           "gpu_options", "last_timing", "make_options"]

@@ -157,6 +157,8 @@ PROTOTYPES = {
     "xmi_gpu_set_replica": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "xmi_gpu_build_surrogate": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, c_double_p]),
     "xmi_gpu_surrogate_report": (C.c_int, [C.c_void_p, c_double_p]),
+    "xmi_gpu_share_surrogate": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "xmi_gpu_last_transfers": (C.c_int, [C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]),
     "xmi_gpu_last_surrogate": (C.c_int, [c_double_p, C.POINTER(C.c_longlong)]),
     "xmi_mlp_nparam": (C.c_int, []),
     "xmi_gpu_mlp_forward": (C.c_int, [C.POINTER(C.c_float), C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_float)]),

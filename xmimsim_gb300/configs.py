@@ -81,3 +81,56 @@ def caso4(n_photons_line: int = 1000000) -> InputSpec:
     return InputSpec(layers=[layer], reference_layer=1, n_photons_line=n_photons_line,
                      n_interactions_trajectory=1, p_detector_window=(0.0, 10.0, 100.0),
                      discrete=[DiscreteLine(10.0, 1e12, 1e9)])
+
+
+def config5(n_configs: int = 512, seed: int = 5, budget_scale: float = 1.0) -> list[InputSpec]:
+    """The batched quantification sweep: n_configs independent samples in the
+    45/45 geometry of config 1 (detector 10 cm away, no collimator), 1-8
+    layers of 2-20 elements whose weight fractions vary by +-20% around the
+    config-1 sample (renormalised; extra elements drawn from Z 6-82 share
+    the rest), mixed excitation (1-5 discrete lines or 50-400 continuous
+    intervals of the Rh-tube spectrum), photon budgets log-uniform in
+    [1e6, 1e8] (times budget_scale), 4 interactions."""
+    rng = np.random.default_rng(seed)
+    base_Z = [14, 8, 26, 29, 30]
+    base_w = np.array([0.40, 0.50, 0.05, 0.03, 0.02])
+    out = []
+    for _ in range(n_configs):
+        n_layers = int(rng.integers(1, 9))
+        layers = []
+        for _ in range(n_layers):
+            n_el = int(rng.integers(2, 21))
+            k = min(n_el, len(base_Z))
+            Z = list(base_Z[:k])
+            w = list(base_w[:k] * rng.uniform(0.8, 1.2, size=k))
+            extra = [z for z in rng.permutation(np.arange(6, 83)).tolist() if z not in Z][:n_el - k]
+            Z += extra
+            w += list(rng.uniform(0.001, 0.02, size=len(extra)))
+            w = np.array(w) / np.sum(w)
+            order = np.argsort(Z)
+            layers.append(Layer([int(Z[i]) for i in order], [float(w[i]) for i in order],
+                                float(rng.uniform(1.0, 5.0)), float(np.exp(rng.uniform(np.log(1e-4), np.log(0.1))))))
+        budget = int(np.exp(rng.uniform(np.log(1e6), np.log(1e8))) * budget_scale)
+        if rng.uniform() < 0.5:
+            n_lines = int(rng.integers(1, 6))
+            energies = rng.uniform(8.0, 30.0, size=n_lines)
+            disc = [DiscreteLine(float(e), 1e9, 1e7) for e in energies]
+            spec = InputSpec(layers=layers, reference_layer=1, n_photons_line=max(1, budget // n_lines),
+                             n_interactions_trajectory=4, discrete=disc, continuous=[],
+                             p_detector_window=(0.0, 10.0, 100.0))
+        else:
+            n_int = int(rng.integers(50, 401))
+            cont, lines = tube.rh_tube_40kv(n_intervals=n_int)
+            spec = InputSpec(layers=layers, reference_layer=1,
+                             n_photons_interval=max(1, budget // (n_int + len(lines))),
+                             n_photons_line=max(1, budget // (n_int + len(lines))),
+                             n_interactions_trajectory=4, discrete=lines, continuous=cont,
+                             p_detector_window=(0.0, 10.0, 100.0))
+        spec.n_sample_orientation = (0.0, -math.sqrt(2.0) / 2.0, math.sqrt(2.0) / 2.0)
+        spec.n_detector_orientation = (0.0, -1.0, 0.0)
+        out.append(spec)
+    return out
+
+
+C5_OPTIONS = dict(use_variance_reduction=1, use_escape_peaks=0, use_sum_peaks=0, use_M_lines=1,
+                  use_cascade_auger=1, use_cascade_radiative=1, use_default_seeds=1)

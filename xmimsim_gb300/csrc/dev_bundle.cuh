@@ -45,7 +45,10 @@ struct DevBundle {
   const R *seg_lo, *seg_lnlo, *seg_invh;
   const int *seg_off, *seg_n;
   const R *el_tab, *mu_tab, *exc_tab;
-  const R *icdf_e, *icdf_r, *rayl_icdf, *compt_icdf, *phi_t, *phi_icdf, *dop_r, *dop_icdf, *ff2, *sf;
+  const R *icdf_e, *icdf_r, *phi_t, *phi_icdf, *dop_r;
+  /* per element: device copies of the tables that depend on Z alone, shared
+   * by every bundle on the device */
+  const R *const *rayl_icdf, *const *compt_icdf, *const *dop_icdf, *const *ff2, *const *sf;
   const xmi_source_item *items;
   const long long *item_first; /* [n_items] global id of the first photon */
   const double *sa_r, *sa_t;

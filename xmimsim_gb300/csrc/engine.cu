@@ -10,7 +10,9 @@
 #include <cstdlib>
 #include <cstring>
 #include <chrono>
+#include <map>
 #include <mutex>
+#include <tuple>
 #include <vector>
 
 #include "estimator.cuh"
@@ -29,6 +31,8 @@ struct Timing {
   /* phases of the last xmi_main_msim: transport, event sort, surrogate solid angles, estimator */
   double phase_ms[4] = {0.0, 0.0, 0.0, 0.0};
   long long events = 0, surrogate_fallbacks = 0;
+  /* host<->device bytes copied by the last xmi_main_msim / _batch call */
+  long long h2d_bytes = 0, d2h_bytes = 0;
 };
 thread_local Timing g_timing;
 
@@ -119,6 +123,47 @@ const R *upload(DevSide &s, const double *src, size_t n) {
   s.allocs.push_back(p);
   cudaMemcpy(p, tmp.data(), sizeof(R) * n, cudaMemcpyHostToDevice);
   return (const R *)p;
+}
+
+/* Device copies of the tables that depend on Z alone, made once per device
+ * and precision and shared by every bundle: keyed by the host table they
+ * copy, which the host keeps for the life of the process.  A batch of
+ * hundreds of configurations over the same elements then holds one copy of
+ * each element's angular tables instead of one per configuration. */
+std::mutex g_ztab_lock;
+std::map<std::tuple<int, int, const double *>, void *> g_ztab;
+
+template <typename R>
+const R *shared_table(const double *src, size_t n) {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::lock_guard<std::mutex> lk(g_ztab_lock);
+  const auto key = std::make_tuple(dev, (int)sizeof(R), src);
+  auto it = g_ztab.find(key);
+  if (it != g_ztab.end()) return (const R *)it->second;
+  std::vector<R> tmp(n);
+  for (size_t i = 0; i < n; i++) tmp[i] = (R)src[i];
+  void *p = nullptr;
+  if (cudaMalloc(&p, sizeof(R) * n) != cudaSuccess) return nullptr;
+  if (cudaMemcpy(p, tmp.data(), sizeof(R) * n, cudaMemcpyHostToDevice) != cudaSuccess) {
+    cudaFree(p);
+    return nullptr;
+  }
+  g_ztab[key] = p;
+  return (const R *)p;
+}
+
+/* per-element array of device pointers to the shared tables */
+template <typename R>
+const R *const *upload_per_element(DevSide &s, const double *const *src, int E, size_t n) {
+  std::vector<const R *> ptrs(E > 0 ? E : 1, nullptr);
+  for (int e = 0; e < E; e++)
+    if (!(ptrs[e] = shared_table<R>(src[e], n))) return nullptr;
+  void *p = nullptr;
+  if (cudaMalloc(&p, sizeof(const R *) * ptrs.size()) != cudaSuccess) return nullptr;
+  s.allocs.push_back(p);
+  cudaMemcpy(p, ptrs.data(), sizeof(const R *) * ptrs.size(), cudaMemcpyHostToDevice);
+  return (const R *const *)p;
 }
 
 const int *upload_int(DevSide &s, const int *src, size_t n) {
@@ -220,20 +265,21 @@ bool upload_tables(const xmi_bundle &h, DevSide &s, xmi::DevBundle<R> &d) {
   d.exc_tab = upload<R>(s, h.exc_tab, h.n_nodes);
   d.icdf_e = upload<R>(s, h.icdf_energies, XMI_ICDF_NE);
   d.icdf_r = upload<R>(s, h.icdf_rs, XMI_ICDF_NR);
-  d.rayl_icdf = upload<R>(s, h.rayl_icdf, E * XMI_ICDF_NE * XMI_ICDF_NR);
-  d.compt_icdf = upload<R>(s, h.compt_icdf, E * XMI_ICDF_NE * XMI_ICDF_NR);
+  d.rayl_icdf = upload_per_element<R>(s, h.rayl_icdf, (int)E, (size_t)XMI_ICDF_NE * XMI_ICDF_NR);
+  d.compt_icdf = upload_per_element<R>(s, h.compt_icdf, (int)E, (size_t)XMI_ICDF_NE * XMI_ICDF_NR);
   d.phi_t = upload<R>(s, h.phi_thetas, XMI_PHI_NT);
-  d.phi_icdf = upload<R>(s, h.phi_icdf, (size_t)XMI_PHI_NT * XMI_ICDF_NR);
+  d.phi_icdf = shared_table<R>(h.phi_icdf, (size_t)XMI_PHI_NT * XMI_ICDF_NR);
   d.dop_r = upload<R>(s, h.doppler_rs, XMI_DOPPLER_N);
-  d.dop_icdf = upload<R>(s, h.doppler_icdf, E * XMI_DOPPLER_N);
-  d.ff2 = upload<R>(s, h.ff2, E * XMI_NQ);
-  d.sf = upload<R>(s, h.sf, E * XMI_NQ);
+  d.dop_icdf = upload_per_element<R>(s, h.doppler_icdf, (int)E, XMI_DOPPLER_N);
+  d.ff2 = upload_per_element<R>(s, h.ff2, (int)E, XMI_NQ);
+  d.sf = upload_per_element<R>(s, h.sf, (int)E, XMI_NQ);
   d.ent_off = upload_int(s, h.ent_off, (size_t)h.n_layer_el + 1);
   d.ent_slot = upload_int(s, h.ent_slot, h.n_ent);
   d.ent_shell = upload_int(s, h.ent_shell, h.n_ent);
   d.ent_coef = upload<R>(s, h.ent_coef, h.n_ent);
   d.ent_pmu = upload<R>(s, h.ent_pmu, (size_t)h.n_ent * XMI_MAXL);
-  if (cudaGetLastError() != cudaSuccess || !d.sf || !d.ent_pmu) {
+  if (cudaGetLastError() != cudaSuccess || !d.rayl_icdf || !d.compt_icdf || !d.dop_icdf || !d.ff2 || !d.sf ||
+      !d.phi_icdf || !d.ent_pmu) {
     xmi_set_error("device table upload failed");
     s.release();
     return false;
@@ -346,6 +392,12 @@ int xmi_gpu_last_phases(double *transport_kernel_ms, double *sort_ms, double *es
   if (sort_ms) *sort_ms = g_timing.phase_ms[1];
   if (estimator_ms) *estimator_ms = g_timing.phase_ms[3];
   if (events) *events = g_timing.events;
+  return 1;
+}
+
+int xmi_gpu_last_transfers(long long *h2d_bytes, long long *d2h_bytes) {
+  if (h2d_bytes) *h2d_bytes = g_timing.h2d_bytes;
+  if (d2h_bytes) *d2h_bytes = g_timing.d2h_bytes;
   return 1;
 }
 
@@ -709,6 +761,7 @@ static bool stage_run(DevState *s, xmi::DevBundle<R> &d, const xmi_bundle &h, xm
   if (h.n_items > 0) {
     cudaMemcpyAsync(s->items, h.items, sizeof(xmi_source_item) * h.n_items, cudaMemcpyHostToDevice, s->stream);
     cudaMemcpyAsync(s->item_first, first.data(), sizeof(long long) * h.n_items, cudaMemcpyHostToDevice, s->stream);
+    g_timing.h2d_bytes += (long long)(sizeof(xmi_source_item) + sizeof(long long)) * h.n_items;
   }
   /* solid-angle grid (kept on the device while the caller's grid is the same) */
   if (h.sa_nr > 0 && (s->sa_src != h.sa_grid || s->sa_n != h.sa_nr * h.sa_nt)) {
@@ -731,6 +784,7 @@ static bool stage_run(DevState *s, xmi::DevBundle<R> &d, const xmi_bundle &h, xm
     cudaMemcpy(s->sa_t, h.sa_t, sizeof(double) * h.sa_nt, cudaMemcpyHostToDevice);
     cudaMemcpy(s->sa_g64, h.sa_grid, sizeof(double) * n, cudaMemcpyHostToDevice);
     cudaMemcpy(s->sa_g32, g32.data(), sizeof(float) * n, cudaMemcpyHostToDevice);
+    g_timing.h2d_bytes += (long long)(sizeof(double) * (h.sa_nr + h.sa_nt + n) + sizeof(float) * n);
     s->sa_src = h.sa_grid;
     s->sa_n = (int)n;
   }
@@ -798,6 +852,7 @@ static bool launch_single(DevState *s, xmi::DevBundle<R> &d, const xmi::DevTally
   if (!s->d_tally && !cuda_ok(cudaMalloc(&s->d_tally, sizeof(xmi::DevTally)), "cudaMalloc")) return false;
   cudaMemcpyAsync(s->d_bundle, &d, sizeof(d), cudaMemcpyHostToDevice, s->stream);
   cudaMemcpyAsync(s->d_tally, &tl, sizeof(tl), cudaMemcpyHostToDevice, s->stream);
+  g_timing.h2d_bytes += (long long)(sizeof(d) + sizeof(tl));
   const int stage_cap = stage_cap_for<R>(h.stage_max);
   size_t smem = 0;
   const int est_blocks = estimator_blocks<R>(stage_cap, &smem);
@@ -818,7 +873,7 @@ static bool launch_single(DevState *s, xmi::DevBundle<R> &d, const xmi::DevTally
   };
   auto surrogate = [&](const xmi::VrQueue<R> &vq) -> int {
     if (!d.use_surrogate) return 0;
-    xmi_surrogate_apply(sg, sizeof(R) == 8 ? 0 : 1, s->d_bundle, vq.ev, vq.count, vq.cap, &s->counters[4],
+    xmi_surrogate_apply(sg, sizeof(R) == 8 ? 0 : 1, s->d_bundle, 1, vq.ev, vq.count, vq.cap, &s->counters[4],
                         (int *)&s->counters[5], s->stream);
     return 1;
   };
@@ -836,6 +891,7 @@ static int collect_outputs(DevState *s, const xmi_bundle &h, int n_mpi_hosts, do
   unsigned long long counters[8];
   cudaMemcpyAsync(tally.data(), s->tally, sizeof(double) * tally.size(), cudaMemcpyDeviceToHost, s->stream);
   cudaMemcpyAsync(counters, s->counters, sizeof(counters), cudaMemcpyDeviceToHost, s->stream);
+  g_timing.d2h_bytes += (long long)(sizeof(double) * tally.size() + sizeof(counters));
   if (!cuda_ok(cudaStreamSynchronize(s->stream), "copy back")) return 0;
   if (counters[1] != 0) {
     xmi_set_error("transport kernel reported error code %llu", counters[1]);
@@ -895,6 +951,7 @@ extern "C" int xmi_main_msim(xmi_inputFPtr in, xmi_hdf5FPtr t, int n_mpi_hosts, 
   cudaEvent_t all0, all1;
   if (!ensure_device()) return 0;
   if (!xmi_gpu_prepare_run(in, t, options, n_mpi_hosts, sa)) return 0;
+  g_timing.h2d_bytes = g_timing.d2h_bytes = 0;
   const xmi_bundle &h = t->b;
   const int precision = in->gpu.precision;
   if (!xmi_dev_sync_tables(t, precision)) return 0;
@@ -954,7 +1011,7 @@ std::mutex g_batch_lock;
 
 template <typename R>
 bool launch_batch(int n, DevState **st, xmi_hdf5FPtr *t, const xmi::DevTally *tl, int threads, int blocks_per_sm,
-                  bool graph, Phases &ph) {
+                  const void *sg, bool graph, Phases &ph) {
   BatchState &B = g_batch;
   std::vector<xmi::DevBundle<R>> bundles(n);
   std::vector<long long> first(n + 1, 0);
@@ -983,11 +1040,12 @@ bool launch_batch(int n, DevState **st, xmi_hdf5FPtr *t, const xmi::DevTally *tl
     B.cap = n;
     B.bundles_bytes = sizeof(xmi::DevBundle<double>) * n;
   }
-  if (!B.flags && !cuda_ok(cudaMalloc(&B.flags, 2 * sizeof(unsigned long long)), "cudaMalloc")) return false;
+  if (!B.flags && !cuda_ok(cudaMalloc(&B.flags, 4 * sizeof(unsigned long long)), "cudaMalloc")) return false;
   cudaMemcpyAsync(B.bundles, bundles.data(), sizeof(xmi::DevBundle<R>) * n, cudaMemcpyHostToDevice, B.stream);
   cudaMemcpyAsync(B.tallies, tl, sizeof(xmi::DevTally) * n, cudaMemcpyHostToDevice, B.stream);
   cudaMemcpyAsync(B.cfg_first, first.data(), sizeof(long long) * (n + 1), cudaMemcpyHostToDevice, B.stream);
-  cudaMemsetAsync(B.flags, 0, 2 * sizeof(unsigned long long), B.stream);
+  g_timing.h2d_bytes += (long long)((sizeof(xmi::DevBundle<R>) + sizeof(xmi::DevTally)) * n + sizeof(long long) * (n + 1));
+  cudaMemsetAsync(B.flags, 0, 4 * sizeof(unsigned long long), B.stream);
   const xmi::DevBundle<R> *db = (const xmi::DevBundle<R> *)B.bundles;
   const int sms = num_sms();
   int stage_max = 1;
@@ -1009,18 +1067,30 @@ bool launch_batch(int n, DevState **st, xmi_hdf5FPtr *t, const xmi::DevTally *tl
     xmi::estimator_kernel<R><<<est_blocks, 256, smem, B.stream>>>(db, B.tallies, n, vq.ev, order, vq.count, vq.cap,
                                                                   work, stage_cap, B.flags);
   };
-  auto no_surrogate = [](const xmi::VrQueue<R> &) -> int { return 0; };
-  if (!run_chunks<R>(B.stream, B.q, first[n], N, n * XMI_MAXL * XMI_MAXN, vr, &B.flags[1], transport, no_surrogate,
-                     estimator, ph,
-                     graph))
+  /* flags: [0] estimator error, [1] events, [2] integrator fallbacks of the
+   * surrogate, [3] surrogate error */
+  auto surrogate = [&](const xmi::VrQueue<R> &vq) -> int {
+    if (!sg) return 0;
+    xmi_surrogate_apply(sg, sizeof(R) == 8 ? 0 : 1, db, n, vq.ev, vq.count, vq.cap, &B.flags[2],
+                        (int *)&B.flags[3], B.stream);
+    return 1;
+  };
+  if (!run_chunks<R>(B.stream, B.q, first[n], N, n * XMI_MAXL * XMI_MAXN, vr, &B.flags[1], transport, surrogate,
+                     estimator, ph, graph))
     return false;
-  unsigned long long flags[2];
+  unsigned long long flags[4];
   cudaMemcpy(flags, B.flags, sizeof(flags), cudaMemcpyDeviceToHost);
+  g_timing.d2h_bytes += (long long)sizeof(flags);
   if (flags[0] != 0) {
     xmi_set_error("estimator kernel reported error code %llu", flags[0]);
     return false;
   }
+  if (flags[3] != 0) {
+    xmi_set_error("surrogate solid-angle kernel reported error code %llu", flags[3]);
+    return false;
+  }
   g_timing.events = (long long)flags[1];
+  g_timing.surrogate_fallbacks = (long long)flags[2];
   return true;
 }
 }  // namespace
@@ -1038,6 +1108,8 @@ extern "C" int xmi_main_msim_batch(int n, xmi_inputFPtr *inputFPtrs, xmi_hdf5FPt
   std::vector<DevState *> st(n);
   std::vector<xmi::DevTally> tl(n);
   const auto wall0 = std::chrono::steady_clock::now();
+  g_timing.h2d_bytes = g_timing.d2h_bytes = 0;
+  const void *sg = nullptr;
   for (int c = 0; c < n; c++) {
     channels[c] = brute_histories[c] = var_red_histories[c] = nullptr;
     if (inputFPtrs[c]->gpu.precision != precision) {
@@ -1049,8 +1121,14 @@ extern "C" int xmi_main_msim_batch(int n, xmi_inputFPtr *inputFPtrs, xmi_hdf5FPt
     if (!xmi_dev_sync_tables(hdf5FPtrs[c], precision)) return 0;
     st[c] = state_of(hdf5FPtrs[c]);
     const xmi_bundle &h = hdf5FPtrs[c]->b;
-    bool ok = precision == 0 ? stage_run<double>(st[c], st[c]->b64, h, tl[c], false)
-                             : stage_run<float>(st[c], st[c]->b32, h, tl[c], false);
+    const bool use_sg = surrogate_in_use(inputFPtrs[c], options[c]);
+    if (use_sg && sg && inputFPtrs[c]->surrogate != sg) {
+      xmi_set_error("xmi_main_msim_batch: configuration %d uses another surrogate than the ones before it", c);
+      return 0;
+    }
+    if (use_sg) sg = inputFPtrs[c]->surrogate;
+    bool ok = precision == 0 ? stage_run<double>(st[c], st[c]->b64, h, tl[c], use_sg)
+                             : stage_run<float>(st[c], st[c]->b32, h, tl[c], use_sg);
     if (!ok) return 0;
   }
   for (int c = 0; c < n; c++)
@@ -1058,8 +1136,8 @@ extern "C" int xmi_main_msim_batch(int n, xmi_inputFPtr *inputFPtrs, xmi_hdf5FPt
   const int threads = inputFPtrs[0]->gpu.threads_per_block > 0 ? inputFPtrs[0]->gpu.threads_per_block : 128;
   const int bps = inputFPtrs[0]->gpu.blocks_per_sm > 0 ? inputFPtrs[0]->gpu.blocks_per_sm : 8;
   Phases ph;
-  bool ok = precision == 0 ? launch_batch<double>(n, st.data(), hdf5FPtrs, tl.data(), threads, bps, true, ph)
-                           : launch_batch<float>(n, st.data(), hdf5FPtrs, tl.data(), threads, bps, true, ph);
+  bool ok = precision == 0 ? launch_batch<double>(n, st.data(), hdf5FPtrs, tl.data(), threads, bps, sg, true, ph)
+                           : launch_batch<float>(n, st.data(), hdf5FPtrs, tl.data(), threads, bps, sg, true, ph);
   if (!ok) return 0;
   for (int c = 0; c < n; c++)
     if (!collect_outputs(st[c], hdf5FPtrs[c]->b, 1, &channels[c], &brute_histories[c], &var_red_histories[c],

@@ -115,7 +115,7 @@ __device__ void estimate_event(const DevBundle<R> &b, const DevTally &t, const S
     const R pconv = wi / ev.mu_here;
     const int rs = b.n_lines + 2 * e;
     /* Rayleigh */
-    const R twr = live * (pconv * (ev.pR * qtab(b.ff2 + (size_t)e * XMI_NQ, ev.q)) * ev.pesc_rayl * ev.w);
+    const R twr = live * (pconv * (ev.pR * qtab(b.ff2[e], ev.q)) * ev.pesc_rayl * ev.w);
     contribute<R, Uniform>(t, st, n_line + 2 * i, hbase + rs, twr);
     if (valid) chan_add(b, t, n, ev.E, twr);
     /* Compton: one Doppler-broadened energy per element (N_COMPTON_VARRED = 1) */
@@ -130,7 +130,7 @@ __device__ void estimate_event(const DevBundle<R> &b, const DevTally &t, const S
       R murhod = (R)0;
 #pragma unroll
       for (int j = 0; j < XMI_MAXL; j++) murhod += mus_c[j] * ev.rd[j];
-      twc = live * (pconv * (ev.pC * qtab(b.sf + (size_t)e * XMI_NQ, ev.q)) * exp(-murhod) * ev.w);
+      twc = live * (pconv * (ev.pC * qtab(b.sf[e], ev.q)) * exp(-murhod) * ev.w);
     } else if (valid) {
       ok = false;
     }
@@ -198,7 +198,7 @@ __device__ __forceinline__ void estimate_event_uniform(const DevBundle<R> &b, co
     const R pconv = wi / ev.mu_here;
     const int rs = b.n_lines + 2 * e;
     /* Rayleigh */
-    const R twr = live * (pconv * (ev.pR * qtab(b.ff2 + (size_t)e * XMI_NQ, ev.q)) * ev.pesc_rayl * ev.w);
+    const R twr = live * (pconv * (ev.pR * qtab(b.ff2[e], ev.q)) * ev.pesc_rayl * ev.w);
     contribute<R, true>(t, st, st.n_line + 2 * i, hbase + rs, twr);
     if (valid) chan_add(b, t, n, ev.E, twr);
     /* Compton: one Doppler-broadened energy per element (N_COMPTON_VARRED = 1) */
@@ -213,7 +213,7 @@ __device__ __forceinline__ void estimate_event_uniform(const DevBundle<R> &b, co
       R murhod = (R)0;
 #pragma unroll
       for (int j = 0; j < XMI_MAXL; j++) murhod += mus_c[j] * ev.rd[j];
-      twc = live * (pconv * (ev.pC * qtab(b.sf + (size_t)e * XMI_NQ, ev.q)) * exp(-murhod) * ev.w);
+      twc = live * (pconv * (ev.pC * qtab(b.sf[e], ev.q)) * exp(-murhod) * ev.w);
     } else if (valid) {
       ok = false;
     }

@@ -685,6 +685,22 @@ static void z_tables_fill(const int *Zs, int n, const double *energies, const do
   pthread_mutex_unlock(&z_cache_lock);
 }
 
+/* azimuth inverse CDFs of polarised scattering: independent of the element,
+ * computed once per process and shared like the tables above */
+static const double *phi_table(const double *thetas, const double *rs) {
+  static double *table = NULL;
+  int i;
+  pthread_mutex_lock(&z_cache_lock);
+  if (!table) {
+    double *t = (double *)malloc(sizeof(double) * XMI_PHI_NT * XMI_ICDF_NR);
+#pragma omp parallel for schedule(dynamic, 4)
+    for (i = 0; i < XMI_PHI_NT; i++) phi_icdf_row(thetas[i], rs, t + (size_t)i * XMI_ICDF_NR);
+    table = t;
+  }
+  pthread_mutex_unlock(&z_cache_lock);
+  return table;
+}
+
 void xmi_bundle_free(xmi_bundle *b) {
   free(b->layer_el); free(b->layer_w); free(b->elem_Z); free(b->elem_yield_corr);
   free(b->elem_fluor_yield); free(b->elem_ck); free(b->elem_edge); free(b->elem_line_off);
@@ -692,8 +708,9 @@ void xmi_bundle_free(xmi_bundle *b) {
   free(b->line_energy); free(b->line_rate); free(b->line_channel); free(b->precalc_mu);
   free(b->precalc_xrf); free(b->seg_lo); free(b->seg_lnlo); free(b->seg_invh); free(b->seg_off);
   free(b->seg_n); free(b->el_tab); free(b->mu_tab); free(b->exc_tab); free(b->icdf_energies);
-  free(b->icdf_rs); free(b->rayl_icdf); free(b->compt_icdf); free(b->phi_thetas); free(b->phi_icdf);
-  free(b->doppler_rs); free(b->doppler_icdf); free(b->ff2); free(b->sf); free(b->items);
+  free(b->icdf_rs); free((void *)b->rayl_icdf); free((void *)b->compt_icdf); free(b->phi_thetas);
+  free(b->doppler_rs); free((void *)b->doppler_icdf); free((void *)b->ff2); free((void *)b->sf);
+  free(b->items);
   free(b->ent_off); free(b->ent_slot); free(b->ent_shell); free(b->ent_coef); free(b->ent_pmu);
   memset(b, 0, sizeof(*b));
 }
@@ -1015,28 +1032,25 @@ int xmi_bundle_build(struct xmi_input_handle *in, struct xmi_tables_handle *t,
   b->icdf_rs = (double *)malloc(sizeof(double) * XMI_ICDF_NR);
   for (i = 0; i < XMI_ICDF_NE; i++) b->icdf_energies[i] = 0.1 + (200.0 - 0.1) * i / (XMI_ICDF_NE - 1.0);
   for (i = 0; i < XMI_ICDF_NR; i++) b->icdf_rs[i] = (double)i / (XMI_ICDF_NR - 1.0);
-  b->rayl_icdf = (double *)malloc(sizeof(double) * (size_t)b->n_elem * XMI_ICDF_NE * XMI_ICDF_NR);
-  b->compt_icdf = (double *)malloc(sizeof(double) * (size_t)b->n_elem * XMI_ICDF_NE * XMI_ICDF_NR);
   b->doppler_rs = (double *)malloc(sizeof(double) * XMI_DOPPLER_N);
   for (i = 0; i < XMI_DOPPLER_N; i++) b->doppler_rs[i] = (double)i / (XMI_DOPPLER_N - 1.0);
-  b->doppler_icdf = (double *)malloc(sizeof(double) * (size_t)b->n_elem * XMI_DOPPLER_N);
-  b->ff2 = (double *)malloc(sizeof(double) * (size_t)b->n_elem * XMI_NQ);
-  b->sf = (double *)malloc(sizeof(double) * (size_t)b->n_elem * XMI_NQ);
+  b->rayl_icdf = (const double **)malloc(sizeof(double *) * (size_t)(b->n_elem > 0 ? b->n_elem : 1));
+  b->compt_icdf = (const double **)malloc(sizeof(double *) * (size_t)(b->n_elem > 0 ? b->n_elem : 1));
+  b->doppler_icdf = (const double **)malloc(sizeof(double *) * (size_t)(b->n_elem > 0 ? b->n_elem : 1));
+  b->ff2 = (const double **)malloc(sizeof(double *) * (size_t)(b->n_elem > 0 ? b->n_elem : 1));
+  b->sf = (const double **)malloc(sizeof(double *) * (size_t)(b->n_elem > 0 ? b->n_elem : 1));
   z_tables_fill(b->elem_Z, b->n_elem, b->icdf_energies, b->icdf_rs, b->doppler_rs);
   for (e = 0; e < b->n_elem; e++) {
     const z_tables *zt = &z_cache[b->elem_Z[e]];
-    memcpy(b->rayl_icdf + (size_t)e * XMI_ICDF_NE * XMI_ICDF_NR, zt->rayl, sizeof(double) * XMI_ICDF_NE * XMI_ICDF_NR);
-    memcpy(b->compt_icdf + (size_t)e * XMI_ICDF_NE * XMI_ICDF_NR, zt->compt,
-           sizeof(double) * XMI_ICDF_NE * XMI_ICDF_NR);
-    memcpy(b->doppler_icdf + (size_t)e * XMI_DOPPLER_N, zt->dop, sizeof(double) * XMI_DOPPLER_N);
-    memcpy(b->ff2 + (size_t)e * XMI_NQ, zt->ff2, sizeof(double) * XMI_NQ);
-    memcpy(b->sf + (size_t)e * XMI_NQ, zt->sf, sizeof(double) * XMI_NQ);
+    b->rayl_icdf[e] = zt->rayl;
+    b->compt_icdf[e] = zt->compt;
+    b->doppler_icdf[e] = zt->dop;
+    b->ff2[e] = zt->ff2;
+    b->sf[e] = zt->sf;
   }
   b->phi_thetas = (double *)malloc(sizeof(double) * XMI_PHI_NT);
-  b->phi_icdf = (double *)malloc(sizeof(double) * XMI_PHI_NT * XMI_ICDF_NR);
   for (i = 0; i < XMI_PHI_NT; i++) b->phi_thetas[i] = 0.5 * i / (XMI_PHI_NT - 1.0);
-#pragma omp parallel for schedule(dynamic, 4)
-  for (i = 0; i < XMI_PHI_NT; i++) phi_icdf_row(b->phi_thetas[i], b->icdf_rs, b->phi_icdf + (size_t)i * XMI_ICDF_NR);
+  b->phi_icdf = phi_table(b->phi_thetas, b->icdf_rs);
   return 1;
 }
 

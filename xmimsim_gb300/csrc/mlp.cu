@@ -27,6 +27,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -248,9 +249,9 @@ __host__ __device__ __forceinline__ void features_of(const Domain &d, R r, R t, 
  * box, zero below the box's lowest theta (as the grid path). */
 template <typename R>
 __global__ void __launch_bounds__(128, 1) omega_kernel(const unsigned char *packed, const float *theta, Domain dom,
-                                                       const unsigned char *flags, const DevBundle<R> *bundle,
-                                                       VrEvent<R> *ev, const unsigned long long *count, long long cap,
-                                                       unsigned long long *fallbacks, int *err) {
+                                                       const unsigned char *flags, const DevBundle<R> *bundles,
+                                                       int n_cfg, VrEvent<R> *ev, const unsigned long long *count,
+                                                       long long cap, unsigned long long *fallbacks, int *err) {
   extern __shared__ __align__(1024) unsigned char sm[];
   FwdCtx c;
   fwd_setup(sm, packed, theta, c);
@@ -269,6 +270,15 @@ __global__ void __launch_bounds__(128, 1) omega_kernel(const unsigned char *pack
       break;
     }
     if (!valid) continue;
+    /* events of a batch carry their configuration; those of configurations
+     * served by the grid were already weighted in transport */
+    const int cfg = ev[i].cfg;
+    if (cfg < 0 || cfg >= n_cfg) {
+      atomicExch(err, 2);
+      continue;
+    }
+    const DevBundle<R> *bundle = bundles + cfg;
+    if (!bundle->use_surrogate) continue;
     R omega;
     if (!(t >= (R)dom.tmin)) {
       omega = (R)0;
@@ -748,6 +758,8 @@ bool train_loop(MlpTrainer &tr, int epochs, float lr, double *loss_per_epoch) {
 
 /* trained surrogate of one input's solid-angle grid */
 struct SurrogateState {
+  std::atomic<int> refs{1}; /* input handles sharing this network */
+  xmi::SaGeom geom;         /* detector and collimator it was trained for */
   xmi::mlp::Domain dom;
   std::vector<float> theta;
   float *theta_d = nullptr;
@@ -772,7 +784,7 @@ extern "C" {
 
 void xmi_surrogate_free(void *p) {
   SurrogateState *sg = (SurrogateState *)p;
-  if (!sg) return;
+  if (!sg || --sg->refs > 0) return;
   cudaFree(sg->theta_d);
   cudaFree(sg->packed_d);
   cudaFree(sg->flags_d);
@@ -802,6 +814,7 @@ int xmi_gpu_build_surrogate(xmi_inputFPtr in, int n_train, int hits_train, int e
   sg->dom.nct = 32;
   sg->dom.eps = 1e-10f;
   const xmi::SaGeom geom{in->det_radius, in->coll_radius, in->coll_height, in->coll_present};
+  sg->geom = geom;
   const int ncell = sg->dom.ncr * sg->dom.nct, n_check = 16 * ncell;
 
   /* training and checking points uniform over the sample volume: the slab
@@ -809,7 +822,7 @@ int xmi_gpu_build_surrogate(xmi_inputFPtr in, int n_train, int hits_train, int e
    * axis, mapped to the (r, theta) of the solid-angle grid */
   std::mt19937_64 rng(0x5EED0004ull);
   std::uniform_real_distribution<double> u01(0.0, 1.0);
-  std::vector<double> r_h(n_train + n_check), t_h(n_train + n_check);
+  std::vector<double> r_h(n_train + 2 * n_check), t_h(n_train + 2 * n_check);
   {
     const double kLateral = 2.0; /* cm */
     const double *nv = in->n_sample;
@@ -856,10 +869,18 @@ int xmi_gpu_build_surrogate(xmi_inputFPtr in, int n_train, int hits_train, int e
     sg->dom.t0 = tlo;
     sg->dom.t1 = std::max(thi, tlo + 1e-6f);
   }
+  /* every checking point is integrated twice with independent streams of
+   * hits_check / 2 samples: their mean is the reference value and their
+   * difference measures its own Monte Carlo noise */
+  for (int i = 0; i < n_check; i++) {
+    r_h[n_train + n_check + i] = r_h[n_train + i];
+    t_h[n_train + n_check + i] = t_h[n_train + i];
+  }
+  const int half_check = hits_check / 2 > 0 ? hits_check / 2 : 1;
   double *r_d = nullptr, *t_d = nullptr, *o_d = nullptr;
   float *feat_d = nullptr, *pred_d = nullptr;
   int *err_d = nullptr;
-  const int ntot = n_train + n_check;
+  const int ntot = n_train + 2 * n_check;
   bool ok = cudaMalloc(&r_d, sizeof(double) * ntot) == cudaSuccess &&
             cudaMalloc(&t_d, sizeof(double) * ntot) == cudaSuccess &&
             cudaMalloc(&o_d, sizeof(double) * ntot) == cudaSuccess &&
@@ -877,8 +898,12 @@ int xmi_gpu_build_surrogate(xmi_inputFPtr in, int n_train, int hits_train, int e
     const unsigned long long seed = in->gpu.seed ? in->gpu.seed : 0x5EED0001ull;
     /* training targets: FP32 integrator; checking values: FP64 integrator */
     xmi::solid_angle_points_kernel<float><<<sms * 8, 256>>>(geom, r_d, t_d, n_train, hits_train, seed, o_d);
-    xmi::solid_angle_points_kernel<double><<<sms * 8, 256>>>(geom, r_d + n_train, t_d + n_train, n_check, hits_check,
-                                                             seed ^ 0x9E3779B97F4A7C15ull, o_d + n_train);
+    xmi::solid_angle_points_kernel<double><<<sms * 8, 256>>>(geom, r_d + n_train, t_d + n_train, n_check,
+                                                             half_check, seed ^ 0x9E3779B97F4A7C15ull,
+                                                             o_d + n_train);
+    xmi::solid_angle_points_kernel<double><<<sms * 8, 256>>>(geom, r_d + n_train + n_check,
+                                                             t_d + n_train + n_check, n_check, half_check,
+                                                             seed ^ 0xC2B2AE3D27D4EB4Full, o_d + n_train + n_check);
     ok = cudaDeviceSynchronize() == cudaSuccess;
     if (ok) cudaMemcpy(o_h.data(), o_d, sizeof(double) * ntot, cudaMemcpyDeviceToHost);
   }
@@ -937,27 +962,40 @@ int xmi_gpu_build_surrogate(xmi_inputFPtr in, int n_train, int hits_train, int e
      * tolerance are served by the integrator */
     std::vector<float> pred(n_check);
     cudaMemcpy(pred.data(), pred_d, sizeof(float) * n_check, cudaMemcpyDeviceToHost);
-    /* per cell: largest relative error of its checking points; cells
-     * without checking points (outside the sample volume) are flagged */
-    std::vector<double> cell_max(ncell, -1.0), errs;
+    /* per cell: the RMS relative error of the network over its checking
+     * points, with the reference values' own noise variance (from the two
+     * independent integrations) subtracted; cells without checking points
+     * (outside the sample volume) and cells with a point whose reference is
+     * 0 but the network's is not are flagged */
+    std::vector<double> cell_e2(ncell, 0.0), cell_n2(ncell, 0.0), errs;
+    std::vector<int> cell_n(ncell, 0), cell_bad(ncell, 0);
     for (int i = 0; i < n_check; i++) {
       bool inside;
       int cell;
       float f[NIN];
       features_of(sg->dom, r_h[n_train + i], t_h[n_train + i], f, inside, cell);
       if (!inside) continue;
-      const double truth = o_h[n_train + i], net = std::max(0.0, std::exp((double)pred[i]) - sg->dom.eps);
-      const double e = truth > 0.0 ? std::fabs(net - truth) / truth : (net > 1e3 * sg->dom.eps ? 1.0 : 0.0);
-      errs.push_back(e);
-      cell_max[cell] = std::max(cell_max[cell], e);
+      const double a = o_h[n_train + i], b = o_h[n_train + n_check + i], truth = 0.5 * (a + b);
+      const double net = std::max(0.0, std::exp((double)pred[i]) - sg->dom.eps);
+      cell_n[cell]++;
+      if (truth > 0.0) {
+        const double e = (net - truth) / truth, nz = (a - b) / (2.0 * truth);
+        errs.push_back(std::fabs(e));
+        cell_e2[cell] += e * e;
+        cell_n2[cell] += nz * nz;
+      } else if (net > 1e3 * sg->dom.eps) {
+        cell_bad[cell] = 1;
+        errs.push_back(1.0);
+      }
     }
     if (errs.empty()) errs.push_back(1.0);
     std::vector<unsigned char> flags(ncell, 0);
     double worst_kept = 0.0;
     const double tol = in->gpu.surrogate_tolerance > 0 ? in->gpu.surrogate_tolerance : 1e-3;
     for (int c = 0; c < ncell; c++) {
-      flags[c] = (cell_max[c] < 0.0 || cell_max[c] > tol) ? 1 : 0;
-      if (!flags[c]) worst_kept = std::max(worst_kept, cell_max[c]);
+      const double err = cell_n[c] > 0 ? std::sqrt(std::max(0.0, (cell_e2[c] - cell_n2[c]) / cell_n[c])) : 1.0;
+      flags[c] = (cell_n[c] == 0 || cell_bad[c] || err > tol) ? 1 : 0;
+      if (!flags[c]) worst_kept = std::max(worst_kept, err);
     }
     std::vector<double> sorted = errs;
     std::nth_element(sorted.begin(), sorted.begin() + sorted.size() / 2, sorted.end());
@@ -996,7 +1034,30 @@ int xmi_gpu_build_surrogate(xmi_inputFPtr in, int n_train, int hits_train, int e
   return 1;
 }
 
-int xmi_surrogate_apply(const void *p, int precision, const void *dev_bundle, void *events,
+/* The solid angle at (r, theta) depends on the detector radius and the
+ * collimator alone, so a network trained for one input serves every input
+ * with the same detector; their points outside its checked box go to the
+ * integrator. */
+int xmi_gpu_share_surrogate(xmi_inputFPtr from, xmi_inputFPtr to) {
+  if (!from || !to || !from->surrogate || !to->initialized) {
+    xmi_set_error("xmi_gpu_share_surrogate: the source input has no trained surrogate");
+    return 0;
+  }
+  SurrogateState *sg = (SurrogateState *)from->surrogate;
+  const xmi::SaGeom g{to->det_radius, to->coll_radius, to->coll_height, to->coll_present};
+  if (g.det_radius != sg->geom.det_radius || g.coll_present != sg->geom.coll_present ||
+      (g.coll_present && (g.coll_radius != sg->geom.coll_radius || g.coll_height != sg->geom.coll_height))) {
+    xmi_set_error("xmi_gpu_share_surrogate: detector or collimator differ from the ones the network was trained for");
+    return 0;
+  }
+  if (to->surrogate == sg) return 1;
+  sg->refs++;
+  xmi_surrogate_free(to->surrogate);
+  to->surrogate = sg;
+  return 1;
+}
+
+int xmi_surrogate_apply(const void *p, int precision, const void *dev_bundles, int n_cfg, void *events,
                         const unsigned long long *count, long long cap, unsigned long long *fallbacks, int *err,
                         void *stream) {
   using namespace xmi::mlp;
@@ -1009,12 +1070,12 @@ int xmi_surrogate_apply(const void *p, int precision, const void *dev_bundle, vo
   if (precision == 0) {
     cudaFuncSetAttribute(omega_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, SM_TOTAL);
     omega_kernel<double><<<sms, 128, SM_TOTAL, st>>>(sg->packed_d, sg->theta_d, sg->dom, sg->flags_d,
-                                                      (const xmi::DevBundle<double> *)dev_bundle,
+                                                      (const xmi::DevBundle<double> *)dev_bundles, n_cfg,
                                                       (xmi::VrEvent<double> *)events, count, cap, fallbacks, err);
   } else {
     cudaFuncSetAttribute(omega_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, SM_TOTAL);
     omega_kernel<float><<<sms, 128, SM_TOTAL, st>>>(sg->packed_d, sg->theta_d, sg->dom, sg->flags_d,
-                                                     (const xmi::DevBundle<float> *)dev_bundle,
+                                                     (const xmi::DevBundle<float> *)dev_bundles, n_cfg,
                                                      (xmi::VrEvent<float> *)events, count, cap, fallbacks, err);
   }
   return cudaGetLastError() == cudaSuccess ? 1 : 0;

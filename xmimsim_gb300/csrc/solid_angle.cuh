@@ -6,8 +6,8 @@
  * Each cone sample i of a point draws its two uniforms from Philox block i
  * of the point's stream (seed, point, 0xF0000000), so the lanes of a warp
  * take samples i = lane, lane+32, ... independently and the hit count is
- * exactly that of the sequential oracle.  FP32 and FP64 variants use the
- * same draws.  The work is FP32/FP64 issue-bound (about 40 flops and 3-5
+ * exactly that of the sequential oracle.  The FP32 variant uses the same
+ * draws truncated to 24 bits.  The work is FP32/FP64 issue-bound (about 40 flops and 3-5
  * transcendental ops per sample, no memory traffic beyond the result).
  *
  * stream = 1 replaces the Philox draws by the OpenCL backend's own stream
@@ -90,6 +90,18 @@ __device__ __forceinline__ int sa_sample(const SaGeom &s, R cfca, R st, R ct, R 
   return sqrt(ix * ix + iy * iy + iz * iz) <= detr ? 1 : 0;
 }
 
+/* the two uniforms of a cone sample from one Philox block: in FP64 the
+ * 53-bit draws of the transport's generator; in FP32 the same draws
+ * truncated to 24 bits (the transport's FP32 rule), with no FP64 arithmetic */
+__device__ __forceinline__ void cone_draws(const xmi_u32x4 &o, double &u1, double &u2) {
+  u1 = ((double)(o.v[0] >> 5) * 67108864.0 + (double)(o.v[1] >> 6)) * (1.0 / 9007199254740992.0);
+  u2 = ((double)(o.v[2] >> 5) * 67108864.0 + (double)(o.v[3] >> 6)) * (1.0 / 9007199254740992.0);
+}
+__device__ __forceinline__ void cone_draws(const xmi_u32x4 &o, float &u1, float &u2) {
+  u1 = (float)(o.v[0] >> 8) * 0x1p-24f;
+  u2 = (float)(o.v[2] >> 8) * 0x1p-24f;
+}
+
 /* out[t*nr + r] = solid angle of grid point (r_vals[r], t_vals[t]) */
 template <typename R>
 __global__ void __launch_bounds__(256) solid_angle_grid_kernel(SaGeom s, const double *r_vals, int nr,
@@ -131,13 +143,8 @@ __global__ void __launch_bounds__(256) solid_angle_grid_kernel(SaGeom s, const d
         c.v[2] = (uint32_t)p;
         c.v[3] = (uint32_t)((unsigned long long)p >> 32);
         xmi_u32x4 o = xmi_philox4x32_10(c, (uint32_t)seed, (uint32_t)(seed >> 32));
-        double d1 = ((double)(o.v[0] >> 5) * 67108864.0 + (double)(o.v[1] >> 6)) * (1.0 / 9007199254740992.0);
-        double d2 = ((double)(o.v[2] >> 5) * 67108864.0 + (double)(o.v[3] >> 6)) * (1.0 / 9007199254740992.0);
-        R u1 = (R)d1, u2 = (R)d2;
-        if (sizeof(R) == 4) {
-          u1 = u1 < (R)1 ? u1 : (R)0x1.fffffep-1f;
-          u2 = u2 < (R)1 ? u2 : (R)0x1.fffffep-1f;
-        }
+        R u1, u2;
+        cone_draws(o, u1, u2);
         hits += sa_sample<R>(s, cfca, st, ct, py, pz, outside, u1, u2);
       }
     }
@@ -168,13 +175,8 @@ __global__ void __launch_bounds__(256) solid_angle_points_kernel(SaGeom s, const
         c.v[2] = (uint32_t)p;
         c.v[3] = (uint32_t)((unsigned long long)p >> 32);
         xmi_u32x4 o = xmi_philox4x32_10(c, (uint32_t)seed, (uint32_t)(seed >> 32));
-        double d1 = ((double)(o.v[0] >> 5) * 67108864.0 + (double)(o.v[1] >> 6)) * (1.0 / 9007199254740992.0);
-        double d2 = ((double)(o.v[2] >> 5) * 67108864.0 + (double)(o.v[3] >> 6)) * (1.0 / 9007199254740992.0);
-        R u1 = (R)d1, u2 = (R)d2;
-        if (sizeof(R) == 4) {
-          u1 = u1 < (R)1 ? u1 : (R)0x1.fffffep-1f;
-          u2 = u2 < (R)1 ? u2 : (R)0x1.fffffep-1f;
-        }
+        R u1, u2;
+        cone_draws(o, u1, u2);
         hits += sa_sample<R>(s, cfca, st, ct, py, pz, outside, u1, u2);
       }
     }

@@ -464,7 +464,7 @@ template <typename R>
 __device__ __forceinline__ R compton_energy(const DevBundle<R> &b, int e, R E, R theta_i, xmi_rng *g, bool varred,
                                            bool &ok) {
   const R c = (R)(double)1.2399e-6f, c0 = (R)(double)4.85e-12f, c1 = (R)(double)1.456e-2f;
-  const R *rn = b.dop_r, *icdf = b.dop_icdf + (size_t)e * XMI_DOPPLER_N;
+  const R *rn = b.dop_r, *icdf = b.dop_icdf[e];
   const R dr = __ldg(rn + 1) - __ldg(rn);
   R energy = E * (R)1000, c_lamb0 = c / energy, sth2 = sin(theta_i / (R)2);
   int it = 0;
@@ -668,7 +668,7 @@ __device__ bool rayleigh(const DevBundle<R> &b, Photon<R> &p, xmi_rng *g) {
   const int e = p.elem;
   const R rinv = (R)(XMI_ICDF_NR - 1), einv = (R)((XMI_ICDF_NE - 1) / (200.0 - 0.1));
   R r = uni<R>(g);
-  R theta_i = bilinear(b.rayl_icdf + (size_t)e * XMI_ICDF_NE * XMI_ICDF_NR, b.icdf_r, XMI_ICDF_NR, (R)0, rinv,
+  R theta_i = bilinear(b.rayl_icdf[e], b.icdf_r, XMI_ICDF_NR, (R)0, rinv,
                        b.icdf_e, XMI_ICDF_NE, (R)0.1, einv, r, p.E, ok);
   if (!ok) return false;
   R tt = sin(theta_i) * sin(theta_i);
@@ -692,7 +692,7 @@ __device__ bool compton(const DevBundle<R> &b, Photon<R> &p, xmi_rng *g) {
   const R rinv = (R)(XMI_ICDF_NR - 1), einv = (R)((XMI_ICDF_NE - 1) / (200.0 - 0.1));
   const R mec2 = (R)(9.10938188e-31 * 2.99792458e8 * 2.99792458e8 / 1.602176487e-19 / 1000.0);
   R r = uni<R>(g);
-  R theta_i = bilinear(b.compt_icdf + (size_t)e * XMI_ICDF_NE * XMI_ICDF_NR, b.icdf_r, XMI_ICDF_NR, (R)0, rinv,
+  R theta_i = bilinear(b.compt_icdf[e], b.icdf_r, XMI_ICDF_NR, (R)0, rinv,
                        b.icdf_e, XMI_ICDF_NE, (R)0.1, einv, r, p.E, ok);
   if (!ok) return false;
   R k0k = (R)1 + p.E * ((R)1 - cos(theta_i)) / mec2;

@@ -158,6 +158,25 @@ def _check(rv: int, what: str) -> None:
         raise XmiError(f"{what} failed: {abi.last_error()}")
 
 
+def last_timing() -> dict:
+    """Device and wall times, phases, surrogate counters and host<->device
+    bytes of the calling thread's last xmi_main_msim / xmi_main_msim_batch."""
+    lib = abi.load()
+    t, tot, n = C.c_double(), C.c_double(), C.c_int()
+    lib.xmi_gpu_last_timing(C.byref(t), C.byref(tot), C.byref(n))
+    out = {"kernel_ms": t.value, "total_ms": tot.value, "launches": n.value}
+    tr, so, es, ev = C.c_double(), C.c_double(), C.c_double(), C.c_longlong()
+    lib.xmi_gpu_last_phases(C.byref(tr), C.byref(so), C.byref(es), C.byref(ev))
+    out.update(transport_ms=tr.value, sort_ms=so.value, estimator_ms=es.value, events=ev.value)
+    sg, fb = C.c_double(), C.c_longlong()
+    lib.xmi_gpu_last_surrogate(C.byref(sg), C.byref(fb))
+    out.update(surrogate_ms=sg.value, surrogate_fallbacks=fb.value)
+    hd, dh = C.c_longlong(), C.c_longlong()
+    lib.xmi_gpu_last_transfers(C.byref(hd), C.byref(dh))
+    out.update(h2d_bytes=hd.value, d2h_bytes=dh.value)
+    return out
+
+
 class Simulation:
     """One simulation set-up: input handle + table bundle (no GPU work yet)."""
 
@@ -264,7 +283,8 @@ class Simulation:
         tabs = (C.c_void_p * n)(*[s.tables.value for s in sims])
         opts = (C.POINTER(abi.XmiMainOptions) * n)(*[C.pointer(s.options) for s in sims])
         sas = (C.POINTER(abi.XmiSolidAngle) * n)(
-            *[s.solid_angle() if s.options.use_variance_reduction else C.POINTER(abi.XmiSolidAngle)() for s in sims])
+            *[s.solid_angle() if s.options.use_variance_reduction and not s.surrogate_on()
+              else C.POINTER(abi.XmiSolidAngle)() for s in sims])
         ch = (abi.c_double_p * n)()
         br = (abi.c_double_p * n)()
         vr = (abi.c_double_p * n)()
@@ -288,22 +308,18 @@ class Simulation:
         keys = ("median_rel_err", "max_rel_err_kept", "flagged_fraction", "train_loss", "seconds", "cells")
         return dict(zip(keys, rep.tolist()))
 
+    def share_surrogate(self, other: "Simulation") -> None:
+        """Serves this configuration's solid angles from the network trained
+        for `other` (same detector and collimator; xmi_gpu_share_surrogate)."""
+        _check(self.lib.xmi_gpu_share_surrogate(other.inputF, self.inputF), "xmi_gpu_share_surrogate")
+
     def free_raw(self, out: dict) -> None:
         for p in out.pop("raw", ()):
             if p:
                 self.lib.xmi_free(C.cast(p, C.c_void_p))
 
     def timing(self) -> dict:
-        t, tot, n = C.c_double(), C.c_double(), C.c_int()
-        self.lib.xmi_gpu_last_timing(C.byref(t), C.byref(tot), C.byref(n))
-        out = {"kernel_ms": t.value, "total_ms": tot.value, "launches": n.value}
-        tr, so, es, ev = C.c_double(), C.c_double(), C.c_double(), C.c_longlong()
-        self.lib.xmi_gpu_last_phases(C.byref(tr), C.byref(so), C.byref(es), C.byref(ev))
-        out.update(transport_ms=tr.value, sort_ms=so.value, estimator_ms=es.value, events=ev.value)
-        sg, fb = C.c_double(), C.c_longlong()
-        self.lib.xmi_gpu_last_surrogate(C.byref(sg), C.byref(fb))
-        out.update(surrogate_ms=sg.value, surrogate_fallbacks=fb.value)
-        return out
+        return last_timing()
 
     # -- detector response -------------------------------------------------
     def escape_ratios(self, n_photons: int | None = None, n_input_energies: int | None = None):
