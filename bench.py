@@ -70,6 +70,7 @@ def parse():
     p.add_argument("--epochs", type=int, default=8)
     p.add_argument("--tolerance", type=float, default=1e-3, help="surrogate held-out error limit")
     p.add_argument("--plain-grids", type=int, default=4, help="grids timed for the plain comparison")
+    p.add_argument("--tune-share", type=float, default=1.0 / 16, help="share of a step the autotuner's trials run")
     p.add_argument("--line-configs", type=int, default=3, help="configurations of the FP64 line-error check")
     p.add_argument("--no-plain", action="store_true")
     p.add_argument("--photons", type=float, default=1e7, help="photons per step of the plain workload")
@@ -334,6 +335,10 @@ def batched_arm(args, ws, rank, local):
     for i, s in enumerate(sims):
         if i != deep:
             s.share_surrogate(sims[deep])
+    # launch shape and queue size of the batched call
+    t0 = time.perf_counter()
+    tune = Simulation.autotune_batch(sims, share=args.tune_share)
+    tune["wall_s"] = time.perf_counter() - t0
 
     last = {}
 
@@ -354,7 +359,7 @@ def batched_arm(args, ws, rank, local):
     extra = {"photons_per_step": n_hist, "photons_full_job": full_hist,
              "elements_per_config_mean": statistics.mean(sum(len(l.Z) for l in s.layers) for s in specs),
              "l2": "inputs larger than L2 (tables of 512 configurations, several GB)",
-             "host_tables_s": host_tables_s,
+             "host_tables_s": host_tables_s, "autotuned": tune,
              "surrogate": dict(rep, n_train=args.n_train, epochs=args.epochs, tolerance=args.tolerance,
                                wall_s=train_s)}
     line = {"metric": METRIC, "value": value, "unit": "histories/s", "n_gpus": ws, "steps": args.steps,
@@ -374,43 +379,16 @@ def batched_arm(args, ws, rank, local):
     sb_full_s = train_s + steps_full * wall / args.steps
 
     if not args.no_plain:
-        # the plain GPU method one by one: a grid per configuration, then its transport
-        g_plain = gpu_options(precision=1, seed=seed)
-        grid_s = []
-        for i in np.linspace(0, len(sims) - 1, args.plain_grids).astype(int):
-            ps = Simulation(specs[i], options=options, gpu=g_plain)
-            t0 = time.perf_counter()
-            ps.solid_angle()
-            grid_s.append(time.perf_counter() - t0)
-            ps.close()
-        # transport of all configurations one by one, each on a grid (the
-        # deepest sample's, whose axes span every other's) -- timed
-        gd = sims[deep]
-        gd.set_gpu(g_plain)
-        ax = gd.solid_angle_grid()
-        for s in sims:
-            s.set_gpu(g_plain)
-            s.set_solid_angle(ax["r"], ax["theta"], ax["grid"])
-        load_cudart().cudaDeviceSynchronize()
-        t0 = time.perf_counter()
-        dev_ms = 0.0
-        for s in sims:
-            o = s.msim()
-            dev_ms += s.timing()["kernel_ms"]
-            s.free_raw(o)
-        one_by_one_s = time.perf_counter() - t0
-        plain_full_s = len(sims) * statistics.mean(grid_s) + steps_full * one_by_one_s
-        line["plain"] = {
-            "method": "one xmi_solid_angle_calculation grid + one xmi_main_msim per configuration, FP32",
-            "value": n_hist / one_by_one_s, "unit": "histories/s",
-            "note": "value: one-by-one transport of one step's budgets (wall, grids excluded)",
-            "device_value": n_hist / (dev_ms / 1e3),
-            "grid_s_per_config": statistics.mean(grid_s), "grids_timed": len(grid_s),
-            "full_job_s": plain_full_s, "full_job_histories_per_s": full_hist / plain_full_s}
-        line["surrogate_batched_full_job"] = {"full_job_s": sb_full_s,
-                                              "full_job_histories_per_s": full_hist / sb_full_s,
-                                              "includes": "network training + 16 batched steps (wall)"}
-        line["speedup_full_job_vs_plain"] = plain_full_s / sb_full_s
+        sb = {"full_job_s": sb_full_s, "full_job_histories_per_s": full_hist / sb_full_s,
+              "includes": "network training + autotuning + %d batched steps (wall)" % round(steps_full)}
+        line["surrogate_batched_full_job"] = sb
+        line["plain"] = {}
+        for prec, name in ((0, "fp64"), (1, "fp32")):
+            line["plain"][name] = one_by_one(args, sims, specs, options, deep, seed, prec, tune, n_hist,
+                                             full_hist, steps_full)
+        # the plain GPU method: all-FP64 transport and grid, one configuration per call
+        line["speedup_full_job_vs_plain"] = line["plain"]["fp64"]["full_job_s"] / sb_full_s
+        line["speedup_full_job_vs_fp32_one_by_one"] = line["plain"]["fp32"]["full_job_s"] / sb_full_s
         for s in sims:
             s.set_gpu(g_sur)
 
@@ -433,6 +411,56 @@ def batched_arm(args, ws, rank, local):
         for s, o in zip(sims, last["outs"]):
             s.free_raw(o)
     return line, sims, specs, options
+
+
+def one_by_one(args, sims, specs, options, deep, seed, prec, tune, n_hist, full_hist, steps_full):
+    """The configurations one by one, each with its own solid-angle grid and
+    one xmi_main_msim call, in the given precision.  Grids are timed on
+    `--plain-grids` configurations; the transport on every configuration
+    (FP32) or every k-th one (FP64, scaled by photons), after an untimed pass
+    over 1/1000 of the photons that puts tables and grids on the device.  The
+    transport runs on the deepest sample's grid (axes spanning every other's)."""
+    import numpy as np
+    from xmimsim_gb300 import Simulation, gpu_options
+    g = gpu_options(precision=prec, seed=seed, threads_per_block=tune["threads_per_block"],
+                    blocks_per_sm=tune["blocks_per_sm"])
+    g.queue_events = tune["queue_events"]
+    grid_s = []
+    for i in np.linspace(0, len(sims) - 1, args.plain_grids).astype(int):
+        ps = Simulation(specs[i], options=options, gpu=g)
+        t0 = time.perf_counter()
+        ps.solid_angle()
+        grid_s.append(time.perf_counter() - t0)
+        ps.close()
+    gd = Simulation(specs[deep], options=options, gpu=g)
+    ax = gd.solid_angle_grid()
+    gd.close()
+    k = 1 if prec == 1 else max(1, len(sims) // 128)
+    sub = sims[::k]
+    for s in sub:
+        s.set_gpu(g)
+        s.set_solid_angle(ax["r"], ax["theta"], ax["grid"])
+        s.set_replica(0, 1000)
+        s.free_raw(s.msim())
+        s.set_replica(0, 1)
+    load_cudart().cudaDeviceSynchronize()
+    t0 = time.perf_counter()
+    dev_ms = 0.0
+    for s in sub:
+        o = s.msim()
+        dev_ms += s.timing()["kernel_ms"]
+        s.free_raw(o)
+    wall = time.perf_counter() - t0
+    n_sub = sum(histories(specs[i]) for i in range(0, len(sims), k))
+    step_s = wall * n_hist / n_sub
+    full_s = len(sims) * statistics.mean(grid_s) + steps_full * step_s
+    return {"method": "one xmi_solid_angle_calculation grid + one xmi_main_msim per configuration, %s"
+                      % ("all FP64" if prec == 0 else "FP32 transport, FP64 tallies"),
+            "value": n_sub / wall, "unit": "histories/s", "device_value": n_sub / (dev_ms / 1e3),
+            "note": "value: one-by-one transport (wall, grids excluded) over %d of %d configurations"
+                    % (len(sub), len(sims)),
+            "grid_s_per_config": statistics.mean(grid_s), "grids_timed": len(grid_s),
+            "full_job_s": full_s, "full_job_histories_per_s": full_hist / full_s}
 
 
 def plain_arm(args, ws, rank, local):

@@ -59,6 +59,7 @@ enum { XMI_NO_INTERACTION = 0, XMI_RAYLEIGH = 1, XMI_COMPTON = 2,
        XMI_PHOTOELECTRIC = 3 };
 
 /* theta ICDF grids (reference src/xmi_data.c:148-151) */
+#define XMI_SEG_LUT 4096
 #define XMI_ICDF_NE 400
 #define XMI_ICDF_NR 2000
 #define XMI_PHI_NT 200
@@ -145,6 +146,11 @@ typedef struct {
   double *seg_invh;     /* [n_seg] 1/log-step */
   int *seg_off;         /* [n_seg] first node */
   int *seg_n;           /* [n_seg] nodes in segment (>= 2) */
+  /* segment search table: bin i of XMI_SEG_LUT uniform bins in log E over
+   * [seg_lo[0], seg_lo[n_seg]] holds the segment of its lower edge, so the
+   * segment of an energy is found from its bin with a step or two */
+  int *seg_lut;         /* [XMI_SEG_LUT] */
+  double seg_lut_ln0, seg_lut_inv;
   int n_nodes;
   double *el_tab;       /* [n_elem][n_nodes][XMI_EL_REC] */
   double *mu_tab;       /* [n_nodes][XMI_MAXL] layer mu (xmi_mu_calc) */

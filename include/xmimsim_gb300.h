@@ -43,6 +43,7 @@ typedef struct {
   int solid_angle_stream;   /* 0: Philox grid draws; 1: the OpenCL backend's Threefry
                                stream (src/xmi_kernels.cl:226-227), for point-by-point
                                comparison with that kernel */
+  long long queue_events;   /* estimator events per chunk (device queue size); 0: default 2^25 */
 } xmi_gpu_options;
 
 /* ---- data model helpers (reference src/xmi_data_structs.c) ---- */
@@ -134,6 +135,17 @@ int xmi_detector_convolute_spectrum_noalloc(xmi_inputFPtr inputFPtr, const doubl
 int xmi_main_msim_batch(int n, xmi_inputFPtr *inputFPtrs, xmi_hdf5FPtr *hdf5FPtrs, xmi_main_options **options,
                         xmi_solid_angle **solid_angles, double **channels, double **brute_histories,
                         double **var_red_histories);
+
+/* Autotuner of the batched call (no counterpart in the reference): times
+ * xmi_main_msim_batch on `share` of every configuration's photons (the
+ * first 1/R of each source item, R = round(1 / share)) for the candidate
+ * launch shapes of the wavefront kernels -- threads per block 64/128/256 x
+ * blocks per SM 4/8/16 -- and then the estimator queue sizes 2^23/2^24/2^25
+ * events, keeps the fastest by device time and writes it into every
+ * configuration's xmi_gpu_options.  report[4]: threads per block, blocks
+ * per SM, queue events, device ms of the best trial. */
+int xmi_gpu_autotune_batch(int n, xmi_inputFPtr *inputFPtrs, xmi_hdf5FPtr *hdf5FPtrs, xmi_main_options **options,
+                           xmi_solid_angle **solid_angles, double share, double *report);
 
 /* ---- solid-angle surrogate network (no counterpart in the reference) ----
  * A 3 -> 4 x 128 (SiLU) -> 1 network, BF16 weights and FP32 accumulation on

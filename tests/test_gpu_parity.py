@@ -293,3 +293,23 @@ def test_transport_fp32_tracks_fp64_production_stack():
     np.testing.assert_allclose(v32.ravel()[top], v64.ravel()[top], rtol=1e-2)
     s64.close()
     s32.close()
+
+
+def test_autotuned_batch_keeps_results():
+    """xmi_gpu_autotune_batch picks a launch shape and queue size from its
+    candidates, writes them into every configuration, and the batched run with
+    them gives the untuned run's result (photon streams are keyed by photon,
+    not by launch shape; only the order of FP64 additions differs)."""
+    specs = [configs.config1(n_photons_line=3000), mixed_source_spec()]
+    sims = [Simulation(sp, options=configs.C1_OPTIONS, gpu=gpu_options(seed=SEED)) for sp in specs]
+    before = Simulation.msim_batch(sims)
+    tune = Simulation.autotune_batch(sims, share=0.5)
+    assert tune["threads_per_block"] in (64, 128) and tune["blocks_per_sm"] in (4, 8, 12, 16, 24)
+    assert tune["queue_events"] in (1 << 23, 1 << 24, 1 << 25) and tune["best_trial_ms"] > 0
+    after = Simulation.msim_batch(sims)
+    for s, a, b in zip(sims, before, after):
+        assert s.gpu.blocks_per_sm == tune["blocks_per_sm"]
+        np.testing.assert_allclose(b["var_red"], a["var_red"], rtol=1e-9, atol=1e-12 * abs(a["var_red"]).max())
+        s.free_raw(a)
+        s.free_raw(b)
+        s.close()

@@ -106,7 +106,7 @@ class XmiEscapeRatiosOptions(C.Structure):
 class XmiGpuOptions(C.Structure):
     _fields_ = [("precision", C.c_int), ("use_surrogate", C.c_int), ("surrogate_tolerance", C.c_double),
                 ("threads_per_block", C.c_int), ("blocks_per_sm", C.c_int), ("seed", C.c_ulonglong),
-                ("solid_angle_stream", C.c_int)]
+                ("solid_angle_stream", C.c_int), ("queue_events", C.c_longlong)]
 
 
 # exported symbols and their prototypes (name -> (restype, argtypes))
@@ -158,6 +158,9 @@ PROTOTYPES = {
     "xmi_gpu_build_surrogate": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, c_double_p]),
     "xmi_gpu_surrogate_report": (C.c_int, [C.c_void_p, c_double_p]),
     "xmi_gpu_share_surrogate": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "xmi_gpu_autotune_batch": (C.c_int, [C.c_int, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p),
+                                         C.POINTER(C.POINTER(XmiMainOptions)), C.POINTER(C.POINTER(XmiSolidAngle)),
+                                         C.c_double, c_double_p]),
     "xmi_gpu_last_transfers": (C.c_int, [C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]),
     "xmi_gpu_last_surrogate": (C.c_int, [c_double_p, C.POINTER(C.c_longlong)]),
     "xmi_mlp_nparam": (C.c_int, []),

@@ -43,7 +43,8 @@ struct DevBundle {
   const R *line_energy, *line_rate;
   const R *precalc_mu, *precalc_xrf;
   const R *seg_lo, *seg_lnlo, *seg_invh;
-  const int *seg_off, *seg_n;
+  const int *seg_off, *seg_n, *seg_lut;
+  R seg_lut_ln0, seg_lut_inv;
   const R *el_tab, *mu_tab, *exc_tab;
   const R *icdf_e, *icdf_r, *phi_t, *phi_icdf, *dop_r;
   /* per element: device copies of the tables that depend on Z alone, shared

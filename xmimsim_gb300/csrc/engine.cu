@@ -107,11 +107,42 @@ struct DevState {
   unsigned long long *counters = nullptr;
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-  EventQueue q; /* estimator event queue of one chunk */
-  WfBuffers wf; /* wavefront transport state of one chunk */
   void *d_bundle = nullptr;      /* device copy of the run's DevBundle (estimator argument) */
   xmi::DevTally *d_tally = nullptr;
 };
+
+/* Event queue and wavefront state of a run (several GB at the default
+ * queue size).  Runs borrow them from a per-device pool instead of owning
+ * them per handle, so hundreds of handles run one after another in the
+ * memory of one run; concurrent runs on different host threads each take
+ * their own set. */
+struct RunBuffers {
+  int device = 0;
+  EventQueue q;
+  WfBuffers wf;
+};
+std::mutex g_pool_lock;
+std::vector<RunBuffers *> g_pool;
+
+RunBuffers *acquire_buffers() {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::lock_guard<std::mutex> lk(g_pool_lock);
+  for (size_t i = 0; i < g_pool.size(); i++)
+    if (g_pool[i]->device == dev) {
+      RunBuffers *rb = g_pool[i];
+      g_pool.erase(g_pool.begin() + (long)i);
+      return rb;
+    }
+  RunBuffers *rb = new RunBuffers();
+  rb->device = dev;
+  return rb;
+}
+
+void release_buffers(RunBuffers *rb) {
+  std::lock_guard<std::mutex> lk(g_pool_lock);
+  g_pool.push_back(rb);
+}
 
 template <typename R>
 const R *upload(DevSide &s, const double *src, size_t n) {
@@ -258,6 +289,9 @@ bool upload_tables(const xmi_bundle &h, DevSide &s, xmi::DevBundle<R> &d) {
   d.seg_lo = upload<R>(s, h.seg_lo, h.n_seg + 1);
   d.seg_lnlo = upload<R>(s, h.seg_lnlo, h.n_seg);
   d.seg_invh = upload<R>(s, h.seg_invh, h.n_seg);
+  d.seg_lut = upload_int(s, h.seg_lut, XMI_SEG_LUT);
+  d.seg_lut_ln0 = (R)h.seg_lut_ln0;
+  d.seg_lut_inv = (R)h.seg_lut_inv;
   d.seg_off = upload_int(s, h.seg_off, h.n_seg);
   d.seg_n = upload_int(s, h.seg_n, h.n_seg);
   d.el_tab = upload<R>(s, h.el_tab, E * h.n_nodes * XMI_EL_REC);
@@ -353,8 +387,6 @@ void xmi_dev_free_tables(struct xmi_tables_handle *t) {
   cudaFree(s->sa_g32);
   cudaFree(s->tally);
   cudaFree(s->counters);
-  s->q.release();
-  s->wf.release();
   cudaFree(s->d_bundle);
   cudaFree(s->d_tally);
   if (s->ev0) cudaEventDestroy(s->ev0);
@@ -567,6 +599,9 @@ static bool surrogate_in_use(xmi_inputFPtr in, const xmi_main_options *options) 
 /* events held on the device per chunk; a chunk is as many photons as can
  * each make N estimator events (one per interaction) within it */
 constexpr long long kMaxQueuedEvents = 1ll << 25;
+static long long queue_events_of(const xmi_gpu_options &g) {
+  return g.queue_events >= (1ll << 16) && g.queue_events <= (1ll << 27) ? g.queue_events : kMaxQueuedEvents;
+}
 /* photons per chunk without variance reduction (wavefront state ~170 B each) */
 constexpr long long kMaxChunkPhotons = 1ll << 23;
 
@@ -658,7 +693,7 @@ struct Phases {
  * the estimator launch.  CUDA events around each phase give the device times.
  * transport(w0, w1, vq) and estimator(vq, order) enqueue the two kernels. */
 template <typename R, typename TF, typename SF, typename EF>
-static bool run_chunks(cudaStream_t st, EventQueue &q, long long n, int N, int nkeys, bool vr,
+static bool run_chunks(cudaStream_t st, EventQueue &q, long long n, int N, int nkeys, bool vr, long long qev,
                        unsigned long long *total_events, TF &&transport, SF &&surrogate, EF &&estimator, Phases &ph,
                        bool graph = false) {
   const int sms = num_sms();
@@ -666,7 +701,7 @@ static bool run_chunks(cudaStream_t st, EventQueue &q, long long n, int N, int n
   if (chunk < 1) chunk = 1;
   xmi::VrQueue<R> vq{nullptr, nullptr, nullptr, 0};
   if (vr) {
-    chunk = kMaxQueuedEvents / (N > 0 ? N : 1);
+    chunk = qev / (N > 0 ? N : 1);
     if (chunk > n) chunk = n;
     if (chunk < 1) chunk = 1;
     if (!ensure_queue<R>(q, chunk * N, nkeys)) return false;
@@ -702,7 +737,7 @@ static bool run_chunks(cudaStream_t st, EventQueue &q, long long n, int N, int n
       /* positions of events whose key the sort would skip stay -1 and are refused by the estimator */
       cudaMemsetAsync(q.order, 0xff, sizeof(int) * (w1 - w0) * N, st);
       xmi::event_key_histogram<<<sms * 4, 256, 0, st>>>(q.key, q.count, vq.cap, nkeys, q.hist);
-      xmi::event_key_scan<<<1, 32, 0, st>>>(q.hist, nkeys, q.hist + nkeys, q.count, total_events);
+      xmi::event_key_scan<<<1, xmi::kScanThreads, 0, st>>>(q.hist, nkeys, q.hist + nkeys, q.count, total_events);
       xmi::event_key_scatter<<<sms * 4, 256, 0, st>>>(q.key, q.count, vq.cap, nkeys, q.hist + nkeys, q.order);
       cudaMemsetAsync(q.count + 1, 0, sizeof(unsigned long long), st);
       mark();
@@ -846,7 +881,7 @@ static int estimator_blocks(int stage_cap, size_t *smem) {
 /* one configuration on its handle's stream */
 template <typename R>
 static bool launch_single(DevState *s, xmi::DevBundle<R> &d, const xmi::DevTally &tl, const xmi_bundle &h,
-                          int threads, int blocks_per_sm, const void *sg, Phases &ph) {
+                          int threads, int blocks_per_sm, long long qev, const void *sg, Phases &ph) {
   const int sms = num_sms();
   if (!s->d_bundle && !cuda_ok(cudaMalloc(&s->d_bundle, sizeof(xmi::DevBundle<double>)), "cudaMalloc")) return false;
   if (!s->d_tally && !cuda_ok(cudaMalloc(&s->d_tally, sizeof(xmi::DevTally)), "cudaMalloc")) return false;
@@ -856,14 +891,24 @@ static bool launch_single(DevState *s, xmi::DevBundle<R> &d, const xmi::DevTally
   const int stage_cap = stage_cap_for<R>(h.stage_max);
   size_t smem = 0;
   const int est_blocks = estimator_blocks<R>(stage_cap, &smem);
-  const long long chunk_cap = h.use_vr ? kMaxQueuedEvents / (h.n_interactions > 0 ? h.n_interactions : 1)
-                                       : kMaxChunkPhotons;
-  if (!ensure_wf<R>(s->wf, h.n_photons_total < chunk_cap ? (h.n_photons_total > 0 ? h.n_photons_total : 1)
+  const long long chunk_cap = h.use_vr ? qev / (h.n_interactions > 0 ? h.n_interactions : 1) : kMaxChunkPhotons;
+  /* back to the pool once the run's stream is idle */
+  struct Borrow {
+    cudaStream_t st;
+    RunBuffers *rb = acquire_buffers();
+    ~Borrow() {
+      cudaStreamSynchronize(st);
+      release_buffers(rb);
+    }
+  } borrow{s->stream};
+  EventQueue &q = borrow.rb->q;
+  WfBuffers &wf = borrow.rb->wf;
+  if (!ensure_wf<R>(wf, h.n_photons_total < chunk_cap ? (h.n_photons_total > 0 ? h.n_photons_total : 1)
                                                            : chunk_cap))
     return false;
   const int rounds = wavefront_rounds(h);
   auto transport = [&](long long w0, long long w1, const xmi::VrQueue<R> &vq) {
-    return launch_wavefront<R, false>(s->stream, s->wf, d, tl, nullptr, nullptr, nullptr, 1, w0, w1, rounds, vq,
+    return launch_wavefront<R, false>(s->stream, wf, d, tl, nullptr, nullptr, nullptr, 1, w0, w1, rounds, vq,
                                       threads, sms * blocks_per_sm);
   };
   auto estimator = [&](const xmi::VrQueue<R> &vq, const int *order, unsigned long long *work) {
@@ -877,8 +922,8 @@ static bool launch_single(DevState *s, xmi::DevBundle<R> &d, const xmi::DevTally
                         (int *)&s->counters[5], s->stream);
     return 1;
   };
-  return run_chunks<R>(s->stream, s->q, h.n_photons_total, h.n_interactions, XMI_MAXL * XMI_MAXN, h.use_vr != 0,
-                       &s->counters[3], transport, surrogate, estimator, ph);
+  return run_chunks<R>(s->stream, q, h.n_photons_total, h.n_interactions, XMI_MAXL * XMI_MAXN, h.use_vr != 0,
+                       qev, &s->counters[3], transport, surrogate, estimator, ph);
 }
 
 /* device tallies -> the reference's output layouts (host) */
@@ -961,13 +1006,19 @@ extern "C" int xmi_main_msim(xmi_inputFPtr in, xmi_hdf5FPtr t, int n_mpi_hosts, 
   cudaEventRecord(all0, s->stream);
   xmi::DevTally tl;
   const int threads = in->gpu.threads_per_block > 0 ? in->gpu.threads_per_block : 128;
+  if (threads > 128 || threads % 32) {
+    xmi_set_error("threads_per_block must be a multiple of 32 up to 128 (got %d)", threads);
+    return 0;
+  }
   const int bps = in->gpu.blocks_per_sm > 0 ? in->gpu.blocks_per_sm : 8;
   Phases ph;
   const bool use_sg = surrogate_in_use(in, options);
   const void *sg = use_sg ? in->surrogate : nullptr;
   bool ok = precision == 0
-                ? stage_run<double>(s, s->b64, h, tl, use_sg) && launch_single<double>(s, s->b64, tl, h, threads, bps, sg, ph)
-                : stage_run<float>(s, s->b32, h, tl, use_sg) && launch_single<float>(s, s->b32, tl, h, threads, bps, sg, ph);
+                ? stage_run<double>(s, s->b64, h, tl, use_sg) &&
+                      launch_single<double>(s, s->b64, tl, h, threads, bps, queue_events_of(in->gpu), sg, ph)
+                : stage_run<float>(s, s->b32, h, tl, use_sg) &&
+                      launch_single<float>(s, s->b32, tl, h, threads, bps, queue_events_of(in->gpu), sg, ph);
   if (!ok) return 0;
   unsigned long long events = 0, fallbacks = 0;
   if (!collect_outputs(s, h, n_mpi_hosts, channels_out, brute_out, var_red_out, &events, &fallbacks)) return 0;
@@ -1011,7 +1062,7 @@ std::mutex g_batch_lock;
 
 template <typename R>
 bool launch_batch(int n, DevState **st, xmi_hdf5FPtr *t, const xmi::DevTally *tl, int threads, int blocks_per_sm,
-                  const void *sg, bool graph, Phases &ph) {
+                  long long qev, const void *sg, bool graph, Phases &ph) {
   BatchState &B = g_batch;
   std::vector<xmi::DevBundle<R>> bundles(n);
   std::vector<long long> first(n + 1, 0);
@@ -1055,7 +1106,7 @@ bool launch_batch(int n, DevState **st, xmi_hdf5FPtr *t, const xmi::DevTally *tl
   const int est_blocks = estimator_blocks<R>(stage_cap, &smem);
   int rounds = 1;
   for (int c = 0; c < n; c++) rounds = wavefront_rounds(t[c]->b) > rounds ? wavefront_rounds(t[c]->b) : rounds;
-  const long long chunk_cap = vr ? kMaxQueuedEvents / N : kMaxChunkPhotons;
+  const long long chunk_cap = vr ? qev / N : kMaxChunkPhotons;
   if (!ensure_wf<R>(B.wf, first[n] < chunk_cap ? (first[n] > 0 ? first[n] : 1) : chunk_cap)) return false;
   xmi::DevBundle<R> unused_b{};
   xmi::DevTally unused_t{};
@@ -1075,8 +1126,8 @@ bool launch_batch(int n, DevState **st, xmi_hdf5FPtr *t, const xmi::DevTally *tl
                         (int *)&B.flags[3], B.stream);
     return 1;
   };
-  if (!run_chunks<R>(B.stream, B.q, first[n], N, n * XMI_MAXL * XMI_MAXN, vr, &B.flags[1], transport, surrogate,
-                     estimator, ph, graph))
+  if (!run_chunks<R>(B.stream, B.q, first[n], N, n * XMI_MAXL * XMI_MAXN, vr, qev, &B.flags[1], transport,
+                     surrogate, estimator, ph, graph))
     return false;
   unsigned long long flags[4];
   cudaMemcpy(flags, B.flags, sizeof(flags), cudaMemcpyDeviceToHost);
@@ -1134,10 +1185,15 @@ extern "C" int xmi_main_msim_batch(int n, xmi_inputFPtr *inputFPtrs, xmi_hdf5FPt
   for (int c = 0; c < n; c++)
     if (!cuda_ok(cudaStreamSynchronize(st[c]->stream), "staging")) return 0;
   const int threads = inputFPtrs[0]->gpu.threads_per_block > 0 ? inputFPtrs[0]->gpu.threads_per_block : 128;
+  if (threads > 128 || threads % 32) {
+    xmi_set_error("threads_per_block must be a multiple of 32 up to 128 (got %d)", threads);
+    return 0;
+  }
   const int bps = inputFPtrs[0]->gpu.blocks_per_sm > 0 ? inputFPtrs[0]->gpu.blocks_per_sm : 8;
   Phases ph;
-  bool ok = precision == 0 ? launch_batch<double>(n, st.data(), hdf5FPtrs, tl.data(), threads, bps, sg, true, ph)
-                           : launch_batch<float>(n, st.data(), hdf5FPtrs, tl.data(), threads, bps, sg, true, ph);
+  const long long qev = queue_events_of(inputFPtrs[0]->gpu);
+  bool ok = precision == 0 ? launch_batch<double>(n, st.data(), hdf5FPtrs, tl.data(), threads, bps, qev, sg, true, ph)
+                           : launch_batch<float>(n, st.data(), hdf5FPtrs, tl.data(), threads, bps, qev, sg, true, ph);
   if (!ok) return 0;
   for (int c = 0; c < n; c++)
     if (!collect_outputs(st[c], hdf5FPtrs[c]->b, 1, &channels[c], &brute_histories[c], &var_red_histories[c],
@@ -1147,5 +1203,75 @@ extern "C" int xmi_main_msim_batch(int n, xmi_inputFPtr *inputFPtrs, xmi_hdf5FPt
   g_timing.total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - wall0).count();
   g_timing.launches = ph.launches;
   for (int k = 0; k < 4; k++) g_timing.phase_ms[k] = ph.ms[k];
+  return 1;
+}
+
+/* ---------------------------------------------------------------- */
+/* autotuner of the batched call                                     */
+/* ---------------------------------------------------------------- */
+extern "C" int xmi_gpu_autotune_batch(int n, xmi_inputFPtr *inputFPtrs, xmi_hdf5FPtr *hdf5FPtrs,
+                                      xmi_main_options **options, xmi_solid_angle **solid_angles, double share,
+                                      double *report) {
+  if (n < 1 || !inputFPtrs || !hdf5FPtrs || !options || !(share > 0.0 && share <= 1.0)) {
+    xmi_set_error("xmi_gpu_autotune_batch: invalid arguments");
+    return 0;
+  }
+  const int R = std::max(1, (int)std::lround(1.0 / share));
+  std::vector<int> rep0(n), nrep0(n);
+  for (int c = 0; c < n; c++) {
+    rep0[c] = hdf5FPtrs[c]->replica;
+    nrep0[c] = hdf5FPtrs[c]->n_replicas;
+    hdf5FPtrs[c]->replica = 0;
+    hdf5FPtrs[c]->n_replicas = R;
+  }
+  std::vector<double *> ch(n), br(n), vr(n);
+  auto trial = [&](int tpb, int bps, long long qev, double &ms) -> bool {
+    for (int c = 0; c < n; c++) {
+      inputFPtrs[c]->gpu.threads_per_block = tpb;
+      inputFPtrs[c]->gpu.blocks_per_sm = bps;
+      inputFPtrs[c]->gpu.queue_events = qev;
+    }
+    if (!xmi_main_msim_batch(n, inputFPtrs, hdf5FPtrs, options, solid_angles, ch.data(), br.data(), vr.data()))
+      return false;
+    ms = g_timing.transport_ms;
+    for (int c = 0; c < n; c++) {
+      free(ch[c]);
+      free(br[c]);
+      free(vr[c]);
+    }
+    return true;
+  };
+  int best_tpb = 128, best_bps = 8;
+  long long best_qev = kMaxQueuedEvents;
+  double best_ms = 0.0, ms = 0.0;
+  bool ok = trial(best_tpb, best_bps, best_qev, best_ms); /* warm-up: buffers and tables */
+  ok = ok && trial(best_tpb, best_bps, best_qev, best_ms);
+  const int tpbs[] = {64, 128}, bpss[] = {4, 8, 12, 16, 24};
+  for (int tpb : tpbs)
+    for (int bps : bpss) {
+      if (!ok) break;
+      ok = trial(tpb, bps, best_qev, ms);
+      if (ok && ms < best_ms) best_ms = ms, best_tpb = tpb, best_bps = bps;
+    }
+  const long long qevs[] = {1ll << 23, 1ll << 24};
+  for (long long qev : qevs) {
+    if (!ok) break;
+    ok = trial(best_tpb, best_bps, qev, ms);
+    if (ok && ms < best_ms) best_ms = ms, best_qev = qev;
+  }
+  for (int c = 0; c < n; c++) {
+    hdf5FPtrs[c]->replica = rep0[c];
+    hdf5FPtrs[c]->n_replicas = nrep0[c];
+    inputFPtrs[c]->gpu.threads_per_block = best_tpb;
+    inputFPtrs[c]->gpu.blocks_per_sm = best_bps;
+    inputFPtrs[c]->gpu.queue_events = best_qev;
+  }
+  if (!ok) return 0;
+  if (report) {
+    report[0] = best_tpb;
+    report[1] = best_bps;
+    report[2] = (double)best_qev;
+    report[3] = best_ms;
+  }
   return 1;
 }

@@ -100,7 +100,7 @@ __device__ __forceinline__ void contribute(const DevTally &t, const StageRow<R> 
 }
 
 template <typename R, bool Uniform>
-__device__ void estimate_event(const DevBundle<R> &b, const DevTally &t, const StageRow<R> &st, const VrEvent<R> &ev,
+__device__ __forceinline__ void estimate_event(const DevBundle<R> &b, const DevTally &t, const StageRow<R> &st, const VrEvent<R> &ev,
                                bool valid, bool &ok) {
   const int layer = ev.layer, n = ev.n;
   const int nel = b.nel[layer], off = b.off[layer];
@@ -108,6 +108,7 @@ __device__ void estimate_event(const DevBundle<R> &b, const DevTally &t, const S
   const int k_first = XMI_LDG(b.ent_off, off, b.n_layer_el + 1, 15);
   const int n_line = XMI_LDG(b.ent_off, off + nel, b.n_layer_el + 1, 15) - k_first;
   const R live = valid ? (R)1 : (R)0;
+  R rayl_sum = (R)0; /* Rayleigh keeps the photon energy: one channel add per event */
   for (int i = 0; i < nel; i++) {
     const int pair = off + i;
     const int e = XMI_LDG(b.layer_el, pair, b.n_layer_el, 9);
@@ -117,7 +118,7 @@ __device__ void estimate_event(const DevBundle<R> &b, const DevTally &t, const S
     /* Rayleigh */
     const R twr = live * (pconv * (ev.pR * qtab(b.ff2[e], ev.q)) * ev.pesc_rayl * ev.w);
     contribute<R, Uniform>(t, st, n_line + 2 * i, hbase + rs, twr);
-    if (valid) chan_add(b, t, n, ev.E, twr);
+    rayl_sum += twr;
     /* Compton: one Doppler-broadened energy per element (N_COMPTON_VARRED = 1) */
     xmi_rng g;
     xmi_rng_init(&g, b.seed, (uint64_t)ev.id, vr_stream(n, i));
@@ -168,6 +169,7 @@ __device__ void estimate_event(const DevBundle<R> &b, const DevTally &t, const S
       contribute<R, Uniform>(t, st, k - k_first, hbase + sl, tw);
     }
   }
+  if (valid) chan_add(b, t, n, ev.E, rayl_sum);
 }
 
 /* per-warp scratch of the uniform path: the 32 events' path sums rho*d per
@@ -189,6 +191,7 @@ __device__ __forceinline__ void estimate_event_uniform(const DevBundle<R> &b, co
   const long long hbase = (long long)(n - 1) * b.n_slots;
   R *s_rd = scratch, *s_a = scratch + 32 * XMI_MAXL;
   const R live = valid ? (R)1 : (R)0;
+  R rayl_sum = (R)0; /* Rayleigh keeps the photon energy: one channel add per event */
 #pragma unroll
   for (int j = 0; j < XMI_MAXL; j++) s_rd[lane * XMI_MAXL + j] = ev.rd[j];
   for (int i = 0; i < nel; i++) {
@@ -200,7 +203,7 @@ __device__ __forceinline__ void estimate_event_uniform(const DevBundle<R> &b, co
     /* Rayleigh */
     const R twr = live * (pconv * (ev.pR * qtab(b.ff2[e], ev.q)) * ev.pesc_rayl * ev.w);
     contribute<R, true>(t, st, st.n_line + 2 * i, hbase + rs, twr);
-    if (valid) chan_add(b, t, n, ev.E, twr);
+    rayl_sum += twr;
     /* Compton: one Doppler-broadened energy per element (N_COMPTON_VARRED = 1) */
     xmi_rng g;
     xmi_rng_init(&g, b.seed, (uint64_t)ev.id, vr_stream(n, i));
@@ -258,6 +261,7 @@ __device__ __forceinline__ void estimate_event_uniform(const DevBundle<R> &b, co
     }
     __syncwarp();
   }
+  if (valid) chan_add(b, t, n, ev.E, rayl_sum);
 }
 
 /* number of events the queue holds: the count, capped at the capacity (a
@@ -291,7 +295,7 @@ constexpr int kEventsPerGrab = 256;
  * the counter `work`; stage rows of stage_cap values per warp sit in dynamic
  * shared memory. */
 template <typename R>
-__global__ void __launch_bounds__(256, 3) estimator_kernel(const DevBundle<R> *bundles, const DevTally *tallies,
+__global__ void __launch_bounds__(256, 2) estimator_kernel(const DevBundle<R> *bundles, const DevTally *tallies,
                                                            int n_cfg, const VrEvent<R> *events, const int *order,
                                                            const unsigned long long *count, long long cap,
                                                            unsigned long long *work, int stage_cap,
@@ -361,16 +365,31 @@ __global__ void event_key_histogram(const int *key, const unsigned long long *co
 
 /* exclusive scan of the key counts into the scatter cursors; also adds the
  * chunk's event count to the run total */
-__global__ void event_key_scan(const unsigned *hist, int nkeys, unsigned *cursor, const unsigned long long *count,
-                               unsigned long long *total) {
-  if (threadIdx.x == 0 && blockIdx.x == 0) {
-    unsigned acc = 0;
-    for (int i = 0; i < nkeys; i++) {
-      cursor[i] = acc;
-      acc += hist[i];
-    }
-    *total += *count;
+constexpr int kScanThreads = 1024;
+__global__ void __launch_bounds__(kScanThreads) event_key_scan(const unsigned *hist, int nkeys, unsigned *cursor,
+                                                               const unsigned long long *count,
+                                                               unsigned long long *total) {
+  /* one block: each thread scans a contiguous run of keys; the runs' sums
+   * are scanned across the block */
+  __shared__ unsigned part[kScanThreads];
+  const int per = (nkeys + kScanThreads - 1) / kScanThreads;
+  const int k0 = threadIdx.x * per, k1 = k0 + per < nkeys ? k0 + per : nkeys;
+  unsigned sum = 0;
+  for (int k = k0; k < k1; k++) sum += hist[k];
+  part[threadIdx.x] = sum;
+  __syncthreads();
+  for (int d = 1; d < kScanThreads; d <<= 1) {
+    const unsigned v = threadIdx.x >= d ? part[threadIdx.x - d] : 0u;
+    __syncthreads();
+    part[threadIdx.x] += v;
+    __syncthreads();
   }
+  unsigned acc = part[threadIdx.x] - sum;
+  for (int k = k0; k < k1; k++) {
+    cursor[k] = acc;
+    acc += hist[k];
+  }
+  if (threadIdx.x == 0) *total += *count;
 }
 
 __global__ void event_key_scatter(const int *key, const unsigned long long *count, long long cap, int nkeys,

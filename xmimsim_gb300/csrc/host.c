@@ -706,7 +706,7 @@ void xmi_bundle_free(xmi_bundle *b) {
   free(b->elem_fluor_yield); free(b->elem_ck); free(b->elem_edge); free(b->elem_line_off);
   free(b->elem_shell_off); free(b->line_index); free(b->line_elem); free(b->line_shell);
   free(b->line_energy); free(b->line_rate); free(b->line_channel); free(b->precalc_mu);
-  free(b->precalc_xrf); free(b->seg_lo); free(b->seg_lnlo); free(b->seg_invh); free(b->seg_off);
+  free(b->precalc_xrf); free(b->seg_lo); free(b->seg_lnlo); free(b->seg_invh); free(b->seg_lut); free(b->seg_off);
   free(b->seg_n); free(b->el_tab); free(b->mu_tab); free(b->exc_tab); free(b->icdf_energies);
   free(b->icdf_rs); free((void *)b->rayl_icdf); free((void *)b->compt_icdf); free(b->phi_thetas);
   free(b->doppler_rs); free((void *)b->doppler_icdf); free((void *)b->ff2); free((void *)b->sf);
@@ -917,6 +917,17 @@ int xmi_bundle_build(struct xmi_input_handle *in, struct xmi_tables_handle *t,
     b->n_nodes += n;
   }
   free(brk);
+  b->seg_lut = (int *)malloc(sizeof(int) * XMI_SEG_LUT);
+  b->seg_lut_ln0 = log(b->seg_lo[0]);
+  b->seg_lut_inv = XMI_SEG_LUT / (log(b->seg_lo[b->n_seg]) - b->seg_lut_ln0);
+  {
+    int lo = 0;
+    for (i = 0; i < XMI_SEG_LUT; i++) {
+      const double x = exp(b->seg_lut_ln0 + i / b->seg_lut_inv);
+      while (lo < b->n_seg - 1 && x >= b->seg_lo[lo + 1]) lo++;
+      b->seg_lut[i] = lo;
+    }
+  }
 
   /* per-node element records and layer mu */
   b->el_tab = (double *)calloc((size_t)b->n_elem * b->n_nodes * XMI_EL_REC, sizeof(double));

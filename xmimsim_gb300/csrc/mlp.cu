@@ -819,7 +819,9 @@ int xmi_gpu_build_surrogate(xmi_inputFPtr in, int n_train, int hits_train, int e
 
   /* training and checking points uniform over the sample volume: the slab
    * between the first and last layer planes, within kLateral of the beam
-   * axis, mapped to the (r, theta) of the solid-angle grid */
+   * axis (the z axis), mapped to the (r, theta) of the solid-angle grid.
+   * The layer plane at offset h along the sample normal n (x . n = h) meets
+   * the beam at (0, 0, h / n_z). */
   std::mt19937_64 rng(0x5EED0004ull);
   std::uniform_real_distribution<double> u01(0.0, 1.0);
   std::vector<double> r_h(n_train + 2 * n_check), t_h(n_train + 2 * n_check);
@@ -839,7 +841,8 @@ int xmi_gpu_build_surrogate(xmi_inputFPtr in, int n_train, int hits_train, int e
       const double a = (2.0 * u01(rng) - 1.0) * kLateral, b = (2.0 * u01(rng) - 1.0) * kLateral;
       const double h = h0 + (h1 - h0) * u01(rng);
       double x[3], dv[3];
-      for (int k = 0; k < 3; k++) x[k] = h * nv[k] + a * e1[k] + b * e2[k];
+      for (int k = 0; k < 3; k++) x[k] = a * e1[k] + b * e2[k];
+      x[2] += h / nv[2];
       for (int k = 0; k < 3; k++) dv[k] = x[k] - in->p_det[k];
       const double r = std::sqrt(dv[0] * dv[0] + dv[1] * dv[1] + dv[2] * dv[2]);
       double tt = std::acos((dv[0] * in->n_det[0] + dv[1] * in->n_det[1] + dv[2] * in->n_det[2]) / r);

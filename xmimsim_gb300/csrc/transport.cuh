@@ -150,12 +150,15 @@ template <typename R>
 __device__ __forceinline__ void locate(const DevBundle<R> &b, R E, int &node, R &f) {
   if (E <= __ldg(b.seg_lo)) { node = 0; f = (R)0; return; }
   if (E >= __ldg(b.seg_lo + b.n_seg)) { node = b.n_nodes - 2; f = (R)1; return; }
-  int lo = 0, hi = b.n_seg - 1;
-  while (lo < hi) {
-    int mid = (lo + hi + 1) >> 1;
-    if (E >= __ldg(b.seg_lo + mid)) lo = mid; else hi = mid - 1;
-  }
-  R t = (log(E) - __ldg(b.seg_lnlo + lo)) * __ldg(b.seg_invh + lo);
+  /* the segment with seg_lo[lo] <= E < seg_lo[lo + 1] (the bisection's
+   * answer): a guess from the search table, then steps until both hold */
+  const R lnE = log(E);
+  R gb = (lnE - b.seg_lut_ln0) * b.seg_lut_inv;
+  gb = gb > (R)0 ? (gb < (R)(XMI_SEG_LUT - 1) ? gb : (R)(XMI_SEG_LUT - 1)) : (R)0;
+  int lo = __ldg(b.seg_lut + (int)gb);
+  while (lo < b.n_seg - 1 && E >= __ldg(b.seg_lo + lo + 1)) lo++;
+  while (lo > 0 && E < __ldg(b.seg_lo + lo)) lo--;
+  R t = (lnE - __ldg(b.seg_lnlo + lo)) * __ldg(b.seg_invh + lo);
   int i = (int)t;
   int n = __ldg(b.seg_n + lo);
   if (i < 0) i = 0;

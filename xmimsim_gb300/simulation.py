@@ -299,6 +299,27 @@ class Simulation:
                          "raw": (ch[i], br[i], vr[i])})
         return outs
 
+    @staticmethod
+    def autotune_batch(sims: "Sequence[Simulation]", share: float = 1.0 / 64) -> dict:
+        """Picks the wavefront launch shape and the estimator queue size of a
+        batch by timing short batched runs (xmi_gpu_autotune_batch) and keeps
+        them in every configuration's GPU options."""
+        lib = abi.load()
+        n = len(sims)
+        ins = (C.c_void_p * n)(*[s.inputF.value for s in sims])
+        tabs = (C.c_void_p * n)(*[s.tables.value for s in sims])
+        opts = (C.POINTER(abi.XmiMainOptions) * n)(*[C.pointer(s.options) for s in sims])
+        sas = (C.POINTER(abi.XmiSolidAngle) * n)(
+            *[s.solid_angle() if s.options.use_variance_reduction and not s.surrogate_on()
+              else C.POINTER(abi.XmiSolidAngle)() for s in sims])
+        rep = np.zeros(4)
+        _check(lib.xmi_gpu_autotune_batch(n, ins, tabs, opts, sas, share, rep.ctypes.data_as(abi.c_double_p)),
+               "xmi_gpu_autotune_batch")
+        for s in sims:
+            s.gpu.threads_per_block, s.gpu.blocks_per_sm, s.gpu.queue_events = int(rep[0]), int(rep[1]), int(rep[2])
+        return {"threads_per_block": int(rep[0]), "blocks_per_sm": int(rep[1]), "queue_events": int(rep[2]),
+                "best_trial_ms": float(rep[3]), "share": share}
+
     def build_surrogate(self, n_train: int = 1 << 21, hits_train: int = 2048, epochs: int = 8,
                         hits_check: int = 1 << 20) -> dict:
         """Trains the solid-angle surrogate network (xmi_gpu_build_surrogate)."""
