@@ -327,10 +327,25 @@ def batched_arm(args, ws, rank, local):
     full_specs, _ = batched_specs(args.configs, 1.0, rank)
     full_hist = sum(histories(s) for s in full_specs)
 
-    # one network for the detector, trained on the deepest sample's volume
+    # one network for the detector, trained where the estimator queries solid
+    # angles: points from pilot runs of 8 configurations (the deepest sample
+    # and 7 spread over the sweep)
+    import numpy as np
     deep = max(range(len(specs)), key=lambda i: total_thickness(specs[i]))
+    pick = sorted(set([deep] + [int(i) for i in np.linspace(0, len(specs) - 1, 7)]))
     t0 = time.perf_counter()
-    rep = sims[deep].build_surrogate(n_train=args.n_train, hits_train=1024, epochs=args.epochs, hits_check=1 << 20)
+    per = (args.n_train + (1 << 14)) // len(pick) + 1
+    rs, ts = [], []
+    for i in pick:
+        share = min(1.0, 2.0 * per / max(1, histories(specs[i])))
+        r, t = sims[i].sample_event_points(share, per)
+        rs.append(r)
+        ts.append(t)
+    pilot_s = time.perf_counter() - t0
+    rep = sims[deep].build_surrogate_points(np.concatenate(rs), np.concatenate(ts), hits_train=1024,
+                                            epochs=args.epochs, hits_check=1 << 20)
+    rep["pilot_s"] = pilot_s
+    rep["pilot_configs"] = len(pick)
     train_s = time.perf_counter() - t0
     for i, s in enumerate(sims):
         if i != deep:

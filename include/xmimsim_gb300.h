@@ -168,6 +168,20 @@ int xmi_gpu_autotune_batch(int n, xmi_inputFPtr *inputFPtrs, xmi_hdf5FPtr *hdf5F
 int xmi_gpu_build_surrogate(xmi_inputFPtr inputFPtr, int n_train, int hits_train, int epochs, int hits_check,
                             double *report);
 int xmi_gpu_surrogate_report(xmi_inputFPtr inputFPtr, double *report);
+/* the same training and check on caller-given points (r, theta) of the
+ * solid-angle grid's frame -- typically the points where the estimator of a
+ * pilot run queried solid angles (xmi_gpu_sample_event_points): the first
+ * 16 x 1024 points (after a fixed shuffle) check, the rest train */
+int xmi_gpu_build_surrogate_points(xmi_inputFPtr inputFPtr, int n_points, const double *r, const double *theta,
+                                   int hits_train, int epochs, int hits_check, double *report);
+/* Pilot run for surrogate training: runs the transport of a prepared
+ * configuration on `share` of its photons (the first 1/R of each source item,
+ * R = round(1 / share)) and returns the (r, theta) of about max_points of the
+ * estimator's solid-angle queries, drawn uniformly over all of them (two
+ * passes: count, then a hash-selected share).  Needs variance reduction; no
+ * grid or network is used (the pilot's tallies are discarded). */
+int xmi_gpu_sample_event_points(xmi_inputFPtr inputFPtr, xmi_hdf5FPtr hdf5FPtr, xmi_main_options *options,
+                                double share, int max_points, double *r, double *theta, int *n_points);
 /* lets input `to` use the network trained for input `from` (same detector
  * radius and collimator required; points outside the network's checked box
  * are served by the integrator) -- one training serves a batch of samples

@@ -205,3 +205,30 @@ def test_shared_surrogate_in_a_batch_matches_single_runs():
         odd.share_surrogate(sims[0])
     for s in sims + [odd]:
         s.close()
+
+
+@pytest.mark.gpu
+def test_surrogate_trained_where_the_estimator_queries():
+    """Training points from a pilot run (the (r, theta) of the estimator's own
+    solid-angle queries): on the collimated geometry the network serves most
+    events of the production run, and its lines agree with the grid run."""
+    from xmimsim_gb300 import Simulation, configs, gpu_options
+    spec = collimated_spec(20000)
+    grid = Simulation(spec, options=configs.C1_OPTIONS, gpu=gpu_options(seed=0x5EED0001))
+    ref_out = grid.msim()
+    sur = Simulation(spec, options=configs.C1_OPTIONS, gpu=gpu_options(seed=0x5EED0001, use_surrogate=1,
+                                                                       surrogate_tolerance=2e-2))
+    r, t = sur.sample_event_points(share=0.5, max_points=1 << 17)
+    assert len(r) > (1 << 16) and np.all(r > 0) and np.all((t >= 0) & (t <= np.pi / 2 + 1e-6))
+    rep = sur.build_surrogate_points(r, t, hits_train=1024, epochs=20, hits_check=1 << 16)
+    assert rep["cells"] == 1024 and rep["flagged_fraction"] < 0.5, rep
+    out = sur.msim()
+    tm = sur.timing()
+    assert tm["surrogate_fallbacks"] < 0.5 * tm["events"], tm
+    v_g, v_s = ref_out["var_red"][:, :, 0], out["var_red"][:, :, 0]
+    assert v_g.max() > 0
+    assert v_s.sum() == pytest.approx(v_g.sum(), rel=1e-2)
+    big = v_g > 1e-3 * v_g.max()
+    np.testing.assert_allclose(v_s[big], v_g[big], rtol=3e-2)
+    grid.close()
+    sur.close()

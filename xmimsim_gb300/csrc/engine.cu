@@ -60,8 +60,9 @@ struct DevSide {
 struct EventQueue {
   void *events = nullptr;
   int *key = nullptr, *order = nullptr;
+  int *fb = nullptr;        /* events the surrogate leaves to the integrator */
   unsigned *hist = nullptr; /* [2][nkeys]: counts, then scatter cursors */
-  unsigned long long *count = nullptr; /* [0] events queued, [1] estimator work counter */
+  unsigned long long *count = nullptr; /* [0] events queued, [1] estimator work counter, [2] fb entries */
   size_t bytes = 0;
   long long cap = 0;
   int nkeys = 0;
@@ -69,6 +70,7 @@ struct EventQueue {
     cudaFree(events);
     cudaFree(key);
     cudaFree(order);
+    cudaFree(fb);
     cudaFree(hist);
     cudaFree(count);
     *this = EventQueue();
@@ -552,8 +554,17 @@ static int attach_solid_angles(struct xmi_tables_handle *t, xmi_solid_angle *sa)
   return 1;
 }
 
+static int prepare_run(xmi_inputFPtr in, xmi_hdf5FPtr t, xmi_main_options *options, int n_mpi_hosts,
+                       xmi_solid_angle *sa, bool need_solid_angles);
+
 int xmi_gpu_prepare_run(xmi_inputFPtr in, xmi_hdf5FPtr t, xmi_main_options *options, int n_mpi_hosts,
                         xmi_solid_angle *sa) {
+  return prepare_run(in, t, options, n_mpi_hosts, sa, true);
+}
+}  // extern "C"
+
+static int prepare_run(xmi_inputFPtr in, xmi_hdf5FPtr t, xmi_main_options *options, int n_mpi_hosts,
+                       xmi_solid_angle *sa, bool need_solid_angles) {
   if (!in || !t || !options) {
     xmi_set_error("xmi_gpu_prepare_run: NULL argument");
     return 0;
@@ -582,14 +593,13 @@ int xmi_gpu_prepare_run(xmi_inputFPtr in, xmi_hdf5FPtr t, xmi_main_options *opti
     xmi_bundle_set_run(in, t, options, n_mpi_hosts, r, R);
   }
   attach_solid_angles(t, sa);
-  if (options->use_variance_reduction && (!sa || !sa->solid_angles) && !(in->gpu.use_surrogate && in->surrogate)) {
+  if (need_solid_angles && options->use_variance_reduction && (!sa || !sa->solid_angles) &&
+      !(in->gpu.use_surrogate && in->surrogate)) {
     xmi_set_error("variance reduction requires a solid angle grid (or a trained surrogate with use_surrogate = 1)");
     return 0;
   }
   return 1;
 }
-
-}  // extern "C"
 
 /* the estimator's solid angles come from the input's trained surrogate */
 static bool surrogate_in_use(xmi_inputFPtr in, const xmi_main_options *options) {
@@ -660,13 +670,15 @@ static bool ensure_queue(EventQueue &q, long long cap, int nkeys) {
     cudaFree(q.events);
     cudaFree(q.key);
     cudaFree(q.order);
+    cudaFree(q.fb);
     q.events = nullptr;
-    q.key = q.order = nullptr;
+    q.key = q.order = q.fb = nullptr;
     q.bytes = 0;
     q.cap = 0;
     if (!cuda_ok(cudaMalloc(&q.events, bytes), "cudaMalloc event queue") ||
         !cuda_ok(cudaMalloc(&q.key, sizeof(int) * cap), "cudaMalloc event keys") ||
-        !cuda_ok(cudaMalloc(&q.order, sizeof(int) * cap), "cudaMalloc event order"))
+        !cuda_ok(cudaMalloc(&q.order, sizeof(int) * cap), "cudaMalloc event order") ||
+        !cuda_ok(cudaMalloc(&q.fb, sizeof(int) * cap), "cudaMalloc fallback list"))
       return false;
     q.bytes = bytes;
     q.cap = cap;
@@ -678,7 +690,7 @@ static bool ensure_queue(EventQueue &q, long long cap, int nkeys) {
     if (!cuda_ok(cudaMalloc(&q.hist, 2 * sizeof(unsigned) * nkeys), "cudaMalloc key histogram")) return false;
     q.nkeys = nkeys;
   }
-  if (!q.count && !cuda_ok(cudaMalloc(&q.count, 2 * sizeof(unsigned long long)), "cudaMalloc")) return false;
+  if (!q.count && !cuda_ok(cudaMalloc(&q.count, 3 * sizeof(unsigned long long)), "cudaMalloc")) return false;
   return true;
 }
 
@@ -739,9 +751,9 @@ static bool run_chunks(cudaStream_t st, EventQueue &q, long long n, int N, int n
       xmi::event_key_histogram<<<sms * 4, 256, 0, st>>>(q.key, q.count, vq.cap, nkeys, q.hist);
       xmi::event_key_scan<<<1, xmi::kScanThreads, 0, st>>>(q.hist, nkeys, q.hist + nkeys, q.count, total_events);
       xmi::event_key_scatter<<<sms * 4, 256, 0, st>>>(q.key, q.count, vq.cap, nkeys, q.hist + nkeys, q.order);
-      cudaMemsetAsync(q.count + 1, 0, sizeof(unsigned long long), st);
+      cudaMemsetAsync(q.count + 1, 0, 2 * sizeof(unsigned long long), st);
       mark();
-      launches += surrogate(vq);
+      launches += surrogate(vq, q.fb, q.count + 2);
       mark();
       estimator(vq, (const int *)q.order, q.count + 1);
       mark();
@@ -879,9 +891,44 @@ static int estimator_blocks(int stage_cap, size_t *smem) {
 }
 
 /* one configuration on its handle's stream */
+/* Records the (r, theta) of a pseudo-random share p of the queued estimator
+ * events (selected by a hash of photon id and order, so the selection does
+ * not depend on the queue's order) -- the points a surrogate network will be
+ * queried at. */
+struct PointRecorder {
+  double p = 0.0;
+  float *r = nullptr, *t = nullptr;
+  unsigned long long *n = nullptr;
+  long long max = 0;
+};
+
+__device__ __forceinline__ double event_hash01(long long id, int n) {
+  unsigned long long z = (unsigned long long)id * 0x9E3779B97F4A7C15ull + (unsigned long long)n * 0xD1B54A32D192ED03ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  z ^= z >> 31;
+  return (double)(z >> 11) * (1.0 / 9007199254740992.0);
+}
+
+template <typename R>
+__global__ void record_points_kernel(const xmi::VrEvent<R> *ev, const unsigned long long *count, long long cap,
+                                     double p, float *out_r, float *out_t, unsigned long long *out_n,
+                                     long long max_out) {
+  const long long n = (long long)*count < cap ? (long long)*count : cap;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    if (event_hash01(ev[i].id, ev[i].n) >= p) continue;
+    const unsigned long long pos = atomicAdd(out_n, 1ull);
+    if ((long long)pos < max_out) {
+      out_r[pos] = (float)ev[i].sa_r;
+      out_t[pos] = (float)ev[i].sa_t;
+    }
+  }
+}
+
 template <typename R>
 static bool launch_single(DevState *s, xmi::DevBundle<R> &d, const xmi::DevTally &tl, const xmi_bundle &h,
-                          int threads, int blocks_per_sm, long long qev, const void *sg, Phases &ph) {
+                          int threads, int blocks_per_sm, long long qev, const void *sg, Phases &ph,
+                          const PointRecorder *rec = nullptr) {
   const int sms = num_sms();
   if (!s->d_bundle && !cuda_ok(cudaMalloc(&s->d_bundle, sizeof(xmi::DevBundle<double>)), "cudaMalloc")) return false;
   if (!s->d_tally && !cuda_ok(cudaMalloc(&s->d_tally, sizeof(xmi::DevTally)), "cudaMalloc")) return false;
@@ -916,11 +963,16 @@ static bool launch_single(DevState *s, xmi::DevBundle<R> &d, const xmi::DevTally
         (const xmi::DevBundle<R> *)s->d_bundle, s->d_tally, 1, vq.ev, order, vq.count, vq.cap, work, stage_cap,
         &s->counters[1]);
   };
-  auto surrogate = [&](const xmi::VrQueue<R> &vq) -> int {
+  auto surrogate = [&](const xmi::VrQueue<R> &vq, int *fb, unsigned long long *fb_count) -> int {
     if (!d.use_surrogate) return 0;
-    xmi_surrogate_apply(sg, sizeof(R) == 8 ? 0 : 1, s->d_bundle, 1, vq.ev, vq.count, vq.cap, &s->counters[4],
-                        (int *)&s->counters[5], s->stream);
-    return 1;
+    if (rec) {
+      record_points_kernel<R><<<sms * 4, 256, 0, s->stream>>>(vq.ev, vq.count, vq.cap, rec->p, rec->r, rec->t, rec->n,
+                                                               rec->max);
+      return 1;
+    }
+    xmi_surrogate_apply(sg, sizeof(R) == 8 ? 0 : 1, s->d_bundle, 1, vq.ev, vq.count, vq.cap, &s->counters[4], fb,
+                        fb_count, (int *)&s->counters[5], s->stream);
+    return 2;
   };
   return run_chunks<R>(s->stream, q, h.n_photons_total, h.n_interactions, XMI_MAXL * XMI_MAXN, h.use_vr != 0,
                        qev, &s->counters[3], transport, surrogate, estimator, ph);
@@ -1120,11 +1172,11 @@ bool launch_batch(int n, DevState **st, xmi_hdf5FPtr *t, const xmi::DevTally *tl
   };
   /* flags: [0] estimator error, [1] events, [2] integrator fallbacks of the
    * surrogate, [3] surrogate error */
-  auto surrogate = [&](const xmi::VrQueue<R> &vq) -> int {
+  auto surrogate = [&](const xmi::VrQueue<R> &vq, int *fb, unsigned long long *fb_count) -> int {
     if (!sg) return 0;
-    xmi_surrogate_apply(sg, sizeof(R) == 8 ? 0 : 1, db, n, vq.ev, vq.count, vq.cap, &B.flags[2],
+    xmi_surrogate_apply(sg, sizeof(R) == 8 ? 0 : 1, db, n, vq.ev, vq.count, vq.cap, &B.flags[2], fb, fb_count,
                         (int *)&B.flags[3], B.stream);
-    return 1;
+    return 2;
   };
   if (!run_chunks<R>(B.stream, B.q, first[n], N, n * XMI_MAXL * XMI_MAXN, vr, qev, &B.flags[1], transport,
                      surrogate, estimator, ph, graph))
@@ -1204,6 +1256,85 @@ extern "C" int xmi_main_msim_batch(int n, xmi_inputFPtr *inputFPtrs, xmi_hdf5FPt
   g_timing.launches = ph.launches;
   for (int k = 0; k < 4; k++) g_timing.phase_ms[k] = ph.ms[k];
   return 1;
+}
+
+/* ---------------------------------------------------------------- */
+/* points where the estimator queries solid angles (surrogate training)  */
+/* ---------------------------------------------------------------- */
+extern "C" int xmi_gpu_sample_event_points(xmi_inputFPtr in, xmi_hdf5FPtr t, xmi_main_options *options,
+                                           double share, int max_points, double *r_out, double *theta_out,
+                                           int *n_out) {
+  if (!in || !t || !options || !(share > 0.0 && share <= 1.0) || max_points < 1 || !r_out || !theta_out || !n_out) {
+    xmi_set_error("xmi_gpu_sample_event_points: invalid arguments");
+    return 0;
+  }
+  if (!options->use_variance_reduction) {
+    xmi_set_error("xmi_gpu_sample_event_points: the estimator runs only with variance reduction");
+    return 0;
+  }
+  if (!ensure_device()) return 0;
+  const int rep0 = t->replica, nrep0 = t->n_replicas;
+  t->replica = 0;
+  t->n_replicas = std::max(1, (int)std::lround(1.0 / share));
+  bool ok = prepare_run(in, t, options, 1, nullptr, false) != 0;
+  const int precision = in->gpu.precision;
+  ok = ok && xmi_dev_sync_tables(t, precision);
+  DevState *s = ok ? state_of(t) : nullptr;
+  float *pr = nullptr, *pt = nullptr;
+  unsigned long long *pn = nullptr, n_rec = 0;
+  ok = ok && cuda_ok(cudaMalloc(&pr, sizeof(float) * max_points), "cudaMalloc") &&
+       cuda_ok(cudaMalloc(&pt, sizeof(float) * max_points), "cudaMalloc") &&
+       cuda_ok(cudaMalloc(&pn, sizeof(unsigned long long)), "cudaMalloc");
+  const int threads = in->gpu.threads_per_block > 0 ? in->gpu.threads_per_block : 128;
+  const int bps = in->gpu.blocks_per_sm > 0 ? in->gpu.blocks_per_sm : 8;
+  /* pass 1 counts the events (share 0 recorded), pass 2 records about
+   * max_points of them */
+  double p = 0.0;
+  for (int pass = 0; pass < 2 && ok; pass++) {
+    PointRecorder rec;
+    rec.p = p;
+    rec.r = pr;
+    rec.t = pt;
+    rec.n = pn;
+    rec.max = max_points;
+    cudaMemsetAsync(pn, 0, sizeof(unsigned long long), s->stream);
+    xmi::DevTally tl;
+    Phases ph;
+    ok = precision == 0 ? stage_run<double>(s, s->b64, t->b, tl, true) &&
+                              launch_single<double>(s, s->b64, tl, t->b, threads, bps, queue_events_of(in->gpu),
+                                                    nullptr, ph, &rec)
+                        : stage_run<float>(s, s->b32, t->b, tl, true) &&
+                              launch_single<float>(s, s->b32, tl, t->b, threads, bps, queue_events_of(in->gpu),
+                                                   nullptr, ph, &rec);
+    unsigned long long counters[8];
+    ok = ok && cuda_ok(cudaMemcpy(counters, s->counters, sizeof(counters), cudaMemcpyDeviceToHost), "copy") &&
+         cuda_ok(cudaMemcpy(&n_rec, pn, sizeof(n_rec), cudaMemcpyDeviceToHost), "copy");
+    if (ok && counters[1] != 0) {
+      xmi_set_error("transport kernel reported error code %llu", counters[1]);
+      ok = false;
+    }
+    if (ok && pass == 0) {
+      const double events = (double)counters[3];
+      p = events > 0.0 ? std::min(1.0, 0.98 * max_points / events) : 1.0;
+    }
+  }
+  const long long n = std::min((long long)n_rec, (long long)max_points);
+  if (ok) {
+    std::vector<float> hr(n > 0 ? n : 1), ht(n > 0 ? n : 1);
+    ok = cuda_ok(cudaMemcpy(hr.data(), pr, sizeof(float) * n, cudaMemcpyDeviceToHost), "copy") &&
+         cuda_ok(cudaMemcpy(ht.data(), pt, sizeof(float) * n, cudaMemcpyDeviceToHost), "copy");
+    for (long long i = 0; ok && i < n; i++) {
+      r_out[i] = hr[i];
+      theta_out[i] = ht[i];
+    }
+    *n_out = (int)n;
+  }
+  cudaFree(pr);
+  cudaFree(pt);
+  cudaFree(pn);
+  t->replica = rep0;
+  t->n_replicas = nrep0;
+  return ok ? 1 : 0;
 }
 
 /* ---------------------------------------------------------------- */

@@ -109,6 +109,7 @@ __device__ __forceinline__ void estimate_event(const DevBundle<R> &b, const DevT
   const int n_line = XMI_LDG(b.ent_off, off + nel, b.n_layer_el + 1, 15) - k_first;
   const R live = valid ? (R)1 : (R)0;
   R rayl_sum = (R)0; /* Rayleigh keeps the photon energy: one channel add per event */
+  const ComptonEvent<R> ce = compton_event(ev.E, ev.theta);
   for (int i = 0; i < nel; i++) {
     const int pair = off + i;
     const int e = XMI_LDG(b.layer_el, pair, b.n_layer_el, 9);
@@ -123,7 +124,7 @@ __device__ __forceinline__ void estimate_event(const DevBundle<R> &b, const DevT
     xmi_rng g;
     xmi_rng_init(&g, b.seed, (uint64_t)ev.id, vr_stream(n, i));
     bool cok = true;
-    const R ec = compton_energy(b, e, ev.E, ev.theta, &g, true, cok);
+    const R ec = compton_energy_est(b, e, ce, &g, cok);
     R twc = (R)0;
     if (cok) {
       R mus_c[XMI_MAXL];
@@ -192,6 +193,7 @@ __device__ __forceinline__ void estimate_event_uniform(const DevBundle<R> &b, co
   R *s_rd = scratch, *s_a = scratch + 32 * XMI_MAXL;
   const R live = valid ? (R)1 : (R)0;
   R rayl_sum = (R)0; /* Rayleigh keeps the photon energy: one channel add per event */
+  const ComptonEvent<R> ce = compton_event(ev.E, ev.theta);
 #pragma unroll
   for (int j = 0; j < XMI_MAXL; j++) s_rd[lane * XMI_MAXL + j] = ev.rd[j];
   for (int i = 0; i < nel; i++) {
@@ -208,7 +210,7 @@ __device__ __forceinline__ void estimate_event_uniform(const DevBundle<R> &b, co
     xmi_rng g;
     xmi_rng_init(&g, b.seed, (uint64_t)ev.id, vr_stream(n, i));
     bool cok = true;
-    const R ec = compton_energy(b, e, ev.E, ev.theta, &g, true, cok);
+    const R ec = compton_energy_est(b, e, ce, &g, cok);
     R twc = (R)0;
     if (cok) {
       R mus_c[XMI_MAXL];
@@ -245,9 +247,19 @@ __device__ __forceinline__ void estimate_event_uniform(const DevBundle<R> &b, co
       if (k < k1) {
         const int sh = XMI_LDG(b.ent_shell, k, b.n_ent, 16);
         R pmu[XMI_MAXL];
+#ifndef XMI_CHECKED
+        if constexpr (sizeof(R) == 4 && XMI_MAXL == 8) {
+          const float4 *pp = reinterpret_cast<const float4 *>(b.ent_pmu + (long long)k * XMI_MAXL);
+          const float4 a0 = __ldg(pp), a1 = __ldg(pp + 1);
+          pmu[0] = a0.x, pmu[1] = a0.y, pmu[2] = a0.z, pmu[3] = a0.w;
+          pmu[4] = a1.x, pmu[5] = a1.y, pmu[6] = a1.z, pmu[7] = a1.w;
+        } else
+#endif
+        {
 #pragma unroll
-        for (int j = 0; j < XMI_MAXL; j++)
-          pmu[j] = XMI_LDG(b.ent_pmu, (long long)k * XMI_MAXL + j, (long long)b.n_ent * XMI_MAXL, 17);
+          for (int j = 0; j < XMI_MAXL; j++)
+            pmu[j] = XMI_LDG(b.ent_pmu, (long long)k * XMI_MAXL + j, (long long)b.n_ent * XMI_MAXL, 17);
+        }
         R acc = (R)0;
 #pragma unroll 4
         for (int q = 0; q < 32; q++) {
@@ -295,7 +307,7 @@ constexpr int kEventsPerGrab = 256;
  * the counter `work`; stage rows of stage_cap values per warp sit in dynamic
  * shared memory. */
 template <typename R>
-__global__ void __launch_bounds__(256, 2) estimator_kernel(const DevBundle<R> *bundles, const DevTally *tallies,
+__global__ void __launch_bounds__(256, 3) estimator_kernel(const DevBundle<R> *bundles, const DevTally *tallies,
                                                            int n_cfg, const VrEvent<R> *events, const int *order,
                                                            const unsigned long long *count, long long cap,
                                                            unsigned long long *work, int stage_cap,

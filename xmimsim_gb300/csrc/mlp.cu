@@ -244,14 +244,15 @@ __host__ __device__ __forceinline__ void features_of(const Domain &d, R r, R t, 
 }
 
 /* Fills the solid angle of every queued estimator event: the network on the
- * tensor cores for 128 events per tile, the integrator (the same Monte Carlo
- * as an off-grid point of the grid path) in flagged cells and outside the
- * box, zero below the box's lowest theta (as the grid path). */
+ * tensor cores for 128 events per tile, zero below the box's lowest theta
+ * (as the grid path).  Events in flagged cells or outside the box are
+ * appended to fb_list for omega_fallback_kernel. */
 template <typename R>
 __global__ void __launch_bounds__(128, 1) omega_kernel(const unsigned char *packed, const float *theta, Domain dom,
                                                        const unsigned char *flags, const DevBundle<R> *bundles,
                                                        int n_cfg, VrEvent<R> *ev, const unsigned long long *count,
-                                                       long long cap, unsigned long long *fallbacks, int *err) {
+                                                       long long cap, unsigned long long *fallbacks, int *fb_list,
+                                                       unsigned long long *fb_count, int *err) {
   extern __shared__ __align__(1024) unsigned char sm[];
   FwdCtx c;
   fwd_setup(sm, packed, theta, c);
@@ -269,34 +270,95 @@ __global__ void __launch_bounds__(128, 1) omega_kernel(const unsigned char *pack
       failed = true;
       break;
     }
-    if (!valid) continue;
     /* events of a batch carry their configuration; those of configurations
      * served by the grid were already weighted in transport */
-    const int cfg = ev[i].cfg;
-    if (cfg < 0 || cfg >= n_cfg) {
-      atomicExch(err, 2);
-      continue;
+    bool apply = false, need_fb = false;
+    R omega = (R)0;
+    if (valid) {
+      const int cfg = ev[i].cfg;
+      if (cfg < 0 || cfg >= n_cfg) {
+        atomicExch(err, 2);
+      } else if (bundles[cfg].use_surrogate) {
+        if (!(t >= (R)dom.tmin)) {
+          apply = true;
+        } else if (!inside || flags[cell]) {
+          need_fb = true;
+        } else {
+          const float o = __expf(y) - dom.eps;
+          omega = (R)(o > 0.0f ? o : 0.0f);
+          apply = true;
+        }
+      }
     }
-    const DevBundle<R> *bundle = bundles + cfg;
-    if (!bundle->use_surrogate) continue;
-    R omega;
-    if (!(t >= (R)dom.tmin)) {
-      omega = (R)0;
-    } else if (!inside || flags[cell]) {
-      xmi_rng g;
-      xmi_rng_init(&g, bundle->seed, (uint64_t)ev[i].id, 0x80000000u | (uint32_t)ev[i].n);
-      omega = single_solid_angle(*bundle, r, t, &g, bundle->sa_hits);
-      atomicAdd(fallbacks, 1ull);
-    } else {
-      const float o = __expf(y) - dom.eps;
-      omega = (R)(o > 0.0f ? o : 0.0f);
+    /* warp-aggregated append to the integrator's list */
+    const unsigned fb = __ballot_sync(0xffffffffu, need_fb);
+    if (fb) {
+      const int lane = threadIdx.x & 31, leader = __ffs(fb) - 1;
+      unsigned long long base = 0;
+      if (lane == leader) {
+        base = atomicAdd(fb_count, (unsigned long long)__popc(fb));
+        atomicAdd(fallbacks, (unsigned long long)__popc(fb));
+      }
+      base = __shfl_sync(0xffffffffu, base, leader);
+      const unsigned long long pos = base + __popc(fb & ((1u << lane) - 1u));
+      if (need_fb && (long long)pos < cap) fb_list[pos] = (int)i;
     }
-    ev[i].pR *= omega;
-    ev[i].pC *= omega;
-    ev[i].pdir_fluo *= omega;
+    if (apply) {
+      ev[i].pR *= omega;
+      ev[i].pC *= omega;
+      ev[i].pdir_fluo *= omega;
+    }
   }
   if (failed && threadIdx.x == 0) atomicExch(err, 1);
   fwd_teardown(c);
+}
+
+/* The integrator for the events omega_kernel could not serve: one warp per
+ * event, lane l taking cone samples l, l + 32, ... of the event's own stream
+ * (seed, id, 0x80000000 | n) -- sample i is Philox block i of that stream,
+ * so the hit count and the solid angle are those of the serial off-grid
+ * integral of the grid path (single_solid_angle). */
+template <typename R>
+__global__ void __launch_bounds__(256) omega_fallback_kernel(const DevBundle<R> *bundles, int n_cfg, VrEvent<R> *ev,
+                                                             const int *fb_list, const unsigned long long *fb_count,
+                                                             long long cap) {
+  const int lane = threadIdx.x & 31;
+  const long long n = (long long)*fb_count < cap ? (long long)*fb_count : cap;
+  const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
+  for (long long w = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); w < n; w += warps) {
+    const int i = fb_list[w];
+    if (i < 0 || (long long)i >= cap) continue;
+    const int cfg = ev[i].cfg;
+    if (cfg < 0 || cfg >= n_cfg) continue;
+    const DevBundle<R> &b = bundles[cfg];
+    const SaGeom g{b.det_radius, b.coll_radius, b.coll_height, b.coll_present};
+    const uint64_t id = (uint64_t)ev[i].id;
+    const uint32_t stream = 0x80000000u | (uint32_t)ev[i].n;
+    R cfca, fcsa, st, ct, py, pz;
+    bool outside;
+    int hits = 0;
+    const bool live = sa_setup<R>(g, ev[i].sa_r, ev[i].sa_t, cfca, fcsa, st, ct, py, pz, outside);
+    if (live) {
+      for (int s = lane; s < b.sa_hits; s += 32) {
+        xmi_u32x4 c;
+        c.v[0] = (uint32_t)s;
+        c.v[1] = stream;
+        c.v[2] = (uint32_t)id;
+        c.v[3] = (uint32_t)(id >> 32);
+        const xmi_u32x4 o = xmi_philox4x32_10(c, (uint32_t)b.seed, (uint32_t)(b.seed >> 32));
+        R u1, u2;
+        cone_draws(o, u1, u2);
+        hits += sa_sample<R>(g, cfca, st, ct, py, pz, outside, u1, u2);
+      }
+    }
+    hits = __reduce_add_sync(0xffffffffu, hits);
+    if (lane == 0) {
+      const R omega = live ? fcsa * (R)hits / (R)b.sa_hits : (R)0;
+      ev[i].pR *= omega;
+      ev[i].pC *= omega;
+      ev[i].pdir_fluo *= omega;
+    }
+  }
 }
 
 /* ---------------- training ---------------- */
@@ -793,29 +855,30 @@ void xmi_surrogate_free(void *p) {
 
 /* Trains the solid-angle surrogate of an initialised input handle (see
  * xmi_gpu_build_surrogate in the public header for the procedure). */
+constexpr int kCells = 32, kCheckPerCell = 16, kCheckPoints = kCells * kCells * kCheckPerCell;
+
+static int build_from_points(xmi_inputFPtr in, std::vector<double> &r_h, std::vector<double> &t_h, int n_train,
+                             int hits_train, int epochs, int hits_check, double *report,
+                             std::chrono::steady_clock::time_point t_start);
+
+static bool surrogate_device_ok() {
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
+    xmi_set_error("no CUDA device available: the engine has no CPU fallback");
+    return false;
+  }
+  return true;
+}
+
 int xmi_gpu_build_surrogate(xmi_inputFPtr in, int n_train, int hits_train, int epochs, int hits_check,
                             double *report) {
-  using namespace xmi::mlp;
   if (!in || !in->initialized || n_train < 128 || hits_train < 1 || epochs < 1 || hits_check < 1) {
     xmi_set_error("xmi_gpu_build_surrogate: invalid arguments");
     return 0;
   }
-  int ndev = 0;
-  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
-    xmi_set_error("no CUDA device available: the engine has no CPU fallback");
-    return 0;
-  }
+  if (!surrogate_device_ok()) return 0;
   const auto t_start = std::chrono::steady_clock::now();
-  SurrogateState *sg = new SurrogateState();
-  std::vector<double> rv(1024), tv(1024);
-  xmi_solid_angle_axes(in, 1024, 1024, rv.data(), tv.data());
-  sg->dom.tmin = (float)tv.front();
-  sg->dom.ncr = 32;
-  sg->dom.nct = 32;
-  sg->dom.eps = 1e-10f;
-  const xmi::SaGeom geom{in->det_radius, in->coll_radius, in->coll_height, in->coll_present};
-  sg->geom = geom;
-  const int ncell = sg->dom.ncr * sg->dom.nct, n_check = 16 * ncell;
+  const int n_check = kCheckPoints;
 
   /* training and checking points uniform over the sample volume: the slab
    * between the first and last layer planes, within kLateral of the beam
@@ -850,6 +913,54 @@ int xmi_gpu_build_surrogate(xmi_inputFPtr in, int n_train, int hits_train, int e
       r_h[i] = r;
       t_h[i] = M_PI / 2.0 - tt;
     }
+  }
+  return build_from_points(in, r_h, t_h, n_train, hits_train, epochs, hits_check, report, t_start);
+}
+
+int xmi_gpu_build_surrogate_points(xmi_inputFPtr in, int n_points, const double *r, const double *theta,
+                                   int hits_train, int epochs, int hits_check, double *report) {
+  if (!in || !in->initialized || !r || !theta || n_points < kCheckPoints + 128 || hits_train < 1 || epochs < 1 ||
+      hits_check < 1) {
+    xmi_set_error("xmi_gpu_build_surrogate_points: invalid arguments (at least %d points)", kCheckPoints + 128);
+    return 0;
+  }
+  if (!surrogate_device_ok()) return 0;
+  const auto t_start = std::chrono::steady_clock::now();
+  /* fixed shuffle; the first kCheckPoints check, the rest train (points are
+   * stored training first) */
+  std::vector<int> perm(n_points);
+  for (int i = 0; i < n_points; i++) perm[i] = i;
+  std::mt19937_64 rng(0x5EED0006ull);
+  std::shuffle(perm.begin(), perm.end(), rng);
+  const int n_train = n_points - kCheckPoints;
+  std::vector<double> r_h(n_points + kCheckPoints), t_h(n_points + kCheckPoints);
+  for (int i = 0; i < n_points; i++) {
+    const int src = perm[i], dst = i < kCheckPoints ? n_train + i : i - kCheckPoints;
+    r_h[dst] = r[src];
+    t_h[dst] = theta[src];
+  }
+  return build_from_points(in, r_h, t_h, n_train, hits_train, epochs, hits_check, report, t_start);
+}
+
+/* Trains the network on points [0, n_train) of r_h/t_h (targets from the
+ * FP32 integrator) and checks it on the next kCheckPoints (FP64 integrator,
+ * twice); r_h/t_h hold n_train + 2 kCheckPoints entries. */
+static int build_from_points(xmi_inputFPtr in, std::vector<double> &r_h, std::vector<double> &t_h, int n_train,
+                             int hits_train, int epochs, int hits_check, double *report,
+                             std::chrono::steady_clock::time_point t_start) {
+  using namespace xmi::mlp;
+  SurrogateState *sg = new SurrogateState();
+  std::vector<double> rv(1024), tv(1024);
+  xmi_solid_angle_axes(in, 1024, 1024, rv.data(), tv.data());
+  sg->dom.tmin = (float)tv.front();
+  sg->dom.ncr = kCells;
+  sg->dom.nct = kCells;
+  sg->dom.eps = 1e-10f;
+  const xmi::SaGeom geom{in->det_radius, in->coll_radius, in->coll_height, in->coll_present};
+  sg->geom = geom;
+  const int ncell = sg->dom.ncr * sg->dom.nct, n_check = kCheckPoints;
+  std::mt19937_64 rng(0x5EED0004ull);
+  {
     /* feature scaling and checked box from the training points */
     float lo[3] = {1e30f, 1e30f, 1e30f}, hi[3] = {-1e30f, -1e30f, -1e30f};
     float tlo = 1e30f, thi = -1e30f;
@@ -911,6 +1022,12 @@ int xmi_gpu_build_surrogate(xmi_inputFPtr in, int n_train, int hits_train, int e
     if (ok) cudaMemcpy(o_h.data(), o_d, sizeof(double) * ntot, cudaMemcpyDeviceToHost);
   }
   if (ok) {
+    /* log target log(omega + eps) with eps 1e-4 of the largest training
+     * solid angle: relative accuracy where the solid angle matters, and no
+     * cliff of 20 units in log space at a collimator's shadow edge */
+    double omax = 0.0;
+    for (int i = 0; i < n_train; i++) omax = std::max(omax, o_h[i]);
+    sg->dom.eps = omax > 0.0 ? (float)(1e-4 * omax) : 1e-10f;
     std::vector<float> feat(3 * (size_t)n_train), targ(n_train);
     for (int i = 0; i < n_train; i++) {
       bool inside;
@@ -966,12 +1083,13 @@ int xmi_gpu_build_surrogate(xmi_inputFPtr in, int n_train, int hits_train, int e
     std::vector<float> pred(n_check);
     cudaMemcpy(pred.data(), pred_d, sizeof(float) * n_check, cudaMemcpyDeviceToHost);
     /* per cell: the RMS relative error of the network over its checking
-     * points, with the reference values' own noise variance (from the two
-     * independent integrations) subtracted; cells without checking points
-     * (outside the sample volume) and cells with a point whose reference is
-     * 0 but the network's is not are flagged */
+     * points -- relative to omega + eps, as the network's target -- with the
+     * reference values' own noise variance (from the two independent
+     * integrations) subtracted; cells without checking points (outside the
+     * sample volume) are flagged */
     std::vector<double> cell_e2(ncell, 0.0), cell_n2(ncell, 0.0), errs;
-    std::vector<int> cell_n(ncell, 0), cell_bad(ncell, 0);
+    std::vector<int> cell_n(ncell, 0);
+    const double eps = sg->dom.eps;
     for (int i = 0; i < n_check; i++) {
       bool inside;
       int cell;
@@ -981,15 +1099,10 @@ int xmi_gpu_build_surrogate(xmi_inputFPtr in, int n_train, int hits_train, int e
       const double a = o_h[n_train + i], b = o_h[n_train + n_check + i], truth = 0.5 * (a + b);
       const double net = std::max(0.0, std::exp((double)pred[i]) - sg->dom.eps);
       cell_n[cell]++;
-      if (truth > 0.0) {
-        const double e = (net - truth) / truth, nz = (a - b) / (2.0 * truth);
-        errs.push_back(std::fabs(e));
-        cell_e2[cell] += e * e;
-        cell_n2[cell] += nz * nz;
-      } else if (net > 1e3 * sg->dom.eps) {
-        cell_bad[cell] = 1;
-        errs.push_back(1.0);
-      }
+      const double e = (net - truth) / (truth + eps), nz = (a - b) / (2.0 * (truth + eps));
+      errs.push_back(std::fabs(e));
+      cell_e2[cell] += e * e;
+      cell_n2[cell] += nz * nz;
     }
     if (errs.empty()) errs.push_back(1.0);
     std::vector<unsigned char> flags(ncell, 0);
@@ -997,7 +1110,7 @@ int xmi_gpu_build_surrogate(xmi_inputFPtr in, int n_train, int hits_train, int e
     const double tol = in->gpu.surrogate_tolerance > 0 ? in->gpu.surrogate_tolerance : 1e-3;
     for (int c = 0; c < ncell; c++) {
       const double err = cell_n[c] > 0 ? std::sqrt(std::max(0.0, (cell_e2[c] - cell_n2[c]) / cell_n[c])) : 1.0;
-      flags[c] = (cell_n[c] == 0 || cell_bad[c] || err > tol) ? 1 : 0;
+      flags[c] = (cell_n[c] == 0 || err > tol) ? 1 : 0;
       if (!flags[c]) worst_kept = std::max(worst_kept, err);
     }
     std::vector<double> sorted = errs;
@@ -1061,8 +1174,8 @@ int xmi_gpu_share_surrogate(xmi_inputFPtr from, xmi_inputFPtr to) {
 }
 
 int xmi_surrogate_apply(const void *p, int precision, const void *dev_bundles, int n_cfg, void *events,
-                        const unsigned long long *count, long long cap, unsigned long long *fallbacks, int *err,
-                        void *stream) {
+                        const unsigned long long *count, long long cap, unsigned long long *fallbacks, int *fb_list,
+                        unsigned long long *fb_count, int *err, void *stream) {
   using namespace xmi::mlp;
   const SurrogateState *sg = (const SurrogateState *)p;
   if (!sg) return 0;
@@ -1074,12 +1187,18 @@ int xmi_surrogate_apply(const void *p, int precision, const void *dev_bundles, i
     cudaFuncSetAttribute(omega_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, SM_TOTAL);
     omega_kernel<double><<<sms, 128, SM_TOTAL, st>>>(sg->packed_d, sg->theta_d, sg->dom, sg->flags_d,
                                                       (const xmi::DevBundle<double> *)dev_bundles, n_cfg,
-                                                      (xmi::VrEvent<double> *)events, count, cap, fallbacks, err);
+                                                      (xmi::VrEvent<double> *)events, count, cap, fallbacks, fb_list,
+                                                      fb_count, err);
+    omega_fallback_kernel<double><<<sms * 8, 256, 0, st>>>((const xmi::DevBundle<double> *)dev_bundles, n_cfg,
+                                                          (xmi::VrEvent<double> *)events, fb_list, fb_count, cap);
   } else {
     cudaFuncSetAttribute(omega_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, SM_TOTAL);
     omega_kernel<float><<<sms, 128, SM_TOTAL, st>>>(sg->packed_d, sg->theta_d, sg->dom, sg->flags_d,
                                                      (const xmi::DevBundle<float> *)dev_bundles, n_cfg,
-                                                     (xmi::VrEvent<float> *)events, count, cap, fallbacks, err);
+                                                     (xmi::VrEvent<float> *)events, count, cap, fallbacks, fb_list,
+                                                     fb_count, err);
+    omega_fallback_kernel<float><<<sms * 8, 256, 0, st>>>((const xmi::DevBundle<float> *)dev_bundles, n_cfg,
+                                                         (xmi::VrEvent<float> *)events, fb_list, fb_count, cap);
   }
   return cudaGetLastError() == cudaSuccess ? 1 : 0;
 }

@@ -59,11 +59,12 @@ int xmi_dev_bundle_copy64(struct xmi_tables_handle *t, void *out);
 void xmi_surrogate_free(void *sg);
 /* multiplies the solid-angle factors of the queued estimator events of the
  * configurations that use the network (dev_bundles[n_cfg] on the device,
- * indexed by the events' configuration) by its solid angle, the integrator
- * serving flagged cells; all on stream */
+ * indexed by the events' configuration) by its solid angle; events in
+ * flagged cells go through fb_list (cap entries, *fb_count zeroed by the
+ * caller) to the integrator; all on stream */
 int xmi_surrogate_apply(const void *sg, int precision, const void *dev_bundles, int n_cfg, void *events,
-                        const unsigned long long *count, long long cap, unsigned long long *fallbacks,
-                        int *err, void *stream);
+                        const unsigned long long *count, long long cap, unsigned long long *fallbacks, int *fb_list,
+                        unsigned long long *fb_count, int *err, void *stream);
 
 #ifdef __cplusplus
 }

@@ -329,6 +329,31 @@ class Simulation:
         keys = ("median_rel_err", "max_rel_err_kept", "flagged_fraction", "train_loss", "seconds", "cells")
         return dict(zip(keys, rep.tolist()))
 
+    def sample_event_points(self, share: float, max_points: int) -> tuple[np.ndarray, np.ndarray]:
+        """(r, theta) of about max_points solid-angle queries of the estimator
+        in a pilot run over `share` of the photons (xmi_gpu_sample_event_points)."""
+        r = np.zeros(max_points)
+        t = np.zeros(max_points)
+        n = C.c_int(0)
+        _check(self.lib.xmi_gpu_sample_event_points(self.inputF, self.tables, C.byref(self.options), share,
+                                                    max_points, r.ctypes.data_as(abi.c_double_p),
+                                                    t.ctypes.data_as(abi.c_double_p), C.byref(n)),
+               "xmi_gpu_sample_event_points")
+        return r[:n.value].copy(), t[:n.value].copy()
+
+    def build_surrogate_points(self, r: np.ndarray, theta: np.ndarray, hits_train: int = 1024, epochs: int = 8,
+                               hits_check: int = 1 << 20) -> dict:
+        """Trains the surrogate on the given (r, theta) points (xmi_gpu_build_surrogate_points)."""
+        r = np.ascontiguousarray(r, dtype=np.float64)
+        theta = np.ascontiguousarray(theta, dtype=np.float64)
+        rep = np.zeros(6)
+        _check(self.lib.xmi_gpu_build_surrogate_points(self.inputF, len(r), r.ctypes.data_as(abi.c_double_p),
+                                                       theta.ctypes.data_as(abi.c_double_p), hits_train, epochs,
+                                                       hits_check, rep.ctypes.data_as(abi.c_double_p)),
+               "xmi_gpu_build_surrogate_points")
+        keys = ("median_rel_err", "max_rel_err_kept", "flagged_fraction", "train_loss", "seconds", "cells")
+        return dict(zip(keys, rep.tolist()))
+
     def share_surrogate(self, other: "Simulation") -> None:
         """Serves this configuration's solid angles from the network trained
         for `other` (same detector and collimator; xmi_gpu_share_surrogate)."""
