@@ -141,29 +141,56 @@ def collimated_spec(n_photons: int):
 
 @pytest.mark.gpu
 def test_surrogate_replaces_the_grid_in_transport():
-    """Trains the surrogate on the collimated geometry (reduced budget), then
-    runs the transport with it: every first-order line intensity within 3%
-    of the grid run (whose own grid noise is ~1.4% per point) and the total
-    within 1%; the training report is sane."""
+    """The collimated geometry with the network trained where the estimator
+    queries solid angles (points of a pilot run): the network, with the
+    tabulated integrator in its flagged cells, serves all but a few events,
+    and every first-order line is within 3% of the grid run (whose own grid
+    noise is ~1.4% per point), the total within 1%."""
     from xmimsim_gb300 import Simulation, configs, gpu_options
     spec = collimated_spec(20000)
     grid = Simulation(spec, options=configs.C1_OPTIONS, gpu=gpu_options(seed=0x5EED0001))
     ref_out = grid.msim()
-    sur = Simulation(spec, options=configs.C1_OPTIONS, gpu=gpu_options(seed=0x5EED0001, use_surrogate=1,
-                                                                       surrogate_tolerance=2e-2))
-    rep = sur.build_surrogate(n_train=1 << 18, hits_train=2048, epochs=20, hits_check=1 << 16)
-    assert rep["cells"] == 1024 and 0 <= rep["flagged_fraction"] < 0.5, rep
-    assert rep["median_rel_err"] < 0.02, rep
+    g_sur = gpu_options(seed=0x5EED0001, use_surrogate=1, surrogate_tolerance=2e-2)
+    pilot = Simulation(collimated_spec(200000), options=configs.C1_OPTIONS, gpu=g_sur)
+    r, t = pilot.sample_event_points(share=1.0, max_points=1 << 18)
+    assert len(r) > (1 << 17) and np.all(r > 0) and np.all((t >= 0) & (t <= np.pi / 2 + 1e-6))
+    rep = pilot.build_surrogate_points(r, t, hits_train=1024, epochs=20, hits_check=1 << 16)
+    assert rep["cells"] == 1024 and rep["flagged_fraction"] < 0.5, rep
+    sur = Simulation(spec, options=configs.C1_OPTIONS, gpu=g_sur)
+    sur.share_surrogate(pilot)
     out = sur.msim()
     tm = sur.timing()
     assert tm["surrogate_ms"] > 0
+    assert tm["surrogate_fallbacks"] < 0.05 * tm["events"], tm
     v_g, v_s = ref_out["var_red"][:, :, 0], out["var_red"][:, :, 0]
-    # the collimated detector sees the sample: the lines are there, and the
-    # network (not the integrator fallback) served most estimator events
     assert v_g.max() > 0 and (v_g > 1e-3 * v_g.max()).sum() >= 5
-    assert tm["surrogate_fallbacks"] < 0.5 * tm["events"], tm
     assert v_s.sum() == pytest.approx(v_g.sum(), rel=1e-2)
     big = v_g > 1e-3 * v_g.max()
+    np.testing.assert_allclose(v_s[big], v_g[big], rtol=3e-2)
+    for s_ in (grid, pilot, sur):
+        s_.close()
+
+
+@pytest.mark.gpu
+def test_geometric_training_and_tabulated_fallback():
+    """The geometric sampler (points uniform over the sample volume): with a
+    tolerance no cell meets, every cell of the checked region is served by its
+    tabulated integrator; the run then agrees with the grid run as closely as
+    two grids do (2%)."""
+    from xmimsim_gb300 import Simulation, configs, gpu_options
+    spec = configs.config1(n_photons_line=20000)
+    grid = Simulation(spec, options=configs.C1_OPTIONS, gpu=gpu_options(seed=0x5EED0001))
+    ref_out = grid.msim()
+    sur = Simulation(spec, options=configs.C1_OPTIONS, gpu=gpu_options(seed=0x5EED0001, use_surrogate=1,
+                                                                       surrogate_tolerance=1e-12))
+    rep = sur.build_surrogate(n_train=1 << 16, hits_train=512, epochs=2, hits_check=1 << 12)
+    assert rep["cells"] == 1024 and rep["flagged_fraction"] == 1.0, rep
+    out = sur.msim()
+    tm = sur.timing()
+    assert tm["surrogate_fallbacks"] < 0.5 * tm["events"], tm
+    v_g, v_s = ref_out["var_red"][:, :, 0], out["var_red"][:, :, 0]
+    assert v_s.sum() == pytest.approx(v_g.sum(), rel=2e-2)
+    big = v_g > 1e-2 * v_g.max()
     np.testing.assert_allclose(v_s[big], v_g[big], rtol=3e-2)
     grid.close()
     sur.close()
@@ -206,29 +233,3 @@ def test_shared_surrogate_in_a_batch_matches_single_runs():
     for s in sims + [odd]:
         s.close()
 
-
-@pytest.mark.gpu
-def test_surrogate_trained_where_the_estimator_queries():
-    """Training points from a pilot run (the (r, theta) of the estimator's own
-    solid-angle queries): on the collimated geometry the network serves most
-    events of the production run, and its lines agree with the grid run."""
-    from xmimsim_gb300 import Simulation, configs, gpu_options
-    spec = collimated_spec(20000)
-    grid = Simulation(spec, options=configs.C1_OPTIONS, gpu=gpu_options(seed=0x5EED0001))
-    ref_out = grid.msim()
-    sur = Simulation(spec, options=configs.C1_OPTIONS, gpu=gpu_options(seed=0x5EED0001, use_surrogate=1,
-                                                                       surrogate_tolerance=2e-2))
-    r, t = sur.sample_event_points(share=0.5, max_points=1 << 17)
-    assert len(r) > (1 << 16) and np.all(r > 0) and np.all((t >= 0) & (t <= np.pi / 2 + 1e-6))
-    rep = sur.build_surrogate_points(r, t, hits_train=1024, epochs=20, hits_check=1 << 16)
-    assert rep["cells"] == 1024 and rep["flagged_fraction"] < 0.5, rep
-    out = sur.msim()
-    tm = sur.timing()
-    assert tm["surrogate_fallbacks"] < 0.5 * tm["events"], tm
-    v_g, v_s = ref_out["var_red"][:, :, 0], out["var_red"][:, :, 0]
-    assert v_g.max() > 0
-    assert v_s.sum() == pytest.approx(v_g.sum(), rel=1e-2)
-    big = v_g > 1e-3 * v_g.max()
-    np.testing.assert_allclose(v_s[big], v_g[big], rtol=3e-2)
-    grid.close()
-    sur.close()

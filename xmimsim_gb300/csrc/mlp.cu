@@ -79,7 +79,28 @@ __global__ void pack_weights(const float *theta, unsigned char *packed) {
   }
 }
 
-__device__ __forceinline__ float silu(float z) { return z / (1.0f + __expf(-z)); }
+/* logistic function as 1/2 + tanh(z/2)/2 with the hardware tanh
+ * approximation (one MUFU op, relative error about 2^-11, below the BF16
+ * rounding the activations get) -- used by inference and training alike */
+__device__ __forceinline__ float sigmoid_fast(float z) {
+  float t;
+  asm("tanh.approx.f32 %0, %1;" : "=f"(t) : "f"(0.5f * z));
+  return fmaf(0.5f, t, 0.5f);
+}
+__device__ __forceinline__ float silu(float z) { return z * sigmoid_fast(z); }
+
+/* eight consecutive activations of one row as one 16-byte store of the
+ * K-major BF16 operand tile (k0 a multiple of 8) */
+__device__ __forceinline__ void store_bf16x8(unsigned char *sm, int row, int k0, const float *h) {
+  uint4 u;
+  __nv_bfloat162 p0 = __floats2bfloat162_rn(h[0], h[1]), p1 = __floats2bfloat162_rn(h[2], h[3]);
+  __nv_bfloat162 p2 = __floats2bfloat162_rn(h[4], h[5]), p3 = __floats2bfloat162_rn(h[6], h[7]);
+  u.x = *reinterpret_cast<uint32_t *>(&p0);
+  u.y = *reinterpret_cast<uint32_t *>(&p1);
+  u.z = *reinterpret_cast<uint32_t *>(&p2);
+  u.w = *reinterpret_cast<uint32_t *>(&p3);
+  *reinterpret_cast<uint4 *>(sm + SM_A + umma::kmajor_offset(row, k0, H)) = u;
+}
 
 /* per-CTA context of the tensor-core forward pass (weights resident in
  * shared memory, one 128-column TMEM accumulator) */
@@ -128,11 +149,17 @@ __device__ void fwd_setup(unsigned char *sm, const unsigned char *packed, const 
 __device__ __forceinline__ void layer0_row(unsigned char *sm, const float *w0, const float *b0, const float *f,
                                            float *zrow, size_t zstride) {
   const int tid = threadIdx.x;
-#pragma unroll 4
-  for (int j = 0; j < H; j++) {
-    const float z = b0[j] + w0[j * NIN] * f[0] + w0[j * NIN + 1] * f[1] + w0[j * NIN + 2] * f[2];
-    if (zrow) zrow[(size_t)j * zstride] = z;
-    *(__nv_bfloat16 *)(sm + SM_A + umma::kmajor_offset(tid, j, H)) = __float2bfloat16_rn(silu(z));
+#pragma unroll 1
+  for (int j0 = 0; j0 < H; j0 += 8) {
+    float h[8];
+#pragma unroll
+    for (int u = 0; u < 8; u++) {
+      const int j = j0 + u;
+      const float z = b0[j] + w0[j * NIN] * f[0] + w0[j * NIN + 1] * f[1] + w0[j * NIN + 2] * f[2];
+      if (zrow) zrow[(size_t)j * zstride] = z;
+      h[u] = silu(z);
+    }
+    store_bf16x8(sm, tid, j0, h);
   }
 }
 
@@ -166,12 +193,13 @@ __device__ bool fwd_tile(unsigned char *sm, FwdCtx &c, const float *f, float &y)
       float v[32];
       umma::tmem_ld_32x32b_x32(c.trow + q * 32, v);
 #pragma unroll
-      for (int j = 0; j < 32; j++) {
-        const float h = silu(v[j] + c.bias[l * H + q * 32 + j]);
-        if (l < 3)
-          *(__nv_bfloat16 *)(sm + SM_A + umma::kmajor_offset(tid, q * 32 + j, H)) = __float2bfloat16_rn(h);
-        else
-          y += h * c.wo[q * 32 + j];
+      for (int j = 0; j < 32; j++) v[j] = silu(v[j] + c.bias[l * H + q * 32 + j]);
+      if (l < 3) {
+#pragma unroll
+        for (int j8 = 0; j8 < 32; j8 += 8) store_bf16x8(sm, tid, q * 32 + j8, v + j8);
+      } else {
+#pragma unroll
+        for (int j = 0; j < 32; j++) y += v[j] * c.wo[q * 32 + j];
       }
     }
   }
@@ -222,6 +250,28 @@ struct Domain {
   float eps;              /* log target = log(omega + eps) */
 };
 
+/* Flagged cells keep the integrator as their solid angle, tabulated: the
+ * integrator's values on a (kPatch + 1)^2 lattice of nodes spanning the cell
+ * in (log r, theta), interpolated bilinearly -- the reference grid's method
+ * (integrator values at nodes, bilinear in between) at a node spacing finer
+ * than its 1024 x 1024 grid over this region. */
+constexpr int kPatch = 8, kPatchNodes = (kPatch + 1) * (kPatch + 1);
+
+__host__ __device__ __forceinline__ float patch_omega(const Domain &d, const float *patch, float lr, float t, int cell) {
+  const int cr = cell % d.ncr, ct = cell / d.ncr;
+  const float dlr = (d.lr1 - d.lr0) / d.ncr, dt = (d.t1 - d.t0) / d.nct;
+  float u = (lr - (d.lr0 + cr * dlr)) / dlr * kPatch, v = (t - (d.t0 + ct * dt)) / dt * kPatch;
+  u = u < 0.0f ? 0.0f : (u > (float)kPatch ? (float)kPatch : u);
+  v = v < 0.0f ? 0.0f : (v > (float)kPatch ? (float)kPatch : v);
+  int i = (int)u, j = (int)v;
+  i = i > kPatch - 1 ? kPatch - 1 : i;
+  j = j > kPatch - 1 ? kPatch - 1 : j;
+  const float fu = u - i, fv = v - j;
+  const float *p = patch + j * (kPatch + 1) + i;
+  const float a = p[0] + fu * (p[1] - p[0]), b = p[kPatch + 1] + fu * (p[kPatch + 2] - p[kPatch + 1]);
+  return a + fv * (b - a);
+}
+
 template <typename R>
 __host__ __device__ __forceinline__ void raw_features(R r, R t, float *raw) {
   const float st = sinf((float)t);
@@ -244,15 +294,16 @@ __host__ __device__ __forceinline__ void features_of(const Domain &d, R r, R t, 
 }
 
 /* Fills the solid angle of every queued estimator event: the network on the
- * tensor cores for 128 events per tile, zero below the box's lowest theta
- * (as the grid path).  Events in flagged cells or outside the box are
- * appended to fb_list for omega_fallback_kernel. */
+ * tensor cores for 128 events per tile, the tabulated integrator in flagged
+ * cells, zero below the box's lowest theta (as the grid path).  Events
+ * outside the box are appended to fb_list for omega_fallback_kernel. */
 template <typename R>
 __global__ void __launch_bounds__(128, 1) omega_kernel(const unsigned char *packed, const float *theta, Domain dom,
                                                        const unsigned char *flags, const DevBundle<R> *bundles,
                                                        int n_cfg, VrEvent<R> *ev, const unsigned long long *count,
                                                        long long cap, unsigned long long *fallbacks, int *fb_list,
-                                                       unsigned long long *fb_count, int *err) {
+                                                       unsigned long long *fb_count, const int *patch_of,
+                                                       const float *patches, int *err) {
   extern __shared__ __align__(1024) unsigned char sm[];
   FwdCtx c;
   fwd_setup(sm, packed, theta, c);
@@ -281,8 +332,16 @@ __global__ void __launch_bounds__(128, 1) omega_kernel(const unsigned char *pack
       } else if (bundles[cfg].use_surrogate) {
         if (!(t >= (R)dom.tmin)) {
           apply = true;
-        } else if (!inside || flags[cell]) {
+        } else if (!inside) {
           need_fb = true;
+        } else if (flags[cell]) {
+          const int pc = patch_of[cell];
+          if (pc >= 0) {
+            omega = (R)patch_omega(dom, patches + (size_t)pc * kPatchNodes, logf((float)r), (float)t, cell);
+            apply = true;
+          } else {
+            need_fb = true;
+          }
         } else {
           const float o = __expf(y) - dom.eps;
           omega = (R)(o > 0.0f ? o : 0.0f);
@@ -397,7 +456,7 @@ __device__ __forceinline__ void copy_tile(unsigned char *dst, const unsigned cha
 }
 
 __device__ __forceinline__ float dsilu(float z) {
-  const float s = 1.0f / (1.0f + __expf(-z));
+  const float s = sigmoid_fast(z);
   return s * (1.0f + z * (1.0f - s));
 }
 
@@ -826,6 +885,9 @@ struct SurrogateState {
   std::vector<float> theta;
   float *theta_d = nullptr;
   unsigned char *packed_d = nullptr, *flags_d = nullptr;
+  int *patch_of_d = nullptr;  /* [ncell]: patch of a flagged cell, -1 otherwise */
+  float *patches_d = nullptr; /* [n_patch][kPatchNodes] */
+  int n_patch = 0;
   double report[6] = {0, 0, 0, 0, 0, 0};
 };
 
@@ -850,12 +912,15 @@ void xmi_surrogate_free(void *p) {
   cudaFree(sg->theta_d);
   cudaFree(sg->packed_d);
   cudaFree(sg->flags_d);
+  cudaFree(sg->patch_of_d);
+  cudaFree(sg->patches_d);
   delete sg;
 }
 
 /* Trains the solid-angle surrogate of an initialised input handle (see
  * xmi_gpu_build_surrogate in the public header for the procedure). */
 constexpr int kCells = 32, kCheckPerCell = 16, kCheckPoints = kCells * kCells * kCheckPerCell;
+constexpr int kPatchHits = 1 << 16; /* integrator samples per node of a flagged cell's table */
 
 static int build_from_points(xmi_inputFPtr in, std::vector<double> &r_h, std::vector<double> &t_h, int n_train,
                              int hits_train, int epochs, int hits_check, double *report,
@@ -1129,6 +1194,50 @@ static int build_from_points(xmi_inputFPtr in, std::vector<double> &r_h, std::ve
     sg->report[1] = worst_kept;
     sg->report[2] = (double)nflag / (ntot > 0 ? ntot : 1);
     cudaMemcpy(sg->flags_d, flags.data(), ncell, cudaMemcpyHostToDevice);
+    /* the tabulated integrator of the flagged cells, FP64, patch_hits
+     * samples per node */
+    std::vector<int> patch_of(ncell, -1);
+    std::vector<double> pr, pt;
+    for (int c = 0; c < ncell; c++) {
+      if (!flags[c]) continue;
+      patch_of[c] = sg->n_patch++;
+      const int cr = c % sg->dom.ncr, ct = c / sg->dom.ncr;
+      const double dlr = ((double)sg->dom.lr1 - sg->dom.lr0) / sg->dom.ncr;
+      const double dt = ((double)sg->dom.t1 - sg->dom.t0) / sg->dom.nct;
+      for (int j = 0; j <= kPatch; j++)
+        for (int i = 0; i <= kPatch; i++) {
+          pr.push_back(std::exp(sg->dom.lr0 + (cr + (double)i / kPatch) * dlr));
+          pt.push_back(sg->dom.t0 + (ct + (double)j / kPatch) * dt);
+        }
+    }
+    const int np = (int)pr.size();
+    ok = cudaMalloc(&sg->patch_of_d, sizeof(int) * ncell) == cudaSuccess &&
+         cudaMalloc(&sg->patches_d, sizeof(float) * (np > 0 ? np : 1)) == cudaSuccess;
+    if (ok && np > 0) {
+      double *nr_d = nullptr, *nt_d = nullptr, *no_d = nullptr;
+      ok = cudaMalloc(&nr_d, sizeof(double) * np) == cudaSuccess &&
+           cudaMalloc(&nt_d, sizeof(double) * np) == cudaSuccess &&
+           cudaMalloc(&no_d, sizeof(double) * np) == cudaSuccess;
+      if (ok) {
+        cudaMemcpy(nr_d, pr.data(), sizeof(double) * np, cudaMemcpyHostToDevice);
+        cudaMemcpy(nt_d, pt.data(), sizeof(double) * np, cudaMemcpyHostToDevice);
+        int dev = 0, sms = 1;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        const unsigned long long seed = in->gpu.seed ? in->gpu.seed : 0x5EED0001ull;
+        xmi::solid_angle_points_kernel<double><<<sms * 8, 256>>>(geom, nr_d, nt_d, np, kPatchHits,
+                                                                 seed ^ 0x165667B19E3779F9ull, no_d);
+        std::vector<double> po(np);
+        ok = cudaDeviceSynchronize() == cudaSuccess &&
+             cudaMemcpy(po.data(), no_d, sizeof(double) * np, cudaMemcpyDeviceToHost) == cudaSuccess;
+        std::vector<float> pf(po.begin(), po.end());
+        if (ok) cudaMemcpy(sg->patches_d, pf.data(), sizeof(float) * np, cudaMemcpyHostToDevice);
+      }
+      cudaFree(nr_d);
+      cudaFree(nt_d);
+      cudaFree(no_d);
+    }
+    if (ok) cudaMemcpy(sg->patch_of_d, patch_of.data(), sizeof(int) * ncell, cudaMemcpyHostToDevice);
   }
   cudaFree(r_d);
   cudaFree(t_d);
@@ -1188,7 +1297,7 @@ int xmi_surrogate_apply(const void *p, int precision, const void *dev_bundles, i
     omega_kernel<double><<<sms, 128, SM_TOTAL, st>>>(sg->packed_d, sg->theta_d, sg->dom, sg->flags_d,
                                                       (const xmi::DevBundle<double> *)dev_bundles, n_cfg,
                                                       (xmi::VrEvent<double> *)events, count, cap, fallbacks, fb_list,
-                                                      fb_count, err);
+                                                      fb_count, sg->patch_of_d, sg->patches_d, err);
     omega_fallback_kernel<double><<<sms * 8, 256, 0, st>>>((const xmi::DevBundle<double> *)dev_bundles, n_cfg,
                                                           (xmi::VrEvent<double> *)events, fb_list, fb_count, cap);
   } else {
@@ -1196,7 +1305,7 @@ int xmi_surrogate_apply(const void *p, int precision, const void *dev_bundles, i
     omega_kernel<float><<<sms, 128, SM_TOTAL, st>>>(sg->packed_d, sg->theta_d, sg->dom, sg->flags_d,
                                                      (const xmi::DevBundle<float> *)dev_bundles, n_cfg,
                                                      (xmi::VrEvent<float> *)events, count, cap, fallbacks, fb_list,
-                                                     fb_count, err);
+                                                     fb_count, sg->patch_of_d, sg->patches_d, err);
     omega_fallback_kernel<float><<<sms * 8, 256, 0, st>>>((const xmi::DevBundle<float> *)dev_bundles, n_cfg,
                                                          (xmi::VrEvent<float> *)events, fb_list, fb_count, cap);
   }
