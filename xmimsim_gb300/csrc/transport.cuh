@@ -117,12 +117,22 @@ struct PlaneWalk {
 
 template <typename R>
 __device__ __forceinline__ bool plane_walk_init(const double *p, const R *d, const double *n, PlaneWalk &w) {
-  const double dd[3] = {(double)d[0], (double)d[1], (double)d[2]};
-  const double itn = dd[0] * n[0] + dd[1] * n[1] + dd[2] * n[2];
-  if (itn == 0.0) return false;
   w.h = p[0] * n[0] + p[1] * n[1] + p[2] * n[2];
-  w.inv = 1.0 / itn;
-  w.dlen = sqrt(dd[0] * dd[0] + dd[1] * dd[1] + dd[2] * dd[2]);
+  if constexpr (sizeof(R) == 4) {
+    /* FP32 transport: the direction is FP32, so are 1/cos and |d| (relative
+     * error ~1e-7 on the steps); only the heights stay FP64.  This keeps the
+     * FP64 divide and square root, slow on this GPU, off the step */
+    const float itn = d[0] * (float)n[0] + d[1] * (float)n[1] + d[2] * (float)n[2];
+    if (itn == 0.0f) return false;
+    w.inv = (double)(1.0f / itn);
+    w.dlen = (double)sqrtf(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+  } else {
+    const double dd[3] = {(double)d[0], (double)d[1], (double)d[2]};
+    const double itn = dd[0] * n[0] + dd[1] * n[1] + dd[2] * n[2];
+    if (itn == 0.0) return false;
+    w.inv = 1.0 / itn;
+    w.dlen = sqrt(dd[0] * dd[0] + dd[1] * dd[1] + dd[2] * dd[2]);
+  }
   return true;
 }
 
@@ -366,9 +376,20 @@ __device__ R single_solid_angle(const DevBundle<R> &b, R r1, R theta1, xmi_rng *
 template <typename R>
 __device__ __forceinline__ void sa_coords(const DevBundle<R> &b, const double *coords, R &r, R &theta) {
   double dv[3] = {coords[0] - b.p_det[0], coords[1] - b.p_det[1], coords[2] - b.p_det[2]};
-  double rr = sqrt(dv[0] * dv[0] + dv[1] * dv[1] + dv[2] * dv[2]);
-  double inv = 1.0 / rr;
-  R dn[3] = {(R)(dv[0] * inv), (R)(dv[1] * inv), (R)(dv[2] * inv)};
+  R dn[3];
+  double rr;
+  if constexpr (sizeof(R) == 4) {
+    /* the offset from the detector is FP64 (a difference of positions), its
+     * length and direction FP32 */
+    const float f[3] = {(float)dv[0], (float)dv[1], (float)dv[2]};
+    const float rf = sqrtf(f[0] * f[0] + f[1] * f[1] + f[2] * f[2]), inv = 1.0f / rf;
+    rr = rf;
+    dn[0] = f[0] * inv, dn[1] = f[1] * inv, dn[2] = f[2] * inv;
+  } else {
+    rr = sqrt(dv[0] * dv[0] + dv[1] * dv[1] + dv[2] * dv[2]);
+    const double inv = 1.0 / rr;
+    dn[0] = (R)(dv[0] * inv), dn[1] = (R)(dv[1] * inv), dn[2] = (R)(dv[2] * inv);
+  }
   R nd[3] = {(R)b.n_det[0], (R)b.n_det[1], (R)b.n_det[2]};
   R tt = acos(rdot(dn, nd));
   r = (R)rr;
@@ -381,9 +402,18 @@ template <typename R>
 __device__ R get_solid_angle(const DevBundle<R> &b, const double *coords, const Photon<R> &p, const DevTally &t,
                              bool &ok) {
   double dv[3] = {coords[0] - b.p_det[0], coords[1] - b.p_det[1], coords[2] - b.p_det[2]};
-  double rr = sqrt(dv[0] * dv[0] + dv[1] * dv[1] + dv[2] * dv[2]);
-  double inv = 1.0 / rr;
-  R dn[3] = {(R)(dv[0] * inv), (R)(dv[1] * inv), (R)(dv[2] * inv)};
+  R dn[3];
+  double rr;
+  if constexpr (sizeof(R) == 4) {
+    const float f[3] = {(float)dv[0], (float)dv[1], (float)dv[2]};
+    const float rf = sqrtf(f[0] * f[0] + f[1] * f[1] + f[2] * f[2]), inv = 1.0f / rf;
+    rr = rf;
+    dn[0] = f[0] * inv, dn[1] = f[1] * inv, dn[2] = f[2] * inv;
+  } else {
+    rr = sqrt(dv[0] * dv[0] + dv[1] * dv[1] + dv[2] * dv[2]);
+    const double inv = 1.0 / rr;
+    dn[0] = (R)(dv[0] * inv), dn[1] = (R)(dv[1] * inv), dn[2] = (R)(dv[2] * inv);
+  }
   R nd[3] = {(R)b.n_det[0], (R)b.n_det[1], (R)b.n_det[2]};
   R tt = acos(rdot(dn, nd));
   R r = (R)rr;
@@ -627,7 +657,12 @@ __device__ bool vr_prologue(const DevBundle<R> &b, const Photon<R> &p, const Dev
   double total_distance;
   {
     double e0 = (double)dp[0] - lcp_d[0], e1 = (double)dp[1] - lcp_d[1], e2 = (double)dp[2] - lcp_d[2];
-    total_distance = sqrt(e0 * e0 + e1 * e1 + e2 * e2);
+    if constexpr (sizeof(R) == 4) {
+      const float f0 = (float)e0, f1 = (float)e1, f2 = (float)e2;
+      total_distance = sqrtf(f0 * f0 + f1 * f1 + f2 * f2);
+    } else {
+      total_distance = sqrt(e0 * e0 + e1 * e1 + e2 * e2);
+    }
   }
   rnorm(dirv);
   rnorm(lcd);
