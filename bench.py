@@ -69,8 +69,9 @@ def parse():
     p.add_argument("--n-train", type=int, default=1 << 21, help="integrator samples the surrogate trains on")
     p.add_argument("--epochs", type=int, default=8)
     p.add_argument("--tolerance", type=float, default=1e-3, help="surrogate held-out error limit")
+    p.add_argument("--hits-check", type=int, default=1 << 19, help="FP64 integrator samples per checking point")
     p.add_argument("--plain-grids", type=int, default=4, help="grids timed for the plain comparison")
-    p.add_argument("--tune-share", type=float, default=1.0 / 16, help="share of a step the autotuner's trials run")
+    p.add_argument("--tune-share", type=float, default=1.0 / 32, help="share of a step the autotuner's trials run")
     p.add_argument("--line-configs", type=int, default=3, help="configurations of the FP64 line-error check")
     p.add_argument("--no-plain", action="store_true")
     p.add_argument("--photons", type=float, default=1e7, help="photons per step of the plain workload")
@@ -343,7 +344,7 @@ def batched_arm(args, ws, rank, local):
         ts.append(t)
     pilot_s = time.perf_counter() - t0
     rep = sims[deep].build_surrogate_points(np.concatenate(rs), np.concatenate(ts), hits_train=1024,
-                                            epochs=args.epochs, hits_check=1 << 20)
+                                            epochs=args.epochs, hits_check=args.hits_check)
     rep["pilot_s"] = pilot_s
     rep["pilot_configs"] = len(pick)
     train_s = time.perf_counter() - t0
@@ -376,7 +377,7 @@ def batched_arm(args, ws, rank, local):
              "l2": "inputs larger than L2 (tables of 512 configurations, several GB)",
              "host_tables_s": host_tables_s, "autotuned": tune,
              "surrogate": dict(rep, n_train=args.n_train, epochs=args.epochs, tolerance=args.tolerance,
-                               wall_s=train_s)}
+                              hits_check=args.hits_check, wall_s=train_s)}
     line = {"metric": METRIC, "value": value, "unit": "histories/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ksum / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32 transport, f64 tallies",

@@ -342,3 +342,26 @@ def test_surrogate_integrator_fallback_matches_oracle():
     sur.free_raw(out)
     sur.close()
     ref.close()
+
+
+def test_thin_layers_fp32_tracks_fp64():
+    """Config 3, the precision form of config 1 (10 nm Cr and 50 nm Au over a
+    2 mm substrate): FP32 transport with FP64 plane heights against the
+    all-FP64 run on the same photon streams -- every line carrying >= 1% of
+    the strongest within 0.5%, the thin layers' own lines (Cr K, Au L)
+    included, and the channel totals within 0.5%."""
+    spec = configs.config3(n_photons_line=200000)
+    s64 = Simulation(spec, options=configs.C1_OPTIONS, gpu=gpu_options(precision=0, seed=SEED))
+    s32 = Simulation(spec, options=configs.C1_OPTIONS, gpu=gpu_options(precision=1, seed=SEED))
+    r64, r32 = s64.msim(), s32.msim()
+    v64, v32 = r64["var_red"].sum(axis=2), r32["var_red"].sum(axis=2)
+    assert v64[24 - 1, 3 - 1] > 0 and v64[79 - 1].sum() > 0  # Cr KL3 and Au L lines exist
+    big = v64 > 1e-2 * v64.max()
+    rel = np.abs(v32[big] - v64[big]) / v64[big]
+    assert rel.max() < 5e-3, (rel.max(), np.argwhere(big)[rel.argmax()])
+    for Z, line in ((24, 3), (79, 3 + 0)):
+        if v64[Z - 1, line - 1] > 1e-3 * v64.max():
+            assert v32[Z - 1, line - 1] == pytest.approx(v64[Z - 1, line - 1], rel=5e-3)
+    np.testing.assert_allclose(r32["channels"].sum(axis=1), r64["channels"].sum(axis=1), rtol=5e-3)
+    s64.close()
+    s32.close()

@@ -34,6 +34,18 @@ def config1(n_photons_line: int = 100000) -> InputSpec:
     )
 
 
+def config3(n_photons_line: int = 100000) -> InputSpec:
+    """The precision form of config 1: thin layers over a 2 mm substrate --
+    10 nm of Cr (7.19 g/cm3) and 50 nm of Au (19.3 g/cm3) on the config-1
+    sample 0.2 cm thick, behind the same 5 cm of air; the FP32 transport with
+    FP64 plane heights must resolve the 10 nm layer 100 cm from the source."""
+    spec = config1(n_photons_line=n_photons_line)
+    sample = Layer([14, 8, 26, 29, 30], [0.40, 0.50, 0.05, 0.03, 0.02], 2.5, 0.2)
+    spec.layers = [AIR, Layer([24], [1.0], 7.19, 1e-6), Layer([79], [1.0], 19.3, 5e-6), sample]
+    spec.reference_layer = 2
+    return spec
+
+
 C1_OPTIONS = dict(use_variance_reduction=1, use_escape_peaks=1, use_sum_peaks=0, use_M_lines=1,
                   use_cascade_auger=1, use_cascade_radiative=1, use_default_seeds=1)
 

@@ -29,6 +29,7 @@ struct DevBundle {
   double det_radius, coll_radius, coll_height, coll_half_apex, coll_vertex_x;
   double d_source_slit, slit_x, slit_y;
   double zbeg[XMI_MAXL], zend[XMI_MAXL];
+  R thick_n[XMI_MAXL]; /* layer thickness along the sample normal, (zend - zbeg) n_z */
   R rho[XMI_MAXL];
   int nel[XMI_MAXL], off[XMI_MAXL];
   /* sa grid metadata (uniform axes) */

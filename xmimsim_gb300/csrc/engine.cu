@@ -263,6 +263,7 @@ void fill_scalars(const xmi_bundle &h, xmi::DevBundle<R> &d) {
   for (int j = 0; j < XMI_MAXL; j++) {
     d.zbeg[j] = h.layer_zbeg[j];
     d.zend[j] = h.layer_zend[j];
+    d.thick_n[j] = (R)((h.layer_zend[j] - h.layer_zbeg[j]) * h.n_sample[2]);
     d.rho[j] = (R)h.layer_rho[j];
     d.nel[j] = h.layer_nel[j];
     d.off[j] = h.layer_off[j];

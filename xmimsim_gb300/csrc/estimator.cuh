@@ -194,13 +194,15 @@ __device__ __forceinline__ void estimate_event_uniform(const DevBundle<R> &b, co
   const R live = valid ? (R)1 : (R)0;
   R rayl_sum = (R)0; /* Rayleigh keeps the photon energy: one channel add per event */
   const ComptonEvent<R> ce = compton_event(ev.E, ev.theta);
+  /* FP32: one reciprocal per event instead of a division per element */
+  const R inv_mu = (R)1 / ev.mu_here;
 #pragma unroll
   for (int j = 0; j < XMI_MAXL; j++) s_rd[lane * XMI_MAXL + j] = ev.rd[j];
   for (int i = 0; i < nel; i++) {
     const int pair = off + i;
     const int e = XMI_LDG(b.layer_el, pair, b.n_layer_el, 9);
     const R wi = XMI_LDG(b.layer_w, pair, b.n_layer_el, 9);
-    const R pconv = wi / ev.mu_here;
+    const R pconv = sizeof(R) == 4 ? wi * inv_mu : wi / ev.mu_here;
     const int rs = b.n_lines + 2 * e;
     /* Rayleigh */
     const R twr = live * (pconv * (ev.pR * qtab(b.ff2[e], ev.q)) * ev.pesc_rayl * ev.w);
@@ -235,7 +237,7 @@ __device__ __forceinline__ void estimate_event_uniform(const DevBundle<R> &b, co
 #pragma unroll
       for (int s = 0; s < XMI_NSHELL; s++) P[s] = el_val(b, e, XMI_REC_XRF + s, ev.node, ev.f);
     }
-    const R scale = live * wi / ev.mu_here * ev.pdir_fluo * ev.w;
+    const R scale = live * (sizeof(R) == 4 ? wi * inv_mu : wi / ev.mu_here) * ev.pdir_fluo * ev.w;
 #pragma unroll
     for (int s = 0; s < XMI_NSHELL; s++)
       s_a[lane * XMI_NSHELL + s] = (s >= 4 && !b.use_M_lines) ? (R)0 : P[s] * scale;

@@ -54,14 +54,38 @@ constexpr int OFF_WO = OFF_B0 + H + 3 * (H * H + H), OFF_BO = OFF_WO + H;
 constexpr int W0_BYTES = H * KIN * 2, WL_BYTES = H * H * 2;
 constexpr int PACK_BYTES = W0_BYTES + 3 * WL_BYTES;
 
-/* shared-memory plan of the forward kernel (offsets in bytes) */
+/* The forward kernels run two independent groups of 128 threads per CTA,
+ * each with its own 128-row tile, activation tile, TMEM accumulator and
+ * mbarrier, sharing the resident weights: while one group's SiLU epilogue
+ * runs on the CUDA cores the other's MMAs run on the tensor cores. */
+constexpr int kGroups = 2, kFwdThreads = 128 * kGroups;
+
+/* shared-memory plan of the forward kernels (offsets in bytes) */
 constexpr int SM_W = 0;                           /* packed weights */
-constexpr int SM_X0 = SM_W + PACK_BYTES;          /* input tile [128 x 16] */
-constexpr int SM_A = SM_X0 + H * KIN * 2;         /* activation tile [128 x 128] */
-constexpr int SM_BIAS = SM_A + H * H * 2;         /* b0..b3 FP32 */
+constexpr int SM_X0 = SM_W + PACK_BYTES;          /* FP32 W0 of layer 0 */
+constexpr int SM_A = SM_X0 + H * KIN * 2;         /* kGroups activation tiles [128 x 128] */
+constexpr int SM_BIAS = SM_A + kGroups * H * H * 2; /* b0..b3 FP32 */
 constexpr int SM_WO = SM_BIAS + 4 * H * 4;        /* w_o FP32 */
-constexpr int SM_BAR = SM_WO + H * 4;             /* mbarrier, TMEM address */
-constexpr int SM_TOTAL = SM_BAR + 16;
+constexpr int SM_BAR = SM_WO + H * 4;             /* kGroups mbarriers, TMEM address */
+constexpr int SM_TOTAL = SM_BAR + 8 * kGroups + 16;
+static_assert(SM_TOTAL <= 227 * 1024, "forward kernel shared memory");
+
+/* barrier and vote among the 128 threads of one group (named barrier 1 + g) */
+__device__ __forceinline__ void group_sync(int g) { asm volatile("bar.sync %0, 128;" ::"r"(1 + g) : "memory"); }
+__device__ __forceinline__ bool group_any(int g, bool v) {
+  int r;
+  asm volatile(
+      "{\n"
+      ".reg .pred p, q;\n"
+      "setp.ne.b32 p, %1, 0;\n"
+      "bar.red.or.pred q, %2, 128, p;\n"
+      "selp.b32 %0, 1, 0, q;\n"
+      "}\n"
+      : "=r"(r)
+      : "r"((int)v), "r"(1 + g)
+      : "memory");
+  return r != 0;
+}
 
 /* packs the FP32 weights into BF16 K-major operand tiles */
 __global__ void pack_weights(const float *theta, unsigned char *packed) {
@@ -91,7 +115,7 @@ __device__ __forceinline__ float silu(float z) { return z * sigmoid_fast(z); }
 
 /* eight consecutive activations of one row as one 16-byte store of the
  * K-major BF16 operand tile (k0 a multiple of 8) */
-__device__ __forceinline__ void store_bf16x8(unsigned char *sm, int row, int k0, const float *h) {
+__device__ __forceinline__ void store_bf16x8(unsigned char *a_tile, int row, int k0, const float *h) {
   uint4 u;
   __nv_bfloat162 p0 = __floats2bfloat162_rn(h[0], h[1]), p1 = __floats2bfloat162_rn(h[2], h[3]);
   __nv_bfloat162 p2 = __floats2bfloat162_rn(h[4], h[5]), p3 = __floats2bfloat162_rn(h[6], h[7]);
@@ -99,7 +123,7 @@ __device__ __forceinline__ void store_bf16x8(unsigned char *sm, int row, int k0,
   u.y = *reinterpret_cast<uint32_t *>(&p1);
   u.z = *reinterpret_cast<uint32_t *>(&p2);
   u.w = *reinterpret_cast<uint32_t *>(&p3);
-  *reinterpret_cast<uint4 *>(sm + SM_A + umma::kmajor_offset(row, k0, H)) = u;
+  *reinterpret_cast<uint4 *>(a_tile + umma::kmajor_offset(row, k0, H)) = u;
 }
 
 /* per-CTA context of the tensor-core forward pass (weights resident in
@@ -107,14 +131,18 @@ __device__ __forceinline__ void store_bf16x8(unsigned char *sm, int row, int k0,
 struct FwdCtx {
   uint64_t *mbar;
   float *bias, *wo;
+  unsigned char *a_tile;  /* this group's activation tile */
   float bo;
-  uint32_t tmem, trow, s_x0, s_a, s_w, phase;
+  int g, row;             /* group, tile row of this thread */
+  uint32_t tmem, dcol, trow, s_a, s_w, phase;
 };
 
 __device__ void fwd_setup(unsigned char *sm, const unsigned char *packed, const float *theta, FwdCtx &c) {
   const int tid = threadIdx.x, warp = tid >> 5;
-  c.mbar = (uint64_t *)(sm + SM_BAR);
-  uint32_t *tmem_slot = (uint32_t *)(sm + SM_BAR + 8);
+  c.g = tid >> 7;
+  c.row = tid & 127;
+  c.mbar = (uint64_t *)(sm + SM_BAR) + c.g;
+  uint32_t *tmem_slot = (uint32_t *)(sm + SM_BAR + 8 * kGroups);
   c.bias = (float *)(sm + SM_BIAS);
   c.wo = (float *)(sm + SM_WO);
   for (int i = tid; i < PACK_BYTES / 16; i += blockDim.x) ((uint4 *)(sm + SM_W))[i] = ((const uint4 *)packed)[i];
@@ -127,9 +155,9 @@ __device__ void fwd_setup(unsigned char *sm, const unsigned char *packed, const 
   float *w0 = (float *)(sm + SM_X0);
   for (int i = tid; i < H * NIN; i += blockDim.x) w0[i] = theta[OFF_W0 + i];
   c.bo = theta[OFF_BO];
-  if (warp == 0) umma::tmem_alloc(tmem_slot, 128);
+  if (warp == 0) umma::tmem_alloc(tmem_slot, 128 * kGroups);
   if (tid == 0) {
-    umma::mbar_init(c.mbar, 1);
+    for (int g = 0; g < kGroups; g++) umma::mbar_init((uint64_t *)(sm + SM_BAR) + g, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   umma::fence_proxy_async_smem();
@@ -137,18 +165,19 @@ __device__ void fwd_setup(unsigned char *sm, const unsigned char *packed, const 
   __syncthreads();
   umma::fence_after_sync();
   c.tmem = *tmem_slot;
-  c.trow = c.tmem + ((uint32_t)(warp * 32) << 16);
-  c.s_x0 = umma::smem_u32(sm + SM_X0);
-  c.s_a = umma::smem_u32(sm + SM_A);
+  c.dcol = c.tmem + (uint32_t)(c.g * 128);
+  /* a warp reads TMEM lanes 32 (warp % 4) .. +31: its group's tile rows */
+  c.trow = c.dcol + ((uint32_t)((warp & 3) * 32) << 16);
+  c.a_tile = sm + SM_A + c.g * H * H * 2;
+  c.s_a = umma::smem_u32(c.a_tile);
   c.s_w = umma::smem_u32(sm + SM_W);
   c.phase = 0;
 }
 
 /* layer 0 of this thread's row in FP32 on the CUDA cores; BF16 activations
  * into the operand tile (and, when zrow is given, the pre-activations) */
-__device__ __forceinline__ void layer0_row(unsigned char *sm, const float *w0, const float *b0, const float *f,
-                                           float *zrow, size_t zstride) {
-  const int tid = threadIdx.x;
+__device__ __forceinline__ void layer0_row(unsigned char *a_tile, int row, const float *w0, const float *b0,
+                                           const float *f, float *zrow, size_t zstride) {
 #pragma unroll 1
   for (int j0 = 0; j0 < H; j0 += 8) {
     float h[8];
@@ -159,33 +188,32 @@ __device__ __forceinline__ void layer0_row(unsigned char *sm, const float *w0, c
       if (zrow) zrow[(size_t)j * zstride] = z;
       h[u] = silu(z);
     }
-    store_bf16x8(sm, tid, j0, h);
+    store_bf16x8(a_tile, row, j0, h);
   }
 }
 
 /* network output for this thread's feature row f (tile row = thread); all
  * 128 threads call it together; false (for every thread) when a wait ran out */
 __device__ bool fwd_tile(unsigned char *sm, FwdCtx &c, const float *f, float &y) {
-  const int tid = threadIdx.x;
   const uint32_t idesc = umma::idesc_bf16_f32(128, 128);
-  layer0_row(sm, (const float *)(sm + SM_X0), c.bias, f, nullptr, 0);
+  layer0_row(c.a_tile, c.row, (const float *)(sm + SM_X0), c.bias, f, nullptr, 0);
   y = c.bo;
   for (int l = 1; l < 4; l++) {
     umma::fence_proxy_async_smem();
     umma::fence_before_sync();
-    __syncthreads();
-    if (tid == 0) {
+    group_sync(c.g);
+    if (c.row == 0) {
       umma::fence_after_sync();
       const uint32_t wl = c.s_w + W0_BYTES + (l - 1) * WL_BYTES;
 #pragma unroll
       for (int kk = 0; kk < H / 16; kk++)
-        umma::mma_bf16(c.tmem, umma::smem_desc(c.s_a + kk * 256, 128, 2048), umma::smem_desc(wl + kk * 256, 128, 2048),
+        umma::mma_bf16(c.dcol, umma::smem_desc(c.s_a + kk * 256, 128, 2048), umma::smem_desc(wl + kk * 256, 128, 2048),
                        idesc, kk > 0);
       umma::mma_commit(c.mbar);
     }
     const bool ok = umma::mbar_wait(c.mbar, c.phase);
     c.phase ^= 1u;
-    if (__syncthreads_or(!ok)) return false;
+    if (group_any(c.g, !ok)) return false;
     umma::fence_after_sync();
     /* epilogue of layer l: bias, SiLU; the next layer's operand or the output */
 #pragma unroll 1
@@ -196,7 +224,7 @@ __device__ bool fwd_tile(unsigned char *sm, FwdCtx &c, const float *f, float &y)
       for (int j = 0; j < 32; j++) v[j] = silu(v[j] + c.bias[l * H + q * 32 + j]);
       if (l < 3) {
 #pragma unroll
-        for (int j8 = 0; j8 < 32; j8 += 8) store_bf16x8(sm, tid, q * 32 + j8, v + j8);
+        for (int j8 = 0; j8 < 32; j8 += 8) store_bf16x8(c.a_tile, c.row, q * 32 + j8, v + j8);
       } else {
 #pragma unroll
         for (int j = 0; j < 32; j++) y += v[j] * c.wo[q * 32 + j];
@@ -209,19 +237,19 @@ __device__ bool fwd_tile(unsigned char *sm, FwdCtx &c, const float *f, float &y)
 __device__ void fwd_teardown(FwdCtx &c) {
   umma::fence_before_sync();
   __syncthreads();
-  if ((threadIdx.x >> 5) == 0) umma::tmem_dealloc(c.tmem, 128);
+  if ((threadIdx.x >> 5) == 0) umma::tmem_dealloc(c.tmem, 128 * kGroups);
 }
 
 /* features [n][3] (already scaled) -> out [n] = network output (log solid
  * angle); *err set non-zero when a wait ran out */
-__global__ void __launch_bounds__(128, 1) forward_kernel(const unsigned char *packed, const float *theta,
-                                                         const float *features, float *out, int n, int *err) {
+__global__ void __launch_bounds__(kFwdThreads, 1) forward_kernel(const unsigned char *packed, const float *theta,
+                                                                 const float *features, float *out, int n, int *err) {
   extern __shared__ __align__(1024) unsigned char sm[];
   FwdCtx c;
   fwd_setup(sm, packed, theta, c);
   bool failed = false;
-  for (int tile = blockIdx.x; tile * 128 < n; tile += gridDim.x) {
-    const int row = tile * 128 + threadIdx.x;
+  for (int tile = blockIdx.x * kGroups + c.g; tile * 128 < n; tile += gridDim.x * kGroups) {
+    const int row = tile * 128 + c.row;
     const bool valid = row < n;
     float f[NIN], y;
     for (int k = 0; k < NIN; k++) f[k] = valid ? features[(size_t)row * NIN + k] : 0.0f;
@@ -231,7 +259,7 @@ __global__ void __launch_bounds__(128, 1) forward_kernel(const unsigned char *pa
     }
     if (valid) out[row] = y;
   }
-  if (failed && threadIdx.x == 0) atomicExch(err, 1);
+  if (failed && c.row == 0) atomicExch(err, 1);
   fwd_teardown(c);
 }
 
@@ -298,7 +326,7 @@ __host__ __device__ __forceinline__ void features_of(const Domain &d, R r, R t, 
  * cells, zero below the box's lowest theta (as the grid path).  Events
  * outside the box are appended to fb_list for omega_fallback_kernel. */
 template <typename R>
-__global__ void __launch_bounds__(128, 1) omega_kernel(const unsigned char *packed, const float *theta, Domain dom,
+__global__ void __launch_bounds__(kFwdThreads, 1) omega_kernel(const unsigned char *packed, const float *theta, Domain dom,
                                                        const unsigned char *flags, const DevBundle<R> *bundles,
                                                        int n_cfg, VrEvent<R> *ev, const unsigned long long *count,
                                                        long long cap, unsigned long long *fallbacks, int *fb_list,
@@ -309,8 +337,8 @@ __global__ void __launch_bounds__(128, 1) omega_kernel(const unsigned char *pack
   fwd_setup(sm, packed, theta, c);
   const long long n = (long long)*count < cap ? (long long)*count : cap;
   bool failed = false;
-  for (long long tile = blockIdx.x; tile * 128 < n; tile += gridDim.x) {
-    const long long i = tile * 128 + threadIdx.x;
+  for (long long tile = (long long)blockIdx.x * kGroups + c.g; tile * 128 < n; tile += (long long)gridDim.x * kGroups) {
+    const long long i = tile * 128 + c.row;
     const bool valid = i < n;
     const R r = valid ? ev[i].sa_r : (R)1, t = valid ? ev[i].sa_t : (R)dom.tmin;
     float f[NIN], y;
@@ -368,7 +396,7 @@ __global__ void __launch_bounds__(128, 1) omega_kernel(const unsigned char *pack
       ev[i].pdir_fluo *= omega;
     }
   }
-  if (failed && threadIdx.x == 0) atomicExch(err, 1);
+  if (failed && c.row == 0) atomicExch(err, 1);
   fwd_teardown(c);
 }
 
@@ -823,7 +851,7 @@ int xmi_gpu_mlp_forward(const float *theta, int n, const float *features, float 
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const int tiles = (n + 127) / 128;
-    forward_kernel<<<tiles < sms ? tiles : sms, 128, SM_TOTAL>>>(d_pack, d_theta, d_feat, d_out, n, d_err);
+    forward_kernel<<<tiles < sms ? tiles : sms, kFwdThreads, SM_TOTAL>>>(d_pack, d_theta, d_feat, d_out, n, d_err);
     cudaError_t e = cudaDeviceSynchronize();
     if (e != cudaSuccess) {
       xmi_set_error("xmi_gpu_mlp_forward: %s", cudaGetErrorString(e));
@@ -899,7 +927,7 @@ bool device_forward(const SurrogateState &sg, const float *feat_d, float *out_d,
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   const int tiles = (n + 127) / 128;
-  forward_kernel<<<tiles < sms ? tiles : sms, 128, SM_TOTAL>>>(sg.packed_d, sg.theta_d, feat_d, out_d, n, err_d);
+  forward_kernel<<<tiles < sms ? tiles : sms, kFwdThreads, SM_TOTAL>>>(sg.packed_d, sg.theta_d, feat_d, out_d, n, err_d);
   return cudaDeviceSynchronize() == cudaSuccess;
 }
 }  // namespace
@@ -1294,7 +1322,7 @@ int xmi_surrogate_apply(const void *p, int precision, const void *dev_bundles, i
   cudaStream_t st = (cudaStream_t)stream;
   if (precision == 0) {
     cudaFuncSetAttribute(omega_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, SM_TOTAL);
-    omega_kernel<double><<<sms, 128, SM_TOTAL, st>>>(sg->packed_d, sg->theta_d, sg->dom, sg->flags_d,
+    omega_kernel<double><<<sms, kFwdThreads, SM_TOTAL, st>>>(sg->packed_d, sg->theta_d, sg->dom, sg->flags_d,
                                                       (const xmi::DevBundle<double> *)dev_bundles, n_cfg,
                                                       (xmi::VrEvent<double> *)events, count, cap, fallbacks, fb_list,
                                                       fb_count, sg->patch_of_d, sg->patches_d, err);
@@ -1302,7 +1330,7 @@ int xmi_surrogate_apply(const void *p, int precision, const void *dev_bundles, i
                                                           (xmi::VrEvent<double> *)events, fb_list, fb_count, cap);
   } else {
     cudaFuncSetAttribute(omega_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, SM_TOTAL);
-    omega_kernel<float><<<sms, 128, SM_TOTAL, st>>>(sg->packed_d, sg->theta_d, sg->dom, sg->flags_d,
+    omega_kernel<float><<<sms, kFwdThreads, SM_TOTAL, st>>>(sg->packed_d, sg->theta_d, sg->dom, sg->flags_d,
                                                      (const xmi::DevBundle<float> *)dev_bundles, n_cfg,
                                                      (xmi::VrEvent<float> *)events, count, cap, fallbacks, fb_list,
                                                      fb_count, sg->patch_of_d, sg->patches_d, err);

@@ -144,6 +144,30 @@ __device__ __forceinline__ double plane_walk(PlaneWalk &w, double zp, const doub
   return s;
 }
 
+/* Path length from the walk's position through layer j toward its far
+ * boundary (up: zend[j], down: zbeg[j]), the walk moving onto it.  FP64 for
+ * the first boundary (a difference of heights ~100 cm from the origin), then,
+ * in the FP32 transport, the layers' own thicknesses along the normal times
+ * 1/cos in FP32: one FP64 subtraction per walk instead of three FP64 ops
+ * per crossed boundary. */
+template <typename R>
+__device__ __forceinline__ double layer_path(const DevBundle<R> &b, PlaneWalk &w, int j, bool up, bool &first) {
+  if constexpr (sizeof(R) == 4) {
+    float s;
+    if (first) {
+      const double P = (up ? b.zend[j] : b.zbeg[j]) * b.n_sample[2];
+      s = (float)(P - w.h) * (float)w.inv;
+      first = false;
+    } else {
+      s = (float)b.thick_n[j] * (float)w.inv;
+    }
+    return (double)(fabsf(s) * (float)w.dlen);
+  } else {
+    first = false;
+    return fabs(plane_walk(w, up ? b.zend[j] : b.zbeg[j], b.n_sample)) * w.dlen;
+  }
+}
+
 /* uniform draw in the working precision; FP32 uses the rounded FP64 draw so
  * that FP32 and FP64 runs consume identical random sequences */
 template <typename R> __device__ __forceinline__ R uni(xmi_rng *g);
@@ -301,7 +325,9 @@ __device__ __forceinline__ void tally_add(double *addr, double v) {
  * evaluated in the working precision */
 template <typename R>
 __device__ __forceinline__ int channel_of(const DevBundle<R> &b, R E) {
-  return (int)((E - (R)b.zero) / (R)b.gain);
+  /* FP32: a multiply by 1/gain (a channel edge may move by an ulp) */
+  if constexpr (sizeof(R) == 4) return (int)((E - (R)b.zero) * (R)(1.0 / b.gain));
+  else return (int)((E - (R)b.zero) / (R)b.gain);
 }
 
 template <typename R>
@@ -583,7 +609,10 @@ __device__ __forceinline__ R compton_energy_est(const DevBundle<R> &b, int e, co
     }
     if (uni<R>(g) < (R)0.5) pz = -pz;
     const R dlamb = ce.k0 - ce.k1 * pz;
-    if (dlamb >= (R)0) return c / (ce.c_lamb0 + dlamb) / (R)1000;
+    if (dlamb >= (R)0) {
+      if constexpr (sizeof(R) == 4) return (c / (R)1000) / (ce.c_lamb0 + dlamb); /* one division */
+      else return c / (ce.c_lamb0 + dlamb) / (R)1000;
+    }
     if (it == 100) break;
     it++;
   }
@@ -696,11 +725,11 @@ __device__ bool vr_prologue(const DevBundle<R> &b, const Photon<R> &p, const Dev
   {
     PlaneWalk pw;
     if (!plane_walk_init(p.c, ndc, b.n_sample, pw)) { ok = false; return false; }
-    bool done = false;
+    bool done = false, first = true;
     layers_in_direction(up, [&](int j) {
       bool active = up ? (j >= layer && j < b.n_layers) : (j <= layer);
       if (active && !done) {
-        const double dd = fabs(plane_walk(pw, up ? b.zend[j] : b.zbeg[j], b.n_sample)) * pw.dlen;
+        const double dd = layer_path(b, pw, j, up, first);
         if (dd > total_distance) {
           ev.rd[j] = b.rho[j] * (R)total_distance;
           done = true;
@@ -1083,11 +1112,12 @@ __device__ int step_photon(const DevBundle<R> &b, Photon<R> &p, const DevTally &
     const int cur = p.layer;
     PlaneWalk pw;
     if (!plane_walk_init(p.c, p.d, b.n_sample, pw)) return kStepError;
+    bool first = true;
     layers_in_direction(up, [&](int j) {
       bool active = up ? (j >= cur && j < b.n_layers) : (j <= cur);
       dist[j] = (R)0;
       if (active) {
-        dist[j] = (R)(fabs(plane_walk(pw, up ? b.zend[j] : b.zbeg[j], b.n_sample)) * pw.dlen);
+        dist[j] = (R)layer_path(b, pw, j, up, first);
         pabs = pabs + p.mus[j] * b.rho[j] * dist[j];
       }
     });
