@@ -876,13 +876,13 @@ static bool stage_run(DevState *s, xmi::DevBundle<R> &d, const xmi_bundle &h, xm
  * rows of a CTA fit shared memory (layers that need more run per-lane) */
 template <typename R>
 static int stage_cap_for(int stage_max) {
-  const int limit = (int)(200 * 1024 / (8 * sizeof(R))) - xmi::kScratchPerWarp;
+  const int limit = (int)(200 * 1024 / (8 * sizeof(R))) - xmi::scratch_per_warp<R>();
   return stage_max < limit ? stage_max : limit;
 }
 
 template <typename R>
 static int estimator_blocks(int stage_cap, size_t *smem) {
-  *smem = (size_t)8 * (stage_cap + xmi::kScratchPerWarp) * sizeof(R);
+  *smem = (size_t)8 * (stage_cap + xmi::scratch_per_warp<R>()) * sizeof(R);
   if (*smem > 48 * 1024)
     cudaFuncSetAttribute(xmi::estimator_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)*smem);
   int per_sm = 1;
