@@ -253,6 +253,15 @@ void fill_scalars(const xmi_bundle &h, xmi::DevBundle<R> &d) {
     d.det_inv[k] = h.det_inv[k];
   }
   d.det_radius = h.det_radius;
+  d.det_radius_r = (R)h.det_radius;
+  for (int k = 0; k < 3; k++) {
+    d.n_sample_r[k] = (R)h.n_sample[k];
+    d.n_det_r[k] = (R)h.n_det[k];
+  }
+  for (int k = 0; k < 9; k++) {
+    d.det_new_r[k] = (R)h.det_new[k];
+    d.det_inv_r[k] = (R)h.det_inv[k];
+  }
   d.coll_radius = h.coll_radius;
   d.coll_height = h.coll_height;
   d.coll_half_apex = h.coll_half_apex;
@@ -876,13 +885,13 @@ static bool stage_run(DevState *s, xmi::DevBundle<R> &d, const xmi_bundle &h, xm
  * rows of a CTA fit shared memory (layers that need more run per-lane) */
 template <typename R>
 static int stage_cap_for(int stage_max) {
-  const int limit = (int)(200 * 1024 / (8 * sizeof(R))) - xmi::scratch_per_warp<R>();
+  const int limit = (int)(200 * 1024 / (8 * sizeof(R))) - xmi::kScratchPerWarp;
   return stage_max < limit ? stage_max : limit;
 }
 
 template <typename R>
 static int estimator_blocks(int stage_cap, size_t *smem) {
-  *smem = (size_t)8 * (stage_cap + xmi::scratch_per_warp<R>()) * sizeof(R);
+  *smem = (size_t)8 * (stage_cap + xmi::kScratchPerWarp) * sizeof(R);
   if (*smem > 48 * 1024)
     cudaFuncSetAttribute(xmi::estimator_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)*smem);
   int per_sm = 1;

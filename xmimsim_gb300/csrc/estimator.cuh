@@ -173,18 +173,9 @@ __device__ __forceinline__ void estimate_event(const DevBundle<R> &b, const DevT
   if (valid) chan_add(b, t, n, ev.E, rayl_sum);
 }
 
-/* Line loops are run for groups of up to kLineGroup consecutive elements of
- * the layer whose line entries together fit one 32-lane pass (FP32; FP64
- * keeps one element per pass to keep its shared memory, and occupancy,
- * as it was): elements with a handful of lines no longer leave most lanes
- * idle. */
-template <typename R>
-__host__ __device__ constexpr int line_group() { return sizeof(R) == 4 ? 4 : 1; }
-
 /* per-warp scratch of the uniform path: the 32 events' path sums rho*d per
- * layer and, per element of the open group, shell probability x event scale */
-template <typename R>
-__host__ __device__ constexpr int scratch_per_warp() { return 32 * XMI_MAXL + 32 * XMI_NSHELL * line_group<R>(); }
+ * layer and, per element, shell probability x event scale */
+constexpr int kScratchPerWarp = 32 * XMI_MAXL + 32 * XMI_NSHELL;
 
 /* The estimator for the 32 events of a warp that share configuration, layer
  * and order.  Elements: lane = event, as in the per-lane path, contributions
@@ -205,8 +196,6 @@ __device__ __forceinline__ void estimate_event_uniform(const DevBundle<R> &b, co
   const ComptonEvent<R> ce = compton_event(ev.E, ev.theta);
   /* FP32: one reciprocal per event instead of a division per element */
   const R inv_mu = (R)1 / ev.mu_here;
-  constexpr int G = line_group<R>(), SA = G * XMI_NSHELL;
-  int ga = 0, gk0 = XMI_LDG(b.ent_off, off, b.n_layer_el + 1, 15); /* open group: first element, first entry */
 #pragma unroll
   for (int j = 0; j < XMI_MAXL; j++) s_rd[lane * XMI_MAXL + j] = ev.rd[j];
   for (int i = 0; i < nel; i++) {
@@ -237,7 +226,7 @@ __device__ __forceinline__ void estimate_event_uniform(const DevBundle<R> &b, co
     }
     contribute<R, true>(t, st, st.n_line + 2 * i + 1, hbase + rs + 1, twc);
     if (valid) chan_add(b, t, n, ec, twc);
-    /* shell factors of this event for element i, in slot g of the group */
+    /* shell factors of this event for element i */
     R P[XMI_NSHELL];
     if (ev.h_slot >= 0) {
 #pragma unroll
@@ -249,30 +238,16 @@ __device__ __forceinline__ void estimate_event_uniform(const DevBundle<R> &b, co
       for (int s = 0; s < XMI_NSHELL; s++) P[s] = el_val(b, e, XMI_REC_XRF + s, ev.node, ev.f);
     }
     const R scale = live * (sizeof(R) == 4 ? wi * inv_mu : wi / ev.mu_here) * ev.pdir_fluo * ev.w;
-    const int gslot = i - ga;
 #pragma unroll
     for (int s = 0; s < XMI_NSHELL; s++)
-      s_a[lane * SA + gslot * XMI_NSHELL + s] = (s >= 4 && !b.use_M_lines) ? (R)0 : P[s] * scale;
-    /* run the group's lines when the next element would not fit */
-    const int k_end = XMI_LDG(b.ent_off, pair + 1, b.n_layer_el + 1, 15);
-    const bool flush = i + 1 == nel || gslot + 1 == G ||
-                       XMI_LDG(b.ent_off, pair + 2, b.n_layer_el + 1, 15) - gk0 > 32;
-    if (!flush) continue;
+      s_a[lane * XMI_NSHELL + s] = (s >= 4 && !b.use_M_lines) ? (R)0 : P[s] * scale;
     __syncwarp();
-    /* element boundaries within the group: entry k belongs to slot gs */
-    int bnd[G];
-#pragma unroll
-    for (int u = 1; u < G; u++)
-      bnd[u] = ga + u <= i ? XMI_LDG(b.ent_off, off + ga + u, b.n_layer_el + 1, 15) : 0x7fffffff;
-    /* lines of the group: lane = entry */
-    for (int kb = gk0; kb < k_end; kb += 32) {
+    /* lines of element i: lane = entry */
+    const int k0 = XMI_LDG(b.ent_off, pair, b.n_layer_el + 1, 15), k1 = XMI_LDG(b.ent_off, pair + 1, b.n_layer_el + 1, 15);
+    for (int kb = k0; kb < k1; kb += 32) {
       const int k = kb + lane;
-      if (k < k_end) {
-        int gs = 0;
-#pragma unroll
-        for (int u = 1; u < G; u++) gs += k >= bnd[u] ? 1 : 0;
+      if (k < k1) {
         const int sh = XMI_LDG(b.ent_shell, k, b.n_ent, 16);
-        const int sa = gs * XMI_NSHELL + sh;
         R pmu[XMI_MAXL];
 #ifndef XMI_CHECKED
         if constexpr (sizeof(R) == 4 && XMI_MAXL == 8) {
@@ -293,14 +268,12 @@ __device__ __forceinline__ void estimate_event_uniform(const DevBundle<R> &b, co
           R murhod = (R)0;
 #pragma unroll
           for (int j = 0; j < XMI_MAXL; j++) murhod += pmu[j] * s_rd[q * XMI_MAXL + j];
-          acc += s_a[q * SA + sa] * exp(-murhod);
+          acc += s_a[q * XMI_NSHELL + sh] * exp(-murhod);
         }
         st.v[k - st.k_first] += acc * XMI_LDG(b.ent_coef, k, b.n_ent, 16);
       }
     }
     __syncwarp();
-    ga = i + 1;
-    gk0 = k_end;
   }
   if (valid) chan_add(b, t, n, ev.E, rayl_sum);
 }
@@ -343,7 +316,7 @@ __global__ void __launch_bounds__(256, 3) estimator_kernel(const DevBundle<R> *b
                                                            unsigned long long *flags) {
   extern __shared__ unsigned char stage_mem[];
   StageRow<R> st;
-  st.v = (R *)stage_mem + (size_t)(threadIdx.x >> 5) * (stage_cap + scratch_per_warp<R>());
+  st.v = (R *)stage_mem + (size_t)(threadIdx.x >> 5) * (stage_cap + kScratchPerWarp);
   R *scratch = st.v + stage_cap;
   const int lane = threadIdx.x & 31;
   for (int j = lane; j < stage_cap; j += 32) st.v[j] = (R)0;

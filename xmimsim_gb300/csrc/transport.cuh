@@ -80,6 +80,11 @@ template <typename R> __device__ __forceinline__ void matvec(const double *m, co
   r[1] = (R)m[3] * v[0] + (R)m[4] * v[1] + (R)m[5] * v[2];
   r[2] = (R)m[6] * v[0] + (R)m[7] * v[1] + (R)m[8] * v[2];
 }
+template <typename R> __device__ __forceinline__ void matvec_r(const R *m, const R *v, R *r) {
+  r[0] = m[0] * v[0] + m[1] * v[1] + m[2] * v[2];
+  r[1] = m[3] * v[0] + m[4] * v[1] + m[5] * v[2];
+  r[2] = m[6] * v[0] + m[7] * v[1] + m[8] * v[2];
+}
 __device__ __forceinline__ void matvec_d(const double *m, const double *v, double *r) {
   r[0] = m[0] * v[0] + m[1] * v[1] + m[2] * v[2];
   r[1] = m[3] * v[0] + m[4] * v[1] + m[5] * v[2];
@@ -113,19 +118,24 @@ __device__ __forceinline__ bool plane_step(const double *p, const R *d, const do
  * same quantity). */
 struct PlaneWalk {
   double h, inv, dlen;
+  float invf, dlenf; /* FP32 transport: the same in FP32 */
 };
 
 template <typename R>
-__device__ __forceinline__ bool plane_walk_init(const double *p, const R *d, const double *n, PlaneWalk &w) {
+__device__ __forceinline__ bool plane_walk_init(const double *p, const R *d, const double *n, PlaneWalk &w,
+                                                const R *nr = nullptr) {
   w.h = p[0] * n[0] + p[1] * n[1] + p[2] * n[2];
   if constexpr (sizeof(R) == 4) {
     /* FP32 transport: the direction is FP32, so are 1/cos and |d| (relative
      * error ~1e-7 on the steps); only the heights stay FP64.  This keeps the
      * FP64 divide and square root, slow on this GPU, off the step */
-    const float itn = d[0] * (float)n[0] + d[1] * (float)n[1] + d[2] * (float)n[2];
+    const float itn = nr ? d[0] * nr[0] + d[1] * nr[1] + d[2] * nr[2]
+                         : d[0] * (float)n[0] + d[1] * (float)n[1] + d[2] * (float)n[2];
     if (itn == 0.0f) return false;
-    w.inv = (double)(1.0f / itn);
-    w.dlen = (double)sqrtf(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+    w.invf = 1.0f / itn;
+    w.dlenf = sqrtf(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+    w.inv = (double)w.invf;
+    w.dlen = (double)w.dlenf;
   } else {
     const double dd[3] = {(double)d[0], (double)d[1], (double)d[2]};
     const double itn = dd[0] * n[0] + dd[1] * n[1] + dd[2] * n[2];
@@ -156,12 +166,12 @@ __device__ __forceinline__ double layer_path(const DevBundle<R> &b, PlaneWalk &w
     float s;
     if (first) {
       const double P = (up ? b.zend[j] : b.zbeg[j]) * b.n_sample[2];
-      s = (float)(P - w.h) * (float)w.inv;
+      s = (float)(P - w.h) * w.invf;
       first = false;
     } else {
-      s = (float)b.thick_n[j] * (float)w.inv;
+      s = (float)b.thick_n[j] * w.invf;
     }
-    return (double)(fabsf(s) * (float)w.dlen);
+    return (double)(fabsf(s) * w.dlenf);
   } else {
     first = false;
     return fabs(plane_walk(w, up ? b.zend[j] : b.zbeg[j], b.n_sample)) * w.dlen;
@@ -416,7 +426,7 @@ __device__ __forceinline__ void sa_coords(const DevBundle<R> &b, const double *c
     const double inv = 1.0 / rr;
     dn[0] = (R)(dv[0] * inv), dn[1] = (R)(dv[1] * inv), dn[2] = (R)(dv[2] * inv);
   }
-  R nd[3] = {(R)b.n_det[0], (R)b.n_det[1], (R)b.n_det[2]};
+  const R *nd = b.n_det_r;
   R tt = acos(rdot(dn, nd));
   r = (R)rr;
   if (tt > (R)(kPi / 2.0)) tt = (R)kPi - tt;
@@ -440,7 +450,7 @@ __device__ R get_solid_angle(const DevBundle<R> &b, const double *coords, const 
     const double inv = 1.0 / rr;
     dn[0] = (R)(dv[0] * inv), dn[1] = (R)(dv[1] * inv), dn[2] = (R)(dv[2] * inv);
   }
-  R nd[3] = {(R)b.n_det[0], (R)b.n_det[1], (R)b.n_det[2]};
+  const R *nd = b.n_det_r;
   R tt = acos(rdot(dn, nd));
   R r = (R)rr;
   if (tt > (R)(kPi / 2.0)) tt = (R)kPi - tt;
@@ -672,31 +682,34 @@ __device__ bool vr_prologue(const DevBundle<R> &b, const Photon<R> &p, const Dev
   const int n = p.n_int, layer = p.layer;
   xmi_rng g;
   xmi_rng_init(&g, b.seed, (uint64_t)p.id, vr_stream(n, 0xFF));
-  R radius = sqrt(uni<R>(&g)) * (R)b.det_radius;
+  R radius = sqrt(uni<R>(&g)) * b.det_radius_r;
   R ang = (R)(2.0 * kPi) * uni<R>(&g);
   R dp[3] = {(R)0, cos(ang) * radius, sin(ang) * radius};
   double rel[3] = {p.c[0] - b.p_det[0], p.c[1] - b.p_det[1], p.c[2] - b.p_det[2]};
-  double lcp_d[3];
-  matvec_d(b.det_inv, rel, lcp_d);
-  R lcp[3] = {(R)lcp_d[0], (R)lcp_d[1], (R)lcp_d[2]};
+  R lcp[3];
+  double total_distance;
+  if constexpr (sizeof(R) == 4) {
+    /* the offset from the detector is FP64 (a difference of positions), its
+     * detector-frame coordinates and length FP32 */
+    const float relf[3] = {(float)rel[0], (float)rel[1], (float)rel[2]};
+    matvec_r(b.det_inv_r, relf, lcp);
+    const float f0 = dp[0] - lcp[0], f1 = dp[1] - lcp[1], f2 = dp[2] - lcp[2];
+    total_distance = sqrtf(f0 * f0 + f1 * f1 + f2 * f2);
+  } else {
+    double lcp_d[3];
+    matvec_d(b.det_inv, rel, lcp_d);
+    lcp[0] = (R)lcp_d[0], lcp[1] = (R)lcp_d[1], lcp[2] = (R)lcp_d[2];
+    double e0 = (double)dp[0] - lcp_d[0], e1 = (double)dp[1] - lcp_d[1], e2 = (double)dp[2] - lcp_d[2];
+    total_distance = sqrt(e0 * e0 + e1 * e1 + e2 * e2);
+  }
   R dirv[3];
-  matvec(b.det_inv, p.d, dirv);
+  matvec_r(b.det_inv_r, p.d, dirv);
   R lcd[3] = {dp[0] - lcp[0], dp[1] - lcp[1], dp[2] - lcp[2]};
   if (lcd[0] >= (R)0) return false;
-  double total_distance;
-  {
-    double e0 = (double)dp[0] - lcp_d[0], e1 = (double)dp[1] - lcp_d[1], e2 = (double)dp[2] - lcp_d[2];
-    if constexpr (sizeof(R) == 4) {
-      const float f0 = (float)e0, f1 = (float)e1, f2 = (float)e2;
-      total_distance = sqrtf(f0 * f0 + f1 * f1 + f2 * f2);
-    } else {
-      total_distance = sqrt(e0 * e0 + e1 * e1 + e2 * e2);
-    }
-  }
   rnorm(dirv);
   rnorm(lcd);
   R ndc[3];
-  matvec(b.det_new, lcd, ndc);
+  matvec_r(b.det_new_r, lcd, ndc);
   R dotprod = rdot(dirv, lcd);
   dotprod = dotprod > (R)1 ? (R)1 : (dotprod < (R)-1 ? (R)-1 : dotprod);
   const R theta = acos(dotprod);
@@ -716,7 +729,7 @@ __device__ bool vr_prologue(const DevBundle<R> &b, const Photon<R> &p, const Dev
   }
   dotprod = dotprod > (R)1 ? (R)1 : (dotprod < (R)-1 ? (R)-1 : dotprod);
   const R phi = acos(dotprod);
-  R nsam[3] = {(R)b.n_sample[0], (R)b.n_sample[1], (R)b.n_sample[2]};
+  const R *nsam = b.n_sample_r;
   const bool up = rdot(ndc, nsam) > (R)0;
 
   /* path toward the detector point through the layers, as density x length */
@@ -724,7 +737,7 @@ __device__ bool vr_prologue(const DevBundle<R> &b, const Photon<R> &p, const Dev
   for (int j = 0; j < XMI_MAXL; j++) ev.rd[j] = (R)0;
   {
     PlaneWalk pw;
-    if (!plane_walk_init(p.c, ndc, b.n_sample, pw)) { ok = false; return false; }
+    if (!plane_walk_init(p.c, ndc, b.n_sample, pw, b.n_sample_r)) { ok = false; return false; }
     bool done = false, first = true;
     layers_in_direction(up, [&](int j) {
       bool active = up ? (j >= layer && j < b.n_layers) : (j <= layer);
@@ -1056,7 +1069,7 @@ __device__ int step_photon(const DevBundle<R> &b, Photon<R> &p, const DevTally &
   if (p.E < (R)kEnergyThreshold) return kStepDone;
   p.inside = 0;
   xmi_rng_init(&g, b.seed, (uint64_t)p.id, (uint32_t)(p.n_int + 1));
-  R dn[3] = {(R)b.n_sample[0], (R)b.n_sample[1], (R)b.n_sample[2]};
+  const R *dn = b.n_sample_r;
   const bool up = rdot(p.d, dn) > (R)0;
   const R R0 = uni<R>(&g);
   if ((b.escape_mode == 1 && p.n_int == 1) || (b.use_vr == 0 && b.escape_mode == 0)) {
@@ -1064,7 +1077,7 @@ __device__ int step_photon(const DevBundle<R> &b, Photon<R> &p, const DevTally &
     bool stop = false;
     int outcome = 0; /* 0 continue, 1 photon absorbed by collimator/bad hit, 2 detector hit, 3 error */
     PlaneWalk pw;
-    if (!plane_walk_init(p.c, p.d, b.n_sample, pw)) return kStepError;
+    if (!plane_walk_init(p.c, p.d, b.n_sample, pw, b.n_sample_r)) return kStepError;
     layers_in_direction(up, [&](int j) {
       bool active = up ? (j >= p.layer && j < b.n_layers) : (j <= p.layer);
       if (!active || stop) return;
@@ -1111,7 +1124,7 @@ __device__ int step_photon(const DevBundle<R> &b, Photon<R> &p, const DevTally &
     R pabs = (R)0;
     const int cur = p.layer;
     PlaneWalk pw;
-    if (!plane_walk_init(p.c, p.d, b.n_sample, pw)) return kStepError;
+    if (!plane_walk_init(p.c, p.d, b.n_sample, pw, b.n_sample_r)) return kStepError;
     bool first = true;
     layers_in_direction(up, [&](int j) {
       bool active = up ? (j >= cur && j < b.n_layers) : (j <= cur);
