@@ -72,6 +72,8 @@ def parse():
     p.add_argument("--hits-check", type=int, default=1 << 19, help="FP64 integrator samples per checking point")
     p.add_argument("--plain-grids", type=int, default=4, help="grids timed for the plain comparison")
     p.add_argument("--tune-share", type=float, default=1.0 / 32, help="share of a step the autotuner's trials run")
+    p.add_argument("--queue-events", type=int, default=0,
+                   help="skip the autotuner: default launch shape and this estimator queue size (small profiling runs)")
     p.add_argument("--line-configs", type=int, default=3, help="configurations of the FP64 line-error check")
     p.add_argument("--no-plain", action="store_true")
     p.add_argument("--photons", type=float, default=1e7, help="photons per step of the plain workload")
@@ -353,13 +355,21 @@ def batched_arm(args, ws, rank, local):
             s.share_surrogate(sims[deep])
     # launch shape and queue size of the batched call
     t0 = time.perf_counter()
-    tune = Simulation.autotune_batch(sims, share=args.tune_share)
+    if args.queue_events:
+        # fixed shape (small profiling runs): default launch shape, given queue size
+        for s in sims:
+            s.gpu.queue_events = args.queue_events
+            s.set_gpu(s.gpu)
+        tune = {"threads_per_block": 128, "blocks_per_sm": 8, "queue_events": args.queue_events,
+                "best_trial_ms": None, "share": 0.0}
+    else:
+        tune = Simulation.autotune_batch(sims, share=args.tune_share)
     tune["wall_s"] = time.perf_counter() - t0
 
     last = {}
 
     def step():
-        outs = Simulation.msim_batch(sims)
+        outs = Simulation.msim_batch(sims, copy=False)
         tm = last_timing()
         if "outs" in last:
             for s, o in zip(sims, last["outs"]):

@@ -139,8 +139,8 @@ int xmi_main_msim_batch(int n, xmi_inputFPtr *inputFPtrs, xmi_hdf5FPtr *hdf5FPtr
 /* Autotuner of the batched call (no counterpart in the reference): times
  * xmi_main_msim_batch on `share` of every configuration's photons (the
  * first 1/R of each source item, R = round(1 / share)) for the candidate
- * launch shapes of the wavefront kernels -- threads per block 64/128/256 x
- * blocks per SM 4/8/16 -- and then the estimator queue sizes 2^23/2^24/2^25
+ * launch shapes of the wavefront kernels -- threads per block 64/128 x
+ * blocks per SM 4/8/12/16 -- and then the estimator queue sizes 2^23/2^24/2^25
  * events, keeps the fastest by device time and writes it into every
  * configuration's xmi_gpu_options.  report[4]: threads per block, blocks
  * per SM, queue events, device ms of the best trial. */

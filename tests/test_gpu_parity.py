@@ -304,7 +304,7 @@ def test_autotuned_batch_keeps_results():
     sims = [Simulation(sp, options=configs.C1_OPTIONS, gpu=gpu_options(seed=SEED)) for sp in specs]
     before = Simulation.msim_batch(sims)
     tune = Simulation.autotune_batch(sims, share=0.5)
-    assert tune["threads_per_block"] in (64, 128) and tune["blocks_per_sm"] in (4, 8, 12, 16, 24)
+    assert tune["threads_per_block"] in (64, 128) and tune["blocks_per_sm"] in (4, 8, 12, 16)
     assert tune["queue_events"] in (1 << 23, 1 << 24, 1 << 25) and tune["best_trial_ms"] > 0
     after = Simulation.msim_batch(sims)
     for s, a, b in zip(sims, before, after):

@@ -274,9 +274,12 @@ class Simulation:
         return out
 
     @staticmethod
-    def msim_batch(sims: "Sequence[Simulation]") -> list[dict]:
+    def msim_batch(sims: "Sequence[Simulation]", copy: bool = True) -> list[dict]:
         """Runs several configurations in one batched launch sequence
-        (xmi_main_msim_batch); one output dict per configuration, as msim()."""
+        (xmi_main_msim_batch); one output dict per configuration, as msim().
+        copy=False returns views of the library's output arrays instead of
+        copies (no host copy of the dense reference layouts); they stay valid
+        until free_raw releases them."""
         lib = abi.load()
         n = len(sims)
         ins = (C.c_void_p * n)(*[s.inputF.value for s in sims])
@@ -290,12 +293,13 @@ class Simulation:
         vr = (abi.c_double_p * n)()
         _check(lib.xmi_main_msim_batch(n, ins, tabs, opts, sas, ch, br, vr), "xmi_main_msim_batch")
         outs = []
+        cp = (lambda a: a.copy()) if copy else (lambda a: a)
         for i, s in enumerate(sims):
             N = s.spec.n_interactions_trajectory
             nch = s.spec.nchannels
-            outs.append({"channels": np.ctypeslib.as_array(ch[i], ((N + 1), nch)).copy(),
-                         "brute": np.ctypeslib.as_array(br[i], (100, 385, N)).copy(),
-                         "var_red": np.ctypeslib.as_array(vr[i], (100, 385, N)).copy() if vr[i] else None,
+            outs.append({"channels": cp(np.ctypeslib.as_array(ch[i], ((N + 1), nch))),
+                         "brute": cp(np.ctypeslib.as_array(br[i], (100, 385, N))),
+                         "var_red": cp(np.ctypeslib.as_array(vr[i], (100, 385, N))) if vr[i] else None,
                          "raw": (ch[i], br[i], vr[i])})
         return outs
 
