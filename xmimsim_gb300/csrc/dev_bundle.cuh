@@ -28,6 +28,7 @@ struct DevBundle {
   double n_sample[3], p_det[3], n_det[3], det_new[9], det_inv[9];
   /* the same in the working precision (no FP64 -> FP32 conversions on the step) */
   R n_sample_r[3], n_det_r[3], det_new_r[9], det_inv_r[9], det_radius_r;
+  R zero_r, inv_gain_r; /* channel = (E - zero) / gain as (E - zero_r) * inv_gain_r */
   double det_radius, coll_radius, coll_height, coll_half_apex, coll_vertex_x;
   double d_source_slit, slit_x, slit_y;
   double zbeg[XMI_MAXL], zend[XMI_MAXL];

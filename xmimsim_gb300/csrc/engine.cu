@@ -254,6 +254,8 @@ void fill_scalars(const xmi_bundle &h, xmi::DevBundle<R> &d) {
   }
   d.det_radius = h.det_radius;
   d.det_radius_r = (R)h.det_radius;
+  d.zero_r = (R)h.zero;
+  d.inv_gain_r = (R)(1.0 / h.gain);
   for (int k = 0; k < 3; k++) {
     d.n_sample_r[k] = (R)h.n_sample[k];
     d.n_det_r[k] = (R)h.n_det[k];

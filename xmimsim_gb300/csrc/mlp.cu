@@ -54,11 +54,12 @@ constexpr int OFF_WO = OFF_B0 + H + 3 * (H * H + H), OFF_BO = OFF_WO + H;
 constexpr int W0_BYTES = H * KIN * 2, WL_BYTES = H * H * 2;
 constexpr int PACK_BYTES = W0_BYTES + 3 * WL_BYTES;
 
-/* The forward kernels run two independent groups of 128 threads per CTA,
+/* The forward kernels run three independent groups of 128 threads per CTA,
  * each with its own 128-row tile, activation tile, TMEM accumulator and
  * mbarrier, sharing the resident weights: while one group's SiLU epilogue
- * runs on the CUDA cores the other's MMAs run on the tensor cores. */
-constexpr int kGroups = 2, kFwdThreads = 128 * kGroups;
+ * runs on the CUDA cores another's MMAs run on the tensor cores. */
+constexpr int kGroups = 3, kFwdThreads = 128 * kGroups;
+constexpr uint32_t kTmemCols = 512; /* power of two >= 128 kGroups */
 
 /* shared-memory plan of the forward kernels (offsets in bytes) */
 constexpr int SM_W = 0;                           /* packed weights */
@@ -155,7 +156,7 @@ __device__ void fwd_setup(unsigned char *sm, const unsigned char *packed, const 
   float *w0 = (float *)(sm + SM_X0);
   for (int i = tid; i < H * NIN; i += blockDim.x) w0[i] = theta[OFF_W0 + i];
   c.bo = theta[OFF_BO];
-  if (warp == 0) umma::tmem_alloc(tmem_slot, 128 * kGroups);
+  if (warp == 0) umma::tmem_alloc(tmem_slot, kTmemCols);
   if (tid == 0) {
     for (int g = 0; g < kGroups; g++) umma::mbar_init((uint64_t *)(sm + SM_BAR) + g, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -237,7 +238,7 @@ __device__ bool fwd_tile(unsigned char *sm, FwdCtx &c, const float *f, float &y)
 __device__ void fwd_teardown(FwdCtx &c) {
   umma::fence_before_sync();
   __syncthreads();
-  if ((threadIdx.x >> 5) == 0) umma::tmem_dealloc(c.tmem, 128 * kGroups);
+  if ((threadIdx.x >> 5) == 0) umma::tmem_dealloc(c.tmem, kTmemCols);
 }
 
 /* features [n][3] (already scaled) -> out [n] = network output (log solid

@@ -336,7 +336,7 @@ __device__ __forceinline__ void tally_add(double *addr, double v) {
 template <typename R>
 __device__ __forceinline__ int channel_of(const DevBundle<R> &b, R E) {
   /* FP32: a multiply by 1/gain (a channel edge may move by an ulp) */
-  if constexpr (sizeof(R) == 4) return (int)((E - (R)b.zero) * (R)(1.0 / b.gain));
+  if constexpr (sizeof(R) == 4) return (int)((E - b.zero_r) * b.inv_gain_r);
   else return (int)((E - (R)b.zero) / (R)b.gain);
 }
 
