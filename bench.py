@@ -289,17 +289,34 @@ def timed_steps(args, step, local):
     return tms, wall, clocks.summary()
 
 
-def roofline_block(ph_ms: dict, n_hist_per_step: int, words_tr: float, words_est: float, word: int):
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per history of
+# one estimator_kernel launch, from ncu captures of the FP32 kernel: the
+# batched sweep's small case (16 configurations, a 2^20-photon chunk:
+# 335.4 + 4.5 MB) and the plain production workload (1e6 photons: 391.6 +
+# 3.6 MB).  Traffic grows in proportion to the histories of a launch.
+ESTIMATOR_DRAM_BYTES_PER_HISTORY = {"batched": 340.0e6 / 1048576, "plain": 395.1e6 / 1.0e6}
+
+
+def roofline_block(ph_ms: dict, n_hist_per_step: int, words_tr: float, words_est: float, word: int,
+                   traffic_per_history: float | None = None, hist_per_launch: float | None = None):
     """Dominant kernel: algorithmic table bytes it reads per history (counted
-    by the instrumented oracle on the CPU sample) over its device time."""
+    by the instrumented oracle on the CPU sample) over its device time;
+    traffic: measured DRAM bytes of one launch (per-history figure scaled to
+    the histories of one launch of this run)."""
     kern = "estimator_kernel" if ph_ms["estimator"] >= ph_ms["transport"] else "wf_step + wf_interact"
     kms = ph_ms["estimator"] if kern == "estimator_kernel" else ph_ms["transport"]
     bph = (words_est if kern == "estimator_kernel" else words_tr) * word
     pk = peaks()
     peak = pk.get("hbm_gbs", 6800.0)
     achieved = bph * n_hist_per_step / (kms / 1e3) / 1e9 if kms > 0 else 0.0
+    traffic = None
+    if kern == "estimator_kernel" and traffic_per_history and hist_per_launch:
+        traffic = traffic_per_history * hist_per_launch
     return {"bound": "hbm", "kernel": kern, "achieved": achieved, "peak": peak, "unit": "GB/s",
-            "frac": achieved / peak, "traffic": None, "algorithmic_bytes_per_history": bph,
+            "frac": achieved / peak, "traffic": traffic, "traffic_per_history": traffic_per_history,
+            "algorithmic_bytes_per_history": bph,
+            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one estimator launch "
+                              "(small case of this workload), scaled to this run's histories per launch",
             "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if pk else "fallback 6.8 TB/s"}
 
 
@@ -557,8 +574,12 @@ def main():
         line["cpu_baseline"] = {"value": cv, "unit": "histories/s", "cores": os.cpu_count(), "kind": "port",
                                 "sample": "%d photons (%.2f s) over %s" % (cn, cdt, what)}
         word = 4 if line["dtype"].startswith("f32") else 8
+        qev = line["config"].get("autotuned", {}).get("queue_events") or (1 << 25)
+        n_int = 4 if args.workload == "batched" else 6
+        per_launch = min(qev // n_int, line["config"]["photons_per_step"])
+        tph = ESTIMATOR_DRAM_BYTES_PER_HISTORY[args.workload] if word == 4 else None
         line["roofline"] = roofline_block(line["phases_ms_per_step"], line["config"]["photons_per_step"],
-                                          words_tr, words_est, word)
+                                          words_tr, words_est, word, tph, per_launch)
     if rank == 0:
         print(json.dumps(line))
     for s in sims:
