@@ -211,6 +211,10 @@ void xmi_escape_ratios_calculation(xmi_input *inputPtr, xmi_escape_ratios **esca
 void xmi_free_escape_ratios(xmi_escape_ratios *escape_ratios);   /* include/xmi_detector.h:71 */
 
 /* ---- introspection used by the test-suite and benchmark ---- */
+/* the escape-mode input and tables xmi_escape_ratios_calculation builds for
+ * a detector (crystal layers as the sample, src/xmi_detector.c:91-141) */
+int xmi_gpu_escape_tables(xmi_input *inputPtr, xmi_main_options *options, xmi_inputFPtr *inputFPtr,
+                          xmi_hdf5FPtr *hdf5FPtr);
 struct xmi_bundle_s; /* see xmimsim_bundle.h */
 const void *xmi_gpu_bundle(xmi_hdf5FPtr hdf5FPtr);
 /* prepares the run-dependent part of the bundle (source items, options)

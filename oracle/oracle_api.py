@@ -45,6 +45,9 @@ def load() -> C.CDLL:
                                                              C.POINTER(C.c_int), C.c_int, C.c_long, dp]
         _lib.oracle_threefry_block.restype = None
         _lib.oracle_threefry_block.argtypes = [C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]
+        _lib.oracle_escape_ratios.restype = C.c_int
+        _lib.oracle_escape_ratios.argtypes = [C.c_void_p, C.c_long, C.c_double, C.c_double, C.c_long, C.c_long,
+                                              C.c_double, C.c_double, C.c_int, dp, dp, dp]
         _lib.oracle_convolute_spectrum.restype = C.c_int
         _lib.oracle_convolute_spectrum.argtypes = [dp, dp, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
                                                    C.c_int, C.c_double, C.c_double, C.POINTER(OracleEscape), C.c_int,
@@ -54,6 +57,19 @@ def load() -> C.CDLL:
 
 def _dp(a: np.ndarray):
     return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def escape_ratios(bundle_ptr: int, n_elem: int, n_input: int, e_min: float, e_delta: float, n_photons: int,
+                  n_compton: int, c_min: float, c_delta: float, threads: int = 0):
+    """Raw sums of the escape-ratio Monte Carlo (oracle_escape_ratios):
+    fluo[nE][n_elem][109], comp[nE][nco], interacted[nE]."""
+    fluo = np.zeros(n_input * n_elem * 109)
+    comp = np.zeros(n_input * n_compton)
+    inter = np.zeros(n_input)
+    if load().oracle_escape_ratios(C.c_void_p(bundle_ptr), n_input, e_min, e_delta, n_photons, n_compton, c_min,
+                                   c_delta, threads, _dp(fluo), _dp(comp), _dp(inter)) != 1:
+        raise RuntimeError("oracle escape ratios failed")
+    return fluo.reshape(n_input, n_elem, 109), comp.reshape(n_input, n_compton), inter
 
 
 def msim(bundle_ptr: int, n_interactions: int, nchannels: int, n_mpi_hosts: int = 1, threads: int = 0,

@@ -1192,6 +1192,103 @@ long long oracle_words_counted(long long *estimator) {
 }
 
 /* known-answer helper: raw Philox block */
+/* Escape-ratio Monte Carlo, src/xmi_main.F90:5473-5800 (the photon loop
+ * 5645-5755): photon w of input energy iE = w / n_photons starts at the point
+ * source with a slit direction (xmi_coords_dir, 957-1010) and a random
+ * E-vector, is simulated in escape mode, and, when it leaves after at least
+ * one interaction, is tallied by its last interaction: a Compton photon by
+ * its energy bin, a fluorescence photon (lines KL1..L3P3) by element and line
+ * with its escape weight.  Raw sums: fluo[nE][n_elem][109], comp[nE][nco],
+ * interacted[nE] (the ratios are these over interacted).  Same Philox
+ * streams as the engine's escape kernel: (photon w, stream 0) for the source,
+ * (w, k) for step k. */
+int oracle_escape_ratios(const xmi_bundle *b, long nE, double emin, double de, long n_photons, long nco,
+                         double cmin, double cde, int nthreads, double *fluo, double *comp, double *interacted) {
+  const long long n_total = (long long)nE * n_photons;
+  size_t nf = (size_t)nE * b->n_elem * 109, i;
+  int ok = 1;
+  memset(fluo, 0, sizeof(double) * nf);
+  memset(comp, 0, sizeof(double) * (size_t)nE * nco);
+  memset(interacted, 0, sizeof(double) * nE);
+#ifdef _OPENMP
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#endif
+#pragma omp parallel
+  {
+    size_t nc = (size_t)(b->n_interactions + 1) * b->nchannels, nh = (size_t)100 * 385 * b->n_interactions;
+    otally t;
+    memset(&t, 0, sizeof(t));
+    t.channels = (double *)calloc(nc > 0 ? nc : 1, sizeof(double));
+    t.var_red = (double *)calloc(nh > 0 ? nh : 1, sizeof(double));
+    t.brute = (double *)calloc(nh > 0 ? nh : 1, sizeof(double));
+#pragma omp for schedule(dynamic, 256)
+    for (long long w = 0; w < n_total; w++) {
+      ophoton p;
+      orng g;
+      const long iE = (long)(w / n_photons);
+      double x1m, y1m, x1, y1, te, cosalfa, c_alfa, c_ae, c_be;
+      int k;
+      memset(&p, 0, sizeof(p));
+      p.id = w;
+      p.energy = emin + iE * de;
+      mu_calc(b, p.energy, p.mus);
+      orng_init(&g, b->seed, (uint64_t)w, 0u);
+      x1m = atan(b->slit_x / b->d_source_slit / 2.0);
+      y1m = atan(b->slit_y / b->d_source_slit / 2.0);
+      x1 = x1m * ran_flat(&g, -1.0, 1.0);
+      y1 = y1m * ran_flat(&g, -1.0, 1.0);
+      p.dirv[0] = tan(x1);
+      p.dirv[1] = tan(y1);
+      p.dirv[2] = 1.0;
+      normalize3(p.dirv);
+      p.theta = acos(p.dirv[2]);
+      p.phi = atan2(p.dirv[1], p.dirv[0]);
+      p.weight = 1.0;
+      p.weight_escape = p.weight;
+      te = orng_uniform(&g) * M_PI * 2.0;
+      p.elecv[0] = cos(te);
+      p.elecv[1] = sin(te);
+      p.elecv[2] = 0.0;
+      cosalfa = dot3(p.elecv, p.dirv);
+      c_alfa = acos(cosalfa);
+      c_ae = 1.0 / sin(c_alfa);
+      c_be = -c_ae * cosalfa;
+      for (k = 0; k < 3; k++) p.elecv[k] = c_ae * p.elecv[k] + c_be * p.dirv[k];
+      if (!shift_first_layer(b, &p)) continue;
+      p.last_interaction = XMI_NO_INTERACTION;
+      if (!simulate_photon(b, &p, &t)) continue;
+      if (p.last_interaction != XMI_NO_INTERACTION) {
+#pragma omp atomic
+        interacted[iE] += p.weight;
+      }
+      if (!p.inside && p.last_interaction != XMI_NO_INTERACTION) {
+        if (p.last_interaction == XMI_COMPTON) {
+          const int ci = (int)((p.energy - cmin) / cde) + 1;
+          if (ci >= 1 && ci <= nco) {
+#pragma omp atomic
+            comp[(size_t)iE * nco + (ci - 1)] += p.weight;
+          }
+        } else if (p.last_interaction == XMI_PHOTOELECTRIC) {
+          const int ht = p.hist_type[p.n_int];
+          if (ht <= -1 && ht >= -109) {
+#pragma omp atomic
+            fluo[((size_t)iE * b->n_elem + p.hist_elem[p.n_int]) * 109 + (-ht - 1)] += p.weight_escape;
+          }
+        }
+      }
+    }
+    if (t.error) {
+#pragma omp atomic write
+      ok = 0;
+    }
+    free(t.channels);
+    free(t.var_red);
+    free(t.brute);
+  }
+  (void)i;
+  return ok;
+}
+
 void oracle_philox_block(const uint32_t *ctr, const uint32_t *key, uint32_t *out) { orng_block(ctr, key, out); }
 
 void oracle_threefry_block(const uint32_t *ctr, const uint32_t *key, uint32_t *out) { othreefry4x32(ctr, key, out); }

@@ -365,3 +365,35 @@ def test_thin_layers_fp32_tracks_fp64():
     np.testing.assert_allclose(r32["channels"].sum(axis=1), r64["channels"].sum(axis=1), rtol=5e-3)
     s64.close()
     s32.close()
+
+
+def test_escape_ratios_match_oracle():
+    """Escape ratios (src/xmi_main.F90:5473-5800): the GPU escape-mode Monte
+    Carlo against the FP64 oracle on the same escape tables and Philox
+    streams -- fluorescence and Compton escape ratios equal to within the
+    order of FP64 additions, for input energies across the Si K edge."""
+    from xmimsim_gb300 import abi
+    spec = configs.config1(n_photons_line=10)
+    sim = Simulation(spec, options=configs.C1_OPTIONS, gpu=gpu_options(seed=SEED))
+    nE, n_ph = 40, 4000
+    er = sim.escape_ratios(n_photons=n_ph, n_input_energies=nE).contents
+    nel, nco = er.n_elements, er.n_compton_output_energies
+    fluo_g = np.ctypeslib.as_array(er.fluo_escape_ratios, (nE * 109 * nel,)).reshape(nE, 109, nel)
+    comp_g = np.ctypeslib.as_array(er.compton_escape_ratios, (nco * nE,)).reshape(nco, nE)
+    E = np.ctypeslib.as_array(er.fluo_escape_input_energies, (nE,)).copy()
+    co = np.ctypeslib.as_array(er.compton_escape_output_energies, (nco,)).copy()
+    lib = abi.load()
+    h, t = C.c_void_p(), C.c_void_p()
+    assert lib.xmi_gpu_escape_tables(C.byref(sim.cinput.input), C.byref(sim.options), C.byref(h), C.byref(t)) == 1
+    f, c, it = oracle().escape_ratios(lib.xmi_gpu_bundle(t), nel, nE, E[0], E[1] - E[0], n_ph, nco, co[0],
+                                      co[1] - co[0])
+    assert (it > 0).all()
+    fluo_o = f / it[:, None, None]          # [nE][nel][109]
+    comp_o = c / it[:, None]                 # [nE][nco]
+    np.testing.assert_allclose(fluo_g.transpose(0, 2, 1), fluo_o, rtol=1e-9, atol=1e-12)
+    np.testing.assert_allclose(comp_g.T, comp_o, rtol=1e-9, atol=1e-12)
+    assert fluo_o[E > 2.0].sum() > 0        # Si K escape above the edge
+    lib.xmi_free_hdf5_F(C.byref(t))
+    lib.xmi_free_input_F(C.byref(h))
+    sim.lib.xmi_free_escape_ratios(C.pointer(er))
+    sim.close()

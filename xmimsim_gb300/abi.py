@@ -158,6 +158,8 @@ PROTOTYPES = {
     "xmi_gpu_build_surrogate": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, c_double_p]),
     "xmi_gpu_surrogate_report": (C.c_int, [C.c_void_p, c_double_p]),
     "xmi_gpu_share_surrogate": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "xmi_gpu_escape_tables": (C.c_int, [C.POINTER(XmiInput), C.POINTER(XmiMainOptions), C.POINTER(C.c_void_p),
+                                        C.POINTER(C.c_void_p)]),
     "xmi_gpu_build_surrogate_points": (C.c_int, [C.c_void_p, C.c_int, c_double_p, c_double_p, C.c_int, C.c_int,
                                                  C.c_int, c_double_p]),
     "xmi_gpu_sample_event_points": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(XmiMainOptions), C.c_double,

@@ -669,16 +669,10 @@ __global__ void __launch_bounds__(256) escape_kernel(xmi::DevBundle<R> b, xmi::D
 
 }  // namespace
 
-extern "C" void xmi_escape_ratios_calculation(xmi_input *inputPtr, xmi_escape_ratios **escape_ratios,
-                                              char *input_string, char *hdf5_file, xmi_main_options *options,
-                                              xmi_escape_ratios_options ero) {
-  (void)hdf5_file;
-  *escape_ratios = nullptr;
-  int ndev = 0;
-  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
-    xmi_set_error("no CUDA device available: the escape-ratio Monte Carlo has no CPU fallback");
-    return;
-  }
+/* The escape-mode input and tables of a detector: its crystal layers become
+ * the sample (src/xmi_detector.c:91-141), run part prepared, seeded. */
+static bool escape_handles(xmi_input *inputPtr, xmi_main_options *options, xmi_inputFPtr *h_out,
+                           xmi_hdf5FPtr *t_out) {
   /* escape input: the detector crystal becomes the sample (src/xmi_detector.c:91-141) */
   xmi_input *esc = nullptr;
   xmi_input_copy(inputPtr, &esc);
@@ -723,12 +717,46 @@ extern "C" void xmi_escape_ratios_calculation(xmi_input *inputPtr, xmi_escape_ra
   bool ok = xmi_input_C2F(esc, &h) && xmi_init_input_escape_ratios(&h);
   xmi_input_free(esc);
   if (ok) ok = xmi_init_from_hdf5(nullptr, h, &t, eo) == 1;
-  xmi_escape_ratios *er = nullptr;
   if (ok) {
     xmi_bundle_set_run(h, t, eo, 1, 0, 1);
     t->b.seed = seed_for(nullptr, options, 0xE5Cull);
-    ok = xmi_dev_sync_tables(t, 0) == 1;
   }
+  xmi_main_options_free(eo);
+  if (!ok) {
+    if (t) xmi_free_hdf5_F(&t);
+    if (h) xmi_free_input_F(&h);
+    return false;
+  }
+  *h_out = h;
+  *t_out = t;
+  return true;
+}
+
+extern "C" int xmi_gpu_escape_tables(xmi_input *inputPtr, xmi_main_options *options, xmi_inputFPtr *h,
+                                     xmi_hdf5FPtr *t) {
+  if (!inputPtr || !h || !t) {
+    xmi_set_error("xmi_gpu_escape_tables: NULL argument");
+    return 0;
+  }
+  return escape_handles(inputPtr, options, h, t) ? 1 : 0;
+}
+
+extern "C" void xmi_escape_ratios_calculation(xmi_input *inputPtr, xmi_escape_ratios **escape_ratios,
+                                              char *input_string, char *hdf5_file, xmi_main_options *options,
+                                              xmi_escape_ratios_options ero) {
+  (void)hdf5_file;
+  *escape_ratios = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
+    xmi_set_error("no CUDA device available: the escape-ratio Monte Carlo has no CPU fallback");
+    return;
+  }
+  xmi_inputFPtr h = nullptr;
+  xmi_hdf5FPtr t = nullptr;
+  bool ok = escape_handles(inputPtr, options, &h, &t);
+  xmi_escape_ratios *er = nullptr;
+  if (ok) ok = xmi_dev_sync_tables(t, 0) == 1;
+
   if (ok) {
     const xmi_bundle &hb = t->b;
     const long nE = ero.n_input_energies, nco = ero.n_compton_output_energies;
@@ -795,7 +823,6 @@ extern "C" void xmi_escape_ratios_calculation(xmi_input *inputPtr, xmi_escape_ra
     cudaFree(d_tally);
     cudaFree(d_cnt);
   }
-  xmi_main_options_free(eo);
   if (t) xmi_free_hdf5_F(&t);
   if (h) xmi_free_input_F(&h);
   *escape_ratios = er;
