@@ -20,6 +20,8 @@
 #ifndef XMIMSIM_GB300_H
 #define XMIMSIM_GB300_H
 
+#include <stddef.h>
+
 #include "xmi_data_structs.h"
 
 #ifdef __cplusplus
@@ -202,6 +204,20 @@ int xmi_gpu_mlp_grad(const float *theta, int n, const float *features, const flo
                      double *loss);
 int xmi_gpu_mlp_train(float *theta, int n, const float *features, const float *targets, int epochs, float lr,
                       double *loss_per_epoch);
+
+/* ---- X-ray tube spectra (include/xmi_ebel.h:26-33) ----
+ * Ebel's model of the tube's continuum and K/L lines (src/xmi_ebel.F90:115-521),
+ * window and filter attenuation, optional transmission-efficiency profile
+ * (natural cubic spline through the given points).  Allocates
+ * *ebel_spectrum (free with xmi_free on its arrays and itself). */
+int xmi_tube_ebel(xmi_layer *tube_anode, xmi_layer *tube_window, xmi_layer *tube_filter, double tube_voltage,
+                  double tube_current, double tube_angle_electron, double tube_angle_xray, double tube_delta_energy,
+                  double tube_solid_angle, int tube_transmission, size_t tube_nefficiencies, double *tube_energies,
+                  double *tube_efficiencies, xmi_excitation **ebel_spectrum);
+/* include/xmi_transmission_efficiency.h:27; the reference's GError is the
+ * 0 return with the reason in xmi_gpu_last_error() */
+int xmi_transmission_efficiency_read(const char *filename, size_t *nefficiencies, double **energies,
+                                     double **efficiencies);
 
 /* ---- escape ratios (include/xmi_detector.h:55-57) ---- */
 xmi_escape_ratios_options xmi_get_default_escape_ratios_options(void);

@@ -158,6 +158,11 @@ PROTOTYPES = {
     "xmi_gpu_build_surrogate": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, c_double_p]),
     "xmi_gpu_surrogate_report": (C.c_int, [C.c_void_p, c_double_p]),
     "xmi_gpu_share_surrogate": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "xmi_tube_ebel": (C.c_int, [C.POINTER(XmiLayer), C.POINTER(XmiLayer), C.POINTER(XmiLayer), C.c_double,
+                                C.c_double, C.c_double, C.c_double, C.c_double, C.c_double, C.c_int, C.c_size_t,
+                                c_double_p, c_double_p, C.POINTER(C.POINTER(XmiExcitation))]),
+    "xmi_transmission_efficiency_read": (C.c_int, [C.c_char_p, C.POINTER(C.c_size_t), C.POINTER(c_double_p),
+                                                   C.POINTER(c_double_p)]),
     "xmi_gpu_escape_tables": (C.c_int, [C.POINTER(XmiInput), C.POINTER(XmiMainOptions), C.POINTER(C.c_void_p),
                                         C.POINTER(C.c_void_p)]),
     "xmi_gpu_build_surrogate_points": (C.c_int, [C.c_void_p, C.c_int, c_double_p, c_double_p, C.c_int, C.c_int,
