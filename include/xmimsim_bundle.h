@@ -38,9 +38,9 @@ enum {
   XMI_REC_PR = 1,     /* CS_Rayl/CS_Total (interaction_probs col 1) */
   XMI_REC_PRC = 2,    /* (CS_Rayl+CS_Compt)/CS_Total (col 2) */
   XMI_REC_PHOTO = 3,  /* CS_Photo_Total */
-  XMI_REC_PART = 4,   /* 4..12: CS_Photo_Partial(Z,shell,E) */
-  XMI_REC_XRF = 13,   /* 13..21: cascade-corrected P_shell (PK..PM5) */
-  XMI_EL_REC = 22
+  XMI_REC_XRF = 4,    /* 4..12: cascade-corrected P_shell (PK..PM5), 16-byte aligned */
+  XMI_REC_PART = 13,  /* 13..21: CS_Photo_Partial(Z,shell,E) */
+  XMI_EL_REC = 24     /* 96-byte records (2 unused), so a record starts on 16 bytes */
 };
 
 /* Coster-Kronig transition indices (xraylib FL12_TRANS..FM45_TRANS order) */

@@ -234,8 +234,7 @@ __device__ __forceinline__ void estimate_event_uniform(const DevBundle<R> &b, co
         P[s] = XMI_LDG(b.precalc_xrf, ((long long)e * XMI_NSHELL + s) * b.n_lines + ev.h_slot,
                        (long long)b.n_elem * XMI_NSHELL * b.n_lines, 10);
     } else {
-#pragma unroll
-      for (int s = 0; s < XMI_NSHELL; s++) P[s] = el_val(b, e, XMI_REC_XRF + s, ev.node, ev.f);
+      el_xrf(b, e, ev.node, ev.f, P);
     }
     const R scale = live * (sizeof(R) == 4 ? wi * inv_mu : wi / ev.mu_here) * ev.pdir_fluo * ev.w;
 #pragma unroll

@@ -219,6 +219,28 @@ __device__ __forceinline__ R el_val(const DevBundle<R> &b, int e, int col, int n
   return v0 + f * (v1 - v0);
 }
 
+/* the 9 cascade-corrected shell probabilities of element e at (node, f);
+ * FP32 reads each node's 9 values as two 16-byte loads and one word */
+template <typename R>
+__device__ __forceinline__ void el_xrf(const DevBundle<R> &b, int e, int node, R f, R *P) {
+#ifndef XMI_CHECKED
+  if constexpr (sizeof(R) == 4 && XMI_REC_XRF % 4 == 0 && XMI_EL_REC % 4 == 0) {
+    const float *r0 = b.el_tab + ((long long)e * b.n_nodes + node) * XMI_EL_REC + XMI_REC_XRF;
+    const float *r1 = r0 + XMI_EL_REC;
+    const float4 a0 = __ldg(reinterpret_cast<const float4 *>(r0)), a1 = __ldg(reinterpret_cast<const float4 *>(r0) + 1);
+    const float4 c0 = __ldg(reinterpret_cast<const float4 *>(r1)), c1 = __ldg(reinterpret_cast<const float4 *>(r1) + 1);
+    const float a8 = __ldg(r0 + 8), c8 = __ldg(r1 + 8);
+    const float v0[9] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w, a8};
+    const float v1[9] = {c0.x, c0.y, c0.z, c0.w, c1.x, c1.y, c1.z, c1.w, c8};
+#pragma unroll
+    for (int s = 0; s < 9; s++) P[s] = v0[s] + f * (v1[s] - v0[s]);
+    return;
+  }
+#endif
+#pragma unroll
+  for (int s = 0; s < XMI_NSHELL; s++) P[s] = el_val(b, e, XMI_REC_XRF + s, node, f);
+}
+
 template <typename R>
 __device__ __forceinline__ void mu_calc(const DevBundle<R> &b, R E, R *mus) {
   int node;
