@@ -308,7 +308,7 @@ constexpr int kEventsPerGrab = 256;
  * the counter `work`; stage rows of stage_cap values per warp sit in dynamic
  * shared memory. */
 template <typename R>
-__global__ void __launch_bounds__(256, 3) estimator_kernel(const DevBundle<R> *bundles, const DevTally *tallies,
+__global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 3) estimator_kernel(const DevBundle<R> *bundles, const DevTally *tallies,
                                                            int n_cfg, const VrEvent<R> *events, const int *order,
                                                            const unsigned long long *count, long long cap,
                                                            unsigned long long *work, int stage_cap,
