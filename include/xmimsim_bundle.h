@@ -65,6 +65,8 @@ enum { XMI_NO_INTERACTION = 0, XMI_RAYLEIGH = 1, XMI_COMPTON = 2,
 #define XMI_PHI_NT 200
 #define XMI_DOPPLER_N 10001
 #define XMI_NQ 4096
+#define XMI_CP_N 10001    /* Compton profile grids (reference src/xmi_data.c:152) */
+#define XMI_CP_SH 32      /* room for every shell with electrons (29 in xraylib's K..Q1 order) */
 #define XMI_QMAX 20.0
 
 /* one source item: a valid continuous interval or a discrete line
@@ -92,6 +94,7 @@ typedef struct {
   int use_M_lines;
   int cascade_type;     /* XMI_CASCADE_* */
   int escape_mode;      /* escape_ratios_mode (escape-ratio MC) */
+  int use_advanced_compton; /* 1: per-shell impulse-approximation Compton (needs the cp_* tables) */
   int nchannels;
   double gain, zero, live_time;
   uint64_t seed;        /* Philox key */
@@ -196,6 +199,18 @@ typedef struct {
   double *ent_coef;      /* [n_ent] FluorYield(Z, shell) x RadRate(Z, line) */
   double *ent_pmu;       /* [n_ent][XMI_MAXL] precalc_mu of every layer at the line energy (0 beyond n_layers) */
   int stage_max;         /* max over layers of (line entries + 2 x elements): history slots one layer feeds */
+
+  /* ---- per-shell Compton profiles (advanced Compton; reference
+   * src/xmi_data_f.F90:1124-1230), built on demand by
+   * xmi_bundle_compton_profiles: NULL until then.  Shell k of element e is
+   * the k-th shell with electrons, K first.  Q grid: Q_j = 100 j / (N - 1);
+   * CDF grid: c_j = 0.5 j / (N - 1), N = XMI_CP_N. ---- */
+  int *cp_nshell;          /* [n_elem] */
+  int *cp_shell;           /* [n_elem][XMI_CP_SH] xraylib shell index */
+  double *cp_occ;          /* [n_elem][XMI_CP_SH] electrons in the shell (ElectronConfig_Biggs) */
+  double *cp_edge;         /* [n_elem][XMI_CP_SH] binding energy EdgeEnergy(Z, shell), keV */
+  const double **cp_cdf;   /* [n_elem] -> [nshell][N] partial profile integral over [0, Q_j], scaled to 0.5 at Q = 100 */
+  const double **cp_qinv;  /* [n_elem] -> [nshell][N] Q at which that integral reaches c_j */
 } xmi_bundle;
 
 /* Evaluation rule of every energy table of the bundle: E is located in the

@@ -194,3 +194,52 @@ def convolute_spectrum(noconv, det_corr, gain, zero, fano, noise, det_type, live
     if rv != 1:
         raise RuntimeError("oracle convolution failed")
     return out
+
+
+def compton_qimax(energy: float, binding: float, theta: float) -> float:
+    f = load().oracle_compton_qimax
+    f.restype, f.argtypes = C.c_double, [C.c_double] * 3
+    return f(energy, binding, theta)
+
+
+def compton_q_from_energy(old_e: float, new_e: float, theta: float) -> float:
+    f = load().oracle_compton_q_from_energy
+    f.restype, f.argtypes = C.c_double, [C.c_double] * 3
+    return f(old_e, new_e, theta)
+
+
+def compton_energy_from_q(energy: float, q: float, theta: float) -> tuple[float, int]:
+    """(scattered energy, error flag): the flag is set where the reference stops."""
+    f = load().oracle_compton_energy_from_q
+    f.restype, f.argtypes = C.c_double, [C.c_double, C.c_double, C.c_double, C.POINTER(C.c_int)]
+    err = C.c_int(0)
+    return f(energy, q, theta, C.byref(err)), err.value
+
+
+def compton_shells(bundle_ptr: int, e: int):
+    """(shell indices, occupancies, binding energies) of element e's Compton profiles."""
+    lib = load()
+    sh = (C.c_int * 32)()
+    occ, edge = np.zeros(32), np.zeros(32)
+    n = lib.oracle_compton_shells(C.c_void_p(bundle_ptr), e, sh, _dp(occ), _dp(edge))
+    if n < 0:
+        raise RuntimeError("no Compton profile tables in this bundle")
+    return np.array(sh[:n]), occ[:n], edge[:n]
+
+
+def compton_rows(bundle_ptr: int, e: int, k: int, n: int = 10001):
+    cdf, qinv = np.zeros(n), np.zeros(n)
+    load().oracle_compton_rows(C.c_void_p(bundle_ptr), e, k, _dp(cdf), _dp(qinv))
+    return cdf, qinv
+
+
+def compton_energy_advanced(bundle_ptr: int, e: int, energy: float, theta: float, photon_id: int, stream: int):
+    """(scattered energy, shell cumulative values, error flag) of one transport draw."""
+    f = load().oracle_compton_energy_advanced
+    f.restype = C.c_double
+    f.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_uint64, C.c_uint32, C.POINTER(C.c_double),
+                  C.POINTER(C.c_int)]
+    cdfs = np.zeros(32)
+    err = C.c_int(0)
+    E = f(C.c_void_p(bundle_ptr), e, energy, theta, photon_id, stream, _dp(cdfs), C.byref(err))
+    return E, cdfs, err.value

@@ -9,6 +9,10 @@
  *   xmi_check_photon_detector_hit src/xmi_main.F90:1920-1984
  *   xmi_simulate_photon_rayleigh/compton/fluorescence src/xmi_main.F90:1986-2411
  *   xmi_update_photon_energy_compton2 src/xmi_main.F90:4985-5067
+ *   xmi_update_photon_energy_compton (advanced) src/xmi_main.F90:4785-4983,
+ *   xmi_compton_varred src/xmi_variance_reduction.F90:752-947,
+ *   xmi_get_qimax / xmi_get_energy_from_q / xmi_get_q_from_energy
+ *   src/xmi_aux_f.F90:1951-2074
  *   xmi_update_photon_dirv/elecv src/xmi_main.F90:5071-5182
  *   xmi_coster_kronig_check, xmi_fluorescence_yield_check,
  *   xmi_fluorescence_line_check src/xmi_main.F90:5184-5437
@@ -410,6 +414,127 @@ static double compton_energy(const xmi_bundle *b, int e, double E, double theta_
   return energy;
 }
 
+/* ---- advanced Compton: per-shell impulse approximation ----
+ * MEC2 of these functions is xraylib's constant (keV); the tolerances
+ * 1E-8, 1E-4 and 1E-10 of the reference are default-real literals. */
+#define O_XRL_MEC2 510.998928
+
+/* xmi_get_qimax, src/xmi_aux_f.F90:1951-1977 (ctheta = cos theta) */
+static double o_qimax(double energy, double Ii, double ctheta) {
+  double emi, q;
+  if (Ii != 0.0 && energy < Ii) return 0.0;
+  emi = energy - Ii;
+  q = 137.0 * (emi * energy * (1.0 - ctheta) / O_XRL_MEC2 - Ii);
+  return q / sqrt(emi * emi + energy * energy - 2.0 * emi * energy * ctheta);
+}
+
+/* xmi_get_q_from_energy, src/xmi_aux_f.F90:2058-2074 */
+static double o_q_from_energy(double old_e, double new_e, double c) {
+  double q = 137.0 * (new_e - old_e + (1.0 - c) * old_e * new_e / O_XRL_MEC2);
+  return q / sqrt(new_e * new_e + old_e * old_e - 2.0 * old_e * new_e * c);
+}
+
+/* xmi_get_energy_from_q, src/xmi_aux_f.F90:1979-2056; *err = 1 where the
+ * reference stops the program (neither root has the sign of Q) */
+static double o_energy_from_q(double a, double Q, double theta, int *err) {
+  const double b = O_XRL_MEC2, c = cos(theta), k2 = 137.0 * 137.0;
+  double d, aq, bq, cq, e1, e2, q1, q2, delta;
+  if (fabs(c - 1.0) < (double)1e-8f) return 0.0;
+  if (fabs(Q) < (double)1e-4f) return a / (1.0 + a * (1.0 - c) / b);
+  d = 1.0 + a / b - a * c / b;
+  aq = k2 * (d * d) - Q * Q;
+  bq = -(2.0 * k2 * a * d) + 2.0 * a * c * (Q * Q);
+  cq = k2 * (a * a) - (a * a) * (Q * Q);
+  /* xmi_poly_solve_quadratic, src/xmi_aux_f.F90:1872-1905 */
+  if (aq == 0.0) {
+    if (bq == 0.0) return 0.0;
+    e1 = e2 = -1.0 * cq / bq;
+  } else {
+    delta = bq * bq - 4.0 * aq * cq;
+    if (delta < 0.0) return 0.0;
+    if (delta == 0.0) {
+      e1 = e2 = -bq / 2.0 / aq;
+    } else {
+      const double sd = sqrt(delta), r1 = (-bq + sd) / 2.0 / aq, r2 = (-bq - sd) / 2.0 / aq;
+      e1 = r1 < r2 ? r1 : r2;
+      e2 = r1 < r2 ? r2 : r1;
+    }
+  }
+  q1 = o_q_from_energy(a, e1, c);
+  q2 = o_q_from_energy(a, e2, c);
+  if (Q * q1 > 0.0) return e1;
+  if (Q * q2 > 0.0) return e2;
+  if (fabs(e1 - e2) < (double)1e-10f || fabs(q1 - q2) < (double)1e-10f) return e1;
+  *err = 1;
+  return 0.0;
+}
+
+/* the cumulative profile of one shell up to qimax (the cdfs of
+ * src/xmi_main.F90:4808-4856): row = the shell's cdf table */
+static double o_shell_cdf(const double *row, double qimax) {
+  const double dq = 100.0 * 1.0 / (XMI_CP_N - 1.0) - 100.0 * 0.0 / (XMI_CP_N - 1.0);
+  double x, v;
+  int pos;
+  if (qimax != qimax) qimax = 0.0; /* 0/0 at theta = 0 with a zero binding energy: undefined in the reference */
+  if (qimax < -100.0) return 0.0;
+  if (qimax > 100.0) return 1.0;
+  x = qimax < 0.0 ? -qimax : qimax;
+  pos = (int)(x / dq);
+  if (pos > XMI_CP_N - 2) pos = XMI_CP_N - 2; /* x = 100 exactly: the last interval */
+  o_words += 2;
+  v = interp_simple(100.0 * pos / (XMI_CP_N - 1.0), row[pos], 100.0 * (pos + 1) / (XMI_CP_N - 1.0), row[pos + 1], x);
+  return qimax < 0.0 ? 1.0 - (0.5 + v) : 0.5 + v;
+}
+
+/* Q of a shell at cumulative value cdf (src/xmi_main.F90:4897-4958) */
+static double o_shell_q(const double *row, double cdf) {
+  const double dc = 0.5 * 1.0 / (XMI_CP_N - 1.0) - 0.5 * 0.0 / (XMI_CP_N - 1.0);
+  const int neg = cdf < 0.5;
+  const double cp = neg ? 0.5 - cdf : cdf - 0.5;
+  double q;
+  int pos = (int)(cp / dc);
+  /* the reference stops the program at pos = N - 1 (cdf exactly 0 or 1) */
+  if (pos > XMI_CP_N - 2) pos = XMI_CP_N - 2;
+  o_words += 2;
+  q = interp_simple(0.5 * pos / (XMI_CP_N - 1.0), row[pos], 0.5 * (pos + 1) / (XMI_CP_N - 1.0), row[pos + 1], cp);
+  return neg ? -q : q;
+}
+
+/* cdfs of every shell of element e and their occupancy-weighted sum */
+static double o_shell_cdfs(const xmi_bundle *b, int e, double energy, double theta, double *cdfs) {
+  const int ns = b->cp_nshell[e];
+  const double c = cos(theta);
+  double sum = 0.0;
+  int k;
+  for (k = 0; k < ns; k++) {
+    const double qi = o_qimax(energy, b->cp_edge[(size_t)e * XMI_CP_SH + k], c);
+    cdfs[k] = o_shell_cdf(b->cp_cdf[e] + (size_t)k * XMI_CP_N, qi);
+  }
+  for (k = 0; k < ns; k++) sum = sum + b->cp_occ[(size_t)e * XMI_CP_SH + k] * cdfs[k];
+  return sum;
+}
+
+/* xmi_update_photon_energy_compton, src/xmi_main.F90:4785-4983: the new
+ * energy (0: photon absorbed) */
+static double compton_energy_advanced(const xmi_bundle *b, int e, double energy, double theta_i, orng *g, int *err) {
+  const int ns = b->cp_nshell[e];
+  double cdfs[XMI_CP_SH], sum, r, tsum = 0.0, q;
+  int k, sel = -1;
+  sum = o_shell_cdfs(b, e, energy, theta_i, cdfs);
+  if (sum == 0.0) return 0.0;
+  r = orng_uniform(g);
+  for (k = 0; k < ns; k++) {
+    const double w = b->cp_occ[(size_t)e * XMI_CP_SH + k] * cdfs[k] / sum;
+    if (w > 0.0) sel = k; /* rounding can leave the running sum below r: the last shell with weight */
+    tsum = tsum + w;
+    if (r <= tsum) { sel = k; break; }
+  }
+  if (sel < 0) { *err = 1; return 0.0; } /* not reached with finite tables */
+  r = orng_uniform(g);
+  q = o_shell_q(b->cp_qinv[e] + (size_t)sel * XMI_CP_N, r * cdfs[sel]);
+  return o_energy_from_q(energy, q, theta_i, err);
+}
+
 /* xmi_check_detector_intersection, src/xmi_aux_f.F90:1622-1834, including
  * the reference's assignment of the scalar segment length to all three
  * direction components in the collimator-free branch */
@@ -509,7 +634,7 @@ static void variance_reduction(const xmi_bundle *b, ophoton *p, otally *t) {
   orng gp, *g = &gp;
   double radius, theta, dp[3], lcp[3], dirv[3], lcd[3], tmp[3], total_distance, ndc[3];
   double dotprod, phi, proj[3], en[3], distances[XMI_MAXL], tc[3], murhod, pesc_rayl, omega, pdir_fluo;
-  int step_max, step_dir, i, k, n = p->n_int, layer = p->cur_layer, err = 0, node;
+  int step_max, step_dir, i, k, kk, n = p->n_int, layer = p->cur_layer, err = 0, node;
   double f;
   if (p->energy <= O_ENERGY_THRESHOLD) return;
   orng_init(g, b->seed, (uint64_t)p->id, vr_stream(n, 0xFF));
@@ -584,8 +709,36 @@ static void variance_reduction(const xmi_bundle *b, ophoton *p, otally *t) {
     tw = pconv * pdir * pesc_rayl * p->weight;
     t->var_red[hidx(b, Z, 384, n)] += tw;
     tally_channel(b, t, n, p->energy, tw);
-    /* Compton (N_COMPTON_VARRED = 1), xmi_compton_varred2 */
+    /* Compton */
     orng_init(g, b->seed, (uint64_t)p->id, vr_stream(n, i));
+    if (b->use_advanced_compton) {
+      /* xmi_compton_varred, src/xmi_variance_reduction.F90:752-947: one
+       * energy per shell, weighted by the shell's share */
+      double cdfs[XMI_CP_SH];
+      const double sum = o_shell_cdfs(b, e, p->energy, theta, cdfs);
+      int k;
+      pdir = omega * dcsp_compt(b, e, p->energy, theta, phi);
+      for (k = 0; sum != 0.0 && k < b->cp_nshell[e]; k++) {
+        const double sw = b->cp_occ[(size_t)e * XMI_CP_SH + k] * cdfs[k] / sum;
+        double q;
+        if (sw == 0.0) continue;
+        q = o_shell_q(b->cp_qinv[e] + (size_t)k * XMI_CP_N, orng_uniform(g) * cdfs[k]);
+        ec = o_energy_from_q(p->energy, q, theta, &err);
+        if (err) { t->error = 6; return; }
+        if (ec == 0.0) continue;
+        mu_calc(b, ec, mus_c);
+        murhod = 0.0;
+        for (kk = layer;; kk += step_dir) {
+          murhod = murhod + mus_c[kk] * b->layer_rho[kk] * distances[kk];
+          if (kk == step_max) break;
+        }
+        pesc = exp(-murhod);
+        tw = pconv * pdir * pesc * p->weight * sw;
+        t->var_red[hidx(b, Z, 385, n)] += tw;
+        tally_channel(b, t, n, ec, tw);
+      }
+      goto fluorescence;
+    }
     ec = compton_energy(b, e, p->energy, theta, g, 1, &err);
     if (err) { t->error = 6; return; }
     mu_calc(b, ec, mus_c);
@@ -599,6 +752,7 @@ static void variance_reduction(const xmi_bundle *b, ophoton *p, otally *t) {
     tw = pconv * pdir * pesc * p->weight / 1.0;
     t->var_red[hidx(b, Z, 385, n)] += tw;
     tally_channel(b, t, n, ec, tw);
+  fluorescence:
     /* fluorescence */
     if (n > 1 && p->hist_type[n - 1] < 0) {
       for (s = 0; s < 9; s++) P[s] = b->precalc_xrf[((size_t)e * 9 + s) * b->n_lines + p->hist_slot[n - 1]];
@@ -672,10 +826,17 @@ static int compton(const xmi_bundle *b, ophoton *p, orng *g) {
   phi_i = bilinear(b->phi_icdf, b->icdf_rs, XMI_ICDF_NR, b->phi_thetas, XMI_PHI_NT, r, tt, &err);
   if (err) return 0;
   phi0 = polarisation_phi0(p);
-  p->energy = compton_energy(b, e, p->energy, theta_i, g, 0, &err);
-  if (err) return 0;
-  mu_calc(b, p->energy, p->mus);
-  if (p->energy == 0.0) return 1;
+  if (b->use_advanced_compton) {
+    p->energy = compton_energy_advanced(b, e, p->energy, theta_i, g, &err);
+    if (err) return 0;
+    if (p->energy == 0.0) return 1;
+    mu_calc(b, p->energy, p->mus);
+  } else {
+    p->energy = compton_energy(b, e, p->energy, theta_i, g, 0, &err);
+    if (err) return 0;
+    mu_calc(b, p->energy, p->mus);
+    if (p->energy == 0.0) return 1;
+  }
   update_dirv(p, theta_i, phi_i + phi0);
   update_elecv(p);
   pp = 2.0 * ((cos(theta_i) * cos(phi_i)) * (cos(theta_i) * cos(phi_i)) + sin(phi_i) * sin(phi_i));
@@ -1292,3 +1453,39 @@ int oracle_escape_ratios(const xmi_bundle *b, long nE, double emin, double de, l
 void oracle_philox_block(const uint32_t *ctr, const uint32_t *key, uint32_t *out) { orng_block(ctr, key, out); }
 
 void oracle_threefry_block(const uint32_t *ctr, const uint32_t *key, uint32_t *out) { othreefry4x32(ctr, key, out); }
+
+/* test hooks of the advanced Compton kinematics and profile tables */
+double oracle_compton_qimax(double energy, double Ii, double theta) { return o_qimax(energy, Ii, cos(theta)); }
+double oracle_compton_q_from_energy(double old_e, double new_e, double theta) {
+  return o_q_from_energy(old_e, new_e, cos(theta));
+}
+double oracle_compton_energy_from_q(double a, double Q, double theta, int *err) {
+  *err = 0;
+  return o_energy_from_q(a, Q, theta, err);
+}
+/* shells of element e (shell index, occupancy, binding energy); -1 before
+ * the tables exist */
+int oracle_compton_shells(const xmi_bundle *b, int e, int *shell, double *occ, double *edge) {
+  int k;
+  if (!b->cp_nshell || e < 0 || e >= b->n_elem) return -1;
+  for (k = 0; k < b->cp_nshell[e]; k++) {
+    shell[k] = b->cp_shell[(size_t)e * XMI_CP_SH + k];
+    occ[k] = b->cp_occ[(size_t)e * XMI_CP_SH + k];
+    edge[k] = b->cp_edge[(size_t)e * XMI_CP_SH + k];
+  }
+  return b->cp_nshell[e];
+}
+void oracle_compton_rows(const xmi_bundle *b, int e, int k, double *cdf, double *qinv) {
+  memcpy(cdf, b->cp_cdf[e] + (size_t)k * XMI_CP_N, sizeof(double) * XMI_CP_N);
+  memcpy(qinv, b->cp_qinv[e] + (size_t)k * XMI_CP_N, sizeof(double) * XMI_CP_N);
+}
+/* the shell cumulative values and the sampled scattered energy of the
+ * transport for element e at (energy, theta) from Philox stream (id, stream) */
+double oracle_compton_energy_advanced(const xmi_bundle *b, int e, double energy, double theta, uint64_t id,
+                                      uint32_t stream, double *cdfs, int *err) {
+  orng g;
+  *err = 0;
+  o_shell_cdfs(b, e, energy, theta, cdfs);
+  orng_init(&g, b->seed, id, stream);
+  return compton_energy_advanced(b, e, energy, theta, &g, err);
+}

@@ -397,3 +397,56 @@ def test_escape_ratios_match_oracle():
     lib.xmi_free_input_F(C.byref(h))
     sim.lib.xmi_free_escape_ratios(C.pointer(er))
     sim.close()
+
+
+def heavy_layer_spec(n=5000):
+    spec = configs.config1(n_photons_line=n)
+    spec.layers = [Layer([82, 8, 26], [0.6, 0.3, 0.1], 5.0, 0.01)]
+    spec.reference_layer = 1
+    return spec
+
+
+@pytest.mark.parametrize("which", ["config1", "mixed", "lead"])
+def test_advanced_compton_fp64_matches_oracle(which):
+    """use_advanced_compton = 1: the per-shell impulse-approximation Compton
+    scattering of the transport (src/xmi_main.F90:4785-4983) and of the
+    estimator (src/xmi_variance_reduction.F90:752-947), FP64 GPU against the
+    oracle on the same profile tables and photon streams."""
+    spec = {"config1": lambda: configs.config1(n_photons_line=20000), "mixed": mixed_source_spec,
+            "lead": heavy_layer_spec}[which]()
+    sim, gpu, ref = run_pair(spec, dict(configs.C1_OPTIONS, use_advanced_compton=1))
+    assert_transport_equal(gpu, ref)
+    assert gpu["var_red"][:, 384].sum() > 0
+    sim.close()
+
+
+def test_advanced_compton_fp32_and_batched():
+    """FP32 transport with the advanced Compton scattering tracks FP64 (2e-3
+    on the line totals and the spectrum orders), and a batch mixing an
+    advanced-Compton configuration with a default one gives each its single
+    run's result."""
+    spec = heavy_layer_spec(20000)
+    opts = dict(configs.C1_OPTIONS, use_advanced_compton=1)
+    s64 = Simulation(spec, options=opts, gpu=gpu_options(precision=0, seed=SEED))
+    s32 = Simulation(spec, options=opts, gpu=gpu_options(precision=1, seed=SEED))
+    r64, r32 = s64.msim(), s32.msim()
+    v64, v32 = r64["var_red"].sum(axis=2), r32["var_red"].sum(axis=2)
+    assert v32.sum() == pytest.approx(v64.sum(), rel=2e-3)
+    assert v32[:, 384].sum() == pytest.approx(v64[:, 384].sum(), rel=2e-3)
+    np.testing.assert_allclose(r32["channels"].sum(axis=1), r64["channels"].sum(axis=1), rtol=2e-3)
+    s64.close()
+    s32.close()
+    sims = [Simulation(heavy_layer_spec(3000), options=opts, gpu=gpu_options(seed=SEED)),
+            Simulation(mixed_source_spec(), options=configs.C1_OPTIONS, gpu=gpu_options(seed=SEED))]
+    for s in sims:
+        s.solid_angle()
+    batched = Simulation.msim_batch(sims)
+    for s, b in zip(sims, batched):
+        single = s.msim()
+        np.testing.assert_allclose(b["var_red"], single["var_red"], rtol=1e-9,
+                                   atol=1e-12 * abs(single["var_red"]).max())
+        np.testing.assert_allclose(b["channels"], single["channels"], rtol=1e-9,
+                                   atol=1e-12 * abs(single["channels"]).max())
+        s.free_raw(b)
+        s.free_raw(single)
+        s.close()

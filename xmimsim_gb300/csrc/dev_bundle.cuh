@@ -62,6 +62,11 @@ struct DevBundle {
   int n_ent, stage_max;
   const int *ent_off, *ent_slot, *ent_shell;
   const R *ent_coef, *ent_pmu;
+  /* per-shell Compton profiles (advanced Compton; null unless in use) */
+  int use_adv_compton;
+  const int *cp_nshell;                 /* [n_elem] */
+  const double *cp_occ, *cp_edge;       /* [n_elem][XMI_CP_SH] */
+  const R *const *cp_cdf, *const *cp_qinv; /* [n_elem] -> [nshell][XMI_CP_N] */
 };
 
 /* Tally buffers of one run (device pointers). */

@@ -209,6 +209,34 @@ const int *upload_int(DevSide &s, const int *src, size_t n) {
   return (const int *)p;
 }
 
+/* the Compton profile tables of the bundle's elements (advanced Compton):
+ * added to a device copy on first use; false on a failed upload */
+template <typename R>
+bool upload_compton_profiles(const xmi_bundle &h, DevSide &s, xmi::DevBundle<R> &d) {
+  if (d.cp_cdf || !h.cp_nshell) return true;
+  const int E = h.n_elem;
+  std::vector<const R *> pc(E > 0 ? E : 1, nullptr), pq(E > 0 ? E : 1, nullptr);
+  for (int e = 0; e < E; e++) {
+    const size_t n = (size_t)h.cp_nshell[e] * XMI_CP_N;
+    if (!(pc[e] = shared_table<R>(h.cp_cdf[e], n)) || !(pq[e] = shared_table<R>(h.cp_qinv[e], n))) return false;
+  }
+  void *a = nullptr, *q = nullptr;
+  if (cudaMalloc(&a, sizeof(const R *) * pc.size()) != cudaSuccess) return false;
+  s.allocs.push_back(a);
+  if (cudaMalloc(&q, sizeof(const R *) * pq.size()) != cudaSuccess) return false;
+  s.allocs.push_back(q);
+  cudaMemcpy(a, pc.data(), sizeof(const R *) * pc.size(), cudaMemcpyHostToDevice);
+  cudaMemcpy(q, pq.data(), sizeof(const R *) * pq.size(), cudaMemcpyHostToDevice);
+  d.cp_nshell = upload_int(s, h.cp_nshell, E);
+  d.cp_occ = upload<double>(s, h.cp_occ, (size_t)E * XMI_CP_SH);
+  d.cp_edge = upload<double>(s, h.cp_edge, (size_t)E * XMI_CP_SH);
+  if (!d.cp_nshell || !d.cp_occ || !d.cp_edge || cudaGetLastError() != cudaSuccess) return false;
+  d.cp_cdf = (const R *const *)a;
+  d.cp_qinv = (const R *const *)q;
+  return true;
+}
+
+
 const double *upload_d(DevSide &s, const double *src, size_t n) {
   if (n == 0) n = 1;
   void *p = nullptr;
@@ -225,6 +253,7 @@ void fill_scalars(const xmi_bundle &h, xmi::DevBundle<R> &d) {
   d.nch = h.nchannels;
   d.use_vr = h.use_vr;
   d.use_M_lines = h.use_M_lines;
+  d.use_adv_compton = h.use_advanced_compton && d.cp_cdf ? 1 : 0;
   d.line_last = h.line_last;
   d.max_shell = h.max_shell;
   d.escape_mode = h.escape_mode;
@@ -284,6 +313,9 @@ void fill_scalars(const xmi_bundle &h, xmi::DevBundle<R> &d) {
 template <typename R>
 bool upload_tables(const xmi_bundle &h, DevSide &s, xmi::DevBundle<R> &d) {
   s.release();
+  d.cp_nshell = nullptr;
+  d.cp_occ = d.cp_edge = nullptr;
+  d.cp_cdf = d.cp_qinv = nullptr;
   fill_scalars(h, d);
   const size_t E = h.n_elem, NL = h.n_lines;
   d.layer_el = upload_int(s, h.layer_el, h.n_layer_el);
@@ -371,10 +403,18 @@ int xmi_dev_sync_tables(struct xmi_tables_handle *t, int precision) {
   if (!ensure_device()) return 0;
   DevState *s = state_of(t);
   if (precision == 0) {
-    if (!s->d64.valid) return upload_tables<double>(t->b, s->d64, s->b64) ? 1 : 0;
+    if (!s->d64.valid && !upload_tables<double>(t->b, s->d64, s->b64)) return 0;
+    if (!upload_compton_profiles<double>(t->b, s->d64, s->b64)) {
+      xmi_set_error("device upload of the Compton profile tables failed");
+      return 0;
+    }
     fill_scalars(t->b, s->b64);
   } else {
-    if (!s->d32.valid) return upload_tables<float>(t->b, s->d32, s->b32) ? 1 : 0;
+    if (!s->d32.valid && !upload_tables<float>(t->b, s->d32, s->b32)) return 0;
+    if (!upload_compton_profiles<float>(t->b, s->d32, s->b32)) {
+      xmi_set_error("device upload of the Compton profile tables failed");
+      return 0;
+    }
     fill_scalars(t->b, s->b32);
   }
   return 1;
@@ -581,11 +621,6 @@ static int prepare_run(xmi_inputFPtr in, xmi_hdf5FPtr t, xmi_main_options *optio
     xmi_set_error("xmi_gpu_prepare_run: NULL argument");
     return 0;
   }
-  if (options->use_advanced_compton == 1) {
-    /* the per-shell impulse-approximation Compton of src/xmi_main.F90:4785-4983 is not implemented */
-    xmi_set_error("use_advanced_compton = 1 is not supported; the default Doppler-broadened Compton is used with 0");
-    return 0;
-  }
   int cascade;
   if (options->use_cascade_auger == 0 && options->use_cascade_radiative == 0) cascade = XMI_CASCADE_NONE;
   else if (options->use_cascade_auger == 1 && options->use_cascade_radiative == 0) cascade = XMI_CASCADE_NONRADIATIVE;
@@ -604,6 +639,8 @@ static int prepare_run(xmi_inputFPtr in, xmi_hdf5FPtr t, xmi_main_options *optio
     if (r >= R) r = R - 1;
     xmi_bundle_set_run(in, t, options, n_mpi_hosts, r, R);
   }
+  /* per-shell Compton profiles of the advanced Compton scattering */
+  if (options->use_advanced_compton == 1 && !xmi_bundle_compton_profiles(&t->b)) return 0;
   attach_solid_angles(t, sa);
   if (need_solid_angles && options->use_variance_reduction && (!sa || !sa->solid_angles) &&
       !(in->gpu.use_surrogate && in->surrogate)) {
@@ -647,7 +684,7 @@ template <typename R, bool Batched>
 static int launch_wavefront(cudaStream_t st, WfBuffers &wb, const xmi::DevBundle<R> &b0, const xmi::DevTally &t0,
                             const xmi::DevBundle<R> *bundles, const xmi::DevTally *tallies, const long long *cfg_first,
                             int n_cfg, long long w0, long long w1, int max_iter, const xmi::VrQueue<R> &vq,
-                            int threads, int blocks) {
+                            int threads, int blocks, bool adv) {
   const long long cap = wb.cap;
   xmi::WfLists q;
   q.active[0] = wb.lists;
@@ -662,8 +699,12 @@ static int launch_wavefront(cudaStream_t st, WfBuffers &wb, const xmi::DevBundle
     const int next = cur ^ 1;
     xmi::wf_reset<<<1, 32, 0, st>>>(q, next);
     xmi::wf_step<R, Batched><<<blocks, threads, 0, st>>>(b0, t0, bundles, tallies, ps, q, cur, cap, vq);
-    for (int k = 0; k < 3; k++)
-      xmi::wf_interact<R, Batched><<<blocks, threads, 0, st>>>(b0, t0, bundles, tallies, ps, q, k, next, cap);
+    for (int k = 0; k < 3; k++) {
+      if (k == 1 && adv)
+        xmi::wf_interact<R, Batched, true><<<blocks, threads, 0, st>>>(b0, t0, bundles, tallies, ps, q, k, next, cap);
+      else
+        xmi::wf_interact<R, Batched><<<blocks, threads, 0, st>>>(b0, t0, bundles, tallies, ps, q, k, next, cap);
+    }
     launches += 5;
     cur = next;
   }
@@ -891,13 +932,13 @@ static int stage_cap_for(int stage_max) {
   return stage_max < limit ? stage_max : limit;
 }
 
-template <typename R>
+template <typename R, bool Adv = false>
 static int estimator_blocks(int stage_cap, size_t *smem) {
   *smem = (size_t)8 * (stage_cap + xmi::kScratchPerWarp) * sizeof(R);
   if (*smem > 48 * 1024)
-    cudaFuncSetAttribute(xmi::estimator_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)*smem);
+    cudaFuncSetAttribute(xmi::estimator_kernel<R, Adv>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)*smem);
   int per_sm = 1;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, xmi::estimator_kernel<R>, 256, *smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, xmi::estimator_kernel<R, Adv>, 256, *smem);
   if (per_sm < 1) per_sm = 1;
   return num_sms() * per_sm;
 }
@@ -949,7 +990,8 @@ static bool launch_single(DevState *s, xmi::DevBundle<R> &d, const xmi::DevTally
   g_timing.h2d_bytes += (long long)(sizeof(d) + sizeof(tl));
   const int stage_cap = stage_cap_for<R>(h.stage_max);
   size_t smem = 0;
-  const int est_blocks = estimator_blocks<R>(stage_cap, &smem);
+  const bool adv = d.use_adv_compton != 0;
+  const int est_blocks = adv ? estimator_blocks<R, true>(stage_cap, &smem) : estimator_blocks<R>(stage_cap, &smem);
   const long long chunk_cap = h.use_vr ? qev / (h.n_interactions > 0 ? h.n_interactions : 1) : kMaxChunkPhotons;
   /* back to the pool once the run's stream is idle */
   struct Borrow {
@@ -968,12 +1010,17 @@ static bool launch_single(DevState *s, xmi::DevBundle<R> &d, const xmi::DevTally
   const int rounds = wavefront_rounds(h);
   auto transport = [&](long long w0, long long w1, const xmi::VrQueue<R> &vq) {
     return launch_wavefront<R, false>(s->stream, wf, d, tl, nullptr, nullptr, nullptr, 1, w0, w1, rounds, vq,
-                                      threads, sms * blocks_per_sm);
+                                      threads, sms * blocks_per_sm, adv);
   };
   auto estimator = [&](const xmi::VrQueue<R> &vq, const int *order, unsigned long long *work) {
-    xmi::estimator_kernel<R><<<est_blocks, 256, smem, s->stream>>>(
-        (const xmi::DevBundle<R> *)s->d_bundle, s->d_tally, 1, vq.ev, order, vq.count, vq.cap, work, stage_cap,
-        &s->counters[1]);
+    if (adv)
+      xmi::estimator_kernel<R, true><<<est_blocks, 256, smem, s->stream>>>(
+          (const xmi::DevBundle<R> *)s->d_bundle, s->d_tally, 1, vq.ev, order, vq.count, vq.cap, work, stage_cap,
+          &s->counters[1]);
+    else
+      xmi::estimator_kernel<R><<<est_blocks, 256, smem, s->stream>>>(
+          (const xmi::DevBundle<R> *)s->d_bundle, s->d_tally, 1, vq.ev, order, vq.count, vq.cap, work, stage_cap,
+          &s->counters[1]);
   };
   auto surrogate = [&](const xmi::VrQueue<R> &vq, int *fb, unsigned long long *fb_count) -> int {
     if (!d.use_surrogate) return 0;
@@ -1165,9 +1212,11 @@ bool launch_batch(int n, DevState **st, xmi_hdf5FPtr *t, const xmi::DevTally *tl
   const int sms = num_sms();
   int stage_max = 1;
   for (int c = 0; c < n; c++) stage_max = t[c]->b.stage_max > stage_max ? t[c]->b.stage_max : stage_max;
+  bool adv = false; /* kernels with the advanced Compton scattering if any configuration uses it */
+  for (int c = 0; c < n; c++) adv = adv || (t[c]->b.use_advanced_compton && t[c]->b.cp_nshell);
   const int stage_cap = stage_cap_for<R>(stage_max);
   size_t smem = 0;
-  const int est_blocks = estimator_blocks<R>(stage_cap, &smem);
+  const int est_blocks = adv ? estimator_blocks<R, true>(stage_cap, &smem) : estimator_blocks<R>(stage_cap, &smem);
   int rounds = 1;
   for (int c = 0; c < n; c++) rounds = wavefront_rounds(t[c]->b) > rounds ? wavefront_rounds(t[c]->b) : rounds;
   const long long chunk_cap = vr ? qev / N : kMaxChunkPhotons;
@@ -1176,11 +1225,15 @@ bool launch_batch(int n, DevState **st, xmi_hdf5FPtr *t, const xmi::DevTally *tl
   xmi::DevTally unused_t{};
   auto transport = [&](long long w0, long long w1, const xmi::VrQueue<R> &vq) {
     return launch_wavefront<R, true>(B.stream, B.wf, unused_b, unused_t, db, B.tallies, B.cfg_first, n, w0, w1,
-                                     rounds, vq, threads, sms * blocks_per_sm);
+                                     rounds, vq, threads, sms * blocks_per_sm, adv);
   };
   auto estimator = [&](const xmi::VrQueue<R> &vq, const int *order, unsigned long long *work) {
-    xmi::estimator_kernel<R><<<est_blocks, 256, smem, B.stream>>>(db, B.tallies, n, vq.ev, order, vq.count, vq.cap,
-                                                                  work, stage_cap, B.flags);
+    if (adv)
+      xmi::estimator_kernel<R, true><<<est_blocks, 256, smem, B.stream>>>(db, B.tallies, n, vq.ev, order, vq.count,
+                                                                          vq.cap, work, stage_cap, B.flags);
+    else
+      xmi::estimator_kernel<R><<<est_blocks, 256, smem, B.stream>>>(db, B.tallies, n, vq.ev, order, vq.count, vq.cap,
+                                                                    work, stage_cap, B.flags);
   };
   /* flags: [0] estimator error, [1] events, [2] integrator fallbacks of the
    * surrogate, [3] surrogate error */

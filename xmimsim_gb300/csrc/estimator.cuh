@@ -38,6 +38,44 @@ __device__ __forceinline__ void chan_add(const DevBundle<R> &b, const DevTally &
     atomicAdd(&t.chan[(size_t)n * b.nch + ch], (double)w);
 }
 
+/* xmi_compton_varred (src/xmi_variance_reduction.F90:752-947), the estimator
+ * of the advanced Compton scattering: one scattered energy per shell of
+ * element e, drawn from g for every shell with a non-zero share, each
+ * weighted by that share; the spectrum gets every shell's energy.  Returns
+ * the element's Compton history weight (the sum over shells).  base = the
+ * event's pconv x pdir x weight (0 for an idle lane). */
+template <typename R>
+__device__ __noinline__ R compton_advanced_est(const DevBundle<R> &b, const DevTally &t, int e, const VrEvent<R> &ev,
+                                               R base, xmi_rng *g, bool valid, bool &ok) {
+  double cdfs[XMI_CP_SH];
+  const double E = (double)ev.E, c = cos((double)ev.theta);
+  const double sum = cp_shell_cdfs(b, e, E, c, cdfs);
+  R total = (R)0;
+  if (sum == 0.0) return total;
+  const int ns = b.cp_nshell[e];
+  for (int k = 0; k < ns; k++) {
+    const double sw = b.cp_occ[e * XMI_CP_SH + k] * cdfs[k] / sum;
+    if (sw == 0.0) continue;
+    const double q = cp_shell_q(b.cp_qinv[e] + (size_t)k * XMI_CP_N, (double)uni<R>(g) * cdfs[k]);
+    bool bad = false;
+    const double ec = cp_energy_from_q(E, q, c, bad);
+    if (bad) {
+      if (valid) ok = false;
+      continue;
+    }
+    if (ec == 0.0) continue;
+    R mus_c[XMI_MAXL];
+    mu_calc(b, (R)ec, mus_c);
+    R murhod = (R)0;
+#pragma unroll
+    for (int j = 0; j < XMI_MAXL; j++) murhod += mus_c[j] * ev.rd[j];
+    const R tw = base * exp(-murhod) * (R)sw;
+    total += tw;
+    if (valid) chan_add(b, t, ev.n, (R)ec, tw);
+  }
+  return total;
+}
+
 /* History contributions of the events of one key (configuration, layer,
  * order) are summed across the warp and staged in a warp-private
  * shared-memory row, stage[j]: j < n_line = the layer's line entries (entry
@@ -99,7 +137,7 @@ __device__ __forceinline__ void contribute(const DevTally &t, const StageRow<R> 
   }
 }
 
-template <typename R, bool Uniform>
+template <typename R, bool Uniform, bool Adv>
 __device__ __forceinline__ void estimate_event(const DevBundle<R> &b, const DevTally &t, const StageRow<R> &st, const VrEvent<R> &ev,
                                bool valid, bool &ok) {
   const int layer = ev.layer, n = ev.n;
@@ -120,24 +158,31 @@ __device__ __forceinline__ void estimate_event(const DevBundle<R> &b, const DevT
     const R twr = live * (pconv * (ev.pR * qtab(b.ff2[e], ev.q)) * ev.pesc_rayl * ev.w);
     contribute<R, Uniform>(t, st, n_line + 2 * i, hbase + rs, twr);
     rayl_sum += twr;
-    /* Compton: one Doppler-broadened energy per element (N_COMPTON_VARRED = 1) */
+    /* Compton: one Doppler-broadened energy per element (N_COMPTON_VARRED = 1),
+     * or one per shell with the advanced Compton scattering */
     xmi_rng g;
     xmi_rng_init(&g, b.seed, (uint64_t)ev.id, vr_stream(n, i));
-    bool cok = true;
-    const R ec = compton_energy_est(b, e, ce, &g, cok);
-    R twc = (R)0;
-    if (cok) {
-      R mus_c[XMI_MAXL];
-      mu_calc(b, ec, mus_c);
-      R murhod = (R)0;
+    if (Adv && b.use_adv_compton) {
+      const R twa = compton_advanced_est(b, t, e, ev, live * (pconv * (ev.pC * qtab(b.sf[e], ev.q))) * ev.w, &g,
+                                         valid, ok);
+      contribute<R, Uniform>(t, st, n_line + 2 * i + 1, hbase + rs + 1, twa);
+    } else {
+      bool cok = true;
+      const R ec = compton_energy_est(b, e, ce, &g, cok);
+      R twc = (R)0;
+      if (cok) {
+        R mus_c[XMI_MAXL];
+        mu_calc(b, ec, mus_c);
+        R murhod = (R)0;
 #pragma unroll
-      for (int j = 0; j < XMI_MAXL; j++) murhod += mus_c[j] * ev.rd[j];
-      twc = live * (pconv * (ev.pC * qtab(b.sf[e], ev.q)) * exp(-murhod) * ev.w);
-    } else if (valid) {
-      ok = false;
+        for (int j = 0; j < XMI_MAXL; j++) murhod += mus_c[j] * ev.rd[j];
+        twc = live * (pconv * (ev.pC * qtab(b.sf[e], ev.q)) * exp(-murhod) * ev.w);
+      } else if (valid) {
+        ok = false;
+      }
+      contribute<R, Uniform>(t, st, n_line + 2 * i + 1, hbase + rs + 1, twc);
+      if (valid) chan_add(b, t, n, ec, twc);
     }
-    contribute<R, Uniform>(t, st, n_line + 2 * i + 1, hbase + rs + 1, twc);
-    if (valid) chan_add(b, t, n, ec, twc);
     /* fluorescence: shell probabilities at the photon energy (first order or
      * after scattering) or at the exciting line's energy (after fluorescence) */
     R P[XMI_NSHELL];
@@ -183,7 +228,7 @@ constexpr int kScratchPerWarp = 32 * XMI_MAXL + 32 * XMI_NSHELL;
  * lane looping over the 32 events (their path sums and shell factors read
  * from shared memory, broadcast) and accumulating its own line's history in a
  * register -- no cross-lane reduction per line. */
-template <typename R>
+template <typename R, bool Adv>
 __device__ __forceinline__ void estimate_event_uniform(const DevBundle<R> &b, const DevTally &t, const StageRow<R> &st, R *scratch,
                                        const VrEvent<R> &ev, bool valid, bool &ok) {
   const int lane = threadIdx.x & 31;
@@ -208,24 +253,31 @@ __device__ __forceinline__ void estimate_event_uniform(const DevBundle<R> &b, co
     const R twr = live * (pconv * (ev.pR * qtab(b.ff2[e], ev.q)) * ev.pesc_rayl * ev.w);
     contribute<R, true>(t, st, st.n_line + 2 * i, hbase + rs, twr);
     rayl_sum += twr;
-    /* Compton: one Doppler-broadened energy per element (N_COMPTON_VARRED = 1) */
+    /* Compton: one Doppler-broadened energy per element (N_COMPTON_VARRED = 1),
+     * or one per shell with the advanced Compton scattering */
     xmi_rng g;
     xmi_rng_init(&g, b.seed, (uint64_t)ev.id, vr_stream(n, i));
-    bool cok = true;
-    const R ec = compton_energy_est(b, e, ce, &g, cok);
-    R twc = (R)0;
-    if (cok) {
-      R mus_c[XMI_MAXL];
-      mu_calc(b, ec, mus_c);
-      R murhod = (R)0;
+    if (Adv && b.use_adv_compton) {
+      const R twa = compton_advanced_est(b, t, e, ev, live * (pconv * (ev.pC * qtab(b.sf[e], ev.q))) * ev.w, &g,
+                                         valid, ok);
+      contribute<R, true>(t, st, st.n_line + 2 * i + 1, hbase + rs + 1, twa);
+    } else {
+      bool cok = true;
+      const R ec = compton_energy_est(b, e, ce, &g, cok);
+      R twc = (R)0;
+      if (cok) {
+        R mus_c[XMI_MAXL];
+        mu_calc(b, ec, mus_c);
+        R murhod = (R)0;
 #pragma unroll
-      for (int j = 0; j < XMI_MAXL; j++) murhod += mus_c[j] * ev.rd[j];
-      twc = live * (pconv * (ev.pC * qtab(b.sf[e], ev.q)) * exp(-murhod) * ev.w);
-    } else if (valid) {
-      ok = false;
+        for (int j = 0; j < XMI_MAXL; j++) murhod += mus_c[j] * ev.rd[j];
+        twc = live * (pconv * (ev.pC * qtab(b.sf[e], ev.q)) * exp(-murhod) * ev.w);
+      } else if (valid) {
+        ok = false;
+      }
+      contribute<R, true>(t, st, st.n_line + 2 * i + 1, hbase + rs + 1, twc);
+      if (valid) chan_add(b, t, n, ec, twc);
     }
-    contribute<R, true>(t, st, st.n_line + 2 * i + 1, hbase + rs + 1, twc);
-    if (valid) chan_add(b, t, n, ec, twc);
     /* shell factors of this event for element i */
     R P[XMI_NSHELL];
     if (ev.h_slot >= 0) {
@@ -307,7 +359,7 @@ constexpr int kEventsPerGrab = 256;
  * not batched).  Warps grab kEventsPerGrab consecutive events at a time from
  * the counter `work`; stage rows of stage_cap values per warp sit in dynamic
  * shared memory. */
-template <typename R>
+template <typename R, bool Adv = false>
 __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 3) estimator_kernel(const DevBundle<R> *bundles, const DevTally *tallies,
                                                            int n_cfg, const VrEvent<R> *events, const int *order,
                                                            const unsigned long long *count, long long cap,
@@ -350,10 +402,10 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 3) estimator_kernel(
             st_cfg = ev.cfg;
           }
         }
-        if (st.key == key) estimate_event_uniform<R>(b, t, st, scratch, ev, valid, ok);
-        else estimate_event<R, false>(b, t, st, ev, valid, ok);
+        if (st.key == key) estimate_event_uniform<R, Adv>(b, t, st, scratch, ev, valid, ok);
+        else estimate_event<R, false, Adv>(b, t, st, ev, valid, ok);
       } else {
-        estimate_event<R, false>(b, t, st, ev, valid, ok);
+        estimate_event<R, false, Adv>(b, t, st, ev, valid, ok);
       }
     }
   }

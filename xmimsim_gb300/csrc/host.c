@@ -640,6 +640,10 @@ static void phi_icdf_row(double t, const double *rs, double *out) {
 typedef struct {
   double *rayl, *compt, *dop, *ff2, *sf;
   int ready;
+  /* per-shell Compton profiles, filled on demand (cp_ready) */
+  int cp_n, cp_shell[XMI_CP_SH], cp_ready;
+  double cp_occ[XMI_CP_SH], cp_edge[XMI_CP_SH], cp_sig[XMI_CP_SH];
+  double *cp_cdf, *cp_qinv;
 } z_tables;
 static z_tables z_cache[XRL_MAXZ + 1];
 static pthread_mutex_t z_cache_lock = PTHREAD_MUTEX_INITIALIZER;
@@ -685,6 +689,134 @@ static void z_tables_fill(const int *Zs, int n, const double *energies, const do
   pthread_mutex_unlock(&z_cache_lock);
 }
 
+/* Per-shell Compton profile tables of the advanced Compton scattering,
+ * src/xmi_data_f.F90:1124-1230.  Shells: K, then every shell L1.. with
+ * electrons, each with its occupancy and binding energy.  Shell k's profile
+ * is the stand-in atomic model's partial profile (the xrl_ComptonProfile
+ * shape: n 8 / (3 pi s) / (1 + (pz/s)^2)^3, s from the binding energy).
+ *  cdf[k][j]:  trapezoid integral of the profile over [0, Q_j] on the
+ *              10001-point grid Q_j = 100 j / 10000, scaled to 0.5 at Q = 100
+ *              (the reference's rule, src/xmi_data_f.F90:1189-1197);
+ *  qinv[k][j]: the Q where the profile's integral, scaled the same way,
+ *              reaches c_j = 0.5 j / 10000.  The reference inverts a 10^7-point
+ *              trapezoid integral (src/xmi_data_f.F90:1198-1228), which
+ *              converges to the exact inverse used here: the shape integrates
+ *              in closed form, int_0^X (1+x^2)^-3 dx =
+ *              X / (4 (1+X^2)^2) + 3 X / (8 (1+X^2)) + 3/8 atan X. */
+static double cp_shape_integral(double X) {
+  const double u = 1.0 + X * X;
+  return X / (4.0 * u * u) + 3.0 * X / (8.0 * u) + 0.375 * atan(X);
+}
+
+static void cp_shell_tables(double sig, double *cdf, double *qinv) {
+  const int N = XMI_CP_N;
+  const double dq = 100.0 * 1.0 / (N - 1.0) - 100.0 * 0.0 / (N - 1.0);
+  const double xm = 100.0 / sig, gm = cp_shape_integral(xm);
+  double prev = 0.0, q0 = 0.0;
+  int j;
+  cdf[0] = 0.0;
+  for (j = 0; j < N; j++) {
+    const double q = 100.0 * j / (N - 1.0), x = q / sig, u = 1.0 + x * x;
+    const double f = 1.0 / (u * u * u); /* the constant factor cancels in the scaling */
+    if (j > 0) cdf[j] = cdf[j - 1] + dq * (f + prev) * 0.5;
+    prev = f;
+  }
+  {
+    const double last = cdf[N - 1];
+    for (j = 1; j < N; j++) cdf[j] = cdf[j] * 0.5 / last;
+  }
+  /* inverse: G(X) / G(xm) = 2 c_j, Newton steps inside a shrinking bracket */
+  qinv[0] = 0.0;
+  for (j = 1; j < N - 1; j++) {
+    const double target = (0.5 * j / (N - 1.0)) * 2.0 * gm;
+    double lo = q0 / sig, hi = xm, x = lo;
+    int it;
+    for (it = 0; it < 200; it++) {
+      const double g = cp_shape_integral(x) - target, u = 1.0 + x * x;
+      double xn;
+      if (g > 0.0) hi = x; else lo = x;
+      xn = x - g * (u * u * u);
+      if (!(xn > lo && xn < hi)) xn = 0.5 * (lo + hi);
+      if (fabs(xn - x) <= 1e-15 * (1.0 + x)) { x = xn; break; }
+      x = xn;
+    }
+    qinv[j] = x * sig;
+    q0 = qinv[j];
+  }
+  qinv[N - 1] = 100.0;
+}
+
+static void cp_tables_fill(const int *Zs, int n) {
+  int todo[XRL_MAXZ + 1], nt = 0, i, k, tasks = 0;
+  int task_z[(XRL_MAXZ + 1) * XMI_CP_SH], task_k[(XRL_MAXZ + 1) * XMI_CP_SH];
+  pthread_mutex_lock(&z_cache_lock);
+  for (i = 0; i < n; i++) {
+    int Z = Zs[i], seen = 0;
+    if (Z < 1 || Z > XRL_MAXZ || z_cache[Z].cp_ready) continue;
+    for (k = 0; k < nt; k++) seen |= todo[k] == Z;
+    if (!seen) todo[nt++] = Z;
+  }
+  for (k = 0; k < nt; k++) {
+    const int Z = todo[k];
+    z_tables *zt = &z_cache[Z];
+    int s, m = 0;
+    for (s = 0; s < XRL_NSHELL_ALL && m < XMI_CP_SH; s++) {
+      const double occ = xrl_ElectronConfig(Z, s);
+      double eb;
+      if (s > 0 && !(occ > 0.0)) continue;
+      eb = xrl_EdgeEnergy(Z, s);
+      zt->cp_shell[m] = s;
+      zt->cp_occ[m] = occ;
+      zt->cp_edge[m] = eb;
+      if (eb < 0.005) eb = 0.005;
+      zt->cp_sig[m] = sqrt(2.0 * eb / 0.0272114);
+      task_z[tasks] = Z;
+      task_k[tasks++] = m;
+      m++;
+    }
+    zt->cp_n = m;
+    zt->cp_cdf = (double *)malloc(sizeof(double) * (size_t)m * XMI_CP_N);
+    zt->cp_qinv = (double *)malloc(sizeof(double) * (size_t)m * XMI_CP_N);
+  }
+#pragma omp parallel for schedule(dynamic, 1)
+  for (i = 0; i < tasks; i++) {
+    z_tables *zt = &z_cache[task_z[i]];
+    const size_t o = (size_t)task_k[i] * XMI_CP_N;
+    cp_shell_tables(zt->cp_sig[task_k[i]], zt->cp_cdf + o, zt->cp_qinv + o);
+  }
+  for (k = 0; k < nt; k++) z_cache[todo[k]].cp_ready = 1;
+  pthread_mutex_unlock(&z_cache_lock);
+}
+
+int xmi_bundle_compton_profiles(xmi_bundle *b) {
+  const size_t E = (size_t)(b->n_elem > 0 ? b->n_elem : 1);
+  int e, k;
+  if (b->cp_nshell) return 1;
+  cp_tables_fill(b->elem_Z, b->n_elem);
+  b->cp_nshell = (int *)calloc(E, sizeof(int));
+  b->cp_shell = (int *)calloc(E * XMI_CP_SH, sizeof(int));
+  b->cp_occ = (double *)calloc(E * XMI_CP_SH, sizeof(double));
+  b->cp_edge = (double *)calloc(E * XMI_CP_SH, sizeof(double));
+  b->cp_cdf = (const double **)calloc(E, sizeof(double *));
+  b->cp_qinv = (const double **)calloc(E, sizeof(double *));
+  if (!b->cp_nshell || !b->cp_shell || !b->cp_occ || !b->cp_edge || !b->cp_cdf || !b->cp_qinv) {
+    xmi_set_error("out of host memory for the Compton profile tables");
+    return 0;
+  }
+  for (e = 0; e < b->n_elem; e++) {
+    const z_tables *zt = &z_cache[b->elem_Z[e]];
+    b->cp_nshell[e] = zt->cp_n;
+    for (k = 0; k < zt->cp_n; k++) {
+      b->cp_shell[(size_t)e * XMI_CP_SH + k] = zt->cp_shell[k];
+      b->cp_occ[(size_t)e * XMI_CP_SH + k] = zt->cp_occ[k];
+      b->cp_edge[(size_t)e * XMI_CP_SH + k] = zt->cp_edge[k];
+    }
+    b->cp_cdf[e] = zt->cp_cdf;
+    b->cp_qinv[e] = zt->cp_qinv;
+  }
+  return 1;
+}
+
 /* azimuth inverse CDFs of polarised scattering: independent of the element,
  * computed once per process and shared like the tables above */
 static const double *phi_table(const double *thetas, const double *rs) {
@@ -712,6 +844,8 @@ void xmi_bundle_free(xmi_bundle *b) {
   free(b->doppler_rs); free((void *)b->doppler_icdf); free((void *)b->ff2); free((void *)b->sf);
   free(b->items);
   free(b->ent_off); free(b->ent_slot); free(b->ent_shell); free(b->ent_coef); free(b->ent_pmu);
+  free(b->cp_nshell); free(b->cp_shell); free(b->cp_occ); free(b->cp_edge);
+  free((void *)b->cp_cdf); free((void *)b->cp_qinv);
   memset(b, 0, sizeof(*b));
 }
 
@@ -1091,6 +1225,7 @@ void xmi_bundle_set_run(struct xmi_input_handle *in, struct xmi_tables_handle *t
   b->n_interactions = inp->general->n_interactions_trajectory;
   b->use_vr = options->use_variance_reduction;
   b->escape_mode = options->escape_ratios_mode;
+  b->use_advanced_compton = options->use_advanced_compton == 1;
   b->nchannels = inp->detector->nchannels;
   b->gain = inp->detector->gain;
   b->zero = inp->detector->zero;

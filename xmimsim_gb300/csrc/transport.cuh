@@ -652,6 +652,135 @@ __device__ __forceinline__ R compton_energy_est(const DevBundle<R> &b, int e, co
   return (R)0;
 }
 
+/* ---------------- advanced Compton: per-shell impulse approximation ----------------
+ * src/xmi_main.F90:4785-4983 (transport), src/xmi_variance_reduction.F90:752-947
+ * (estimator), src/xmi_aux_f.F90:1951-2074 (momentum kinematics).  The
+ * kinematics run in FP64 in both precisions: the quadratic for the scattered
+ * energy cancels badly at small Q.  Tables are read in the working precision.
+ * MEC2 here is xraylib's constant; 1E-8, 1E-4 and 1E-10 are the reference's
+ * default-real literals. */
+constexpr double kXrlMec2 = 510.998928;
+
+/* xmi_get_qimax (c = cos theta) */
+__device__ __forceinline__ double cp_qimax(double energy, double Ii, double c) {
+  if (Ii != 0.0 && energy < Ii) return 0.0;
+  const double emi = energy - Ii;
+  const double q = 137.0 * (emi * energy * (1.0 - c) / kXrlMec2 - Ii);
+  return q / sqrt(emi * emi + energy * energy - 2.0 * emi * energy * c);
+}
+
+/* xmi_get_q_from_energy */
+__device__ __forceinline__ double cp_q_from_energy(double old_e, double new_e, double c) {
+  const double q = 137.0 * (new_e - old_e + (1.0 - c) * old_e * new_e / kXrlMec2);
+  return q / sqrt(new_e * new_e + old_e * old_e - 2.0 * old_e * new_e * c);
+}
+
+/* xmi_get_energy_from_q with xmi_poly_solve_quadratic; bad = true where the
+ * reference stops the program (neither root has the sign of Q) */
+static __device__ __noinline__ double cp_energy_from_q(double a, double Q, double c, bool &bad) {
+  const double b = kXrlMec2, k2 = 137.0 * 137.0;
+  if (fabs(c - 1.0) < (double)1e-8f) return 0.0;
+  if (fabs(Q) < (double)1e-4f) return a / (1.0 + a * (1.0 - c) / b);
+  const double d = 1.0 + a / b - a * c / b;
+  const double aq = k2 * (d * d) - Q * Q;
+  const double bq = -(2.0 * k2 * a * d) + 2.0 * a * c * (Q * Q);
+  const double cq = k2 * (a * a) - (a * a) * (Q * Q);
+  double e1, e2;
+  if (aq == 0.0) {
+    if (bq == 0.0) return 0.0;
+    e1 = e2 = -1.0 * cq / bq;
+  } else {
+    const double delta = bq * bq - 4.0 * aq * cq;
+    if (delta < 0.0) return 0.0;
+    if (delta == 0.0) {
+      e1 = e2 = -bq / 2.0 / aq;
+    } else {
+      const double sd = sqrt(delta), r1 = (-bq + sd) / 2.0 / aq, r2 = (-bq - sd) / 2.0 / aq;
+      e1 = fmin(r1, r2);
+      e2 = fmax(r1, r2);
+    }
+  }
+  const double q1 = cp_q_from_energy(a, e1, c), q2 = cp_q_from_energy(a, e2, c);
+  if (Q * q1 > 0.0) return e1;
+  if (Q * q2 > 0.0) return e2;
+  if (fabs(e1 - e2) < (double)1e-10f || fabs(q1 - q2) < (double)1e-10f) return e1;
+  bad = true;
+  return 0.0;
+}
+
+/* the shell's cumulative profile up to qimax (uniform Q axis, 100 / (N-1)) */
+template <typename R>
+__device__ __forceinline__ double cp_shell_cdf(const R *row, double qimax) {
+  const double dq = 100.0 * 1.0 / (XMI_CP_N - 1.0) - 100.0 * 0.0 / (XMI_CP_N - 1.0);
+  if (qimax != qimax) qimax = 0.0; /* 0/0 at theta = 0 with a zero binding energy: undefined in the reference */
+  if (qimax < -100.0) return 0.0;
+  if (qimax > 100.0) return 1.0;
+  const double x = qimax < 0.0 ? -qimax : qimax;
+  int pos = (int)(x / dq);
+  if (pos > XMI_CP_N - 2) pos = XMI_CP_N - 2; /* x = 100 exactly: the last interval */
+  const double x0 = 100.0 * pos / (XMI_CP_N - 1.0), x1 = 100.0 * (pos + 1) / (XMI_CP_N - 1.0);
+  const double y0 = (double)XMI_LDG(row, pos, XMI_CP_N, 50), y1 = (double)XMI_LDG(row, pos + 1, XMI_CP_N, 50);
+  const double v = y0 + ((y1 - y0) * (x - x0) / (x1 - x0));
+  return qimax < 0.0 ? 1.0 - (0.5 + v) : 0.5 + v;
+}
+
+/* the shell's Q at cumulative value cdf (uniform CDF axis, 0.5 / (N-1)) */
+template <typename R>
+__device__ __forceinline__ double cp_shell_q(const R *row, double cdf) {
+  const double dc = 0.5 * 1.0 / (XMI_CP_N - 1.0) - 0.5 * 0.0 / (XMI_CP_N - 1.0);
+  const bool neg = cdf < 0.5;
+  const double cp = neg ? 0.5 - cdf : cdf - 0.5;
+  int pos = (int)(cp / dc);
+  /* the reference stops the program at pos = N - 1 (cdf exactly 0 or 1) */
+  if (pos > XMI_CP_N - 2) pos = XMI_CP_N - 2;
+  const double c0 = 0.5 * pos / (XMI_CP_N - 1.0), c1 = 0.5 * (pos + 1) / (XMI_CP_N - 1.0);
+  const double y0 = (double)XMI_LDG(row, pos, XMI_CP_N, 51), y1 = (double)XMI_LDG(row, pos + 1, XMI_CP_N, 51);
+  const double q = y0 + ((y1 - y0) * (cp - c0) / (c1 - c0));
+  return neg ? -q : q;
+}
+
+/* every shell's cumulative profile at (energy, c = cos theta) and their
+ * occupancy-weighted sum */
+template <typename R>
+__device__ __forceinline__ double cp_shell_cdfs(const DevBundle<R> &b, int e, double energy, double c, double *cdfs) {
+  const int ns = b.cp_nshell[e];
+  for (int k = 0; k < ns; k++)
+    cdfs[k] = cp_shell_cdf(b.cp_cdf[e] + (size_t)k * XMI_CP_N, cp_qimax(energy, b.cp_edge[e * XMI_CP_SH + k], c));
+  double sum = 0.0;
+  for (int k = 0; k < ns; k++) sum = sum + b.cp_occ[e * XMI_CP_SH + k] * cdfs[k];
+  return sum;
+}
+
+/* xmi_update_photon_energy_compton: the scattered energy, 0 when no shell can
+ * scatter (the photon is then absorbed) */
+template <typename R>
+__device__ __noinline__ double compton_energy_advanced(const DevBundle<R> &b, int e, double energy, double theta_i,
+                                                       xmi_rng *g, bool &bad) {
+  double cdfs[XMI_CP_SH];
+  const double c = cos(theta_i);
+  const double sum = cp_shell_cdfs(b, e, energy, c, cdfs);
+  if (sum == 0.0) return 0.0;
+  const int ns = b.cp_nshell[e];
+  const double r = (double)uni<R>(g);
+  double tsum = 0.0;
+  int sel = -1;
+  for (int k = 0; k < ns; k++) {
+    const double w = b.cp_occ[e * XMI_CP_SH + k] * cdfs[k] / sum;
+    if (w > 0.0) sel = k; /* rounding can leave the running sum below r: the last shell with weight */
+    tsum = tsum + w;
+    if (r <= tsum) {
+      sel = k;
+      break;
+    }
+  }
+  if (sel < 0) { /* not reached with finite tables */
+    bad = true;
+    return 0.0;
+  }
+  const double q = cp_shell_q(b.cp_qinv[e] + (size_t)sel * XMI_CP_N, (double)uni<R>(g) * cdfs[sel]);
+  return cp_energy_from_q(energy, q, c, bad);
+}
+
 /* ---------------- variance reduction: event prologue ---------------- */
 /* The point-detector estimator of one interaction
  * (src/xmi_variance_reduction.F90:29-726) is split in two.  The transport
@@ -851,7 +980,9 @@ __device__ bool rayleigh(const DevBundle<R> &b, Photon<R> &p, xmi_rng *g) {
   return true;
 }
 
-template <typename R>
+/* Adv: compiled with the advanced Compton scattering (used when the bundle
+ * asks for it); the default instantiation carries none of its code */
+template <typename R, bool Adv = false>
 __device__ bool compton(const DevBundle<R> &b, Photon<R> &p, xmi_rng *g) {
   bool ok = true;
   const int e = p.elem;
@@ -869,10 +1000,18 @@ __device__ bool compton(const DevBundle<R> &b, Photon<R> &p, xmi_rng *g) {
                      (R)((XMI_PHI_NT - 1) / 0.5), r, tt, ok);
   if (!ok) return false;
   R phi0 = polarisation_phi0(p);
-  p.E = compton_energy(b, e, p.E, theta_i, g, false, ok);
-  if (!ok) return false;
-  mu_calc(b, p.E, p.mus);
-  if (p.E == (R)0) return true;
+  if (Adv && b.use_adv_compton) {
+    bool bad = false;
+    p.E = (R)compton_energy_advanced(b, e, (double)p.E, (double)theta_i, g, bad);
+    if (bad) return false;
+    if (p.E == (R)0) return true;
+    mu_calc(b, p.E, p.mus);
+  } else {
+    p.E = compton_energy(b, e, p.E, theta_i, g, false, ok);
+    if (!ok) return false;
+    mu_calc(b, p.E, p.mus);
+    if (p.E == (R)0) return true;
+  }
   update_dirv(p, theta_i, phi_i + phi0);
   update_elecv(p);
   R cti = cos(theta_i), cpi = cos(phi_i), spi = sin(phi_i);
@@ -1227,11 +1366,11 @@ __device__ int step_photon(const DevBundle<R> &b, Photon<R> &p, const DevTally &
 }
 
 /* the interaction chosen by step_photon, drawing from g */
-template <typename R>
+template <typename R, bool Adv = false>
 __device__ __forceinline__ bool interact(const DevBundle<R> &b, Photon<R> &p, const DevTally &t, xmi_rng &g) {
   bool ok;
   if (p.last == XMI_RAYLEIGH) ok = rayleigh(b, p, &g);
-  else if (p.last == XMI_COMPTON) ok = compton(b, p, &g);
+  else if (p.last == XMI_COMPTON) ok = compton<R, Adv>(b, p, &g);
   else ok = fluorescence(b, p, &g);
   if (!ok) set_error(t, kErrTable);
   return ok;

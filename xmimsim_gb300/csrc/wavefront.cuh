@@ -124,8 +124,9 @@ __global__ void __launch_bounds__(128) wf_step(DevBundle<R> b0, DevTally t0, con
   }
 }
 
-/* the photons of interaction queue k (0 Rayleigh, 1 Compton, 2 photoelectric) */
-template <typename R, bool Batched>
+/* the photons of interaction queue k (0 Rayleigh, 1 Compton, 2 photoelectric);
+ * Adv: with the advanced Compton scattering compiled in */
+template <typename R, bool Batched, bool Adv = false>
 __global__ void __launch_bounds__(128) wf_interact(DevBundle<R> b0, DevTally t0, const DevBundle<R> *bundles,
                                                    const DevTally *tallies, WfPhoton<R> *st, WfLists q, int k,
                                                    int next, long long cap) {
@@ -139,7 +140,7 @@ __global__ void __launch_bounds__(128) wf_interact(DevBundle<R> b0, DevTally t0,
     const DevTally &t = wf_tally<Batched>(t0, tallies, x.cfg);
     xmi_rng g;
     xmi_rng_resume(&g, b.seed, (uint64_t)x.p.id, (uint32_t)x.p.n_int, x.ctr0, x.pos);
-    if (!interact(b, x.p, t, g)) continue;
+    if (!interact<R, Adv>(b, x.p, t, g)) continue;
     st[slot] = x;
     wf_append(q.active[next], &q.count[next], slot);
   }

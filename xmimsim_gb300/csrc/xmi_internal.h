@@ -41,6 +41,7 @@ struct xmi_tables_handle {
 int xmi_bundle_build(struct xmi_input_handle *in, struct xmi_tables_handle *t,
                      const xmi_main_options *options);
 void xmi_bundle_free(xmi_bundle *b);
+int xmi_bundle_compton_profiles(xmi_bundle *b);
 void xmi_bundle_set_run(struct xmi_input_handle *in, struct xmi_tables_handle *t,
                         const xmi_main_options *options, int n_mpi_hosts,
                         int replica, int n_replicas);
