@@ -65,6 +65,8 @@ enum { XMI_NO_INTERACTION = 0, XMI_RAYLEIGH = 1, XMI_COMPTON = 2,
 #define XMI_PHI_NT 200
 #define XMI_DOPPLER_N 10001
 #define XMI_NQ 4096
+#define XMI_AUGER_K 240   /* Auger transitions of a K vacancy (xraylib K_L1L1..K_M5Q3) */
+#define XMI_AUGER_L 135   /* of an L1, L2 or L3 vacancy (L*_M1M1..L*_M5Q3) */
 #define XMI_CP_N 10001    /* Compton profile grids (reference src/xmi_data.c:152) */
 #define XMI_CP_SH 32      /* room for every shell with electrons (29 in xraylib's K..Q1 order) */
 #define XMI_QMAX 20.0
@@ -199,6 +201,18 @@ typedef struct {
   double *ent_coef;      /* [n_ent] FluorYield(Z, shell) x RadRate(Z, line) */
   double *ent_pmu;       /* [n_ent][XMI_MAXL] precalc_mu of every layer at the line energy (0 beyond n_layers) */
   int stage_max;         /* max over layers of (line entries + 2 x elements): history slots one layer feeds */
+
+  /* ---- analog cascades (VR off; reference src/xmi_main.F90:2413-4783) ----
+   * Radiative: after a line from shell s, the vacancy moves to the line's
+   * upper shell u and may emit again: line_casc_shell[slot] = u for K lines
+   * to L1..M5 and L lines to M1..M5 (the latter only with M lines), else -1.
+   * Auger: a K/L1/L2/L3 vacancy decaying without a photon picks transition t
+   * with probability auger_rate[(e * 4 + s) * XMI_AUGER_K + t]; its two new
+   * vacancies are (1 + t / 30, 1 + t % 30) for K and (4 + t / 27, 4 + t % 27)
+   * for L, as positions of the list L1 L2 L3 M1..M5 N1..N7 O1..O7 P1..P5 Q1..Q3
+   * (positions 1..8 are the shells L1..M5 of the line tables). */
+  int *line_casc_shell;  /* [n_lines] */
+  double *auger_rate;    /* [n_elem][4][XMI_AUGER_K] */
 
   /* ---- per-shell Compton profiles (advanced Compton; reference
    * src/xmi_data_f.F90:1124-1230), built on demand by

@@ -9,6 +9,7 @@
  *   xmi_check_photon_detector_hit src/xmi_main.F90:1920-1984
  *   xmi_simulate_photon_rayleigh/compton/fluorescence src/xmi_main.F90:1986-2411
  *   xmi_update_photon_energy_compton2 src/xmi_main.F90:4985-5067
+ *   xmi_simulate_photon_cascade_auger/radiative src/xmi_main.F90:2413-4783
  *   xmi_update_photon_energy_compton (advanced) src/xmi_main.F90:4785-4983,
  *   xmi_compton_varred src/xmi_variance_reduction.F90:752-947,
  *   xmi_get_qimax / xmi_get_energy_from_q / xmi_get_q_from_energy
@@ -28,8 +29,9 @@
  *
  * Deliberate differences from the reference (same in the engine): Philox
  * streams instead of per-thread MT19937, Box-Muller instead of the ziggurat
- * Gaussian, tables from the bundle instead of xraylib calls.  Cascade
- * offspring of the analog (non-VR) mode are not simulated.
+ * Gaussian, tables from the bundle instead of xraylib calls.  The offspring
+ * of an analog cascade draws from streams of its own (id | 2^62) instead of
+ * continuing its parent's stream, and is walked after its parent.
  */
 #include "../include/xmimsim_bundle.h"
 #include "oracle_rng.h"
@@ -72,7 +74,11 @@ typedef struct {
   int hist_slot[XMI_MAXN + 2];   /* line slot of the emitted line */
   int64_t id;
   long sa_not_found;
+  int casc_used;          /* the photon's analog cascade has been simulated (its cascade options are off) */
 } ophoton;
+
+/* offspring photons of the analog cascades draw from the streams of this id */
+#define O_OFFSPRING_ID (1ll << 62)
 
 typedef struct {
   double *channels;  /* [(N+1)][nch] cumulative */
@@ -906,7 +912,105 @@ static int coster_kronig(const double *ck, int shell, orng *g) {
   }
 }
 
-static int fluorescence(const xmi_bundle *b, ophoton *p, orng *g) {
+/* ---- analog cascades (VR off), src/xmi_main.F90:2413-4783 ---- */
+
+/* The photon of a vacancy in shell s (1..8 = L1..M5) of element e, set up as
+ * the cascade routines set up their photons: xmi_fluorescence_yield_check
+ * with the cascade-corrected yield, xmi_coster_kronig_check,
+ * xmi_fluorescence_line_check, an isotropic direction and a random E-vector
+ * perpendicular to it (src/xmi_main.F90:4696-4760).  Returns 1 when a line
+ * above the threshold is emitted; q's other fields are left to the caller.
+ * Shells beyond M5 emit nothing: they have no lines in the tables, and the
+ * reference reads past its 9-shell yield table for them. */
+static int o_cascade_photon(const xmi_bundle *b, int e, int s, ophoton *q, orng *g) {
+  double r, sumz = 0.0, cosalfa, c_alfa, c_ae, c_be, rr;
+  int sl, slot = -1, k;
+  if (s < 1 || s > 8) return 0;
+  if (s >= 4 && !b->use_M_lines) return 0;
+  r = orng_uniform(g);
+  if (r > b->elem_yield_corr[9 * e + s]) return 0;
+  s = coster_kronig(b->elem_ck + (size_t)e * XMI_NCK, s, g);
+  r = orng_uniform(g);
+  for (sl = b->elem_shell_off[10 * e + s]; sl < b->elem_shell_off[10 * e + s + 1]; sl++) {
+    sumz = sumz + b->line_rate[sl];
+    if (r < sumz) {
+      slot = sl;
+      break;
+    }
+  }
+  if (slot < 0 || b->line_energy[slot] <= O_ENERGY_THRESHOLD) return 0;
+  q->energy = b->line_energy[slot];
+  for (k = 0; k < b->n_layers; k++) q->mus[k] = b->precalc_mu[(size_t)k * b->n_lines + slot];
+  q->theta = acos(2.0 * orng_uniform(g) - 1.0);
+  q->phi = 2.0 * M_PI * orng_uniform(g);
+  q->dirv[0] = sin(q->theta) * cos(q->phi);
+  q->dirv[1] = sin(q->theta) * sin(q->phi);
+  q->dirv[2] = cos(q->theta);
+  rr = 2.0 * M_PI * orng_uniform(g);
+  q->elecv[0] = cos(rr);
+  q->elecv[1] = sin(rr);
+  q->elecv[2] = 0.0;
+  cosalfa = dot3(q->elecv, q->dirv);
+  if (fabs(cosalfa) > 1.0) return 0; /* the reference stops the program here */
+  c_alfa = acos(cosalfa);
+  c_ae = 1.0 / sin(c_alfa);
+  c_be = -c_ae * cosalfa;
+  for (k = 0; k < 3; k++) q->elecv[k] = c_ae * q->elecv[k] + c_be * q->dirv[k];
+  q->hist_type[q->n_int] = -b->line_index[slot];
+  q->hist_elem[q->n_int] = e;
+  q->hist_slot[q->n_int] = slot;
+  q->last_interaction = XMI_PHOTOELECTRIC;
+  return 1;
+}
+
+static int o_casc_auger(const xmi_bundle *b) {
+  return b->use_vr == 0 && b->escape_mode == 0 &&
+         (b->cascade_type == XMI_CASCADE_NONRADIATIVE || b->cascade_type == XMI_CASCADE_FULL);
+}
+static int o_casc_radiative(const xmi_bundle *b) {
+  return b->use_vr == 0 && b->escape_mode == 0 &&
+         (b->cascade_type == XMI_CASCADE_RADIATIVE || b->cascade_type == XMI_CASCADE_FULL);
+}
+
+/* the offspring of photon p: its state at the interaction, its own id */
+static void o_offspring_from(const ophoton *p, ophoton *q) {
+  *q = *p;
+  q->id = p->id | O_OFFSPRING_ID;
+  q->detector_hit = 0;
+  q->inside = 0;
+  q->casc_used = 1; /* offspring simulate no cascade of their own */
+  q->sa_not_found = 0;
+}
+
+/* xmi_simulate_photon_cascade_auger, src/xmi_main.F90:2413-4594: a K/L
+ * vacancy of p's element decayed without a photon (p's energy is already 0).
+ * The transition's first vacancy turns p into its fluorescence photon, the
+ * second gives the offspring. */
+static void o_cascade_auger(const xmi_bundle *b, ophoton *p, int shell, ophoton *child, int *spawned, orng *g) {
+  const int e = p->cur_elem, nt = shell == 0 ? XMI_AUGER_K : XMI_AUGER_L, nb = shell == 0 ? 30 : 27;
+  const int f0 = shell == 0 ? 1 : 4;
+  const double *rate = b->auger_rate + ((size_t)e * 4 + shell) * XMI_AUGER_K;
+  double r = orng_uniform(g), sumz = 0.0;
+  int t = -1, k;
+  ophoton q;
+  for (k = 0; k < nt; k++) {
+    sumz = sumz + rate[k];
+    if (r < sumz) {
+      t = k;
+      break;
+    }
+  }
+  if (t < 0) return;
+  o_offspring_from(p, &q);
+  if (o_cascade_photon(b, e, f0 + t / nb, p, g)) p->casc_used = 1;
+  if (o_cascade_photon(b, e, f0 + t % nb, &q, g)) {
+    *child = q;
+    *spawned = 1;
+  }
+}
+
+/* child: where an analog cascade puts its offspring (NULL: none allowed) */
+static int fluorescence(const xmi_bundle *b, ophoton *p, orng *g, ophoton *child, int *spawned) {
   int e = p->cur_elem, shell, found = 0, sl, slot = -1, node, k;
   double f, photo_total, sumz, r;
   xmi_grid_locate(b, p->energy, &node, &f);
@@ -925,10 +1029,12 @@ static int fluorescence(const xmi_bundle *b, ophoton *p, orng *g) {
     return 1;
   }
   if (b->use_vr == 0 && b->escape_mode == 0) {
-    /* xmi_fluorescence_yield_check: Auger without cascade simulation */
+    /* xmi_fluorescence_yield_check; a non-radiative decay may start the
+     * Auger cascade */
     r = orng_uniform(g);
     if (r > b->elem_yield_corr[9 * e + shell]) {
       p->energy = 0.0;
+      if (child && !p->casc_used && o_casc_auger(b) && shell <= 3) o_cascade_auger(b, p, shell, child, spawned, g);
       return 1;
     }
   } else {
@@ -964,11 +1070,21 @@ static int fluorescence(const xmi_bundle *b, ophoton *p, orng *g) {
   p->hist_type[p->n_int] = -b->line_index[slot];
   p->hist_elem[p->n_int] = e;
   p->hist_slot[p->n_int] = slot;
+  /* xmi_simulate_photon_cascade_radiative, src/xmi_main.F90:4596-4783 */
+  if (child && !p->casc_used && o_casc_radiative(b) && b->line_casc_shell[slot] >= 0) {
+    ophoton q;
+    o_offspring_from(p, &q);
+    if (o_cascade_photon(b, e, b->line_casc_shell[slot], &q, g)) {
+      *child = q;
+      *spawned = 1;
+      p->casc_used = 1;
+    }
+  }
   return 1;
 }
 
 /* xmi_simulate_photon, src/xmi_main.F90:1188-1685 */
-static int simulate_photon(const xmi_bundle *b, ophoton *p, otally *t) {
+static int simulate_photon(const xmi_bundle *b, ophoton *p, otally *t, ophoton *child, int *spawned) {
   for (;;) {
     orng g;
     double R;
@@ -1107,7 +1223,7 @@ static int simulate_photon(const xmi_bundle *b, ophoton *p, otally *t) {
           ok = compton(b, p, &g);
         } else {
           p->last_interaction = XMI_PHOTOELECTRIC;
-          ok = fluorescence(b, p, &g);
+          ok = fluorescence(b, p, &g, child, spawned);
         }
         if (!ok) return 0;
       }
@@ -1213,6 +1329,22 @@ static int shift_first_layer(const xmi_bundle *b, ophoton *p) {
 
 /* Simulates photons [g0, g1) of the run (global ids counted over the items)
  * and accumulates the raw tallies (before live-time scaling). */
+
+/* tallies of a photon leaving the system, src/xmi_main.F90:441-525 */
+static void tally_exit(const xmi_bundle *b, otally *t, const ophoton *p) {
+  t->not_found += p->sa_not_found;
+  if (p->detector_hit) {
+    if (b->use_vr == 0) tally_channel(b, t, p->n_int, p->energy, p->weight);
+    if (p->n_int > 0) {
+      int kk = p->n_int, Z = b->elem_Z[p->hist_elem[kk]];
+      int ht = p->hist_type[kk];
+      if (ht <= -1 && ht >= -383) t->brute[hidx(b, Z, -ht, kk)] += p->weight;
+      else if (ht == XMI_RAYLEIGH) t->brute[hidx(b, Z, 384, kk)] += p->weight;
+      else if (ht == XMI_COMPTON) t->brute[hidx(b, Z, 385, kk)] += p->weight;
+    }
+  }
+}
+
 static int run_photon(const xmi_bundle *b, const xmi_source_item *it, int64_t j, otally *t) {
   ophoton p;
   orng g;
@@ -1266,17 +1398,16 @@ static int run_photon(const xmi_bundle *b, const xmi_source_item *it, int64_t j,
   for (k = 0; k < 3; k++) p.elecv[k] = c_ae * p.elecv[k] + c_be * p.dirv[k];
   if (!shift_first_layer(b, &p)) return 0;
   p.last_interaction = XMI_NO_INTERACTION;
-  if (!simulate_photon(b, &p, t)) return 0;
-  t->not_found += p.sa_not_found;
-  /* tallies of the photon leaving the system, src/xmi_main.F90:441-525 */
-  if (p.detector_hit) {
-    if (b->use_vr == 0) tally_channel(b, t, p.n_int, p.energy, p.weight);
-    if (p.n_int > 0) {
-      int kk = p.n_int, Z = b->elem_Z[p.hist_elem[kk]];
-      int ht = p.hist_type[kk];
-      if (ht <= -1 && ht >= -383) t->brute[hidx(b, Z, -ht, kk)] += p.weight;
-      else if (ht == XMI_RAYLEIGH) t->brute[hidx(b, Z, 384, kk)] += p.weight;
-      else if (ht == XMI_COMPTON) t->brute[hidx(b, Z, 385, kk)] += p.weight;
+  {
+    ophoton child;
+    int spawned = 0, none = 0;
+    if (!simulate_photon(b, &p, t, &child, &spawned)) return 0;
+    tally_exit(b, t, &p);
+    /* the offspring of an analog cascade, walked after its parent as the
+     * reference walks photon%offspring (src/xmi_main.F90:441-555) */
+    if (spawned) {
+      if (!simulate_photon(b, &child, t, NULL, &none)) return 0;
+      tally_exit(b, t, &child);
     }
   }
   return 1;
@@ -1388,7 +1519,7 @@ int oracle_escape_ratios(const xmi_bundle *b, long nE, double emin, double de, l
       orng g;
       const long iE = (long)(w / n_photons);
       double x1m, y1m, x1, y1, te, cosalfa, c_alfa, c_ae, c_be;
-      int k;
+      int k, spawned = 0;
       memset(&p, 0, sizeof(p));
       p.id = w;
       p.energy = emin + iE * de;
@@ -1417,7 +1548,7 @@ int oracle_escape_ratios(const xmi_bundle *b, long nE, double emin, double de, l
       for (k = 0; k < 3; k++) p.elecv[k] = c_ae * p.elecv[k] + c_be * p.dirv[k];
       if (!shift_first_layer(b, &p)) continue;
       p.last_interaction = XMI_NO_INTERACTION;
-      if (!simulate_photon(b, &p, &t)) continue;
+      if (!simulate_photon(b, &p, &t, NULL, &spawned)) continue;
       if (p.last_interaction != XMI_NO_INTERACTION) {
 #pragma omp atomic
         interacted[iE] += p.weight;

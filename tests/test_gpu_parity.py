@@ -450,3 +450,58 @@ def test_advanced_compton_fp32_and_batched():
         s.free_raw(b)
         s.free_raw(single)
         s.close()
+
+
+def analog_cascade_spec(n=100000):
+    spec = configs.config1(n_photons_line=n)
+    spec.layers = [Layer([82, 26, 8], [0.3, 0.4, 0.3], 6.0, 0.02)]
+    spec.reference_layer = 1
+    spec.n_interactions_trajectory = 3
+    spec.p_detector_window = (0.0, 1.0, 100.0)
+    spec.discrete[0].energy = 90.0  # above the Pb K edge
+    return spec
+
+
+@pytest.mark.parametrize("auger,radiative", [(1, 0), (0, 1), (1, 1)])
+def test_analog_cascades_fp64_match_oracle(auger, radiative):
+    """Variance reduction off with the Auger and/or radiative cascades
+    (src/xmi_main.F90:2413-4783): offspring photons in their own slots and
+    streams, FP64 GPU against the oracle on the same tables and streams."""
+    spec = analog_cascade_spec()
+    opts = dict(configs.C1_OPTIONS, use_variance_reduction=0, use_cascade_auger=auger,
+                use_cascade_radiative=radiative)
+    sim, gpu, ref = run_pair(spec, opts)
+    assert gpu["var_red"] is None
+    assert_transport_equal(gpu, ref)
+    assert gpu["brute"][82 - 1, 29:113, 0].sum() > 0  # Pb L lines
+    sim.close()
+
+
+def test_analog_cascades_fp32_and_batched():
+    """FP32 analog transport with both cascades tracks FP64 (1e-2 on the
+    brute-force totals: rounding flips a few analog decisions), and a batch of
+    an analog cascade configuration with a VR one gives each its single run."""
+    spec = analog_cascade_spec(200000)
+    opts = dict(configs.C1_OPTIONS, use_variance_reduction=0)
+    s64 = Simulation(spec, options=opts, gpu=gpu_options(precision=0, seed=SEED))
+    s32 = Simulation(spec, options=opts, gpu=gpu_options(precision=1, seed=SEED))
+    r64, r32 = s64.msim(), s32.msim()
+    assert r32["brute"].sum() == pytest.approx(r64["brute"].sum(), rel=1e-2)
+    pl = slice(29, 113)
+    assert r32["brute"][82 - 1, pl].sum() == pytest.approx(r64["brute"][82 - 1, pl].sum(), rel=2e-2)
+    np.testing.assert_allclose(r32["channels"].sum(axis=1), r64["channels"].sum(axis=1), rtol=1e-2)
+    s64.close()
+    s32.close()
+    sims = [Simulation(analog_cascade_spec(20000), options=opts, gpu=gpu_options(seed=SEED)),
+            Simulation(mixed_source_spec(), options=configs.C1_OPTIONS, gpu=gpu_options(seed=SEED))]
+    sims[1].solid_angle()
+    batched = Simulation.msim_batch(sims)
+    for s, b in zip(sims, batched):
+        single = s.msim()
+        for key in ("var_red", "brute", "channels"):
+            if single[key] is None:
+                continue
+            np.testing.assert_allclose(b[key], single[key], rtol=1e-9, atol=1e-12 * abs(single[key]).max())
+        s.free_raw(b)
+        s.free_raw(single)
+        s.close()

@@ -62,6 +62,11 @@ struct DevBundle {
   int n_ent, stage_max;
   const int *ent_off, *ent_slot, *ent_shell;
   const R *ent_coef, *ent_pmu;
+  /* analog cascades (VR off): flags, the radiative cascade's next shell per
+   * line slot, Auger transition probabilities [n_elem][4][XMI_AUGER_K] */
+  int casc_auger, casc_rad;
+  const int *line_casc;
+  const R *auger_rate;
   /* per-shell Compton profiles (advanced Compton; null unless in use) */
   int use_adv_compton;
   const int *cp_nshell;                 /* [n_elem] */

@@ -82,12 +82,14 @@ struct WfBuffers {
   void *st = nullptr;
   int *lists = nullptr; /* 5 lists of cap entries */
   unsigned *count = nullptr;
+  unsigned char *casc = nullptr; /* [cap] cascade-used flags of the analog cascades */
   size_t st_bytes = 0;
   long long cap = 0;
   void release() {
     cudaFree(st);
     cudaFree(lists);
     cudaFree(count);
+    cudaFree(casc);
     *this = WfBuffers();
   }
 };
@@ -254,6 +256,11 @@ void fill_scalars(const xmi_bundle &h, xmi::DevBundle<R> &d) {
   d.use_vr = h.use_vr;
   d.use_M_lines = h.use_M_lines;
   d.use_adv_compton = h.use_advanced_compton && d.cp_cdf ? 1 : 0;
+  {
+    const bool analog = h.use_vr == 0 && h.escape_mode == 0;
+    d.casc_auger = analog && (h.cascade_type == XMI_CASCADE_NONRADIATIVE || h.cascade_type == XMI_CASCADE_FULL);
+    d.casc_rad = analog && (h.cascade_type == XMI_CASCADE_RADIATIVE || h.cascade_type == XMI_CASCADE_FULL);
+  }
   d.line_last = h.line_last;
   d.max_shell = h.max_shell;
   d.escape_mode = h.escape_mode;
@@ -358,8 +365,10 @@ bool upload_tables(const xmi_bundle &h, DevSide &s, xmi::DevBundle<R> &d) {
   d.ent_shell = upload_int(s, h.ent_shell, h.n_ent);
   d.ent_coef = upload<R>(s, h.ent_coef, h.n_ent);
   d.ent_pmu = upload<R>(s, h.ent_pmu, (size_t)h.n_ent * XMI_MAXL);
+  d.line_casc = upload_int(s, h.line_casc_shell, NL);
+  d.auger_rate = upload<R>(s, h.auger_rate, E * 4 * XMI_AUGER_K);
   if (cudaGetLastError() != cudaSuccess || !d.rayl_icdf || !d.compt_icdf || !d.dop_icdf || !d.ff2 || !d.sf ||
-      !d.phi_icdf || !d.ent_pmu) {
+      !d.phi_icdf || !d.ent_pmu || !d.line_casc || !d.auger_rate) {
     xmi_set_error("device table upload failed");
     s.release();
     return false;
@@ -671,7 +680,8 @@ static bool ensure_wf(WfBuffers &wb, long long cap) {
   wb.release();
   if (!cuda_ok(cudaMalloc(&wb.st, bytes), "cudaMalloc photon states") ||
       !cuda_ok(cudaMalloc(&wb.lists, sizeof(int) * 5 * cap), "cudaMalloc photon lists") ||
-      !cuda_ok(cudaMalloc(&wb.count, sizeof(unsigned) * 5), "cudaMalloc"))
+      !cuda_ok(cudaMalloc(&wb.count, sizeof(unsigned) * 5), "cudaMalloc") ||
+      !cuda_ok(cudaMalloc(&wb.casc, (size_t)cap), "cudaMalloc cascade flags"))
     return false;
   wb.st_bytes = bytes;
   wb.cap = cap;
@@ -684,15 +694,19 @@ template <typename R, bool Batched>
 static int launch_wavefront(cudaStream_t st, WfBuffers &wb, const xmi::DevBundle<R> &b0, const xmi::DevTally &t0,
                             const xmi::DevBundle<R> *bundles, const xmi::DevTally *tallies, const long long *cfg_first,
                             int n_cfg, long long w0, long long w1, int max_iter, const xmi::VrQueue<R> &vq,
-                            int threads, int blocks, bool adv) {
+                            int threads, int blocks, bool adv, bool casc) {
   const long long cap = wb.cap;
   xmi::WfLists q;
   q.active[0] = wb.lists;
   q.active[1] = wb.lists + cap;
   for (int k = 0; k < 3; k++) q.inter[k] = wb.lists + (2 + k) * cap;
   q.count = wb.count;
+  /* analog cascades: photons in [0, cap / 2), offspring in [cap / 2, cap) */
+  q.casc = wb.casc;
+  q.half = casc ? cap / 2 : cap;
   xmi::WfPhoton<R> *ps = (xmi::WfPhoton<R> *)wb.st;
   cudaMemsetAsync(wb.count, 0, sizeof(unsigned) * 5, st);
+  if (casc) cudaMemsetAsync(wb.casc, 0, (size_t)q.half, st);
   xmi::wf_start<R, Batched><<<blocks, threads, 0, st>>>(b0, t0, bundles, tallies, cfg_first, n_cfg, w0, w1, ps, q);
   int launches = 1, cur = 0;
   for (int it = 0; it < max_iter; it++) {
@@ -702,6 +716,9 @@ static int launch_wavefront(cudaStream_t st, WfBuffers &wb, const xmi::DevBundle
     for (int k = 0; k < 3; k++) {
       if (k == 1 && adv)
         xmi::wf_interact<R, Batched, true><<<blocks, threads, 0, st>>>(b0, t0, bundles, tallies, ps, q, k, next, cap);
+      else if (k == 2 && casc)
+        xmi::wf_interact<R, Batched, false, true><<<blocks, threads, 0, st>>>(b0, t0, bundles, tallies, ps, q, k, next,
+                                                                             cap);
       else
         xmi::wf_interact<R, Batched><<<blocks, threads, 0, st>>>(b0, t0, bundles, tallies, ps, q, k, next, cap);
     }
@@ -1004,13 +1021,15 @@ static bool launch_single(DevState *s, xmi::DevBundle<R> &d, const xmi::DevTally
   } borrow{s->stream};
   EventQueue &q = borrow.rb->q;
   WfBuffers &wf = borrow.rb->wf;
-  if (!ensure_wf<R>(wf, h.n_photons_total < chunk_cap ? (h.n_photons_total > 0 ? h.n_photons_total : 1)
-                                                           : chunk_cap))
+  /* analog cascades: one offspring slot per photon slot */
+  const bool casc = d.casc_auger || d.casc_rad;
+  if (!ensure_wf<R>(wf, (casc ? 2 : 1) * (h.n_photons_total < chunk_cap ? (h.n_photons_total > 0 ? h.n_photons_total : 1)
+                                                                         : chunk_cap)))
     return false;
   const int rounds = wavefront_rounds(h);
   auto transport = [&](long long w0, long long w1, const xmi::VrQueue<R> &vq) {
     return launch_wavefront<R, false>(s->stream, wf, d, tl, nullptr, nullptr, nullptr, 1, w0, w1, rounds, vq,
-                                      threads, sms * blocks_per_sm, adv);
+                                      threads, sms * blocks_per_sm, adv, casc);
   };
   auto estimator = [&](const xmi::VrQueue<R> &vq, const int *order, unsigned long long *work) {
     if (adv)
@@ -1220,12 +1239,18 @@ bool launch_batch(int n, DevState **st, xmi_hdf5FPtr *t, const xmi::DevTally *tl
   int rounds = 1;
   for (int c = 0; c < n; c++) rounds = wavefront_rounds(t[c]->b) > rounds ? wavefront_rounds(t[c]->b) : rounds;
   const long long chunk_cap = vr ? qev / N : kMaxChunkPhotons;
-  if (!ensure_wf<R>(B.wf, first[n] < chunk_cap ? (first[n] > 0 ? first[n] : 1) : chunk_cap)) return false;
+  bool casc = false; /* analog cascades in any configuration: one offspring slot per photon slot */
+  for (int c = 0; c < n; c++) {
+    const xmi_bundle &hb = t[c]->b;
+    casc = casc || (hb.use_vr == 0 && hb.escape_mode == 0 && hb.cascade_type != XMI_CASCADE_NONE);
+  }
+  if (!ensure_wf<R>(B.wf, (casc ? 2 : 1) * (first[n] < chunk_cap ? (first[n] > 0 ? first[n] : 1) : chunk_cap)))
+    return false;
   xmi::DevBundle<R> unused_b{};
   xmi::DevTally unused_t{};
   auto transport = [&](long long w0, long long w1, const xmi::VrQueue<R> &vq) {
     return launch_wavefront<R, true>(B.stream, B.wf, unused_b, unused_t, db, B.tallies, B.cfg_first, n, w0, w1,
-                                     rounds, vq, threads, sms * blocks_per_sm, adv);
+                                     rounds, vq, threads, sms * blocks_per_sm, adv, casc);
   };
   auto estimator = [&](const xmi::VrQueue<R> &vq, const int *order, unsigned long long *work) {
     if (adv)

@@ -844,6 +844,7 @@ void xmi_bundle_free(xmi_bundle *b) {
   free(b->doppler_rs); free((void *)b->doppler_icdf); free((void *)b->ff2); free((void *)b->sf);
   free(b->items);
   free(b->ent_off); free(b->ent_slot); free(b->ent_shell); free(b->ent_coef); free(b->ent_pmu);
+  free(b->line_casc_shell); free(b->auger_rate);
   free(b->cp_nshell); free(b->cp_shell); free(b->cp_occ); free(b->cp_edge);
   free((void *)b->cp_cdf); free((void *)b->cp_qinv);
   memset(b, 0, sizeof(*b));
@@ -1002,6 +1003,24 @@ int xmi_bundle_build(struct xmi_input_handle *in, struct xmi_tables_handle *t,
     b->n_lines = n;
   }
   b->n_slots = b->n_lines + 2 * b->n_elem;
+
+  /* analog cascades: the shell a radiative cascade continues from
+   * (src/xmi_main.F90:4606-4686) and the Auger transition probabilities
+   * (src/xmi_main.F90:2433-2470) */
+  b->line_casc_shell = (int *)malloc(sizeof(int) * (size_t)(b->n_lines > 0 ? b->n_lines : 1));
+  for (i = 0; i < b->n_lines; i++) {
+    const int lo = b->line_shell[i], up = xrl_line_upper_shell(b->line_index[i]);
+    b->line_casc_shell[i] = -1;
+    if (lo == 0 && up >= 1 && up <= 8) b->line_casc_shell[i] = up;
+    if (lo >= 1 && lo <= 3 && up >= 4 && up <= 8) b->line_casc_shell[i] = up;
+  }
+  b->auger_rate = (double *)calloc((size_t)(b->n_elem > 0 ? b->n_elem : 1) * 4 * XMI_AUGER_K, sizeof(double));
+  for (e = 0; e < b->n_elem; e++)
+    for (s = 0; s < 4; s++) {
+      const int nt = s == 0 ? XMI_AUGER_K : XMI_AUGER_L, t0 = s == 0 ? 0 : XMI_AUGER_K + (s - 1) * XMI_AUGER_L;
+      int t;
+      for (t = 0; t < nt; t++) b->auger_rate[((size_t)e * 4 + s) * XMI_AUGER_K + t] = xrl_AugerRate(b->elem_Z[e], t0 + t);
+    }
 
   /* energy grid with absorption edges as segment breakpoints */
   e_hi = max_source_energy(inp, &nonmono);

@@ -1081,8 +1081,105 @@ __device__ __forceinline__ int coster_kronig(const R *ck, int shell, xmi_rng *g)
   return shell;
 }
 
+/* ---------------- analog cascades (VR off), src/xmi_main.F90:2413-4783 ----------------
+ * A photon simulates at most one cascade; its offspring (at most one) takes
+ * the photon's state at the interaction, draws from the streams of
+ * id | kOffspringId and simulates no cascade of its own. */
+constexpr long long kOffspringId = 1ll << 62;
+
+/* The photon of a vacancy in shell s (1..8 = L1..M5) of element e, set up as
+ * the cascade routines set up their photons (src/xmi_main.F90:4696-4760):
+ * the cascade-corrected yield, Coster-Kronig, the line, an isotropic
+ * direction and a random E-vector perpendicular to it.  True when a line
+ * above the threshold is emitted.  Shells beyond M5 emit nothing (no lines;
+ * the reference reads past its 9-shell yield table for them). */
 template <typename R>
-__device__ bool fluorescence(const DevBundle<R> &b, Photon<R> &p, xmi_rng *g) {
+__device__ __noinline__ bool cascade_photon(const DevBundle<R> &b, int e, int s, Photon<R> &q, xmi_rng *g) {
+  if (s < 1 || s > 8) return false;
+  if (s >= 4 && !b.use_M_lines) return false;
+  R r = uni<R>(g);
+  if (r > XMI_LDG(b.yield_corr, (long long)e * XMI_NSHELL + s, (long long)b.n_elem * XMI_NSHELL, 15)) return false;
+  s = coster_kronig(b.ck + (size_t)e * XMI_NCK, s, g);
+  r = uni<R>(g);
+  R sumz = (R)0;
+  int slot = -1;
+  const int s0 = XMI_LDG(b.shell_off, 10 * e + s, 10 * b.n_elem, 16);
+  const int s1 = XMI_LDG(b.shell_off, 10 * e + s + 1, 10 * b.n_elem, 16);
+  for (int sl = s0; sl < s1; sl++) {
+    sumz = sumz + XMI_LDG(b.line_rate, sl, b.n_lines, 17);
+    if (r < sumz) { slot = sl; break; }
+  }
+  if (slot < 0) return false;
+  const R E = XMI_LDG(b.line_energy, slot, b.n_lines, 17);
+  if (E <= (R)kEnergyThreshold) return false;
+  q.E = E;
+#pragma unroll
+  for (int j = 0; j < XMI_MAXL; j++)
+    q.mus[j] = j < b.n_layers ? XMI_LDG(b.precalc_mu, (long long)j * b.n_lines + slot,
+                                        (long long)b.n_layers * b.n_lines, 18) : (R)0;
+  q.theta = acos((R)2 * uni<R>(g) - (R)1);
+  q.phi = (R)(2.0 * kPi) * uni<R>(g);
+  q.d[0] = sin(q.theta) * cos(q.phi);
+  q.d[1] = sin(q.theta) * sin(q.phi);
+  q.d[2] = cos(q.theta);
+  const R rr = (R)(2.0 * kPi) * uni<R>(g);
+  q.el[0] = cos(rr);
+  q.el[1] = sin(rr);
+  q.el[2] = (R)0;
+  const R cosalfa = q.el[0] * q.d[0] + q.el[1] * q.d[1] + q.el[2] * q.d[2];
+  if (fabs(cosalfa) > (R)1) return false; /* the reference stops the program here */
+  const R c_ae = (R)1 / sin(acos(cosalfa)), c_be = -c_ae * cosalfa;
+#pragma unroll
+  for (int k = 0; k < 3; k++) q.el[k] = c_ae * q.el[k] + c_be * q.d[k];
+  q.h_type = -XMI_LDG(b.line_index, slot, b.n_lines, 17);
+  q.h_elem = e;
+  q.h_slot = slot;
+  q.last = XMI_PHOTOELECTRIC;
+  return true;
+}
+
+/* the offspring of photon p: its state at the interaction, its own streams */
+template <typename R>
+__device__ __forceinline__ void offspring_from(const Photon<R> &p, Photon<R> &q) {
+  q = p;
+  q.id = p.id | kOffspringId;
+  q.hit = 0;
+  q.inside = 0;
+}
+
+/* cascade flags of the photo-absorption kernel: in kCascAllowed (this photon
+ * may still cascade), out kCascUsed (its cascade happened) and kCascChild
+ * (an offspring was made) */
+enum : int { kCascAllowed = 1, kCascUsed = 2, kCascChild = 4 };
+
+/* xmi_simulate_photon_cascade_auger (src/xmi_main.F90:2413-4594): a K/L
+ * vacancy decayed without a photon (p's energy is already 0); the
+ * transition's first vacancy turns p into its fluorescence photon, the second
+ * gives the offspring */
+template <typename R>
+__device__ __noinline__ void cascade_auger(const DevBundle<R> &b, Photon<R> &p, int shell, Photon<R> &child,
+                                           int &flags, xmi_rng *g) {
+  const int e = p.elem, nt = shell == 0 ? XMI_AUGER_K : XMI_AUGER_L, nb = shell == 0 ? 30 : 27;
+  const int f0 = shell == 0 ? 1 : 4;
+  const long long base = ((long long)e * 4 + shell) * XMI_AUGER_K, lim = (long long)b.n_elem * 4 * XMI_AUGER_K;
+  const R r = uni<R>(g);
+  R sumz = (R)0;
+  int t = -1;
+  for (int k = 0; k < nt; k++) {
+    sumz = sumz + XMI_LDG(b.auger_rate, base + k, lim, 52);
+    if (r < sumz) { t = k; break; }
+  }
+  if (t < 0) return;
+  offspring_from(p, child);
+  if (cascade_photon(b, e, f0 + t / nb, p, g)) flags |= kCascUsed;
+  if (cascade_photon(b, e, f0 + t % nb, child, g)) flags |= kCascChild;
+}
+
+/* Casc: compiled with the analog cascades; child receives the offspring and
+ * flags carries kCasc* */
+template <typename R, bool Casc = false>
+__device__ bool fluorescence(const DevBundle<R> &b, Photon<R> &p, xmi_rng *g, Photon<R> *child = nullptr,
+                             int *flags = nullptr) {
   const int e = p.elem;
   int node;
   R f;
@@ -1103,6 +1200,9 @@ __device__ bool fluorescence(const DevBundle<R> &b, Photon<R> &p, xmi_rng *g) {
     r = uni<R>(g);
     if (r > yc) {
       p.E = (R)0;
+      if constexpr (Casc) {
+        if ((*flags & kCascAllowed) && b.casc_auger && shell <= 3) cascade_auger(b, p, shell, *child, *flags, g);
+      }
       return true;
     }
   } else {
@@ -1136,6 +1236,14 @@ __device__ bool fluorescence(const DevBundle<R> &b, Photon<R> &p, xmi_rng *g) {
   p.h_type = -XMI_LDG(b.line_index, slot, b.n_lines, 17);
   p.h_elem = e;
   p.h_slot = slot;
+  if constexpr (Casc) {
+    /* xmi_simulate_photon_cascade_radiative, src/xmi_main.F90:4596-4783 */
+    const int u = XMI_LDG(b.line_casc, slot, b.n_lines, 53);
+    if ((*flags & kCascAllowed) && b.casc_rad && u >= 0) {
+      offspring_from(p, *child);
+      if (cascade_photon(b, e, u, *child, g)) *flags |= kCascUsed | kCascChild;
+    }
+  }
   return true;
 }
 

@@ -37,6 +37,11 @@ struct WfLists {
   int *active[2];
   int *inter[3];   /* Rayleigh, Compton, photoelectric */
   unsigned *count; /* [0], [1] active lists, [2..4] interaction queues */
+  /* analog cascades: the photons of the chunk sit in slots [0, half), the
+   * offspring of slot i in slot half + i; casc[i] != 0 once photon i's
+   * cascade has happened */
+  unsigned char *casc;
+  long long half;
 };
 
 /* appends `value` to `list`; lanes appending to the same list share one atomic */
@@ -125,8 +130,10 @@ __global__ void __launch_bounds__(128) wf_step(DevBundle<R> b0, DevTally t0, con
 }
 
 /* the photons of interaction queue k (0 Rayleigh, 1 Compton, 2 photoelectric);
- * Adv: with the advanced Compton scattering compiled in */
-template <typename R, bool Batched, bool Adv = false>
+ * Adv: with the advanced Compton scattering compiled in; Casc (queue 2 only):
+ * with the analog cascades, which start offspring photons in slots
+ * [half, 2 half) */
+template <typename R, bool Batched, bool Adv = false, bool Casc = false>
 __global__ void __launch_bounds__(128) wf_interact(DevBundle<R> b0, DevTally t0, const DevBundle<R> *bundles,
                                                    const DevTally *tallies, WfPhoton<R> *st, WfLists q, int k,
                                                    int next, long long cap) {
@@ -140,7 +147,24 @@ __global__ void __launch_bounds__(128) wf_interact(DevBundle<R> b0, DevTally t0,
     const DevTally &t = wf_tally<Batched>(t0, tallies, x.cfg);
     xmi_rng g;
     xmi_rng_resume(&g, b.seed, (uint64_t)x.p.id, (uint32_t)x.p.n_int, x.ctr0, x.pos);
-    if (!interact<R, Adv>(b, x.p, t, g)) continue;
+    if constexpr (Casc) {
+      WfPhoton<R> y;
+      int flags = slot < q.half && slot + q.half < cap && q.casc[slot] == 0 ? kCascAllowed : 0;
+      if (!fluorescence<R, true>(b, x.p, &g, &y.p, &flags)) {
+        set_error(t, kErrTable);
+        continue;
+      }
+      if (flags & kCascUsed) q.casc[slot] = 1;
+      if (flags & kCascChild) {
+        y.ctr0 = 0u;
+        y.pos = 2;
+        y.cfg = x.cfg;
+        st[slot + q.half] = y;
+        wf_append(q.active[next], &q.count[next], (int)(slot + q.half));
+      }
+    } else {
+      if (!interact<R, Adv>(b, x.p, t, g)) continue;
+    }
     st[slot] = x;
     wf_append(q.active[next], &q.count[next], slot);
   }

@@ -349,6 +349,43 @@ double xrl_AugerVacancies(int Z, int s, int t) {
   return 0.0;
 }
 
+/* Probability of Auger transition `trans` in xraylib's numbering (0..239 a
+ * K vacancy, 240..374 L1, 375..509 L2, 510..644 L3) given a non-radiative
+ * decay.  The transition of a K vacancy fills vacancies (a, b) with a in
+ * L1..M5 and b in L1..Q3 (list positions 1..30: L1..L3, M1..M5, N1..N7,
+ * O1..O7, P1..P5, Q1..Q3); of an L vacancy a in M1..M5, b in M1..Q3.  The
+ * stand-in rate is p_a q_b: p follows the expected vacancies of
+ * xrl_AugerVacancies over the first shell's range (normalised), q puts half of
+ * them on the same shells and the rest on the occupied outer shells by
+ * occupancy, so that the mean vacancies per decay stay close to
+ * xrl_AugerVacancies. */
+double xrl_AugerRate(int Z, int trans) {
+  int s0, t, nb, first0, a, b, k;
+  double p[31], q[31], sp = 0.0, sq = 0.0, outer = 0.0, vsum = 0.0;
+  if (!zok(Z) || trans < 0 || trans > 644) return 0.0;
+  if (trans < 240) { s0 = 0; t = trans; nb = 30; first0 = 1; }
+  else { s0 = 1 + (trans - 240) / 135; t = (trans - 240) % 135; nb = 27; first0 = 4; }
+  if (!shell_occupied(Z, s0)) return 0.0;
+  a = first0 + t / nb;
+  b = first0 + t % nb;
+  for (k = 0; k <= 30; k++) p[k] = q[k] = 0.0;
+  for (k = first0; k <= 8; k++) {
+    const double v = xrl_AugerVacancies(Z, s0, k);
+    p[k] = v;
+    q[k] = 0.5 * v;
+    sp += v;
+    vsum += 0.5 * v;
+  }
+  for (k = 9; k <= 30; k++) {
+    q[k] = k < XRL_NSHELL_ALL ? xrl_ElectronConfig(Z, k) : 0.0;
+    outer += q[k];
+  }
+  for (k = 9; k <= 30; k++) q[k] = outer > 0.0 ? q[k] / outer * (vsum < 1.0 ? 1.0 - vsum : 0.0) : 0.0;
+  for (k = first0; k <= 30; k++) sq += q[k];
+  if (sp <= 0.0 || sq <= 0.0) return 0.0;
+  return (p[a] / sp) * (q[b] / sq);
+}
+
 /* ---------------------------------------------------------------------- */
 /* photo-absorption: jump-ratio partition of a power-law envelope           */
 /* ---------------------------------------------------------------------- */

@@ -44,6 +44,9 @@ double xrl_CosKronTransProb(int Z, int trans); /* trans 0..13, XMI_FL12.. */
 double xrl_AugerYield(int Z, int shell);
 /* expected vacancies created in shell t per non-radiative decay of shell s */
 double xrl_AugerVacancies(int Z, int s, int t);
+/* probability of Auger transition trans (xraylib numbering K_L1L1 = 0 ..
+ * L3_M5Q3 = 644) given a non-radiative decay of its initial shell */
+double xrl_AugerRate(int Z, int trans);
 
 /* builds the per-Z scattering cross-section cache; call once per Z from a
  * single thread before using the CS functions from several threads */
