@@ -293,10 +293,17 @@ __device__ __forceinline__ void estimate_event_uniform(const DevBundle<R> &b, co
     for (int s = 0; s < XMI_NSHELL; s++)
       s_a[lane * XMI_NSHELL + s] = (s >= 4 && !b.use_M_lines) ? (R)0 : P[s] * scale;
     __syncwarp();
-    /* lines of element i: lane = entry */
+    /* lines of element i: with nl entries, np2 = the smallest power of two
+     * >= nl (at most 32) lanes take one entry each and the 32 / np2 groups of
+     * lanes split the warp's events (np2 each), their partial sums combined by
+     * shuffles -- an element with few lines still keeps the warp busy */
     const int k0 = XMI_LDG(b.ent_off, pair, b.n_layer_el + 1, 15), k1 = XMI_LDG(b.ent_off, pair + 1, b.n_layer_el + 1, 15);
-    for (int kb = k0; kb < k1; kb += 32) {
-      const int k = kb + lane;
+    int np2 = 1;
+    while (np2 < k1 - k0 && np2 < 32) np2 <<= 1;
+    const int li = lane & (np2 - 1), q0 = lane - li; /* q0 = group x np2: the group's first event */
+    for (int kb = k0; kb < k1; kb += np2) {
+      const int k = kb + li;
+      R acc = (R)0;
       if (k < k1) {
         const int sh = XMI_LDG(b.ent_shell, k, b.n_ent, 16);
         R pmu[XMI_MAXL];
@@ -313,16 +320,16 @@ __device__ __forceinline__ void estimate_event_uniform(const DevBundle<R> &b, co
           for (int j = 0; j < XMI_MAXL; j++)
             pmu[j] = XMI_LDG(b.ent_pmu, (long long)k * XMI_MAXL + j, (long long)b.n_ent * XMI_MAXL, 17);
         }
-        R acc = (R)0;
 #pragma unroll 4
-        for (int q = 0; q < 32; q++) {
+        for (int q = q0; q < q0 + np2; q++) {
           R murhod = (R)0;
 #pragma unroll
           for (int j = 0; j < XMI_MAXL; j++) murhod += pmu[j] * s_rd[q * XMI_MAXL + j];
           acc += s_a[q * XMI_NSHELL + sh] * exp(-murhod);
         }
-        st.v[k - st.k_first] += acc * XMI_LDG(b.ent_coef, k, b.n_ent, 16);
       }
+      for (int off = np2; off < 32; off <<= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
+      if (q0 == 0 && k < k1) st.v[k - st.k_first] += acc * XMI_LDG(b.ent_coef, k, b.n_ent, 16);
     }
     __syncwarp();
   }
