@@ -91,3 +91,33 @@ def test_closed_loop_recovers_known_compositions():
         assert r.sum_k <= quant.CONV_THRESHOLD
         np.testing.assert_allclose(r.weights, t, rtol=1e-2)
         assert sum(r.layer.weight) == pytest.approx(1.0)
+
+
+def test_weight_update_rule_on_synthetic_histories():
+    """One pass of the update of bin/xmimsim-pymca.c:652-770 on a made-up
+    history: the K element grows by measured / simulated when that is below
+    its jump limit, the L element is capped at its limit, and sum_k / sum_l
+    are the squared relative misfits of the simulated intensities."""
+    spec, matrix = _sample_spec([0.05, 0.03, 0.02], n=10)
+    s = quant.QuantSample(spec=spec, ilay=1, matrix=Layer([8, 14], [0.5, 0.5], 2.5, 0.1), z_quant=[26, 82],
+                          k_exp=[2.0, 0.0], l_exp=[0.0, 5.0], weights=[0.05, 0.005])
+    st = quant._State(s)
+    N = spec.n_interactions_trajectory
+    vr = np.zeros((100, 385, N))
+    lib = quant._xrl()
+    kl2, kl3 = lib.xrl_line_from_name(b"KL2"), lib.xrl_line_from_name(b"KL3")
+    l3m4, l3m5 = lib.xrl_line_from_name(b"L3M4"), lib.xrl_line_from_name(b"L3M5")
+    vr[25, kl2 - 1, 0] = 0.5
+    vr[25, kl3 - 1, 1] = 1.0
+    vr[81, l3m4 - 1, 0] = 0.1
+    vr[81, l3m5 - 1, 0] = 0.2
+    st.update({"var_red": vr})
+    k_sim = 0.5 * quant.detector_absorption(spec, 26, "KL2") + 1.0 * quant.detector_absorption(spec, 26, "KL3")
+    l_sim = 0.1 * quant.detector_absorption(spec, 82, "L3M4") + 0.2 * quant.detector_absorption(spec, 82, "L3M5")
+    assert st.k_sim[0] == pytest.approx(k_sim) and st.l_sim[1] == pytest.approx(l_sim)
+    assert st.sum_k == pytest.approx(((2.0 - k_sim) / 2.0) ** 2)
+    assert st.sum_l == pytest.approx(((5.0 - l_sim) / 5.0) ** 2)
+    # Fe: 0.05 <= 0.1 -> limit 2.5; Pb: 0.005 <= 0.01 -> limit 10
+    assert st.weights[0] == pytest.approx(0.05 * min(2.0 / k_sim, 2.5))
+    assert st.weights[1] == pytest.approx(0.005 * min(5.0 / l_sim, 10.0))
+    assert sum(st.layer.weight) == pytest.approx(1.0)
