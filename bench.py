@@ -64,6 +64,8 @@ def parse():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--workload", default="batched", choices=["batched", "plain"])
+    p.add_argument("--plain-mode", default="default", choices=["default", "advanced-compton", "analog"],
+                   help="transport options of the plain workload")
     p.add_argument("--configs", type=int, default=512, help="configurations of the batched workload")
     p.add_argument("--budget-scale", type=float, default=1.0 / 16, help="share of each budget per step")
     p.add_argument("--n-train", type=int, default=1 << 21, help="integrator samples the surrogate trains on")
@@ -153,10 +155,22 @@ def peaks():
 # --------------------------------------------------------------------------
 # workloads
 # --------------------------------------------------------------------------
-def plain_workload(photons: float):
+PLAIN_MODES = {
+    "default": "VR on, Doppler Compton",
+    "advanced-compton": "VR on, per-shell impulse-approximation Compton (use_advanced_compton = 1)",
+    "analog": "VR off, analog Auger and radiative cascades",
+}
+
+
+def plain_workload(photons: float, mode: str = "default"):
     from xmimsim_gb300 import configs
     spec = configs.config2(total_photons=int(photons))
-    return spec, dict(configs.C2_OPTIONS, use_sum_peaks=0)
+    options = dict(configs.C2_OPTIONS, use_sum_peaks=0)
+    if mode == "advanced-compton":
+        options["use_advanced_compton"] = 1
+    elif mode == "analog":
+        options.update(use_variance_reduction=0, use_cascade_auger=1, use_cascade_radiative=1)
+    return spec, options
 
 
 def batched_specs(n: int, scale: float, rank: int = 0):
@@ -208,7 +222,7 @@ def run_cpu_sample(specs, options, n_sample: int, threads: int):
 
 def cpu_sample_specs(args, rank=0):
     if args.workload == "plain":
-        spec, options = plain_workload(args.photons)
+        spec, options = plain_workload(args.photons, args.plain_mode)
         return [spec], options, "the %.0e-photon plain workload" % args.photons
     specs, options = batched_specs(args.configs, args.budget_scale, rank)
     pick = [specs[i] for i in range(0, len(specs), max(1, len(specs) // 8))][:8]
@@ -244,7 +258,8 @@ def reference_arm(args):
 
 def workload_config(args, extra):
     if args.workload == "plain":
-        cfg = {"workload": "plain 5-layer Rh 40 kV, 400 intervals + Rh K/L lines, 6 interactions, VR on",
+        cfg = {"workload": "plain 5-layer Rh 40 kV, 400 intervals + Rh K/L lines, 6 interactions, "
+                           + PLAIN_MODES[args.plain_mode],
                "photons_per_step": int(args.photons)}
     else:
         cfg = {"workload": "%d-configuration quantification sweep: 1-8 layers of 2-20 elements, 1-5 lines or "
@@ -508,7 +523,7 @@ def one_by_one(args, sims, specs, options, deep, seed, prec, tune, n_hist, full_
 
 def plain_arm(args, ws, rank, local):
     from xmimsim_gb300 import Simulation, gpu_options
-    spec, options = plain_workload(args.photons)
+    spec, options = plain_workload(args.photons, args.plain_mode)
     precision = 0 if args.precision == "fp64" else 1
     t0 = time.perf_counter()
     sim = Simulation(spec, options=options, gpu=gpu_options(precision=precision, seed=0x5EED0001 + rank))

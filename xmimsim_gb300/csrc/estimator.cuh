@@ -47,23 +47,24 @@ __device__ __forceinline__ void chan_add(const DevBundle<R> &b, const DevTally &
 template <typename R>
 __device__ __noinline__ R compton_advanced_est(const DevBundle<R> &b, const DevTally &t, int e, const VrEvent<R> &ev,
                                                R base, xmi_rng *g, bool valid, bool &ok) {
-  double cdfs[XMI_CP_SH];
-  const double E = (double)ev.E, c = cos((double)ev.theta);
-  const double sum = cp_shell_cdfs(b, e, E, c, cdfs);
+  using T = cp_real<R>;
+  T cdfs[XMI_CP_SH];
+  const T E = (T)ev.E, th = (T)ev.theta, c = cos(th), sn = sin(th);
+  const T sum = cp_shell_cdfs<T>(b, e, E, c, cdfs);
   R total = (R)0;
-  if (sum == 0.0) return total;
+  if (sum == (T)0) return total;
   const int ns = b.cp_nshell[e];
   for (int k = 0; k < ns; k++) {
-    const double sw = b.cp_occ[e * XMI_CP_SH + k] * cdfs[k] / sum;
-    if (sw == 0.0) continue;
-    const double q = cp_shell_q(b.cp_qinv[e] + (size_t)k * XMI_CP_N, (double)uni<R>(g) * cdfs[k]);
+    const T sw = (T)b.cp_occ[e * XMI_CP_SH + k] * cdfs[k] / sum;
+    if (sw == (T)0) continue;
+    const T q = cp_shell_q<T>(b.cp_qinv[e] + (size_t)k * XMI_CP_N, (T)uni<R>(g) * cdfs[k]);
     bool bad = false;
-    const double ec = cp_energy_from_q(E, q, c, bad);
+    const T ec = cp_energy_from_q(E, q, c, sn, bad);
     if (bad) {
       if (valid) ok = false;
       continue;
     }
-    if (ec == 0.0) continue;
+    if (ec == (T)0) continue;
     R mus_c[XMI_MAXL];
     mu_calc(b, (R)ec, mus_c);
     R murhod = (R)0;

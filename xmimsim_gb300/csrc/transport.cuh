@@ -24,6 +24,8 @@
 
 #include "dev_bundle.cuh"
 
+#include <type_traits>
+
 namespace xmi {
 
 enum : unsigned long long { kErrNone = 0, kErrGeometry = 1, kErrTable = 2, kErrCompton = 3,
@@ -654,19 +656,28 @@ __device__ __forceinline__ R compton_energy_est(const DevBundle<R> &b, int e, co
 
 /* ---------------- advanced Compton: per-shell impulse approximation ----------------
  * src/xmi_main.F90:4785-4983 (transport), src/xmi_variance_reduction.F90:752-947
- * (estimator), src/xmi_aux_f.F90:1951-2074 (momentum kinematics).  The
- * kinematics run in FP64 in both precisions: the quadratic for the scattered
- * energy cancels badly at small Q.  Tables are read in the working precision.
+ * (estimator), src/xmi_aux_f.F90:1951-2074 (momentum kinematics).  The FP64
+ * engine follows the reference's arithmetic (the oracle's parity).  The FP32
+ * engine runs the kinematics in FP32 with the same quadratic solved in a form
+ * without cancellation: its discriminant is 4 a^2 Q^2 (K^2 ((d - c)^2 +
+ * sin^2 theta) - Q^2 sin^2 theta), the larger root comes directly and the
+ * smaller from the product of the roots, and since Q(E) grows with E the root
+ * with the sign of Q is the larger one for Q > 0.  FP64 divides and square
+ * roots are slow on this GPU; the FP32 form keeps them off the per-shell loop.
  * MEC2 here is xraylib's constant; 1E-8, 1E-4 and 1E-10 are the reference's
  * default-real literals. */
 constexpr double kXrlMec2 = 510.998928;
 
+template <typename R>
+using cp_real = typename std::conditional<sizeof(R) == 4, float, double>::type;
+
 /* xmi_get_qimax (c = cos theta) */
-__device__ __forceinline__ double cp_qimax(double energy, double Ii, double c) {
-  if (Ii != 0.0 && energy < Ii) return 0.0;
-  const double emi = energy - Ii;
-  const double q = 137.0 * (emi * energy * (1.0 - c) / kXrlMec2 - Ii);
-  return q / sqrt(emi * emi + energy * energy - 2.0 * emi * energy * c);
+template <typename T>
+__device__ __forceinline__ T cp_qimax(T energy, T Ii, T c) {
+  if (Ii != (T)0 && energy < Ii) return (T)0;
+  const T emi = energy - Ii;
+  const T q = (T)137 * (emi * energy * ((T)1 - c) / (T)kXrlMec2 - Ii);
+  return q / sqrt(emi * emi + energy * energy - (T)2 * emi * energy * c);
 }
 
 /* xmi_get_q_from_energy */
@@ -677,7 +688,8 @@ __device__ __forceinline__ double cp_q_from_energy(double old_e, double new_e, d
 
 /* xmi_get_energy_from_q with xmi_poly_solve_quadratic; bad = true where the
  * reference stops the program (neither root has the sign of Q) */
-static __device__ __noinline__ double cp_energy_from_q(double a, double Q, double c, bool &bad) {
+static __device__ __noinline__ double cp_energy_from_q(double a, double Q, double c, double /*sin theta*/,
+                                                       bool &bad) {
   const double b = kXrlMec2, k2 = 137.0 * 137.0;
   if (fabs(c - 1.0) < (double)1e-8f) return 0.0;
   if (fabs(Q) < (double)1e-4f) return a / (1.0 + a * (1.0 - c) / b);
@@ -708,65 +720,81 @@ static __device__ __noinline__ double cp_energy_from_q(double a, double Q, doubl
   return 0.0;
 }
 
+/* the same energy in FP32, the quadratic solved without cancellation (see above) */
+__device__ __forceinline__ float cp_energy_from_q(float a, float Q, float c, float s, bool & /*bad*/) {
+  const float b = (float)kXrlMec2, k2 = 137.0f * 137.0f;
+  if (fabsf(c - 1.0f) < 1e-8f) return 0.0f;
+  if (fabsf(Q) < 1e-4f) return a / (1.0f + a * (1.0f - c) / b);
+  const float d = 1.0f + a * (1.0f - c) / b;
+  const float A = k2 * d * d - Q * Q;                  /* > 0: d >= 1, |Q| <= 100 */
+  const float dc = d - c, s2 = s * s;
+  const float root = fabsf(Q) * sqrtf(fmaxf(k2 * (dc * dc + s2) - Q * Q * s2, 0.0f));
+  const float B = k2 * d - c * Q * Q;                  /* > 0 for |Q| <= 100 */
+  const float e_big = a * (B + root) / A;
+  return Q > 0.0f ? e_big : a * a * (k2 - Q * Q) / (A * e_big);
+}
+
 /* the shell's cumulative profile up to qimax (uniform Q axis, 100 / (N-1)) */
-template <typename R>
-__device__ __forceinline__ double cp_shell_cdf(const R *row, double qimax) {
-  const double dq = 100.0 * 1.0 / (XMI_CP_N - 1.0) - 100.0 * 0.0 / (XMI_CP_N - 1.0);
-  if (qimax != qimax) qimax = 0.0; /* 0/0 at theta = 0 with a zero binding energy: undefined in the reference */
-  if (qimax < -100.0) return 0.0;
-  if (qimax > 100.0) return 1.0;
-  const double x = qimax < 0.0 ? -qimax : qimax;
+template <typename T, typename R>
+__device__ __forceinline__ T cp_shell_cdf(const R *row, T qimax) {
+  const T dq = (T)(100.0 * 1.0 / (XMI_CP_N - 1.0) - 100.0 * 0.0 / (XMI_CP_N - 1.0));
+  if (qimax != qimax) qimax = (T)0; /* 0/0 at theta = 0 with a zero binding energy: undefined in the reference */
+  if (qimax < (T)-100) return (T)0;
+  if (qimax > (T)100) return (T)1;
+  const T x = qimax < (T)0 ? -qimax : qimax;
   int pos = (int)(x / dq);
   if (pos > XMI_CP_N - 2) pos = XMI_CP_N - 2; /* x = 100 exactly: the last interval */
-  const double x0 = 100.0 * pos / (XMI_CP_N - 1.0), x1 = 100.0 * (pos + 1) / (XMI_CP_N - 1.0);
-  const double y0 = (double)XMI_LDG(row, pos, XMI_CP_N, 50), y1 = (double)XMI_LDG(row, pos + 1, XMI_CP_N, 50);
-  const double v = y0 + ((y1 - y0) * (x - x0) / (x1 - x0));
-  return qimax < 0.0 ? 1.0 - (0.5 + v) : 0.5 + v;
+  const T x0 = (T)100 * (T)pos / (T)(XMI_CP_N - 1.0), x1 = (T)100 * (T)(pos + 1) / (T)(XMI_CP_N - 1.0);
+  const T y0 = (T)XMI_LDG(row, pos, XMI_CP_N, 50), y1 = (T)XMI_LDG(row, pos + 1, XMI_CP_N, 50);
+  const T v = y0 + ((y1 - y0) * (x - x0) / (x1 - x0));
+  return qimax < (T)0 ? (T)1 - ((T)0.5 + v) : (T)0.5 + v;
 }
 
 /* the shell's Q at cumulative value cdf (uniform CDF axis, 0.5 / (N-1)) */
-template <typename R>
-__device__ __forceinline__ double cp_shell_q(const R *row, double cdf) {
-  const double dc = 0.5 * 1.0 / (XMI_CP_N - 1.0) - 0.5 * 0.0 / (XMI_CP_N - 1.0);
-  const bool neg = cdf < 0.5;
-  const double cp = neg ? 0.5 - cdf : cdf - 0.5;
+template <typename T, typename R>
+__device__ __forceinline__ T cp_shell_q(const R *row, T cdf) {
+  const T dc = (T)(0.5 * 1.0 / (XMI_CP_N - 1.0) - 0.5 * 0.0 / (XMI_CP_N - 1.0));
+  const bool neg = cdf < (T)0.5;
+  const T cp = neg ? (T)0.5 - cdf : cdf - (T)0.5;
   int pos = (int)(cp / dc);
   /* the reference stops the program at pos = N - 1 (cdf exactly 0 or 1) */
   if (pos > XMI_CP_N - 2) pos = XMI_CP_N - 2;
-  const double c0 = 0.5 * pos / (XMI_CP_N - 1.0), c1 = 0.5 * (pos + 1) / (XMI_CP_N - 1.0);
-  const double y0 = (double)XMI_LDG(row, pos, XMI_CP_N, 51), y1 = (double)XMI_LDG(row, pos + 1, XMI_CP_N, 51);
-  const double q = y0 + ((y1 - y0) * (cp - c0) / (c1 - c0));
+  const T c0 = (T)0.5 * (T)pos / (T)(XMI_CP_N - 1.0), c1 = (T)0.5 * (T)(pos + 1) / (T)(XMI_CP_N - 1.0);
+  const T y0 = (T)XMI_LDG(row, pos, XMI_CP_N, 51), y1 = (T)XMI_LDG(row, pos + 1, XMI_CP_N, 51);
+  const T q = y0 + ((y1 - y0) * (cp - c0) / (c1 - c0));
   return neg ? -q : q;
 }
 
 /* every shell's cumulative profile at (energy, c = cos theta) and their
  * occupancy-weighted sum */
-template <typename R>
-__device__ __forceinline__ double cp_shell_cdfs(const DevBundle<R> &b, int e, double energy, double c, double *cdfs) {
+template <typename T, typename R>
+__device__ __forceinline__ T cp_shell_cdfs(const DevBundle<R> &b, int e, T energy, T c, T *cdfs) {
   const int ns = b.cp_nshell[e];
   for (int k = 0; k < ns; k++)
-    cdfs[k] = cp_shell_cdf(b.cp_cdf[e] + (size_t)k * XMI_CP_N, cp_qimax(energy, b.cp_edge[e * XMI_CP_SH + k], c));
-  double sum = 0.0;
-  for (int k = 0; k < ns; k++) sum = sum + b.cp_occ[e * XMI_CP_SH + k] * cdfs[k];
+    cdfs[k] = cp_shell_cdf<T>(b.cp_cdf[e] + (size_t)k * XMI_CP_N,
+                              cp_qimax<T>(energy, (T)b.cp_edge[e * XMI_CP_SH + k], c));
+  T sum = (T)0;
+  for (int k = 0; k < ns; k++) sum = sum + (T)b.cp_occ[e * XMI_CP_SH + k] * cdfs[k];
   return sum;
 }
 
 /* xmi_update_photon_energy_compton: the scattered energy, 0 when no shell can
  * scatter (the photon is then absorbed) */
 template <typename R>
-__device__ __noinline__ double compton_energy_advanced(const DevBundle<R> &b, int e, double energy, double theta_i,
+__device__ __noinline__ double compton_energy_advanced(const DevBundle<R> &b, int e, double energy_in, double theta_i,
                                                        xmi_rng *g, bool &bad) {
-  double cdfs[XMI_CP_SH];
-  const double c = cos(theta_i);
-  const double sum = cp_shell_cdfs(b, e, energy, c, cdfs);
-  if (sum == 0.0) return 0.0;
+  using T = cp_real<R>;
+  T cdfs[XMI_CP_SH];
+  const T energy = (T)energy_in, th = (T)theta_i, c = cos(th), sn = sin(th);
+  const T sum = cp_shell_cdfs<T>(b, e, energy, c, cdfs);
+  if (sum == (T)0) return 0.0;
   const int ns = b.cp_nshell[e];
-  const double r = (double)uni<R>(g);
-  double tsum = 0.0;
+  const T r = (T)uni<R>(g);
+  T tsum = (T)0;
   int sel = -1;
   for (int k = 0; k < ns; k++) {
-    const double w = b.cp_occ[e * XMI_CP_SH + k] * cdfs[k] / sum;
-    if (w > 0.0) sel = k; /* rounding can leave the running sum below r: the last shell with weight */
+    const T w = (T)b.cp_occ[e * XMI_CP_SH + k] * cdfs[k] / sum;
+    if (w > (T)0) sel = k; /* rounding can leave the running sum below r: the last shell with weight */
     tsum = tsum + w;
     if (r <= tsum) {
       sel = k;
@@ -777,8 +805,8 @@ __device__ __noinline__ double compton_energy_advanced(const DevBundle<R> &b, in
     bad = true;
     return 0.0;
   }
-  const double q = cp_shell_q(b.cp_qinv[e] + (size_t)sel * XMI_CP_N, (double)uni<R>(g) * cdfs[sel]);
-  return cp_energy_from_q(energy, q, c, bad);
+  const T q = cp_shell_q<T>(b.cp_qinv[e] + (size_t)sel * XMI_CP_N, (T)uni<R>(g) * cdfs[sel]);
+  return (double)cp_energy_from_q(energy, q, c, sn, bad);
 }
 
 /* ---------------- variance reduction: event prologue ---------------- */
