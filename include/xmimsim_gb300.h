@@ -116,9 +116,12 @@ void xmi_detector_convolute_all_custom(xmi_inputFPtr inputFPtr, double **channel
  * 3 x 16384 doubles (384 KiB) kept on every GPU that loads the library until
  * exit.  Returns 0 with an error for nchannels > 16384 or when escape peaks
  * or pile-up are requested.  The first call on a device looks up the
- * scratch address for that device; make it before any stream capture.  All
- * calls share the scratch, which keeps the last call's contents; calls that
- * overlap on the GPU (concurrent host threads) race. */
+ * scratch address for that device; make it before any stream capture.  That
+ * address is cached for the life of the process: after a cudaDeviceReset()
+ * of the device it is stale, so do not call this entry point on a device
+ * that has been reset.  All calls share the scratch, which keeps the last
+ * call's contents; calls that overlap on the GPU (concurrent host threads)
+ * race. */
 int xmi_detector_convolute_spectrum_noalloc(xmi_inputFPtr inputFPtr, const double *channels_noconv,
                                             double *channels_conv, xmi_main_options *options);
 
@@ -250,6 +253,13 @@ int xmi_gpu_last_timing(double *transport_ms, double *total_ms, int *launches);
  * sort of the estimator events, estimator kernel) and the number of
  * estimator events */
 int xmi_gpu_last_phases(double *transport_kernel_ms, double *sort_ms, double *estimator_ms, long long *events);
+/* the device functions of the per-shell Compton kinematics
+ * (xmi_get_qimax / xmi_get_energy_from_q, src/xmi_aux_f.F90:1951-2074) in
+ * their FP32 and FP64 forms on n points (energy, binding energy, theta, Q):
+ * out[6 i ..] = qimax FP32, qimax FP64, scattered energy FP32, FP64, and the
+ * FP32 / FP64 "no root" flags */
+int xmi_gpu_compton_kinematics(int n, const double *energy, const double *binding, const double *theta,
+                               const double *q, double *out);
 
 #ifdef __cplusplus
 }

@@ -196,6 +196,29 @@ def convolute_spectrum(noconv, det_corr, gain, zero, fano, noise, det_type, live
     return out
 
 
+def poisson(channels, seed: int):
+    """oracle_poisson: Poisson noise on a copy of channels, channel i drawn from
+    the Philox stream (seed, i, 0xE0000000)."""
+    lib = load()
+    f = lib.oracle_poisson
+    f.restype, f.argtypes = None, [C.POINTER(C.c_double), C.c_int, C.c_uint64]
+    ch = np.array(channels, dtype=np.float64, copy=True)
+    f(_dp(ch), len(ch), seed)
+    return ch
+
+
+def sum_peaks(channels, live_time: float, pulse_width: float, gain: float, zero: float, seed: int):
+    """oracle_sum_peaks: the pile-up pulse train on a copy of channels."""
+    lib = load()
+    f = lib.oracle_sum_peaks
+    f.restype = C.c_int
+    f.argtypes = [C.POINTER(C.c_double), C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, C.c_uint64]
+    ch = np.array(channels, dtype=np.float64, copy=True)
+    if f(_dp(ch), len(ch), live_time, pulse_width, gain, zero, seed) != 1:
+        raise RuntimeError("oracle pulse train: more than 100 pulses in one group")
+    return ch
+
+
 def compton_qimax(energy: float, binding: float, theta: float) -> float:
     f = load().oracle_compton_qimax
     f.restype, f.argtypes = C.c_double, [C.c_double] * 3

@@ -204,3 +204,53 @@ int oracle_convolute_spectrum(const double *noconv, const double *det_corr, int 
 void oracle_detector_escape(double *ch, int nch, double gain, double zero, const oracle_escape *er) {
   detector_escape(ch, nch, gain, zero, er);
 }
+
+/* xmi_detector_poisson, src/xmi_detector_f.F90:862-905: every channel above
+ * 1 count and below 2^32 - 1 becomes a Poisson variate of that mean.  The
+ * reference draws from one serial MT19937 stream through GSL; here channel i
+ * draws from the Philox stream (seed, i, 0xE0000000) so that the GPU engine
+ * can be checked draw for draw.  The variate is exact: the multiplication
+ * method below a mean of 10, above it the transformed rejection with squeeze
+ * (PTRS) of W. Hormann, Insurance: Mathematics and Economics 12 (1993) 39-45. */
+static double poisson_variate(double lam, orng *g) {
+  if (lam < 10.0) {
+    double L = exp(-lam), prod = orng_uniform(g);
+    int n = 0;
+    while (prod > L && n < 4096) {
+      prod *= orng_uniform(g);
+      n++;
+    }
+    return (double)n;
+  } else {
+    double slam = sqrt(lam), loglam = log(lam);
+    double b = 0.931 + 2.53 * slam, a = -0.059 + 0.02483 * b;
+    double inv_alpha = 1.1239 + 1.1328 / (b - 3.4), vr = 0.9277 - 3.6224 / (b - 2.0);
+    int it;
+    for (it = 0; it < 4096; it++) {
+      double U = orng_uniform(g) - 0.5, V = orng_uniform(g);
+      double us = 0.5 - fabs(U);
+      double k = floor((2.0 * a / us + b) * U + lam + 0.43);
+      if (us >= 0.07 && V <= vr) return k;
+      if (k < 0.0 || (us < 0.013 && V > us)) continue;
+      if (log(V) + log(inv_alpha) - log(a / (us * us) + b) <= -lam + k * loglam - lgamma(k + 1.0)) return k;
+    }
+    return floor(lam + 0.5);
+  }
+}
+
+void oracle_poisson(double *ch, int nch, uint64_t seed) {
+  const double limit = 4294967296.0 - 1.0;
+  int i;
+  for (i = 0; i < nch; i++) {
+    orng g;
+    if (!(ch[i] > 1.0) || ch[i] > limit) continue;
+    orng_init(&g, seed, (uint64_t)i, 0xE0000000u);
+    ch[i] = poisson_variate(ch[i], &g);
+  }
+}
+
+/* the pile-up step alone (in place) */
+int oracle_sum_peaks(double *ch, int nch, double live_time, double pulse_width, double gain, double zero,
+                     uint64_t seed) {
+  return sum_peaks(ch, nch, live_time, pulse_width, gain, zero, seed);
+}

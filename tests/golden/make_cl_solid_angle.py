@@ -11,7 +11,7 @@ point's sampling cone (restated below from the kernel's set-up lines, FP64)
 so that a test can turn values back into hit counts out of 5000.  Also the
 Threefry4x32-20 blocks of the reference's Random123 header for a few inputs.
 
-usage (where the reference tree exists): make -C oracle/ref_cl && python tests/golden/make_cl_solid_angle.py
+usage (where the reference tree exists): make -C oracle/ref_cl REF=<tree> && python tests/golden/make_cl_solid_angle.py
 """
 from __future__ import annotations
 

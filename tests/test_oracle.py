@@ -223,3 +223,35 @@ def test_read_reference_example_input():
     assert spec.n_interactions_trajectory == 4
     assert len(spec.layers) == 2 and spec.reference_layer == 2
     assert spec.nchannels == len(g["unconv_last"])
+
+
+@pytest.mark.parametrize("lam", [0.5, 1.0, 2.5, 9.9, 10.0, 37.0, 1.0e3, 2.0e6])
+def test_oracle_poisson_is_poisson(lam):
+    """The oracle's Poisson step (the checker of the engine's): channels at or
+    below one count stay as they are; above, 40000 draws of mean lam match the
+    Poisson distribution -- mean, variance and third central moment (= lam),
+    and for small means the probability of every count (chi-square)."""
+    from scipy import stats
+    from oracle import oracle_api as O
+    n = 40000
+    k = O.poisson(np.full(n, lam), seed=0x9015)
+    if lam <= 1.0:
+        assert (k == lam).all()
+        return
+    assert np.array_equal(k, np.round(k)) and (k >= 0).all()
+    se = math.sqrt(lam / n)
+    assert abs(k.mean() - lam) < 5 * se
+    assert abs(k.var() / lam - 1.0) < 5 * math.sqrt(2.0 / n)
+    m3 = ((k - k.mean()) ** 3).mean()
+    assert abs(m3 - lam) < 6 * math.sqrt(15.0 * lam ** 3 / n)
+    if lam < 50:
+        top = int(lam + 6 * math.sqrt(lam) + 5)
+        obs = np.bincount(np.minimum(k.astype(int), top), minlength=top + 1)
+        p = stats.poisson.pmf(np.arange(top + 1), lam)
+        p[-1] = stats.poisson.sf(top - 1, lam)
+        exp = p * n
+        keep = exp > 5
+        chi2 = (((obs - exp) ** 2 / exp)[keep]).sum()
+        assert stats.chi2.sf(chi2, keep.sum() - 1) > 1e-4
+    # another seed gives other draws
+    assert not np.array_equal(k, O.poisson(np.full(n, lam), seed=0x9016))

@@ -121,3 +121,54 @@ def test_weight_update_rule_on_synthetic_histories():
     assert st.weights[0] == pytest.approx(0.05 * min(2.0 / k_sim, 2.5))
     assert st.weights[1] == pytest.approx(0.005 * min(5.0 / l_sim, 10.0))
     assert sum(st.layer.weight) == pytest.approx(1.0)
+
+
+def test_unconverged_sample_stops_alone(monkeypatch):
+    """A sample that cannot converge stops at max_iterations and comes back
+    with converged = False while the other sample of the batch converges;
+    strict=True raises instead.  The simulation is replaced by a stand-in that
+    returns K-alpha histories proportional to the Fe weight (sample 0) or
+    fixed (sample 1), so this runs on the CPU."""
+    lib = quant._xrl()
+    kl3 = lib.xrl_line_from_name(b"KL3")
+
+    class FakeSim:
+        def __init__(self, spec, options=None, gpu=None):
+            self.spec = spec
+
+        def solid_angle_grid(self):
+            return {"r": None, "theta": None, "grid": None}
+
+        def set_solid_angle(self, *a):
+            pass
+
+        @staticmethod
+        def msim_batch(sims):
+            outs = []
+            for s in sims:
+                lay = s.spec.layers[1]
+                w_fe = lay.weight[lay.Z.index(26)]
+                vr = np.zeros((100, 385, s.spec.n_interactions_trajectory))
+                vr[25, kl3 - 1, 0] = 1e3 * w_fe if s.spec.live_time == 1.0 else 1e-3
+                outs.append({"var_red": vr})
+            return outs
+
+        def free_raw(self, out):
+            pass
+
+        def close(self):
+            pass
+
+    monkeypatch.setattr(quant, "Simulation", FakeSim)
+    samples = []
+    for i in range(2):
+        spec, matrix = _sample_spec([0.05, 0.03, 0.02], n=10)
+        spec.live_time = 1.0 if i == 0 else 2.0  # marks the sample for the stand-in
+        absorb = quant.detector_absorption(spec, 26, "KL3")
+        samples.append(quant.QuantSample(spec=spec, ilay=1, matrix=matrix, z_quant=[26], k_exp=[50.0 * absorb],
+                                         l_exp=[0.0]))
+    res = quant.quantify(samples, options=dict(configs.C1_OPTIONS), max_iterations=12)
+    assert res[0].converged and res[0].weights[0] == pytest.approx(0.05, rel=0.05)
+    assert not res[1].converged and res[1].iterations == 12
+    with pytest.raises(quant.XmiError):
+        quant.quantify(samples, options=dict(configs.C1_OPTIONS), max_iterations=12, strict=True)

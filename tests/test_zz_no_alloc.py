@@ -23,12 +23,16 @@ def _spectra(nch, seed):
     return base
 
 
-def test_noalloc_matches_allocating_entry_point_twice():
-    from xmimsim_gb300 import Simulation, abi, configs
+@pytest.mark.parametrize("poisson", [0, 1])
+def test_noalloc_matches_allocating_entry_point_twice(poisson):
+    """With Poisson noise on, both entry points draw channel i from the same
+    per-channel stream of the same seed, so the counts are equal too."""
+    from xmimsim_gb300 import Simulation, abi, configs, gpu_options
     lib = abi.load()
     f = lib.xmi_detector_convolute_spectrum_noalloc
     spec = configs.config1(n_photons_line=10)
-    sim = Simulation(spec, options=dict(use_escape_peaks=0, use_sum_peaks=0, use_poisson=0, use_default_seeds=1))
+    sim = Simulation(spec, options=dict(use_escape_peaks=0, use_sum_peaks=0, use_poisson=poisson,
+                                        use_default_seeds=1), gpu=gpu_options(seed=0x5EED0001))
     nch = spec.nchannels
     for call, seed in enumerate((1, 2)):
         x = np.ascontiguousarray(_spectra(nch, seed))

@@ -104,12 +104,32 @@ def build_oracle(verbose: bool = False) -> Path:
     return lib
 
 
+# where the reference source tree is mounted in the build container; absent on
+# GPU machines, where the reference's own OpenCL kernel is not built
+REFERENCE_TREE = Path("/root/reference")
+
+
+def build_reference_kernel(verbose: bool = False) -> Path | None:
+    """Compiles the reference's OpenCL solid-angle kernel as host code into
+    oracle/_ref (test infrastructure: it generates the golden fixture of the
+    grid) when the reference tree is present; returns None otherwise."""
+    if not (REFERENCE_TREE / "src" / "xmi_kernels.cl").exists() or shutil.which("make") is None:
+        return None
+    _run(["make", "-s", "-C", str(ORACLE / "ref_cl"), "REF=%s" % REFERENCE_TREE])
+    lib = ORACLE / "_ref" / "libref_cl.so"
+    if verbose:
+        print("built", lib)
+    return lib
+
+
 def build_all(verbose: bool = False) -> None:
-    with cf.ThreadPoolExecutor(max_workers=2) as ex:
+    with cf.ThreadPoolExecutor(max_workers=3) as ex:
         f1 = ex.submit(build_engine, verbose)
         f2 = ex.submit(build_oracle, verbose)
+        f3 = ex.submit(build_reference_kernel, verbose)
         f1.result()
         f2.result()
+        f3.result()
 
 
 if __name__ == "__main__":

@@ -25,6 +25,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <atomic>
 #include <vector>
 
 #include "dev_bundle.cuh"
@@ -253,8 +254,41 @@ __global__ void pile_tally_kernel(PileParams p, const double *cdf, long long n_u
   if (ch >= 0) atomicAdd(&out[ch], 1.0);
 }
 
-/* Poisson variate (multiplication method for small means, normal
- * approximation with continuity correction above 1e3), stream (seed, channel, 0xE0000000) */
+/* Exact Poisson variate of mean lam from stream r: the multiplication method
+ * (count uniforms until their product drops below exp(-lam)) for lam < 10,
+ * and for lam >= 10 the transformed rejection with squeeze of W. Hörmann,
+ * "The transformed rejection method for generating Poisson random variables",
+ * Insurance: Mathematics and Economics 12 (1993) 39-45 (PTRS).  Both loops
+ * are bounded at 4096 rounds, far beyond what their acceptance rates ever
+ * need (PTRS accepts most candidates at the first or second try). */
+__device__ double poisson_draw(double lam, xmi_rng *r) {
+  if (lam < 10.0) {
+    const double L = exp(-lam);
+    double prod = xmi_rng_uniform(r);
+    int n = 0;
+    while (prod > L && n < 4096) {
+      prod *= xmi_rng_uniform(r);
+      n++;
+    }
+    return (double)n;
+  }
+  const double slam = sqrt(lam), loglam = log(lam);
+  const double b = 0.931 + 2.53 * slam, a = -0.059 + 0.02483 * b;
+  const double inv_alpha = 1.1239 + 1.1328 / (b - 3.4), vr = 0.9277 - 3.6224 / (b - 2.0);
+  for (int it = 0; it < 4096; it++) {
+    const double U = xmi_rng_uniform(r) - 0.5, V = xmi_rng_uniform(r);
+    const double us = 0.5 - fabs(U);
+    const double k = floor((2.0 * a / us + b) * U + lam + 0.43);
+    if (us >= 0.07 && V <= vr) return k;
+    if (k < 0.0 || (us < 0.013 && V > us)) continue;
+    if (log(V) + log(inv_alpha) - log(a / (us * us) + b) <= -lam + k * loglam - lgamma(k + 1.0)) return k;
+  }
+  return floor(lam + 0.5);
+}
+
+/* src/xmi_detector_f.F90:862-905: every channel above 1 count (and below
+ * 2^32 - 1) is replaced by a Poisson variate of that mean; channel i draws
+ * from stream (seed, i, 0xE0000000) */
 __global__ void poisson_kernel(int nch, unsigned long long seed, double *ch) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nch) return;
@@ -263,29 +297,7 @@ __global__ void poisson_kernel(int nch, unsigned long long seed, double *ch) {
   if (!(lam > 1.0) || lam > limit) return;
   xmi_rng r;
   xmi_rng_init(&r, seed, (uint64_t)i, 0xE0000000u);
-  double k;
-  if (lam < 1000.0) {
-    /* split large means into chunks of 30 to keep exp() representable */
-    double rem = lam;
-    k = 0.0;
-    while (rem > 0.0) {
-      double l = rem > 30.0 ? 30.0 : rem, L = exp(-l), prod = xmi_rng_uniform(&r);
-      int n = 0;
-      while (prod > L && n < 10000) {
-        prod *= xmi_rng_uniform(&r);
-        n++;
-      }
-      k += n;
-      rem -= l;
-    }
-  } else {
-    double u1 = xmi_rng_uniform(&r), u2 = xmi_rng_uniform(&r);
-    if (u1 <= 0.0) u1 = 1e-300;
-    double z = sqrt(-2.0 * log(u1)) * cos(2.0 * 3.14159265358979323846 * u2);
-    k = floor(lam + sqrt(lam) * z + 0.5);
-    if (k < 0.0) k = 0.0;
-  }
-  ch[i] = k;
+  ch[i] = poisson_draw(lam, &r);
 }
 
 bool ck(cudaError_t e, const char *w) {
@@ -846,8 +858,14 @@ static __device__ __align__(256) double xmi_noalloc_scratch[3 * XMI_NOALLOC_MAX_
 
 namespace {
 /* device address of the scratch array per device, looked up once per device
- * with that device current; the host-side symbol is only a stand-in */
-double *g_noalloc_ptr[64];
+ * (on the first call made with that device current); the host-side symbol is
+ * only a stand-in.  Threads that make their first calls at the same time may
+ * each look it up; they find the same address and store it atomically.
+ * The address belongs to the device's context at the time of that first
+ * call: after a cudaDeviceReset() of the device the cached address is no
+ * longer valid, so a process that resets a device must not call this entry
+ * point on it again. */
+std::atomic<double *> g_noalloc_ptr[64];
 
 double *noalloc_scratch_for_current_device() {
   int dev = 0;
@@ -855,17 +873,17 @@ double *noalloc_scratch_for_current_device() {
     xmi_set_error("xmi_detector_convolute_spectrum_noalloc: no current CUDA device");
     return nullptr;
   }
-  if (!g_noalloc_ptr[dev]) {
-    double *p = nullptr;
+  double *p = g_noalloc_ptr[dev].load(std::memory_order_acquire);
+  if (!p) {
     cudaError_t rc = cudaGetSymbolAddress((void **)&p, xmi_noalloc_scratch);
     if (rc != cudaSuccess || !p) {
       xmi_set_error("xmi_detector_convolute_spectrum_noalloc: cudaGetSymbolAddress failed: %s",
                     cudaGetErrorString(rc));
       return nullptr;
     }
-    g_noalloc_ptr[dev] = p;
+    g_noalloc_ptr[dev].store(p, std::memory_order_release);
   }
-  return g_noalloc_ptr[dev];
+  return p;
 }
 
 /* host staging of the absorption-corrected input, per calling thread */

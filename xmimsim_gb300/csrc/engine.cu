@@ -1495,3 +1495,54 @@ extern "C" int xmi_gpu_autotune_batch(int n, xmi_inputFPtr *inputFPtrs, xmi_hdf5
   }
   return 1;
 }
+
+/* ---------------------------------------------------------------- */
+/* Diagnostic: the momentum kinematics of the advanced Compton path    */
+/* ---------------------------------------------------------------- */
+namespace {
+__global__ void compton_kinematics_kernel(int n, const double *energy, const double *binding, const double *theta,
+                                          const double *q, double *out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double th = theta[i];
+  const float thf = (float)th, shf = sinf(0.5f * thf);
+  bool bad64 = false, bad32 = false;
+  out[6 * i + 0] = (double)xmi::cp_qimax<float>((float)energy[i], (float)binding[i], cosf(thf), shf * shf);
+  out[6 * i + 1] = xmi::cp_qimax<double>(energy[i], binding[i], cos(th), 0.0);
+  out[6 * i + 2] = (double)xmi::cp_energy_from_q((float)energy[i], (float)q[i], cosf(thf), sinf(thf), bad32);
+  out[6 * i + 3] = xmi::cp_energy_from_q(energy[i], q[i], cos(th), sin(th), bad64);
+  out[6 * i + 4] = bad32 ? 1.0 : 0.0;
+  out[6 * i + 5] = bad64 ? 1.0 : 0.0;
+}
+}  // namespace
+
+/* Runs the device functions of the per-shell Compton kinematics (FP32 and
+ * FP64 forms) on n points: out[6 i ..] = qimax FP32, qimax FP64, scattered
+ * energy FP32, scattered energy FP64, and the two "no root" flags. */
+extern "C" int xmi_gpu_compton_kinematics(int n, const double *energy, const double *binding, const double *theta,
+                                          const double *q, double *out) {
+  if (n < 0 || (n > 0 && (!energy || !binding || !theta || !q || !out))) {
+    xmi_set_error("xmi_gpu_compton_kinematics: bad arguments");
+    return 0;
+  }
+  if (n == 0) return 1;
+  double *d = nullptr;
+  const size_t in_bytes = sizeof(double) * (size_t)n;
+  if (cudaMalloc(&d, in_bytes * 10) != cudaSuccess) {
+    xmi_set_error("xmi_gpu_compton_kinematics: cudaMalloc failed");
+    return 0;
+  }
+  bool ok = cudaMemcpy(d, energy, in_bytes, cudaMemcpyHostToDevice) == cudaSuccess &&
+            cudaMemcpy(d + n, binding, in_bytes, cudaMemcpyHostToDevice) == cudaSuccess &&
+            cudaMemcpy(d + 2 * (size_t)n, theta, in_bytes, cudaMemcpyHostToDevice) == cudaSuccess &&
+            cudaMemcpy(d + 3 * (size_t)n, q, in_bytes, cudaMemcpyHostToDevice) == cudaSuccess;
+  if (ok) {
+    compton_kinematics_kernel<<<(n + 127) / 128, 128>>>(n, d, d + n, d + 2 * (size_t)n, d + 3 * (size_t)n,
+                                                        d + 4 * (size_t)n);
+    ok = cudaGetLastError() == cudaSuccess &&
+         cudaMemcpy(out, d + 4 * (size_t)n, in_bytes * 6, cudaMemcpyDeviceToHost) == cudaSuccess;
+  }
+  cudaFree(d);
+  if (!ok) xmi_set_error("xmi_gpu_compton_kinematics: CUDA error");
+  return ok ? 1 : 0;
+}

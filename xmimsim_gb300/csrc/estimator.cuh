@@ -49,8 +49,8 @@ __device__ __noinline__ R compton_advanced_est(const DevBundle<R> &b, const DevT
                                                R base, xmi_rng *g, bool valid, bool &ok) {
   using T = cp_real<R>;
   T cdfs[XMI_CP_SH];
-  const T E = (T)ev.E, th = (T)ev.theta, c = cos(th), sn = sin(th);
-  const T sum = cp_shell_cdfs<T>(b, e, E, c, cdfs);
+  const T E = (T)ev.E, th = (T)ev.theta, c = cos(th), sn = sin(th), sh = sin(th * (T)0.5);
+  const T sum = cp_shell_cdfs<T>(b, e, E, c, sh * sh, cdfs);
   R total = (R)0;
   if (sum == (T)0) return total;
   const int ns = b.cp_nshell[e];

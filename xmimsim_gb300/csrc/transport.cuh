@@ -1,23 +1,25 @@
 /*
- * Photon transport with the point-detector variance-reduction estimator,
- * GB300 kernel.  Behaviour follows the reference step for step
- * (src/xmi_main.F90:1188-1685 xmi_simulate_photon and the interaction
+ * Photon transport and the point-detector variance-reduction estimator:
+ * the per-photon device functions.  Behaviour follows the reference step for
+ * step (src/xmi_main.F90:1188-1685 xmi_simulate_photon and the interaction
  * routines, src/xmi_variance_reduction.F90:29-1101); the structure is the
  * GPU's own:
- *  - one thread per photon history, persistent grid-stride loop over a
- *    compact work index (history-based: with variance reduction every photon
- *    makes the same number of forced interactions, so trip counts are
- *    uniform and the estimator -- the dominant cost -- runs converged);
+ *  - the functions here work on one photon (or one estimator event) at a
+ *    time; the event-based kernels of wavefront.cuh run them over queues:
+ *    a step kernel moves every active photon to its next interaction point
+ *    and files it into the Rayleigh, Compton or photo-absorption queue, and
+ *    one interaction kernel per queue runs a single code path over its
+ *    lanes (escape_kernel in detector.cu still runs whole histories);
  *  - random numbers from Philox streams keyed (photon, phase, draw), so a
- *    photon's sequence does not depend on the launch shape;
+ *    photon's sequence does not depend on the launch shape, the queue it
+ *    waits in or the kernel that resumes it;
  *  - layer loops fully unrolled over XMI_MAXL with predicates, keeping the
  *    per-layer attenuation state in registers;
  *  - one energy-grid location per energy change, reused by every table;
- *  - line-history tallies accumulated per CTA in shared memory (warp
- *    pre-reduced when the lanes agree), flushed once with FP64 atomics;
- *    fluorescence channel contributions are derived from those histories
- *    after the kernel, Rayleigh/Compton channel contributions go straight to
- *    FP64 global atomics.
+ *  - the geometric part of the estimator (vr_prologue) runs in the step
+ *    kernel and emits one event per interaction; the element and line loops
+ *    run later in estimator.cuh over events sorted by (configuration, layer,
+ *    order), with FP64 tallies.
  */
 #ifndef XMIMSIM_GB300_TRANSPORT_CUH
 #define XMIMSIM_GB300_TRANSPORT_CUH
@@ -671,13 +673,22 @@ constexpr double kXrlMec2 = 510.998928;
 template <typename R>
 using cp_real = typename std::conditional<sizeof(R) == 4, float, double>::type;
 
-/* xmi_get_qimax (c = cos theta) */
+/* xmi_get_qimax (c = cos theta, h2 = sin^2(theta / 2)).  FP64 follows the
+ * reference's arithmetic; FP32 writes 1 - c as 2 h2 and the denominator
+ * (E - I)^2 + E^2 - 2 (E - I) E c as I^2 + 4 (E - I) E h2, which are exact
+ * rewritings without the cancellation both forms of the reference suffer at
+ * small theta (1% error at theta = 5e-3 in FP32). */
 template <typename T>
-__device__ __forceinline__ T cp_qimax(T energy, T Ii, T c) {
+__device__ __forceinline__ T cp_qimax(T energy, T Ii, T c, T h2) {
   if (Ii != (T)0 && energy < Ii) return (T)0;
   const T emi = energy - Ii;
-  const T q = (T)137 * (emi * energy * ((T)1 - c) / (T)kXrlMec2 - Ii);
-  return q / sqrt(emi * emi + energy * energy - (T)2 * emi * energy * c);
+  if constexpr (sizeof(T) == 4) {
+    const T q = (T)137 * ((T)2 * emi * energy * h2 / (T)kXrlMec2 - Ii);
+    return q / sqrt(Ii * Ii + (T)4 * emi * energy * h2);
+  } else {
+    const T q = (T)137 * (emi * energy * ((T)1 - c) / (T)kXrlMec2 - Ii);
+    return q / sqrt(emi * emi + energy * energy - (T)2 * emi * energy * c);
+  }
 }
 
 /* xmi_get_q_from_energy */
@@ -768,11 +779,11 @@ __device__ __forceinline__ T cp_shell_q(const R *row, T cdf) {
 /* every shell's cumulative profile at (energy, c = cos theta) and their
  * occupancy-weighted sum */
 template <typename T, typename R>
-__device__ __forceinline__ T cp_shell_cdfs(const DevBundle<R> &b, int e, T energy, T c, T *cdfs) {
+__device__ __forceinline__ T cp_shell_cdfs(const DevBundle<R> &b, int e, T energy, T c, T h2, T *cdfs) {
   const int ns = b.cp_nshell[e];
   for (int k = 0; k < ns; k++)
     cdfs[k] = cp_shell_cdf<T>(b.cp_cdf[e] + (size_t)k * XMI_CP_N,
-                              cp_qimax<T>(energy, (T)b.cp_edge[e * XMI_CP_SH + k], c));
+                              cp_qimax<T>(energy, (T)b.cp_edge[e * XMI_CP_SH + k], c, h2));
   T sum = (T)0;
   for (int k = 0; k < ns; k++) sum = sum + (T)b.cp_occ[e * XMI_CP_SH + k] * cdfs[k];
   return sum;
@@ -785,8 +796,8 @@ __device__ __noinline__ double compton_energy_advanced(const DevBundle<R> &b, in
                                                        xmi_rng *g, bool &bad) {
   using T = cp_real<R>;
   T cdfs[XMI_CP_SH];
-  const T energy = (T)energy_in, th = (T)theta_i, c = cos(th), sn = sin(th);
-  const T sum = cp_shell_cdfs<T>(b, e, energy, c, cdfs);
+  const T energy = (T)energy_in, th = (T)theta_i, c = cos(th), sn = sin(th), sh = sin(th * (T)0.5);
+  const T sum = cp_shell_cdfs<T>(b, e, energy, c, sh * sh, cdfs);
   if (sum == (T)0) return 0.0;
   const int ns = b.cp_nshell[e];
   const T r = (T)uni<R>(g);

@@ -219,22 +219,26 @@ class _State:
 
 
 def quantify(samples: Sequence[QuantSample], options: dict | None = None, gpu=None,
-             max_iterations: int = MAX_ITERATIONS) -> list[QuantResult]:
+             max_iterations: int = MAX_ITERATIONS, strict: bool = False) -> list[QuantResult]:
     """Quantifies every sample; each iteration simulates all samples that have
     not converged in one batched call.  options: xmi_main_options fields
     (variance reduction must be on: the loop reads its histories); gpu:
-    xmi_gpu_options for every simulation."""
+    xmi_gpu_options for every simulation.
+
+    A sample that has not converged after max_iterations stops there and is
+    returned with converged = False while the others go on: the reference
+    quantifies one sample per process and gives up on that sample alone
+    (bin/xmimsim-pymca.c:602-605).  strict=True raises XmiError instead, once
+    every sample has stopped."""
     opts = dict(options or {})
     if opts.get("use_variance_reduction", 1) != 1:
         raise XmiError("quantify: the loop reads the variance-reduction histories (use_variance_reduction = 1)")
     states = [_State(s) for s in samples]
     while True:
-        active = [st for st in states if not st.done()]
+        active = [st for st in states if not st.done() and st.it < max_iterations]
         if not active:
             break
         for st in active:
-            if st.it + 1 > max_iterations:
-                raise XmiError(f"quantify: no convergence after {st.it} iterations")
             st.it += 1
         sims = []
         try:
@@ -252,5 +256,9 @@ def quantify(samples: Sequence[QuantSample], options: dict | None = None, gpu=No
         finally:
             for sim in sims:
                 sim.close()
+    if strict:
+        failed = [i for i, st in enumerate(states) if not st.done()]
+        if failed:
+            raise XmiError(f"quantify: samples {failed} did not converge in {max_iterations} iterations")
     return [QuantResult(st.weights.copy(), st.layer, st.it, st.done(), st.sum_k, st.sum_l, st.k_sim.copy(),
                         st.l_sim.copy()) for st in states]
