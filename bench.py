@@ -30,6 +30,17 @@ One step = one xmi_main_msim_batch call over all 512 configurations with
 layers (seed 2) of 3-12 elements, Rh tube at 40 kV behind 125 um Be in 400
 intervals plus the Rh K/L lines, 6 interactions, one xmi_main_msim per step.
 
+``--workload surrogate``: the learned solid-angle surrogate on its own
+geometry -- the small plain configuration behind a conical collimator
+(height 1 cm, opening radius 0.1 cm), 1e8 photons per step, FP32 transport.
+The grid path (a 1000 x 1000 FP64 grid, then the transport reading it) and
+the surrogate path (the network trained on 2e6 integrator samples uniform
+over the sample volume, checked per cell at the 1e-3 tolerance, flagged
+cells served by the tabulated integrator, then the transport serving it)
+are both timed; the line is the surrogate path's, with the network's check,
+a held-out validation at the estimator's own query points and the per-line
+error against the grid path beside it.
+
 Multi-GPU (torchrun): every rank runs its own configurations (weak scaling,
 no data-path collective).
 
@@ -63,7 +74,7 @@ def parse():
     p.add_argument("--steps", type=int, default=3)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--workload", default="batched", choices=["batched", "plain"])
+    p.add_argument("--workload", default="batched", choices=["batched", "plain", "surrogate"])
     p.add_argument("--plain-mode", default="default", choices=["default", "advanced-compton", "analog"],
                    help="transport options of the plain workload")
     p.add_argument("--configs", type=int, default=512, help="configurations of the batched workload")
@@ -79,6 +90,13 @@ def parse():
     p.add_argument("--line-configs", type=int, default=3, help="configurations of the FP64 line-error check")
     p.add_argument("--no-plain", action="store_true")
     p.add_argument("--photons", type=float, default=1e7, help="photons per step of the plain workload")
+    p.add_argument("--photons-surrogate", type=float, default=1e8,
+                   help="photons per step of the surrogate workload")
+    p.add_argument("--hits-train", type=int, default=1 << 14,
+                   help="integrator samples per training point of the surrogate workload")
+    p.add_argument("--epochs-surrogate", type=int, default=32, help="training epochs of the surrogate workload")
+    p.add_argument("--n-train-surrogate", type=int, default=2_000_000,
+                   help="training points of the surrogate workload (uniform over the sample volume)")
     p.add_argument("--precision", default="fp32", choices=["fp64", "fp32"])
     p.add_argument("--cpu-sample", type=int, default=100000, help="photons of the CPU-baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
@@ -224,6 +242,10 @@ def cpu_sample_specs(args, rank=0):
     if args.workload == "plain":
         spec, options = plain_workload(args.photons, args.plain_mode)
         return [spec], options, "the %.0e-photon plain workload" % args.photons
+    if args.workload == "surrogate":
+        from xmimsim_gb300 import configs
+        return [configs.config4(int(args.photons_surrogate))], dict(configs.C1_OPTIONS), \
+            "the collimated surrogate workload"
     specs, options = batched_specs(args.configs, args.budget_scale, rank)
     pick = [specs[i] for i in range(0, len(specs), max(1, len(specs) // 8))][:8]
     return pick, options, "8 of the %d batched configurations" % len(specs)
@@ -257,7 +279,11 @@ def reference_arm(args):
 
 
 def workload_config(args, extra):
-    if args.workload == "plain":
+    if args.workload == "surrogate":
+        cfg = {"workload": "collimated config-1 geometry (conical collimator 1 cm high, 0.1 cm opening radius, "
+                           "45/45 degrees, 10 cm), FP32 transport, solid angles from the surrogate network",
+               "photons_per_step": int(args.photons_surrogate)}
+    elif args.workload == "plain":
         cfg = {"workload": "plain 5-layer Rh 40 kV, 400 intervals + Rh K/L lines, 6 interactions, "
                            + PLAIN_MODES[args.plain_mode],
                "photons_per_step": int(args.photons)}
@@ -341,6 +367,9 @@ def line_error(sur_out: dict, ref_out: dict, floor: float = 1e-2) -> dict:
     import numpy as np
     a = sur_out["var_red"].sum(axis=2).ravel()
     b = ref_out["var_red"].sum(axis=2).ravel()
+    bad = int((~np.isfinite(a)).sum() + (~np.isfinite(b)).sum())
+    if bad:
+        return {"nonfinite": bad}
     m = b > floor * b.max()
     rel = np.abs(a[m] - b[m]) / b[m]
     return {"lines": int(m.sum()), "max": float(rel.max()) if m.any() else 0.0,
@@ -558,6 +587,101 @@ def plain_arm(args, ws, rank, local):
     return line, [sim], [spec], options
 
 
+def surrogate_arm(args, ws, rank, local):
+    """The collimated surrogate workload: grid path and surrogate path on the
+    same photon streams."""
+    import numpy as np
+    from xmimsim_gb300 import Simulation, configs, gpu_options
+    spec = configs.config4(n_photons_line=int(args.photons_surrogate))
+    options = dict(configs.C1_OPTIONS)
+    seed = 0x5EED0004 + rank
+    n_hist = histories(spec)
+    cudart = load_cudart()
+
+    # grid path: the reference-style 1000 x 1000 grid, FP64 integrator
+    g64 = gpu_options(precision=0, seed=seed, grid_n=1000)
+    gsim = Simulation(spec, options=options, gpu=g64)
+    t0 = time.perf_counter()
+    ax = gsim.solid_angle_grid()
+    grid_s = time.perf_counter() - t0
+    grid_run = Simulation(spec, options=options, gpu=gpu_options(precision=1, seed=seed, grid_n=1000))
+    grid_run.set_solid_angle(ax["r"], ax["theta"], ax["grid"])
+
+    # surrogate path: 2e6 training samples uniform over the sample volume
+    g_sur = gpu_options(precision=1, seed=seed, use_surrogate=1, surrogate_tolerance=args.tolerance, grid_n=1000)
+    sur = Simulation(spec, options=options, gpu=g_sur)
+    t0 = time.perf_counter()
+    rep = sur.build_surrogate(n_train=args.n_train_surrogate, hits_train=args.hits_train,
+                              epochs=args.epochs_surrogate, hits_check=args.hits_check)
+    train_s = time.perf_counter() - t0
+    # held-out validation at the estimator's own query points (a pilot run
+    # with another seed), judged by the integrator with 2^24 samples per point
+    pilot = Simulation(spec, options=options, gpu=gpu_options(precision=1, seed=seed ^ 0xABCDEF, use_surrogate=1))
+    pilot.share_surrogate(sur)
+    r, t = pilot.sample_event_points(share=min(1.0, 4e5 / n_hist), max_points=1 << 14)
+    held_out = sur.validate_surrogate(r, t, hits=1 << 24)
+    pilot.close()
+
+    def runner(sim):
+        def step():
+            out = sim.msim()
+            tm = sim.timing()
+            if sim in last:
+                sim.free_raw(last[sim])
+            last[sim] = out
+            return tm
+        return step
+
+    last = {}
+    tms_g, wall_g, _ = timed_steps(args, runner(grid_run), local)
+    tms, wall, clocks = timed_steps(args, runner(sur), local)
+    ksum = sum(t["kernel_ms"] for t in tms)
+    ksum_g = sum(t["kernel_ms"] for t in tms_g)
+    out_s, out_g = last[sur], last[grid_run]
+    # all-FP64 grid run of the same photons: the precision reference
+    ref = Simulation(spec, options=options, gpu=g64)
+    ref.set_solid_angle(ax["r"], ax["theta"], ax["grid"])
+    out_64 = ref.msim()
+    errs = {"vs_grid_fp32": line_error(out_s, out_g, floor=1e-3), "vs_grid_fp64": line_error(out_s, out_64, 1e-3),
+            "grid_fp32_vs_grid_fp64": line_error(out_g, out_64, floor=1e-3),
+            "lines": "lines with >= 0.1% of the strongest, summed over orders; same photon streams"}
+    for o, sm in ((out_s, sur), (out_g, grid_run), (out_64, ref)):
+        sm.free_raw(o)
+    ref.close()
+    gsim.close()
+    step_s, step_g = wall / args.steps, wall_g / args.steps
+    extra = {"grid": "1000 x 1000, FP64 integrator, %d samples per point" % 5000, "grid_s": grid_s,
+             "surrogate": dict(rep, n_train=args.n_train_surrogate, hits_train=args.hits_train,
+                               epochs=args.epochs_surrogate,
+                               tolerance=args.tolerance, hits_check=args.hits_check, wall_s=train_s,
+                               sampling="uniform over the sample volume (2 cm around the beam axis)"),
+             "held_out": held_out,
+             "l2": "tables and grid above 129 MB: no; inputs smaller than L2, no flush between steps"}
+    line = {"metric": PLAIN_METRIC + " (surrogate-served transport)", "value": n_hist * args.steps / (ksum / 1e3),
+            "unit": "histories/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ksum / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 transport, f64 tallies", "data": "synthetic (config-1 sample, 17.44 keV line)",
+            "config": workload_config(args, extra),
+            "gpu_launches": sum(t["launches"] for t in tms),
+            "phases_ms_per_step": {k: statistics.mean(t[k + "_ms"] for t in tms)
+                                   for k in ("transport", "sort", "surrogate", "estimator")},
+            "events_per_step": statistics.mean(t["events"] for t in tms),
+            "surrogate_fallbacks_per_step": statistics.mean(t["surrogate_fallbacks"] for t in tms),
+            "e2e": {"value": n_hist * args.steps / wall, "unit": "histories/s",
+                    "h2d_bytes_per_step": int(statistics.mean(t["h2d_bytes"] for t in tms)),
+                    "d2h_bytes_per_step": int(statistics.mean(t["d2h_bytes"] for t in tms))},
+            "grid_path": {"value": n_hist * args.steps / (ksum_g / 1e3), "e2e": n_hist * args.steps / wall_g,
+                          "phases_ms_per_step": {k: statistics.mean(t[k + "_ms"] for t in tms_g)
+                                                 for k in ("transport", "sort", "estimator")},
+                          "job_s": grid_s + step_g, "job": "grid + one step"},
+            "surrogate_path_job_s": train_s + step_s,
+            "line_error": errs,
+            "clocks": clocks}
+    if cudart is not None:
+        cudart.cudaDeviceSynchronize()
+    return line, [grid_run, sur], [spec], options
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -574,7 +698,7 @@ def main():
             cudart.cudaSetDevice(local)
     from xmimsim_gb300.build import build_all
     build_all()
-    arm = batched_arm if args.workload == "batched" else plain_arm
+    arm = {"batched": batched_arm, "plain": plain_arm, "surrogate": surrogate_arm}[args.workload]
     line, sims, specs, options = arm(args, ws, rank, local)
     if ws > 1:
         import torch
@@ -590,9 +714,9 @@ def main():
                                 "sample": "%d photons (%.2f s) over %s" % (cn, cdt, what)}
         word = 4 if line["dtype"].startswith("f32") else 8
         qev = line["config"].get("autotuned", {}).get("queue_events") or (1 << 25)
-        n_int = 4 if args.workload == "batched" else 6
+        n_int = 6 if args.workload == "plain" else 4
         per_launch = min(qev // n_int, line["config"]["photons_per_step"])
-        tph = ESTIMATOR_DRAM_BYTES_PER_HISTORY[args.workload] if word == 4 else None
+        tph = ESTIMATOR_DRAM_BYTES_PER_HISTORY.get(args.workload) if word == 4 else None
         line["roofline"] = roofline_block(line["phases_ms_per_step"], line["config"]["photons_per_step"],
                                           words_tr, words_est, word, tph, per_launch)
     if rank == 0:

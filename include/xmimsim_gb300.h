@@ -46,6 +46,7 @@ typedef struct {
                                stream (src/xmi_kernels.cl:226-227), for point-by-point
                                comparison with that kernel */
   long long queue_events;   /* estimator events per chunk (device queue size); 0: default 2^25 */
+  int grid_nr, grid_nt;     /* solid-angle grid points along r and theta; 0: the reference's 1024 */
 } xmi_gpu_options;
 
 /* ---- data model helpers (reference src/xmi_data_structs.c) ---- */
@@ -173,6 +174,22 @@ int xmi_gpu_autotune_batch(int n, xmi_inputFPtr *inputFPtrs, xmi_hdf5FPtr *hdf5F
 int xmi_gpu_build_surrogate(xmi_inputFPtr inputFPtr, int n_train, int hits_train, int epochs, int hits_check,
                             double *report);
 int xmi_gpu_surrogate_report(xmi_inputFPtr inputFPtr, double *report);
+/* The solid angle the transport would take from the input's trained
+ * surrogate at n points (r, theta of the grid's coordinates), as it serves
+ * them: omega[i], and source[i] = 0 network, 1 tabulated integrator of a
+ * flagged cell, 2 outside the checked region (the transport integrates such
+ * a point itself; omega[i] is then set to -1), 3 below the grid's lowest
+ * theta (omega 0).  No counterpart in the reference (it has no surrogate);
+ * used to validate the network on held-out points. */
+int xmi_gpu_surrogate_eval(xmi_inputFPtr inputFPtr, int n, const double *r, const double *theta, double *omega,
+                           int *source);
+/* The engine's solid-angle integrator (the grid's per-point Monte Carlo of
+ * src/xmi_solid_angle_f.F90:432-710) at n arbitrary points with `hits`
+ * samples each, FP64 (precision 0) or FP32 (1), Philox key `seed`: point i
+ * draws from stream (seed, i, 0xF1000000).  No counterpart in the reference
+ * as an entry point; the judge of the surrogate. */
+int xmi_gpu_solid_angle_points(xmi_inputFPtr inputFPtr, int n, const double *r, const double *theta, int hits,
+                               int precision, unsigned long long seed, double *omega);
 /* the same training and check on caller-given points (r, theta) of the
  * solid-angle grid's frame -- typically the points where the estimator of a
  * pilot run queried solid angles (xmi_gpu_sample_event_points): the first

@@ -106,7 +106,8 @@ class XmiEscapeRatiosOptions(C.Structure):
 class XmiGpuOptions(C.Structure):
     _fields_ = [("precision", C.c_int), ("use_surrogate", C.c_int), ("surrogate_tolerance", C.c_double),
                 ("threads_per_block", C.c_int), ("blocks_per_sm", C.c_int), ("seed", C.c_ulonglong),
-                ("solid_angle_stream", C.c_int), ("queue_events", C.c_longlong)]
+                ("solid_angle_stream", C.c_int), ("queue_events", C.c_longlong),
+                ("grid_nr", C.c_int), ("grid_nt", C.c_int)]
 
 
 # exported symbols and their prototypes (name -> (restype, argtypes))
@@ -158,6 +159,12 @@ PROTOTYPES = {
     "xmi_gpu_build_surrogate": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, c_double_p]),
     "xmi_gpu_surrogate_report": (C.c_int, [C.c_void_p, c_double_p]),
     "xmi_gpu_share_surrogate": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "xmi_gpu_surrogate_eval": (C.c_int, [C.c_void_p, C.c_int, c_double_p, c_double_p, c_double_p,
+                                         C.POINTER(C.c_int)]),
+    "xmi_gpu_solid_angle_points": (C.c_int, [C.c_void_p, C.c_int, c_double_p, c_double_p, C.c_int, C.c_int,
+                                             C.c_ulonglong, c_double_p]),
+    "xmi_gpu_compton_kinematics": (C.c_int, [C.c_int, c_double_p, c_double_p, c_double_p, c_double_p,
+                                             c_double_p]),
     "xmi_tube_ebel": (C.c_int, [C.POINTER(XmiLayer), C.POINTER(XmiLayer), C.POINTER(XmiLayer), C.c_double,
                                 C.c_double, C.c_double, C.c_double, C.c_double, C.c_double, C.c_int, C.c_size_t,
                                 c_double_p, c_double_p, C.POINTER(C.POINTER(XmiExcitation))]),

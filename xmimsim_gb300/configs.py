@@ -6,6 +6,11 @@
 * ``config2``: the production-size plain case (5 random layers, Rh tube at
   40 kV through 125 um Be in 400 intervals plus the Rh K/L lines, 1e8 photons,
   6 interactions).
+* ``config3``: the precision form of config 1 (10 nm and 50 nm layers over a
+  2 mm substrate).
+* ``config4``: the learned solid-angle surrogate's workload (config 1 with a
+  conical collimator, 1e8 photons).
+* ``config5``: the 512-configuration batched quantification sweep.
 * ``caso4``: the reference's CaSO4 first-interaction test input
   (tests/libxmimsim-test.c:182-244).
 """
@@ -43,6 +48,18 @@ def config3(n_photons_line: int = 100000) -> InputSpec:
     sample = Layer([14, 8, 26, 29, 30], [0.40, 0.50, 0.05, 0.03, 0.02], 2.5, 0.2)
     spec.layers = [AIR, Layer([24], [1.0], 7.19, 1e-6), Layer([79], [1.0], 19.3, 5e-6), sample]
     spec.reference_layer = 2
+    return spec
+
+
+def config4(n_photons_line: int = 100_000_000) -> InputSpec:
+    """The learned solid-angle surrogate's workload: the config-1 geometry
+    with a conical collimator of height 1 cm and opening radius 0.1 cm
+    (collimator_diameter 0.2) in front of the 0.3 cm2 detector (radius
+    0.309 cm > 0.1 cm, so the conical case of src/xmi_main.F90:1780-1796),
+    45/45 degrees, 10 cm from the sample, 1e8 photons."""
+    spec = config1(n_photons_line=n_photons_line)
+    spec.collimator_height = 1.0
+    spec.collimator_diameter = 0.2
     return spec
 
 

@@ -507,9 +507,14 @@ int xmi_gpu_last_surrogate(double *surrogate_ms, long long *fallbacks) {
 /* ---------------------------------------------------------------- */
 static int solid_angle_impl(xmi_inputFPtr in, xmi_solid_angle **out, char *input_string, int precision,
                             unsigned long long seed) {
-  const int nr = 1024, nt = 1024;
   if (!in || !out || !in->initialized) {
     xmi_set_error("xmi_solid_angle_calculation: input not initialised");
+    return 0;
+  }
+  /* the reference's grid is 1024 x 1024 (src/xmi_solid_angle_f.F90:62-301) */
+  const int nr = in->gpu.grid_nr > 0 ? in->gpu.grid_nr : 1024, nt = in->gpu.grid_nt > 0 ? in->gpu.grid_nt : 1024;
+  if (nr < 2 || nt < 2 || (long long)nr * nt > (1ll << 28)) {
+    xmi_set_error("xmi_solid_angle_calculation: grid of %d x %d points out of range", nr, nt);
     return 0;
   }
   if (!ensure_device()) return 0;

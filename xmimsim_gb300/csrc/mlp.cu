@@ -1341,6 +1341,119 @@ int xmi_surrogate_apply(const void *p, int precision, const void *dev_bundles, i
   return cudaGetLastError() == cudaSuccess ? 1 : 0;
 }
 
+int xmi_gpu_surrogate_eval(xmi_inputFPtr in, int n, const double *r, const double *theta, double *omega,
+                           int *source) {
+  using namespace xmi::mlp;
+  if (!in || !in->surrogate || n < 0 || (n > 0 && (!r || !theta || !omega || !source))) {
+    xmi_set_error("xmi_gpu_surrogate_eval: no trained surrogate or bad arguments");
+    return 0;
+  }
+  if (n == 0) return 1;
+  if (!surrogate_device_ok()) return 0;
+  const SurrogateState *sg = (const SurrogateState *)in->surrogate;
+  /* where each point is served: decided on the host with the network's own
+   * cell map; the network runs on every point (one batched forward) */
+  std::vector<float> feat(3 * (size_t)n), pred(n);
+  std::vector<int> cell_of(n);
+  std::vector<unsigned char> flags(sg->dom.ncr * sg->dom.nct);
+  std::vector<int> patch_of(flags.size());
+  for (int i = 0; i < n; i++) {
+    bool inside;
+    features_of(sg->dom, r[i], theta[i], &feat[3 * (size_t)i], inside, cell_of[i]);
+    source[i] = !(theta[i] >= (double)sg->dom.tmin) ? 3 : (!inside ? 2 : 0);
+  }
+  float *feat_d = nullptr, *pred_d = nullptr;
+  int *err_d = nullptr;
+  bool ok = cudaMalloc(&feat_d, sizeof(float) * 3 * (size_t)n) == cudaSuccess &&
+            cudaMalloc(&pred_d, sizeof(float) * (size_t)n) == cudaSuccess &&
+            cudaMalloc(&err_d, sizeof(int)) == cudaSuccess;
+  std::vector<float> patches;
+  if (ok) {
+    cudaMemcpy(feat_d, feat.data(), sizeof(float) * 3 * (size_t)n, cudaMemcpyHostToDevice);
+    cudaMemset(err_d, 0, sizeof(int));
+    ok = device_forward(*sg, feat_d, pred_d, n, err_d);
+    int h_err = 0;
+    if (ok) {
+      cudaMemcpy(&h_err, err_d, sizeof(int), cudaMemcpyDeviceToHost);
+      cudaMemcpy(pred.data(), pred_d, sizeof(float) * (size_t)n, cudaMemcpyDeviceToHost);
+      cudaMemcpy(flags.data(), sg->flags_d, flags.size(), cudaMemcpyDeviceToHost);
+      cudaMemcpy(patch_of.data(), sg->patch_of_d, sizeof(int) * patch_of.size(), cudaMemcpyDeviceToHost);
+      patches.resize((size_t)(sg->n_patch > 0 ? sg->n_patch : 1) * kPatchNodes);
+      if (sg->n_patch > 0)
+        cudaMemcpy(patches.data(), sg->patches_d, sizeof(float) * (size_t)sg->n_patch * kPatchNodes,
+                   cudaMemcpyDeviceToHost);
+      ok = cudaGetLastError() == cudaSuccess;
+    }
+    if (h_err) {
+      xmi_set_error("xmi_gpu_surrogate_eval: tensor-core wait ran out");
+      ok = false;
+    }
+  }
+  cudaFree(feat_d);
+  cudaFree(pred_d);
+  cudaFree(err_d);
+  if (!ok) {
+    if (!*xmi_gpu_last_error()) xmi_set_error("xmi_gpu_surrogate_eval: CUDA error");
+    return 0;
+  }
+  /* the same choices as omega_kernel (the host exponential in place of the
+   * device's fast one: they differ by about 1e-6 relative) */
+  for (int i = 0; i < n; i++) {
+    if (source[i] == 3) {
+      omega[i] = 0.0;
+    } else if (source[i] == 2) {
+      omega[i] = -1.0;
+    } else if (flags[cell_of[i]]) {
+      const int pc = patch_of[cell_of[i]];
+      if (pc >= 0) {
+        source[i] = 1;
+        omega[i] = patch_omega(sg->dom, patches.data() + (size_t)pc * kPatchNodes, logf((float)r[i]),
+                               (float)theta[i], cell_of[i]);
+      } else {
+        source[i] = 2;
+        omega[i] = -1.0;
+      }
+    } else {
+      const float o = expf(pred[i]) - sg->dom.eps;
+      omega[i] = o > 0.0f ? o : 0.0f;
+    }
+  }
+  return 1;
+}
+
+int xmi_gpu_solid_angle_points(xmi_inputFPtr in, int n, const double *r, const double *theta, int hits,
+                               int precision, unsigned long long seed, double *omega) {
+  if (!in || !in->initialized || n < 0 || hits < 1 || (n > 0 && (!r || !theta || !omega))) {
+    xmi_set_error("xmi_gpu_solid_angle_points: bad arguments");
+    return 0;
+  }
+  if (n == 0) return 1;
+  if (!surrogate_device_ok()) return 0;
+  const xmi::SaGeom geom{in->det_radius, in->coll_radius, in->coll_height, in->coll_present};
+  double *r_d = nullptr, *t_d = nullptr, *o_d = nullptr;
+  bool ok = cudaMalloc(&r_d, sizeof(double) * (size_t)n) == cudaSuccess &&
+            cudaMalloc(&t_d, sizeof(double) * (size_t)n) == cudaSuccess &&
+            cudaMalloc(&o_d, sizeof(double) * (size_t)n) == cudaSuccess;
+  if (ok) {
+    cudaMemcpy(r_d, r, sizeof(double) * (size_t)n, cudaMemcpyHostToDevice);
+    cudaMemcpy(t_d, theta, sizeof(double) * (size_t)n, cudaMemcpyHostToDevice);
+    int dev = 0, sms = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (precision == 0)
+      xmi::solid_angle_points_kernel<double><<<sms * 8, 256>>>(geom, r_d, t_d, n, hits, seed, o_d);
+    else
+      xmi::solid_angle_points_kernel<float><<<sms * 8, 256>>>(geom, r_d, t_d, n, hits, seed, o_d);
+    ok = cudaGetLastError() == cudaSuccess && cudaDeviceSynchronize() == cudaSuccess &&
+         cudaMemcpy(omega, o_d, sizeof(double) * (size_t)n, cudaMemcpyDeviceToHost) == cudaSuccess;
+  }
+  cudaFree(r_d);
+  cudaFree(t_d);
+  cudaFree(o_d);
+  if (!ok) xmi_set_error("xmi_gpu_solid_angle_points: CUDA error");
+  return ok ? 1 : 0;
+}
+
 int xmi_gpu_surrogate_report(xmi_inputFPtr in, double *report) {
   if (!in || !in->surrogate || !report) return 0;
   const SurrogateState *sg = (const SurrogateState *)in->surrogate;

@@ -41,8 +41,7 @@ __device__ __forceinline__ bool sa_setup(const SaGeom &s, R r1, R theta1, R &cfc
     if (r1 * cos(theta1) <= detr) {
       r = r1; theta = theta1; fcbr = detr;
     } else {
-      r = sqrt(r1 * r1 - (R)2.0 * r1 * sin(theta1) * collh + collh * collh);
-      theta = acos(r1 * cos(theta1) / r);
+      sa_opening<R>(r1, theta1, collh, r, theta);
       fcbr = collr;
     }
     outside = r1 * sin(theta1) > collh;
@@ -52,8 +51,7 @@ __device__ __forceinline__ bool sa_setup(const SaGeom &s, R r1, R theta1, R &cfc
     } else if (r1 * sin(theta1) <= collh) {
       return false;
     } else {
-      r = sqrt(r1 * r1 - (R)2.0 * r1 * sin(theta1) * collh + collh * collh);
-      theta = acos(r1 * cos(theta1) / r);
+      sa_opening<R>(r1, theta1, collh, r, theta);
       fcbr = collr;
     }
     outside = r1 * sin(theta1) > collh;

@@ -375,6 +375,27 @@ __device__ __forceinline__ void tally_channel(const DevBundle<R> &b, const DevTa
 }
 
 /* ---------------- solid angle ---------------- */
+/* distance and angle of a point to the collimator's opening: the reference
+ * computes r = sqrt(r1^2 - 2 r1 sin(theta1) h + h^2) and theta =
+ * acos(r1 cos(theta1) / r).  In FP32 that difference cancels when the point
+ * lies near the height of the opening, and rounding can push the cosine
+ * above 1 (a NaN solid angle, seen on the collimated workload at 1e8
+ * photons); the FP32 engine uses the exact rewriting r^2 = py^2 + (pz - h)^2
+ * with py = r1 cos(theta1), pz = r1 sin(theta1), and theta = atan2(|pz - h|,
+ * py), which neither cancels nor leaves the cosine's range.  FP64 keeps the
+ * reference's arithmetic. */
+template <typename R>
+__device__ __forceinline__ void sa_opening(R r1, R theta1, R collh, R &r, R &theta) {
+  if constexpr (sizeof(R) == 4) {
+    const R py = r1 * cos(theta1), dz = fabs(r1 * sin(theta1) - collh);
+    r = sqrt(py * py + dz * dz);
+    theta = atan2(dz, py);
+  } else {
+    r = sqrt(r1 * r1 - (R)2.0 * r1 * sin(theta1) * collh + collh * collh);
+    theta = acos(r1 * cos(theta1) / r);
+  }
+}
+
 /* xmi_single_solid_angle_calculation (src/xmi_solid_angle_f.F90:432-710) */
 template <typename R>
 __device__ R single_solid_angle(const DevBundle<R> &b, R r1, R theta1, xmi_rng *g, int hits_per_single) {
@@ -387,8 +408,7 @@ __device__ R single_solid_angle(const DevBundle<R> &b, R r1, R theta1, xmi_rng *
     if (r1 * cos(theta1) <= detr) {
       r = r1; theta = theta1; fcbr = detr;
     } else {
-      r = sqrt(r1 * r1 - (R)2.0 * r1 * sin(theta1) * collh + collh * collh);
-      theta = acos(r1 * cos(theta1) / r);
+      sa_opening<R>(r1, theta1, collh, r, theta);
       fcbr = collr;
     }
     outside = r1 * sin(theta1) > collh;
@@ -398,8 +418,7 @@ __device__ R single_solid_angle(const DevBundle<R> &b, R r1, R theta1, xmi_rng *
     } else if (r1 * sin(theta1) <= collh) {
       return (R)0;
     } else {
-      r = sqrt(r1 * r1 - (R)2.0 * r1 * sin(theta1) * collh + collh * collh);
-      theta = acos(r1 * cos(theta1) / r);
+      sa_opening<R>(r1, theta1, collh, r, theta);
       fcbr = collr;
     }
     outside = r1 * sin(theta1) > collh;
@@ -433,6 +452,15 @@ __device__ R single_solid_angle(const DevBundle<R> &b, R r1, R theta1, xmi_rng *
   return fcsa * (R)hits / (R)hits_per_single;
 }
 
+/* a cosine computed from rounded unit vectors, kept in [-1, 1]: on the
+ * detector axis the dot product can round one ulp past 1, and acos would
+ * return NaN (the grid lookup turned that NaN into the axis end; the
+ * surrogate path would have served it a zero solid angle) */
+template <typename R>
+__device__ __forceinline__ R cos_clamp(R c) {
+  return c > (R)1 ? (R)1 : (c < (R)-1 ? (R)-1 : c);
+}
+
 /* (r, theta) of a point in the solid-angle grid's frame: distance to the
  * detector centre and the complement of the angle to the detector normal */
 template <typename R>
@@ -453,7 +481,7 @@ __device__ __forceinline__ void sa_coords(const DevBundle<R> &b, const double *c
     dn[0] = (R)(dv[0] * inv), dn[1] = (R)(dv[1] * inv), dn[2] = (R)(dv[2] * inv);
   }
   const R *nd = b.n_det_r;
-  R tt = acos(rdot(dn, nd));
+  R tt = acos(cos_clamp(rdot(dn, nd)));
   r = (R)rr;
   if (tt > (R)(kPi / 2.0)) tt = (R)kPi - tt;
   theta = (R)(kPi / 2.0) - tt;
@@ -477,7 +505,7 @@ __device__ R get_solid_angle(const DevBundle<R> &b, const double *coords, const 
     dn[0] = (R)(dv[0] * inv), dn[1] = (R)(dv[1] * inv), dn[2] = (R)(dv[2] * inv);
   }
   const R *nd = b.n_det_r;
-  R tt = acos(rdot(dn, nd));
+  R tt = acos(cos_clamp(rdot(dn, nd)));
   R r = (R)rr;
   if (tt > (R)(kPi / 2.0)) tt = (R)kPi - tt;
   R theta = (R)(kPi / 2.0) - tt;

@@ -140,12 +140,15 @@ def make_options(**kw) -> abi.XmiMainOptions:
 
 def gpu_options(precision: int = 0, seed: int = 0, threads_per_block: int = 0, blocks_per_sm: int = 0,
                 use_surrogate: int = 0, surrogate_tolerance: float = 1e-3,
-                solid_angle_stream: int = 0) -> abi.XmiGpuOptions:
+                solid_angle_stream: int = 0, grid_n: int = 0) -> abi.XmiGpuOptions:
+    """grid_n: points of the solid-angle grid along r and along theta (0: the
+    reference's 1024)."""
     g = abi.XmiGpuOptions()
     abi.load().xmi_gpu_default_options(C.byref(g))
     g.precision, g.seed, g.solid_angle_stream = precision, seed, solid_angle_stream
     g.threads_per_block, g.blocks_per_sm = threads_per_block, blocks_per_sm
     g.use_surrogate, g.surrogate_tolerance = use_surrogate, surrogate_tolerance
+    g.grid_nr = g.grid_nt = grid_n
     return g
 
 
@@ -357,6 +360,54 @@ class Simulation:
                "xmi_gpu_build_surrogate_points")
         keys = ("median_rel_err", "max_rel_err_kept", "flagged_fraction", "train_loss", "seconds", "cells")
         return dict(zip(keys, rep.tolist()))
+
+    def surrogate_eval(self, r: np.ndarray, theta: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
+        """(omega, source) the transport would take from the trained surrogate
+        at these points: source 0 network, 1 tabulated integrator of a flagged
+        cell, 2 outside the checked region (integrated per event; omega -1),
+        3 below the lowest theta (omega 0) -- xmi_gpu_surrogate_eval."""
+        r = np.ascontiguousarray(r, dtype=np.float64)
+        theta = np.ascontiguousarray(theta, dtype=np.float64)
+        om = np.zeros(len(r))
+        src = np.zeros(len(r), dtype=np.int32)
+        _check(self.lib.xmi_gpu_surrogate_eval(self.inputF, len(r), r.ctypes.data_as(abi.c_double_p),
+                                               theta.ctypes.data_as(abi.c_double_p), om.ctypes.data_as(abi.c_double_p),
+                                               src.ctypes.data_as(C.POINTER(C.c_int))), "xmi_gpu_surrogate_eval")
+        return om, src
+
+    def solid_angle_points(self, r: np.ndarray, theta: np.ndarray, hits: int, precision: int = 0,
+                           seed: int = 0x5EED0007) -> np.ndarray:
+        """The engine's solid-angle integrator at arbitrary (r, theta) points,
+        `hits` cone samples each (xmi_gpu_solid_angle_points)."""
+        r = np.ascontiguousarray(r, dtype=np.float64)
+        theta = np.ascontiguousarray(theta, dtype=np.float64)
+        om = np.zeros(len(r))
+        _check(self.lib.xmi_gpu_solid_angle_points(self.inputF, len(r), r.ctypes.data_as(abi.c_double_p),
+                                                   theta.ctypes.data_as(abi.c_double_p), hits, precision, seed,
+                                                   om.ctypes.data_as(abi.c_double_p)), "xmi_gpu_solid_angle_points")
+        return om
+
+    def validate_surrogate(self, r: np.ndarray, theta: np.ndarray, hits: int = 1 << 24,
+                           seed: int = 0x5EED0077) -> dict:
+        """Held-out check of the trained surrogate at points it was not
+        trained or checked on: the solid angle the transport would take
+        (surrogate_eval) against the integrator with `hits` samples per point
+        (FP32; its relative noise is sqrt((1 - p) / (p hits)) for a hit share
+        p).  Per source: points, median / RMS / 99th-percentile relative
+        error and the mean (bias)."""
+        om, src = self.surrogate_eval(r, theta)
+        truth = self.solid_angle_points(r, theta, hits=hits, precision=1, seed=seed)
+        out = {"points": int(len(r)), "hits": hits,
+               "share": {name: float((src == k).mean()) for k, name in
+                         enumerate(("network", "table", "integrator", "zero"))}}
+        for k, name in ((0, "network"), (1, "table")):
+            m = (src == k) & (truth > 0)
+            if m.any():
+                e = (om[m] - truth[m]) / truth[m]
+                out[name] = {"points": int(m.sum()), "median": float(np.median(np.abs(e))),
+                             "rms": float(np.sqrt((e ** 2).mean())), "p99": float(np.quantile(np.abs(e), 0.99)),
+                             "bias": float(e.mean())}
+        return out
 
     def share_surrogate(self, other: "Simulation") -> None:
         """Serves this configuration's solid angles from the network trained
