@@ -23,12 +23,22 @@ One step = one xmi_main_msim_batch call over all 512 configurations with
             the one-by-one transport is timed over all 512, the grid on a
             sample of them; both full jobs (all 16 steps, the network's
             training, every grid) are compared.
-  line_error -- surrogate + batched FP32 lines against the all-FP64 plain
-            run (own FP64 grid, same photon streams) on a few configurations.
+  line_error -- the surrogate + batched FP32 output of 32 configurations
+            (the 8 with the thinnest layer, the 8 with the heaviest element,
+            the rest spread over the budgets) against the all-FP64 plain run
+            of the same photons: every line's relative error, every line's
+            and every channel's z-score on the combined Monte Carlo standard
+            error (estimated from 8 disjoint photon ranges of the FP64 run).
 
 ``--workload plain``: the production-size plain configuration -- 5 random
 layers (seed 2) of 3-12 elements, Rh tube at 40 kV behind 125 um Be in 400
 intervals plus the Rh K/L lines, 6 interactions, one xmi_main_msim per step.
+
+``--workload precision``: the precision form of the small plain
+configuration (10 nm Cr and 50 nm Au over a 2 mm substrate, 1e8 photons per
+step), FP32 transport timed, with the error of every line and channel against
+the all-FP64 run of the same photons (relative error and z-score on the
+Monte Carlo standard error from disjoint photon ranges).
 
 ``--workload surrogate``: the learned solid-angle surrogate on its own
 geometry -- the small plain configuration behind a conical collimator
@@ -74,7 +84,7 @@ def parse():
     p.add_argument("--steps", type=int, default=3)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--workload", default="batched", choices=["batched", "plain", "surrogate"])
+    p.add_argument("--workload", default="batched", choices=["batched", "plain", "surrogate", "precision"])
     p.add_argument("--plain-mode", default="default", choices=["default", "advanced-compton", "analog"],
                    help="transport options of the plain workload")
     p.add_argument("--configs", type=int, default=512, help="configurations of the batched workload")
@@ -87,9 +97,12 @@ def parse():
     p.add_argument("--tune-share", type=float, default=1.0 / 32, help="share of a step the autotuner's trials run")
     p.add_argument("--queue-events", type=int, default=0,
                    help="skip the autotuner: default launch shape and this estimator queue size (small profiling runs)")
-    p.add_argument("--line-configs", type=int, default=3, help="configurations of the FP64 line-error check")
+    p.add_argument("--line-configs", type=int, default=32, help="configurations of the FP64 error statement")
+    p.add_argument("--replicas", type=int, default=8,
+                   help="disjoint photon ranges of the FP64 reference runs (their spread is the MC error)")
     p.add_argument("--no-plain", action="store_true")
     p.add_argument("--photons", type=float, default=1e7, help="photons per step of the plain workload")
+    p.add_argument("--photons-precision", type=float, default=1e8, help="photons per step of the precision workload")
     p.add_argument("--photons-surrogate", type=float, default=1e8,
                    help="photons per step of the surrogate workload")
     p.add_argument("--hits-train", type=int, default=1 << 14,
@@ -246,6 +259,10 @@ def cpu_sample_specs(args, rank=0):
         from xmimsim_gb300 import configs
         return [configs.config4(int(args.photons_surrogate))], dict(configs.C1_OPTIONS), \
             "the collimated surrogate workload"
+    if args.workload == "precision":
+        from xmimsim_gb300 import configs
+        return [configs.config3(int(args.photons_precision))], dict(configs.C1_OPTIONS), \
+            "the thin-layer precision workload"
     specs, options = batched_specs(args.configs, args.budget_scale, rank)
     pick = [specs[i] for i in range(0, len(specs), max(1, len(specs) // 8))][:8]
     return pick, options, "8 of the %d batched configurations" % len(specs)
@@ -279,7 +296,11 @@ def reference_arm(args):
 
 
 def workload_config(args, extra):
-    if args.workload == "surrogate":
+    if args.workload == "precision":
+        cfg = {"workload": "precision form of config 1: 10 nm Cr and 50 nm Au over a 2 mm substrate, FP32 transport "
+                           "and tables, FP64 positions and tallies, error statement against all-FP64",
+               "photons_per_step": int(args.photons_precision)}
+    elif args.workload == "surrogate":
         cfg = {"workload": "collimated config-1 geometry (conical collimator 1 cm high, 0.1 cm opening radius, "
                            "45/45 degrees, 10 cm), FP32 transport, solid angles from the surrogate network",
                "photons_per_step": int(args.photons_surrogate)}
@@ -376,6 +397,99 @@ def line_error(sur_out: dict, ref_out: dict, floor: float = 1e-2) -> dict:
             "median": float(np.median(rel)) if m.any() else 0.0,
             "within_0.5pct": float((rel <= 5e-3).mean()) if m.any() else 1.0,
             "total": float(abs(a.sum() - b.sum()) / b.sum()) if b.sum() > 0 else 0.0}
+
+
+def replica_runs(sim, k_rep: int):
+    """The run as k_rep disjoint photon ranges (xmi_gpu_set_replica, each with
+    the full budget's weights): their sum is the full run and their spread
+    its Monte Carlo error.  Returns (lines [k, 100, 385, N], channels
+    [k, N + 1, nch])."""
+    import numpy as np
+    lines, chans = [], []
+    for k in range(k_rep):
+        sim.set_replica(k, k_rep)
+        o = sim.msim()
+        lines.append(o["var_red"].copy())
+        chans.append(o["channels"].copy())
+        sim.free_raw(o)
+    sim.set_replica(0, 1)
+    return np.array(lines), np.array(chans)
+
+
+def error_statement(out32: dict, reps64: tuple, strong: float = 1e-3) -> dict:
+    """Error of an FP32 run against the all-FP64 run of the same photons, for
+    every line and every channel.  reps64: the FP64 run as k replicas
+    (replica_runs); its sum is the reference and k times the variance of the
+    replicas its Monte Carlo variance.  The combined standard error of two
+    independent runs of this size is sqrt(2) sigma_64; z = (FP32 - FP64) /
+    that.  Lines are summed over orders; channels are every order's spectrum
+    (cumulative rows 1..N).  The lines and channels furthest from the FP64
+    run (in sigma) are listed."""
+    import numpy as np
+    l64k, c64k = reps64
+    k = l64k.shape[0]
+    a = out32["var_red"].sum(axis=2)
+    lk = l64k.sum(axis=3)
+    b, sb = lk.sum(axis=0), np.sqrt(k * lk.var(axis=0, ddof=1))
+    if not (np.isfinite(a).all() and np.isfinite(b).all()):
+        return {"nonfinite": int((~np.isfinite(a)).sum() + (~np.isfinite(b)).sum())}
+    m = b > 0
+    rel = np.abs(a[m] - b[m]) / b[m]
+    st = (b >= strong * b.max())[m]
+    zm = m & (sb > 0)
+    z = (a[zm] - b[zm]) / (np.sqrt(2.0) * sb[zm])
+    ca = out32["channels"][1:]
+    cb, scb = c64k.sum(axis=0)[1:], np.sqrt(k * c64k.var(axis=0, ddof=1))[1:]
+    cm = scb > 0
+    zc = (ca[cm] - cb[cm]) / (np.sqrt(2.0) * scb[cm])
+    zl = np.zeros_like(b)
+    zl[zm] = z
+    worst_l = []
+    for flat in np.argsort(-np.abs(zl).ravel())[:4]:
+        zi, li = np.unravel_index(flat, b.shape)
+        if zl[zi, li] != 0:
+            worst_l.append({"Z": int(zi + 1), "line": int(li + 1), "fp64": float(b[zi, li]),
+                            "rel": float((a[zi, li] - b[zi, li]) / b[zi, li]), "z": float(zl[zi, li]),
+                            "sigma_rel": float(sb[zi, li] / b[zi, li]), "share": float(b[zi, li] / b.max())})
+    zcf = np.zeros_like(cb)
+    zcf[cm] = zc
+    worst_c = []
+    for flat in np.argsort(-np.abs(zcf).ravel())[:4]:
+        oi, ci = np.unravel_index(flat, cb.shape)
+        if zcf[oi, ci] != 0:
+            worst_c.append({"order": int(oi + 1), "channel": int(ci), "fp64": float(cb[oi, ci]),
+                            "rel": float((ca[oi, ci] - cb[oi, ci]) / cb[oi, ci]) if cb[oi, ci] else None,
+                            "z": float(zcf[oi, ci]),
+                            "sigma_rel": float(scb[oi, ci] / abs(cb[oi, ci])) if cb[oi, ci] else None})
+    return {"lines": int(m.sum()), "lines_max_rel": float(rel.max()) if m.any() else 0.0,
+            "lines_median_rel": float(np.median(rel)) if m.any() else 0.0,
+            "lines_within_0.5pct": float((rel <= 5e-3).mean()) if m.any() else 1.0,
+            "strong_lines": int(st.sum()), "strong_max_rel": float(rel[st].max()) if st.any() else 0.0,
+            "strong_within_0.5pct": float((rel[st] <= 5e-3).mean()) if st.any() else 1.0,
+            "lines_with_sigma": int(zm.sum()),
+            "lines_within_3sigma": float((np.abs(z) <= 3).mean()) if len(z) else 1.0,
+            "lines_max_abs_z": float(np.abs(z).max()) if len(z) else 0.0,
+            "channels_with_sigma": int(cm.sum()),
+            "channels_within_3sigma": float((np.abs(zc) <= 3).mean()) if len(zc) else 1.0,
+            "channels_max_abs_z": float(np.abs(zc).max()) if len(zc) else 0.0,
+            "total_rel": float(abs(a.sum() - b.sum()) / b.sum()) if b.sum() > 0 else 0.0,
+            "replicas": int(k), "worst_lines": worst_l, "worst_channels": worst_c}
+
+
+def merge_statements(parts: list[dict]) -> dict:
+    """Worst case (max) and pooled fractions of several error statements."""
+    parts = [p for p in parts if "lines" in p]
+    if not parts:
+        return {}
+    out = {"configs": len(parts)}
+    for key in ("lines_max_rel", "strong_max_rel", "lines_max_abs_z", "channels_max_abs_z", "total_rel"):
+        out[key] = max(p[key] for p in parts)
+    for frac, count in (("lines_within_0.5pct", "lines"), ("strong_within_0.5pct", "strong_lines"),
+                        ("lines_within_3sigma", "lines_with_sigma"), ("channels_within_3sigma", "channels_with_sigma")):
+        n = sum(p[count] for p in parts)
+        out[frac] = sum(p[frac] * p[count] for p in parts) / n if n else 1.0
+        out[count] = n
+    return out
 
 
 def batched_arm(args, ws, rank, local):
@@ -480,20 +594,42 @@ def batched_arm(args, ws, rank, local):
             s.set_gpu(g_sur)
 
     if args.line_configs > 0 and "outs" in last:
-        # all-FP64 plain runs (own FP64 grid, same seed) of a few configurations
-        errs = []
-        order = sorted(range(len(specs)), key=lambda i: histories(specs[i]))
-        pick = [order[len(order) * (k + 1) // (args.line_configs + 1)] for k in range(args.line_configs)]
+        # the all-FP64 plain run (FP64 transport on an FP64 grid, same photon
+        # streams) of line_configs configurations: the 8 with the thinnest
+        # layer, the 8 with the heaviest element and the rest spread over the
+        # budgets; each as args.replicas disjoint photon ranges for its
+        # Monte Carlo error
+        t0 = time.perf_counter()
+        by_thin = sorted(range(len(specs)), key=lambda i: min(l.thickness for l in specs[i].layers))
+        by_heavy = sorted(range(len(specs)), key=lambda i: -max(max(l.Z) for l in specs[i].layers))
+        by_budget = sorted(range(len(specs)), key=lambda i: histories(specs[i]))
+        pick = []
+        for i in by_thin[:8] + by_heavy[:8]:
+            if i not in pick:
+                pick.append(i)
+        n_spread = max(0, args.line_configs - len(pick))
+        for k in range(n_spread):
+            i = by_budget[len(by_budget) * (2 * k + 1) // (2 * n_spread)]
+            if i not in pick:
+                pick.append(i)
+        g64 = gpu_options(precision=0, seed=seed)
+        gd = Simulation(specs[deep], options=options, gpu=g64)
+        ax64 = gd.solid_angle_grid()
+        gd.close()
+        parts = []
         for i in pick:
-            ref = Simulation(specs[i], options=options, gpu=gpu_options(precision=0, seed=seed))
-            r = ref.msim()
-            e = line_error(last["outs"][i], r)
-            e.update(config=int(i), photons=histories(specs[i]))
-            errs.append(e)
-            ref.free_raw(r)
+            ref = Simulation(specs[i], options=options, gpu=g64)
+            ref.set_solid_angle(ax64["r"], ax64["theta"], ax64["grid"])
+            e = error_statement(last["outs"][i], replica_runs(ref, args.replicas))
+            e.update(config=int(i), photons=histories(specs[i]),
+                     thinnest_cm=min(l.thickness for l in specs[i].layers),
+                     heaviest_Z=max(max(l.Z) for l in specs[i].layers))
+            parts.append(e)
             ref.close()
-        line["line_error"] = {"reference": "all-FP64 plain GPU run, own FP64 grid, same photon streams",
-                              "lines": "lines with >= 1% of the configuration's strongest", "configs": errs}
+        line["line_error"] = {"reference": "all-FP64 plain GPU run (FP64 transport, FP64 grid of the deepest "
+                                           "sample), same photon streams",
+                              "summary": merge_statements(parts), "configs": parts,
+                              "wall_s": time.perf_counter() - t0}
     if "outs" in last:
         for s, o in zip(sims, last["outs"]):
             s.free_raw(o)
@@ -583,6 +719,55 @@ def plain_arm(args, ws, rank, local):
             "e2e": {"value": n_hist * args.steps / wall, "unit": "histories/s",
                     "h2d_bytes_per_step": int(statistics.mean(t["h2d_bytes"] for t in tms)),
                     "d2h_bytes_per_step": int(statistics.mean(t["d2h_bytes"] for t in tms))},
+            "clocks": clocks}
+    return line, [sim], [spec], options
+
+
+def precision_arm(args, ws, rank, local):
+    """The precision workload: thin layers (10 nm Cr, 50 nm Au) over a 2 mm
+    substrate in the config-1 geometry, FP32 transport timed, and its error
+    statement against the all-FP64 run of the same photons (same FP64 grid)."""
+    from xmimsim_gb300 import Simulation, configs, gpu_options
+    spec = configs.config3(n_photons_line=int(args.photons_precision))
+    options = dict(configs.C1_OPTIONS)
+    seed = 0x5EED0003 + rank
+    n_hist = histories(spec)
+    g64 = gpu_options(precision=0, seed=seed)
+    ref = Simulation(spec, options=options, gpu=g64)
+    ax = ref.solid_angle_grid()
+    sim = Simulation(spec, options=options, gpu=gpu_options(precision=1, seed=seed))
+    sim.set_solid_angle(ax["r"], ax["theta"], ax["grid"])
+    last = {}
+
+    def step():
+        out = sim.msim()
+        tm = sim.timing()
+        if "out" in last:
+            sim.free_raw(last["out"])
+        last["out"] = out
+        return tm
+
+    tms, wall, clocks = timed_steps(args, step, local)
+    ksum = sum(t["kernel_ms"] for t in tms)
+    t0 = time.perf_counter()
+    err = error_statement(last["out"], replica_runs(ref, args.replicas))
+    ref_s = time.perf_counter() - t0
+    sim.free_raw(last["out"])
+    ref.close()
+    line = {"metric": PLAIN_METRIC + " (FP32 transport, thin layers)", "value": n_hist * args.steps / (ksum / 1e3),
+            "unit": "histories/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ksum / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 transport, f64 tallies", "data": "synthetic (config-1 sample under 10 nm Cr and 50 nm Au)",
+            "config": workload_config(args, {"layers_cm": [l.thickness for l in spec.layers]}),
+            "gpu_launches": sum(t["launches"] for t in tms),
+            "phases_ms_per_step": {k: statistics.mean(t[k + "_ms"] for t in tms)
+                                   for k in ("transport", "sort", "estimator")},
+            "events_per_step": statistics.mean(t["events"] for t in tms),
+            "e2e": {"value": n_hist * args.steps / wall, "unit": "histories/s",
+                    "h2d_bytes_per_step": int(statistics.mean(t["h2d_bytes"] for t in tms)),
+                    "d2h_bytes_per_step": int(statistics.mean(t["d2h_bytes"] for t in tms))},
+            "error_vs_fp64": dict(err, reference="all-FP64 run of the same photons and grid, %d replicas (%.1f s)"
+                                  % (args.replicas, ref_s)),
             "clocks": clocks}
     return line, [sim], [spec], options
 
@@ -698,7 +883,8 @@ def main():
             cudart.cudaSetDevice(local)
     from xmimsim_gb300.build import build_all
     build_all()
-    arm = {"batched": batched_arm, "plain": plain_arm, "surrogate": surrogate_arm}[args.workload]
+    arm = {"batched": batched_arm, "plain": plain_arm, "surrogate": surrogate_arm,
+           "precision": precision_arm}[args.workload]
     line, sims, specs, options = arm(args, ws, rank, local)
     if ws > 1:
         import torch

@@ -150,6 +150,15 @@ __device__ __forceinline__ bool plane_walk_init(const double *p, const R *d, con
   return true;
 }
 
+/* moves point c along the unit sample normal n so that its height c . n
+ * becomes h (FP64) */
+__device__ __forceinline__ void set_height(double *c, const double *n, double h) {
+  const double dh = h - (c[0] * n[0] + c[1] * n[1] + c[2] * n[2]);
+  c[0] += dh * n[0];
+  c[1] += dh * n[1];
+  c[2] += dh * n[2];
+}
+
 /* signed parametric step to boundary plane zp; the walk moves onto it */
 __device__ __forceinline__ double plane_walk(PlaneWalk &w, double zp, const double *n) {
   const double P = zp * n[2];
@@ -1422,6 +1431,9 @@ __device__ int step_photon(const DevBundle<R> &b, Photon<R> &p, const DevTally &
       double ip[3];
 #pragma unroll
       for (int q = 0; q < 3; q++) ip[q] = sw * (double)p.d[q] + p.c[q];
+      /* FP32: the step's 1/cos is FP32, so the crossing point's height is
+       * set to the plane's exactly (see the forced step below) */
+      if constexpr (sizeof(R) == 4) set_height(ip, b.n_sample, (up ? b.zend[j] : b.zbeg[j]) * b.n_sample[2]);
       R tp = (R)-1 * (R)dd * b.rho[j] * p.mus[j];
       R tempexp = exp(tp);
       minr = maxr;
@@ -1475,13 +1487,14 @@ __device__ int step_photon(const DevBundle<R> &b, Photon<R> &p, const DevTally &
     if (b.escape_mode == 1) p.we = p.w;
     R negln = (R)-1 * log1p((R)-1 * R0 * pabs2);
     int my_index = cur;
-    R my_sum = (R)0;
+    R my_sum = (R)0, sum_before = (R)0;
     bool found = false;
     layers_in_direction(up, [&](int j) {
       bool active = up ? (j >= cur && j < b.n_layers) : (j <= cur);
       if (active && !found) {
+        const R prev = my_sum;
         my_sum = my_sum + p.mus[j] * b.rho[j] * dist[j];
-        if (my_sum > negln) { my_index = j; found = true; }
+        if (my_sum > negln) { my_index = j; found = true; sum_before = prev; }
       }
     });
     R mr_sel = (R)0;
@@ -1495,8 +1508,24 @@ __device__ int step_photon(const DevBundle<R> &b, Photon<R> &p, const DevTally &
     });
     temp_sum = temp_sum - (R)1 * log1p((R)-1 * R0 * pabs2) / mr_sel;
     if (!XMI_CHK(my_index, b.n_layers, 41)) return kStepError;
+    const double h0 = pw.h;
 #pragma unroll
     for (int q = 0; q < 3; q++) p.c[q] = p.c[q] + (double)temp_sum * (double)p.d[q];
+    if constexpr (sizeof(R) == 4) {
+      /* FP32: after centimetres of air the step's rounding is a few nm, the
+       * same for every photon of a pencil beam -- a systematic shift of all
+       * interaction depths, which biased lines absorbed within ~0.1 um of a
+       * surface (Au M lines: -2% behind 5 cm of air).  The height along the
+       * normal, which every escape path depends on, is therefore set in FP64:
+       * the entry plane of the selected layer (or the current height when
+       * the photon stays in its layer) plus the depth into that layer. */
+      const R into = (negln - (found ? sum_before : (R)0)) / mr_sel;
+      const double h_in = (my_index == cur || !found) ? h0 : (up ? b.zbeg[my_index] : b.zend[my_index]) * b.n_sample[2];
+      const double hb = b.zbeg[my_index] * b.n_sample[2], he = b.zend[my_index] * b.n_sample[2];
+      double h = h_in + (double)(into * rdot(p.d, b.n_sample_r));
+      h = h < hb ? hb : (h > he ? he : h);
+      set_height(p.c, b.n_sample, h);
+    }
     p.inside = 1;
     p.layer = my_index;
   }
