@@ -416,15 +416,24 @@ def replica_runs(sim, k_rep: int):
     return np.array(lines), np.array(chans)
 
 
-def error_statement(out32: dict, reps64: tuple, strong: float = 1e-3) -> dict:
+def error_statement(out32: dict, reps64: tuple, strong: float = 1e-3, floor: float = 1e-9) -> dict:
     """Error of an FP32 run against the all-FP64 run of the same photons, for
     every line and every channel.  reps64: the FP64 run as k replicas
     (replica_runs); its sum is the reference and k times the variance of the
     replicas its Monte Carlo variance.  The combined standard error of two
     independent runs of this size is sqrt(2) sigma_64; z = (FP32 - FP64) /
     that.  Lines are summed over orders; channels are every order's spectrum
-    (cumulative rows 1..N).  The lines and channels furthest from the FP64
-    run (in sigma) are listed."""
+    (cumulative rows 1..N).
+
+    The relative and z statistics cover the resolved entries: lines at least
+    `floor` of the strongest line, channels at least `floor` of their order's
+    largest channel.  Below that an entry is no measurable signal (FP32
+    underflows the attenuation of lines 1e-40 below the strongest, and a
+    single event that takes another Compton energy in FP32 than in FP64 can
+    dominate a channel that holds 1e-12 of the spectrum); those are counted,
+    and every entry's absolute difference is given relative to the strongest
+    line / channel.  The entries furthest from the FP64 run in sigma are
+    listed."""
     import numpy as np
     l64k, c64k = reps64
     k = l64k.shape[0]
@@ -433,35 +442,37 @@ def error_statement(out32: dict, reps64: tuple, strong: float = 1e-3) -> dict:
     b, sb = lk.sum(axis=0), np.sqrt(k * lk.var(axis=0, ddof=1))
     if not (np.isfinite(a).all() and np.isfinite(b).all()):
         return {"nonfinite": int((~np.isfinite(a)).sum() + (~np.isfinite(b)).sum())}
-    m = b > 0
+    bmax = b.max() if b.max() > 0 else 1.0
+    m = b >= floor * bmax
     rel = np.abs(a[m] - b[m]) / b[m]
-    st = (b >= strong * b.max())[m]
+    st = (b >= strong * bmax)[m]
     zm = m & (sb > 0)
     z = (a[zm] - b[zm]) / (np.sqrt(2.0) * sb[zm])
     ca = out32["channels"][1:]
     cb, scb = c64k.sum(axis=0)[1:], np.sqrt(k * c64k.var(axis=0, ddof=1))[1:]
-    cm = scb > 0
+    cmax = np.maximum(np.abs(cb).max(axis=1, keepdims=True), 1e-300)
+    cm = (scb > 0) & (np.abs(cb) >= floor * cmax)
     zc = (ca[cm] - cb[cm]) / (np.sqrt(2.0) * scb[cm])
     zl = np.zeros_like(b)
     zl[zm] = z
     worst_l = []
-    for flat in np.argsort(-np.abs(zl).ravel())[:4]:
+    for flat in np.argsort(-np.abs(zl).ravel())[:3]:
         zi, li = np.unravel_index(flat, b.shape)
         if zl[zi, li] != 0:
             worst_l.append({"Z": int(zi + 1), "line": int(li + 1), "fp64": float(b[zi, li]),
                             "rel": float((a[zi, li] - b[zi, li]) / b[zi, li]), "z": float(zl[zi, li]),
-                            "sigma_rel": float(sb[zi, li] / b[zi, li]), "share": float(b[zi, li] / b.max())})
+                            "sigma_rel": float(sb[zi, li] / b[zi, li]), "share": float(b[zi, li] / bmax)})
     zcf = np.zeros_like(cb)
     zcf[cm] = zc
     worst_c = []
-    for flat in np.argsort(-np.abs(zcf).ravel())[:4]:
+    for flat in np.argsort(-np.abs(zcf).ravel())[:3]:
         oi, ci = np.unravel_index(flat, cb.shape)
         if zcf[oi, ci] != 0:
             worst_c.append({"order": int(oi + 1), "channel": int(ci), "fp64": float(cb[oi, ci]),
-                            "rel": float((ca[oi, ci] - cb[oi, ci]) / cb[oi, ci]) if cb[oi, ci] else None,
-                            "z": float(zcf[oi, ci]),
-                            "sigma_rel": float(scb[oi, ci] / abs(cb[oi, ci])) if cb[oi, ci] else None})
-    return {"lines": int(m.sum()), "lines_max_rel": float(rel.max()) if m.any() else 0.0,
+                            "rel": float((ca[oi, ci] - cb[oi, ci]) / cb[oi, ci]), "z": float(zcf[oi, ci]),
+                            "sigma_rel": float(scb[oi, ci] / abs(cb[oi, ci]))})
+    return {"lines": int(m.sum()), "lines_unresolved": int(((b > 0) & ~m).sum()),
+            "lines_max_rel": float(rel.max()) if m.any() else 0.0,
             "lines_median_rel": float(np.median(rel)) if m.any() else 0.0,
             "lines_within_0.5pct": float((rel <= 5e-3).mean()) if m.any() else 1.0,
             "strong_lines": int(st.sum()), "strong_max_rel": float(rel[st].max()) if st.any() else 0.0,
@@ -469,11 +480,14 @@ def error_statement(out32: dict, reps64: tuple, strong: float = 1e-3) -> dict:
             "lines_with_sigma": int(zm.sum()),
             "lines_within_3sigma": float((np.abs(z) <= 3).mean()) if len(z) else 1.0,
             "lines_max_abs_z": float(np.abs(z).max()) if len(z) else 0.0,
+            "lines_max_abs_diff_over_strongest": float(np.abs(a - b).max() / bmax),
             "channels_with_sigma": int(cm.sum()),
+            "channels_unresolved": int(((scb > 0) & ~cm).sum()),
             "channels_within_3sigma": float((np.abs(zc) <= 3).mean()) if len(zc) else 1.0,
             "channels_max_abs_z": float(np.abs(zc).max()) if len(zc) else 0.0,
+            "channels_max_abs_diff_over_max": float((np.abs(ca - cb) / cmax).max()),
             "total_rel": float(abs(a.sum() - b.sum()) / b.sum()) if b.sum() > 0 else 0.0,
-            "replicas": int(k), "worst_lines": worst_l, "worst_channels": worst_c}
+            "floor": floor, "replicas": int(k), "worst_lines": worst_l, "worst_channels": worst_c}
 
 
 def merge_statements(parts: list[dict]) -> dict:
@@ -482,8 +496,11 @@ def merge_statements(parts: list[dict]) -> dict:
     if not parts:
         return {}
     out = {"configs": len(parts)}
-    for key in ("lines_max_rel", "strong_max_rel", "lines_max_abs_z", "channels_max_abs_z", "total_rel"):
+    for key in ("lines_max_rel", "strong_max_rel", "lines_max_abs_z", "channels_max_abs_z", "total_rel",
+                "lines_max_abs_diff_over_strongest", "channels_max_abs_diff_over_max"):
         out[key] = max(p[key] for p in parts)
+    for key in ("lines_unresolved", "channels_unresolved"):
+        out[key] = sum(p[key] for p in parts)
     for frac, count in (("lines_within_0.5pct", "lines"), ("strong_within_0.5pct", "strong_lines"),
                         ("lines_within_3sigma", "lines_with_sigma"), ("channels_within_3sigma", "channels_with_sigma")):
         n = sum(p[count] for p in parts)
