@@ -57,7 +57,9 @@ no data-path collective).
 ``--impl reference`` times the reference algorithm's CPU path: the FP64 C
 restatement under oracle/ (the reference's Fortran build needs gfortran and
 xraylib, absent here) with all host threads, each step a bounded sample of
-the same workload.
+the same workload: every configuration of the sweep, each source item
+running the same share of its photons (1e6 photons in all by default), one
+call per configuration as the reference runs them.
 """
 from __future__ import annotations
 
@@ -111,7 +113,8 @@ def parse():
     p.add_argument("--n-train-surrogate", type=int, default=2_000_000,
                    help="training points of the surrogate workload (uniform over the sample volume)")
     p.add_argument("--precision", default="fp32", choices=["fp64", "fp32"])
-    p.add_argument("--cpu-sample", type=int, default=100000, help="photons of the CPU-baseline sample")
+    p.add_argument("--cpu-sample", type=int, default=1000000,
+                   help="photons of the CPU-baseline sample (spread over all configurations by budget)")
     p.add_argument("--no-cpu-baseline", action="store_true")
     return p.parse_args()
 
@@ -216,39 +219,63 @@ def total_thickness(spec) -> float:
 # --------------------------------------------------------------------------
 # CPU baseline (the oracle: FP64 restatement of the reference's algorithm)
 # --------------------------------------------------------------------------
-def run_cpu_sample(specs, options, n_sample: int, threads: int):
-    """Times the FP64 CPU restatement (all threads) on a bounded sample of the
-    workload: about n_sample photons spread over the given configurations.
-    Returns (histories/s, histories, seconds, words/history of transport,
-    words/history of the estimator loops)."""
-    from oracle import oracle_api
-    from xmimsim_gb300 import Simulation, gpu_options
-    import numpy as np
-    n_hist, dt, words_tr, words_est = 0, 0.0, 0, 0
-    per_cfg = max(1, n_sample // len(specs))
-    for spec in specs:
-        n_items = len(spec.discrete) + max(0, len(spec.continuous) - 1)
-        per_item = max(1, per_cfg // max(1, n_items))
-        sim = Simulation(spec, options=options, gpu=gpu_options(seed=0x5EED0001))
-        # the CPU path uses a coarse grid over the same axes, built here (untimed) so that no GPU is needed
-        r, t = sim.grid_axes(64, 64)
-        sim.set_solid_angle(r, t, np.zeros((64, 64)))
-        sim.prepare()
-        g = oracle_api.solid_angle_points(sim.bundle_ptr(), r, t, 0, 64 * 64, 500).reshape(64, 64)
-        sim.set_solid_angle(r, t, g)
-        sim.prepare()
-        oracle_api.words_counted_split()
-        t0 = time.perf_counter()
-        oracle_api.msim(sim.bundle_ptr(), spec.n_interactions_trajectory, spec.nchannels, threads=threads,
+class CpuSample:
+    """The FP64 CPU restatement (all threads) on a bounded, budget-weighted
+    sample of a workload: every configuration runs the same share of each of
+    its source items' photons (about n_sample photons in all), so the sample
+    has the workload's own mix of configurations.  The set-up (tables, and a
+    coarse 64 x 64 solid-angle grid of 500 samples per point built by the
+    CPU integrator so that no GPU is needed) is done once and not timed."""
+
+    def __init__(self, specs, options, n_sample: int):
+        from oracle import oracle_api
+        from xmimsim_gb300 import Simulation, gpu_options
+        import numpy as np
+        self.O = oracle_api
+        total = sum(histories(sp) for sp in specs)
+        self.share = min(1.0, n_sample / max(1, total))
+        self.sims, self.items = [], []
+        for spec in specs:
+            sim = Simulation(spec, options=options, gpu=gpu_options(seed=0x5EED0001))
+            r, t = sim.grid_axes(64, 64)
+            sim.set_solid_angle(r, t, np.zeros((64, 64)))
+            sim.prepare()
+            g = oracle_api.solid_angle_points(sim.bundle_ptr(), r, t, 0, 64 * 64, 500).reshape(64, 64)
+            sim.set_solid_angle(r, t, g)
+            sim.prepare()
+            per_item = max(1, int(round(max(int(spec.n_photons_line), int(spec.n_photons_interval)) * self.share)))
+            n = min(per_item, int(spec.n_photons_line)) * len(spec.discrete) + \
+                min(per_item, int(spec.n_photons_interval)) * max(0, len(spec.continuous) - 1)
+            self.sims.append(sim)
+            self.items.append((spec, per_item, n))
+        self.n_hist = sum(n for _, _, n in self.items)
+
+    def run(self, threads: int):
+        """One timed pass: (histories/s, histories, seconds, words/history of
+        transport, words/history of the estimator loops)."""
+        dt, words_tr, words_est = 0.0, 0, 0
+        for sim, (spec, per_item, _) in zip(self.sims, self.items):
+            self.O.words_counted_split()
+            t0 = time.perf_counter()
+            self.O.msim(sim.bundle_ptr(), spec.n_interactions_trajectory, spec.nchannels, threads=threads,
                         max_photons_per_item=per_item)
-        dt += time.perf_counter() - t0
-        w, we = oracle_api.words_counted_split()
-        words_tr += w - we
-        words_est += we
-        n_hist += min(per_item, int(spec.n_photons_line)) * len(spec.discrete) + \
-            min(per_item, int(spec.n_photons_interval)) * max(0, len(spec.continuous) - 1)
-        sim.close()
-    return n_hist / dt, n_hist, dt, words_tr / n_hist, words_est / n_hist
+            dt += time.perf_counter() - t0
+            w, we = self.O.words_counted_split()
+            words_tr += w - we
+            words_est += we
+        return self.n_hist / dt, self.n_hist, dt, words_tr / self.n_hist, words_est / self.n_hist
+
+    def close(self):
+        for sim in self.sims:
+            sim.close()
+
+
+def run_cpu_sample(specs, options, n_sample: int, threads: int):
+    cs = CpuSample(specs, options, n_sample)
+    try:
+        return cs.run(threads)
+    finally:
+        cs.close()
 
 
 def cpu_sample_specs(args, rank=0):
@@ -264,8 +291,7 @@ def cpu_sample_specs(args, rank=0):
         return [configs.config3(int(args.photons_precision))], dict(configs.C1_OPTIONS), \
             "the thin-layer precision workload"
     specs, options = batched_specs(args.configs, args.budget_scale, rank)
-    pick = [specs[i] for i in range(0, len(specs), max(1, len(specs) // 8))][:8]
-    return pick, options, "8 of the %d batched configurations" % len(specs)
+    return specs, options, "all %d batched configurations, each item's photons in the step's proportions" % len(specs)
 
 
 def reference_arm(args):
@@ -275,10 +301,12 @@ def reference_arm(args):
     specs, options, what = cpu_sample_specs(args)
     threads = os.cpu_count() or 1
     vals = []
+    cs = CpuSample(specs, options, args.cpu_sample)
     for i in range(args.warmup + args.steps):
-        v, n, dt, _, _ = run_cpu_sample(specs, options, args.cpu_sample, threads)
+        v, n, dt, _, _ = cs.run(threads)
         if i >= args.warmup:
             vals.append((v, n, dt))
+    cs.close()
     value = statistics.median(v for v, _, _ in vals)
     sample = "%d photons per step over %s" % (vals[0][1], what)
     batched = args.workload == "batched"

@@ -339,8 +339,15 @@ static void tally_channel(const xmi_bundle *b, otally *t, int n, double E, doubl
   if (ch >= 0 && ch <= b->nchannels - 1)
     for (k = n; k <= b->n_interactions; k++) t->channels[(size_t)k * b->nchannels + ch] += w;
 }
+/* thread tallies hold the history rows of the run's elements only: row of
+ * atomic number Z (set per run by oracle_xmi_main_msim; all rows = Z - 1
+ * outside a run) */
+static int o_zrow[101];
+static int o_zrow_set = 0;
+
 static size_t hidx(const xmi_bundle *b, int Z, int line, int n) {
-  return ((size_t)(Z - 1) * 385 + (line - 1)) * b->n_interactions + (n - 1);
+  const int row = o_zrow_set ? o_zrow[Z] : Z - 1;
+  return ((size_t)row * 385 + (line - 1)) * b->n_interactions + (n - 1);
 }
 
 /* ------------------------------------------------------------------ */
@@ -1429,41 +1436,88 @@ int oracle_xmi_main_msim(const xmi_bundle *b, int n_mpi_hosts, int nthreads, int
 #ifdef _OPENMP
   if (nthreads > 0) omp_set_num_threads(nthreads);
 #endif
-#pragma omp parallel
   {
-    otally t;
-    int it_i;
-    t.channels = (double *)calloc(nc, sizeof(double));
-    t.brute = (double *)calloc(nh, sizeof(double));
-    t.var_red = (double *)calloc(nh, sizeof(double));
-    t.not_found = 0;
-    t.error = 0;
+    /* one loop over every (item, photon) pair, so that an item of few photons
+     * costs no barrier; the thread tallies are summed in parallel afterwards */
+    int64_t *first = (int64_t *)malloc(sizeof(int64_t) * (size_t)(b->n_items + 1)), total;
+    int it_i, nt = 1;
+    otally *tl;
+    first[0] = 0;
     for (it_i = 0; it_i < b->n_items; it_i++) {
-      const xmi_source_item *it = &b->items[it_i];
-      int64_t j, n = it->n_photons;
+      int64_t n = b->items[it_i].n_photons;
       if (max_photons_per_item >= 0 && n > max_photons_per_item) n = max_photons_per_item;
-#pragma omp for schedule(dynamic, 64)
-      for (j = 0; j < n; j++) {
-        if (!t.error && !run_photon(b, it, j, &t) && !t.error) t.error = 1;
-      }
+      first[it_i + 1] = first[it_i] + n;
     }
-#pragma omp critical
+    total = first[b->n_items];
+#ifdef _OPENMP
+    nt = omp_get_max_threads();
+#endif
+    tl = (otally *)calloc((size_t)nt, sizeof(otally));
+    /* compact history rows: the thread tallies cover the run's elements only */
+    size_t nhc;
+    for (it_i = 0; it_i <= 100; it_i++) o_zrow[it_i] = 0;
+    for (it_i = 0; it_i < b->n_elem; it_i++) o_zrow[b->elem_Z[it_i]] = it_i;
+    o_zrow_set = 1;
+    nhc = (size_t)(b->n_elem > 0 ? b->n_elem : 1) * 385 * N;
+#pragma omp parallel
     {
-      for (i = 0; i < nc; i++) channels[i] += t.channels[i];
-      for (i = 0; i < nh; i++) {
-        brute[i] += t.brute[i];
-        var_red[i] += t.var_red[i];
+      int tid = 0;
+      int64_t g;
+      otally *t;
+#ifdef _OPENMP
+      tid = omp_get_thread_num();
+#endif
+      t = &tl[tid];
+      t->channels = (double *)calloc(nc, sizeof(double));
+      t->brute = (double *)calloc(nhc, sizeof(double));
+      t->var_red = (double *)calloc(nhc, sizeof(double));
+#pragma omp for schedule(dynamic, 64)
+      for (g = 0; g < total; g++) {
+        int lo = 0, hi = b->n_items - 1;
+        while (lo < hi) { /* the item holding photon g */
+          int mid = (lo + hi + 1) >> 1;
+          if (first[mid] <= g) lo = mid; else hi = mid - 1;
+        }
+        if (!t->error && !run_photon(b, &b->items[lo], g - first[lo], t) && !t->error) t->error = 1;
       }
-      *not_found += t.not_found;
-      if (t.error) ok = 0;
-      o_words_total += o_words;
-      o_words_est_total += o_words_est;
-      o_words = 0;
-      o_words_est = 0;
+#pragma omp critical
+      {
+        o_words_total += o_words;
+        o_words_est_total += o_words_est;
+        o_words = 0;
+        o_words_est = 0;
+      }
+#pragma omp barrier
+#pragma omp for schedule(static)
+      for (i = 0; i < nhc; i++) {
+        const size_t e = i / ((size_t)385 * N);
+        size_t full;
+        int k;
+        if ((int)e >= b->n_elem) continue;
+        full = ((size_t)(b->elem_Z[e] - 1) * 385 * N) + i % ((size_t)385 * N);
+        for (k = 0; k < nt; k++) {
+          if (!tl[k].brute) continue;
+          brute[full] += tl[k].brute[i];
+          var_red[full] += tl[k].var_red[i];
+        }
+      }
+#pragma omp for schedule(static)
+      for (i = 0; i < nc; i++) {
+        int k;
+        for (k = 0; k < nt; k++)
+          if (tl[k].channels) channels[i] += tl[k].channels[i];
+      }
     }
-    free(t.channels);
-    free(t.brute);
-    free(t.var_red);
+    o_zrow_set = 0;
+    for (it_i = 0; it_i < nt; it_i++) {
+      *not_found += tl[it_i].not_found;
+      if (tl[it_i].error) ok = 0;
+      free(tl[it_i].channels);
+      free(tl[it_i].brute);
+      free(tl[it_i].var_red);
+    }
+    free(tl);
+    free(first);
   }
   for (i = 0; i < nc; i++) channels[i] *= b->live_time;
   for (i = 0; i < nh; i++) {

@@ -315,6 +315,31 @@ def test_autotuned_batch_keeps_results():
         s.close()
 
 
+def test_batched_graph_is_updated_in_place():
+    """The second batched call of the same configurations reuses the first
+    call's executable graph (cudaGraphExecUpdate with the new call's buffers
+    and events) and gives the same result; a batch of another shape gets a
+    graph of its own."""
+    from xmimsim_gb300 import last_timing
+    specs = [configs.config1(n_photons_line=3000), mixed_source_spec()]
+    sims = [Simulation(sp, options=configs.C1_OPTIONS, gpu=gpu_options(seed=SEED)) for sp in specs]
+    first = Simulation.msim_batch(sims)
+    second = Simulation.msim_batch(sims)
+    assert last_timing()["graph_updated"] == 1
+    for s, a, b in zip(sims, first, second):
+        np.testing.assert_allclose(b["var_red"], a["var_red"], rtol=1e-9, atol=1e-12 * abs(a["var_red"]).max())
+        np.testing.assert_allclose(b["channels"], a["channels"], rtol=1e-9, atol=1e-12 * abs(a["channels"]).max())
+        s.free_raw(a)
+        s.free_raw(b)
+    one = Simulation.msim_batch(sims[:1])
+    assert last_timing()["graph_updated"] in (0, 1)
+    np.testing.assert_allclose(one[0]["var_red"], second[0]["var_red"], rtol=1e-9,
+                               atol=1e-12 * abs(second[0]["var_red"]).max())
+    sims[0].free_raw(one[0])
+    for s in sims:
+        s.close()
+
+
 def test_surrogate_integrator_fallback_matches_oracle():
     """Estimator events outside the network's checked region go to the
     warp-parallel integrator (omega_fallback_kernel), which must reproduce the

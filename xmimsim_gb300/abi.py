@@ -163,6 +163,7 @@ PROTOTYPES = {
                                          C.POINTER(C.c_int)]),
     "xmi_gpu_solid_angle_points": (C.c_int, [C.c_void_p, C.c_int, c_double_p, c_double_p, C.c_int, C.c_int,
                                              C.c_ulonglong, c_double_p]),
+    "xmi_gpu_last_graph": (C.c_int, [C.POINTER(C.c_int)]),
     "xmi_gpu_compton_kinematics": (C.c_int, [C.c_int, c_double_p, c_double_p, c_double_p, c_double_p,
                                              c_double_p]),
     "xmi_tube_ebel": (C.c_int, [C.POINTER(XmiLayer), C.POINTER(XmiLayer), C.POINTER(XmiLayer), C.c_double,

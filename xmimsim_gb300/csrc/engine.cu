@@ -33,6 +33,8 @@ struct Timing {
   long long events = 0, surrogate_fallbacks = 0;
   /* host<->device bytes copied by the last xmi_main_msim / _batch call */
   long long h2d_bytes = 0, d2h_bytes = 0;
+  /* the batched call's graph: -1 none, 0 instantiated, 1 updated in place */
+  int graph_updated = -1;
 };
 thread_local Timing g_timing;
 
@@ -66,7 +68,16 @@ struct EventQueue {
   size_t bytes = 0;
   long long cap = 0;
   int nkeys = 0;
+  /* executable graph of the last captured chunk sequence on this queue: the
+   * next capture of the same shape updates it in place (cudaGraphExecUpdate)
+   * instead of instantiating a new one */
+  cudaGraphExec_t exec = nullptr;
+  void drop_exec() {
+    if (exec) cudaGraphExecDestroy(exec);
+    exec = nullptr;
+  }
   void release() {
+    drop_exec();
     cudaFree(events);
     cudaFree(key);
     cudaFree(order);
@@ -482,6 +493,11 @@ int xmi_gpu_last_timing(double *transport_ms, double *total_ms, int *launches) {
   return 1;
 }
 
+int xmi_gpu_last_graph(int *updated) {
+  if (updated) *updated = g_timing.graph_updated;
+  return 1;
+}
+
 int xmi_gpu_last_phases(double *transport_kernel_ms, double *sort_ms, double *estimator_ms, long long *events) {
   if (transport_kernel_ms) *transport_kernel_ms = g_timing.phase_ms[0];
   if (sort_ms) *sort_ms = g_timing.phase_ms[1];
@@ -742,6 +758,7 @@ template <typename R>
 static bool ensure_queue(EventQueue &q, long long cap, int nkeys) {
   const size_t bytes = (size_t)cap * sizeof(xmi::VrEvent<R>);
   if (bytes > q.bytes || cap > q.cap) {
+    q.drop_exec();
     cudaFree(q.events);
     cudaFree(q.key);
     cudaFree(q.order);
@@ -759,6 +776,7 @@ static bool ensure_queue(EventQueue &q, long long cap, int nkeys) {
     q.cap = cap;
   }
   if (nkeys > q.nkeys) {
+    q.drop_exec();
     cudaFree(q.hist);
     q.hist = nullptr;
     q.nkeys = 0;
@@ -809,7 +827,6 @@ static bool run_chunks(cudaStream_t st, EventQueue &q, long long n, int N, int n
   };
   int launches = 0;
   cudaGraph_t g = nullptr;
-  cudaGraphExec_t ge = nullptr;
   if (graph && !cuda_ok(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "graph capture")) return false;
   mark();
   for (long long w0 = 0; w0 < n; w0 += chunk) {
@@ -838,12 +855,29 @@ static bool run_chunks(cudaStream_t st, EventQueue &q, long long n, int N, int n
   }
   bool ok = cuda_ok(cudaGetLastError(), "transport launch");
   if (graph) {
-    /* the whole chunk sequence as one graph launch */
-    ok = cuda_ok(cudaStreamEndCapture(st, &g), "graph capture") && ok &&
-         cuda_ok(cudaGraphInstantiate(&ge, g, 0), "graph instantiate") && cuda_ok(cudaGraphLaunch(ge, st), "graph launch");
+    /* the whole chunk sequence as one graph launch; the executable graph of
+     * the previous call is updated with this capture's parameters (buffers,
+     * counts, timing events) when the sequence has the same shape, and
+     * instantiated anew otherwise */
+    ok = cuda_ok(cudaStreamEndCapture(st, &g), "graph capture") && ok;
+    if (ok) {
+      bool updated = false;
+      if (q.exec) {
+        cudaGraphExecUpdateResultInfo info;
+        updated = cudaGraphExecUpdate(q.exec, g, &info) == cudaSuccess;
+        if (!updated) {
+          (void)cudaGetLastError(); /* a different shape: not an error */
+          q.drop_exec();
+        }
+      }
+      if (!updated) ok = cuda_ok(cudaGraphInstantiate(&q.exec, g, 0), "graph instantiate");
+      if (ok) {
+        g_timing.graph_updated = updated ? 1 : 0;
+        ok = cuda_ok(cudaGraphLaunch(q.exec, st), "graph launch");
+      }
+    }
   }
   ok = ok && cuda_ok(cudaEventSynchronize(marks.back()), "transport");
-  if (ge) cudaGraphExecDestroy(ge);
   if (g) cudaGraphDestroy(g);
   if (ok) {
     float total = 0.f;
@@ -1132,6 +1166,7 @@ extern "C" int xmi_main_msim(xmi_inputFPtr in, xmi_hdf5FPtr t, int n_mpi_hosts, 
   if (!ensure_device()) return 0;
   if (!xmi_gpu_prepare_run(in, t, options, n_mpi_hosts, sa)) return 0;
   g_timing.h2d_bytes = g_timing.d2h_bytes = 0;
+  g_timing.graph_updated = -1;
   const xmi_bundle &h = t->b;
   const int precision = in->gpu.precision;
   if (!xmi_dev_sync_tables(t, precision)) return 0;
@@ -1307,6 +1342,7 @@ extern "C" int xmi_main_msim_batch(int n, xmi_inputFPtr *inputFPtrs, xmi_hdf5FPt
   std::vector<xmi::DevTally> tl(n);
   const auto wall0 = std::chrono::steady_clock::now();
   g_timing.h2d_bytes = g_timing.d2h_bytes = 0;
+  g_timing.graph_updated = -1;
   const void *sg = nullptr;
   for (int c = 0; c < n; c++) {
     channels[c] = brute_histories[c] = var_red_histories[c] = nullptr;

@@ -177,6 +177,9 @@ def last_timing() -> dict:
     hd, dh = C.c_longlong(), C.c_longlong()
     lib.xmi_gpu_last_transfers(C.byref(hd), C.byref(dh))
     out.update(h2d_bytes=hd.value, d2h_bytes=dh.value)
+    gu = C.c_int()
+    lib.xmi_gpu_last_graph(C.byref(gu))
+    out.update(graph_updated=gu.value)
     return out
 
 
