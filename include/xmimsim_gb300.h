@@ -272,7 +272,9 @@ int xmi_gpu_last_timing(double *transport_ms, double *total_ms, int *launches);
 int xmi_gpu_last_phases(double *transport_kernel_ms, double *sort_ms, double *estimator_ms, long long *events);
 /* how the last xmi_main_msim_batch ran its chunk sequence: -1 no graph, 0 a
  * graph instantiated for this call, 1 the previous call's executable graph
- * updated in place (same shape) */
+ * updated in place (same shape), 100 + the cudaGraphExecUpdateResult when the
+ * previous graph could not take this call's sequence (a new one was
+ * instantiated) */
 int xmi_gpu_last_graph(int *updated);
 /* the device functions of the per-shell Compton kinematics
  * (xmi_get_qimax / xmi_get_energy_from_q, src/xmi_aux_f.F90:1951-2074) in

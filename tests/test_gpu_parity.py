@@ -332,7 +332,8 @@ def test_batched_graph_is_updated_in_place():
         s.free_raw(a)
         s.free_raw(b)
     one = Simulation.msim_batch(sims[:1])
-    assert last_timing()["graph_updated"] in (0, 1)
+    # another shape: the update is refused (100 + cudaGraphExecUpdateErrorTopologyChanged) and a new graph runs
+    assert last_timing()["graph_updated"] >= 100
     np.testing.assert_allclose(one[0]["var_red"], second[0]["var_red"], rtol=1e-9,
                                atol=1e-12 * abs(second[0]["var_red"]).max())
     sims[0].free_raw(one[0])

@@ -72,12 +72,17 @@ struct EventQueue {
    * next capture of the same shape updates it in place (cudaGraphExecUpdate)
    * instead of instantiating a new one */
   cudaGraphExec_t exec = nullptr;
+  /* timing events of the chunk sequence, kept across calls so that a
+   * captured sequence of the same shape records the same events */
+  std::vector<cudaEvent_t> marks;
   void drop_exec() {
     if (exec) cudaGraphExecDestroy(exec);
     exec = nullptr;
   }
   void release() {
     drop_exec();
+    for (cudaEvent_t e : marks) cudaEventDestroy(e);
+    marks.clear();
     cudaFree(events);
     cudaFree(key);
     cudaFree(order);
@@ -815,15 +820,18 @@ static bool run_chunks(cudaStream_t st, EventQueue &q, long long n, int N, int n
     vq.count = q.count;
     vq.cap = chunk * N;
   }
-  std::vector<cudaEvent_t> marks;
   /* under stream capture an event record must be marked external to become a
    * real record when the graph runs (so that it can be timed and waited on) */
+  size_t n_marks = 0;
   auto mark = [&]() {
-    cudaEvent_t e;
-    cudaEventCreate(&e);
+    if (n_marks == q.marks.size()) {
+      cudaEvent_t e;
+      cudaEventCreate(&e);
+      q.marks.push_back(e);
+    }
+    cudaEvent_t e = q.marks[n_marks++];
     if (graph) cudaEventRecordWithFlags(e, st, cudaEventRecordExternal);
     else cudaEventRecord(e, st);
-    marks.push_back(e);
   };
   int launches = 0;
   cudaGraph_t g = nullptr;
@@ -862,21 +870,24 @@ static bool run_chunks(cudaStream_t st, EventQueue &q, long long n, int N, int n
     ok = cuda_ok(cudaStreamEndCapture(st, &g), "graph capture") && ok;
     if (ok) {
       bool updated = false;
+      int status = 0;
       if (q.exec) {
         cudaGraphExecUpdateResultInfo info;
         updated = cudaGraphExecUpdate(q.exec, g, &info) == cudaSuccess;
         if (!updated) {
           (void)cudaGetLastError(); /* a different shape: not an error */
           q.drop_exec();
+          status = 100 + (int)info.result;
         }
       }
       if (!updated) ok = cuda_ok(cudaGraphInstantiate(&q.exec, g, 0), "graph instantiate");
       if (ok) {
-        g_timing.graph_updated = updated ? 1 : 0;
+        g_timing.graph_updated = updated ? 1 : status;
         ok = cuda_ok(cudaGraphLaunch(q.exec, st), "graph launch");
       }
     }
   }
+  std::vector<cudaEvent_t> marks(q.marks.begin(), q.marks.begin() + n_marks);
   ok = ok && cuda_ok(cudaEventSynchronize(marks.back()), "transport");
   if (g) cudaGraphDestroy(g);
   if (ok) {
@@ -892,7 +903,6 @@ static bool run_chunks(cudaStream_t st, EventQueue &q, long long n, int N, int n
       }
     ph.launches = launches;
   }
-  for (cudaEvent_t e : marks) cudaEventDestroy(e);
   return ok;
 }
 
@@ -984,8 +994,11 @@ static bool stage_run(DevState *s, xmi::DevBundle<R> &d, const xmi_bundle &h, xm
  * rows of a CTA fit shared memory (layers that need more run per-lane) */
 template <typename R>
 static int stage_cap_for(int stage_max) {
-  const int limit = (int)(200 * 1024 / (8 * sizeof(R))) - xmi::kScratchPerWarp;
-  return stage_max < limit ? stage_max : limit;
+  /* a multiple of 4 values, so that each warp's scratch (after its stage
+   * row) starts on 16 bytes for the line loop's vector reads */
+  const int limit = ((int)(200 * 1024 / (8 * sizeof(R))) - xmi::kScratchPerWarp) & ~3;
+  const int cap = (stage_max + 3) & ~3;
+  return cap < limit ? cap : limit;
 }
 
 template <typename R, bool Adv = false>

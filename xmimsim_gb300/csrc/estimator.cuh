@@ -223,6 +223,63 @@ __device__ __forceinline__ void estimate_event(const DevBundle<R> &b, const DevT
  * layer and, per element, shell probability x event scale */
 constexpr int kScratchPerWarp = 32 * XMI_MAXL + 32 * XMI_NSHELL;
 
+/* One line entry k over the events q0 .. q0 + np2 - 1 of the warp (lane
+ * group): sum of shell factor x exp(-sum_j mu_j(line) rho_j d_j).  Only the
+ * first L layers are summed: the warp's configuration has at most L layers,
+ * and the path sums and line mu of the others are zero, so the result is
+ * the same bit for bit while the FP32 engine reads the path sums of an event
+ * from shared memory in 16-byte words and does L instead of XMI_MAXL
+ * multiply-adds per line and event. */
+template <typename R, int L>
+__device__ __forceinline__ R line_entry_events(const DevBundle<R> &b, const R *s_rd, const R *s_a, int k, int q0,
+                                               int np2) {
+  const int sh = XMI_LDG(b.ent_shell, k, b.n_ent, 16);
+  R pmu[L];
+#ifndef XMI_CHECKED
+  if constexpr (sizeof(R) == 4 && XMI_MAXL == 8 && L >= 4) {
+    const float4 *pp = reinterpret_cast<const float4 *>(b.ent_pmu + (long long)k * XMI_MAXL);
+#pragma unroll
+    for (int j4 = 0; j4 < L / 4; j4++) {
+      const float4 a = __ldg(pp + j4);
+      pmu[4 * j4] = a.x, pmu[4 * j4 + 1] = a.y, pmu[4 * j4 + 2] = a.z, pmu[4 * j4 + 3] = a.w;
+    }
+  } else if constexpr (sizeof(R) == 4 && XMI_MAXL == 8 && L == 2) {
+    const float2 a = __ldg(reinterpret_cast<const float2 *>(b.ent_pmu + (long long)k * XMI_MAXL));
+    pmu[0] = a.x, pmu[1] = a.y;
+  } else
+#endif
+  {
+#pragma unroll
+    for (int j = 0; j < L; j++)
+      pmu[j] = XMI_LDG(b.ent_pmu, (long long)k * XMI_MAXL + j, (long long)b.n_ent * XMI_MAXL, 17);
+  }
+  R acc = (R)0;
+#pragma unroll 4
+  for (int q = q0; q < q0 + np2; q++) {
+    R murhod = (R)0;
+    if constexpr (sizeof(R) == 4 && L >= 4) {
+      const float4 *r4 = reinterpret_cast<const float4 *>(s_rd + q * XMI_MAXL);
+#pragma unroll
+      for (int j4 = 0; j4 < L / 4; j4++) {
+        const float4 v = r4[j4];
+        murhod += pmu[4 * j4] * v.x;
+        murhod += pmu[4 * j4 + 1] * v.y;
+        murhod += pmu[4 * j4 + 2] * v.z;
+        murhod += pmu[4 * j4 + 3] * v.w;
+      }
+    } else if constexpr (sizeof(R) == 4 && L == 2) {
+      const float2 v = *reinterpret_cast<const float2 *>(s_rd + q * XMI_MAXL);
+      murhod += pmu[0] * v.x;
+      murhod += pmu[1] * v.y;
+    } else {
+#pragma unroll
+      for (int j = 0; j < L; j++) murhod += pmu[j] * s_rd[q * XMI_MAXL + j];
+    }
+    acc += s_a[q * XMI_NSHELL + sh] * exp(-murhod);
+  }
+  return acc;
+}
+
 /* The estimator for the 32 events of a warp that share configuration, layer
  * and order.  Elements: lane = event, as in the per-lane path, contributions
  * summed across the warp into the stage row.  Lines: lane = line entry, each
@@ -302,32 +359,14 @@ __device__ __forceinline__ void estimate_event_uniform(const DevBundle<R> &b, co
     int np2 = 1;
     while (np2 < k1 - k0 && np2 < 32) np2 <<= 1;
     const int li = lane & (np2 - 1), q0 = lane - li; /* q0 = group x np2: the group's first event */
+    const int nL = b.n_layers; /* warp-uniform: one configuration per warp here */
     for (int kb = k0; kb < k1; kb += np2) {
       const int k = kb + li;
       R acc = (R)0;
       if (k < k1) {
-        const int sh = XMI_LDG(b.ent_shell, k, b.n_ent, 16);
-        R pmu[XMI_MAXL];
-#ifndef XMI_CHECKED
-        if constexpr (sizeof(R) == 4 && XMI_MAXL == 8) {
-          const float4 *pp = reinterpret_cast<const float4 *>(b.ent_pmu + (long long)k * XMI_MAXL);
-          const float4 a0 = __ldg(pp), a1 = __ldg(pp + 1);
-          pmu[0] = a0.x, pmu[1] = a0.y, pmu[2] = a0.z, pmu[3] = a0.w;
-          pmu[4] = a1.x, pmu[5] = a1.y, pmu[6] = a1.z, pmu[7] = a1.w;
-        } else
-#endif
-        {
-#pragma unroll
-          for (int j = 0; j < XMI_MAXL; j++)
-            pmu[j] = XMI_LDG(b.ent_pmu, (long long)k * XMI_MAXL + j, (long long)b.n_ent * XMI_MAXL, 17);
-        }
-#pragma unroll 4
-        for (int q = q0; q < q0 + np2; q++) {
-          R murhod = (R)0;
-#pragma unroll
-          for (int j = 0; j < XMI_MAXL; j++) murhod += pmu[j] * s_rd[q * XMI_MAXL + j];
-          acc += s_a[q * XMI_NSHELL + sh] * exp(-murhod);
-        }
+        if (XMI_MAXL == 8 && nL <= 2) acc = line_entry_events<R, (XMI_MAXL < 2 ? XMI_MAXL : 2)>(b, s_rd, s_a, k, q0, np2);
+        else if (XMI_MAXL == 8 && nL <= 4) acc = line_entry_events<R, (XMI_MAXL < 4 ? XMI_MAXL : 4)>(b, s_rd, s_a, k, q0, np2);
+        else acc = line_entry_events<R, XMI_MAXL>(b, s_rd, s_a, k, q0, np2);
       }
       for (int off = np2; off < 32; off <<= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
       if (q0 == 0 && k < k1) st.v[k - st.k_first] += acc * XMI_LDG(b.ent_coef, k, b.n_ent, 16);
