@@ -77,6 +77,32 @@ __device__ __noinline__ R compton_advanced_est(const DevBundle<R> &b, const DevT
   return total;
 }
 
+/* Channel contributions of the 32 lanes of a warp (every lane calls; w = 0
+ * for a lane without one): the events of a warp share configuration, layer
+ * and order, and their Compton and Rayleigh energies often fall in the same
+ * channel (every first-order Rayleigh contribution of a discrete line does),
+ * where 32 FP64 atomics to one address serialise.  Lanes are grouped by
+ * channel (match_any), the group's leader sums its peers' values from the
+ * warp's buffer buf[32] in shared memory and adds the sum with one atomic. */
+template <typename R>
+__device__ __forceinline__ void chan_add_warp(const DevBundle<R> &b, const DevTally &t, int n, R E, R w, R *buf) {
+  const int lane = threadIdx.x & 31;
+  int ch = -1;
+  if (w != (R)0 && E >= (R)kEnergyThreshold) {
+    ch = channel_of(b, E);
+    if (!(ch >= 0 && ch <= b.nch - 1 && XMI_CHK((long long)n * b.nch + ch, (long long)(b.N + 1) * b.nch, 30))) ch = -1;
+  }
+  const unsigned peers = __match_any_sync(0xffffffffu, ch);
+  buf[lane] = w;
+  __syncwarp();
+  if (ch >= 0 && lane == __ffs(peers) - 1) {
+    R sum = (R)0;
+    for (unsigned m = peers; m; m &= m - 1) sum += buf[__ffs(m) - 1];
+    atomicAdd(&t.chan[(size_t)n * b.nch + ch], (double)sum);
+  }
+  __syncwarp();
+}
+
 /* History contributions of the events of one key (configuration, layer,
  * order) are summed across the warp and staged in a warp-private
  * shared-memory row, stage[j]: j < n_line = the layer's line entries (entry
@@ -221,7 +247,7 @@ __device__ __forceinline__ void estimate_event(const DevBundle<R> &b, const DevT
 
 /* per-warp scratch of the uniform path: the 32 events' path sums rho*d per
  * layer and, per element, shell probability x event scale */
-constexpr int kScratchPerWarp = 32 * XMI_MAXL + 32 * XMI_NSHELL;
+constexpr int kScratchPerWarp = 32 * XMI_MAXL + 32 * XMI_NSHELL + 32;
 
 /* One line entry k over the events q0 .. q0 + np2 - 1 of the warp (lane
  * group): sum of shell factor x exp(-sum_j mu_j(line) rho_j d_j).  Only the
@@ -293,7 +319,7 @@ __device__ __forceinline__ void estimate_event_uniform(const DevBundle<R> &b, co
   const int layer = ev.layer, n = ev.n;
   const int nel = b.nel[layer], off = b.off[layer];
   const long long hbase = (long long)(n - 1) * b.n_slots;
-  R *s_rd = scratch, *s_a = scratch + 32 * XMI_MAXL;
+  R *s_rd = scratch, *s_a = scratch + 32 * XMI_MAXL, *s_ch = s_a + 32 * XMI_NSHELL;
   const R live = valid ? (R)1 : (R)0;
   R rayl_sum = (R)0; /* Rayleigh keeps the photon energy: one channel add per event */
   const ComptonEvent<R> ce = compton_event(ev.E, ev.theta);
@@ -334,7 +360,7 @@ __device__ __forceinline__ void estimate_event_uniform(const DevBundle<R> &b, co
         ok = false;
       }
       contribute<R, true>(t, st, st.n_line + 2 * i + 1, hbase + rs + 1, twc);
-      if (valid) chan_add(b, t, n, ec, twc);
+      chan_add_warp(b, t, n, ec, valid ? twc : (R)0, s_ch);
     }
     /* shell factors of this event for element i */
     R P[XMI_NSHELL];
@@ -373,7 +399,7 @@ __device__ __forceinline__ void estimate_event_uniform(const DevBundle<R> &b, co
     }
     __syncwarp();
   }
-  if (valid) chan_add(b, t, n, ev.E, rayl_sum);
+  chan_add_warp(b, t, n, ev.E, valid ? rayl_sum : (R)0, s_ch);
 }
 
 /* number of events the queue holds: the count, capped at the capacity (a
