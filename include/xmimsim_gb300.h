@@ -49,6 +49,56 @@ typedef struct {
   int grid_nr, grid_nt;     /* solid-angle grid points along r and theta; 0: the reference's 1024 */
 } xmi_gpu_options;
 
+/* ---- atomic data source of the host tabulator ----
+ * Every cross section and atomic parameter the tabulator reads (the values
+ * the reference takes from xraylib: src/xmi_aux_f.F90:22, src/xmi_data_f.F90
+ * :880-1481, src/xmi_variance_reduction.F90:344-709, src/xmi_detector_f.F90,
+ * src/xmi_ebel.F90) comes through this table; the entries have xraylib's
+ * names and argument order.  Index conventions: shell 0 = K, 1..3 = L1..L3,
+ * 4..8 = M1..M5 (xraylib's K_SHELL..M5_SHELL); line = the positive index
+ * 1..383 of the history layout, i.e. minus xraylib's line macro (an xraylib
+ * adapter calls LineEnergy(Z, -line)); CosKronTransProb trans 0..13 in
+ * xraylib's order FL12, FL13, FLP13, FL23, FM12 .. FM45; AugerRate trans
+ * 0..644 in xraylib's order (K_L1L1 = 0 .. L3_M5Q3 = 644); AugerVacancies(Z,
+ * s, t) = expected new vacancies in shell t per non-radiative decay of shell
+ * s (an xraylib adapter sums AugerRate over the transitions of s weighted by
+ * the vacancies each leaves in t).  prepare(Z) may be NULL; it is called once
+ * per element before the others, from one thread.  The default table is the
+ * stand-in model compiled into the library (xrlite: xraylib and its data are
+ * absent on the build and GPU machines).  No counterpart in the reference,
+ * which links xraylib directly. */
+typedef struct {
+  const char *name;
+  double (*AtomicWeight)(int Z);
+  double (*EdgeEnergy)(int Z, int shell);
+  double (*ElectronConfig)(int Z, int shell);
+  double (*LineEnergy)(int Z, int line);
+  double (*RadRate)(int Z, int line);
+  double (*FluorYield)(int Z, int shell);
+  double (*AugerYield)(int Z, int shell);
+  double (*CosKronTransProb)(int Z, int trans);
+  double (*AugerRate)(int Z, int trans);
+  double (*AugerVacancies)(int Z, int shell, int to_shell);
+  double (*CS_Total_Kissel)(int Z, double E);
+  double (*CS_Photo_Total)(int Z, double E);
+  double (*CS_Photo_Partial)(int Z, int shell, double E);
+  double (*CS_Rayl)(int Z, double E);
+  double (*CS_Compt)(int Z, double E);
+  double (*FF_Rayl)(int Z, double q);
+  double (*SF_Compt)(int Z, double q);
+  double (*DCS_Rayl)(int Z, double E, double theta);
+  double (*DCS_Compt)(int Z, double E, double theta);
+  double (*ComptonProfile)(int Z, double pz);
+  void (*prepare)(int Z);
+} xmi_atomic_data;
+/* Installs a data source (copied; NULL restores the default).  Only before
+ * the first table of the process is built: returns 0 with an error once
+ * tables (cached per element and shared by every bundle) exist, or when an
+ * entry other than prepare is NULL. */
+int xmi_set_atomic_data(const xmi_atomic_data *data);
+/* the table in use */
+const xmi_atomic_data *xmi_get_atomic_data(void);
+
 /* ---- data model helpers (reference src/xmi_data_structs.c) ---- */
 xmi_input *xmi_input_init_empty(void);                 /* src/xmi_data_structs.c:551 */
 void xmi_input_free(xmi_input *input);                 /* include/xmi_data_structs.h:331 */

@@ -110,6 +110,26 @@ class XmiGpuOptions(C.Structure):
                 ("grid_nr", C.c_int), ("grid_nt", C.c_int)]
 
 
+# the atomic data source table (xmi_atomic_data): entry name -> argument types
+ATOMIC_DATA_ENTRIES = [
+    ("AtomicWeight", [C.c_int]), ("EdgeEnergy", [C.c_int, C.c_int]), ("ElectronConfig", [C.c_int, C.c_int]),
+    ("LineEnergy", [C.c_int, C.c_int]), ("RadRate", [C.c_int, C.c_int]), ("FluorYield", [C.c_int, C.c_int]),
+    ("AugerYield", [C.c_int, C.c_int]), ("CosKronTransProb", [C.c_int, C.c_int]), ("AugerRate", [C.c_int, C.c_int]),
+    ("AugerVacancies", [C.c_int, C.c_int, C.c_int]), ("CS_Total_Kissel", [C.c_int, C.c_double]),
+    ("CS_Photo_Total", [C.c_int, C.c_double]), ("CS_Photo_Partial", [C.c_int, C.c_int, C.c_double]),
+    ("CS_Rayl", [C.c_int, C.c_double]), ("CS_Compt", [C.c_int, C.c_double]), ("FF_Rayl", [C.c_int, C.c_double]),
+    ("SF_Compt", [C.c_int, C.c_double]), ("DCS_Rayl", [C.c_int, C.c_double, C.c_double]),
+    ("DCS_Compt", [C.c_int, C.c_double, C.c_double]), ("ComptonProfile", [C.c_int, C.c_double]),
+]
+ATOMIC_DATA_FUNC = {name: C.CFUNCTYPE(C.c_double, *args) for name, args in ATOMIC_DATA_ENTRIES}
+PREPARE_FUNC = C.CFUNCTYPE(None, C.c_int)
+
+
+class XmiAtomicData(C.Structure):
+    _fields_ = [("name", C.c_char_p)] + [(name, ATOMIC_DATA_FUNC[name]) for name, _ in ATOMIC_DATA_ENTRIES] + \
+        [("prepare", PREPARE_FUNC)]
+
+
 # exported symbols and their prototypes (name -> (restype, argtypes))
 PROTOTYPES = {
     "xmi_input_init_empty": (C.POINTER(XmiInput), []),
@@ -164,6 +184,8 @@ PROTOTYPES = {
     "xmi_gpu_solid_angle_points": (C.c_int, [C.c_void_p, C.c_int, c_double_p, c_double_p, C.c_int, C.c_int,
                                              C.c_ulonglong, c_double_p]),
     "xmi_gpu_last_graph": (C.c_int, [C.POINTER(C.c_int)]),
+    "xmi_set_atomic_data": (C.c_int, [C.POINTER(XmiAtomicData)]),
+    "xmi_get_atomic_data": (C.POINTER(XmiAtomicData), []),
     "xmi_gpu_compton_kinematics": (C.c_int, [C.c_int, c_double_p, c_double_p, c_double_p, c_double_p,
                                              c_double_p]),
     "xmi_tube_ebel": (C.c_int, [C.POINTER(XmiLayer), C.POINTER(XmiLayer), C.POINTER(XmiLayer), C.c_double,

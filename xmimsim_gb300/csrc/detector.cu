@@ -384,7 +384,7 @@ void xmi_detector_convolute_spectrum(xmi_inputFPtr inputFPtr, double *channels_n
     std::vector<double> le(s.n_el * 64, 0.0), edge(s.n_el * 4, 0.0);
     for (int e = 0; e < s.n_el; e++) {
       int Z = er->Z[e], n = 0;
-      for (int sh = 0; sh < 4; sh++) edge[e * 4 + sh] = xrl_EdgeEnergy(Z, sh);
+      for (int sh = 0; sh < 4; sh++) edge[e * 4 + sh] = XD->EdgeEnergy(Z, sh);
       /* K: KL1..KP5, L1: L1M1..L1P5, L2: L2M1..L2Q1, L3: L3M1..L3P3 */
       const int ranges[4][2] = {{1, 29}, {32, 58}, {60, 85}, {86, 109}};
       for (int r = 0; r < 4; r++)
@@ -393,7 +393,7 @@ void xmi_detector_convolute_spectrum(xmi_inputFPtr inputFPtr, double *channels_n
           for (int ie = 0; ie < s.nfe && !used; ie++) used = er->fluo_escape_ratios[e + s.n_el * ((k - 1) + 109 * ie)] != 0.0;
           if (!used) continue;
           lk[e * 64 + n] = k;
-          le[e * 64 + n] = xrl_LineEnergy(Z, k);
+          le[e * 64 + n] = XD->LineEnergy(Z, k);
           n++;
         }
       ln[e] = n;
@@ -533,7 +533,7 @@ void xmi_detector_convolute_history(xmi_inputFPtr inputFPtr, double *history, xm
         size_t idx = ((size_t)(k - 1) * 385 + (j - 1)) * N + (i - 1);
         double counts = history[idx];
         if (!(counts > 0.0)) continue;
-        if (line_energy < 0.0) line_energy = xrl_LineEnergy(k, j);
+        if (line_energy < 0.0) line_energy = XD->LineEnergy(k, j);
         if (!(line_energy > 0.0)) continue;
         double det_corr = 1.0;
         for (int l = 0; l < in->absorbers->n_det_layers; l++) {

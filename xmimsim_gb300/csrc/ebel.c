@@ -105,7 +105,7 @@ static void spline_free(spline *s) {
 /* exp(-rho t mu(E)) of a single-element layer (window or filter) */
 static double layer_transmission(const xmi_layer *l, double E) {
   if (!l) return 1.0;
-  return exp(-1.0 * l->density * l->thickness * xrl_CS_Total_Kissel(l->Z[0], E));
+  return exp(-1.0 * l->density * l->thickness * XD->CS_Total_Kissel(l->Z[0], E));
 }
 
 int xmi_tube_ebel(xmi_layer *tube_anode, xmi_layer *tube_window, xmi_layer *tube_filter, double tube_voltage,
@@ -130,9 +130,9 @@ int xmi_tube_ebel(xmi_layer *tube_anode, xmi_layer *tube_window, xmi_layer *tube
     xmi_set_error("xmi_tube_ebel: anode element %d outside 1..100", Z);
     return 0;
   }
-  xrl_prepare(Z);
-  if (tube_window) xrl_prepare(tube_window->Z[0]);
-  if (tube_filter) xrl_prepare(tube_filter->Z[0]);
+  if (XD->prepare) XD->prepare(Z);
+  if (tube_window) if (XD->prepare) XD->prepare(tube_window->Z[0]);
+  if (tube_filter) if (XD->prepare) XD->prepare(tube_filter->Z[0]);
 
   /* angles (src/xmi_ebel.F90:221-224) */
   sinalphae = sin(M_PI / 180.0 * tube_angle_electron);
@@ -153,14 +153,14 @@ int xmi_tube_ebel(xmi_layer *tube_anode, xmi_layer *tube_window, xmi_layer *tube
   logz = log((double)Z);
   eta = (0.1904 - 0.2236 * logz + 0.1292 * logz * logz - 0.0149 * logz * logz * logz) * pow(tube_voltage, m);
   p3 = 0.787E-05 * sqrt((double)Z * 0.0135) * pow(tube_voltage, 1.5) + 0.735E-06 * tube_voltage * tube_voltage;
-  rhozmax = xrl_AtomicWeight(Z) * p3 / Z;
+  rhozmax = XD->AtomicWeight(Z) * p3 / Z;
   for (i = 0; i < ncont; i++) {
     const double Em = cont[i].energy + tube_delta_energy / 2.0;
     const double u0 = tube_voltage / Em, logu0 = log(u0);
     const double p1 = logu0 * (0.49269 - 1.09870 * eta + 0.78557 * eta * eta);
     const double p2 = 0.70256 - 1.09865 * eta + 1.00460 * eta * eta + logu0;
     const double rhoz = rhozmax * (p1 / p2);
-    const double tau = xrl_CS_Total_Kissel(Z, Em);
+    const double tau = XD->CS_Total_Kissel(Z, Em);
     const double rhelp = tau * 2.0 * rhoz * sinfactor;
     double I = 0.0;
     if (rhelp > 0.0) {
@@ -183,14 +183,14 @@ int xmi_tube_ebel(xmi_layer *tube_anode, xmi_layer *tube_window, xmi_layer *tube
   for (line = xrl_shell_first_line(0); line <= xrl_shell_last_line(3); line++) {
     int shell;
     double edge;
-    if (!(xrl_RadRate(Z, line) > 0.0 && xrl_LineEnergy(Z, line) > TUBE_MINIMUM_ENERGY)) continue;
+    if (!(XD->RadRate(Z, line) > 0.0 && XD->LineEnergy(Z, line) > TUBE_MINIMUM_ENERGY)) continue;
     for (shell = 0; shell < 4; shell++)
       if (line >= xrl_shell_first_line(shell) && line <= xrl_shell_last_line(shell)) break;
-    edge = xrl_EdgeEnergy(Z, shell);
+    edge = XD->EdgeEnergy(Z, shell);
     if (edge == 0.0 || edge > tube_voltage) continue;
     disc_line[ndisc] = line;
     disc_edge[ndisc] = edge;
-    disc[ndisc].energy = xrl_LineEnergy(Z, line);
+    disc[ndisc].energy = XD->LineEnergy(Z, line);
     ndisc++;
   }
   for (i = 0; i < ndisc; i++) {
@@ -205,7 +205,7 @@ int xmi_tube_ebel(xmi_layer *tube_anode, xmi_layer *tube_window, xmi_layer *tube
     p1 = logu0 * (0.49269 - 1.09870 * eta + 0.78557 * eta * eta);
     p2 = 0.70256 - 1.09865 * eta + 1.00460 * eta * eta + logu0;
     rhoz = rhozmax * (p1 / p2);
-    tau = xrl_CS_Total_Kissel(Z, disc[i].energy);
+    tau = XD->CS_Total_Kissel(Z, disc[i].energy);
     rhelp = tau * 2.0 * rhoz * sinfactor;
     if (rhelp > 0.0) {
       if (tube_transmission == 0)
@@ -216,13 +216,13 @@ int xmi_tube_ebel(xmi_layer *tube_anode, xmi_layer *tube_window, xmi_layer *tube
                 rhelp;
     }
     if (is_k)
-      I = rhelp * const2_K * oneovers * r * xrl_RadRate(Z, ln) * xrl_FluorYield(Z, 0);
+      I = rhelp * const2_K * oneovers * r * XD->RadRate(Z, ln) * XD->FluorYield(Z, 0);
     else if (ln <= xrl_shell_last_line(1))
-      I = rhelp * fcorr(Z) * 0.71E13 * oneovers * r * xrl_RadRate(Z, ln) * omega_l[Z - 1];
+      I = rhelp * fcorr(Z) * 0.71E13 * oneovers * r * XD->RadRate(Z, ln) * omega_l[Z - 1];
     else if (ln <= xrl_shell_last_line(2))
-      I = rhelp * fcorr(Z) * 2.70E13 * oneovers * r * xrl_RadRate(Z, ln) * omega_l[Z - 1];
+      I = rhelp * fcorr(Z) * 2.70E13 * oneovers * r * XD->RadRate(Z, ln) * omega_l[Z - 1];
     else
-      I = rhelp * 4.94E13 * oneovers * r * xrl_RadRate(Z, ln) * omega_l[Z - 1];
+      I = rhelp * 4.94E13 * oneovers * r * XD->RadRate(Z, ln) * omega_l[Z - 1];
     disc[i].horizontal_intensity = I;
     disc[i].distribution_type = XMI_ENERGY_DISCRETE_DISTRIBUTION_MONOCHROMATIC;
     disc[i].scale_parameter = 0.0;

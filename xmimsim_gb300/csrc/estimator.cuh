@@ -38,41 +38,51 @@ __device__ __forceinline__ void chan_add(const DevBundle<R> &b, const DevTally &
     atomicAdd(&t.chan[(size_t)n * b.nch + ch], (double)w);
 }
 
+template <typename R>
+__device__ __forceinline__ void chan_add_warp(const DevBundle<R> &b, const DevTally &t, int n, R E, R w, R *buf);
+
 /* xmi_compton_varred (src/xmi_variance_reduction.F90:752-947), the estimator
  * of the advanced Compton scattering: one scattered energy per shell of
  * element e, drawn from g for every shell with a non-zero share, each
  * weighted by that share; the spectrum gets every shell's energy.  Returns
  * the element's Compton history weight (the sum over shells).  base = the
- * event's pconv x pdir x weight (0 for an idle lane). */
+ * event's pconv x pdir x weight (0 for an idle lane).  ch_buf: the warp's
+ * channel buffer when all 32 lanes run the same element (their channel
+ * contributions are then grouped by channel), nullptr for per-lane atomics. */
 template <typename R>
 __device__ __noinline__ R compton_advanced_est(const DevBundle<R> &b, const DevTally &t, int e, const VrEvent<R> &ev,
-                                               R base, xmi_rng *g, bool valid, bool &ok) {
+                                               R base, xmi_rng *g, bool valid, bool &ok, R *ch_buf) {
   using T = cp_real<R>;
   T cdfs[XMI_CP_SH];
   const T E = (T)ev.E, th = (T)ev.theta, c = cos(th), sn = sin(th), sh = sin(th * (T)0.5);
   const T sum = cp_shell_cdfs<T>(b, e, E, c, sh * sh, cdfs);
   R total = (R)0;
-  if (sum == (T)0) return total;
+  const bool none = sum == (T)0;
+  if (none && !ch_buf) return total;
   const int ns = b.cp_nshell[e];
   for (int k = 0; k < ns; k++) {
-    const T sw = (T)b.cp_occ[e * XMI_CP_SH + k] * cdfs[k] / sum;
-    if (sw == (T)0) continue;
-    const T q = cp_shell_q<T>(b.cp_qinv[e] + (size_t)k * XMI_CP_N, (T)uni<R>(g) * cdfs[k]);
-    bool bad = false;
-    const T ec = cp_energy_from_q(E, q, c, sn, bad);
-    if (bad) {
-      if (valid) ok = false;
-      continue;
-    }
-    if (ec == (T)0) continue;
-    R mus_c[XMI_MAXL];
-    mu_calc(b, (R)ec, mus_c);
-    R murhod = (R)0;
+    R tw = (R)0;
+    T ec = (T)0;
+    const T sw = none ? (T)0 : (T)b.cp_occ[e * XMI_CP_SH + k] * cdfs[k] / sum;
+    if (sw != (T)0) {
+      const T q = cp_shell_q<T>(b.cp_qinv[e] + (size_t)k * XMI_CP_N, (T)uni<R>(g) * cdfs[k]);
+      bool bad = false;
+      ec = cp_energy_from_q(E, q, c, sn, bad);
+      if (bad) {
+        if (valid) ok = false;
+        ec = (T)0;
+      } else if (ec != (T)0) {
+        R mus_c[XMI_MAXL];
+        mu_calc(b, (R)ec, mus_c);
+        R murhod = (R)0;
 #pragma unroll
-    for (int j = 0; j < XMI_MAXL; j++) murhod += mus_c[j] * ev.rd[j];
-    const R tw = base * exp(-murhod) * (R)sw;
-    total += tw;
-    if (valid) chan_add(b, t, ev.n, (R)ec, tw);
+        for (int j = 0; j < XMI_MAXL; j++) murhod += mus_c[j] * ev.rd[j];
+        tw = base * exp(-murhod) * (R)sw;
+        total += tw;
+      }
+    }
+    if (ch_buf) chan_add_warp(b, t, ev.n, (R)ec, valid ? tw : (R)0, ch_buf);
+    else if (valid) chan_add(b, t, ev.n, (R)ec, tw);
   }
   return total;
 }
@@ -191,7 +201,7 @@ __device__ __forceinline__ void estimate_event(const DevBundle<R> &b, const DevT
     xmi_rng_init(&g, b.seed, (uint64_t)ev.id, vr_stream(n, i));
     if (Adv && b.use_adv_compton) {
       const R twa = compton_advanced_est(b, t, e, ev, live * (pconv * (ev.pC * qtab(b.sf[e], ev.q))) * ev.w, &g,
-                                         valid, ok);
+                                         valid, ok, (R *)nullptr);
       contribute<R, Uniform>(t, st, n_line + 2 * i + 1, hbase + rs + 1, twa);
     } else {
       bool cok = true;
@@ -343,7 +353,7 @@ __device__ __forceinline__ void estimate_event_uniform(const DevBundle<R> &b, co
     xmi_rng_init(&g, b.seed, (uint64_t)ev.id, vr_stream(n, i));
     if (Adv && b.use_adv_compton) {
       const R twa = compton_advanced_est(b, t, e, ev, live * (pconv * (ev.pC * qtab(b.sf[e], ev.q))) * ev.w, &g,
-                                         valid, ok);
+                                         valid, ok, s_ch);
       contribute<R, true>(t, st, st.n_line + 2 * i + 1, hbase + rs + 1, twa);
     } else {
       bool cok = true;

@@ -451,7 +451,7 @@ int xmi_init_input_escape_ratios(xmi_inputFPtr *p) {
 double xmi_layer_mu(const xmi_layer *layer, double E) {
   double rv = 0.0;
   int i;
-  for (i = 0; i < layer->n_elements; i++) rv += xrl_CS_Total_Kissel(layer->Z[i], E) * layer->weight[i];
+  for (i = 0; i < layer->n_elements; i++) rv += XD->CS_Total_Kissel(layer->Z[i], E) * layer->weight[i];
   return rv;
 }
 
@@ -487,17 +487,17 @@ static void cascade_coefficients(int Z, int cascade, double T[9][9]) {
   int s, t, l;
   memset(T, 0, sizeof(double) * 81);
   for (t = 0; t < 9; t++) {
-    double w = xrl_FluorYield(Z, t), a = xrl_AugerYield(Z, t);
+    double w = XD->FluorYield(Z, t), a = XD->AugerYield(Z, t);
     for (s = t + 1; s < 9; s++) {
       int same_group = (t >= 1 && t <= 3 && s <= 3) || (t >= 4 && s >= 4);
       if (same_group) {
-        if (ck_of[t][s] >= 0) T[t][s] = xrl_CosKronTransProb(Z, ck_of[t][s]);
+        if (ck_of[t][s] >= 0) T[t][s] = XD->CosKronTransProb(Z, ck_of[t][s]);
         continue;
       }
       if (rad)
         for (l = xrl_shell_first_line(t); l <= xrl_shell_last_line(t); l++)
-          if (xrl_line_upper_shell(l) == s) T[t][s] += w * xrl_RadRate(Z, l);
-      if (aug) T[t][s] += a * xrl_AugerVacancies(Z, t, s);
+          if (xrl_line_upper_shell(l) == s) T[t][s] += w * XD->RadRate(Z, l);
+      if (aug) T[t][s] += a * XD->AugerVacancies(Z, t, s);
     }
   }
 }
@@ -517,8 +517,8 @@ static void cascade_partials(double T[9][9], double edge_k, const double *part, 
 static void yield_corr(int Z, double *y) {
   double w[9], c[XMI_NCK];
   int s;
-  for (s = 0; s < 9; s++) w[s] = xrl_FluorYield(Z, s);
-  for (s = 0; s < XMI_NCK; s++) c[s] = xrl_CosKronTransProb(Z, s);
+  for (s = 0; s < 9; s++) w[s] = XD->FluorYield(Z, s);
+  for (s = 0; s < XMI_NCK; s++) c[s] = XD->CosKronTransProb(Z, s);
   y[0] = w[0];
   y[1] = w[1] + c[XMI_FL12] * w[2] + (c[XMI_FL13] + c[XMI_FL12] * c[XMI_FL23]) * w[3];
   y[2] = w[2] + c[XMI_FL23] * w[3];
@@ -548,7 +548,7 @@ static void theta_icdf(int Z, double E, int rayl, const double *rs, double *out)
   prev = 0.0;
   for (i = 1; i < NT; i++) {
     double th = i * h;
-    double f = (rayl ? xrl_DCS_Rayl(Z, E, th) : xrl_DCS_Compt(Z, E, th)) * sin(th);
+    double f = (rayl ? XD->DCS_Rayl(Z, E, th) : XD->DCS_Compt(Z, E, th)) * sin(th);
     sum += 0.5 * (prev + f) * h;
     cdf[i] = sum;
     prev = f;
@@ -577,8 +577,8 @@ static void doppler_icdf(int Z, const double *rs, double *out) {
   double h = 100.0 / (NP - 1), prev = 0.0, sum = 0.0;
   int i, k, s;
   for (s = 0; s < NS; s++) {
-    double eb = xrl_EdgeEnergy(Z, s);
-    nel[s] = xrl_ElectronConfig(Z, s);
+    double eb = XD->EdgeEnergy(Z, s);
+    nel[s] = XD->ElectronConfig(Z, s);
     if (eb < 0.005) eb = 0.005;
     sig[s] = sqrt(2.0 * eb / 0.0272114);
   }
@@ -646,6 +646,9 @@ typedef struct {
   double *cp_cdf, *cp_qinv;
 } z_tables;
 static z_tables z_cache[XRL_MAXZ + 1];
+static int z_cache_used = 0;
+
+int xmi_host_tables_built(void) { return z_cache_used; }
 static pthread_mutex_t z_cache_lock = PTHREAD_MUTEX_INITIALIZER;
 
 static void z_tables_fill(const int *Zs, int n, const double *energies, const double *rs, const double *dop_rs) {
@@ -677,12 +680,12 @@ static void z_tables_fill(const int *Zs, int n, const double *energies, const do
   for (k = 0; k < nt; k++) {
     int Z = todo[k];
     z_tables *zt = &z_cache[Z];
-    double scale = XRL_RE2 * XRL_AVOGNUM / xrl_AtomicWeight(Z);
+    double scale = XRL_RE2 * XRL_AVOGNUM / XD->AtomicWeight(Z);
     for (i = 0; i < XMI_NQ; i++) {
       double q = XMI_QMAX * i / (XMI_NQ - 1.0);
-      double ff = xrl_FF_Rayl(Z, q);
+      double ff = XD->FF_Rayl(Z, q);
       zt->ff2[i] = ff * ff * scale;
-      zt->sf[i] = xrl_SF_Compt(Z, q) * scale;
+      zt->sf[i] = XD->SF_Compt(Z, q) * scale;
     }
     zt->ready = 1;
   }
@@ -761,10 +764,10 @@ static void cp_tables_fill(const int *Zs, int n) {
     z_tables *zt = &z_cache[Z];
     int s, m = 0;
     for (s = 0; s < XRL_NSHELL_ALL && m < XMI_CP_SH; s++) {
-      const double occ = xrl_ElectronConfig(Z, s);
+      const double occ = XD->ElectronConfig(Z, s);
       double eb;
       if (s > 0 && !(occ > 0.0)) continue;
-      eb = xrl_EdgeEnergy(Z, s);
+      eb = XD->EdgeEnergy(Z, s);
       zt->cp_shell[m] = s;
       zt->cp_occ[m] = occ;
       zt->cp_edge[m] = eb;
@@ -877,6 +880,7 @@ int xmi_bundle_build(struct xmi_input_handle *in, struct xmi_tables_handle *t,
   const xmi_input *inp = in->input;
   const xmi_composition *comp = inp->composition;
   int cascade, i, j, e, s, n_pairs = 0, nonmono;
+  z_cache_used = 1; /* the atomic data source is fixed from here on */
   int zs[XMI_MAXL * 128];
   int nz = 0;
   double e_lo = 0.1, e_hi, ln_span, h_target;
@@ -928,9 +932,9 @@ int xmi_bundle_build(struct xmi_input_handle *in, struct xmi_tables_handle *t,
   b->elem_Z = (int *)malloc(sizeof(int) * nz);
   for (i = 0; i < nz; i++)
     if (b->n_elem == 0 || b->elem_Z[b->n_elem - 1] != zs[i]) b->elem_Z[b->n_elem++] = zs[i];
-  for (e = 0; e < b->n_elem; e++) xrl_prepare(b->elem_Z[e]);
+  for (e = 0; e < b->n_elem; e++) if (XD->prepare) XD->prepare(b->elem_Z[e]);
   for (j = 0; j < inp->absorbers->n_exc_layers; j++)
-    for (i = 0; i < inp->absorbers->exc_layers[j].n_elements; i++) xrl_prepare(inp->absorbers->exc_layers[j].Z[i]);
+    for (i = 0; i < inp->absorbers->exc_layers[j].n_elements; i++) if (XD->prepare) XD->prepare(inp->absorbers->exc_layers[j].Z[i]);
 
   b->n_layer_el = n_pairs;
   b->layer_el = (int *)malloc(sizeof(int) * n_pairs);
@@ -955,10 +959,10 @@ int xmi_bundle_build(struct xmi_input_handle *in, struct xmi_tables_handle *t,
     int Z = b->elem_Z[e];
     yield_corr(Z, &b->elem_yield_corr[9 * e]);
     for (s = 0; s < 9; s++) {
-      b->elem_fluor_yield[9 * e + s] = xrl_FluorYield(Z, s);
-      b->elem_edge[9 * e + s] = xrl_EdgeEnergy(Z, s);
+      b->elem_fluor_yield[9 * e + s] = XD->FluorYield(Z, s);
+      b->elem_edge[9 * e + s] = XD->EdgeEnergy(Z, s);
     }
-    for (s = 0; s < XMI_NCK; s++) b->elem_ck[XMI_NCK * e + s] = xrl_CosKronTransProb(Z, s);
+    for (s = 0; s < XMI_NCK; s++) b->elem_ck[XMI_NCK * e + s] = XD->CosKronTransProb(Z, s);
   }
 
   /* line slots */
@@ -977,7 +981,7 @@ int xmi_bundle_build(struct xmi_input_handle *in, struct xmi_tables_handle *t,
       for (s = 0; s < 9; s++) {
         b->elem_shell_off[10 * e + s] = n;
         for (l = xrl_shell_first_line(s); l <= xrl_shell_last_line(s); l++) {
-          double rr = xrl_RadRate(Z, l);
+          double rr = XD->RadRate(Z, l);
           if (rr <= 0.0) continue;
           if (n >= cap) {
             cap *= 2;
@@ -991,7 +995,7 @@ int xmi_bundle_build(struct xmi_input_handle *in, struct xmi_tables_handle *t,
           b->line_index[n] = l;
           b->line_elem[n] = e;
           b->line_shell[n] = s;
-          b->line_energy[n] = xrl_LineEnergy(Z, l);
+          b->line_energy[n] = XD->LineEnergy(Z, l);
           b->line_rate[n] = rr;
           b->line_channel[n] = -1;
           n++;
@@ -1019,7 +1023,7 @@ int xmi_bundle_build(struct xmi_input_handle *in, struct xmi_tables_handle *t,
     for (s = 0; s < 4; s++) {
       const int nt = s == 0 ? XMI_AUGER_K : XMI_AUGER_L, t0 = s == 0 ? 0 : XMI_AUGER_K + (s - 1) * XMI_AUGER_L;
       int t;
-      for (t = 0; t < nt; t++) b->auger_rate[((size_t)e * 4 + s) * XMI_AUGER_K + t] = xrl_AugerRate(b->elem_Z[e], t0 + t);
+      for (t = 0; t < nt; t++) b->auger_rate[((size_t)e * 4 + s) * XMI_AUGER_K + t] = XD->AugerRate(b->elem_Z[e], t0 + t);
     }
 
   /* energy grid with absorption edges as segment breakpoints */
@@ -1104,13 +1108,13 @@ int xmi_bundle_build(struct xmi_input_handle *in, struct xmi_tables_handle *t,
       for (e = 0; e < b->n_elem; e++) {
         int Z = b->elem_Z[e];
         double *r = &b->el_tab[((size_t)e * b->n_nodes + i) * XMI_EL_REC];
-        double cr = xrl_CS_Rayl(Z, E), cc = xrl_CS_Compt(Z, E), ph = xrl_CS_Photo_Total(Z, E);
+        double cr = XD->CS_Rayl(Z, E), cc = XD->CS_Compt(Z, E), ph = XD->CS_Photo_Total(Z, E);
         double tot = cr + cc + ph, part[9], P[9];
         r[XMI_REC_TOT] = tot;
         r[XMI_REC_PR] = cr / tot;
         r[XMI_REC_PRC] = cc / tot + cr / tot;
         r[XMI_REC_PHOTO] = ph;
-        for (s = 0; s < 9; s++) part[s] = r[XMI_REC_PART + s] = xrl_CS_Photo_Partial(Z, s, E);
+        for (s = 0; s < 9; s++) part[s] = r[XMI_REC_PART + s] = XD->CS_Photo_Partial(Z, s, E);
         cascade_partials(T[e], b->elem_edge[9 * e], part, E, P);
         for (s = 0; s < 9; s++) r[XMI_REC_XRF + s] = P[s];
       }

@@ -48,6 +48,10 @@ void xmi_bundle_set_run(struct xmi_input_handle *in, struct xmi_tables_handle *t
 double xmi_layer_mu(const xmi_layer *layer, double E);
 void xmi_solid_angle_axes(const struct xmi_input_handle *h, int nr, int nt, double *r_vals, double *t_vals);
 void xmi_set_error(const char *fmt, ...);
+/* 1 once the host tabulator has built a table of any element */
+int xmi_host_tables_built(void);
+/* the atomic data source in use (xmi_set_atomic_data) */
+#define XD (xmi_get_atomic_data())
 void xmi_log(int verbose, const char *fmt, ...);
 
 /* device side (engine.cu) */
