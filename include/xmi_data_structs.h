@@ -191,6 +191,44 @@ typedef struct _xmi_escape_ratios_options {
   double compton_output_energy_delta; /* default 0.1 keV */
 } xmi_escape_ratios_options;
 
+/* reference include/xmi_data_structs.h:337-399: the unpacked output of one
+ * simulation (xmi_output_raw2struct) -- spectra per interaction order and
+ * the histories per element, line and interaction number */
+typedef struct _xmi_counts {
+  double counts;
+  int interaction_number;
+} xmi_counts;
+
+typedef struct _xmi_fluorescence_line {
+  char *line_type;
+  double energy;
+  double total_counts;
+  int n_interactions;
+  xmi_counts *interactions;
+} xmi_fluorescence_line;
+
+typedef struct _xmi_fluorescence_line_counts {
+  int atomic_number;
+  double total_counts;
+  int n_lines;
+  xmi_fluorescence_line *lines;
+} xmi_fluorescence_line_counts;
+
+typedef struct _xmi_output {
+  float version;
+  char *inputfile;
+  char *outputfile;
+  xmi_input *input;
+  xmi_fluorescence_line_counts *brute_force_history;
+  xmi_fluorescence_line_counts *var_red_history;
+  int nbrute_force_history;
+  int nvar_red_history;
+  double **channels_conv;
+  double **channels_unconv;
+  int ninteractions;
+  int use_zero_interactions;
+} xmi_output;
+
 #ifdef __cplusplus
 }
 #endif

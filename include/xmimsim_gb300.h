@@ -122,6 +122,24 @@ int xmi_update_input_from_hdf5(xmi_inputFPtr inputFPtr, xmi_hdf5FPtr hdf5FPtr); 
 void xmi_free_hdf5_F(xmi_hdf5FPtr *hdf5FPtr);                    /* include/xmi_data.h:48 */
 int xmi_gpu_set_options(xmi_inputFPtr inputFPtr, const xmi_gpu_options *gpu);
 
+/* ---- output: unpacking and .xmso files ---- */
+/* GLib's error type, declared here only so that a caller's GError ** passes
+ * through; the library never sets it (the reason of a failure is available
+ * from xmi_gpu_last_error()) */
+typedef struct _GError GError;
+/* the raw outputs of xmi_main_msim (channels_unconv[(N+1)*nchannels],
+ * histories [100*385*N]) and the convolved spectra per order unpacked into
+ * an xmi_output: per element of the sample with counts, per line with
+ * counts, per interaction number with counts (src/xmi_data_structs.c
+ * :1371-1518).  The input is copied; free with xmi_output_free. */
+xmi_output *xmi_output_raw2struct(xmi_input *input, double *brute_history, double *var_red_history,
+                                  double **channels_conv, double *channels_unconv, char *inputfile,
+                                  int use_zero_interactions); /* include/xmi_data_structs.h:574 */
+void xmi_output_free(xmi_output *output);                   /* include/xmi_data_structs.h:406 */
+/* writes the output as an .xmso document (xmimsim-1.0 DTD), numbers with 17
+ * significant digits, without the GUI's SVG graphs (src/xmi_xml.c:1638) */
+int xmi_output_write_to_xml_file(xmi_output *output, const char *xmsofile, GError **error);
+
 /* ---- solid-angle grid (include/xmi_solid_angle.h:39) ---- */
 extern long hits_per_single; /* samples per grid point, src/xmi_solid_angle_f.F90:43-44 */
 void xmi_solid_angle_calculation(xmi_inputFPtr inputFPtr, xmi_solid_angle **solid_angle,

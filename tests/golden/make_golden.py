@@ -79,6 +79,19 @@ def main(ref: Path) -> None:
         "conv_last": xmso["spectrum_conv"][N].tolist(),
         "pileup_channel": 1077, "pileup_min_ratio": 100.0}) + "\n")
 
+    # the whole output of the srm1155 example: spectra of every order and both
+    # histories, for the round trip through the library's output writer
+    hist = {}
+    for tag in ("brute_force_history", "variance_reduction_history"):
+        hist[tag] = [[Z, name, sorted([int(k), c] for k, c in counts.items())]
+                     for (Z, name), counts in sorted(xmso[tag].items())]
+    (HERE / "srm1155_output.json").write_text(json.dumps({
+        "source": "examples/srm1155.xmso",
+        "n_interactions": N,
+        "spectrum_conv": xmso["spectrum_conv"][1:].tolist(),
+        "spectrum_unconv": xmso["spectrum_unconv"][1:].tolist(),
+        "histories": hist}) + "\n")
+
     kat = [{"ctr": [0, 0, 0, 0], "key": [0, 0], "out": [0x6627e8d5, 0xe169c58d, 0xbc57ac4c, 0x9b00dbd8]},
            {"ctr": [0xffffffff] * 4, "key": [0xffffffff] * 2,
             "out": [0x408f276d, 0x41c83b0e, 0xa20bc7c6, 0x6d5451fd]},

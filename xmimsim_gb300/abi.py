@@ -74,6 +74,29 @@ class XmiInput(C.Structure):
                 ("absorbers", C.POINTER(XmiAbsorbers)), ("detector", C.POINTER(XmiDetector))]
 
 
+class XmiCounts(C.Structure):
+    _fields_ = [("counts", C.c_double), ("interaction_number", C.c_int)]
+
+
+class XmiFluorescenceLine(C.Structure):
+    _fields_ = [("line_type", C.c_char_p), ("energy", C.c_double), ("total_counts", C.c_double),
+                ("n_interactions", C.c_int), ("interactions", C.POINTER(XmiCounts))]
+
+
+class XmiFluorescenceLineCounts(C.Structure):
+    _fields_ = [("atomic_number", C.c_int), ("total_counts", C.c_double), ("n_lines", C.c_int),
+                ("lines", C.POINTER(XmiFluorescenceLine))]
+
+
+class XmiOutput(C.Structure):
+    _fields_ = [("version", C.c_float), ("inputfile", C.c_char_p), ("outputfile", C.c_char_p),
+                ("input", C.POINTER(XmiInput)), ("brute_force_history", C.POINTER(XmiFluorescenceLineCounts)),
+                ("var_red_history", C.POINTER(XmiFluorescenceLineCounts)), ("nbrute_force_history", C.c_int),
+                ("nvar_red_history", C.c_int), ("channels_conv", C.POINTER(C.POINTER(C.c_double))),
+                ("channels_unconv", C.POINTER(C.POINTER(C.c_double))), ("ninteractions", C.c_int),
+                ("use_zero_interactions", C.c_int)]
+
+
 class XmiMainOptions(C.Structure):
     _fields_ = [("use_M_lines", C.c_int), ("use_cascade_auger", C.c_int), ("use_cascade_radiative", C.c_int),
                 ("use_variance_reduction", C.c_int), ("use_sum_peaks", C.c_int), ("use_escape_peaks", C.c_int),
@@ -185,6 +208,10 @@ PROTOTYPES = {
                                              C.c_ulonglong, c_double_p]),
     "xmi_gpu_last_graph": (C.c_int, [C.POINTER(C.c_int)]),
     "xmi_set_atomic_data": (C.c_int, [C.POINTER(XmiAtomicData)]),
+    "xmi_output_raw2struct": (C.POINTER(XmiOutput), [C.POINTER(XmiInput), c_double_p, c_double_p,
+                                                     C.POINTER(c_double_p), c_double_p, C.c_char_p, C.c_int]),
+    "xmi_output_free": (None, [C.POINTER(XmiOutput)]),
+    "xmi_output_write_to_xml_file": (C.c_int, [C.POINTER(XmiOutput), C.c_char_p, C.c_void_p]),
     "xmi_get_atomic_data": (C.POINTER(XmiAtomicData), []),
     "xmi_gpu_compton_kinematics": (C.c_int, [C.c_int, c_double_p, c_double_p, c_double_p, c_double_p,
                                              c_double_p]),

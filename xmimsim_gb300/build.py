@@ -26,7 +26,7 @@ CFLAGS = ["-std=gnu11", "-O2", "-fPIC", "-fopenmp", "-ffp-contract=off", "-Wall"
 NVFLAGS = ARCH + ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC",
                   "-Xcompiler", "-fopenmp"]
 
-HOST_SOURCES = ["xrlite.c", "atomic_data.c", "host.c", "ebel.c"]
+HOST_SOURCES = ["xrlite.c", "atomic_data.c", "host.c", "ebel.c", "xmso.c"]
 CUDA_SOURCES = ["engine.cu", "detector.cu", "mlp.cu"]
 ORACLE_SOURCES = ["oracle_transport.c", "oracle_detector.c"]
 
