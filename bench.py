@@ -758,8 +758,9 @@ def plain_arm(args, ws, rank, local):
                                              "l2": "inputs larger than L2 (angular tables exceed 129 MB)",
                                              "solid_angle_grid_s": grid_s}),
             "gpu_launches": sum(t["launches"] for t in tms),
-            "phases_ms_per_step": {k: statistics.mean(t[k + "_ms"] for t in tms)
-                                   for k in ("transport", "sort", "estimator")},
+            "phases_ms_per_step": dict({k: statistics.mean(t[k + "_ms"] for t in tms)
+                                        for k in ("transport", "sort", "estimator")},
+                                       off_grid_solid_angles=statistics.mean(t["surrogate_ms"] for t in tms)),
             "events_per_step": statistics.mean(t["events"] for t in tms),
             "e2e": {"value": n_hist * args.steps / wall, "unit": "histories/s",
                     "h2d_bytes_per_step": int(statistics.mean(t["h2d_bytes"] for t in tms)),
@@ -805,8 +806,9 @@ def precision_arm(args, ws, rank, local):
             "dtype": "f32 transport, f64 tallies", "data": "synthetic (config-1 sample under 10 nm Cr and 50 nm Au)",
             "config": workload_config(args, {"layers_cm": [l.thickness for l in spec.layers]}),
             "gpu_launches": sum(t["launches"] for t in tms),
-            "phases_ms_per_step": {k: statistics.mean(t[k + "_ms"] for t in tms)
-                                   for k in ("transport", "sort", "estimator")},
+            "phases_ms_per_step": dict({k: statistics.mean(t[k + "_ms"] for t in tms)
+                                        for k in ("transport", "sort", "estimator")},
+                                       off_grid_solid_angles=statistics.mean(t["surrogate_ms"] for t in tms)),
             "events_per_step": statistics.mean(t["events"] for t in tms),
             "e2e": {"value": n_hist * args.steps / wall, "unit": "histories/s",
                     "h2d_bytes_per_step": int(statistics.mean(t["h2d_bytes"] for t in tms)),
@@ -901,8 +903,10 @@ def surrogate_arm(args, ws, rank, local):
                     "h2d_bytes_per_step": int(statistics.mean(t["h2d_bytes"] for t in tms)),
                     "d2h_bytes_per_step": int(statistics.mean(t["d2h_bytes"] for t in tms))},
             "grid_path": {"value": n_hist * args.steps / (ksum_g / 1e3), "e2e": n_hist * args.steps / wall_g,
-                          "phases_ms_per_step": {k: statistics.mean(t[k + "_ms"] for t in tms_g)
-                                                 for k in ("transport", "sort", "estimator")},
+                          "phases_ms_per_step": dict({k: statistics.mean(t[k + "_ms"] for t in tms_g)
+                                                      for k in ("transport", "sort", "estimator")},
+                                                     off_grid_solid_angles=statistics.mean(t["surrogate_ms"]
+                                                                                           for t in tms_g)),
                           "job_s": grid_s + step_g, "job": "grid + one step"},
             "surrogate_path_job_s": train_s + step_s,
             "line_error": errs,

@@ -31,6 +31,7 @@ struct DevBundle {
   R zero_r, inv_gain_r; /* channel = (E - zero) / gain as (E - zero_r) * inv_gain_r */
   double det_radius, coll_radius, coll_height, coll_half_apex, coll_vertex_x;
   double d_source_slit, slit_x, slit_y;
+  double slit_ax, slit_ay; /* half-angles of the slit seen from the source, atan(slit / d / 2), from the host */
   double zbeg[XMI_MAXL], zend[XMI_MAXL];
   R thick_n[XMI_MAXL]; /* layer thickness along the sample normal, (zend - zbeg) n_z */
   R rho[XMI_MAXL];

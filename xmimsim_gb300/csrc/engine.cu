@@ -323,6 +323,8 @@ void fill_scalars(const xmi_bundle &h, xmi::DevBundle<R> &d) {
   d.d_source_slit = h.d_source_slit;
   d.slit_x = h.slit_x;
   d.slit_y = h.slit_y;
+  d.slit_ax = std::atan(h.slit_x / h.d_source_slit / 2.0);
+  d.slit_ay = std::atan(h.slit_y / h.d_source_slit / 2.0);
   for (int j = 0; j < XMI_MAXL; j++) {
     d.zbeg[j] = h.layer_zbeg[j];
     d.zend[j] = h.layer_zend[j];
@@ -1094,7 +1096,12 @@ static bool launch_single(DevState *s, xmi::DevBundle<R> &d, const xmi::DevTally
           &s->counters[1]);
   };
   auto surrogate = [&](const xmi::VrQueue<R> &vq, int *fb, unsigned long long *fb_count) -> int {
-    if (!d.use_surrogate) return 0;
+    if (!d.use_surrogate) {
+      /* the grid path: integrals of the events off the grid */
+      xmi_solid_angle_deferred(sizeof(R) == 8 ? 0 : 1, s->d_bundle, 1, vq.ev, vq.count, vq.cap, fb, fb_count,
+                               s->stream);
+      return 2;
+    }
     if (rec) {
       record_points_kernel<R><<<sms * 4, 256, 0, s->stream>>>(vq.ev, vq.count, vq.cap, rec->p, rec->r, rec->t, rec->n,
                                                                rec->max);
@@ -1316,10 +1323,14 @@ bool launch_batch(int n, DevState **st, xmi_hdf5FPtr *t, const xmi::DevTally *tl
   /* flags: [0] estimator error, [1] events, [2] integrator fallbacks of the
    * surrogate, [3] surrogate error */
   auto surrogate = [&](const xmi::VrQueue<R> &vq, int *fb, unsigned long long *fb_count) -> int {
-    if (!sg) return 0;
+    /* the integrals of the events off their configuration's grid first (a
+     * configuration served by the network leaves none), then the network */
+    xmi_solid_angle_deferred(sizeof(R) == 8 ? 0 : 1, db, n, vq.ev, vq.count, vq.cap, fb, fb_count, B.stream);
+    if (!sg) return 2;
+    cudaMemsetAsync(fb_count, 0, sizeof(unsigned long long), B.stream);
     xmi_surrogate_apply(sg, sizeof(R) == 8 ? 0 : 1, db, n, vq.ev, vq.count, vq.cap, &B.flags[2], fb, fb_count,
                         (int *)&B.flags[3], B.stream);
-    return 2;
+    return 4;
   };
   if (!run_chunks<R>(B.stream, B.q, first[n], N, n * XMI_MAXL * XMI_MAXN, vr, qev, &B.flags[1], transport,
                      surrogate, estimator, ph, graph))

@@ -449,6 +449,28 @@ __global__ void __launch_bounds__(256) omega_fallback_kernel(const DevBundle<R> 
   }
 }
 
+/* the queued events whose point lay off the solid-angle grid (sa_pending),
+ * appended (warp-aggregated) to fb_list for omega_fallback_kernel */
+template <typename R>
+__global__ void __launch_bounds__(256) collect_pending_kernel(const VrEvent<R> *ev, const unsigned long long *count,
+                                                              long long cap, int *fb_list,
+                                                              unsigned long long *fb_count) {
+  const long long n = (long long)*count < cap ? (long long)*count : cap;
+  const int lane = threadIdx.x & 31;
+  for (long long base = ((long long)blockIdx.x * blockDim.x + threadIdx.x) & ~31ll; base < n;
+       base += (long long)gridDim.x * blockDim.x) {
+    const long long i = base + lane;
+    const bool pend = i < n && ev[i].sa_pending != 0;
+    const unsigned m = __ballot_sync(0xffffffffu, pend);
+    if (!m) continue;
+    const int leader = __ffs(m) - 1;
+    unsigned long long pos = 0;
+    if (lane == leader) pos = atomicAdd(fb_count, (unsigned long long)__popc(m));
+    pos = __shfl_sync(0xffffffffu, pos, leader) + __popc(m & ((1u << lane) - 1u));
+    if (pend && (long long)pos < cap) fb_list[pos] = (int)i;
+  }
+}
+
 /* ---------------- training ---------------- */
 /* transposed hidden weights W_l^T (l = 1..3) as K-major tiles: element
  * (in, out) = W_l[out][in]; the B operand of dX = dZ W_l */
@@ -1452,6 +1474,28 @@ int xmi_gpu_solid_angle_points(xmi_inputFPtr in, int n, const double *r, const d
   cudaFree(o_d);
   if (!ok) xmi_set_error("xmi_gpu_solid_angle_points: CUDA error");
   return ok ? 1 : 0;
+}
+
+int xmi_solid_angle_deferred(int precision, const void *dev_bundles, int n_cfg, void *events,
+                             const unsigned long long *count, long long cap, int *fb_list,
+                             unsigned long long *fb_count, void *stream) {
+  using namespace xmi::mlp;
+  int dev = 0, sms = 1;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaStream_t st = (cudaStream_t)stream;
+  if (precision == 0) {
+    collect_pending_kernel<double><<<sms * 4, 256, 0, st>>>((const xmi::VrEvent<double> *)events, count, cap, fb_list,
+                                                           fb_count);
+    omega_fallback_kernel<double><<<sms * 8, 256, 0, st>>>((const xmi::DevBundle<double> *)dev_bundles, n_cfg,
+                                                          (xmi::VrEvent<double> *)events, fb_list, fb_count, cap);
+  } else {
+    collect_pending_kernel<float><<<sms * 4, 256, 0, st>>>((const xmi::VrEvent<float> *)events, count, cap, fb_list,
+                                                          fb_count);
+    omega_fallback_kernel<float><<<sms * 8, 256, 0, st>>>((const xmi::DevBundle<float> *)dev_bundles, n_cfg,
+                                                         (xmi::VrEvent<float> *)events, fb_list, fb_count, cap);
+  }
+  return cudaGetLastError() == cudaSuccess ? 1 : 0;
 }
 
 int xmi_gpu_surrogate_report(xmi_inputFPtr in, double *report) {

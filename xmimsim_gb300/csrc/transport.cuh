@@ -108,8 +108,10 @@ __device__ __forceinline__ bool plane_step(const double *p, const R *d, const do
   ip[0] = s * dd[0] + p[0];
   ip[1] = s * dd[1] + p[1];
   ip[2] = s * dd[2] + p[2];
-  double e0 = p[0] - ip[0], e1 = p[1] - ip[1], e2 = p[2] - ip[2];
-  *dist = sqrt(e0 * e0 + e1 * e1 + e2 * e2);
+  if (dist) { /* the distance is optional: the first-layer shift does not use it */
+    double e0 = p[0] - ip[0], e1 = p[1] - ip[1], e2 = p[2] - ip[2];
+    *dist = sqrt(e0 * e0 + e1 * e1 + e2 * e2);
+  }
   return true;
 }
 
@@ -499,7 +501,7 @@ __device__ __forceinline__ void sa_coords(const DevBundle<R> &b, const double *c
 /* xmi_get_solid_angle (src/xmi_solid_angle_f.F90:712-801) */
 template <typename R>
 __device__ R get_solid_angle(const DevBundle<R> &b, const double *coords, const Photon<R> &p, const DevTally &t,
-                             bool &ok) {
+                             bool &ok, bool *deferred = nullptr, R *def_r = nullptr, R *def_t = nullptr) {
   double dv[3] = {coords[0] - b.p_det[0], coords[1] - b.p_det[1], coords[2] - b.p_det[2]};
   R dn[3];
   double rr;
@@ -526,9 +528,18 @@ __device__ R get_solid_angle(const DevBundle<R> &b, const double *coords, const 
   int p1 = findpos_u<double>(b.sa_r, b.sa_nr, (double)r, b.sa_r0, b.sa_rinv);
   int p2 = findpos_u<double>(b.sa_t, b.sa_nt, th, b.sa_t0, b.sa_tinv);
   if (p1 == -1 || p2 == -1) {
+    atomicAdd(&t.counters[0], 1ull);
+    if (deferred) {
+      /* the caller leaves the integral to a warp-parallel pass over the
+       * queued events (the same draws: sample i is Philox block i of the
+       * stream below) */
+      *deferred = true;
+      *def_r = r;
+      *def_t = theta;
+      return (R)1;
+    }
     xmi_rng g;
     xmi_rng_init(&g, b.seed, (uint64_t)p.id, 0x80000000u | (uint32_t)p.n_int);
-    atomicAdd(&t.counters[0], 1ull);
     return single_solid_angle(b, r, theta, &g, b.sa_hits);
   }
   /* bilinear on the grid; axes are FP64, values in R */
@@ -881,6 +892,7 @@ struct __align__(16) VrEvent {
   int node, layer, n, h_slot; /* h_slot >= 0: exciting line of a fluorescence photon */
   long long id;
   int cfg;           /* configuration of a batched run (0 otherwise) */
+  int sa_pending;    /* 1: off the solid-angle grid; the integral at (sa_r, sa_t) is still to be multiplied in */
 };
 
 /* sort key of an event: configuration, layer, interaction order */
@@ -985,13 +997,19 @@ __device__ bool vr_prologue(const DevBundle<R> &b, const Photon<R> &p, const Dev
   for (int j = 0; j < XMI_MAXL; j++) murhod += p.mus[j] * ev.rd[j];
   ev.pesc_rayl = exp(-murhod);
   R omega;
+  ev.sa_pending = 0;
   if (b.use_surrogate) {
     /* the solid angle comes later from the surrogate network: the factors
      * below are stored without it, with the point's (r, theta) */
     sa_coords(b, p.c, ev.sa_r, ev.sa_t);
     omega = (R)1;
   } else {
-    omega = get_solid_angle(b, p.c, p, t, ok);
+    /* a point off the grid needs a 5000-sample integral: it is left to the
+     * warp-parallel pass before the estimator (xmi_solid_angle_deferred)
+     * instead of one thread of the step kernel */
+    bool deferred = false;
+    omega = get_solid_angle(b, p.c, p, t, ok, &deferred, &ev.sa_r, &ev.sa_t);
+    ev.sa_pending = deferred ? 1 : 0;
   }
   ev.pdir_fluo = omega / (R)4 / (R)kPi;
   locate(b, p.E, ev.node, ev.f);
@@ -1655,7 +1673,8 @@ __device__ bool start_photon(const DevBundle<R> &b, const xmi_source_item &it, l
   /* xmi_coords_dir */
   double x1, y1;
   if (fabs(it.sigma_x * it.sigma_y) < (double)1.0e-20f) {
-    double x1m = atan(b.slit_x / b.d_source_slit / 2.0), y1m = atan(b.slit_y / b.d_source_slit / 2.0);
+    /* atan(slit / d_source_slit / 2), a constant of the run computed once on the host */
+    const double x1m = b.slit_ax, y1m = b.slit_ay;
     double u = xmi_rng_uniform(&g);
     x1 = x1m * (-1.0 * (1.0 - u) + 1.0 * u);
     u = xmi_rng_uniform(&g);
@@ -1668,7 +1687,12 @@ __device__ bool start_photon(const DevBundle<R> &b, const xmi_source_item &it, l
     p.c[1] = ran_gauss<double>(&g, it.sigma_y) - b.d_source_slit * sin(y1);
     p.c[2] = 0.0;
   }
-  {
+  if constexpr (sizeof(R) == 4) {
+    /* FP32 direction: the FP64 tangent, square root and divisions are slow on
+     * this GPU and the result is stored in FP32 anyway */
+    const float dx = tanf((float)x1), dy = tanf((float)y1), inv = 1.0f / sqrtf(dx * dx + dy * dy + 1.0f);
+    p.d[0] = dx * inv; p.d[1] = dy * inv; p.d[2] = inv;
+  } else {
     double dx = tan(x1), dy = tan(y1), dz = 1.0, nn = sqrt(dx * dx + dy * dy + dz * dz);
     p.d[0] = (R)(dx / nn); p.d[1] = (R)(dy / nn); p.d[2] = (R)(dz / nn);
   }
@@ -1694,7 +1718,7 @@ __device__ bool start_photon(const DevBundle<R> &b, const xmi_source_item &it, l
     if (p.layer < 0) return false;
   } else {
     double ip[3], dd;
-    if (!plane_step(p.c, p.d, b.n_sample, b.zbeg[0], ip, &dd)) return false;
+    if (!plane_step(p.c, p.d, b.n_sample, b.zbeg[0], ip, sizeof(R) == 4 ? nullptr : &dd)) return false;
     p.c[0] = ip[0]; p.c[1] = ip[1]; p.c[2] = ip[2];
     p.layer = 0;
   }

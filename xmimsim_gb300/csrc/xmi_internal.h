@@ -70,6 +70,13 @@ void xmi_surrogate_free(void *sg);
 int xmi_surrogate_apply(const void *sg, int precision, const void *dev_bundles, int n_cfg, void *events,
                         const unsigned long long *count, long long cap, unsigned long long *fallbacks, int *fb_list,
                         unsigned long long *fb_count, int *err, void *stream);
+/* The grid path's off-grid solid angles: the queued events that the step
+ * kernel flagged (sa_pending) get the 5000-sample integral at their (r,
+ * theta), one warp per event, draw for draw as the serial integral; fb_list
+ * (cap entries, *fb_count zeroed by the caller); on stream */
+int xmi_solid_angle_deferred(int precision, const void *dev_bundles, int n_cfg, void *events,
+                             const unsigned long long *count, long long cap, int *fb_list,
+                             unsigned long long *fb_count, void *stream);
 
 #ifdef __cplusplus
 }
