@@ -112,6 +112,9 @@ def parse():
     p.add_argument("--epochs-surrogate", type=int, default=32, help="training epochs of the surrogate workload")
     p.add_argument("--n-train-surrogate", type=int, default=2_000_000,
                    help="training points of the surrogate workload (uniform over the sample volume)")
+    p.add_argument("--surrogate-points", default="volume", choices=["volume", "pilot"],
+                   help="surrogate workload: train on points uniform over the sample volume (the workload's "
+                        "definition) or on the estimator's query points of a pilot run")
     p.add_argument("--precision", default="fp32", choices=["fp64", "fp32"])
     p.add_argument("--cpu-sample", type=int, default=1000000,
                    help="photons of the CPU-baseline sample (spread over all configurations by budget)")
@@ -843,8 +846,16 @@ def surrogate_arm(args, ws, rank, local):
     g_sur = gpu_options(precision=1, seed=seed, use_surrogate=1, surrogate_tolerance=args.tolerance, grid_n=1000)
     sur = Simulation(spec, options=options, gpu=g_sur)
     t0 = time.perf_counter()
-    rep = sur.build_surrogate(n_train=args.n_train_surrogate, hits_train=args.hits_train,
-                              epochs=args.epochs_surrogate, hits_check=args.hits_check)
+    if args.surrogate_points == "pilot":
+        pil = Simulation(spec, options=options, gpu=gpu_options(precision=1, seed=seed ^ 0x1234, use_surrogate=1))
+        pr, pt = pil.sample_event_points(share=min(1.0, 2.0 * args.n_train_surrogate / n_hist),
+                                         max_points=args.n_train_surrogate)
+        pil.close()
+        rep = sur.build_surrogate_points(pr, pt, hits_train=args.hits_train, epochs=args.epochs_surrogate,
+                                         hits_check=args.hits_check)
+    else:
+        rep = sur.build_surrogate(n_train=args.n_train_surrogate, hits_train=args.hits_train,
+                                  epochs=args.epochs_surrogate, hits_check=args.hits_check)
     train_s = time.perf_counter() - t0
     # held-out validation at the estimator's own query points (a pilot run
     # with another seed), judged by the integrator with 2^24 samples per point
@@ -886,7 +897,9 @@ def surrogate_arm(args, ws, rank, local):
              "surrogate": dict(rep, n_train=args.n_train_surrogate, hits_train=args.hits_train,
                                epochs=args.epochs_surrogate,
                                tolerance=args.tolerance, hits_check=args.hits_check, wall_s=train_s,
-                               sampling="uniform over the sample volume (2 cm around the beam axis)"),
+                               sampling="uniform over the sample volume (2 cm around the beam axis)"
+                               if args.surrogate_points == "volume" else
+                               "the estimator's query points of a pilot run (another seed)"),
              "held_out": held_out,
              "l2": "tables and grid above 129 MB: no; inputs smaller than L2, no flush between steps"}
     line = {"metric": PLAIN_METRIC + " (surrogate-served transport)", "value": n_hist * args.steps / (ksum / 1e3),
