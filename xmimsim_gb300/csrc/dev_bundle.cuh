@@ -13,6 +13,39 @@ constexpr double kEnergyThreshold = 1.0;  /* src/xmi_aux_f.F90:673 */
 constexpr double kEnergyMax = 200.0;      /* src/xmi_aux_f.F90:674 */
 constexpr double kPi = 3.14159265358979323846;
 
+/* FP32 working copy of a source item, read by the FP32 transport's source
+ * sampling instead of the FP64 fields.  Intensities are divided by
+ * max(i0, i1): the trapezoid's inverse CDF and the horizontal share are
+ * ratios, unchanged by a common scale, and the scaled values stay far from
+ * FP32 overflow. */
+struct __align__(16) ItemF {
+  float e0, de, inv_de, y1;  /* interval start (line energy), width, 1 / width, intensity at e0 */
+  float m, area, h0, dh;     /* slope, area, horizontal intensity at e0 and its change over the interval */
+  float i0, di, weight, scale; /* total intensity at e0 and its change, photon weight, line width */
+  int gauss, pad0, pad1, pad2; /* 1: Gaussian beam (sigma_x * sigma_y != 0) */
+};
+
+__host__ inline ItemF item_f_of(const xmi_source_item &it) {
+  ItemF f = {};
+  const double big = it.i0 > it.i1 ? it.i0 : it.i1, s = big > 0.0 ? 1.0 / big : 1.0;
+  f.e0 = (float)it.e0;
+  if (it.kind == 0) {
+    f.de = (float)(it.e1 - it.e0);
+    f.inv_de = (float)(1.0 / (it.e1 - it.e0));
+    f.y1 = (float)(it.trap[4] * s);
+    f.m = (float)(it.trap[1] * s);
+    f.area = (float)(it.trap[0] * s);
+    f.h0 = (float)(it.h0 * s);
+    f.dh = (float)((it.h1 - it.h0) * s);
+    f.i0 = (float)(it.i0 * s);
+    f.di = (float)((it.i1 - it.i0) * s);
+  }
+  f.weight = (float)it.weight;
+  f.scale = (float)it.scale;
+  f.gauss = (it.sigma_x * it.sigma_y < 0.0 ? -(it.sigma_x * it.sigma_y) : it.sigma_x * it.sigma_y) < (double)1.0e-20f ? 0 : 1;
+  return f;
+}
+
 /* Device copy of an xmi_bundle.  R is the precision of the physics tables
  * and of the per-photon arithmetic except positions, which are always FP64
  * (FP32 cannot resolve 10 nm layers at 10-100 cm from the origin). */
@@ -32,6 +65,8 @@ struct DevBundle {
   double det_radius, coll_radius, coll_height, coll_half_apex, coll_vertex_x;
   double d_source_slit, slit_x, slit_y;
   double slit_ax, slit_ay; /* half-angles of the slit seen from the source, atan(slit / d / 2), from the host */
+  R slit_ax_r, slit_ay_r, d_source_slit_r;
+  double hbeg0; /* height of the first layer's entry plane along the sample normal, zbeg[0] n_z */
   double zbeg[XMI_MAXL], zend[XMI_MAXL];
   R thick_n[XMI_MAXL]; /* layer thickness along the sample normal, (zend - zbeg) n_z */
   R rho[XMI_MAXL];
@@ -56,6 +91,7 @@ struct DevBundle {
    * by every bundle on the device */
   const R *const *rayl_icdf, *const *compt_icdf, *const *dop_icdf, *const *ff2, *const *sf;
   const xmi_source_item *items;
+  const ItemF *items_f;        /* [n_items] FP32 working copies (FP32 transport) */
   const long long *item_first; /* [n_items] global id of the first photon */
   const double *sa_r, *sa_t;
   const R *sa_grid;

@@ -116,6 +116,7 @@ struct DevState {
   xmi::DevBundle<float> b32;
   /* run buffers */
   xmi_source_item *items = nullptr;
+  xmi::ItemF *items_f = nullptr;
   long long *item_first = nullptr;
   int items_cap = 0;
   double *sa_r = nullptr, *sa_t = nullptr, *sa_g64 = nullptr;
@@ -325,6 +326,10 @@ void fill_scalars(const xmi_bundle &h, xmi::DevBundle<R> &d) {
   d.slit_y = h.slit_y;
   d.slit_ax = std::atan(h.slit_x / h.d_source_slit / 2.0);
   d.slit_ay = std::atan(h.slit_y / h.d_source_slit / 2.0);
+  d.slit_ax_r = (R)d.slit_ax;
+  d.slit_ay_r = (R)d.slit_ay;
+  d.d_source_slit_r = (R)h.d_source_slit;
+  d.hbeg0 = h.layer_zbeg[0] * h.n_sample[2];
   for (int j = 0; j < XMI_MAXL; j++) {
     d.zbeg[j] = h.layer_zbeg[j];
     d.zend[j] = h.layer_zend[j];
@@ -461,6 +466,7 @@ void xmi_dev_free_tables(struct xmi_tables_handle *t) {
   s->d64.release();
   s->d32.release();
   cudaFree(s->items);
+  cudaFree(s->items_f);
   cudaFree(s->item_first);
   cudaFree(s->sa_r);
   cudaFree(s->sa_t);
@@ -917,19 +923,25 @@ static bool stage_run(DevState *s, xmi::DevBundle<R> &d, const xmi_bundle &h, xm
   for (int i = 1; i < h.n_items; i++) first[i] = first[i - 1] + h.items[i - 1].n_photons;
   if (h.n_items > s->items_cap) {
     cudaFree(s->items);
+    cudaFree(s->items_f);
     cudaFree(s->item_first);
     s->items = nullptr;
+    s->items_f = nullptr;
     s->item_first = nullptr;
     s->items_cap = 0;
     if (!cuda_ok(cudaMalloc(&s->items, sizeof(xmi_source_item) * h.n_items), "cudaMalloc items") ||
+        !cuda_ok(cudaMalloc(&s->items_f, sizeof(xmi::ItemF) * h.n_items), "cudaMalloc items") ||
         !cuda_ok(cudaMalloc(&s->item_first, sizeof(long long) * h.n_items), "cudaMalloc items"))
       return false;
     s->items_cap = h.n_items;
   }
   if (h.n_items > 0) {
+    std::vector<xmi::ItemF> items_f(h.n_items);
+    for (int i = 0; i < h.n_items; i++) items_f[i] = xmi::item_f_of(h.items[i]);
     cudaMemcpyAsync(s->items, h.items, sizeof(xmi_source_item) * h.n_items, cudaMemcpyHostToDevice, s->stream);
+    cudaMemcpyAsync(s->items_f, items_f.data(), sizeof(xmi::ItemF) * h.n_items, cudaMemcpyHostToDevice, s->stream);
     cudaMemcpyAsync(s->item_first, first.data(), sizeof(long long) * h.n_items, cudaMemcpyHostToDevice, s->stream);
-    g_timing.h2d_bytes += (long long)(sizeof(xmi_source_item) + sizeof(long long)) * h.n_items;
+    g_timing.h2d_bytes += (long long)(sizeof(xmi_source_item) + sizeof(xmi::ItemF) + sizeof(long long)) * h.n_items;
   }
   /* solid-angle grid (kept on the device while the caller's grid is the same) */
   if (h.sa_nr > 0 && (s->sa_src != h.sa_grid || s->sa_n != h.sa_nr * h.sa_nt)) {
@@ -974,6 +986,7 @@ static bool stage_run(DevState *s, xmi::DevBundle<R> &d, const xmi_bundle &h, xm
   tl.chan = s->tally + 2 * nh;
   tl.counters = s->counters;
   d.items = s->items;
+  d.items_f = s->items_f;
   d.item_first = s->item_first;
   d.sa_r = s->sa_r;
   d.sa_t = s->sa_t;

@@ -506,7 +506,9 @@ __global__ void event_key_histogram(const int *key, const unsigned long long *co
        base += (long long)gridDim.x * blockDim.x) {
     const long long i = base + lane;
     const int k = i < n ? key[i] : -1;
-    const unsigned peers = __match_any_sync(0xffffffffu, k);
+    /* consecutive events mostly share their key: one vote settles that case */
+    const unsigned peers = __all_sync(0xffffffffu, k == __shfl_sync(0xffffffffu, k, 0)) ? 0xffffffffu
+                                                                                        : __match_any_sync(0xffffffffu, k);
     if (k >= 0 && k < nkeys && lane == __ffs(peers) - 1) atomicAdd(&hist[k], (unsigned)__popc(peers));
   }
 }
@@ -548,7 +550,8 @@ __global__ void event_key_scatter(const int *key, const unsigned long long *coun
        base += (long long)gridDim.x * blockDim.x) {
     const long long i = base + lane;
     const int k = i < n ? key[i] : -1;
-    const unsigned peers = __match_any_sync(0xffffffffu, k);
+    const unsigned peers = __all_sync(0xffffffffu, k == __shfl_sync(0xffffffffu, k, 0)) ? 0xffffffffu
+                                                                                        : __match_any_sync(0xffffffffu, k);
     if (k >= 0 && k < nkeys) {
       const int leader = __ffs(peers) - 1;
       unsigned pos = 0;

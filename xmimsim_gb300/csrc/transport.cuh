@@ -1615,9 +1615,112 @@ __device__ bool simulate_photon(const DevBundle<R> &b, Photon<R> &p, const DevTa
 /* ---------------- source sampling (src/xmi_main.F90:319-858) ---------------- */
 template <typename R>
 __device__ __forceinline__ R ran_gauss(xmi_rng *g, R sigma) {
-  double u1 = xmi_rng_uniform(g), u2 = xmi_rng_uniform(g);
-  if (u1 <= 0.0) u1 = 1.0 / 9007199254740992.0;
-  return (R)(sigma * sqrt(-2.0 * log(u1)) * cos(2.0 * kPi * u2));
+  if constexpr (sizeof(R) == 4) {
+    /* Box-Muller in FP32 on the same two draws */
+    float u1 = uni<float>(g);
+    const float u2 = uni<float>(g);
+    if (u1 <= 0.0f) u1 = 0x1p-25f;
+    return sigma * sqrtf(-2.0f * logf(u1)) * cosf((float)(2.0 * kPi) * u2);
+  } else {
+    double u1 = xmi_rng_uniform(g), u2 = xmi_rng_uniform(g);
+    if (u1 <= 0.0) u1 = 1.0 / 9007199254740992.0;
+    return (R)(sigma * sqrt(-2.0 * log(u1)) * cos(2.0 * kPi * u2));
+  }
+}
+
+/* FP32 source sampling of one photon (energy, weight, direction, position on
+ * the first layer's entry plane): the same draws and distributions as the
+ * FP64 path below, without FP64 arithmetic except the position.
+ * The trapezoid's inverse CDF is the root t = E - x1 of
+ * m/2 t^2 + y1 t - area u = 0 in [0, x2 - x1] (xmi_ran_trap), written as
+ * 2 area u / (y1 + sqrt(y1^2 + 2 m area u)), which does not cancel. */
+__device__ __forceinline__ bool start_photon_f32(const DevBundle<float> &b, const xmi_source_item &it, long long j, Photon<float> &p,
+                                 bool &skip) {
+  xmi_rng g;
+  xmi_rng_init(&g, b.seed, (uint64_t)p.id, 0u);
+  skip = false;
+  const ItemF &f = b.items_f[&it - b.items];
+  float hvr = 0.0f;
+  if (it.kind == 0) {
+    const float du = f.area * uni<float>(&g);
+    const float disc = fmaxf(fmaf(2.0f * f.m, du, f.y1 * f.y1), 0.0f);
+    const float den = f.y1 + sqrtf(disc);
+    float t = den > 0.0f ? 2.0f * du / den : 0.0f;
+    t = fminf(fmaxf(t, 0.0f), f.de);
+    p.E = f.e0 + t;
+    const float fr = t * f.inv_de;
+    hvr = fmaf(f.dh, fr, f.h0) / fmaf(f.di, fr, f.i0);
+    int node;
+    float fl;
+    locate(b, p.E, node, fl);
+    const float ex0 = XMI_LDG(b.exc_tab, node, b.n_nodes, 20), ex1 = XMI_LDG(b.exc_tab, node + 1, b.n_nodes, 20);
+    const float exc_corr = expf(-(ex0 + fl * (ex1 - ex0)));
+    mu_calc(b, p.E, p.mus);
+    p.w = f.weight * exc_corr;
+  } else {
+    if (it.dist_type == 1) {
+      p.E = ran_gauss<float>(&g, f.scale) + f.e0;
+      if (p.E <= (float)kEnergyThreshold || p.E > (float)kEnergyMax) { skip = true; return true; }
+    } else if (it.dist_type == 2) {
+      float u;
+      do { u = uni<float>(&g); } while (u == 0.5f);
+      p.E = f.scale * tanf((float)kPi * u) + f.e0;
+      if (!(p.E > (float)kEnergyThreshold && p.E <= (float)kEnergyMax)) { skip = true; return true; }
+    } else {
+      p.E = f.e0;
+    }
+    mu_calc(b, p.E, p.mus);
+    p.w = f.weight;
+  }
+  /* xmi_coords_dir */
+  float x1, y1;
+  double h = 0.0;
+  if (!f.gauss) {
+    x1 = b.slit_ax_r * fmaf(2.0f, uni<float>(&g), -1.0f);
+    y1 = b.slit_ay_r * fmaf(2.0f, uni<float>(&g), -1.0f);
+    p.c[0] = p.c[1] = p.c[2] = 0.0;
+  } else {
+    x1 = ran_gauss<float>(&g, (float)it.sigma_xp);
+    y1 = ran_gauss<float>(&g, (float)it.sigma_yp);
+    p.c[0] = (double)(ran_gauss<float>(&g, (float)it.sigma_x) - b.d_source_slit_r * sinf(x1));
+    p.c[1] = (double)(ran_gauss<float>(&g, (float)it.sigma_y) - b.d_source_slit_r * sinf(y1));
+    p.c[2] = 0.0;
+    h = p.c[0] * b.n_sample[0] + p.c[1] * b.n_sample[1];
+  }
+  const float dx = tanf(x1), dy = tanf(y1), inv = 1.0f / sqrtf(dx * dx + dy * dy + 1.0f);
+  p.d[0] = dx * inv; p.d[1] = dy * inv; p.d[2] = inv;
+  p.theta = acosf(p.d[2]);
+  p.phi = atan2f(p.d[1], p.d[0]);
+  bool horizontal;
+  if (it.kind == 0) horizontal = uni<float>(&g) <= hvr;
+  else horizontal = (double)(it.local0 + j + 1) <= it.hor_ver_ratio;
+  if (horizontal) { p.el[0] = 0.0f; p.el[1] = 1.0f; p.el[2] = 0.0f; }
+  else { p.el[0] = 1.0f; p.el[1] = 0.0f; p.el[2] = 0.0f; }
+  p.we = p.w;
+  const float cosalfa = rdot(p.el, p.d);
+  if (fabsf(cosalfa) > 1.0f) return false;
+  const float c_ae = 1.0f / sinf(acosf(cosalfa)), c_be = -c_ae * cosalfa;
+#pragma unroll
+  for (int k = 0; k < 3; k++) p.el[k] = c_ae * p.el[k] + c_be * p.d[k];
+  /* xmi_photon_shift_first_layer: the source lies before the first layer
+   * (zbeg[0] > 0 after xmi_init_input), so the photon moves onto its entry
+   * plane; the step's 1/cos is FP32 (the lateral position is off by ~1e-7
+   * of the source distance) and the height is set to the plane's in FP64 */
+  p.layer = -1;
+  if (p.c[2] >= b.zbeg[0]) {
+    for (int i = 0; i < b.n_layers; i++)
+      if (p.c[2] < b.zend[i]) { p.layer = i; break; }
+    if (p.layer < 0) return false;
+  } else {
+    const float itn = rdot(p.d, b.n_sample_r);
+    if (itn == 0.0f) return false;
+    const float sw = (float)(b.hbeg0 - h) / itn;
+#pragma unroll
+    for (int k = 0; k < 3; k++) p.c[k] += (double)(sw * p.d[k]);
+    set_height(p.c, b.n_sample, b.hbeg0);
+    p.layer = 0;
+  }
+  return true;
 }
 
 template <typename R>
@@ -1762,7 +1865,10 @@ __device__ __forceinline__ bool init_photon(const DevBundle<R> &b, const DevTall
   p.h_slot = 0;
   p.elem = 0;
   bool skip;
-  if (!start_photon(b, it, j, p, skip)) { set_error(t, kErrSource); return false; }
+  bool ok;
+  if constexpr (sizeof(R) == 4) ok = start_photon_f32(b, it, j, p, skip);
+  else ok = start_photon(b, it, j, p, skip);
+  if (!ok) { set_error(t, kErrSource); return false; }
   return !skip;
 }
 

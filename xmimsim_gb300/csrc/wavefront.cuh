@@ -75,11 +75,21 @@ __global__ void __launch_bounds__(128) wf_start(DevBundle<R> b0, DevTally t0, co
     int c = 0;
     long long wl = w;
     if (Batched) {
-      int lo = 0, hi = n_cfg - 1;
-      while (lo < hi) {
-        int mid = (lo + hi + 1) >> 1;
-        if (w >= __ldg(cfg_first + mid)) lo = mid; else hi = mid - 1;
+      /* the warp's work indices are consecutive: the first active lane finds
+       * its configuration by bisection and every lane steps forward from it
+       * (a warp spans few configurations) */
+      const unsigned act = __activemask();
+      const int lead = __ffs(act) - 1;
+      int lo = 0;
+      if ((int)(threadIdx.x & 31) == lead) {
+        int hi = n_cfg - 1;
+        while (lo < hi) {
+          int mid = (lo + hi + 1) >> 1;
+          if (w >= __ldg(cfg_first + mid)) lo = mid; else hi = mid - 1;
+        }
       }
+      lo = __shfl_sync(act, lo, lead);
+      while (lo + 1 < n_cfg && w >= __ldg(cfg_first + lo + 1)) lo++;
       c = lo;
       wl = w - __ldg(cfg_first + lo);
     }
@@ -102,8 +112,11 @@ __global__ void wf_reset(WfLists q, int next) {
   }
 }
 
+/* FP32: at most 128 registers, four blocks of 128 per SM (the unbounded
+ * build takes 146 registers and fits three; bounded it spills 12 bytes);
+ * FP64: three blocks, as unbounded */
 template <typename R, bool Batched>
-__global__ void __launch_bounds__(128) wf_step(DevBundle<R> b0, DevTally t0, const DevBundle<R> *bundles,
+__global__ void __launch_bounds__(128, sizeof(R) == 4 ? 4 : 3) wf_step(DevBundle<R> b0, DevTally t0, const DevBundle<R> *bundles,
                                                const DevTally *tallies, WfPhoton<R> *st, WfLists q, int cur,
                                                long long cap, VrQueue<R> vq) {
   const long long n = (long long)q.count[cur] < cap ? (long long)q.count[cur] : cap;
