@@ -102,6 +102,9 @@ def parse():
     p.add_argument("--line-configs", type=int, default=32, help="configurations of the FP64 error statement")
     p.add_argument("--replicas", type=int, default=8,
                    help="disjoint photon ranges of the FP64 reference runs (their spread is the MC error)")
+    p.add_argument("--overlap-chunks", type=int, default=0,
+                   help="1: the next chunk's transport beside the current chunk's sort, solid angles and estimator")
+    p.add_argument("--estimator-blocks-per-sm", type=int, default=0, help="estimator blocks per SM (0: as many as fit)")
     p.add_argument("--no-plain", action="store_true")
     p.add_argument("--photons", type=float, default=1e7, help="photons per step of the plain workload")
     p.add_argument("--photons-precision", type=float, default=1e8, help="photons per step of the precision workload")
@@ -545,7 +548,8 @@ def batched_arm(args, ws, rank, local):
     from xmimsim_gb300 import Simulation, gpu_options, last_timing
     specs, options = batched_specs(args.configs, args.budget_scale, rank)
     seed = 0x5EED0005 + rank
-    g_sur = gpu_options(precision=1, seed=seed, use_surrogate=1, surrogate_tolerance=args.tolerance)
+    g_sur = gpu_options(precision=1, seed=seed, use_surrogate=1, surrogate_tolerance=args.tolerance,
+                        overlap_chunks=args.overlap_chunks, estimator_blocks_per_sm=args.estimator_blocks_per_sm)
     t0 = time.perf_counter()
     sims = [Simulation(s, options=options, gpu=g_sur) for s in specs]
     host_tables_s = time.perf_counter() - t0

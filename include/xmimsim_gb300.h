@@ -47,6 +47,12 @@ typedef struct {
                                comparison with that kernel */
   long long queue_events;   /* estimator events per chunk (device queue size); 0: default 2^25 */
   int grid_nr, grid_nt;     /* solid-angle grid points along r and theta; 0: the reference's 1024 */
+  int overlap_chunks;       /* 1: the transport of the next chunk runs beside the sort, solid
+                               angles and estimator of the current one (second stream, two
+                               event queues); 0: the phases of consecutive chunks run one after
+                               another (faster on GB300: both phases wait on table gathers
+                               through the same caches) */
+  int estimator_blocks_per_sm; /* estimator blocks resident per SM; 0: as many as fit */
 } xmi_gpu_options;
 
 /* ---- atomic data source of the host tabulator ----

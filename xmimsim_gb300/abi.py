@@ -130,7 +130,8 @@ class XmiGpuOptions(C.Structure):
     _fields_ = [("precision", C.c_int), ("use_surrogate", C.c_int), ("surrogate_tolerance", C.c_double),
                 ("threads_per_block", C.c_int), ("blocks_per_sm", C.c_int), ("seed", C.c_ulonglong),
                 ("solid_angle_stream", C.c_int), ("queue_events", C.c_longlong),
-                ("grid_nr", C.c_int), ("grid_nt", C.c_int)]
+                ("grid_nr", C.c_int), ("grid_nt", C.c_int), ("overlap_chunks", C.c_int),
+                ("estimator_blocks_per_sm", C.c_int)]
 
 
 # the atomic data source table (xmi_atomic_data): entry name -> argument types

@@ -86,6 +86,9 @@ struct DevBundle {
   const int *seg_off, *seg_n, *seg_lut;
   R seg_lut_ln0, seg_lut_inv;
   const R *el_tab, *mu_tab, *exc_tab;
+  /* [n_nodes][n_layer_el]: per layer, the running sum over its elements of
+   * weight x total cross section (the last term of a layer is its mu) */
+  const R *layer_cs;
   const R *icdf_e, *icdf_r, *phi_t, *phi_icdf, *dop_r;
   /* per element: device copies of the tables that depend on Z alone, shared
    * by every bundle on the device */

@@ -59,7 +59,7 @@ struct DevSide {
 };
 
 /* device buffers of the estimator event queue of one chunk */
-struct EventQueue {
+struct QueueBufs {
   void *events = nullptr;
   int *key = nullptr, *order = nullptr;
   int *fb = nullptr;        /* events the surrogate leaves to the integrator */
@@ -68,6 +68,24 @@ struct EventQueue {
   size_t bytes = 0;
   long long cap = 0;
   int nkeys = 0;
+  void release() {
+    cudaFree(events);
+    cudaFree(key);
+    cudaFree(order);
+    cudaFree(fb);
+    cudaFree(hist);
+    cudaFree(count);
+    *this = QueueBufs();
+  }
+};
+
+/* The event queues of a chunk sequence: two, so that chunk k+1's transport
+ * fills one while chunk k's sort, solid angles and estimator read the other
+ * on a second stream. */
+struct EventQueue {
+  QueueBufs buf[2];
+  cudaStream_t side = nullptr; /* stream of the sort / solid-angle / estimator phases */
+  cudaEvent_t filled[2] = {nullptr, nullptr}, drained[2] = {nullptr, nullptr}, joined = nullptr;
   /* executable graph of the last captured chunk sequence on this queue: the
    * next capture of the same shape updates it in place (cudaGraphExecUpdate)
    * instead of instantiating a new one */
@@ -79,16 +97,30 @@ struct EventQueue {
     if (exec) cudaGraphExecDestroy(exec);
     exec = nullptr;
   }
+  bool ensure_side() {
+    if (side) return true;
+    if (cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking) != cudaSuccess) return false;
+    bool ok = cudaEventCreateWithFlags(&joined, cudaEventDisableTiming) == cudaSuccess;
+    for (int i = 0; i < 2; i++)
+      ok = ok && cudaEventCreateWithFlags(&filled[i], cudaEventDisableTiming) == cudaSuccess &&
+           cudaEventCreateWithFlags(&drained[i], cudaEventDisableTiming) == cudaSuccess;
+    return ok;
+  }
   void release() {
     drop_exec();
     for (cudaEvent_t e : marks) cudaEventDestroy(e);
     marks.clear();
-    cudaFree(events);
-    cudaFree(key);
-    cudaFree(order);
-    cudaFree(fb);
-    cudaFree(hist);
-    cudaFree(count);
+    buf[0].release();
+    buf[1].release();
+    if (side) {
+      cudaStreamSynchronize(side);
+      cudaStreamDestroy(side);
+    }
+    for (int i = 0; i < 2; i++) {
+      if (filled[i]) cudaEventDestroy(filled[i]);
+      if (drained[i]) cudaEventDestroy(drained[i]);
+    }
+    if (joined) cudaEventDestroy(joined);
     *this = EventQueue();
   }
 };
@@ -372,6 +404,21 @@ bool upload_tables(const xmi_bundle &h, DevSide &s, xmi::DevBundle<R> &d) {
   d.seg_n = upload_int(s, h.seg_n, h.n_seg);
   d.el_tab = upload<R>(s, h.el_tab, E * h.n_nodes * XMI_EL_REC);
   d.mu_tab = upload<R>(s, h.mu_tab, (size_t)h.n_nodes * XMI_MAXL);
+  {
+    /* running sums in the order and arithmetic of mu_tab's, so a layer's
+     * last sum is its mu */
+    std::vector<double> cs((size_t)h.n_nodes * (h.n_layer_el > 0 ? h.n_layer_el : 1), 0.0);
+    for (int i = 0; i < h.n_nodes; i++)
+      for (int j = 0; j < h.n_layers; j++) {
+        double mu = 0.0;
+        for (int k = 0; k < h.layer_nel[j]; k++) {
+          const int p = h.layer_off[j] + k;
+          mu += h.el_tab[((size_t)h.layer_el[p] * h.n_nodes + i) * XMI_EL_REC + XMI_REC_TOT] * h.layer_w[p];
+          cs[(size_t)i * h.n_layer_el + p] = mu;
+        }
+      }
+    d.layer_cs = upload<R>(s, cs.data(), cs.size());
+  }
   d.exc_tab = upload<R>(s, h.exc_tab, h.n_nodes);
   d.icdf_e = upload<R>(s, h.icdf_energies, XMI_ICDF_NE);
   d.icdf_r = upload<R>(s, h.icdf_rs, XMI_ICDF_NR);
@@ -391,7 +438,7 @@ bool upload_tables(const xmi_bundle &h, DevSide &s, xmi::DevBundle<R> &d) {
   d.line_casc = upload_int(s, h.line_casc_shell, NL);
   d.auger_rate = upload<R>(s, h.auger_rate, E * 4 * XMI_AUGER_K);
   if (cudaGetLastError() != cudaSuccess || !d.rayl_icdf || !d.compt_icdf || !d.dop_icdf || !d.ff2 || !d.sf ||
-      !d.phi_icdf || !d.ent_pmu || !d.line_casc || !d.auger_rate) {
+      !d.phi_icdf || !d.ent_pmu || !d.line_casc || !d.auger_rate || !d.layer_cs) {
     xmi_set_error("device table upload failed");
     s.release();
     return false;
@@ -768,10 +815,10 @@ static int launch_wavefront(cudaStream_t st, WfBuffers &wb, const xmi::DevBundle
 static int wavefront_rounds(const xmi_bundle &h) { return h.use_vr ? h.n_interactions + 1 : 4 * XMI_MAXN + 8; }
 
 template <typename R>
-static bool ensure_queue(EventQueue &q, long long cap, int nkeys) {
+static bool ensure_queue(EventQueue &eq, QueueBufs &q, long long cap, int nkeys) {
   const size_t bytes = (size_t)cap * sizeof(xmi::VrEvent<R>);
   if (bytes > q.bytes || cap > q.cap) {
-    q.drop_exec();
+    eq.drop_exec();
     cudaFree(q.events);
     cudaFree(q.key);
     cudaFree(q.order);
@@ -789,7 +836,7 @@ static bool ensure_queue(EventQueue &q, long long cap, int nkeys) {
     q.cap = cap;
   }
   if (nkeys > q.nkeys) {
-    q.drop_exec();
+    eq.drop_exec();
     cudaFree(q.hist);
     q.hist = nullptr;
     q.nkeys = 0;
@@ -807,68 +854,102 @@ struct Phases {
 };
 
 /* Runs work indices [0, n) in chunks on stream st: per chunk the transport
- * launch (events into the queue), the counting sort of the events by key and
- * the estimator launch.  CUDA events around each phase give the device times.
- * transport(w0, w1, vq) and estimator(vq, order) enqueue the two kernels. */
+ * launch (events into an event queue), the counting sort of the events by
+ * key, the solid angles of the events and the estimator launch.  With
+ * variance reduction and more than one chunk (and overlap set), two event
+ * queues alternate: chunk k's sort, solid angles and estimator run on a
+ * second stream while chunk k+1's transport fills the other queue on st;
+ * a queue is refilled once the estimator that read it is done.  CUDA events
+ * around each phase give its device time (with overlap, phases of different
+ * chunks run at the same time, so their sum exceeds the total).
+ * transport(stream, w0, w1, vq), surrogate(stream, vq, fb, fb_count) and
+ * estimator(stream, vq, order, work) enqueue the phases. */
 template <typename R, typename TF, typename SF, typename EF>
 static bool run_chunks(cudaStream_t st, EventQueue &q, long long n, int N, int nkeys, bool vr, long long qev,
                        unsigned long long *total_events, TF &&transport, SF &&surrogate, EF &&estimator, Phases &ph,
-                       bool graph = false) {
+                       bool graph = false, bool overlap = false) {
   const int sms = num_sms();
   long long chunk = n < kMaxChunkPhotons ? n : kMaxChunkPhotons;
   if (chunk < 1) chunk = 1;
-  xmi::VrQueue<R> vq{nullptr, nullptr, nullptr, 0};
+  long long cap = 0;
   if (vr) {
     chunk = qev / (N > 0 ? N : 1);
     if (chunk > n) chunk = n;
     if (chunk < 1) chunk = 1;
-    if (!ensure_queue<R>(q, chunk * N, nkeys)) return false;
-    vq.ev = (xmi::VrEvent<R> *)q.events;
-    vq.key = q.key;
-    vq.count = q.count;
-    vq.cap = chunk * N;
+    cap = chunk * N;
   }
+  const bool two = vr && overlap && n > chunk;
+  if (vr) {
+    if (!ensure_queue<R>(q, q.buf[0], cap, nkeys)) return false;
+    if (two && (!ensure_queue<R>(q, q.buf[1], cap, nkeys) || !q.ensure_side())) {
+      xmi_set_error("second event queue or stream could not be created");
+      return false;
+    }
+  }
+  cudaStream_t as = two ? q.side : st; /* stream of the phases after transport */
   /* under stream capture an event record must be marked external to become a
    * real record when the graph runs (so that it can be timed and waited on) */
   size_t n_marks = 0;
-  auto mark = [&]() {
+  auto mark = [&](cudaStream_t s) {
     if (n_marks == q.marks.size()) {
       cudaEvent_t e;
       cudaEventCreate(&e);
       q.marks.push_back(e);
     }
     cudaEvent_t e = q.marks[n_marks++];
-    if (graph) cudaEventRecordWithFlags(e, st, cudaEventRecordExternal);
-    else cudaEventRecord(e, st);
+    if (graph) cudaEventRecordWithFlags(e, s, cudaEventRecordExternal);
+    else cudaEventRecord(e, s);
   };
   int launches = 0;
   cudaGraph_t g = nullptr;
   if (graph && !cuda_ok(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "graph capture")) return false;
-  mark();
-  for (long long w0 = 0; w0 < n; w0 += chunk) {
+  mark(st);
+  long long k = 0;
+  for (long long w0 = 0; w0 < n; w0 += chunk, k++) {
     const long long w1 = w0 + chunk < n ? w0 + chunk : n;
+    const int qi = two ? (int)(k & 1) : 0;
+    QueueBufs &qb = q.buf[qi];
+    xmi::VrQueue<R> vq{nullptr, nullptr, nullptr, 0};
     if (vr) {
-      cudaMemsetAsync(q.count, 0, sizeof(unsigned long long), st);
-      cudaMemsetAsync(q.hist, 0, sizeof(unsigned) * nkeys, st);
+      vq.ev = (xmi::VrEvent<R> *)qb.events;
+      vq.key = qb.key;
+      vq.count = qb.count;
+      vq.cap = cap;
+      /* the queue's previous chunk must be through its estimator */
+      if (two && k >= 2) cudaStreamWaitEvent(st, q.drained[qi], 0);
+      cudaMemsetAsync(qb.count, 0, sizeof(unsigned long long), st);
+      cudaMemsetAsync(qb.hist, 0, sizeof(unsigned) * nkeys, st);
     }
-    launches += transport(w0, w1, vq);
-    mark();
+    mark(st);
+    launches += transport(st, w0, w1, vq);
+    mark(st);
     if (vr) {
+      if (two) {
+        cudaEventRecord(q.filled[qi], st);
+        cudaStreamWaitEvent(as, q.filled[qi], 0);
+      }
+      mark(as);
       /* positions of events whose key the sort would skip stay -1 and are refused by the estimator */
-      cudaMemsetAsync(q.order, 0xff, sizeof(int) * (w1 - w0) * N, st);
-      xmi::event_key_histogram<<<sms * 4, 256, 0, st>>>(q.key, q.count, vq.cap, nkeys, q.hist);
-      xmi::event_key_scan<<<1, xmi::kScanThreads, 0, st>>>(q.hist, nkeys, q.hist + nkeys, q.count, total_events);
-      xmi::event_key_scatter<<<sms * 4, 256, 0, st>>>(q.key, q.count, vq.cap, nkeys, q.hist + nkeys, q.order);
-      cudaMemsetAsync(q.count + 1, 0, 2 * sizeof(unsigned long long), st);
-      mark();
-      launches += surrogate(vq, q.fb, q.count + 2);
-      mark();
-      estimator(vq, (const int *)q.order, q.count + 1);
-      mark();
+      cudaMemsetAsync(qb.order, 0xff, sizeof(int) * (w1 - w0) * N, as);
+      xmi::event_key_histogram<<<sms * 4, 256, 0, as>>>(qb.key, qb.count, cap, nkeys, qb.hist);
+      xmi::event_key_scan<<<1, xmi::kScanThreads, 0, as>>>(qb.hist, nkeys, qb.hist + nkeys, qb.count, total_events);
+      xmi::event_key_scatter<<<sms * 4, 256, 0, as>>>(qb.key, qb.count, cap, nkeys, qb.hist + nkeys, qb.order);
+      cudaMemsetAsync(qb.count + 1, 0, 2 * sizeof(unsigned long long), as);
+      mark(as);
+      launches += surrogate(as, vq, qb.fb, qb.count + 2);
+      mark(as);
+      estimator(as, vq, (const int *)qb.order, qb.count + 1);
+      mark(as);
       launches += 4;
+      if (two) cudaEventRecord(q.drained[qi], as);
     }
     if (!cuda_ok(cudaGetLastError(), "transport launch")) break;
   }
+  if (two) {
+    cudaEventRecord(q.joined, as);
+    cudaStreamWaitEvent(st, q.joined, 0);
+  }
+  mark(st);
   bool ok = cuda_ok(cudaGetLastError(), "transport launch");
   if (graph) {
     /* the whole chunk sequence as one graph launch; the executable graph of
@@ -899,16 +980,21 @@ static bool run_chunks(cudaStream_t st, EventQueue &q, long long n, int N, int n
   ok = ok && cuda_ok(cudaEventSynchronize(marks.back()), "transport");
   if (g) cudaGraphDestroy(g);
   if (ok) {
+    /* marks: start, per chunk (transport begin, end[, sort begin, sort end,
+     * solid angles end, estimator end]), end */
     float total = 0.f;
     cudaEventElapsedTime(&total, marks.front(), marks.back());
     ph.total_ms = total;
-    const size_t per = vr ? 4 : 1;
-    for (size_t i = 0; i + per < marks.size(); i += per)
-      for (size_t k = 0; k < per; k++) {
-        float f = 0.f;
-        cudaEventElapsedTime(&f, marks[i + k], marks[i + k + 1]);
-        ph.ms[k] += f;
+    const size_t per = vr ? 6 : 2;
+    for (size_t i = 1; i + per < marks.size(); i += per) {
+      float f = 0.f;
+      cudaEventElapsedTime(&f, marks[i], marks[i + 1]);
+      ph.ms[0] += f;
+      for (size_t k2 = 0; vr && k2 < 3; k2++) {
+        cudaEventElapsedTime(&f, marks[i + 2 + k2], marks[i + 3 + k2]);
+        ph.ms[1 + k2] += f;
       }
+    }
     ph.launches = launches;
   }
   return ok;
@@ -1017,12 +1103,13 @@ static int stage_cap_for(int stage_max) {
 }
 
 template <typename R, bool Adv = false>
-static int estimator_blocks(int stage_cap, size_t *smem) {
+static int estimator_blocks(int stage_cap, size_t *smem, int cap_per_sm = 0) {
   *smem = (size_t)8 * (stage_cap + xmi::kScratchPerWarp) * sizeof(R);
   if (*smem > 48 * 1024)
     cudaFuncSetAttribute(xmi::estimator_kernel<R, Adv>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)*smem);
   int per_sm = 1;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, xmi::estimator_kernel<R, Adv>, 256, *smem);
+  if (cap_per_sm > 0 && per_sm > cap_per_sm) per_sm = cap_per_sm;
   if (per_sm < 1) per_sm = 1;
   return num_sms() * per_sm;
 }
@@ -1064,8 +1151,9 @@ __global__ void record_points_kernel(const xmi::VrEvent<R> *ev, const unsigned l
 
 template <typename R>
 static bool launch_single(DevState *s, xmi::DevBundle<R> &d, const xmi::DevTally &tl, const xmi_bundle &h,
-                          int threads, int blocks_per_sm, long long qev, const void *sg, Phases &ph,
+                          int threads, int blocks_per_sm, const xmi_gpu_options &go, const void *sg, Phases &ph,
                           const PointRecorder *rec = nullptr) {
+  const long long qev = queue_events_of(go);
   const int sms = num_sms();
   if (!s->d_bundle && !cuda_ok(cudaMalloc(&s->d_bundle, sizeof(xmi::DevBundle<double>)), "cudaMalloc")) return false;
   if (!s->d_tally && !cuda_ok(cudaMalloc(&s->d_tally, sizeof(xmi::DevTally)), "cudaMalloc")) return false;
@@ -1075,7 +1163,8 @@ static bool launch_single(DevState *s, xmi::DevBundle<R> &d, const xmi::DevTally
   const int stage_cap = stage_cap_for<R>(h.stage_max);
   size_t smem = 0;
   const bool adv = d.use_adv_compton != 0;
-  const int est_blocks = adv ? estimator_blocks<R, true>(stage_cap, &smem) : estimator_blocks<R>(stage_cap, &smem);
+  const int est_blocks = adv ? estimator_blocks<R, true>(stage_cap, &smem, go.estimator_blocks_per_sm)
+                             : estimator_blocks<R>(stage_cap, &smem, go.estimator_blocks_per_sm);
   const long long chunk_cap = h.use_vr ? qev / (h.n_interactions > 0 ? h.n_interactions : 1) : kMaxChunkPhotons;
   /* back to the pool once the run's stream is idle */
   struct Borrow {
@@ -1094,38 +1183,38 @@ static bool launch_single(DevState *s, xmi::DevBundle<R> &d, const xmi::DevTally
                                                                          : chunk_cap)))
     return false;
   const int rounds = wavefront_rounds(h);
-  auto transport = [&](long long w0, long long w1, const xmi::VrQueue<R> &vq) {
-    return launch_wavefront<R, false>(s->stream, wf, d, tl, nullptr, nullptr, nullptr, 1, w0, w1, rounds, vq,
+  auto transport = [&](cudaStream_t ts, long long w0, long long w1, const xmi::VrQueue<R> &vq) {
+    return launch_wavefront<R, false>(ts, wf, d, tl, nullptr, nullptr, nullptr, 1, w0, w1, rounds, vq,
                                       threads, sms * blocks_per_sm, adv, casc);
   };
-  auto estimator = [&](const xmi::VrQueue<R> &vq, const int *order, unsigned long long *work) {
+  auto estimator = [&](cudaStream_t es, const xmi::VrQueue<R> &vq, const int *order, unsigned long long *work) {
     if (adv)
-      xmi::estimator_kernel<R, true><<<est_blocks, 256, smem, s->stream>>>(
+      xmi::estimator_kernel<R, true><<<est_blocks, 256, smem, es>>>(
           (const xmi::DevBundle<R> *)s->d_bundle, s->d_tally, 1, vq.ev, order, vq.count, vq.cap, work, stage_cap,
           &s->counters[1]);
     else
-      xmi::estimator_kernel<R><<<est_blocks, 256, smem, s->stream>>>(
+      xmi::estimator_kernel<R><<<est_blocks, 256, smem, es>>>(
           (const xmi::DevBundle<R> *)s->d_bundle, s->d_tally, 1, vq.ev, order, vq.count, vq.cap, work, stage_cap,
           &s->counters[1]);
   };
-  auto surrogate = [&](const xmi::VrQueue<R> &vq, int *fb, unsigned long long *fb_count) -> int {
+  auto surrogate = [&](cudaStream_t ss, const xmi::VrQueue<R> &vq, int *fb, unsigned long long *fb_count) -> int {
     if (!d.use_surrogate) {
       /* the grid path: integrals of the events off the grid */
       xmi_solid_angle_deferred(sizeof(R) == 8 ? 0 : 1, s->d_bundle, 1, vq.ev, vq.count, vq.cap, fb, fb_count,
-                               s->stream);
+                               ss);
       return 2;
     }
     if (rec) {
-      record_points_kernel<R><<<sms * 4, 256, 0, s->stream>>>(vq.ev, vq.count, vq.cap, rec->p, rec->r, rec->t, rec->n,
+      record_points_kernel<R><<<sms * 4, 256, 0, ss>>>(vq.ev, vq.count, vq.cap, rec->p, rec->r, rec->t, rec->n,
                                                                rec->max);
       return 1;
     }
     xmi_surrogate_apply(sg, sizeof(R) == 8 ? 0 : 1, s->d_bundle, 1, vq.ev, vq.count, vq.cap, &s->counters[4], fb,
-                        fb_count, (int *)&s->counters[5], s->stream);
+                        fb_count, (int *)&s->counters[5], ss);
     return 2;
   };
   return run_chunks<R>(s->stream, q, h.n_photons_total, h.n_interactions, XMI_MAXL * XMI_MAXN, h.use_vr != 0,
-                       qev, &s->counters[3], transport, surrogate, estimator, ph);
+                       qev, &s->counters[3], transport, surrogate, estimator, ph, false, go.overlap_chunks != 0);
 }
 
 /* device tallies -> the reference's output layouts (host) */
@@ -1219,9 +1308,9 @@ extern "C" int xmi_main_msim(xmi_inputFPtr in, xmi_hdf5FPtr t, int n_mpi_hosts, 
   const void *sg = use_sg ? in->surrogate : nullptr;
   bool ok = precision == 0
                 ? stage_run<double>(s, s->b64, h, tl, use_sg) &&
-                      launch_single<double>(s, s->b64, tl, h, threads, bps, queue_events_of(in->gpu), sg, ph)
+                      launch_single<double>(s, s->b64, tl, h, threads, bps, in->gpu, sg, ph)
                 : stage_run<float>(s, s->b32, h, tl, use_sg) &&
-                      launch_single<float>(s, s->b32, tl, h, threads, bps, queue_events_of(in->gpu), sg, ph);
+                      launch_single<float>(s, s->b32, tl, h, threads, bps, in->gpu, sg, ph);
   if (!ok) return 0;
   unsigned long long events = 0, fallbacks = 0;
   if (!collect_outputs(s, h, n_mpi_hosts, channels_out, brute_out, var_red_out, &events, &fallbacks)) return 0;
@@ -1265,7 +1354,8 @@ std::mutex g_batch_lock;
 
 template <typename R>
 bool launch_batch(int n, DevState **st, xmi_hdf5FPtr *t, const xmi::DevTally *tl, int threads, int blocks_per_sm,
-                  long long qev, const void *sg, bool graph, Phases &ph) {
+                  const xmi_gpu_options &go, const void *sg, bool graph, Phases &ph) {
+  const long long qev = queue_events_of(go);
   BatchState &B = g_batch;
   std::vector<xmi::DevBundle<R>> bundles(n);
   std::vector<long long> first(n + 1, 0);
@@ -1308,7 +1398,8 @@ bool launch_batch(int n, DevState **st, xmi_hdf5FPtr *t, const xmi::DevTally *tl
   for (int c = 0; c < n; c++) adv = adv || (t[c]->b.use_advanced_compton && t[c]->b.cp_nshell);
   const int stage_cap = stage_cap_for<R>(stage_max);
   size_t smem = 0;
-  const int est_blocks = adv ? estimator_blocks<R, true>(stage_cap, &smem) : estimator_blocks<R>(stage_cap, &smem);
+  const int est_blocks = adv ? estimator_blocks<R, true>(stage_cap, &smem, go.estimator_blocks_per_sm)
+                             : estimator_blocks<R>(stage_cap, &smem, go.estimator_blocks_per_sm);
   int rounds = 1;
   for (int c = 0; c < n; c++) rounds = wavefront_rounds(t[c]->b) > rounds ? wavefront_rounds(t[c]->b) : rounds;
   const long long chunk_cap = vr ? qev / N : kMaxChunkPhotons;
@@ -1321,32 +1412,32 @@ bool launch_batch(int n, DevState **st, xmi_hdf5FPtr *t, const xmi::DevTally *tl
     return false;
   xmi::DevBundle<R> unused_b{};
   xmi::DevTally unused_t{};
-  auto transport = [&](long long w0, long long w1, const xmi::VrQueue<R> &vq) {
-    return launch_wavefront<R, true>(B.stream, B.wf, unused_b, unused_t, db, B.tallies, B.cfg_first, n, w0, w1,
+  auto transport = [&](cudaStream_t ts, long long w0, long long w1, const xmi::VrQueue<R> &vq) {
+    return launch_wavefront<R, true>(ts, B.wf, unused_b, unused_t, db, B.tallies, B.cfg_first, n, w0, w1,
                                      rounds, vq, threads, sms * blocks_per_sm, adv, casc);
   };
-  auto estimator = [&](const xmi::VrQueue<R> &vq, const int *order, unsigned long long *work) {
+  auto estimator = [&](cudaStream_t es, const xmi::VrQueue<R> &vq, const int *order, unsigned long long *work) {
     if (adv)
-      xmi::estimator_kernel<R, true><<<est_blocks, 256, smem, B.stream>>>(db, B.tallies, n, vq.ev, order, vq.count,
+      xmi::estimator_kernel<R, true><<<est_blocks, 256, smem, es>>>(db, B.tallies, n, vq.ev, order, vq.count,
                                                                           vq.cap, work, stage_cap, B.flags);
     else
-      xmi::estimator_kernel<R><<<est_blocks, 256, smem, B.stream>>>(db, B.tallies, n, vq.ev, order, vq.count, vq.cap,
+      xmi::estimator_kernel<R><<<est_blocks, 256, smem, es>>>(db, B.tallies, n, vq.ev, order, vq.count, vq.cap,
                                                                     work, stage_cap, B.flags);
   };
   /* flags: [0] estimator error, [1] events, [2] integrator fallbacks of the
    * surrogate, [3] surrogate error */
-  auto surrogate = [&](const xmi::VrQueue<R> &vq, int *fb, unsigned long long *fb_count) -> int {
+  auto surrogate = [&](cudaStream_t ss, const xmi::VrQueue<R> &vq, int *fb, unsigned long long *fb_count) -> int {
     /* the integrals of the events off their configuration's grid first (a
      * configuration served by the network leaves none), then the network */
-    xmi_solid_angle_deferred(sizeof(R) == 8 ? 0 : 1, db, n, vq.ev, vq.count, vq.cap, fb, fb_count, B.stream);
+    xmi_solid_angle_deferred(sizeof(R) == 8 ? 0 : 1, db, n, vq.ev, vq.count, vq.cap, fb, fb_count, ss);
     if (!sg) return 2;
-    cudaMemsetAsync(fb_count, 0, sizeof(unsigned long long), B.stream);
+    cudaMemsetAsync(fb_count, 0, sizeof(unsigned long long), ss);
     xmi_surrogate_apply(sg, sizeof(R) == 8 ? 0 : 1, db, n, vq.ev, vq.count, vq.cap, &B.flags[2], fb, fb_count,
-                        (int *)&B.flags[3], B.stream);
+                        (int *)&B.flags[3], ss);
     return 4;
   };
   if (!run_chunks<R>(B.stream, B.q, first[n], N, n * XMI_MAXL * XMI_MAXN, vr, qev, &B.flags[1], transport,
-                     surrogate, estimator, ph, graph))
+                     surrogate, estimator, ph, graph, go.overlap_chunks != 0))
     return false;
   unsigned long long flags[4];
   cudaMemcpy(flags, B.flags, sizeof(flags), cudaMemcpyDeviceToHost);
@@ -1411,9 +1502,9 @@ extern "C" int xmi_main_msim_batch(int n, xmi_inputFPtr *inputFPtrs, xmi_hdf5FPt
   }
   const int bps = inputFPtrs[0]->gpu.blocks_per_sm > 0 ? inputFPtrs[0]->gpu.blocks_per_sm : 8;
   Phases ph;
-  const long long qev = queue_events_of(inputFPtrs[0]->gpu);
-  bool ok = precision == 0 ? launch_batch<double>(n, st.data(), hdf5FPtrs, tl.data(), threads, bps, qev, sg, true, ph)
-                           : launch_batch<float>(n, st.data(), hdf5FPtrs, tl.data(), threads, bps, qev, sg, true, ph);
+  const xmi_gpu_options &go = inputFPtrs[0]->gpu;
+  bool ok = precision == 0 ? launch_batch<double>(n, st.data(), hdf5FPtrs, tl.data(), threads, bps, go, sg, true, ph)
+                           : launch_batch<float>(n, st.data(), hdf5FPtrs, tl.data(), threads, bps, go, sg, true, ph);
   if (!ok) return 0;
   for (int c = 0; c < n; c++)
     if (!collect_outputs(st[c], hdf5FPtrs[c]->b, 1, &channels[c], &brute_histories[c], &var_red_histories[c],
@@ -1469,10 +1560,10 @@ extern "C" int xmi_gpu_sample_event_points(xmi_inputFPtr in, xmi_hdf5FPtr t, xmi
     xmi::DevTally tl;
     Phases ph;
     ok = precision == 0 ? stage_run<double>(s, s->b64, t->b, tl, true) &&
-                              launch_single<double>(s, s->b64, tl, t->b, threads, bps, queue_events_of(in->gpu),
+                              launch_single<double>(s, s->b64, tl, t->b, threads, bps, in->gpu,
                                                     nullptr, ph, &rec)
                         : stage_run<float>(s, s->b32, t->b, tl, true) &&
-                              launch_single<float>(s, s->b32, tl, t->b, threads, bps, queue_events_of(in->gpu),
+                              launch_single<float>(s, s->b32, tl, t->b, threads, bps, in->gpu,
                                                    nullptr, ph, &rec);
     unsigned long long counters[8];
     ok = ok && cuda_ok(cudaMemcpy(counters, s->counters, sizeof(counters), cudaMemcpyDeviceToHost), "copy") &&

@@ -1281,9 +1281,19 @@ __device__ bool fluorescence(const DevBundle<R> &b, Photon<R> &p, xmi_rng *g, Ph
   R photo_total = el_val(b, e, XMI_REC_PHOTO, node, f);
   R sumz = (R)0, r = uni<R>(g);
   int shell = -1;
-  for (int s = 0; s <= b.max_shell; s++) {
-    sumz = sumz + el_val(b, e, XMI_REC_PART + s, node, f) / photo_total;
-    if (r < sumz) { shell = s; break; }
+  if constexpr (sizeof(R) == 4) {
+    /* r < sum of partial / total, as r total < sum of partials: no division
+     * per shell */
+    const R target = r * photo_total;
+    for (int s = 0; s <= b.max_shell; s++) {
+      sumz = sumz + el_val(b, e, XMI_REC_PART + s, node, f);
+      if (target < sumz) { shell = s; break; }
+    }
+  } else {
+    for (int s = 0; s <= b.max_shell; s++) {
+      sumz = sumz + el_val(b, e, XMI_REC_PART + s, node, f) / photo_total;
+      if (r < sumz) { shell = s; break; }
+    }
   }
   if (shell < 0) {
     p.E = (R)0;
@@ -1571,12 +1581,25 @@ __device__ int step_photon(const DevBundle<R> &b, Photon<R> &p, const DevTally &
 #pragma unroll
   for (int j = 0; j < XMI_MAXL; j++)
     if (j == L) mu_l = p.mus[j];
-  R thr = (R)0;
   int sel = nel - 1;
-  for (int i = 0; i < nel; i++) {
-    thr = thr + XMI_LDG(b.layer_w, off + i, b.n_layer_el, 19) *
-                    el_val(b, XMI_LDG(b.layer_el, off + i, b.n_layer_el, 19), XMI_REC_TOT, node, f) / mu_l;
-    if (r < thr) { sel = i; break; }
+  if constexpr (sizeof(R) == 4) {
+    /* the same choice, r < sum_k<=i w_k sigma_k(E) / mu, as r mu < the
+     * layer's running sum at E: the running sums interpolate linearly like
+     * each term, and a node's sums are one contiguous row instead of one
+     * element record (a dependent gather) per term */
+    const long long c0 = (long long)node * b.n_layer_el + off, lim = (long long)b.n_nodes * b.n_layer_el;
+    const R target = r * mu_l;
+    for (int i = 0; i < nel; i++) {
+      const R v0 = XMI_LDG(b.layer_cs, c0 + i, lim, 60), v1 = XMI_LDG(b.layer_cs, c0 + b.n_layer_el + i, lim, 60);
+      if (target < v0 + f * (v1 - v0)) { sel = i; break; }
+    }
+  } else {
+    R thr = (R)0;
+    for (int i = 0; i < nel; i++) {
+      thr = thr + XMI_LDG(b.layer_w, off + i, b.n_layer_el, 19) *
+                      el_val(b, XMI_LDG(b.layer_el, off + i, b.n_layer_el, 19), XMI_REC_TOT, node, f) / mu_l;
+      if (r < thr) { sel = i; break; }
+    }
   }
   p.elem = XMI_LDG(b.layer_el, off + sel, b.n_layer_el, 19);
   if (!XMI_CHK(p.elem, b.n_elem, 42)) return kStepError;

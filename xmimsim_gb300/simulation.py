@@ -140,15 +140,20 @@ def make_options(**kw) -> abi.XmiMainOptions:
 
 def gpu_options(precision: int = 0, seed: int = 0, threads_per_block: int = 0, blocks_per_sm: int = 0,
                 use_surrogate: int = 0, surrogate_tolerance: float = 1e-3,
-                solid_angle_stream: int = 0, grid_n: int = 0) -> abi.XmiGpuOptions:
+                solid_angle_stream: int = 0, grid_n: int = 0, overlap_chunks: int = 0,
+                estimator_blocks_per_sm: int = 0) -> abi.XmiGpuOptions:
     """grid_n: points of the solid-angle grid along r and along theta (0: the
-    reference's 1024)."""
+    reference's 1024).  overlap_chunks=1 runs the next chunk's transport
+    beside the current chunk's sort, solid angles and estimator (two event
+    queues) instead of one after another; estimator_blocks_per_sm caps the
+    estimator's resident blocks per SM (0: as many as fit)."""
     g = abi.XmiGpuOptions()
     abi.load().xmi_gpu_default_options(C.byref(g))
     g.precision, g.seed, g.solid_angle_stream = precision, seed, solid_angle_stream
     g.threads_per_block, g.blocks_per_sm = threads_per_block, blocks_per_sm
     g.use_surrogate, g.surrogate_tolerance = use_surrogate, surrogate_tolerance
     g.grid_nr = g.grid_nt = grid_n
+    g.overlap_chunks, g.estimator_blocks_per_sm = overlap_chunks, estimator_blocks_per_sm
     return g
 
 
