@@ -434,7 +434,14 @@ bool upload_tables(const xmi_bundle &h, DevSide &s, xmi::DevBundle<R> &d) {
   d.ent_slot = upload_int(s, h.ent_slot, h.n_ent);
   d.ent_shell = upload_int(s, h.ent_shell, h.n_ent);
   d.ent_coef = upload<R>(s, h.ent_coef, h.n_ent);
-  d.ent_pmu = upload<R>(s, h.ent_pmu, (size_t)h.n_ent * XMI_MAXL);
+  if (sizeof(R) == 4) {
+    /* FP32: the line mu scaled by -log2(e), for exp2 in the estimator */
+    std::vector<double> pmu2((size_t)h.n_ent * XMI_MAXL);
+    for (size_t i = 0; i < pmu2.size(); i++) pmu2[i] = h.ent_pmu ? -1.4426950408889634 * h.ent_pmu[i] : 0.0;
+    d.ent_pmu = upload<R>(s, pmu2.data(), pmu2.size());
+  } else {
+    d.ent_pmu = upload<R>(s, h.ent_pmu, (size_t)h.n_ent * XMI_MAXL);
+  }
   d.line_casc = upload_int(s, h.line_casc_shell, NL);
   d.auger_rate = upload<R>(s, h.auger_rate, E * 4 * XMI_AUGER_K);
   if (cudaGetLastError() != cudaSuccess || !d.rayl_icdf || !d.compt_icdf || !d.dop_icdf || !d.ff2 || !d.sf ||

@@ -23,6 +23,23 @@
 
 namespace xmi {
 
+/* exp(-sum_j mu_j rho_j d_j) of a line from the sum over its line-table mu
+ * (ent_pmu): the FP32 tables hold -log2(e) mu, so that the attenuation is
+ * one exp2; the FP64 tables hold mu */
+template <typename R>
+__device__ __forceinline__ R line_atten(R s) {
+  if constexpr (sizeof(R) == 4) return exp2f(s);
+  else return exp(-s);
+}
+
+/* exp(-x) of an attenuation exponent: FP32 as exp2(-log2(e) x) */
+template <typename R>
+__device__ __forceinline__ R atten(R x) {
+  if constexpr (sizeof(R) == 4) return exp2f(-1.44269504088896341f * x);
+  else return exp(-x);
+}
+
+
 template <typename R>
 __device__ __forceinline__ R warp_sum_r(R v) {
 #pragma unroll
@@ -77,7 +94,7 @@ __device__ __noinline__ R compton_advanced_est(const DevBundle<R> &b, const DevT
         R murhod = (R)0;
 #pragma unroll
         for (int j = 0; j < XMI_MAXL; j++) murhod += mus_c[j] * ev.rd[j];
-        tw = base * exp(-murhod) * (R)sw;
+        tw = base * atten<R>(murhod) * (R)sw;
         total += tw;
       }
     }
@@ -213,7 +230,7 @@ __device__ __forceinline__ void estimate_event(const DevBundle<R> &b, const DevT
         R murhod = (R)0;
 #pragma unroll
         for (int j = 0; j < XMI_MAXL; j++) murhod += mus_c[j] * ev.rd[j];
-        twc = live * (pconv * (ev.pC * qtab(b.sf[e], ev.q)) * exp(-murhod) * ev.w);
+        twc = live * (pconv * (ev.pC * qtab(b.sf[e], ev.q)) * atten<R>(murhod) * ev.w);
       } else if (valid) {
         ok = false;
       }
@@ -248,7 +265,7 @@ __device__ __forceinline__ void estimate_event(const DevBundle<R> &b, const DevT
 #pragma unroll
       for (int j = 0; j < XMI_MAXL; j++)
         murhod += XMI_LDG(b.ent_pmu, (long long)k * XMI_MAXL + j, (long long)b.n_ent * XMI_MAXL, 17) * ev.rd[j];
-      const R tw = ps * XMI_LDG(b.ent_coef, k, b.n_ent, 16) * scale * exp(-murhod);
+      const R tw = ps * XMI_LDG(b.ent_coef, k, b.n_ent, 16) * scale * line_atten<R>(murhod);
       contribute<R, Uniform>(t, st, k - k_first, hbase + sl, tw);
     }
   }
@@ -311,7 +328,7 @@ __device__ __forceinline__ R line_entry_events(const DevBundle<R> &b, const R *s
 #pragma unroll
       for (int j = 0; j < L; j++) murhod += pmu[j] * s_rd[q * XMI_MAXL + j];
     }
-    acc += s_a[q * XMI_NSHELL + sh] * exp(-murhod);
+    acc += s_a[q * XMI_NSHELL + sh] * line_atten<R>(murhod);
   }
   return acc;
 }
@@ -365,7 +382,7 @@ __device__ __forceinline__ void estimate_event_uniform(const DevBundle<R> &b, co
         R murhod = (R)0;
 #pragma unroll
         for (int j = 0; j < XMI_MAXL; j++) murhod += mus_c[j] * ev.rd[j];
-        twc = live * (pconv * (ev.pC * qtab(b.sf[e], ev.q)) * exp(-murhod) * ev.w);
+        twc = live * (pconv * (ev.pC * qtab(b.sf[e], ev.q)) * atten<R>(murhod) * ev.w);
       } else if (valid) {
         ok = false;
       }
