@@ -919,6 +919,9 @@ __device__ bool vr_prologue(const DevBundle<R> &b, const Photon<R> &p, const Dev
   if (p.E <= (R)kEnergyThreshold) return false;
   if (!XMI_CHK(p.layer, b.n_layers, 34)) { ok = false; return false; }
   const int n = p.n_int, layer = p.layer;
+  /* the energy-grid location first: its gathers are in flight during the
+   * geometry below (the step's atom choice reuses it) */
+  locate(b, p.E, ev.node, ev.f);
   xmi_rng g;
   xmi_rng_init(&g, b.seed, (uint64_t)p.id, vr_stream(n, 0xFF));
   R radius = sqrt(uni<R>(&g)) * b.det_radius_r;
@@ -1012,7 +1015,6 @@ __device__ bool vr_prologue(const DevBundle<R> &b, const Photon<R> &p, const Dev
     ev.sa_pending = deferred ? 1 : 0;
   }
   ev.pdir_fluo = omega / (R)4 / (R)kPi;
-  locate(b, p.E, ev.node, ev.f);
   ev.mu_here = select_layer(p.mus, layer);
   ev.q = p.E / (R)12.39852 * sin(theta / (R)2);
   const R st = sin(theta), cp = cos(phi), ct = cos(theta);
@@ -1563,17 +1565,21 @@ __device__ int step_photon(const DevBundle<R> &b, Photon<R> &p, const DevTally &
   }
   if (p.n_int == b.N) return kStepDone;
   p.n_int = p.n_int + 1;
+  int node = -1; /* energy-grid location of p.E: from the event when there is one */
+  R f = (R)0;
   if (b.use_vr == 1) {
     bool ok = true;
     VrEvent<R> ev;
     ev.cfg = cfg;
-    if (vr_prologue(b, p, t, ev, ok) && !vr_emit(vq, ev, vr_key(ev))) { set_error(t, kErrQueue); return kStepError; }
+    if (vr_prologue(b, p, t, ev, ok)) {
+      node = ev.node;
+      f = ev.f;
+      if (!vr_emit(vq, ev, vr_key(ev))) { set_error(t, kErrQueue); return kStepError; }
+    }
     if (!ok) { set_error(t, kErrTable); return kStepError; }
   }
   /* atom selection and interaction type, src/xmi_main.F90:1556-1652 */
-  int node;
-  R f;
-  locate(b, p.E, node, f);
+  if (node < 0) locate(b, p.E, node, f);
   R r = uni<R>(&g);
   if (!XMI_CHK(p.layer, b.n_layers, 33)) return kStepError;
   const int L = p.layer, nel = b.nel[L], off = b.off[L];
