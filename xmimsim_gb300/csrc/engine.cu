@@ -938,9 +938,9 @@ static bool run_chunks(cudaStream_t st, EventQueue &q, long long n, int N, int n
       mark(as);
       /* positions of events whose key the sort would skip stay -1 and are refused by the estimator */
       cudaMemsetAsync(qb.order, 0xff, sizeof(int) * (w1 - w0) * N, as);
-      xmi::event_key_histogram<<<sms * 4, 256, 0, as>>>(qb.key, qb.count, cap, nkeys, qb.hist);
+      xmi::event_key_histogram<<<sms * 8, 256, 0, as>>>(qb.key, qb.count, cap, nkeys, qb.hist);
       xmi::event_key_scan<<<1, xmi::kScanThreads, 0, as>>>(qb.hist, nkeys, qb.hist + nkeys, qb.count, total_events);
-      xmi::event_key_scatter<<<sms * 4, 256, 0, as>>>(qb.key, qb.count, cap, nkeys, qb.hist + nkeys, qb.order);
+      xmi::event_key_scatter<<<sms * 8, 256, 0, as>>>(qb.key, qb.count, cap, nkeys, qb.hist + nkeys, qb.order);
       cudaMemsetAsync(qb.count + 1, 0, 2 * sizeof(unsigned long long), as);
       mark(as);
       launches += surrogate(as, vq, qb.fb, qb.count + 2);

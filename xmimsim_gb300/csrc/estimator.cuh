@@ -513,21 +513,78 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 3) estimator_kernel(
   if (!ok) atomicCAS(flags, 0ull, kErrCompton);
 }
 
-/* counting sort of the chunk's events by key (vr_key): histogram with one
- * atomic per group of equal keys in a warp, exclusive scan, scatter */
-__global__ void event_key_histogram(const int *key, const unsigned long long *count, long long cap, int nkeys,
-                                    unsigned *hist) {
-  const long long n = queued_events(count, cap);
-  const int lane = threadIdx.x & 31;
-  for (long long base = ((long long)blockIdx.x * blockDim.x + threadIdx.x) & ~31ll; base < n;
-       base += (long long)gridDim.x * blockDim.x) {
-    const long long i = base + lane;
-    const int k = i < n ? key[i] : -1;
-    /* consecutive events mostly share their key: one vote settles that case */
-    const unsigned peers = __all_sync(0xffffffffu, k == __shfl_sync(0xffffffffu, k, 0)) ? 0xffffffffu
-                                                                                        : __match_any_sync(0xffffffffu, k);
-    if (k >= 0 && k < nkeys && lane == __ffs(peers) - 1) atomicAdd(&hist[k], (unsigned)__popc(peers));
+/* counting sort of the chunk's events by key (vr_key): histogram, exclusive
+ * scan, scatter.  A block takes a contiguous range of the queue, where few
+ * keys occur (the queue fills round by round, photon by photon, and a chunk
+ * spans a few configurations): it counts its keys in a shared-memory table
+ * (one shared atomic per group of equal keys in a warp) and adds each key's
+ * count to the global histogram once, instead of every warp's groups
+ * contending for the same few global counters.  A key that finds the table
+ * full is counted with global atomics (the probe loop is bounded by the
+ * table size). */
+constexpr int kSortSlots = 1024;
+
+/* slot of `k` in a block's key table (linear probing from a multiplicative
+ * hash); insert: claim an empty slot for it; -1: not found / table full */
+__device__ __forceinline__ int sort_slot(volatile int *keys, int k, bool insert) {
+  int s = (int)(((unsigned)k * 2654435761u) >> 22); /* top 10 bits */
+  for (int probe = 0; probe < kSortSlots; probe++) {
+    const int cur = keys[s];
+    if (cur == k) return s;
+    if (cur == -1) {
+      if (!insert) return -1;
+      const int old = atomicCAS((int *)&keys[s], -1, k);
+      if (old == -1 || old == k) return s;
+      if (keys[s] == k) return s;
+    }
+    s = (s + 1) & (kSortSlots - 1);
   }
+  return -1;
+}
+
+/* the block's contiguous share [r0, r1) of the n queued events (a multiple of 32 long) */
+__device__ __forceinline__ void sort_range(long long n, long long &r0, long long &r1) {
+  const long long per = ((n + gridDim.x - 1) / gridDim.x + 31) & ~31ll;
+  r0 = (long long)blockIdx.x * per;
+  r1 = r0 + per < n ? r0 + per : n;
+}
+
+/* groups of equal keys in a warp: consecutive events mostly share theirs,
+ * and one vote settles that case */
+__device__ __forceinline__ unsigned key_peers(int k) {
+  return __all_sync(0xffffffffu, k == __shfl_sync(0xffffffffu, k, 0)) ? 0xffffffffu
+                                                                     : __match_any_sync(0xffffffffu, k);
+}
+
+/* counts of the block's range into the table s_key / s_cnt (keys without a
+ * slot go straight to `spill`, when given) */
+__device__ __forceinline__ void count_block_keys(const int *key, long long r0, long long r1, int nkeys, int *s_key,
+                                                 unsigned *s_cnt, unsigned *spill) {
+  const int lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  for (long long base = r0 + (long long)(threadIdx.x >> 5) * 32; base < r1; base += (long long)nw * 32) {
+    const long long i = base + lane;
+    const int k = i < r1 ? key[i] : -1;
+    const unsigned peers = key_peers(k);
+    if (k >= 0 && k < nkeys && lane == __ffs(peers) - 1) {
+      const int sl = sort_slot(s_key, k, true);
+      if (sl >= 0) atomicAdd(&s_cnt[sl], (unsigned)__popc(peers));
+      else if (spill) atomicAdd(&spill[k], (unsigned)__popc(peers));
+    }
+  }
+}
+
+__global__ void __launch_bounds__(256) event_key_histogram(const int *key, const unsigned long long *count,
+                                                           long long cap, int nkeys, unsigned *hist) {
+  __shared__ int s_key[kSortSlots];
+  __shared__ unsigned s_cnt[kSortSlots];
+  for (int j = threadIdx.x; j < kSortSlots; j += blockDim.x) s_key[j] = -1, s_cnt[j] = 0u;
+  __syncthreads();
+  long long r0, r1;
+  sort_range(queued_events(count, cap), r0, r1);
+  count_block_keys(key, r0, r1, nkeys, s_key, s_cnt, hist);
+  __syncthreads();
+  for (int j = threadIdx.x; j < kSortSlots; j += blockDim.x)
+    if (s_key[j] >= 0 && s_cnt[j] != 0u) atomicAdd(&hist[s_key[j]], s_cnt[j]);
 }
 
 /* exclusive scan of the key counts into the scatter cursors; also adds the
@@ -559,20 +616,40 @@ __global__ void __launch_bounds__(kScanThreads) event_key_scan(const unsigned *h
   if (threadIdx.x == 0) *total += *count;
 }
 
-__global__ void event_key_scatter(const int *key, const unsigned long long *count, long long cap, int nkeys,
-                                  unsigned *cursor, int *order) {
+/* positions: the block counts its range's keys again, reserves one run of
+ * positions per key with one global atomic, then hands out positions within
+ * each run with shared atomics (keys without a slot take theirs from the
+ * global cursor per warp group) */
+__global__ void __launch_bounds__(256) event_key_scatter(const int *key, const unsigned long long *count,
+                                                         long long cap, int nkeys, unsigned *cursor, int *order) {
+  __shared__ int s_key[kSortSlots];
+  __shared__ unsigned s_cnt[kSortSlots], s_base[kSortSlots];
+  for (int j = threadIdx.x; j < kSortSlots; j += blockDim.x) s_key[j] = -1, s_cnt[j] = 0u;
+  __syncthreads();
   const long long n = queued_events(count, cap);
-  const int lane = threadIdx.x & 31;
-  for (long long base = ((long long)blockIdx.x * blockDim.x + threadIdx.x) & ~31ll; base < n;
-       base += (long long)gridDim.x * blockDim.x) {
+  long long r0, r1;
+  sort_range(n, r0, r1);
+  count_block_keys(key, r0, r1, nkeys, s_key, s_cnt, nullptr);
+  __syncthreads();
+  for (int j = threadIdx.x; j < kSortSlots; j += blockDim.x)
+    if (s_key[j] >= 0) {
+      s_base[j] = s_cnt[j] != 0u ? atomicAdd(&cursor[s_key[j]], s_cnt[j]) : 0u;
+      s_cnt[j] = 0u;
+    }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  for (long long base = r0 + (long long)(threadIdx.x >> 5) * 32; base < r1; base += (long long)nw * 32) {
     const long long i = base + lane;
-    const int k = i < n ? key[i] : -1;
-    const unsigned peers = __all_sync(0xffffffffu, k == __shfl_sync(0xffffffffu, k, 0)) ? 0xffffffffu
-                                                                                        : __match_any_sync(0xffffffffu, k);
+    const int k = i < r1 ? key[i] : -1;
+    const unsigned peers = key_peers(k);
     if (k >= 0 && k < nkeys) {
       const int leader = __ffs(peers) - 1;
       unsigned pos = 0;
-      if (lane == leader) pos = atomicAdd(&cursor[k], (unsigned)__popc(peers));
+      if (lane == leader) {
+        const int sl = sort_slot(s_key, k, false);
+        pos = sl >= 0 ? s_base[sl] + atomicAdd(&s_cnt[sl], (unsigned)__popc(peers))
+                      : atomicAdd(&cursor[k], (unsigned)__popc(peers));
+      }
       pos = __shfl_sync(peers, pos, leader) + __popc(peers & ((1u << lane) - 1u));
       if ((long long)pos < n) order[pos] = (int)i;
     }
