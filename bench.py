@@ -388,9 +388,9 @@ def timed_steps(args, step, local):
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per history of
 # one estimator_kernel launch, from ncu captures of the FP32 kernel: the
 # batched sweep's small case (16 configurations, a 2^20-photon chunk:
-# 307.7 + 17.3 MB) and the plain production workload (1e6 photons: 393.9 +
+# 304.9 + 17.1 MB) and the plain production workload (1e6 photons: 393.9 +
 # 15.2 MB).  Traffic grows in proportion to the histories of a launch.
-ESTIMATOR_DRAM_BYTES_PER_HISTORY = {"batched": 325.1e6 / 1048576, "plain": 409.1e6 / 1.0e6}
+ESTIMATOR_DRAM_BYTES_PER_HISTORY = {"batched": 322.0e6 / 1048576, "plain": 409.1e6 / 1.0e6}
 
 
 def roofline_block(ph_ms: dict, n_hist_per_step: int, words_tr: float, words_est: float, word: int,
