@@ -113,6 +113,14 @@ __device__ __forceinline__ float sigmoid_fast(float z) {
   return fmaf(0.5f, t, 0.5f);
 }
 __device__ __forceinline__ float silu(float z) { return z * sigmoid_fast(z); }
+/* SiLU(z) from h = z / 2: z sigmoid(z) = z (1 + tanh(z/2)) / 2 = h + h tanh(h),
+ * one MUFU op and one FMA (the inference pass gets h directly from weights
+ * and biases halved in shared memory, exact in binary) */
+__device__ __forceinline__ float silu_half(float h) {
+  float t;
+  asm("tanh.approx.f32 %0, %1;" : "=f"(t) : "f"(h));
+  return fmaf(h, t, h);
+}
 
 /* eight consecutive activations of one row as one 16-byte store of the
  * K-major BF16 operand tile (k0 a multiple of 8) */
@@ -146,15 +154,28 @@ __device__ void fwd_setup(unsigned char *sm, const unsigned char *packed, const 
   uint32_t *tmem_slot = (uint32_t *)(sm + SM_BAR + 8 * kGroups);
   c.bias = (float *)(sm + SM_BIAS);
   c.wo = (float *)(sm + SM_WO);
-  for (int i = tid; i < PACK_BYTES / 16; i += blockDim.x) ((uint4 *)(sm + SM_W))[i] = ((const uint4 *)packed)[i];
+  /* every layer's weights and biases halved (W0, b0 below): the accumulators
+   * then hold z / 2, the input of silu_half (a power-of-two scale: the BF16
+   * weights and the FP32 accumulation round exactly as unscaled) */
+  for (int i = tid; i < PACK_BYTES / 16; i += blockDim.x) {
+    uint4 u = ((const uint4 *)packed)[i];
+    if (i * 16 >= W0_BYTES) {
+      __nv_bfloat162 *p2 = reinterpret_cast<__nv_bfloat162 *>(&u);
+      const __nv_bfloat162 half2 = __float2bfloat162_rn(0.5f);
+#pragma unroll
+      for (int k = 0; k < 4; k++) p2[k] = __hmul2(p2[k], half2);
+    }
+    ((uint4 *)(sm + SM_W))[i] = u;
+  }
   for (int i = tid; i < H; i += blockDim.x) {
-    c.bias[i] = theta[OFF_B0 + i];
-    for (int l = 1; l <= 3; l++) c.bias[l * H + i] = theta[off_b(l) + i];
+    c.bias[i] = 0.5f * theta[OFF_B0 + i];
+    for (int l = 1; l <= 3; l++) c.bias[l * H + i] = 0.5f * theta[off_b(l) + i];
     c.wo[i] = theta[OFF_WO + i];
   }
-  /* FP32 W0 of the CUDA-core layer 0, in the (otherwise unused) input-tile area */
+  /* FP32 W0 of the CUDA-core layer 0 (halved, as the others), in the
+   * (otherwise unused) input-tile area */
   float *w0 = (float *)(sm + SM_X0);
-  for (int i = tid; i < H * NIN; i += blockDim.x) w0[i] = theta[OFF_W0 + i];
+  for (int i = tid; i < H * NIN; i += blockDim.x) w0[i] = 0.5f * theta[OFF_W0 + i];
   c.bo = theta[OFF_BO];
   if (warp == 0) umma::tmem_alloc(tmem_slot, kTmemCols);
   if (tid == 0) {
@@ -175,19 +196,18 @@ __device__ void fwd_setup(unsigned char *sm, const unsigned char *packed, const 
   c.phase = 0;
 }
 
-/* layer 0 of this thread's row in FP32 on the CUDA cores; BF16 activations
- * into the operand tile (and, when zrow is given, the pre-activations) */
+/* layer 0 of this thread's row in FP32 on the CUDA cores (w0 and b0 halved:
+ * z / 2 comes out of the FMAs); BF16 activations into the operand tile */
 __device__ __forceinline__ void layer0_row(unsigned char *a_tile, int row, const float *w0, const float *b0,
-                                           const float *f, float *zrow, size_t zstride) {
+                                           const float *f) {
 #pragma unroll 1
   for (int j0 = 0; j0 < H; j0 += 8) {
     float h[8];
 #pragma unroll
     for (int u = 0; u < 8; u++) {
       const int j = j0 + u;
-      const float z = b0[j] + w0[j * NIN] * f[0] + w0[j * NIN + 1] * f[1] + w0[j * NIN + 2] * f[2];
-      if (zrow) zrow[(size_t)j * zstride] = z;
-      h[u] = silu(z);
+      const float zh = b0[j] + w0[j * NIN] * f[0] + w0[j * NIN + 1] * f[1] + w0[j * NIN + 2] * f[2];
+      h[u] = silu_half(zh);
     }
     store_bf16x8(a_tile, row, j0, h);
   }
@@ -197,7 +217,7 @@ __device__ __forceinline__ void layer0_row(unsigned char *a_tile, int row, const
  * 128 threads call it together; false (for every thread) when a wait ran out */
 __device__ bool fwd_tile(unsigned char *sm, FwdCtx &c, const float *f, float &y) {
   const uint32_t idesc = umma::idesc_bf16_f32(128, 128);
-  layer0_row(c.a_tile, c.row, (const float *)(sm + SM_X0), c.bias, f, nullptr, 0);
+  layer0_row(c.a_tile, c.row, (const float *)(sm + SM_X0), c.bias, f);
   y = c.bo;
   for (int l = 1; l < 4; l++) {
     umma::fence_proxy_async_smem();
@@ -216,13 +236,14 @@ __device__ bool fwd_tile(unsigned char *sm, FwdCtx &c, const float *f, float &y)
     c.phase ^= 1u;
     if (group_any(c.g, !ok)) return false;
     umma::fence_after_sync();
-    /* epilogue of layer l: bias, SiLU; the next layer's operand or the output */
+    /* epilogue of layer l: bias, SiLU (of the halved pre-activation); the
+     * next layer's operand or the output */
 #pragma unroll 1
     for (int q = 0; q < H / 32; q++) {
       float v[32];
       umma::tmem_ld_32x32b_x32(c.trow + q * 32, v);
 #pragma unroll
-      for (int j = 0; j < 32; j++) v[j] = silu(v[j] + c.bias[l * H + q * 32 + j]);
+      for (int j = 0; j < 32; j++) v[j] = silu_half(v[j] + c.bias[l * H + q * 32 + j]);
       if (l < 3) {
 #pragma unroll
         for (int j8 = 0; j8 < 32; j8 += 8) store_bf16x8(c.a_tile, c.row, q * 32 + j8, v + j8);
