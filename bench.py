@@ -52,7 +52,10 @@ a held-out validation at the estimator's own query points and the per-line
 error against the grid path beside it.
 
 Multi-GPU (torchrun): every rank runs its own configurations (weak scaling,
-no data-path collective).
+no data-path collective); with --partition the ranks split one batched sweep,
+whole configurations balanced by budget (strong scaling; the configuration
+outputs are each one rank's, the same as a single process's).  The job's
+value is the histories of all ranks over the slowest rank's time.
 
 ``--impl reference`` times the reference algorithm's CPU path: the FP64 C
 restatement under oracle/ (the reference's Fortran build needs gfortran and
@@ -105,6 +108,9 @@ def parse():
     p.add_argument("--overlap-chunks", type=int, default=0,
                    help="1: the next chunk's transport beside the current chunk's sort, solid angles and estimator")
     p.add_argument("--estimator-blocks-per-sm", type=int, default=0, help="estimator blocks per SM (0: as many as fit)")
+    p.add_argument("--partition", action="store_true",
+                   help="batched workload on N ranks: one sweep, whole configurations split by budget "
+                        "(strong scaling) instead of a sweep per rank (weak scaling)")
     p.add_argument("--no-plain", action="store_true")
     p.add_argument("--photons", type=float, default=1e7, help="photons per step of the plain workload")
     p.add_argument("--photons-precision", type=float, default=1e8, help="photons per step of the precision workload")
@@ -546,15 +552,24 @@ def merge_statements(parts: list[dict]) -> dict:
 def batched_arm(args, ws, rank, local):
     import numpy as np
     from xmimsim_gb300 import Simulation, gpu_options, last_timing
-    specs, options = batched_specs(args.configs, args.budget_scale, rank)
-    seed = 0x5EED0005 + rank
+    # weak scaling: a sweep of its own per rank; --partition: one sweep, each
+    # rank runs its share of whole configurations (balanced by budget) with
+    # the same photon streams as a single process would
+    part = args.partition and ws > 1
+    sweep_rank = 0 if args.partition else rank
+    specs, options = batched_specs(args.configs, args.budget_scale, sweep_rank)
+    full_specs, _ = batched_specs(args.configs, 1.0, sweep_rank)
+    if part:
+        from xmimsim_gb300.replicas import rank_share
+        mine = rank_share(specs, rank, ws)
+        specs, full_specs = [specs[i] for i in mine], [full_specs[i] for i in mine]
+    seed = 0x5EED0005 + sweep_rank
     g_sur = gpu_options(precision=1, seed=seed, use_surrogate=1, surrogate_tolerance=args.tolerance,
                         overlap_chunks=args.overlap_chunks, estimator_blocks_per_sm=args.estimator_blocks_per_sm)
     t0 = time.perf_counter()
     sims = [Simulation(s, options=options, gpu=g_sur) for s in specs]
     host_tables_s = time.perf_counter() - t0
     n_hist = sum(histories(s) for s in specs)
-    full_specs, _ = batched_specs(args.configs, 1.0, rank)
     full_hist = sum(histories(s) for s in full_specs)
 
     # one network for the detector, trained where the estimator queries solid
@@ -610,13 +625,16 @@ def batched_arm(args, ws, rank, local):
     e2e = n_hist * args.steps / wall
     phases = {k: statistics.mean(t[k + "_ms"] for t in tms) for k in ("transport", "sort", "surrogate", "estimator")}
     extra = {"photons_per_step": n_hist, "photons_full_job": full_hist,
+             "ranks": ("one sweep, %d of its configurations on this rank (whole configurations balanced by "
+                       "budget)" % len(specs)) if part else "a sweep per rank",
              "elements_per_config_mean": statistics.mean(sum(len(l.Z) for l in s.layers) for s in specs),
              "l2": "inputs larger than L2 (tables of 512 configurations, several GB)",
              "host_tables_s": host_tables_s, "autotuned": tune,
              "surrogate": dict(rep, n_train=args.n_train, epochs=args.epochs, tolerance=args.tolerance,
                               hits_check=args.hits_check, wall_s=train_s)}
     line = {"metric": METRIC, "value": value, "unit": "histories/s", "n_gpus": ws, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ksum / args.steps, "higher_is_better": True, "scaling": "weak",
+            "warmup": args.warmup, "ms_per_step": ksum / args.steps, "higher_is_better": True,
+            "scaling": "strong" if part else "weak",
             "vs_baseline": None, "dtype": "f32 transport, f64 tallies",
             "data": "synthetic (seeded random samples, Rh tube spectrum / discrete lines)",
             "config": workload_config(args, extra),
@@ -953,12 +971,19 @@ def main():
            "precision": precision_arm}[args.workload]
     line, sims, specs, options = arm(args, ws, rank, local)
     if ws > 1:
+        # whole job: the histories of every rank over the slowest rank's time
+        # (device time for value, host wall for e2e)
         import torch
-        t = torch.tensor([line["ms_per_step"]], dtype=torch.float64, device="cuda")
+        n_step = line["value"] * line["ms_per_step"] / 1e3  # this rank's histories per step
+        e2e_s = n_step / line["e2e"]["value"] if line.get("e2e") else 0.0
+        t = torch.tensor([line["ms_per_step"], e2e_s], dtype=torch.float64, device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        line["ms_per_step"] = t.item()
-        n_step = line["value"] * line["ms_per_step"] / 1e3  # per-rank histories per step
-        line["value"] = n_step * ws / (line["ms_per_step"] / 1e3)
+        n = torch.tensor([n_step], dtype=torch.float64, device="cuda")
+        dist.all_reduce(n, op=dist.ReduceOp.SUM)
+        line["ms_per_step"] = t[0].item()
+        line["value"] = n.item() / (line["ms_per_step"] / 1e3)
+        if line.get("e2e") and t[1].item() > 0:
+            line["e2e"]["value"] = n.item() / t[1].item()
     if rank == 0 and not args.no_cpu_baseline:
         cspecs, coptions, what = cpu_sample_specs(args, rank)
         cv, cn, cdt, words_tr, words_est = run_cpu_sample(cspecs, coptions, args.cpu_sample, os.cpu_count() or 1)
