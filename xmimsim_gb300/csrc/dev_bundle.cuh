@@ -84,6 +84,11 @@ struct DevBundle {
   const R *precalc_mu, *precalc_xrf;
   const R *seg_lo, *seg_lnlo, *seg_invh;
   const int *seg_off, *seg_n, *seg_lut;
+  /* FP32 copies of a segment's fields in one record, for the FP32 grid
+   * location: {seg_lo[i], seg_lo[i + 1], seg_lnlo[i], seg_invh[i]} and
+   * {seg_off[i], seg_n[i]} */
+  const float4 *seg_rec;
+  const int2 *seg_on;
   R seg_lut_ln0, seg_lut_inv;
   const R *el_tab, *mu_tab, *exc_tab;
   /* [n_nodes][n_layer_el]: per layer, the running sum over its elements of

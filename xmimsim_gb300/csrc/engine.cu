@@ -250,6 +250,14 @@ const R *const *upload_per_element(DevSide &s, const double *const *src, int E, 
   return (const R *const *)p;
 }
 
+const void *upload_bytes(DevSide &s, const void *src, size_t bytes) {
+  void *p = nullptr;
+  if (cudaMalloc(&p, bytes) != cudaSuccess) return nullptr;
+  s.allocs.push_back(p);
+  cudaMemcpy(p, src, bytes, cudaMemcpyHostToDevice);
+  return p;
+}
+
 const int *upload_int(DevSide &s, const int *src, size_t n) {
   if (n == 0) n = 1;
   void *p = nullptr;
@@ -402,6 +410,17 @@ bool upload_tables(const xmi_bundle &h, DevSide &s, xmi::DevBundle<R> &d) {
   d.seg_lut_inv = (R)h.seg_lut_inv;
   d.seg_off = upload_int(s, h.seg_off, h.n_seg);
   d.seg_n = upload_int(s, h.seg_n, h.n_seg);
+  {
+    const size_t ns = h.n_seg > 0 ? (size_t)h.n_seg : 1;
+    std::vector<float4> rec(ns, make_float4(0.f, 0.f, 0.f, 0.f));
+    std::vector<int2> on(ns, make_int2(0, 0));
+    for (int i = 0; i < h.n_seg; i++) {
+      rec[i] = make_float4((float)h.seg_lo[i], (float)h.seg_lo[i + 1], (float)h.seg_lnlo[i], (float)h.seg_invh[i]);
+      on[i] = make_int2(h.seg_off[i], h.seg_n[i]);
+    }
+    d.seg_rec = (const float4 *)upload_bytes(s, rec.data(), sizeof(float4) * ns);
+    d.seg_on = (const int2 *)upload_bytes(s, on.data(), sizeof(int2) * ns);
+  }
   d.el_tab = upload<R>(s, h.el_tab, E * h.n_nodes * XMI_EL_REC);
   d.mu_tab = upload<R>(s, h.mu_tab, (size_t)h.n_nodes * XMI_MAXL);
   {
@@ -445,7 +464,7 @@ bool upload_tables(const xmi_bundle &h, DevSide &s, xmi::DevBundle<R> &d) {
   d.line_casc = upload_int(s, h.line_casc_shell, NL);
   d.auger_rate = upload<R>(s, h.auger_rate, E * 4 * XMI_AUGER_K);
   if (cudaGetLastError() != cudaSuccess || !d.rayl_icdf || !d.compt_icdf || !d.dop_icdf || !d.ff2 || !d.sf ||
-      !d.phi_icdf || !d.ent_pmu || !d.line_casc || !d.auger_rate || !d.layer_cs) {
+      !d.phi_icdf || !d.ent_pmu || !d.line_casc || !d.auger_rate || !d.layer_cs || !d.seg_rec || !d.seg_on) {
     xmi_set_error("device table upload failed");
     s.release();
     return false;

@@ -215,6 +215,28 @@ __device__ __forceinline__ void locate(const DevBundle<R> &b, R E, int &node, R 
   R gb = (lnE - b.seg_lut_ln0) * b.seg_lut_inv;
   gb = gb > (R)0 ? (gb < (R)(XMI_SEG_LUT - 1) ? gb : (R)(XMI_SEG_LUT - 1)) : (R)0;
   int lo = __ldg(b.seg_lut + (int)gb);
+#ifndef XMI_CHECKED
+  if constexpr (sizeof(R) == 4) {
+    /* FP32: the segment's bounds, log base, 1/h, first node and node count
+     * in two loads issued together; the steps below only when the table's
+     * cell straddles a segment boundary (the same segment either way) */
+    float4 r = __ldg(b.seg_rec + lo);
+    int2 on = __ldg(b.seg_on + lo);
+    if (!(E >= r.x && E < r.y)) {
+      while (lo < b.n_seg - 1 && E >= __ldg(b.seg_lo + lo + 1)) lo++;
+      while (lo > 0 && E < __ldg(b.seg_lo + lo)) lo--;
+      r = __ldg(b.seg_rec + lo);
+      on = __ldg(b.seg_on + lo);
+    }
+    const float t = (lnE - r.z) * r.w;
+    int i = (int)t;
+    if (i < 0) i = 0;
+    if (i > on.y - 2) i = on.y - 2;
+    node = on.x + i;
+    f = t - (float)i;
+    return;
+  }
+#endif
   while (lo < b.n_seg - 1 && E >= __ldg(b.seg_lo + lo + 1)) lo++;
   while (lo > 0 && E < __ldg(b.seg_lo + lo)) lo--;
   R t = (lnE - __ldg(b.seg_lnlo + lo)) * __ldg(b.seg_invh + lo);
