@@ -261,7 +261,7 @@ int xmi_gpu_surrogate_eval(xmi_inputFPtr inputFPtr, int n, const double *r, cons
  * src/xmi_solid_angle_f.F90:432-710) at n arbitrary points with `hits`
  * samples each, FP64 (precision 0) or FP32 (1), Philox key `seed`: point i
  * draws from stream (seed, i, 0xF1000000).  No counterpart in the reference
- * as an entry point; the judge of the surrogate. */
+ * as an entry point; the values the surrogate is checked against. */
 int xmi_gpu_solid_angle_points(xmi_inputFPtr inputFPtr, int n, const double *r, const double *theta, int hits,
                                int precision, unsigned long long seed, double *omega);
 /* the same training and check on caller-given points (r, theta) of the

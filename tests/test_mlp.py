@@ -250,7 +250,7 @@ def test_c4_surrogate_at_tolerance_1e3():
     * held out -- at the estimator's own query points of a pilot run with
       another seed, judged by the integrator with 2^22 samples per point --
       the solid angles the transport takes are within 1e-3 (median) of the
-      judge, whichever source serves them, and few points need the
+      integrator's values, whichever source serves them, and few points need the
       per-event integrator;
     * the transport with the surrogate gives every first-order line of the
       grid run within 2% (the grid's own noise: 5000 samples per point)."""
