@@ -12,6 +12,9 @@ namespace xmi {
 constexpr double kEnergyThreshold = 1.0;  /* src/xmi_aux_f.F90:673 */
 constexpr double kEnergyMax = 200.0;      /* src/xmi_aux_f.F90:674 */
 constexpr double kPi = 3.14159265358979323846;
+/* words per (element, line) record of the device copy of precalc_xrf: the 9
+ * shell factors, padded to 12 so that a record is three 16-byte words (FP32) */
+constexpr int kXrfRec = 12;
 
 /* FP32 working copy of a source item, read by the FP32 transport's source
  * sampling instead of the FP64 fields.  Intensities are divided by
@@ -81,7 +84,8 @@ struct DevBundle {
   const int *line_off, *shell_off;
   const int *line_index, *line_shell;
   const R *line_energy, *line_rate;
-  const R *precalc_mu, *precalc_xrf;
+  const R *precalc_mu;
+  const R *precalc_xrf; /* [n_elem][n_lines][kXrfRec]: the host's [n_elem][9][n_lines] regrouped by line */
   const R *seg_lo, *seg_lnlo, *seg_invh;
   const int *seg_off, *seg_n, *seg_lut;
   /* FP32 copies of a segment's fields in one record, for the FP32 grid

@@ -401,7 +401,15 @@ bool upload_tables(const xmi_bundle &h, DevSide &s, xmi::DevBundle<R> &d) {
   d.line_energy = upload<R>(s, h.line_energy, NL);
   d.line_rate = upload<R>(s, h.line_rate, NL);
   d.precalc_mu = upload<R>(s, h.precalc_mu, (size_t)h.n_layers * NL);
-  d.precalc_xrf = upload<R>(s, h.precalc_xrf, E * 9 * NL);
+  {
+    /* one record per (element, line): the shell factors of an event excited
+     * by that line are one 48-byte read instead of nine words n_lines apart */
+    std::vector<double> xr(E * (NL > 0 ? NL : 1) * xmi::kXrfRec, 0.0);
+    for (size_t e = 0; e < E; e++)
+      for (size_t i = 0; i < NL; i++)
+        for (int sh = 0; sh < 9; sh++) xr[(e * NL + i) * xmi::kXrfRec + sh] = h.precalc_xrf[(e * 9 + sh) * NL + i];
+    d.precalc_xrf = upload<R>(s, xr.data(), xr.size());
+  }
   d.seg_lo = upload<R>(s, h.seg_lo, h.n_seg + 1);
   d.seg_lnlo = upload<R>(s, h.seg_lnlo, h.n_seg);
   d.seg_invh = upload<R>(s, h.seg_invh, h.n_seg);

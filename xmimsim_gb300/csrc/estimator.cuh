@@ -32,6 +32,24 @@ __device__ __forceinline__ R line_atten(R s) {
   else return exp(-s);
 }
 
+/* the 9 shell factors of element e at the energy of line `slot` (an event
+ * of a fluorescence photon): one record of the device's precalc_xrf */
+template <typename R>
+__device__ __forceinline__ void xrf_at_line(const DevBundle<R> &b, int e, int slot, R *P) {
+  const long long base = ((long long)e * b.n_lines + slot) * kXrfRec;
+#ifndef XMI_CHECKED
+  if constexpr (sizeof(R) == 4 && XMI_NSHELL == 9) {
+    const float4 *p = reinterpret_cast<const float4 *>(b.precalc_xrf + base);
+    const float4 a = __ldg(p), c = __ldg(p + 1), d = __ldg(p + 2);
+    P[0] = a.x, P[1] = a.y, P[2] = a.z, P[3] = a.w, P[4] = c.x, P[5] = c.y, P[6] = c.z, P[7] = c.w, P[8] = d.x;
+    return;
+  }
+#endif
+#pragma unroll
+  for (int s = 0; s < XMI_NSHELL; s++)
+    P[s] = XMI_LDG(b.precalc_xrf, base + s, (long long)b.n_elem * b.n_lines * kXrfRec, 10);
+}
+
 /* exp(-x) of an attenuation exponent: FP32 as exp2(-log2(e) x) */
 template <typename R>
 __device__ __forceinline__ R atten(R x) {
@@ -241,10 +259,7 @@ __device__ __forceinline__ void estimate_event(const DevBundle<R> &b, const DevT
      * after scattering) or at the exciting line's energy (after fluorescence) */
     R P[XMI_NSHELL];
     if (ev.h_slot >= 0) {
-#pragma unroll
-      for (int s = 0; s < XMI_NSHELL; s++)
-        P[s] = XMI_LDG(b.precalc_xrf, ((long long)e * XMI_NSHELL + s) * b.n_lines + ev.h_slot,
-                       (long long)b.n_elem * XMI_NSHELL * b.n_lines, 10);
+      xrf_at_line(b, e, ev.h_slot, P);
     } else {
 #pragma unroll
       for (int s = 0; s < XMI_NSHELL; s++) P[s] = el_val(b, e, XMI_REC_XRF + s, ev.node, ev.f);
@@ -392,10 +407,7 @@ __device__ __forceinline__ void estimate_event_uniform(const DevBundle<R> &b, co
     /* shell factors of this event for element i */
     R P[XMI_NSHELL];
     if (ev.h_slot >= 0) {
-#pragma unroll
-      for (int s = 0; s < XMI_NSHELL; s++)
-        P[s] = XMI_LDG(b.precalc_xrf, ((long long)e * XMI_NSHELL + s) * b.n_lines + ev.h_slot,
-                       (long long)b.n_elem * XMI_NSHELL * b.n_lines, 10);
+      xrf_at_line(b, e, ev.h_slot, P);
     } else {
       el_xrf(b, e, ev.node, ev.f, P);
     }
