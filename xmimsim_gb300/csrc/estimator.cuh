@@ -50,6 +50,40 @@ __device__ __forceinline__ void xrf_at_line(const DevBundle<R> &b, int e, int sl
     P[s] = XMI_LDG(b.precalc_xrf, base + s, (long long)b.n_elem * b.n_lines * kXrfRec, 10);
 }
 
+/* sum_j mu_j(E) rd_j over the layers: FP32 reads the first four layers' mu
+ * only when the configuration has no more (the others' mu and path sums are
+ * zero) */
+template <typename R>
+__device__ __forceinline__ R mu_path(const DevBundle<R> &b, R E, const R *rd) {
+#ifndef XMI_CHECKED
+  if constexpr (sizeof(R) == 4 && XMI_MAXL == 8) {
+    int node;
+    float f;
+    locate(b, E, node, f);
+    const float4 *p = reinterpret_cast<const float4 *>(b.mu_tab + (long long)node * XMI_MAXL);
+    const float4 a0 = __ldg(p), c0 = __ldg(p + 2);
+    float s = (a0.x + f * (c0.x - a0.x)) * rd[0];
+    s += (a0.y + f * (c0.y - a0.y)) * rd[1];
+    s += (a0.z + f * (c0.z - a0.z)) * rd[2];
+    s += (a0.w + f * (c0.w - a0.w)) * rd[3];
+    if (b.n_layers > 4) {
+      const float4 a1 = __ldg(p + 1), c1 = __ldg(p + 3);
+      s += (a1.x + f * (c1.x - a1.x)) * rd[4];
+      s += (a1.y + f * (c1.y - a1.y)) * rd[5];
+      s += (a1.z + f * (c1.z - a1.z)) * rd[6];
+      s += (a1.w + f * (c1.w - a1.w)) * rd[7];
+    }
+    return s;
+  }
+#endif
+  R mus[XMI_MAXL];
+  mu_calc(b, E, mus);
+  R s = (R)0;
+#pragma unroll
+  for (int j = 0; j < XMI_MAXL; j++) s += mus[j] * rd[j];
+  return s;
+}
+
 /* exp(-x) of an attenuation exponent: FP32 as exp2(-log2(e) x) */
 template <typename R>
 __device__ __forceinline__ R atten(R x) {
@@ -392,11 +426,7 @@ __device__ __forceinline__ void estimate_event_uniform(const DevBundle<R> &b, co
       const R ec = compton_energy_est(b, e, ce, &g, cok);
       R twc = (R)0;
       if (cok) {
-        R mus_c[XMI_MAXL];
-        mu_calc(b, ec, mus_c);
-        R murhod = (R)0;
-#pragma unroll
-        for (int j = 0; j < XMI_MAXL; j++) murhod += mus_c[j] * ev.rd[j];
+        const R murhod = mu_path(b, ec, ev.rd);
         twc = live * (pconv * (ev.pC * qtab(b.sf[e], ev.q)) * atten<R>(murhod) * ev.w);
       } else if (valid) {
         ok = false;
